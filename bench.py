@@ -1,0 +1,384 @@
+#!/usr/bin/env python3
+"""Mrays/s of the GB300 hair ray tracer on the Phantom precision-pattern workload.
+
+Workload (default): 150,000 seeded strands x 128 vertices -> 19,050,000 cubic Bezier segments,
+quantised BVH8 (8-bit child boxes) with FP16 control-point offsets from FP32 strand roots,
+1920x1080 at 4 jittered samples per pixel, Shade() plus one shadow ray per hit. A step is one
+frame. `value` counts primary + shadow rays per second with the BVH resident in HBM (the BVH
+and primitives, ~0.8 GB, exceed the 129 MB L2, so no flush is needed between steps); `e2e`
+goes through the C ABI per frame (camera in, framebuffer copied to pinned host memory).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
+
+Under torchrun (N > 1) every rank renders its own full frame (replicas, weak scaling); rank 0
+prints one JSON line. `--impl reference` times the CPU restatement of the reference's trace
+path (oracle/, FP32, all host threads) on bounded samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s on 1 GB300: quantized/batched vs plain FP32 at >=99.99% hit agreement"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+class Dist:
+    """Rank bookkeeping; torch.distributed only when WORLD_SIZE > 1."""
+
+    def __init__(self):
+        self.rank = env_int("RANK", 0)
+        self.world = env_int("WORLD_SIZE", 1)
+        self.local = env_int("LOCAL_RANK", 0)
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait(timeout=5)
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def load_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def workload(name: str):
+    import vkhrt_gb300 as H
+    cfg = dict(H.CONFIGS[name])
+    sp = H.StrandParams(seed=cfg["seed"], nstrands=cfg["nstrands"], nverts=cfg["nverts"], r_root=cfg["r_root"],
+                        r_tip=cfg["r_tip"])
+    return cfg, sp
+
+
+def uniform_lines(v, r, ns, nv):
+    vv = v.reshape(ns, nv, 3)
+    rr = r.reshape(ns, nv)
+    lines = np.ascontiguousarray(np.concatenate([vv[:, :-1], vv[:, 1:]], axis=2).reshape(-1, 6), np.float32)
+    lrad = np.ascontiguousarray(np.stack([rr[:, :-1], rr[:, 1:]], axis=2).reshape(-1, 2), np.float32)
+    return lines, lrad
+
+
+def oracle_scene(cfg, v, r, precision):
+    """CPU oracle scene for the workload (the checker and the CPU baseline)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from hairscene import OracleScene, load_oracle, oracle_geometry
+    orc = load_oracle()
+    lines, lrad = uniform_lines(v, r, cfg["nstrands"], cfg["nverts"])
+    data, rad = oracle_geometry(orc, int(cfg["type"]), lines, lrad, quantised=(precision == 1 and int(cfg["type"]) == 0))
+    del lines, lrad
+    return OracleScene(orc, [(int(cfg["type"]), data, rad)]), orc
+
+
+def sample_pixels(w, h, n, seed=7):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(w * h, size=min(n, w * h), replace=False)).astype(np.uint32)
+
+
+def cpu_sample_rate(osc, cam_arrays, cfg, precision, target_s=12.0, threads=0):
+    """Rays/s of the oracle on a growing pixel sample until ~target_s of work; returns (Mrays/s, desc)."""
+    vi, pi = cam_arrays
+    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
+    npx = 512
+    while True:
+        px = sample_pixels(w, h, npx, seed=npx)
+        t0 = time.perf_counter()
+        o = osc.render(vi, pi, w, h, spp=spp, jitter=1 if spp > 1 else 0, seed=17, shading=2, precision=precision,
+                       pixel_list=px, threads=threads)
+        dt = time.perf_counter() - t0
+        rays = len(px) * spp + int((o["t"] >= 0).sum())
+        if dt >= target_s or npx >= w * h:
+            return rays / dt / 1e6, f"{len(px)} random pixels x {spp} spp (+{int((o['t'] >= 0).sum())} shadow rays)", dt
+        npx = min(w * h, int(npx * max(2.0, min(8.0, target_s / max(dt, 1e-3)))))
+
+
+def run_reference(args, dist):
+    """CPU restatement of the reference's trace path (FP32 Prhi, all host threads)."""
+    if dist.rank != 0:
+        return
+    import vkhrt_gb300 as H
+    cfg, sp = workload(args.config)
+    v, r, off = H.generate_strands(sp)
+    osc, orc = oracle_scene(cfg, v, r, int(cfg["precision"]))
+    cam = H.scene_camera(cfg["width"], cfg["height"])
+    vi, pi = H.camera_arrays(cam)
+    threads = orc.orc_hardware_threads()
+    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
+    npx = args.ref_pixels
+    rates = []
+    total_t = 0.0
+    total_rays = 0
+    for step in range(args.warmup + args.steps):
+        px = sample_pixels(w, h, npx, seed=1000 + step)
+        t0 = time.perf_counter()
+        o = osc.render(vi, pi, w, h, spp=spp, jitter=1 if spp > 1 else 0, seed=17, shading=2, precision=32,
+                       pixel_list=px, threads=threads)
+        dt = time.perf_counter() - t0
+        rays = len(px) * spp + int((o["t"] >= 0).sum())
+        if step >= args.warmup:
+            total_t += dt
+            total_rays += rays
+            rates.append(rays / dt / 1e6)
+    value = total_rays / total_t / 1e6
+    sample = f"{npx} random pixels x {spp} spp per step (+ shadow rays)"
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_t / max(args.steps, 1), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
+            "config": config_block(cfg, args.config),
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_block(cfg, name):
+    nseg = cfg["nstrands"] * (cfg["nverts"] - 1)
+    return {"workload": f"{name}: {cfg['nstrands']} strands x {cfg['nverts']} vertices = {nseg} "
+                        f"{'Bezier' if int(cfg['type']) == 0 else 'LSS' if int(cfg['type']) == 1 else 'DOTS'} segments, "
+                        f"{cfg['width']}x{cfg['height']} x {cfg['spp']} spp, Shade + 1 shadow ray",
+            "segments": nseg, "image": f"{cfg['width']}x{cfg['height']}", "spp": cfg["spp"],
+            "precision": "quantised (8-bit BVH8 boxes, FP16 control points)" if int(cfg["precision"]) else "fp32",
+            "l2": "inputs larger than L2 (BVH + primitives resident, no flush)", "parallelism": "replicas"}
+
+
+def time_frames(ctx, tlas, cam, frame, params, steps, warmup):
+    import torch
+    import vkhrt_gb300 as H
+    for _ in range(warmup):
+        H.trace(ctx, tlas, cam, frame, params)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        H.trace(ctx, tlas, cam, frame, params)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_ours(args, dist):
+    import torch
+    import vkhrt_gb300 as H
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    ctx = H.Context(dev)
+    cfg, sp = workload(args.config)
+    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
+    t_gen = time.perf_counter()
+    v, r, off = H.generate_strands(sp)
+    t_gen = time.perf_counter() - t_gen
+    # ---- build (untimed for `value`; reported) ----
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    blas = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=cfg["precision"]), ctx)
+    tlas = H.TopLevelAccelerationStructure([blas], ctx)
+    build_wall = time.perf_counter() - t0
+    cam = H.scene_camera(w, h)
+    frame = H.Frame(ctx, w, h, spp, with_hits=True)
+    params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, **{"async": 1})
+    # rays per step (deterministic: fixed camera, jitter seed)
+    H.trace(ctx, tlas, cam, frame, H.trace_params(spp=spp, jitter=1, seed=17, shading=2, count_stats=1))
+    st = frame.stats()
+    rays_per_step = st["primary_rays"] + st["shadow_rays"]
+    # ---- timed region ----
+    dist.barrier()
+    clocks = Clocks(dev)
+    clocks.start()
+    ms = time_frames(ctx, tlas, cam, frame, params, args.steps, args.warmup)
+    clk = clocks.stop()
+    ms_max = dist.max(ms)
+    value = dist.world * rays_per_step / (ms_max * 1e-3) / 1e6
+    if dist.rank != 0:
+        dist.close()
+        return
+    info = blas.info
+    # ---- roofline: algorithmic bytes per launch / launch time ----
+    node_b = info["node_bytes"]
+    prim_b = info["prim_bytes"] + (16 if int(cfg["precision"]) == 1 and int(cfg["type"]) == 0 else 0)
+    alg_bytes = st["nodes_visited"] * node_b + st["prims_tested"] * prim_b + w * h * 16
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "bytes_per_launch": int(alg_bytes), "nodes_visited": int(st["nodes_visited"]),
+                "prims_tested": int(st["prims_tested"]), "node_bytes": int(node_b), "prim_bytes": int(prim_b)}
+    # ---- e2e: C ABI per frame, camera in, framebuffer to pinned host memory ----
+    lib = ctx.lib
+    pinned = torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True)
+    sync_params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2)
+    for _ in range(2):
+        H.trace(ctx, tlas, cam, frame, sync_params)
+        ctx.check(lib.hrt_frame_download(frame.handle, ctypes.c_void_p(pinned.data_ptr()), None, None))
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        H.trace(ctx, tlas, cam, frame, sync_params)
+        ctx.check(lib.hrt_frame_download(frame.handle, ctypes.c_void_p(pinned.data_ptr()), None, None))
+    te = (time.perf_counter() - te) / e2e_steps
+    e2e = {"value": round(rays_per_step / te / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 128,
+           "d2h_bytes_per_step": w * h * 16, "ms_per_step": round(te * 1e3, 3)}
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32 (fp16 control-point storage, 8-bit node boxes)",
+            "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
+            "config": config_block(cfg, args.config), "rays_per_step": int(rays_per_step),
+            "primary_rays_per_step": int(st["primary_rays"]), "shadow_rays_per_step": int(st["shadow_rays"]),
+            "fp64_resolves_per_step": int(st["fp64_resolves"]), "gpu_launches": args.steps,
+            "roofline": roofline, "e2e": e2e, "clocks": clk,
+            "build": {"blas_build_ms": round(info["build_ms"], 2), "build_wall_s": round(build_wall, 3),
+                      "strand_generation_s": round(t_gen, 3), "nodes": int(info["nnodes"]),
+                      "device_bytes": int(info["device_bytes"])}}
+    # ---- plain FP32 tracer on the same strands (the comparison the metric names) ----
+    if not args.quick and int(cfg["precision"]) == 1:
+        blas32 = H.BottomLevelAccelerationStructure(
+            H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=H.Precision.FP32), ctx)
+        tlas32 = H.TopLevelAccelerationStructure([blas32], ctx)
+        f32 = H.Frame(ctx, w, h, spp, with_hits=False)
+        H.trace(ctx, tlas32, cam, f32, H.trace_params(spp=spp, jitter=1, seed=17, shading=2))
+        s32 = f32.stats()
+        ms32 = time_frames(ctx, tlas32, cam, f32, params, args.steps, args.warmup)
+        line["plain_fp32"] = {"value": round((s32["primary_rays"] + s32["shadow_rays"]) / (ms32 * 1e-3) / 1e6, 3),
+                              "ms_per_step": round(ms32, 3), "build_ms": round(blas32.info["build_ms"], 2)}
+        del f32, tlas32, blas32
+    # ---- agreement with the FP64 oracle on 65,536 sampled rays, and the CPU baseline ----
+    if not args.no_cpu:
+        H.trace(ctx, tlas, cam, frame, H.trace_params(spp=spp, jitter=1, seed=17, shading=2, record_hits=1))
+        rgba, hits = frame.download(hits=True)
+        osc, orc = oracle_scene(cfg, v, r, int(cfg["precision"]))
+        vi, pi = H.camera_arrays(cam)
+        px = sample_pixels(w, h, 65536 // spp, seed=3)
+        o = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=64, pixel_list=px)
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from hairscene import compare_hits
+        gh = hits.reshape(h * w, spp)[px].reshape(-1)
+        g_t = np.where(gh["t"] >= 0, gh["t"].astype(np.float64), -1.0)
+        cmp = compare_hits(g_t, gh["prim"], gh["inst"], o["t"], o["prim"], o["inst"])
+        same = (gh["prim"] == o["prim"]) & (((gh["flags"] & H.HIT_SHADOWED) != 0) == (o["shadow"] != 0))
+        ok_px = same.reshape(-1, spp).all(axis=1)
+        dpx = np.abs(rgba.reshape(-1, 4)[px] - o["fb"]).max(axis=1)
+        line["agreement"] = {"rays": int(cmp["n"]), "hit_id": round(cmp["agreement"], 6), "mismatches": cmp["mismatches"],
+                             "ties": cmp["ties"], "max_rel_t": cmp["max_rel_t"], "p9999_rel_t": cmp["p9999_rel_t"],
+                             "pixels_agreeing": round(float(ok_px.mean()), 6),
+                             "max_rgb_err_agreeing": float(dpx[ok_px].max()) if ok_px.any() else None,
+                             "oracle": "FP64 CPU restatement on the same (dequantised) geometry"}
+        rate, desc, secs = cpu_sample_rate(osc, (vi, pi), cfg, 32, target_s=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": round(rate, 4), "unit": "Mrays/s", "cores": orc.orc_hardware_threads(),
+                                "kind": "port", "sample": f"{desc}, FP32 oracle, {secs:.1f} s"}
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="c4_phantom_quantised")
+    ap.add_argument("--quick", action="store_true", help="skip the plain FP32 comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the oracle agreement and CPU baseline")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-pixels", type=int, default=4096)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+        dist.close()
+        return
+    run_ours(args, dist)
+
+
+if __name__ == "__main__":
+    main()

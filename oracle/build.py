@@ -68,6 +68,7 @@ def load() -> ctypes.CDLL:
         "orc_generate_dots": (None, [P, P, f32, i64, P]),
         "orc_generate_lss": (None, [P, i64, f32, P, P]),
         "orc_f32_to_f16": (ctypes.c_uint16, [f32]),
+        "orc_quantise_phantom": (i64, [P, P, P, i64, u32, P, P, P, P]),
         "orc_f16_to_f32": (f32, [ctypes.c_uint16]),
         "orc_prim_boxes": (None, [i32, P, P, i64, P]),
         "orc_morton": (None, [P, i64, P]),
@@ -79,7 +80,7 @@ def load() -> ctypes.CDLL:
         "orc_scene_add_instance": (i32, [P, i32, P]),
         "orc_trace_rays": (None, [P, P, i64, f32, f32, i32, i32, P, P, P, P]),
         "orc_render": (None, [P, P, P, u32, u32, u32, i32, u32, f32, f32, i32, f32, i32, i32, i64, i64,
-                              P, P, P, P, P]),
+                              P, P, P, P, P, P]),
         "orc_hardware_threads": (i32, []),
     }
     for name, (res, args) in sig.items():

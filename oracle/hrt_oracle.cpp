@@ -427,7 +427,7 @@ static void morton_codes(const Box* boxes, int64_t n, uint64_t* codes) {
         uint64_t code = 0;
         for (int k = 0; k < 3; ++k) {
             float q = (cen[3 * i + k] - cmin[k]) * scale[k];
-            uint32_t qi = q <= 0.0f ? 0u : (q >= 2097151.0f ? 2097151u : uint32_t(q));
+            uint32_t qi = !(q > 0.0f) ? 0u : (q >= 2097151.0f ? 2097151u : uint32_t(q));  // NaN -> 0
             code |= expand21(qi) << (2 - k);
         }
         codes[i] = code;
@@ -739,14 +739,15 @@ static inline double xf_dir(const double* m, const double* p, int k) {
 
 // Intersect one BVH primitive; returns true and fills *h when it beats (t, prim) of *h.
 // mode64: 0 = precision T only; 1 = T then FP64 re-solve of unresolved Phantom candidates.
+// Closest-hit order: smaller t, then smaller instance, then smaller primitive id.
 template <class T>
-static bool intersect_prim(const Blas& b, uint32_t s, const tvec3<T>& o, const tvec3<T>& d, T tmin,
+static bool intersect_prim(const Blas& b, uint32_t inst, uint32_t s, const tvec3<T>& o, const tvec3<T>& d, T tmin,
                            HitT<T>* h, int resolve64) {
     bool better = false;
     auto take = [&](T t, uint32_t prim, T u, int r64) {
         if (!(t >= tmin) || !(t <= h->t)) return;
-        if (t == h->t && prim >= h->prim) return;
-        h->t = t; h->prim = prim; h->seg = s; h->u = u; h->resolved64 = r64;
+        if (t == h->t && (inst > h->inst || (inst == h->inst && prim >= h->prim))) return;
+        h->t = t; h->inst = inst; h->prim = prim; h->seg = s; h->u = u; h->resolved64 = r64;
         better = true;
     };
     if (b.type == kPhantom) {
@@ -829,9 +830,7 @@ static bool trace_one(const Scene& sc, const tvec3<T>& wo, const tvec3<T>& wd, T
                 uint32_t s = b.sorted[cur & 0x7fffffffu];
                 bool skip = any_hit && ii == skip_inst && s == skip_seg;
                 if (!skip) {
-                    uint32_t keep_inst = h.inst;
-                    h.inst = ii;
-                    if (intersect_prim(b, s, o, d, tmin, &h, resolve64)) {
+                    if (intersect_prim(b, ii, s, o, d, tmin, &h, resolve64)) {
                         found = true;
                         if (!in.identity) {
                             double pn[3] = {double(h.n.x), double(h.n.y), double(h.n.z)};
@@ -842,7 +841,7 @@ static bool trace_one(const Scene& sc, const tvec3<T>& wo, const tvec3<T>& wd, T
                             h.n = shim::normalize(n2);
                         }
                         if (any_hit) { *out = h; return true; }
-                    } else h.inst = keep_inst;
+                    }
                 }
             } else {
                 uint32_t l = b.bt.left[cur], r = b.bt.right[cur];
@@ -975,6 +974,31 @@ void orc_generate_lss(const float* lines, int64_t n, float r, float* pos, float*
 }
 uint16_t orc_f32_to_f16(float f) { return f32_to_f16(f); }
 float orc_f16_to_f32(uint16_t h) { return f16_to_f32(h); }
+
+// Quantised Phantom geometry: a chunk is a run of connected lines (end == next start, exact)
+// of at most `chunk` lines; its root is the start of its first line. Control points become
+// root + float(half(cp - root)) and radii float(half(r)) (round to nearest even).
+// Outputs: dequantised curves (n x 12), radii (n x 2), chunk index and first line per line.
+int64_t orc_quantise_phantom(const float* lines, const float* curves, const float* lrad, int64_t n, uint32_t chunk,
+                             float* dq, float* dqr, uint32_t* chunk_id, uint32_t* chunk_first) {
+    if (chunk == 0 || chunk > 256) chunk = 256;
+    int64_t run_start = 0, nchunks = 0, first = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        bool start = i == 0 || !(ld3(lines + 6 * (i - 1) + 3) == ld3(lines + 6 * i));
+        if (start) run_start = i;
+        if ((i - run_start) % chunk == 0) { ++nchunks; first = i; }
+        chunk_id[i] = uint32_t(nchunks - 1);
+        chunk_first[i] = uint32_t(first);
+        const float* root = curves + 12 * first;
+        for (int j = 0; j < 12; ++j) {
+            float off = curves[12 * i + j] - root[j % 3];
+            dq[12 * i + j] = root[j % 3] + f16_to_f32(f32_to_f16(off));
+        }
+        dqr[2 * i] = f16_to_f32(f32_to_f16(lrad[2 * i]));
+        dqr[2 * i + 1] = f16_to_f32(f32_to_f16(lrad[2 * i + 1]));
+    }
+    return nchunks;
+}
 
 // ---- LBVH pipeline (for bit-exact comparison with the device build) -------------------------
 void orc_prim_boxes(int type, const float* data, const float* radius, int64_t n, float* boxes_out) {
@@ -1112,15 +1136,16 @@ void orc_trace_rays(void* s, const float* rays, int64_t n, float tmin, float tma
 // Jitter: spp == 1 and jitter == 0 uses the pixel centre 0.5 (ray_gen.rgen:18); otherwise the
 // offset of sample k of pixel p is (h1 >> 8) * 2^-24, (h2 >> 8) * 2^-24 with
 // h1 = hash(seed ^ hash(p * spp + k)), h2 = hash(h1).
-// Per-sample outputs (W*H*spp): t (double, -1 miss), prim, inst, shadow flag;
-// framebuffer W*H*4 floats (RGBA, A = 1), averaged over samples in sample order.
+// Pixels: first_pixel .. first_pixel + npixels - 1, or pixel_list[0 .. npixels-1] when given.
+// Per-sample outputs (npixels*spp): t (double, -1 miss), prim, inst, shadow flag;
+// framebuffer npixels*4 floats (RGBA, A = 1), averaged over samples in sample order.
 void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t w, uint32_t h, uint32_t spp,
                 int jitter, uint32_t seed, float tmin, float tmax, int shading, float shadow_tmin, int precision,
-                int nthreads, int64_t first_pixel, int64_t npixels, double* t_out, uint32_t* prim_out,
-                uint32_t* inst_out, uint8_t* shadow_out, float* fb) {
+                int nthreads, int64_t first_pixel, int64_t npixels, const uint32_t* pixel_list, double* t_out,
+                uint32_t* prim_out, uint32_t* inst_out, uint8_t* shadow_out, float* fb) {
     const Scene& sc = *static_cast<Scene*>(s);
     parallel_for(npixels, nthreads, [&](int64_t pi) {
-        int64_t p = first_pixel + pi;
+        int64_t p = pixel_list ? int64_t(pixel_list[pi]) : first_pixel + pi;
         uint32_t px = uint32_t(p % w), py = uint32_t(p / w);
         double acc[3] = {0, 0, 0};
         float accf[3] = {0, 0, 0};

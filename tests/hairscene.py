@@ -1,0 +1,153 @@
+"""Test helpers: seeded hair scenes for the GPU library and the CPU oracle, and hit comparison.
+
+The oracle (oracle/) is the checker; it receives the same strands and processes them with its
+own restatement of the reference's geometry code.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from oracle import build as oracle_build  # noqa: E402
+
+PHANTOM, LSS, DOTS = 0, 1, 2
+
+
+def P(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def lines_from_strands(v: np.ndarray, r: np.ndarray | None, off: np.ndarray, const_r: float = 0.02):
+    """Consecutive vertices of each strand form lines (n x 6) with end radii (n x 2)."""
+    ls, rs = [], []
+    for s in range(len(off) - 1):
+        a, b = int(off[s]), int(off[s + 1])
+        if b - a < 2:
+            continue
+        vv = v[a:b]
+        ls.append(np.concatenate([vv[:-1], vv[1:]], axis=1))
+        if r is None:
+            rs.append(np.full((b - a - 1, 2), const_r, np.float32))
+        else:
+            rr = r[a:b]
+            rs.append(np.stack([rr[:-1], rr[1:]], axis=1))
+    if not ls:
+        return np.zeros((0, 6), np.float32), np.zeros((0, 2), np.float32)
+    return (np.ascontiguousarray(np.concatenate(ls), np.float32),
+            np.ascontiguousarray(np.concatenate(rs), np.float32))
+
+
+def oracle_geometry(orc, gtype: int, lines: np.ndarray, lrad: np.ndarray, quantised: bool = False, chunk: int = 0):
+    """Geometry as the oracle restates it: (data, radius) in the layout orc_scene_add_blas takes."""
+    n = lines.shape[0]
+    if gtype == PHANTOM:
+        curves = np.zeros((n, 12), np.float32)
+        orc.orc_generate_curves(P(lines), n, P(curves))
+        rad = lrad.copy()
+        if quantised:
+            dq = np.zeros_like(curves)
+            dqr = np.zeros_like(rad)
+            cid = np.zeros(n, np.uint32)
+            cfirst = np.zeros(n, np.uint32)
+            orc.orc_quantise_phantom(P(lines), P(curves), P(lrad), n, chunk, P(dq), P(dqr), P(cid), P(cfirst))
+            return dq, dqr
+        return curves, rad
+    if gtype == LSS:
+        rad = np.where(lrad < np.float32(0.001), np.float32(0.001), lrad).astype(np.float32)
+        return lines.copy(), np.ascontiguousarray(rad)
+    verts = np.zeros((n, 36), np.float32)
+    orc.orc_generate_dots(P(lines), P(lrad), 0.0, n, P(verts))
+    return verts, np.zeros((n, 2), np.float32)
+
+
+class OracleScene:
+    def __init__(self, orc, blases, transforms=None):
+        """blases: list of (gtype, data, radius); transforms: list of 4x4 row-major or None."""
+        self.orc = orc
+        self.h = orc.orc_scene_create()
+        self._keep = []
+        for i, (gt, data, rad) in enumerate(blases):
+            d = np.ascontiguousarray(data, np.float32)
+            r = np.ascontiguousarray(rad, np.float32)
+            self._keep += [d, r]
+            b = orc.orc_scene_add_blas(self.h, gt, d.shape[0], P(d), P(r))
+            xf = None if transforms is None or transforms[i] is None else \
+                np.ascontiguousarray(np.asarray(transforms[i], np.float32).T.reshape(-1))
+            self._keep.append(xf)
+            orc.orc_scene_add_instance(self.h, b, P(xf))
+
+    def trace_rays(self, rays: np.ndarray, precision: int = 64, tmin=0.001, tmax=10000.0, threads: int = 0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        t = np.zeros(n)
+        prim = np.zeros(n, np.uint32)
+        inst = np.zeros(n, np.uint32)
+        nrm = np.zeros((n, 3))
+        th = threads or max(1, self.orc.orc_hardware_threads())
+        self.orc.orc_trace_rays(self.h, P(rays), n, tmin, tmax, precision, th, P(t), P(prim), P(inst), P(nrm))
+        return t, prim, inst, nrm
+
+    def render(self, view_inv, proj_inv, w, h, spp=1, jitter=0, seed=0, shading=2, precision=64, tmin=0.001,
+               tmax=10000.0, shadow_tmin=1e-4, threads: int = 0, first_pixel=0, npixels=None, pixel_list=None):
+        if pixel_list is not None:
+            pixel_list = np.ascontiguousarray(pixel_list, np.uint32)
+            npixels = len(pixel_list)
+        npx = w * h if npixels is None else npixels
+        t = np.zeros(npx * spp)
+        prim = np.zeros(npx * spp, np.uint32)
+        inst = np.zeros(npx * spp, np.uint32)
+        sh = np.zeros(npx * spp, np.uint8)
+        fb = np.zeros((npx, 4), np.float32)
+        th = threads or max(1, self.orc.orc_hardware_threads())
+        vi = np.ascontiguousarray(view_inv, np.float32)
+        pi = np.ascontiguousarray(proj_inv, np.float32)
+        self.orc.orc_render(self.h, P(vi), P(pi), w, h, spp, jitter, seed, tmin, tmax, shading, shadow_tmin, precision,
+                            th, first_pixel, npx, P(pixel_list), P(t), P(prim), P(inst), P(sh), P(fb))
+        return dict(t=t, prim=prim, inst=inst, shadow=sh, fb=fb)
+
+    def __del__(self):
+        try:
+            self.orc.orc_scene_destroy(self.h)
+        except Exception:
+            pass
+
+
+def compare_hits(g_t, g_prim, g_inst, o_t, o_prim, o_inst, tie_rel=1e-5):
+    """Closest-hit agreement: ids must match unless both hit within tie_rel * t (a tie)."""
+    g_hit = g_t >= 0
+    o_hit = o_t >= 0
+    same = (g_hit == o_hit) & (~g_hit | ((g_prim == o_prim) & (g_inst == o_inst)))
+    both = g_hit & o_hit
+    tie = both & ~same & (np.abs(g_t - o_t) <= tie_rel * np.maximum(np.abs(o_t), 1e-30))
+    mism = ~same & ~tie
+    agree_both = both & same
+    rel = np.abs(g_t[agree_both] - o_t[agree_both]) / o_t[agree_both] if agree_both.any() else np.zeros(0)
+    n = len(g_t)
+    counted = n - tie.sum()
+    return dict(n=n, hits=int(o_hit.sum()), mismatches=int(mism.sum()), ties=int(tie.sum()),
+                agreement=float(1.0 - mism.sum() / max(counted, 1)),
+                max_rel_t=float(rel.max()) if rel.size else 0.0,
+                p9999_rel_t=float(np.quantile(rel, 0.9999)) if rel.size else 0.0,
+                mism_idx=np.nonzero(mism)[0])
+
+
+def load_oracle():
+    return oracle_build.load()
+
+
+def aimed_rays(rng, lines: np.ndarray, n: int, spread: float = 0.01, dist: float = 3.0):
+    """Rays from random directions aimed at points near random segments (hits and near misses)."""
+    idx = rng.integers(0, lines.shape[0], n)
+    a, b = lines[idx, :3], lines[idx, 3:]
+    tgt = a + (b - a) * rng.random((n, 1)) + rng.normal(size=(n, 3)) * spread
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    org = tgt - d * dist
+    return np.concatenate([org, d], axis=1).astype(np.float32)

@@ -1,0 +1,173 @@
+"""Device BVH build vs the CPU oracle: every integer and FP32 stage bit for bit.
+
+Geometry processing (GenerateCurves, DOTS vertices, LSS radii, FP16 chunk quantisation),
+primitive boxes, Morton codes, the stable sort, the Karras hierarchy, the refit, the BVH8
+collapse (topology, child boxes, leaf order) and the 8-bit node quantisation.
+"""
+import numpy as np
+import pytest
+
+import vkhrt_gb300 as H
+from hairscene import DOTS, LSS, PHANTOM, P, lines_from_strands, oracle_geometry
+
+pytestmark = pytest.mark.gpu
+
+NODEF = np.dtype([("lo_x", "<f4", 8), ("hi_x", "<f4", 8), ("lo_y", "<f4", 8), ("hi_y", "<f4", 8),
+                  ("lo_z", "<f4", 8), ("hi_z", "<f4", 8), ("child_base", "<u4"), ("prim_base", "<u4"),
+                  ("meta", "u1", 8), ("pad", "<u4", 4)])
+NODEQ = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("nchild", "u1"), ("child_base", "<u4"), ("prim_base", "<u4"),
+                  ("meta", "u1", 8), ("qlo_x", "u1", 8), ("qhi_x", "u1", 8), ("qlo_y", "u1", 8), ("qhi_y", "u1", 8),
+                  ("qlo_z", "u1", 8), ("qhi_z", "u1", 8)])
+PRIMH = np.dtype([("h", "<u2", 14), ("key", "<u4")])
+assert NODEF.itemsize == 224 and NODEQ.itemsize == 80 and PRIMH.itemsize == 32
+
+
+def oracle_bvh(orc, boxes, max_leaf):
+    n = len(boxes)
+    out = dict(codes=np.zeros(n, np.uint64), srt=np.zeros(n, np.uint32), L=np.zeros(max(n - 1, 0), np.uint32),
+               R=np.zeros(max(n - 1, 0), np.uint32), F=np.zeros(max(n - 1, 0), np.uint32),
+               La=np.zeros(max(n - 1, 0), np.uint32), pi=np.zeros(max(n - 1, 0), np.uint32),
+               pl=np.zeros(n, np.uint32), nb=np.zeros((max(n - 1, 0), 6), np.float32))
+    orc.orc_lbvh(P(boxes), n, *[P(out[k]) for k in ("codes", "srt", "L", "R", "F", "La", "pi", "pl", "nb")])
+    mx = max(n, 1)
+    w = dict(cb=np.zeros(mx, np.uint32), pb=np.zeros(mx, np.uint32), meta=np.zeros((mx, 8), np.uint8),
+             cbox=np.zeros((mx, 8, 6), np.float32), order=np.zeros(n, np.uint32), qp=np.zeros((mx, 3), np.float32),
+             qe=np.zeros((mx, 3), np.uint8), qlo=np.zeros((mx, 3, 8), np.uint8), qhi=np.zeros((mx, 3, 8), np.uint8))
+    nn = orc.orc_bvh8(P(boxes), n, max_leaf, mx, *[P(w[k]) for k in ("cb", "pb", "meta", "cbox", "order", "qp", "qe",
+                                                                    "qlo", "qhi")])
+    out.update(w)
+    out["nn"] = nn
+    return out
+
+
+def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=None, const_radius=0.02, chunk=0):
+    inp = H.BLASInput(type=H.BLASType(gtype), vertices=v, radius=r, strand_offsets=None if line_indices is not None else off,
+                      line_indices=line_indices, precision=H.Precision(precision), max_leaf=max_leaf,
+                      const_radius=const_radius, keep_intermediate=True, quant_chunk=chunk)
+    blas = H.BottomLevelAccelerationStructure(inp, ctx)
+    if line_indices is None:
+        lines, lrad = lines_from_strands(v, r, off, const_radius)
+    else:
+        li = np.asarray(line_indices).reshape(-1, 2)
+        lines = np.ascontiguousarray(np.concatenate([v[li[:, 0]], v[li[:, 1]]], axis=1), np.float32)
+        lrad = np.ascontiguousarray(np.stack([r[li[:, 0]], r[li[:, 1]]], axis=1) if r is not None
+                                    else np.full((len(li), 2), const_radius, np.float32), np.float32)
+    n = len(lines)
+    assert blas.info["nprims"] == n
+    quant_prims = precision == 1 and gtype == PHANTOM
+    data, rad = oracle_geometry(orc, gtype, lines, lrad, quantised=quant_prims, chunk=chunk)
+    if n == 0:
+        assert blas.info["nnodes"] == 0
+        return blas
+    if gtype == PHANTOM:
+        ref_curves = np.zeros((n, 12), np.float32)
+        orc.orc_generate_curves(P(lines), n, P(ref_curves))
+        assert blas.get(H.Part.CURVES, np.float32, (n, 12)).tobytes() == ref_curves.tobytes()
+    elif gtype == LSS:
+        g = blas.get(H.Part.LSS, np.float32, (n, 8))
+        assert g[:, :6].tobytes() == np.ascontiguousarray(data).tobytes()
+        assert np.ascontiguousarray(g[:, 6:]).tobytes() == rad.tobytes()
+    else:
+        assert blas.get(H.Part.DOTS_VERTICES, np.float32, (n, 36)).tobytes() == data.tobytes()
+    ref_boxes = np.zeros((n, 6), np.float32)
+    orc.orc_prim_boxes(gtype, P(np.ascontiguousarray(data)), P(np.ascontiguousarray(rad)), n, P(ref_boxes))
+    assert blas.get(H.Part.PRIM_BOXES, np.float32, (n, 6)).tobytes() == ref_boxes.tobytes()
+    o = oracle_bvh(orc, ref_boxes, max_leaf)
+    assert np.array_equal(blas.get(H.Part.MORTON_SORTED, np.uint64, n), o["codes"])
+    assert np.array_equal(blas.get(H.Part.SORTED_INDEX, np.uint32, n), o["srt"])
+    if n >= 2:
+        assert np.array_equal(blas.get(H.Part.BIN_LEFT, np.uint32, n - 1), o["L"])
+        assert np.array_equal(blas.get(H.Part.BIN_RIGHT, np.uint32, n - 1), o["R"])
+        assert blas.get(H.Part.BIN_BOXES, np.float32, (n - 1, 6)).tobytes() == o["nb"].tobytes()
+    nn = o["nn"]
+    assert blas.info["nnodes"] == nn
+    assert np.array_equal(blas.get(H.Part.PRIM_ORDER, np.uint32, n), o["order"])
+    qn = blas.get(H.Part.QNODES, np.uint8, nn * 80).view(NODEQ)
+    assert np.array_equal(qn["child_base"], o["cb"][:nn]) and np.array_equal(qn["prim_base"], o["pb"][:nn])
+    assert np.array_equal(qn["meta"], o["meta"][:nn])
+    assert qn["p"].tobytes() == o["qp"][:nn].tobytes() and np.array_equal(qn["e"], o["qe"][:nn])
+    for k, ax in enumerate("xyz"):
+        assert np.array_equal(qn["qlo_" + ax], o["qlo"][:nn, k]) and np.array_equal(qn["qhi_" + ax], o["qhi"][:nn, k])
+    if precision == 0:
+        fn = blas.get(H.Part.NODES, np.uint8, nn * 224).view(NODEF)
+        for k, ax in enumerate("xyz"):
+            assert fn["lo_" + ax].tobytes() == np.ascontiguousarray(o["cbox"][:nn, :, k]).tobytes()
+            assert fn["hi_" + ax].tobytes() == np.ascontiguousarray(o["cbox"][:nn, :, 3 + k]).tobytes()
+        assert np.array_equal(fn["meta"], o["meta"][:nn])
+    if quant_prims:
+        recs = blas.get(H.Part.PRIMS, np.uint8, n * 32).view(PRIMH)
+        halves = recs["h"].view(np.float16).astype(np.float32)
+        key = recs["key"]
+        nroots = int(key.max() >> 8) + 1
+        roots = blas.get(H.Part.ROOTS, np.float32, (nroots, 4))
+        rt = roots[key >> 8, :3]
+        deq = (np.repeat(rt, 4, axis=0).reshape(n, 4, 3) + halves[:, :12].reshape(n, 4, 3)).astype(np.float32)
+        order = o["order"]
+        assert deq.reshape(n, 12).tobytes() == np.ascontiguousarray(data[order]).tobytes()
+        assert np.ascontiguousarray(halves[:, 12:14]).tobytes() == np.ascontiguousarray(rad[order]).tobytes()
+        first = roots[key >> 8, 3].view(np.uint32)
+        assert np.array_equal(first + (key & 0xff), order)
+    return blas
+
+
+@pytest.mark.parametrize("gtype", [PHANTOM, LSS, DOTS])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_build_bit_exact(ctx, orc, gtype, precision):
+    v, r, off = H.generate_strands(H.StrandParams(seed=5, nstrands=400, nverts=17))
+    check_blas(ctx, orc, gtype, precision, v, r, off)
+
+
+@pytest.mark.parametrize("max_leaf", [2, 3])
+def test_build_multi_primitive_leaves(ctx, orc, max_leaf):
+    v, r, off = H.generate_strands(H.StrandParams(seed=6, nstrands=300, nverts=9))
+    check_blas(ctx, orc, PHANTOM, 0, v, r, off, max_leaf=max_leaf)
+
+
+def test_build_large_bit_exact(ctx, orc):
+    # 20,000 strands x 32 vertices = 620,000 segments: several radix-sort tiles and scan levels
+    v, r, off = H.generate_strands(H.StrandParams(seed=9, nstrands=20000, nverts=32))
+    check_blas(ctx, orc, PHANTOM, 1, v, r, off)
+
+
+def test_build_reference_literal_radius(ctx, orc):
+    # no per-vertex radii: the reference's constant 0.02 (geometry_processor.cpp:635)
+    v, _, off = H.generate_strands(H.StrandParams(seed=8, nstrands=100, nverts=12))
+    check_blas(ctx, orc, PHANTOM, 0, v, None, off, const_radius=0.02)
+    check_blas(ctx, orc, DOTS, 0, v, None, off, const_radius=0.02)
+
+
+def test_build_line_indices_and_chunks(ctx, orc):
+    # explicit index pairs (GenerateLines) in shuffled order: neighbours are only found when
+    # consecutive; quantised chunks of at most 5 segments
+    v, r, off = H.generate_strands(H.StrandParams(seed=10, nstrands=50, nverts=20))
+    pairs = np.array([(i, i + 1) for s in range(50) for i in range(int(off[s]), int(off[s + 1]) - 1)], np.uint32)
+    rng = np.random.default_rng(0)
+    sh = pairs.copy()
+    rng.shuffle(sh[: len(sh) // 2])
+    check_blas(ctx, orc, PHANTOM, 1, v, r, off, line_indices=sh, chunk=5)
+    check_blas(ctx, orc, LSS, 0, v, r, off, line_indices=sh)
+
+
+def test_build_edge_cases(ctx, orc):
+    # empty (single-vertex strands), one segment, two segments, a zero-length segment
+    v = np.array([[0, 0, 0], [0, 1, 0], [0, 2, 0], [1, 0, 0], [1, 0, 0], [1, 1, 0]], np.float32)
+    r = np.full(6, 0.01, np.float32)
+    check_blas(ctx, orc, PHANTOM, 0, v, r, np.array([0, 1, 2, 3], np.uint32))      # no lines
+    check_blas(ctx, orc, PHANTOM, 0, v, r, np.array([0, 2], np.uint32))            # one line
+    check_blas(ctx, orc, LSS, 0, v, r, np.array([0, 3], np.uint32))                # two lines
+    check_blas(ctx, orc, PHANTOM, 1, v, r, np.array([0, 3, 6], np.uint32))         # zero-length line
+
+
+def test_build_rejects_bad_input(ctx):
+    v = np.zeros((4, 3), np.float32)
+    with pytest.raises(H.HrtError) as e:
+        H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v,
+                                                       strand_offsets=np.array([0, 5], np.uint32)), ctx)
+    assert e.value.status == 1
+    with pytest.raises(H.HrtError) as e:
+        H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v,
+                                                       line_indices=np.array([[0, 9]], np.uint32)), ctx)
+    assert e.value.status == 1
+    with pytest.raises(H.HrtError):
+        H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v, max_leaf=4,
+                                                       strand_offsets=np.array([0, 4], np.uint32)), ctx)

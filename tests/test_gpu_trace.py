@@ -1,0 +1,214 @@
+"""The CUDA trace pass vs the FP64 CPU oracle on the same seeded scenes.
+
+Closest-hit primitive ids must agree except within t-ties (|t1 - t2| <= 1e-5 t), at >= 99.99 %
+of the rays; distances of agreeing hits within 1e-5 relative; pixels within 1e-4 where the hits
+(and shadow rays) agree.
+"""
+import numpy as np
+import pytest
+
+import vkhrt_gb300 as H
+from hairscene import DOTS, LSS, PHANTOM, OracleScene, aimed_rays, compare_hits, lines_from_strands, oracle_geometry
+
+pytestmark = pytest.mark.gpu
+
+T_REL = 1e-5     # hit distance, relative
+RGB_ABS = 1e-4   # pixel colour, absolute
+AGREE = 0.9999   # closest-hit id agreement outside t-ties
+
+
+def make_scene(ctx, orc, gtype, precision=0, seed=21, ns=300, nv=17, radius=True, const_radius=0.02,
+               transform=None):
+    v, r, off = H.generate_strands(H.StrandParams(seed=seed, nstrands=ns, nverts=nv))
+    if not radius:
+        r = None
+    xf = np.eye(4, dtype=np.float32) if transform is None else transform
+    blas = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=H.BLASType(gtype), vertices=v, radius=r, strand_offsets=off, precision=H.Precision(precision),
+                    const_radius=const_radius, transform=xf), ctx)
+    tlas = H.TopLevelAccelerationStructure([blas], ctx)
+    lines, lrad = lines_from_strands(v, r, off, const_radius)
+    data, rad = oracle_geometry(orc, gtype, lines, lrad, quantised=(precision == 1 and gtype == PHANTOM))
+    osc = OracleScene(orc, [(gtype, data, rad)], [None if transform is None else transform])
+    return blas, tlas, osc, lines
+
+
+@pytest.mark.parametrize("gtype", [PHANTOM, LSS, DOTS])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_trace_rays_vs_fp64_oracle(ctx, orc, gtype, precision):
+    blas, tlas, osc, lines = make_scene(ctx, orc, gtype, precision)
+    rng = np.random.default_rng(100 + gtype)
+    rays = aimed_rays(rng, lines, 20000, spread=0.006)
+    g = H.trace_rays(ctx, tlas, rays)
+    o_t, o_prim, o_inst, _ = osc.trace_rays(rays, precision=64)
+    g_t = np.where(g["t"] >= 0, g["t"].astype(np.float64), -1.0)
+    st = compare_hits(g_t, g["prim"], g["inst"], o_t, o_prim, o_inst)
+    print(gtype, precision, {k: v for k, v in st.items() if k != "mism_idx"})
+    assert st["hits"] > 3000
+    assert st["agreement"] >= AGREE
+    assert st["p9999_rel_t"] <= T_REL
+
+
+def test_trace_rays_fp32_resolve_off_vs_fp32_oracle(ctx, orc):
+    """Without the FP64 re-solve the GPU's FP32 Phantom is the oracle's FP32 algorithm."""
+    blas, tlas, osc, lines = make_scene(ctx, orc, PHANTOM, 0, seed=22)
+    rays = aimed_rays(np.random.default_rng(5), lines, 20000, spread=0.006)
+    g = H.trace_rays(ctx, tlas, rays, H.trace_params(fp64_resolve=0))
+    o_t, o_prim, o_inst, _ = osc.trace_rays(rays, precision=32)
+    g_t = np.where(g["t"] >= 0, g["t"].astype(np.float64), -1.0)
+    st = compare_hits(g_t, g["prim"], g["inst"], o_t, o_prim, o_inst)
+    assert st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
+
+
+def render_both(ctx, tlas, osc, w, h, spp=1, shading=2, jitter=0, seed=0):
+    cam = H.scene_camera(w, h)
+    vi, pi = H.camera_arrays(cam)
+    fr = H.Frame(ctx, w, h, spp, with_hits=True)
+    H.trace(ctx, tlas, cam, fr, H.trace_params(spp=spp, shading=shading, jitter=jitter, seed=seed, record_hits=1))
+    rgba, hits = fr.download(hits=True)
+    o = osc.render(vi, pi, w, h, spp=spp, jitter=jitter, seed=seed, shading=shading, precision=64)
+    return fr, rgba, hits, o
+
+
+def frame_checks(rgba, hits, o, spp):
+    g_t = np.where(hits["t"] >= 0, hits["t"].astype(np.float64), -1.0)
+    st = compare_hits(g_t, hits["prim"], hits["inst"], o["t"], o["prim"], o["inst"])
+    # pixels whose samples all agree (ids and shadow flags) must match in colour
+    shadow_g = (hits["flags"] & H.HIT_SHADOWED) != 0
+    same = (hits["prim"] == o["prim"]) & (shadow_g == (o["shadow"] != 0))
+    px_ok = same.reshape(-1, spp).all(axis=1)
+    diff = np.abs(rgba.reshape(-1, 4) - o["fb"]).max(axis=1)
+    return st, px_ok, diff
+
+
+@pytest.mark.parametrize("gtype", [PHANTOM, LSS, DOTS])
+def test_frame_shaded_with_shadows(ctx, orc, gtype):
+    blas, tlas, osc, _ = make_scene(ctx, orc, gtype, 0, seed=31, ns=1000, nv=32)
+    fr, rgba, hits, o = render_both(ctx, tlas, osc, 160, 120, spp=1, shading=2)
+    st, px_ok, diff = frame_checks(rgba, hits, o, 1)
+    print(gtype, {k: v for k, v in st.items() if k != "mism_idx"}, "pixels agreeing", px_ok.mean(),
+          "max rgb diff there", diff[px_ok].max())
+    assert st["hits"] > 1000
+    assert st["agreement"] >= AGREE
+    assert st["p9999_rel_t"] <= T_REL
+    assert px_ok.mean() >= 0.999
+    assert diff[px_ok].max() <= RGB_ABS
+    assert np.all(rgba[..., 3] == 1.0)
+    s = fr.stats()
+    assert s["primary_rays"] == 160 * 120 and s["shadow_rays"] == int((hits["t"] >= 0).sum())
+
+
+def test_frame_reference_literal_debug_colours(ctx, orc):
+    """Constant radius 0.02 and the debug palette: the reference's own closest-hit output."""
+    blas, tlas, osc, _ = make_scene(ctx, orc, PHANTOM, 0, seed=32, ns=300, nv=16, radius=False, const_radius=0.02)
+    fr, rgba, hits, o = render_both(ctx, tlas, osc, 128, 96, spp=1, shading=0)
+    st, px_ok, diff = frame_checks(rgba, hits, o, 1)
+    assert st["agreement"] >= AGREE
+    assert diff[px_ok].max() == 0.0  # palette colours are exact
+    hit = hits["t"] >= 0
+    pal = np.array([[1.0, 0.0, 0.3], [0.8, 0.2, 0.3], [0.6, 0.4, 0.3], [0.4, 0.6, 0.3], [0.2, 0.8, 0.3],
+                    [0.0, 1.0, 0.3]], np.float32)
+    assert np.array_equal(rgba.reshape(-1, 4)[hit, :3], pal[hits["prim"][hit] % 6])
+    assert np.all(rgba.reshape(-1, 4)[~hit, :3] == 0.0)  # miss: black background
+
+
+def test_frame_quantised_jittered_spp4(ctx, orc):
+    blas, tlas, osc, _ = make_scene(ctx, orc, PHANTOM, 1, seed=33, ns=600, nv=64)
+    fr, rgba, hits, o = render_both(ctx, tlas, osc, 96, 64, spp=4, shading=2, jitter=1, seed=9)
+    st, px_ok, diff = frame_checks(rgba, hits, o, 4)
+    print({k: v for k, v in st.items() if k != "mism_idx"}, px_ok.mean())
+    assert st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
+    assert px_ok.mean() >= 0.998 and diff[px_ok].max() <= RGB_ABS
+
+
+def test_instance_transform(ctx, orc):
+    xf = np.array([[0.0, -1.2, 0.0, 0.1], [1.2, 0.0, 0.0, -0.3], [0.0, 0.0, 1.2, 0.2], [0, 0, 0, 1]], np.float32)
+    blas, tlas, osc, lines = make_scene(ctx, orc, LSS, 0, seed=34, transform=xf)
+    np.testing.assert_array_equal(blas.Transform(), xf)
+    assert blas.Type() == H.BLASType.eLSS
+    wl = lines.reshape(-1, 3) @ xf[:3, :3].T + xf[:3, 3]
+    rays = aimed_rays(np.random.default_rng(8), wl.reshape(-1, 6).astype(np.float32), 10000, spread=0.006)
+    g = H.trace_rays(ctx, tlas, rays)
+    o_t, o_prim, o_inst, _ = osc.trace_rays(rays, precision=64)
+    st = compare_hits(np.where(g["t"] >= 0, g["t"].astype(np.float64), -1.0), g["prim"], g["inst"], o_t, o_prim, o_inst)
+    assert st["hits"] > 1000 and st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
+
+
+def test_two_instances_ids(ctx, orc):
+    v1, r1, o1 = H.generate_strands(H.StrandParams(seed=40, nstrands=200, nverts=16))
+    v2, r2, o2 = H.generate_strands(H.StrandParams(seed=41, nstrands=200, nverts=16))
+    b1 = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.eDOTS, vertices=v1, radius=r1, strand_offsets=o1), ctx)
+    b2 = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v2, radius=r2, strand_offsets=o2), ctx)
+    tlas = H.TopLevelAccelerationStructure([b1, b2], ctx)
+    l1, lr1 = lines_from_strands(v1, r1, o1)
+    l2, lr2 = lines_from_strands(v2, r2, o2)
+    osc = OracleScene(orc, [(DOTS, *oracle_geometry(orc, DOTS, l1, lr1)), (PHANTOM, *oracle_geometry(orc, PHANTOM, l2, lr2))])
+    rng = np.random.default_rng(3)
+    rays = np.concatenate([aimed_rays(rng, l1, 5000, 0.006), aimed_rays(rng, l2, 5000, 0.006)])
+    g = H.trace_rays(ctx, tlas, rays)
+    o_t, o_prim, o_inst, _ = osc.trace_rays(rays, precision=64)
+    st = compare_hits(np.where(g["t"] >= 0, g["t"].astype(np.float64), -1.0), g["prim"], g["inst"], o_t, o_prim, o_inst)
+    assert set(np.unique(g["inst"][g["t"] >= 0])) == {0, 1}
+    assert st["agreement"] >= AGREE
+
+
+def test_batch_equals_single_launches(ctx, orc):
+    scenes = []
+    for k, (gt, ns, w, h, spp) in enumerate([(PHANTOM, 200, 64, 48, 1), (LSS, 300, 80, 40, 2), (DOTS, 150, 40, 40, 3)]):
+        v, r, off = H.generate_strands(H.StrandParams(seed=50 + k, nstrands=ns, nverts=16))
+        b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType(gt), vertices=v, radius=r, strand_offsets=off), ctx)
+        t = H.TopLevelAccelerationStructure([b], ctx)
+        scenes.append((b, t, H.scene_camera(w, h), H.Frame(ctx, w, h, spp, with_hits=True), w, h, spp))
+    p = H.trace_params(shading=2, record_hits=1, jitter=1, seed=4)
+    batch = H.Batch(ctx, [(t, cam, fr) for (_, t, cam, fr, *_r) in scenes], p)
+    batch.launch()
+    batch_out = [fr.download(hits=True) for (_, _, _, fr, *_r) in scenes]
+    batch.launch()  # graph replay is repeatable
+    for (rgba, hits), (_, _, _, fr, *_r) in zip(batch_out, scenes):
+        rgba2, hits2 = fr.download(hits=True)
+        assert np.array_equal(rgba, rgba2) and np.array_equal(hits, hits2)
+    for (rgba, hits), (b, t, cam, _, w, h, spp) in zip(batch_out, scenes):
+        fr = H.Frame(ctx, w, h, spp, with_hits=True)
+        H.trace(ctx, t, cam, fr, p)
+        rgba1, hits1 = fr.download(hits=True)
+        assert np.array_equal(rgba, rgba1) and np.array_equal(hits, hits1)
+
+
+def test_empty_scene_and_misses(ctx):
+    v = np.zeros((2, 3), np.float32)
+    b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v,
+                                                       strand_offsets=np.array([0, 1, 2], np.uint32)), ctx)
+    t = H.TopLevelAccelerationStructure([b], ctx)
+    fr = H.Frame(ctx, 16, 16, 1, with_hits=True)
+    H.trace(ctx, t, H.scene_camera(16, 16), fr, H.trace_params(shading=2, record_hits=1))
+    rgba, hits = fr.download(hits=True)
+    assert np.all(hits["t"] == -1.0) and np.all(hits["prim"] == 0xffffffff)
+    assert np.all(rgba[..., :3] == 0.0) and np.all(rgba[..., 3] == 1.0)
+    t0 = H.TopLevelAccelerationStructure([], ctx)
+    H.trace(ctx, t0, H.scene_camera(16, 16), fr, H.trace_params())
+
+
+def test_trace_rejects_bad_arguments(ctx):
+    v, r, off = H.generate_strands(H.StrandParams(seed=60, nstrands=10, nverts=8))
+    b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r, strand_offsets=off), ctx)
+    bq = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r, strand_offsets=off,
+                                                        precision=H.Precision.QUANTISED), ctx)
+    with pytest.raises(H.HrtError) as e:
+        H.TopLevelAccelerationStructure([b, bq], ctx)
+    assert e.value.status == 6
+    t = H.TopLevelAccelerationStructure([b], ctx)
+    fr = H.Frame(ctx, 8, 8, 1, with_hits=False)
+    with pytest.raises(H.HrtError) as e:
+        H.trace(ctx, t, H.scene_camera(8, 8), fr, H.trace_params(record_hits=1))
+    assert e.value.status == 1
+    with pytest.raises(H.HrtError):
+        H.trace(ctx, t, H.scene_camera(8, 8), fr, H.trace_params(shading=7))
+    with pytest.raises(H.HrtError):
+        H.Frame(ctx, 0, 8, 1)
+
+
+def test_generator_checksum_on_this_host():
+    """The strand generator gives the same bits on the GPU machine's host as elsewhere."""
+    from test_abi import C1_CHECKSUM
+    v, r, _ = H.generate_strands(H.StrandParams())
+    assert H.checksum(v, r) == C1_CHECKSUM

@@ -1,0 +1,165 @@
+"""Known-answer and property tests of the CPU oracle (no GPU)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from hairscene import DOTS, LSS, PHANTOM, P, OracleScene
+
+
+def test_f16_round_trip_matches_ieee(orc):
+    rng = np.random.default_rng(3)
+    xs = np.concatenate([rng.normal(size=20000) * s for s in (1e-6, 1e-3, 1, 100, 6e4)]).astype(np.float32)
+    xs = np.concatenate([xs, np.float32([0.0, -0.0, 65504.0, 65520.0, 6.1e-5, 5.96e-8, 2.98e-8, 1e-9])])
+    with np.errstate(over="ignore"):
+        ref = np.float16(xs)
+    for x, hx in zip(xs, ref):
+        h = orc.orc_f32_to_f16(float(x))
+        assert h == int(hx.view(np.uint16)), x
+        assert np.float32(orc.orc_f16_to_f32(h)).tobytes() == np.float32(hx).tobytes()
+
+
+def test_prhi_straight_curve_known_answer(orc):
+    # straight curve along x at y = z = 0; a ray down -z at x = 0.3 meets the tube at z = r
+    st = ctypes.c_int()
+    curve = np.array([0, 0, 0, 1 / 3, 0, 0, 2 / 3, 0, 0, 1, 0, 0], np.float64)
+    ray = np.array([0.3, 0.0, 5.0, 0.0, 0.0, -1.0], np.float64)
+    nrm = np.zeros(3)
+    t = orc.orc_prhi_f64(P(ray), P(curve), 0.02, 0.02, P(nrm), ctypes.byref(st))
+    assert st.value == 1
+    assert abs(t - 4.98) < 1e-9
+    assert np.allclose(nrm, [0, 0, 1], atol=1e-6)
+    # tapered radius 0.01 -> 0.03: at x = 0.3 the radius is 0.016
+    t = orc.orc_prhi_f64(P(ray), P(curve), 0.01, 0.03, P(nrm), ctypes.byref(st))
+    assert st.value == 1 and abs(t - (5.0 - 0.016)) < 1e-6
+
+
+def test_prhi_axis_parallel_ray_is_a_miss(orc):
+    # ray along the axis of a straight curve: c = 0 in cone.glsl:55 gives NaN -> no report
+    st = ctypes.c_int()
+    curve = np.array([0, 0, 0, 0, 0, 1 / 3, 0, 0, 2 / 3, 0, 0, 1], np.float32)
+    ray = np.array([0, 0, -5, 0, 0, 1], np.float32)
+    nrm = np.zeros(3, np.float32)
+    t = orc.orc_prhi_f32(P(ray), P(curve), 0.02, 0.02, P(nrm), ctypes.byref(st))
+    assert t == 0.0 and st.value != 1
+
+
+def test_lss_known_answers(orc):
+    # one swept sphere from (0,0,0) r=0.1 to (1,0,0) r=0.2
+    data = np.array([[0, 0, 0, 1, 0, 0]], np.float32)
+    rad = np.array([[0.1, 0.2]], np.float32)
+    sc = OracleScene(orc, [(LSS, data, rad)])
+    rays = np.array([
+        [-5, 0, 0, 1, 0, 0],      # along the axis: hits the start sphere at x = -0.1
+        [6, 0, 0, -1, 0, 0],      # from the other side: end sphere at x = 1.2
+        [0.5, 5, 0, 0, -1, 0],    # side: tangent cone, analytic below
+        [0.5, 5, 0.5, 0, -1, 0],  # miss
+    ], np.float32)
+    t, prim, inst, nrm = sc.trace_rays(rays)
+    assert abs(t[0] - 4.9) < 1e-6 and abs(t[1] - 4.8) < 1e-6  # radii are float32
+    # side hit on the tangent cone: in the xy-plane the surface is the outer common tangent
+    # y = m x + c of the circles (0,0; 0.1) and (1,0; 0.2): c = 0.1 s, m + c = 0.2 s, s = sqrt(1+m^2)
+    m = np.sqrt(0.01 / 0.99)
+    c = 0.1 * np.sqrt(1 + m * m)
+    assert abs(t[2] - (5.0 - (m * 0.5 + c))) < 1e-6
+    assert np.allclose(nrm[2], [-m / np.sqrt(1 + m * m), 1 / np.sqrt(1 + m * m), 0], atol=1e-6)
+    assert t[3] < 0
+
+
+def test_triangle_dots_known_answer(orc):
+    # one vertical DOTS segment along +y from the origin, radius 0.05
+    lines = np.array([[0, 0, 0, 0, 1, 0]], np.float32)
+    verts = np.zeros((1, 36), np.float32)
+    orc.orc_generate_dots(P(lines), None, 0.05, 1, P(verts))
+    sc = OracleScene(orc, [(DOTS, verts, np.zeros((1, 2), np.float32))])
+    rays = np.array([[0.01, 0.5, 5, 0, 0, -1], [0.2, 0.5, 5, 0, 0, -1]], np.float32)
+    t, prim, inst, _ = sc.trace_rays(rays)
+    assert t[1] < 0
+    assert t[0] > 4.9 and (prim[0] >> 2) == 0
+
+
+def _random_boxes(rng, n):
+    c = rng.random((n, 3)).astype(np.float32) * 4 - 2
+    e = (rng.random((n, 3)) * 0.05).astype(np.float32)
+    return np.ascontiguousarray(np.concatenate([c - e, c + e], axis=1), np.float32)
+
+
+@pytest.mark.parametrize("n,max_leaf", [(1, 1), (2, 1), (3, 2), (1000, 1), (1000, 3), (5000, 2)])
+def test_bvh8_properties(orc, n, max_leaf):
+    rng = np.random.default_rng(n + max_leaf)
+    boxes = _random_boxes(rng, n)
+    if n > 10:
+        boxes[10:20] = boxes[10]  # duplicate boxes -> duplicate Morton codes
+    mx = max(n, 1)
+    cb = np.zeros(mx, np.uint32)
+    pb = np.zeros(mx, np.uint32)
+    meta = np.zeros((mx, 8), np.uint8)
+    cbox = np.zeros((mx, 8, 6), np.float32)
+    order = np.zeros(n, np.uint32)
+    qp = np.zeros((mx, 3), np.float32)
+    qe = np.zeros((mx, 3), np.uint8)
+    qlo = np.zeros((mx, 3, 8), np.uint8)
+    qhi = np.zeros((mx, 3, 8), np.uint8)
+    nn = orc.orc_bvh8(P(boxes), n, max_leaf, mx, P(cb), P(pb), P(meta), P(cbox), P(order), P(qp), P(qe), P(qlo), P(qhi))
+    assert nn > 0
+    # every primitive exactly once
+    assert np.array_equal(np.sort(order), np.arange(n))
+    seen_nodes = {0}
+    for i in range(nn):
+        poff = 0
+        for q in range(8):
+            m = int(meta[i, q])
+            if m == 0:
+                continue
+            if m & 0x80:
+                child = int(cb[i]) + (m & 7)
+                assert child < nn and child not in seen_nodes
+                seen_nodes.add(child)
+                # the child's boxes lie inside this slot's box
+                inner = cbox[child][meta[child] != 0]
+                assert (inner[:, :3] >= cbox[i, q, :3]).all() and (inner[:, 3:] <= cbox[i, q, 3:]).all()
+            else:
+                cnt, off = m >> 5, m & 31
+                assert 1 <= cnt <= max_leaf and off == poff
+                poff += cnt
+                for j in range(cnt):
+                    b = boxes[order[int(pb[i]) + off + j]]
+                    assert (b[:3] >= cbox[i, q, :3]).all() and (b[3:] <= cbox[i, q, 3:]).all()
+            # quantised box is conservative: p + q 2^e (one rounding) encloses the FP32 box
+            for k in range(3):
+                s = np.float32(2.0 ** (int(qe[i, k]) - 127))
+                lo = np.float32(qp[i, k]) + np.float32(qlo[i, k, q]) * s
+                hi = np.float32(qp[i, k]) + np.float32(qhi[i, k, q]) * s
+                assert lo <= cbox[i, q, k] and hi >= cbox[i, q, 3 + k]
+    assert len(seen_nodes) == nn
+
+
+def test_karras_ranges(orc):
+    rng = np.random.default_rng(11)
+    n = 3000
+    boxes = _random_boxes(rng, n)
+    boxes[100:140] = boxes[100]
+    codes = np.zeros(n, np.uint64)
+    srt = np.zeros(n, np.uint32)
+    L = np.zeros(n - 1, np.uint32)
+    R = np.zeros(n - 1, np.uint32)
+    F = np.zeros(n - 1, np.uint32)
+    La = np.zeros(n - 1, np.uint32)
+    pi = np.zeros(n - 1, np.uint32)
+    pl = np.zeros(n, np.uint32)
+    nb = np.zeros((n - 1, 6), np.float32)
+    orc.orc_lbvh(P(boxes), n, P(codes), P(srt), P(L), P(R), P(F), P(La), P(pi), P(pl), P(nb))
+    assert np.all(codes[1:] >= codes[:-1])
+    assert np.array_equal(np.sort(srt), np.arange(n))
+    leaf = 0x80000000
+
+    def rng_of(c):
+        return (c & ~leaf, c & ~leaf) if c & leaf else (F[c], La[c])
+
+    for i in range(n - 1):
+        a0, a1 = rng_of(int(L[i]))
+        b0, b1 = rng_of(int(R[i]))
+        assert a0 == F[i] and b1 == La[i] and a1 + 1 == b0
+    assert F[0] == 0 and La[0] == n - 1
+    # root box = union of all boxes
+    assert np.array_equal(nb[0, :3], boxes[:, :3].min(0)) and np.array_equal(nb[0, 3:], boxes[:, 3:].max(0))

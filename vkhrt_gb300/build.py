@@ -1,0 +1,82 @@
+"""Builds vkhrt_gb300/libhrt.so (the C ABI of include/hrt.h) for sm_103a with nvcc.
+
+Translation units compile in parallel:
+  csrc/build.cu    --fmad=false (bit-exact BVH build)
+  csrc/trace.cu    trace kernels
+  csrc/api.cu      C ABI (host code)
+  csrc/strands.cpp synthetic strands (host, -ffp-contract=off)
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libhrt.so")
+INCLUDE = os.path.join(ROOT, "include")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+UNITS = {
+    "build.cu": ["--fmad=false"],
+    "trace.cu": [],
+    "api.cu": [],
+    "strands.cpp": ["-x", "c++", "-Xcompiler", "-ffp-contract=off"],
+}
+
+
+def _deps() -> list[str]:
+    out = [os.path.join(INCLUDE, "hrt.h")]
+    for f in os.listdir(CSRC):
+        out.append(os.path.join(CSRC, f))
+    return out
+
+
+def _compile(nvcc: str, src: str, extra: list[str], verbose: bool) -> str:
+    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-I" + INCLUDE, "-I" + CSRC,
+           "-Xcompiler", "-fPIC", *extra, "-c", src, "-o", obj]
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    if verbose and r.stderr:
+        print(r.stderr)
+    return obj
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile and link libhrt.so in-tree; a no-op when it is newer than its sources."""
+    if not force and os.path.exists(LIB):
+        t = os.path.getmtime(LIB)
+        if all(os.path.getmtime(d) <= t for d in _deps()):
+            return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        futs = [ex.submit(_compile, nvcc, os.path.join(CSRC, f), extra, verbose) for f, extra in UNITS.items()]
+        objs = [f.result() for f in futs]
+    tmp = LIB + ".tmp"
+    r = subprocess.run([nvcc, *ARCH, "-shared", "-o", tmp, *objs], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(force=True, verbose="-v" in sys.argv))

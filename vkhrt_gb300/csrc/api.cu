@@ -1,0 +1,808 @@
+// api.cu -- the C ABI (include/hrt.h): contexts, BLAS/TLAS objects, frames, batches.
+// Host code only; kernels live in build.cu and trace.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "hrt_internal.h"
+
+using namespace hrt;
+
+struct hrt_context {
+    int device = 0;
+    int sm_count = 0;
+    std::string last_error;
+};
+
+struct hrt_blas {
+    hrt_context* ctx = nullptr;
+    int type = 0, precision = 0;
+    float transform[16];
+    uint64_t nprims = 0;
+    float build_ms = 0.0f;
+    bool keep = false;
+    BuildOutput out;
+};
+
+struct hrt_tlas {
+    hrt_context* ctx = nullptr;
+    DevInstance* dev = nullptr;
+    uint32_t n = 0;
+    bool quantised = false;
+};
+
+struct hrt_frame {
+    hrt_context* ctx = nullptr;
+    uint32_t w = 0, h = 0, spp = 0;
+    float4* fb = nullptr;
+    hrt_hit* hits = nullptr;
+    SceneLaunch* dscene = nullptr;
+    TraceCounters* counters = nullptr;
+    hrt_frame_stats stats{};
+    bool stats_pending = false;
+    uint64_t pending_primary = 0;
+};
+
+struct hrt_batch {
+    hrt_context* ctx = nullptr;
+    SceneLaunch* dscenes = nullptr;
+    TraceCounters* counters = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<hrt_frame*> frames;
+    uint64_t primary = 0;
+    bool async = false;
+};
+
+namespace {
+
+hrt_status fail(hrt_context* ctx, hrt_status s, const char* fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        ctx->last_error = buf;
+    }
+    return s;
+}
+
+hrt_status cuda_fail(hrt_context* ctx, cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(ctx, HRT_ERR_OOM, "%s: out of device memory", what);
+    return fail(ctx, HRT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(ctx, call, what)                                         \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, (what)); \
+    } while (0)
+
+struct DeviceSet {  // makes ctx->device current for the scope of a call
+    int prev = -1;
+    explicit DeviceSet(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceSet() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+bool is_identity(const float* m) {
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r)
+            if (m[4 * c + r] != (c == r ? 1.0f : 0.0f)) return false;
+    return true;
+}
+
+// Inverse of a column-major 4x4 matrix in double: Gauss-Jordan elimination with partial
+// pivoting on the row-major copy [A | I].
+bool invert4(const double* m, double* out) {
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            a[r][c] = m[4 * c + r];
+            a[r][4 + c] = r == c ? 1.0 : 0.0;
+        }
+    for (int col = 0; col < 4; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < 4; ++r)
+            if (std::fabs(a[r][col]) > std::fabs(a[piv][col])) piv = r;
+        if (!(std::fabs(a[piv][col]) > 0.0) || !std::isfinite(a[piv][col])) return false;
+        if (piv != col)
+            for (int c = 0; c < 8; ++c) std::swap(a[piv][c], a[col][c]);
+        double d = a[col][col];
+        for (int c = 0; c < 8; ++c) a[col][c] /= d;
+        for (int r = 0; r < 4; ++r) {
+            if (r == col || a[r][col] == 0.0) continue;
+            double f = a[r][col];
+            for (int c = 0; c < 8; ++c) a[r][c] -= f * a[col][c];
+        }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) out[4 * c + r] = a[r][4 + c];
+    return true;
+}
+
+hrt_status read_counters(hrt_context* ctx, TraceCounters* dev, TraceCounters* host, cudaStream_t s) {
+    CK(ctx, cudaMemcpyAsync(host, dev, sizeof(TraceCounters), cudaMemcpyDeviceToHost, s), "read counters");
+    CK(ctx, cudaStreamSynchronize(s), "synchronise trace");
+    if (host->error & kErrStackOverflow)
+        return fail(ctx, HRT_ERR_STACK_OVERFLOW, "traversal stack of %d entries overflowed", kStackSize);
+    if (host->error & kErrTimeout)
+        return fail(ctx, HRT_ERR_TIMEOUT, "a traversal exceeded %u steps", kMaxTraversalSteps);
+    return HRT_OK;
+}
+
+void counters_to_stats(const TraceCounters& c, uint64_t primary, hrt_frame_stats* st) {
+    st->primary_rays = primary;
+    st->shadow_rays = c.shadow;
+    st->nodes_visited = c.nodes;
+    st->prims_tested = c.prims;
+    st->fp64_resolves = c.fp64_resolves;
+    st->fp64_hits = c.fp64_hits;
+}
+
+void fill_scene(SceneLaunch& sl, const hrt_tlas* t, const hrt_camera* cam, hrt_frame* f, uint64_t work_begin) {
+    sl.inst = t->dev;
+    sl.ninst = t->n;
+    sl.width = f->w;
+    sl.height = f->h;
+    sl.spp = f->spp;
+    sl.tiles_x = (f->w + 7) / 8;
+    uint64_t tiles_y = (f->h + 3) / 4;
+    sl.work_begin = work_begin;
+    sl.work_count = uint64_t(sl.tiles_x) * tiles_y * 32;
+    memcpy(sl.view_inv, cam->view_inverse, sizeof(sl.view_inv));
+    memcpy(sl.proj_inv, cam->proj_inverse, sizeof(sl.proj_inv));
+    sl.fb = f->fb;
+    sl.hits = f->hits;
+}
+
+TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32_t n, uint64_t total, TraceCounters* c) {
+    TraceLaunch L;
+    L.scenes = ds;
+    L.nscenes = n;
+    L.total_work = total;
+    L.tmin = p->tmin;
+    L.tmax = p->tmax;
+    L.shadow_tmin = p->shadow_tmin;
+    L.jitter = p->jitter;
+    L.seed = p->seed;
+    L.shading = p->shading;
+    L.fp64_resolve = p->fp64_resolve;
+    L.record_hits = p->record_hits;
+    L.count_stats = p->count_stats;
+    L.counters = c;
+    return L;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hrt_abi_version(void) { return HRT_ABI_VERSION; }
+
+const char* hrt_status_string(hrt_status s) {
+    switch (s) {
+        case HRT_OK: return "ok";
+        case HRT_ERR_INVALID_ARG: return "invalid argument";
+        case HRT_ERR_OOM: return "out of device memory";
+        case HRT_ERR_CUDA: return "CUDA error";
+        case HRT_ERR_STACK_OVERFLOW: return "traversal stack overflow";
+        case HRT_ERR_TIMEOUT: return "device loop iteration cap reached";
+        case HRT_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}
+
+hrt_status hrt_context_create(int device, hrt_context** out) {
+    if (!out) return HRT_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return HRT_ERR_CUDA;
+    if (device < 0 || device >= count) return HRT_ERR_INVALID_ARG;
+    hrt_context* c = new (std::nothrow) hrt_context();
+    if (!c) return HRT_ERR_OOM;
+    c->device = device;
+    DeviceSet ds(device);
+    if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        delete c;
+        return HRT_ERR_CUDA;
+    }
+    *out = c;
+    return HRT_OK;
+}
+
+hrt_status hrt_context_destroy(hrt_context* ctx) {
+    delete ctx;
+    return HRT_OK;
+}
+
+const char* hrt_last_error(const hrt_context* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+void hrt_blas_input_default(hrt_blas_input* in) {
+    memset(in, 0, sizeof(*in));
+    in->type = HRT_BLAS_PHANTOM;
+    in->precision = HRT_PRECISION_FP32;
+    in->memory = HRT_MEMORY_HOST;
+    in->max_leaf = 1;
+    in->const_radius = 0.02f;
+    for (int k = 0; k < 4; ++k) in->transform[5 * k] = 1.0f;
+}
+
+hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stream, hrt_blas** out) {
+    if (!ctx) return HRT_ERR_INVALID_ARG;
+    if (!in || !out) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: null input or output");
+    *out = nullptr;
+    if (in->type < HRT_BLAS_PHANTOM || in->type > HRT_BLAS_DOTS)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: unknown geometry type %d", in->type);
+    if (in->precision != HRT_PRECISION_FP32 && in->precision != HRT_PRECISION_QUANTISED)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: unknown precision %d", in->precision);
+    if (in->memory != HRT_MEMORY_HOST && in->memory != HRT_MEMORY_DEVICE)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: unknown memory kind %d", in->memory);
+    if (!!in->strand_offsets == !!in->line_indices)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: give exactly one of strand_offsets and line_indices");
+    if (in->nvertices > 0 && !in->vertices)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: null vertices");
+    if (in->nvertices >= (1ull << 32))
+        return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_build: more than 2^32 - 1 vertices");
+    uint32_t max_leaf = in->max_leaf ? in->max_leaf : 1;
+    if (max_leaf > 3) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: max_leaf must be 1..3");
+    if (!in->radius && !(in->const_radius >= 0.0f))
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: const_radius must be >= 0");
+    DeviceSet dset(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    // ---- lines: count and per-strand offsets (host) ------------------------------------------
+    uint64_t nlines = 0;
+    std::vector<uint32_t> line_off, vert_off;
+    if (in->strand_offsets) {
+        std::vector<uint32_t> so(in->nstrands + 1);
+        if (in->memory == HRT_MEMORY_HOST) memcpy(so.data(), in->strand_offsets, so.size() * 4);
+        else CK(ctx, cudaMemcpy(so.data(), in->strand_offsets, so.size() * 4, cudaMemcpyDeviceToHost), "read strand offsets");
+        line_off.resize(in->nstrands + 1);
+        vert_off.resize(in->nstrands + 1);
+        for (uint64_t st = 0; st < in->nstrands; ++st) {
+            if (so[st + 1] < so[st] || so[st + 1] > in->nvertices)
+                return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: strand_offsets[%llu..] not increasing or past nvertices",
+                            (unsigned long long)st);
+            line_off[st] = uint32_t(nlines);
+            vert_off[st] = so[st];
+            uint32_t len = so[st + 1] - so[st];
+            nlines += len >= 2 ? len - 1 : 0;
+        }
+        line_off[in->nstrands] = uint32_t(nlines);
+        vert_off[in->nstrands] = so[in->nstrands];
+    } else {
+        nlines = in->nlines;
+        if (in->memory == HRT_MEMORY_HOST)
+            for (uint64_t i = 0; i < 2 * nlines; ++i)
+                if (in->line_indices[i] >= in->nvertices)
+                    return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: line index %llu out of range",
+                                (unsigned long long)i);
+    }
+    if (nlines >= (1ull << 29))
+        return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_build: %llu segments; the limit is 2^29", (unsigned long long)nlines);
+
+    hrt_blas* b = new (std::nothrow) hrt_blas();
+    if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_blas_build: host allocation");
+    b->ctx = ctx;
+    b->type = in->type;
+    b->precision = in->precision;
+    b->nprims = nlines;
+    b->keep = (in->flags & HRT_BUILD_KEEP_INTERMEDIATE) != 0;
+    memcpy(b->transform, in->transform, sizeof(b->transform));
+
+    // ---- device copies of the inputs ------------------------------------------------------------
+    float *dv = nullptr, *dr = nullptr, *lines = nullptr, *lrad = nullptr;
+    uint32_t *dlo = nullptr, *dvo = nullptr, *didx = nullptr;
+    auto cleanup = [&]() {
+        if (in->memory == HRT_MEMORY_HOST) {
+            if (dv) cudaFree(dv);
+            if (dr) cudaFree(dr);
+            if (didx) cudaFree(didx);
+        }
+        if (dlo) cudaFree(dlo);
+        if (dvo) cudaFree(dvo);
+        if (lines) cudaFree(lines);
+        if (lrad) cudaFree(lrad);
+    };
+    auto bail = [&](cudaError_t e, const char* what) {
+        cleanup();
+        free_build_output(b->out);
+        delete b;
+        return cuda_fail(ctx, e, what);
+    };
+    cudaError_t e = cudaSuccess;
+    if (in->memory == HRT_MEMORY_HOST) {
+        if (in->nvertices) {
+            if ((e = cudaMalloc(&dv, in->nvertices * 12)) != cudaSuccess) return bail(e, "allocate vertices");
+            if ((e = cudaMemcpyAsync(dv, in->vertices, in->nvertices * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+                return bail(e, "copy vertices");
+            if (in->radius) {
+                if ((e = cudaMalloc(&dr, in->nvertices * 4)) != cudaSuccess) return bail(e, "allocate radii");
+                if ((e = cudaMemcpyAsync(dr, in->radius, in->nvertices * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+                    return bail(e, "copy radii");
+            }
+        }
+        if (in->line_indices && nlines) {
+            if ((e = cudaMalloc(&didx, nlines * 8)) != cudaSuccess) return bail(e, "allocate line indices");
+            if ((e = cudaMemcpyAsync(didx, in->line_indices, nlines * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+                return bail(e, "copy line indices");
+        }
+    } else {
+        dv = const_cast<float*>(in->vertices);
+        dr = const_cast<float*>(in->radius);
+        didx = const_cast<uint32_t*>(in->line_indices);
+    }
+    if (in->strand_offsets) {
+        if ((e = cudaMalloc(&dlo, line_off.size() * 4)) != cudaSuccess) return bail(e, "allocate strand tables");
+        if ((e = cudaMalloc(&dvo, vert_off.size() * 4)) != cudaSuccess) return bail(e, "allocate strand tables");
+        if ((e = cudaMemcpyAsync(dlo, line_off.data(), line_off.size() * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return bail(e, "copy strand tables");
+        if ((e = cudaMemcpyAsync(dvo, vert_off.data(), vert_off.size() * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return bail(e, "copy strand tables");
+    }
+    if (nlines) {
+        if ((e = cudaMalloc(&lines, nlines * 24)) != cudaSuccess) return bail(e, "allocate lines");
+        if ((e = cudaMalloc(&lrad, nlines * 8)) != cudaSuccess) return bail(e, "allocate line radii");
+        if ((e = make_lines(dv, dr, in->const_radius, dlo, dvo, in->nstrands, didx, nlines, lines, lrad, s)) != cudaSuccess)
+            return bail(e, "generate lines");
+    }
+
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    BuildInput bi{in->type, in->precision, int(max_leaf), in->quant_chunk, lines, lrad, nlines, b->keep};
+    char msg[256] = {0};
+    e = build_blas_device(bi, b->out, s, msg, sizeof(msg));
+    cudaEventRecord(e1, s);
+    if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        std::string m = msg;
+        cleanup();
+        free_build_output(b->out);
+        delete b;
+        if (e == cudaErrorInvalidValue && !m.empty()) return fail(ctx, HRT_ERR_UNSUPPORTED, "%s", m.c_str());
+        if (e == cudaErrorMemoryAllocation) return fail(ctx, HRT_ERR_OOM, "BVH build: %s", m.c_str());
+        return fail(ctx, HRT_ERR_CUDA, "BVH build: %s", m.empty() ? cudaGetErrorString(e) : m.c_str());
+    }
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&b->build_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cleanup();
+    *out = b;
+    return HRT_OK;
+}
+
+hrt_status hrt_blas_destroy(hrt_blas* b) {
+    if (!b) return HRT_OK;
+    DeviceSet ds(b->ctx->device);
+    free_build_output(b->out);
+    delete b;
+    return HRT_OK;
+}
+
+int32_t hrt_blas_type(const hrt_blas* b) { return b ? b->type : -1; }
+
+hrt_status hrt_blas_transform(const hrt_blas* b, float out[16]) {
+    if (!b || !out) return HRT_ERR_INVALID_ARG;
+    memcpy(out, b->transform, sizeof(b->transform));
+    return HRT_OK;
+}
+
+hrt_status hrt_blas_get_info(const hrt_blas* b, hrt_blas_info* o) {
+    if (!b || !o) return HRT_ERR_INVALID_ARG;
+    o->nprims = b->nprims;
+    o->nnodes = b->out.nnodes;
+    o->node_bytes = b->out.node_bytes;
+    o->prim_bytes = b->out.prim_bytes;
+    o->device_bytes = b->out.device_bytes;
+    memcpy(o->bounds, b->out.bounds, sizeof(o->bounds));
+    o->build_ms = b->build_ms;
+    return HRT_OK;
+}
+
+hrt_status hrt_blas_get(const hrt_blas* b, int32_t part, void* dst, uint64_t bytes) {
+    if (!b || !dst) return HRT_ERR_INVALID_ARG;
+    hrt_context* ctx = b->ctx;
+    DeviceSet ds(ctx->device);
+    const uint64_t n = b->nprims;
+    const void* src = nullptr;
+    uint64_t need = 0;
+    const BuildOutput& o = b->out;
+    switch (part) {
+        case HRT_PART_PRIM_BOXES: src = o.prim_boxes; need = n * 24; break;
+        case HRT_PART_MORTON_SORTED: src = o.morton_sorted; need = n * 8; break;
+        case HRT_PART_SORTED_INDEX: src = o.sorted_index; need = n * 4; break;
+        case HRT_PART_BIN_LEFT: src = o.bin_left; need = n ? (n - 1) * 4 : 0; break;
+        case HRT_PART_BIN_RIGHT: src = o.bin_right; need = n ? (n - 1) * 4 : 0; break;
+        case HRT_PART_BIN_BOXES: src = o.bin_boxes; need = n ? (n - 1) * 24 : 0; break;
+        case HRT_PART_NODES: src = o.nodes; need = o.nnodes * o.node_bytes; break;
+        case HRT_PART_QNODES:
+            src = b->precision == HRT_PRECISION_QUANTISED ? o.nodes : o.qnodes_aux;
+            need = o.nnodes * sizeof(NodeQ);
+            break;
+        case HRT_PART_PRIM_ORDER: src = o.prim_ids; need = n * 4; break;
+        case HRT_PART_PRIMS: src = o.prims; need = n * o.prim_bytes; break;
+        case HRT_PART_CURVES: src = o.curves; need = n * 48; break;
+        case HRT_PART_LSS: src = b->type == HRT_BLAS_LSS ? o.geom : nullptr; need = n * 32; break;
+        case HRT_PART_ROOTS: src = o.roots; need = o.nroots * 16; break;
+        case HRT_PART_DOTS_VERTICES: {
+            if (b->type != HRT_BLAS_DOTS) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_get: not a DOTS BLAS");
+            need = n * 144;
+            if (bytes != need) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_get: part needs %llu bytes", (unsigned long long)need);
+            if (!n) return HRT_OK;
+            float* tmp = nullptr;
+            CK(ctx, cudaMalloc(&tmp, need), "allocate DOTS vertices");
+            cudaError_t e = expand_dots(o.geom, n, tmp, nullptr);
+            if (e == cudaSuccess) e = cudaMemcpy(dst, tmp, need, cudaMemcpyDeviceToHost);
+            cudaFree(tmp);
+            CK(ctx, e, "expand DOTS vertices");
+            return HRT_OK;
+        }
+        default: return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_get: unknown part %d", part);
+    }
+    if (bytes != need)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_get: part %d needs %llu bytes, got %llu", part,
+                    (unsigned long long)need, (unsigned long long)bytes);
+    if (need == 0) return HRT_OK;
+    if (!src) return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_get: part %d was not kept by this build", part);
+    CK(ctx, cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost), "hrt_blas_get");
+    return HRT_OK;
+}
+
+hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint32_t n, void* stream, hrt_tlas** out) {
+    if (!ctx) return HRT_ERR_INVALID_ARG;
+    if (!out || (n && !blases)) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_tlas_build: null argument");
+    *out = nullptr;
+    DeviceSet ds(ctx->device);
+    std::vector<DevInstance> inst(n);
+    bool quant = false;
+    for (uint32_t i = 0; i < n; ++i) {
+        const hrt_blas* b = blases[i];
+        if (!b) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_tlas_build: null BLAS %u", i);
+        bool q = b->precision == HRT_PRECISION_QUANTISED;
+        if (i == 0) quant = q;
+        else if (q != quant)
+            return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_tlas_build: FP32 and quantised BLASes cannot share a TLAS");
+        DevInstance& d = inst[i];
+        memset(&d, 0, sizeof(d));
+        d.b.nodes = b->out.nodes;
+        d.b.prims = b->out.prims;
+        d.b.roots = b->out.roots;
+        d.b.prim_ids = b->out.prim_ids;
+        d.b.type = uint32_t(b->type);
+        d.b.precision = uint32_t(b->precision);
+        d.b.nprims = uint32_t(b->nprims);
+        d.b.nnodes = uint32_t(b->out.nnodes);
+        for (int k = 0; k < 3; ++k) { d.b.lo[k] = b->out.bounds[k]; d.b.hi[k] = b->out.bounds[3 + k]; }
+        d.identity = is_identity(b->transform) ? 1u : 0u;
+        double m[16], iv[16];
+        for (int k = 0; k < 16; ++k) m[k] = b->transform[k];
+        if (!invert4(m, iv)) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_tlas_build: BLAS %u transform is singular", i);
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 4; ++c) d.w2o[4 * r + c] = float(iv[4 * c + r]);
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) d.nrm[3 * r + c] = float(iv[4 * r + c]);  // (M^-1)^T
+    }
+    hrt_tlas* t = new (std::nothrow) hrt_tlas();
+    if (!t) return fail(ctx, HRT_ERR_OOM, "hrt_tlas_build: host allocation");
+    t->ctx = ctx;
+    t->n = n;
+    t->quantised = quant;
+    if (n) {
+        cudaError_t e = cudaMalloc(&t->dev, n * sizeof(DevInstance));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(t->dev, inst.data(), n * sizeof(DevInstance), cudaMemcpyHostToDevice,
+                                static_cast<cudaStream_t>(stream));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) {
+            if (t->dev) cudaFree(t->dev);
+            delete t;
+            return cuda_fail(ctx, e, "hrt_tlas_build");
+        }
+    }
+    *out = t;
+    return HRT_OK;
+}
+
+hrt_status hrt_tlas_destroy(hrt_tlas* t) {
+    if (!t) return HRT_OK;
+    DeviceSet ds(t->ctx->device);
+    if (t->dev) cudaFree(t->dev);
+    delete t;
+    return HRT_OK;
+}
+
+hrt_status hrt_camera_look_at(const float eye[3], const float center[3], const float up[3], float fovy_deg,
+                              float aspect, float znear, float zfar, hrt_camera* out) {
+    if (!eye || !center || !up || !out || !(aspect > 0.0f) || !(zfar > znear) || !(fovy_deg > 0.0f) ||
+        !(fovy_deg < 180.0f))
+        return HRT_ERR_INVALID_ARG;
+    // glm::lookAtRH: f = normalize(center - eye), s = normalize(cross(f, up)), u = cross(s, f)
+    double e[3] = {eye[0], eye[1], eye[2]}, c[3] = {center[0], center[1], center[2]}, u0[3] = {up[0], up[1], up[2]};
+    double f[3] = {c[0] - e[0], c[1] - e[1], c[2] - e[2]};
+    double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    if (!(fl > 0.0)) return HRT_ERR_INVALID_ARG;
+    for (double& x : f) x /= fl;
+    double s[3] = {f[1] * u0[2] - f[2] * u0[1], f[2] * u0[0] - f[0] * u0[2], f[0] * u0[1] - f[1] * u0[0]};
+    double sl = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    if (!(sl > 0.0)) return HRT_ERR_INVALID_ARG;
+    for (double& x : s) x /= sl;
+    double u[3] = {s[1] * f[2] - s[2] * f[1], s[2] * f[0] - s[0] * f[2], s[0] * f[1] - s[1] * f[0]};
+    double V[16] = {0};
+    V[0] = s[0]; V[4] = s[1]; V[8] = s[2];
+    V[1] = u[0]; V[5] = u[1]; V[9] = u[2];
+    V[2] = -f[0]; V[6] = -f[1]; V[10] = -f[2];
+    V[12] = -(s[0] * e[0] + s[1] * e[1] + s[2] * e[2]);
+    V[13] = -(u[0] * e[0] + u[1] * e[1] + u[2] * e[2]);
+    V[14] = f[0] * e[0] + f[1] * e[1] + f[2] * e[2];
+    V[15] = 1.0;
+    // glm::perspectiveRH_ZO, then [1][1] *= -1 (fly_camera.cpp:32-33)
+    double th = std::tan(double(fovy_deg) * 3.14159265358979323846 / 360.0);
+    double P[16] = {0};
+    P[0] = 1.0 / (double(aspect) * th);
+    P[5] = -(1.0 / th);
+    P[10] = double(zfar) / (double(znear) - double(zfar));
+    P[11] = -1.0;
+    P[14] = -(double(zfar) * double(znear)) / (double(zfar) - double(znear));
+    double Vi[16], Pi[16];
+    if (!invert4(V, Vi) || !invert4(P, Pi)) return HRT_ERR_INVALID_ARG;
+    for (int k = 0; k < 16; ++k) {
+        out->view_inverse[k] = float(Vi[k]);
+        out->proj_inverse[k] = float(Pi[k]);
+    }
+    return HRT_OK;
+}
+
+void hrt_trace_params_default(hrt_trace_params* p) {
+    memset(p, 0, sizeof(*p));
+    p->tmin = 0.001f;
+    p->tmax = 10000.0f;
+    p->spp = 1;
+    p->shading = HRT_SHADE_DEBUG;
+    p->shadow_tmin = 1e-4f;
+    p->fp64_resolve = 1;
+}
+
+hrt_status hrt_frame_create(hrt_context* ctx, uint32_t w, uint32_t h, uint32_t spp, int32_t with_hits, hrt_frame** out) {
+    if (!ctx) return HRT_ERR_INVALID_ARG;
+    if (!out || w == 0 || h == 0 || spp == 0 || spp > 1024)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_frame_create: bad size %ux%u x %u spp", w, h, spp);
+    if (uint64_t(w) * h * spp >= (1ull << 32))
+        return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_frame_create: more than 2^32 samples");
+    DeviceSet ds(ctx->device);
+    hrt_frame* f = new (std::nothrow) hrt_frame();
+    if (!f) return fail(ctx, HRT_ERR_OOM, "hrt_frame_create: host allocation");
+    f->ctx = ctx;
+    f->w = w;
+    f->h = h;
+    f->spp = spp;
+    cudaError_t e = cudaMalloc(&f->fb, uint64_t(w) * h * sizeof(float4));
+    if (e == cudaSuccess && with_hits) e = cudaMalloc(&f->hits, uint64_t(w) * h * spp * sizeof(hrt_hit));
+    if (e == cudaSuccess) e = cudaMalloc(&f->dscene, sizeof(SceneLaunch));
+    if (e == cudaSuccess) e = cudaMalloc(&f->counters, sizeof(TraceCounters));
+    if (e != cudaSuccess) {
+        hrt_frame_destroy(f);
+        return cuda_fail(ctx, e, "hrt_frame_create");
+    }
+    *out = f;
+    return HRT_OK;
+}
+
+hrt_status hrt_frame_destroy(hrt_frame* f) {
+    if (!f) return HRT_OK;
+    DeviceSet ds(f->ctx->device);
+    if (f->fb) cudaFree(f->fb);
+    if (f->hits) cudaFree(f->hits);
+    if (f->dscene) cudaFree(f->dscene);
+    if (f->counters) cudaFree(f->counters);
+    delete f;
+    return HRT_OK;
+}
+
+hrt_status hrt_frame_device_ptrs(const hrt_frame* f, float** rgba, hrt_hit** hits) {
+    if (!f) return HRT_ERR_INVALID_ARG;
+    if (rgba) *rgba = reinterpret_cast<float*>(f->fb);
+    if (hits) *hits = f->hits;
+    return HRT_OK;
+}
+
+hrt_status hrt_frame_download(hrt_frame* f, float* rgba, hrt_hit* hits, void* stream) {
+    if (!f) return HRT_ERR_INVALID_ARG;
+    hrt_context* ctx = f->ctx;
+    DeviceSet ds(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (rgba) CK(ctx, cudaMemcpyAsync(rgba, f->fb, uint64_t(f->w) * f->h * 16, cudaMemcpyDeviceToHost, s), "download frame");
+    if (hits) {
+        if (!f->hits) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_frame_download: frame has no hit records");
+        CK(ctx, cudaMemcpyAsync(hits, f->hits, uint64_t(f->w) * f->h * f->spp * sizeof(hrt_hit), cudaMemcpyDeviceToHost, s),
+           "download hits");
+    }
+    CK(ctx, cudaStreamSynchronize(s), "download frame");
+    return HRT_OK;
+}
+
+hrt_status hrt_frame_get_stats(const hrt_frame* cf, hrt_frame_stats* out) {
+    if (!cf || !out) return HRT_ERR_INVALID_ARG;
+    hrt_frame* f = const_cast<hrt_frame*>(cf);
+    if (f->stats_pending) {
+        DeviceSet ds(f->ctx->device);
+        TraceCounters c;
+        hrt_status st = read_counters(f->ctx, f->counters, &c, nullptr);
+        if (st != HRT_OK) return st;
+        counters_to_stats(c, f->pending_primary, &f->stats);
+        f->stats_pending = false;
+    }
+    *out = f->stats;
+    return HRT_OK;
+}
+
+hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* cam, const hrt_trace_params* p,
+                     hrt_frame* f, void* stream) {
+    if (!ctx) return HRT_ERR_INVALID_ARG;
+    if (!tlas || !cam || !p || !f) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace: null argument");
+    if (f->spp == 0 || !(p->tmax > p->tmin)) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace: bad parameters");
+    if (p->shading > HRT_SHADE_LAMBERT_SHADOW) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace: unknown shading %u", p->shading);
+    if (p->record_hits && !f->hits) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace: record_hits on a frame without hit records");
+    DeviceSet ds(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    SceneLaunch sl;
+    fill_scene(sl, tlas, cam, f, 0);
+    CK(ctx, cudaMemcpyAsync(f->dscene, &sl, sizeof(sl), cudaMemcpyHostToDevice, s), "upload scene");
+    CK(ctx, cudaMemsetAsync(f->counters, 0, sizeof(TraceCounters), s), "reset counters");
+    TraceLaunch L = make_launch(p, f->dscene, 1, sl.work_count, f->counters);
+    CK(ctx, launch_trace(L, tlas->quantised, s, ctx->sm_count), "launch trace");
+    f->pending_primary = uint64_t(f->w) * f->h * f->spp;
+    f->stats_pending = true;
+    if (p->async) return HRT_OK;
+    TraceCounters c;
+    hrt_status st = read_counters(ctx, f->counters, &c, s);
+    if (st != HRT_OK) return st;
+    counters_to_stats(c, f->pending_primary, &f->stats);
+    f->stats_pending = false;
+    return HRT_OK;
+}
+
+hrt_status hrt_trace_rays(hrt_context* ctx, const hrt_tlas* tlas, const float* rays, uint64_t n, const hrt_trace_params* p,
+                          hrt_hit* hits, int32_t memory, void* stream) {
+    if (!ctx) return HRT_ERR_INVALID_ARG;
+    if (!tlas || !p || (n && (!rays || !hits))) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays: null argument");
+    if (memory != HRT_MEMORY_HOST && memory != HRT_MEMORY_DEVICE)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays: unknown memory kind");
+    if (n == 0) return HRT_OK;
+    DeviceSet ds(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const float* dr = rays;
+    hrt_hit* dh = hits;
+    float* tr = nullptr;
+    hrt_hit* th = nullptr;
+    TraceCounters* ctr = nullptr;
+    auto done = [&]() {
+        if (tr) cudaFree(tr);
+        if (th) cudaFree(th);
+        if (ctr) cudaFree(ctr);
+    };
+    cudaError_t e = cudaMalloc(&ctr, sizeof(TraceCounters));
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof(TraceCounters), s);
+    if (e == cudaSuccess && memory == HRT_MEMORY_HOST) {
+        e = cudaMalloc(&tr, n * 24);
+        if (e == cudaSuccess) e = cudaMalloc(&th, n * sizeof(hrt_hit));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tr, rays, n * 24, cudaMemcpyHostToDevice, s);
+        dr = tr;
+        dh = th;
+    }
+    if (e == cudaSuccess)
+        e = launch_trace_rays(tlas->dev, tlas->n, dr, n, p->tmin, p->tmax, p->fp64_resolve, dh, ctr, tlas->quantised, s,
+                              ctx->sm_count);
+    if (e == cudaSuccess && memory == HRT_MEMORY_HOST) e = cudaMemcpyAsync(hits, th, n * sizeof(hrt_hit), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) {
+        done();
+        return cuda_fail(ctx, e, "hrt_trace_rays");
+    }
+    TraceCounters c;
+    hrt_status st = read_counters(ctx, ctr, &c, s);
+    done();
+    return st;
+}
+
+hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* p,
+                            void* stream, hrt_batch** out) {
+    if (!ctx) return HRT_ERR_INVALID_ARG;
+    if (!scenes || !n || !p || !out) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_create: null or empty argument");
+    *out = nullptr;
+    DeviceSet ds(ctx->device);
+    std::vector<SceneLaunch> sl(n);
+    uint64_t work = 0, primary = 0;
+    bool quant = false;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!scenes[i].tlas || !scenes[i].frame) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_create: scene %u incomplete", i);
+        if (i == 0) quant = scenes[i].tlas->quantised;
+        else if (scenes[i].tlas->quantised != quant)
+            return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_batch_create: scenes mix FP32 and quantised BLASes");
+        if (p->record_hits && !scenes[i].frame->hits)
+            return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_create: record_hits on a frame without hit records");
+        fill_scene(sl[i], scenes[i].tlas, &scenes[i].camera, scenes[i].frame, work);
+        work += sl[i].work_count;
+        primary += uint64_t(scenes[i].frame->w) * scenes[i].frame->h * scenes[i].frame->spp;
+    }
+    hrt_batch* b = new (std::nothrow) hrt_batch();
+    if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_batch_create: host allocation");
+    b->ctx = ctx;
+    b->primary = primary;
+    b->async = p->async != 0;
+    for (uint32_t i = 0; i < n; ++i) b->frames.push_back(scenes[i].frame);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMalloc(&b->dscenes, n * sizeof(SceneLaunch));
+    if (e == cudaSuccess) e = cudaMalloc(&b->counters, sizeof(TraceCounters));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->dscenes, sl.data(), n * sizeof(SceneLaunch), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // capture: counter reset + the persistent trace launch
+    cudaStream_t cap = nullptr;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t e1 = cudaMemsetAsync(b->counters, 0, sizeof(TraceCounters), cap);
+        TraceLaunch L = make_launch(p, b->dscenes, n, work, b->counters);
+        cudaError_t e2 = e1 == cudaSuccess ? launch_trace(L, quant, cap, ctx->sm_count) : e1;
+        cudaError_t e3 = cudaStreamEndCapture(cap, &b->graph);
+        e = e2 != cudaSuccess ? e2 : e3;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (cap) cudaStreamDestroy(cap);
+    if (e != cudaSuccess) {
+        hrt_batch_destroy(b);
+        return cuda_fail(ctx, e, "hrt_batch_create");
+    }
+    *out = b;
+    return HRT_OK;
+}
+
+hrt_status hrt_batch_launch(hrt_batch* b, void* stream) {
+    if (!b) return HRT_ERR_INVALID_ARG;
+    hrt_context* ctx = b->ctx;
+    DeviceSet ds(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CK(ctx, cudaGraphLaunch(b->exec, s), "hrt_batch_launch");
+    if (b->async) return HRT_OK;
+    TraceCounters c;
+    hrt_status st = read_counters(ctx, b->counters, &c, s);
+    if (st != HRT_OK) return st;
+    // the batch's counters are shared; report them on the first frame
+    if (!b->frames.empty()) {
+        counters_to_stats(c, b->primary, &b->frames[0]->stats);
+        b->frames[0]->stats_pending = false;
+    }
+    return HRT_OK;
+}
+
+hrt_status hrt_batch_destroy(hrt_batch* b) {
+    if (!b) return HRT_OK;
+    DeviceSet ds(b->ctx->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->dscenes) cudaFree(b->dscenes);
+    if (b->counters) cudaFree(b->counters);
+    delete b;
+    return HRT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,990 @@
+// build.cu -- device BVH build for one BLAS: geometry processing, LBVH, BVH8 collapse, encoding.
+//
+// Compiled with --fmad=false: every float operation is a separately rounded IEEE operation and
+// division / square root are correctly rounded, so each stage is bit-identical to the CPU
+// restatement (compiled with -ffp-contract=off) on the same inputs.
+//
+// Pipeline (one stream, temporaries from the stream-ordered allocator):
+//   lines -> per type: Bezier curves (GenerateCurves, geometry_processor.cpp:123-156) and, for
+//   the quantised format, FP16 offsets from chunk roots | LSS spheres (:273-298) | DOTS frames
+//   (:201-271) -> primitive boxes -> centroid bounds -> 63-bit Morton codes -> stable LSD radix
+//   sort (8 passes of 8 bits) -> Karras hierarchy -> bottom-up refit -> greedy surface-area
+//   collapse to BVH8, breadth first -> FP32 and 8-bit quantised node encodings -> primitive
+//   records in leaf-slot order.
+#include <cuda_fp16.h>
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "hrt_internal.h"
+
+namespace hrt {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float fmin_t(float a, float b) { return (b < a) ? b : a; }  // glm::min
+__device__ __forceinline__ float fmax_t(float a, float b) { return (a < b) ? b : a; }  // glm::max
+
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 ld3(const float* p) { return {p[0], p[1], p[2]}; }
+__device__ __forceinline__ void st3(float* p, f3 v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ bool operator==(f3 a, f3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+// glm: dot = (x*x' + y*y') + z*z'; normalize = v * (1 / sqrt(dot(v, v)))
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 normalize3(f3 v) { return v * (1.0f / sqrtf(dot3(v, v))); }
+__device__ __forceinline__ f3 cross3(f3 x, f3 y) {
+    return {x.y * y.z - y.y * x.z, x.z * y.x - y.z * x.x, x.x * y.y - y.x * x.y};
+}
+__device__ __forceinline__ float gabs(float x) { return x >= 0.0f ? x : -x; }
+
+inline unsigned grid_for(uint64_t n, unsigned threads) { return unsigned((n + threads - 1) / threads); }
+
+// ================================ scans ===========================================================
+constexpr int kScanThreads = 256, kScanItems = 4, kScanTile = kScanThreads * kScanItems;
+struct SumOp {
+    __device__ static uint32_t id() { return 0u; }
+    __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return a + b; }
+};
+struct MaxOp {
+    __device__ static uint32_t id() { return 0u; }
+    __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return a > b ? a : b; }
+};
+
+template <class Op>
+__device__ uint32_t block_inclusive(uint32_t v, uint32_t* sm, uint32_t* total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    Op op;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t n = __shfl_up_sync(kFull, v, o);
+        if (lane >= o) v = op(n, v);
+    }
+    if (lane == 31) sm[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = lane < nw ? sm[lane] : Op::id();
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t n = __shfl_up_sync(kFull, s, o);
+            if (lane >= o) s = op(n, s);
+        }
+        sm[lane] = s;
+    }
+    __syncthreads();
+    if (w > 0) v = op(sm[w - 1], v);
+    *total = sm[nw - 1];
+    __syncthreads();
+    return v;
+}
+
+template <class Op>
+__global__ void scan_reduce_kernel(const uint32_t* in, uint64_t n, uint32_t* sums) {
+    __shared__ uint32_t sm[32];
+    Op op;
+    uint64_t base = uint64_t(blockIdx.x) * kScanTile + uint64_t(threadIdx.x) * kScanItems;
+    uint32_t acc = Op::id();
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < n) acc = op(acc, in[base + k]);
+    uint32_t total;
+    block_inclusive<Op>(acc, sm, &total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+template <class Op>
+__global__ void scan_apply_kernel(const uint32_t* in, uint32_t* out, uint64_t n, const uint32_t* prefix,
+                                  bool inclusive, uint32_t* grand_total) {
+    __shared__ uint32_t sm[32];
+    Op op;
+    uint64_t base = uint64_t(blockIdx.x) * kScanTile + uint64_t(threadIdx.x) * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t acc = Op::id();
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < n ? in[base + k] : Op::id();
+        acc = op(acc, v[k]);
+    }
+    uint32_t total;
+    uint32_t incl = block_inclusive<Op>(acc, sm, &total);
+    uint32_t pre = prefix ? prefix[blockIdx.x] : Op::id();
+    __shared__ uint32_t s_incl[kScanThreads];
+    s_incl[threadIdx.x] = incl;
+    __syncthreads();
+    uint32_t excl_block = threadIdx.x > 0 ? s_incl[threadIdx.x - 1] : Op::id();
+    uint32_t run;
+    run = op(pre, excl_block);
+    for (int k = 0; k < kScanItems; ++k) {
+        uint32_t before = run;
+        run = op(run, v[k]);
+        if (base + k < n) out[base + k] = inclusive ? run : before;
+    }
+    if (grand_total && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *grand_total = op(pre, total);
+}
+
+// Scan of n uint32 values (exclusive or inclusive) with Op; optional device grand total.
+template <class Op>
+cudaError_t device_scan(const uint32_t* in, uint32_t* out, uint64_t n, bool inclusive, uint32_t* grand_total,
+                        cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    uint64_t nb = (n + kScanTile - 1) / kScanTile;
+    if (nb == 1) {
+        scan_apply_kernel<Op><<<1, kScanThreads, 0, s>>>(in, out, n, nullptr, inclusive, grand_total);
+        return cudaGetLastError();
+    }
+    uint32_t* sums = nullptr;
+    cudaError_t e = cudaMallocAsync(&sums, nb * sizeof(uint32_t) * 2, s);
+    if (e != cudaSuccess) return e;
+    uint32_t* pre = sums + nb;
+    scan_reduce_kernel<Op><<<unsigned(nb), kScanThreads, 0, s>>>(in, n, sums);
+    e = device_scan<Op>(sums, pre, nb, false, nullptr, s);
+    if (e == cudaSuccess) {
+        scan_apply_kernel<Op><<<unsigned(nb), kScanThreads, 0, s>>>(in, out, n, pre, inclusive, grand_total);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(sums, s);
+    return e;
+}
+
+// ================================ lines ===========================================================
+__global__ void lines_from_strands_kernel(const float* v, const float* vr, float cr, const uint32_t* line_off,
+                                          const uint32_t* vert_off, uint64_t nstrands, uint64_t nlines,
+                                          float* lines, float* lrad) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= nlines) return;
+    uint64_t lo = 0, hi = nstrands;  // largest s with line_off[s] <= i
+    while (hi - lo > 1) {
+        uint64_t mid = (lo + hi) / 2;
+        if (line_off[mid] <= i) lo = mid; else hi = mid;
+    }
+    uint64_t a = uint64_t(vert_off[lo]) + (i - line_off[lo]);
+    uint64_t b = a + 1;
+    for (int k = 0; k < 3; ++k) { lines[6 * i + k] = v[3 * a + k]; lines[6 * i + 3 + k] = v[3 * b + k]; }
+    lrad[2 * i] = vr ? vr[a] : cr;
+    lrad[2 * i + 1] = vr ? vr[b] : cr;
+}
+
+__global__ void lines_from_indices_kernel(const float* v, const float* vr, float cr, const uint32_t* idx,
+                                          uint64_t nlines, float* lines, float* lrad) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= nlines) return;
+    uint64_t a = idx[2 * i], b = idx[2 * i + 1];
+    for (int k = 0; k < 3; ++k) { lines[6 * i + k] = v[3 * a + k]; lines[6 * i + 3 + k] = v[3 * b + k]; }
+    lrad[2 * i] = vr ? vr[a] : cr;
+    lrad[2 * i + 1] = vr ? vr[b] : cr;
+}
+
+// ============================ geometry processing =================================================
+// GenerateCurves geometry_processor.cpp:123-156, tension 1: neighbours by exact point equality.
+__global__ void curves_kernel(const float* lines, uint64_t n, float* curves) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* L = lines + 6 * i;
+    f3 p1 = ld3(L), p2 = ld3(L + 3);
+    uint64_t prev = (i > 0 && ld3(lines + 6 * (i - 1) + 3) == p1) ? i - 1 : i;
+    uint64_t next = (i + 1 < n && p2 == ld3(lines + 6 * (i + 1))) ? i + 1 : i;
+    f3 p0 = ld3(lines + 6 * prev), p3 = ld3(lines + 6 * next + 3);
+    const float k = 1.0f / 6.0f;
+    float* c = curves + 12 * i;
+    st3(c, p1);
+    st3(c + 3, p1 + (p2 - p0) * k);
+    st3(c + 6, p2 - (p3 - p1) * k);
+    st3(c + 9, p2);
+}
+
+// Quantised Phantom chunks: a chunk is a run of connected lines (end == next start) of at most
+// `chunk` lines; its root is the start point of its first line.
+__global__ void run_flags_kernel(const float* lines, uint64_t n, uint32_t* run_start_pos) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bool start = i == 0 || !(ld3(lines + 6 * (i - 1) + 3) == ld3(lines + 6 * i));
+    run_start_pos[i] = start ? uint32_t(i) : 0u;
+}
+__global__ void chunk_flags_kernel(const uint32_t* run_start, uint64_t n, uint32_t chunk, uint32_t* flags) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t d = uint32_t(i) - run_start[i];
+    flags[i] = (d % chunk) == 0 ? 1u : 0u;
+}
+__global__ void chunk_roots_kernel(const float* curves, const uint32_t* flags, const uint32_t* chunk_incl, uint64_t n,
+                                   float4* roots) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n || !flags[i]) return;
+    uint32_t c = chunk_incl[i] - 1;
+    const float* p = curves + 12 * i;
+    roots[c] = make_float4(p[0], p[1], p[2], __uint_as_float(uint32_t(i)));
+}
+// Dequantised control points: root + float(half(cp - root)); radii float(half(r)).
+__global__ void dequant_curves_kernel(const float* curves, const float* lrad, const uint32_t* chunk_incl,
+                                      const float4* roots, uint64_t n, float* dq, float* dqr, uint32_t* keys) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t c = chunk_incl[i] - 1;
+    float4 r = roots[c];
+    float rt[3] = {r.x, r.y, r.z};
+    for (int j = 0; j < 12; ++j) {
+        float off = curves[12 * i + j] - rt[j % 3];
+        dq[12 * i + j] = rt[j % 3] + __half2float(__float2half_rn(off));
+    }
+    dqr[2 * i] = __half2float(__float2half_rn(lrad[2 * i]));
+    dqr[2 * i + 1] = __half2float(__float2half_rn(lrad[2 * i + 1]));
+    keys[i] = (c << 8) | (uint32_t(i) - __float_as_uint(r.w));
+}
+
+// GenerateLinearSweptSpheres geometry_processor.cpp:273-298: radius glm::max(r, 0.001).
+__global__ void lss_kernel(const float* lines, const float* lrad, uint64_t n, float* geom) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float* g = geom + 8 * i;
+    for (int k = 0; k < 6; ++k) g[k] = lines[6 * i + k];
+    g[6] = fmax_t(lrad[2 * i], 0.001f);
+    g[7] = fmax_t(lrad[2 * i + 1], 0.001f);
+}
+
+// PerpStark geometry_processor.cpp:201-212
+__device__ f3 perp_stark(f3 u) {
+    f3 a = {gabs(u.x), gabs(u.y), gabs(u.z)};
+    uint32_t uyx = (a.x - a.y) < 0 ? 1 : 0;
+    uint32_t uzx = (a.x - a.z) < 0 ? 1 : 0;
+    uint32_t uzy = (a.y - a.z) < 0 ? 1 : 0;
+    uint32_t xm = uyx & uzx;
+    uint32_t ym = (1 ^ xm) & uzy;
+    uint32_t zm = 1 ^ (xm | ym);
+    return normalize3(cross3(u, f3{float(xm), float(ym), float(zm)}));
+}
+// DOTS frame per segment (geometry_processor.cpp:237-265): geom = start, end, s*ra, t*ra,
+// s*rb, t*rb; the reference's vertices are start +- v*ra and end +- v*rb.
+__global__ void dots_kernel(const float* lines, const float* lrad, uint64_t n, float* geom) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f3 s0 = ld3(lines + 6 * i), e0 = ld3(lines + 6 * i + 3);
+    float ra = lrad[2 * i], rb = lrad[2 * i + 1];
+    f3 fwd = normalize3(e0 - s0);
+    f3 s = perp_stark(fwd);
+    f3 t = cross3(fwd, s);
+    float* g = geom + 18 * i;
+    st3(g, s0);
+    st3(g + 3, e0);
+    st3(g + 6, s * ra);
+    st3(g + 9, t * ra);
+    st3(g + 12, s * rb);
+    st3(g + 15, t * rb);
+}
+
+// ============================== primitive boxes ==================================================
+// Phantom: hull +- max(r0, r1) (GenerateAABBs :431-432); LSS: spheres; DOTS: 12 vertices in
+// the reference's order.
+__global__ void boxes_phantom_kernel(const float* curves, const float* rad, uint64_t n, float* boxes) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* c = curves + 12 * i;
+    float r = fmax_t(rad[2 * i], rad[2 * i + 1]);
+    for (int k = 0; k < 3; ++k) {
+        boxes[6 * i + k] = fmin_t(fmin_t(c[k], c[9 + k]), fmin_t(c[3 + k], c[6 + k])) - r;
+        boxes[6 * i + 3 + k] = fmax_t(fmax_t(c[k], c[9 + k]), fmax_t(c[3 + k], c[6 + k])) + r;
+    }
+}
+__global__ void boxes_lss_kernel(const float* geom, uint64_t n, float* boxes) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* g = geom + 8 * i;
+    float ra = g[6], rb = g[7];
+    for (int k = 0; k < 3; ++k) {
+        boxes[6 * i + k] = fmin_t(g[k] - ra, g[3 + k] - rb);
+        boxes[6 * i + 3 + k] = fmax_t(g[k] + ra, g[3 + k] + rb);
+    }
+}
+__device__ void dots_vertices(const float* g, float* v36) {
+    f3 s0 = ld3(g), e0 = ld3(g + 3);
+    for (int face = 0; face < 2; ++face) {
+        f3 va = ld3(g + 6 + 3 * face), vb = ld3(g + 12 + 3 * face);
+        float* o = v36 + 18 * face;
+        st3(o + 0, s0 + va);
+        st3(o + 3, e0 - vb);
+        st3(o + 6, e0 + vb);
+        st3(o + 9, s0 + va);
+        st3(o + 12, s0 - va);
+        st3(o + 15, e0 - vb);
+    }
+}
+__global__ void boxes_dots_kernel(const float* geom, uint64_t n, float* boxes) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float v[36];
+    dots_vertices(geom + 18 * i, v);
+    for (int k = 0; k < 3; ++k) {
+        float lo = v[k], hi = v[k];
+        for (int j = 1; j < 12; ++j) { lo = fmin_t(lo, v[3 * j + k]); hi = fmax_t(hi, v[3 * j + k]); }
+        boxes[6 * i + k] = lo;
+        boxes[6 * i + 3 + k] = hi;
+    }
+}
+__global__ void expand_dots_kernel(const float* geom, uint64_t n, float* out36) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dots_vertices(geom + 18 * i, out36 + 36 * i);
+}
+
+// ================================ Morton codes ===================================================
+__device__ __forceinline__ uint32_t f2ord(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+__global__ void centroid_bounds_kernel(const float* boxes, uint64_t n, uint32_t* ob /*6: min xyz, max xyz*/) {
+    __shared__ uint32_t s[6];
+    if (threadIdx.x < 3) s[threadIdx.x] = 0xffffffffu;
+    else if (threadIdx.x < 6) s[threadIdx.x] = 0u;
+    __syncthreads();
+    uint32_t lmin[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, lmax[3] = {0, 0, 0};
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+        for (int k = 0; k < 3; ++k) {
+            float cf = (boxes[6 * i + k] + boxes[6 * i + 3 + k]) * 0.5f;
+            if (!(cf == cf)) continue;  // NaN centroids (degenerate input) do not widen the bounds
+            uint32_t c = f2ord(cf);
+            lmin[k] = min(lmin[k], c);
+            lmax[k] = max(lmax[k], c);
+        }
+    for (int k = 0; k < 3; ++k) { atomicMin(&s[k], lmin[k]); atomicMax(&s[3 + k], lmax[k]); }
+    __syncthreads();
+    if (threadIdx.x < 3) atomicMin(&ob[threadIdx.x], s[threadIdx.x]);
+    else if (threadIdx.x < 6) atomicMax(&ob[threadIdx.x], s[threadIdx.x]);
+}
+__device__ __forceinline__ uint64_t expand21(uint32_t v) {
+    uint64_t x = v & 0x1fffff;
+    x = (x | (x << 32)) & 0x1f00000000ffffULL;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffULL;
+    x = (x | (x << 8)) & 0x100f00f00f00f00fULL;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ULL;
+    x = (x | (x << 2)) & 0x1249249249249249ULL;
+    return x;
+}
+__global__ void morton_kernel(const float* boxes, uint64_t n, const uint32_t* ob, uint64_t* codes, uint32_t* values) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t code = 0;
+    for (int k = 0; k < 3; ++k) {
+        float cmin = ord2f(ob[k]), cmax = ord2f(ob[3 + k]);
+        float ext = cmax - cmin;
+        float scale = ext > 0.0f ? 2097152.0f / ext : 0.0f;
+        float c = (boxes[6 * i + k] + boxes[6 * i + 3 + k]) * 0.5f;
+        float q = (c - cmin) * scale;
+        uint32_t qi = !(q > 0.0f) ? 0u : (q >= 2097151.0f ? 2097151u : uint32_t(q));
+        code |= expand21(qi) << (2 - k);
+    }
+    codes[i] = code;
+    values[i] = uint32_t(i);
+}
+
+// ================================ radix sort =====================================================
+// Stable LSD sort of 64-bit keys with 32-bit values, 8 bits per pass. Per pass: tile histograms
+// (digit-major), one exclusive scan, then a stable scatter: each tile is walked in 256-key
+// rounds; within a round keys are ranked per warp with __match_any_sync and across warps by a
+// per-digit prefix, so equal digits keep their input order.
+constexpr int kSortThreads = 256, kSortItems = 8, kSortTile = kSortThreads * kSortItems;
+
+__global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint64_t* keys, uint64_t n, int shift,
+                                                                  uint32_t* counts, uint32_t nblocks) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    uint64_t base = uint64_t(blockIdx.x) * kSortTile;
+    for (int r = 0; r < kSortItems; ++r) {
+        uint64_t i = base + uint64_t(r) * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    counts[uint64_t(threadIdx.x) * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(const uint64_t* kin, const uint32_t* vin,
+                                                                     uint64_t* kout, uint32_t* vout, uint64_t n,
+                                                                     int shift, const uint32_t* offsets,
+                                                                     uint32_t nblocks) {
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_w[8][256];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    s_base[t] = offsets[uint64_t(t) * nblocks + blockIdx.x];
+    uint64_t base = uint64_t(blockIdx.x) * kSortTile;
+    for (int r = 0; r < kSortItems; ++r) {
+        for (int k = t; k < 8 * 256; k += kSortThreads) (&s_w[0][0])[k] = 0;
+        __syncthreads();
+        uint64_t i = base + uint64_t(r) * kSortThreads + t;
+        bool valid = i < n;
+        uint64_t key = valid ? kin[i] : 0;
+        uint32_t val = valid ? vin[i] : 0;
+        uint32_t digit = valid ? uint32_t((key >> shift) & 255u) : 256u;
+        uint32_t peers = __match_any_sync(kFull, digit);
+        uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && lane == __ffs(peers) - 1) s_w[w][digit] = __popc(peers);
+        __syncthreads();
+        uint32_t run = s_base[t];
+        for (int ww = 0; ww < 8; ++ww) {
+            uint32_t c = s_w[ww][t];
+            s_w[ww][t] = run;
+            run += c;
+        }
+        s_base[t] = run;
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = s_w[w][digit] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t radix_sort(uint64_t* keys, uint32_t* vals, uint64_t n, cudaStream_t s) {
+    if (n <= 1) return cudaSuccess;
+    uint32_t nb = uint32_t((n + kSortTile - 1) / kSortTile);
+    uint64_t* k2 = nullptr;
+    uint32_t* v2 = nullptr;
+    uint32_t* counts = nullptr;
+    cudaError_t e = cudaMallocAsync(&k2, n * 8, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&v2, n * 4, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&counts, uint64_t(nb) * 256 * 4 * 2, s);
+    uint64_t* ka = keys;
+    uint64_t* kb = k2;
+    uint32_t* va = vals;
+    uint32_t* vb = v2;
+    for (int pass = 0; pass < 8 && e == cudaSuccess; ++pass) {
+        int shift = 8 * pass;
+        radix_hist_kernel<<<nb, kSortThreads, 0, s>>>(ka, n, shift, counts, nb);
+        e = device_scan<SumOp>(counts, counts + uint64_t(nb) * 256, uint64_t(nb) * 256, false, nullptr, s);
+        if (e != cudaSuccess) break;
+        radix_scatter_kernel<<<nb, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, counts + uint64_t(nb) * 256, nb);
+        e = cudaGetLastError();
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    // 8 passes: the result is back in (keys, vals)
+    cudaFreeAsync(k2, s);
+    cudaFreeAsync(v2, s);
+    cudaFreeAsync(counts, s);
+    return e;
+}
+
+// ============================ Karras hierarchy + refit ==========================================
+__device__ __forceinline__ int delta(const uint64_t* k, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = k[i], b = k[j];
+    if (a != b) return __clzll(a ^ b);
+    return 64 + __clz(uint32_t(i) ^ uint32_t(j));
+}
+__global__ void karras_kernel(const uint64_t* k, int64_t n, uint32_t* left, uint32_t* right, uint32_t* first,
+                              uint32_t* last, uint32_t* parent_int, uint32_t* parent_leaf) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(k, n, i, i + 1) - delta(k, n, i, i - 1)) > 0 ? 1 : -1;
+    int dmin = delta(k, n, i, i - d);
+    int64_t lmax = 2;
+    while (delta(k, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int64_t l = 0;
+    for (int64_t t = lmax / 2; t >= 1; t /= 2)
+        if (delta(k, n, i, i + (l + t) * d) > dmin) l += t;
+    int64_t j = i + l * d;
+    int dnode = delta(k, n, i, j);
+    int64_t s = 0;
+    for (int64_t div = 2;; div *= 2) {
+        int64_t t = (l + div - 1) / div;
+        if (delta(k, n, i, i + (s + t) * d) > dnode) s += t;
+        if (t == 1) break;
+    }
+    int64_t g = i + s * d + (d < 0 ? d : 0);
+    int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+    first[i] = uint32_t(lo);
+    last[i] = uint32_t(hi);
+    if (lo == g) { left[i] = kLeafFlag | uint32_t(g); parent_leaf[g] = uint32_t(i); }
+    else { left[i] = uint32_t(g); parent_int[g] = uint32_t(i); }
+    if (hi == g + 1) { right[i] = kLeafFlag | uint32_t(g + 1); parent_leaf[g + 1] = uint32_t(i); }
+    else { right[i] = uint32_t(g + 1); parent_int[g + 1] = uint32_t(i); }
+}
+
+__global__ void gather_boxes_kernel(const float* boxes, const uint32_t* order, uint64_t n, float* out) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t j = order[i];
+    for (int k = 0; k < 6; ++k) out[6 * i + k] = boxes[6 * j + k];
+}
+
+// Bottom-up refit: the second thread to reach a node computes union(left, right).
+__global__ void refit_kernel(const uint32_t* parent_leaf, const uint32_t* parent_int, const uint32_t* left,
+                             const uint32_t* right, const float* sboxes, float* nboxes, uint32_t* visits,
+                             uint64_t n, uint32_t* err) {
+    uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t node = parent_leaf[j];
+    for (int steps = 0; node != 0xffffffffu; ++steps) {
+        if (steps > 200) { atomicOr(err, kErrTimeout); return; }
+        __threadfence();
+        if (atomicAdd(&visits[node], 1u) == 0u) return;
+        __threadfence();
+        float b[6];
+        uint32_t c[2] = {left[node], right[node]};
+        for (int q = 0; q < 2; ++q) {
+            const float* src = (c[q] & kLeafFlag) ? sboxes + 6 * uint64_t(c[q] & ~kLeafFlag) : nboxes + 6 * uint64_t(c[q]);
+            float v[6];
+            for (int k = 0; k < 6; ++k) v[k] = __ldcg(src + k);
+            if (q == 0) for (int k = 0; k < 6; ++k) b[k] = v[k];
+            else for (int k = 0; k < 3; ++k) { b[k] = fmin_t(b[k], v[k]); b[3 + k] = fmax_t(b[3 + k], v[3 + k]); }
+        }
+        for (int k = 0; k < 6; ++k) __stcg(nboxes + 6 * uint64_t(node) + k, b[k]);
+        node = parent_int[node];
+    }
+}
+
+// ============================ collapse to BVH8 ====================================================
+struct BinView {
+    const uint32_t *left, *right, *first, *last;
+    const float* nboxes;  // internal node boxes
+    const float* sboxes;  // sorted leaf boxes
+};
+__device__ __forceinline__ uint32_t bcount(const BinView& b, uint32_t c) {
+    return (c & kLeafFlag) ? 1u : b.last[c] - b.first[c] + 1u;
+}
+__device__ __forceinline__ const float* bbox(const BinView& b, uint32_t c) {
+    return (c & kLeafFlag) ? b.sboxes + 6 * uint64_t(c & ~kLeafFlag) : b.nboxes + 6 * uint64_t(c);
+}
+__device__ __forceinline__ uint32_t bfirst(const BinView& b, uint32_t c) {
+    return (c & kLeafFlag) ? (c & ~kLeafFlag) : b.first[c];
+}
+__device__ __forceinline__ float sa_measure(const float* bx) {
+    float dx = bx[3] - bx[0], dy = bx[4] - bx[1], dz = bx[5] - bx[2];
+    return (dx * dy + dy * dz) + dz * dx;
+}
+
+__global__ void collapse_expand_kernel(BinView bv, const uint32_t* level, uint32_t count, int max_leaf,
+                                       uint32_t* kids, uint32_t* nk, uint32_t* nint, uint32_t* nprim) {
+    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= count) return;
+    uint32_t b = level[w];
+    uint32_t k[8];
+    int n = 0;
+    if (b & kLeafFlag) k[n++] = b;
+    else { k[n++] = bv.left[b]; k[n++] = bv.right[b]; }
+    while (n < 8) {
+        int best = -1;
+        float bsa = -1.0f;
+        for (int q = 0; q < n; ++q) {
+            uint32_t c = k[q];
+            if ((c & kLeafFlag) || bcount(bv, c) <= uint32_t(max_leaf)) continue;
+            float s = sa_measure(bbox(bv, c));
+            if (best < 0 || s > bsa) { best = q; bsa = s; }
+        }
+        if (best < 0) break;
+        uint32_t c = k[best];
+        k[best] = bv.left[c];
+        k[n++] = bv.right[c];
+    }
+    uint32_t ni = 0, np = 0;
+    for (int q = 0; q < n; ++q) {
+        uint32_t c = k[q];
+        kids[8 * uint64_t(w) + q] = c;
+        uint32_t cnt = bcount(bv, c);
+        if (!(c & kLeafFlag) && cnt > uint32_t(max_leaf)) ++ni;
+        else np += cnt;
+    }
+    nk[w] = uint32_t(n);
+    nint[w] = ni;
+    nprim[w] = np;
+}
+
+__global__ void collapse_emit_kernel(BinView bv, const uint32_t* level, uint32_t count, int max_leaf,
+                                     const uint32_t* kids, const uint32_t* nk, const uint32_t* int_off,
+                                     const uint32_t* prim_off, uint32_t node_base, uint32_t next_node_base,
+                                     uint32_t prim_base_g, NodeF* nodes, uint32_t* next_level, uint32_t* prim_order) {
+    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= count) return;
+    NodeF nd;
+    for (int q = 0; q < 8; ++q) {
+        nd.lo_x[q] = nd.hi_x[q] = nd.lo_y[q] = nd.hi_y[q] = nd.lo_z[q] = nd.hi_z[q] = 0.0f;
+        nd.meta[q] = 0;
+    }
+    for (int q = 0; q < 4; ++q) nd.pad[q] = 0;
+    nd.child_base = next_node_base + int_off[w];
+    nd.prim_base = prim_base_g + prim_off[w];
+    uint32_t rank = 0, poff = 0;
+    int n = int(nk[w]);
+    for (int q = 0; q < n; ++q) {
+        uint32_t c = kids[8 * uint64_t(w) + q];
+        const float* bx = bbox(bv, c);
+        nd.lo_x[q] = bx[0]; nd.lo_y[q] = bx[1]; nd.lo_z[q] = bx[2];
+        nd.hi_x[q] = bx[3]; nd.hi_y[q] = bx[4]; nd.hi_z[q] = bx[5];
+        uint32_t cnt = bcount(bv, c);
+        if (!(c & kLeafFlag) && cnt > uint32_t(max_leaf)) {
+            nd.meta[q] = uint8_t(0x80u | rank);
+            next_level[int_off[w] + rank] = c;
+            ++rank;
+        } else {
+            nd.meta[q] = uint8_t((cnt << 5) | poff);
+            uint32_t f = bfirst(bv, c);
+            for (uint32_t j = 0; j < cnt; ++j) prim_order[nd.prim_base + poff + j] = f + j;
+            poff += cnt;
+        }
+    }
+    nodes[node_base + w] = nd;
+}
+
+// ============================ encodings ===========================================================
+// 8-bit child boxes: origin p = min of the child boxes; e = least exponent with 255*2^e >= extent
+// (in double); qlo = floor((lo-p)*2^-e), qhi = ceil((hi-p)*2^-e), clamped to [0,255].
+__global__ void quantise_kernel(const NodeF* in, uint64_t nn, NodeQ* out) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    const NodeF& a = in[i];
+    NodeQ q;
+    const float* LO[3] = {a.lo_x, a.lo_y, a.lo_z};
+    const float* HI[3] = {a.hi_x, a.hi_y, a.hi_z};
+    uint8_t* QL[3] = {q.qlo_x, q.qlo_y, q.qlo_z};
+    uint8_t* QH[3] = {q.qhi_x, q.qhi_y, q.qhi_z};
+    float pp[3];
+    uint8_t ee[3];
+    uint32_t nc = 0;
+    for (int c = 0; c < 8; ++c) nc += a.meta[c] ? 1u : 0u;
+    for (int k = 0; k < 3; ++k) {
+        float p = __int_as_float(0x7f800000), P = -__int_as_float(0x7f800000);
+        for (int c = 0; c < 8; ++c) {
+            if (!a.meta[c]) continue;
+            p = fmin_t(p, LO[k][c]);
+            P = fmax_t(P, HI[k][c]);
+        }
+        double ext = double(P) - double(p);
+        int e;
+        if (!(ext > 0.0)) e = -126;
+        else {
+            int ex;
+            double m = frexp(ext / 255.0, &ex);
+            e = (m == 0.5) ? ex - 1 : ex;
+            while (ldexp(255.0, e) < ext) ++e;
+            if (e < -126) e = -126;
+            if (e > 127) e = 127;
+        }
+        pp[k] = p;
+        ee[k] = uint8_t(e + 127);
+        double inv = ldexp(1.0, -e);
+        for (int c = 0; c < 8; ++c) {
+            if (!a.meta[c]) { QL[k][c] = 255; QH[k][c] = 0; continue; }
+            double lo = floor((double(LO[k][c]) - double(p)) * inv);
+            double hi = ceil((double(HI[k][c]) - double(p)) * inv);
+            QL[k][c] = uint8_t(lo < 0.0 ? 0.0 : (lo > 255.0 ? 255.0 : lo));
+            QH[k][c] = uint8_t(hi < 0.0 ? 0.0 : (hi > 255.0 ? 255.0 : hi));
+        }
+    }
+    q.px = pp[0]; q.py = pp[1]; q.pz = pp[2];
+    q.ex = ee[0]; q.ey = ee[1]; q.ez = ee[2];
+    q.nchild = uint8_t(nc);
+    q.child_base = a.child_base;
+    q.prim_base = a.prim_base;
+    for (int c = 0; c < 8; ++c) q.meta[c] = a.meta[c];
+    out[i] = q;
+}
+
+__global__ void map_order_kernel(const uint32_t* sorted_pos, const uint32_t* sorted_index, uint64_t n, uint32_t* out) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = sorted_index[sorted_pos[i]];
+}
+
+// Primitive records in slot order.
+__global__ void records_kernel(int type, int precision, const uint32_t* ids, uint64_t n, const float* curves,
+                               const float* lrad, const float* geom, const uint32_t* chunk_incl, const float4* roots,
+                               void* prims) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t s = ids[i];
+    if (type == HRT_BLAS_PHANTOM && precision == HRT_PRECISION_FP32) {
+        const float* c = curves + 12 * uint64_t(s);
+        PrimPhantomF r;
+        r.a = make_float4(c[0], c[1], c[2], lrad[2 * uint64_t(s)]);
+        r.b = make_float4(c[3], c[4], c[5], lrad[2 * uint64_t(s) + 1]);
+        r.c = make_float4(c[6], c[7], c[8], __uint_as_float(s));
+        r.d = make_float4(c[9], c[10], c[11], 0.0f);
+        static_cast<PrimPhantomF*>(prims)[i] = r;
+    } else if (type == HRT_BLAS_PHANTOM) {
+        const float* c = curves + 12 * uint64_t(s);
+        uint32_t ch = chunk_incl[s] - 1;
+        float4 rt = roots[ch];
+        float root[3] = {rt.x, rt.y, rt.z};
+        __half h[16];
+        for (int j = 0; j < 12; ++j) h[j] = __float2half_rn(c[j] - root[j % 3]);
+        h[12] = __float2half_rn(lrad[2 * uint64_t(s)]);
+        h[13] = __float2half_rn(lrad[2 * uint64_t(s) + 1]);
+        uint32_t key = (ch << 8) | (s - __float_as_uint(rt.w));
+        uint32_t w[8];
+        for (int j = 0; j < 7; ++j)
+            w[j] = uint32_t(__half_as_ushort(h[2 * j])) | (uint32_t(__half_as_ushort(h[2 * j + 1])) << 16);
+        w[7] = key;
+        PrimPhantomH r;
+        r.q0 = make_uint4(w[0], w[1], w[2], w[3]);
+        r.q1 = make_uint4(w[4], w[5], w[6], w[7]);
+        static_cast<PrimPhantomH*>(prims)[i] = r;
+    } else if (type == HRT_BLAS_LSS) {
+        const float* g = geom + 8 * uint64_t(s);
+        PrimLss r;
+        r.a = make_float4(g[0], g[1], g[2], g[6]);
+        r.b = make_float4(g[3], g[4], g[5], g[7]);
+        static_cast<PrimLss*>(prims)[i] = r;
+    } else {
+        const float* g = geom + 18 * uint64_t(s);
+        PrimDots r;
+        r.a = make_float4(g[0], g[1], g[2], g[3]);
+        r.b = make_float4(g[4], g[5], g[6], g[7]);
+        r.c = make_float4(g[8], g[9], g[10], g[11]);
+        r.d = make_float4(g[12], g[13], g[14], g[15]);
+        r.e = make_float4(g[16], g[17], __uint_as_float(s), 0.0f);
+        static_cast<PrimDots*>(prims)[i] = r;
+    }
+}
+
+template <class T> cudaError_t dalloc(T** p, uint64_t count, cudaStream_t s) {
+    return cudaMallocAsync(reinterpret_cast<void**>(p), count * sizeof(T) + 16, s);
+}
+
+}  // namespace
+
+// =================================================================================================
+cudaError_t make_lines(const float* verts, const float* vrad, float const_radius, const uint32_t* strand_line_off,
+                       const uint32_t* strand_vert_off, uint64_t nstrands, const uint32_t* line_idx, uint64_t nlines,
+                       float* lines, float* lrad, cudaStream_t s) {
+    if (nlines == 0) return cudaSuccess;
+    if (line_idx)
+        lines_from_indices_kernel<<<grid_for(nlines, 256), 256, 0, s>>>(verts, vrad, const_radius, line_idx, nlines, lines, lrad);
+    else
+        lines_from_strands_kernel<<<grid_for(nlines, 256), 256, 0, s>>>(verts, vrad, const_radius, strand_line_off,
+                                                                         strand_vert_off, nstrands, nlines, lines, lrad);
+    return cudaGetLastError();
+}
+
+void free_build_output(BuildOutput& o) {
+    void* ptrs[] = {o.nodes, o.qnodes_aux, o.prims, o.roots, o.prim_ids, o.prim_boxes, o.curves, o.geom,
+                    o.morton_sorted, o.sorted_index, o.bin_left, o.bin_right, o.bin_boxes, o.prim_order};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    o = BuildOutput{};
+}
+
+#define HRT_CK(x)                                                                              \
+    do {                                                                                       \
+        cudaError_t e_ = (x);                                                                  \
+        if (e_ != cudaSuccess) {                                                               \
+            snprintf(msg, msglen, "%s failed: %s (build.cu:%d)", #x, cudaGetErrorString(e_), __LINE__); \
+            return e_;                                                                         \
+        }                                                                                      \
+    } while (0)
+
+cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream_t s, char* msg, size_t msglen) {
+    const uint64_t n = in.n;
+    const unsigned T = 256;
+    out.node_bytes = in.precision == HRT_PRECISION_QUANTISED ? sizeof(NodeQ) : sizeof(NodeF);
+    if (in.type == HRT_BLAS_PHANTOM) out.prim_bytes = in.precision == HRT_PRECISION_QUANTISED ? 32 : 64;
+    else out.prim_bytes = in.type == HRT_BLAS_LSS ? 32 : 80;
+    if (n == 0) return cudaSuccess;
+
+    // ---- geometry processing -> per-segment boxes (and the intersected geometry) ----------------
+    HRT_CK(cudaMalloc(&out.prim_boxes, n * 6 * sizeof(float)));
+    float* rad_for_boxes = nullptr;   // Phantom radii used for the boxes
+    float* dq = nullptr;              // dequantised curves (quantised Phantom)
+    uint32_t* chunk_incl = nullptr;
+    uint32_t* keys_tmp = nullptr;
+    uint64_t nchunks = 0;
+    if (in.type == HRT_BLAS_PHANTOM) {
+        HRT_CK(cudaMalloc(&out.curves, n * 12 * sizeof(float)));
+        curves_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, n, out.curves);
+        HRT_CK(cudaGetLastError());
+        if (in.precision == HRT_PRECISION_QUANTISED) {
+            uint32_t chunk = in.quant_chunk ? in.quant_chunk : 256u;
+            if (chunk > 256u) chunk = 256u;
+            uint32_t *runpos, *runstart, *flags, *total;
+            HRT_CK(dalloc(&runpos, n, s));
+            HRT_CK(dalloc(&runstart, n, s));
+            HRT_CK(dalloc(&flags, n, s));
+            HRT_CK(dalloc(&chunk_incl, n, s));
+            HRT_CK(dalloc(&total, 1, s));
+            run_flags_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, n, runpos);
+            HRT_CK(device_scan<MaxOp>(runpos, runstart, n, true, nullptr, s));
+            chunk_flags_kernel<<<grid_for(n, T), T, 0, s>>>(runstart, n, chunk, flags);
+            HRT_CK(device_scan<SumOp>(flags, chunk_incl, n, true, total, s));
+            uint32_t h_total = 0;
+            HRT_CK(cudaMemcpyAsync(&h_total, total, 4, cudaMemcpyDeviceToHost, s));
+            HRT_CK(cudaStreamSynchronize(s));
+            nchunks = h_total;
+            if (nchunks >= (1ull << 24)) {
+                snprintf(msg, msglen, "quantised Phantom BLAS needs %llu chunk roots; the limit is 2^24",
+                         (unsigned long long)nchunks);
+                return cudaErrorInvalidValue;
+            }
+            HRT_CK(cudaMalloc(&out.roots, nchunks * sizeof(float4)));
+            out.nroots = nchunks;
+            chunk_roots_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, flags, chunk_incl, n, out.roots);
+            HRT_CK(dalloc(&dq, n * 12, s));
+            HRT_CK(dalloc(&rad_for_boxes, n * 2, s));
+            HRT_CK(dalloc(&keys_tmp, n, s));
+            dequant_curves_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, in.lrad, chunk_incl, out.roots, n, dq,
+                                                                rad_for_boxes, keys_tmp);
+            HRT_CK(cudaGetLastError());
+            boxes_phantom_kernel<<<grid_for(n, T), T, 0, s>>>(dq, rad_for_boxes, n, out.prim_boxes);
+            cudaFreeAsync(runpos, s);
+            cudaFreeAsync(runstart, s);
+            cudaFreeAsync(flags, s);
+            cudaFreeAsync(total, s);
+        } else {
+            boxes_phantom_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, in.lrad, n, out.prim_boxes);
+        }
+    } else if (in.type == HRT_BLAS_LSS) {
+        HRT_CK(cudaMalloc(&out.geom, n * 8 * sizeof(float)));
+        lss_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, out.geom);
+        boxes_lss_kernel<<<grid_for(n, T), T, 0, s>>>(out.geom, n, out.prim_boxes);
+    } else {
+        HRT_CK(cudaMalloc(&out.geom, n * 18 * sizeof(float)));
+        dots_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, out.geom);
+        boxes_dots_kernel<<<grid_for(n, T), T, 0, s>>>(out.geom, n, out.prim_boxes);
+    }
+    HRT_CK(cudaGetLastError());
+
+    // ---- Morton codes + sort ----------------------------------------------------------------
+    uint32_t* ob;
+    uint64_t* codes;
+    uint32_t* order;
+    float* sboxes;
+    uint32_t* err;
+    HRT_CK(dalloc(&ob, 6, s));
+    HRT_CK(dalloc(&err, 1, s));
+    HRT_CK(cudaMemsetAsync(err, 0, 4, s));
+    uint32_t init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+    HRT_CK(cudaMemcpyAsync(ob, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    centroid_bounds_kernel<<<unsigned(grid_for(n, T) < 1024 ? grid_for(n, T) : 1024), T, 0, s>>>(out.prim_boxes, n, ob);
+    HRT_CK(cudaMalloc(&codes, n * 8));
+    HRT_CK(cudaMalloc(&order, n * 4));
+    morton_kernel<<<grid_for(n, T), T, 0, s>>>(out.prim_boxes, n, ob, codes, order);
+    HRT_CK(cudaGetLastError());
+    HRT_CK(radix_sort(codes, order, n, s));
+    HRT_CK(dalloc(&sboxes, n * 6, s));
+    gather_boxes_kernel<<<grid_for(n, T), T, 0, s>>>(out.prim_boxes, order, n, sboxes);
+
+    // ---- Karras + refit -------------------------------------------------------------------------
+    uint64_t ni = n - 1;
+    uint32_t *left = nullptr, *right = nullptr, *first = nullptr, *last = nullptr, *pint = nullptr, *pleaf = nullptr,
+             *visits = nullptr;
+    float* nboxes = nullptr;
+    if (n >= 2) {
+        HRT_CK(cudaMalloc(&left, ni * 4));
+        HRT_CK(cudaMalloc(&right, ni * 4));
+        HRT_CK(dalloc(&first, ni, s));
+        HRT_CK(dalloc(&last, ni, s));
+        HRT_CK(dalloc(&pint, ni, s));
+        HRT_CK(dalloc(&pleaf, n, s));
+        HRT_CK(dalloc(&visits, ni, s));
+        HRT_CK(cudaMalloc(&nboxes, ni * 6 * sizeof(float)));
+        HRT_CK(cudaMemsetAsync(pint, 0xff, ni * 4, s));
+        HRT_CK(cudaMemsetAsync(visits, 0, ni * 4, s));
+        karras_kernel<<<grid_for(ni, T), T, 0, s>>>(codes, int64_t(n), left, right, first, last, pint, pleaf);
+        refit_kernel<<<grid_for(n, T), T, 0, s>>>(pleaf, pint, left, right, sboxes, nboxes, visits, n, err);
+        HRT_CK(cudaGetLastError());
+    }
+
+    // ---- collapse to BVH8, breadth first -----------------------------------------------------
+    BinView bv{left, right, first, last, nboxes, sboxes};
+    NodeF* nodes_tmp;
+    HRT_CK(dalloc(&nodes_tmp, n, s));
+    uint32_t *lvl_a, *lvl_b, *kids, *nk, *nint, *nprim, *int_off, *prim_off, *totals, *porder;
+    HRT_CK(dalloc(&lvl_a, n, s));
+    HRT_CK(dalloc(&lvl_b, n, s));
+    HRT_CK(dalloc(&kids, 8 * n, s));
+    HRT_CK(dalloc(&nk, n, s));
+    HRT_CK(dalloc(&nint, n, s));
+    HRT_CK(dalloc(&nprim, n, s));
+    HRT_CK(dalloc(&int_off, n, s));
+    HRT_CK(dalloc(&prim_off, n, s));
+    HRT_CK(dalloc(&totals, 2, s));
+    HRT_CK(dalloc(&porder, n, s));
+    uint32_t root = n == 1 ? kLeafFlag : 0u;
+    HRT_CK(cudaMemcpyAsync(lvl_a, &root, 4, cudaMemcpyHostToDevice, s));
+    uint32_t count = 1, node_base = 0, next_node_base = 1, prim_base = 0;
+    for (int level = 0; count > 0; ++level) {
+        if (level > 4096) { snprintf(msg, msglen, "BVH8 collapse did not terminate"); return cudaErrorUnknown; }
+        collapse_expand_kernel<<<grid_for(count, T), T, 0, s>>>(bv, lvl_a, count, in.max_leaf, kids, nk, nint, nprim);
+        HRT_CK(cudaGetLastError());
+        HRT_CK(device_scan<SumOp>(nint, int_off, count, false, totals, s));
+        HRT_CK(device_scan<SumOp>(nprim, prim_off, count, false, totals + 1, s));
+        collapse_emit_kernel<<<grid_for(count, T), T, 0, s>>>(bv, lvl_a, count, in.max_leaf, kids, nk, int_off, prim_off,
+                                                              node_base, next_node_base, prim_base, nodes_tmp, lvl_b,
+                                                              porder);
+        HRT_CK(cudaGetLastError());
+        uint32_t h_tot[2];
+        HRT_CK(cudaMemcpyAsync(h_tot, totals, 8, cudaMemcpyDeviceToHost, s));
+        HRT_CK(cudaStreamSynchronize(s));
+        node_base = next_node_base;
+        next_node_base += h_tot[0];
+        prim_base += h_tot[1];
+        count = h_tot[0];
+        std::swap(lvl_a, lvl_b);
+    }
+    out.nnodes = node_base;
+    if (prim_base != n) {
+        snprintf(msg, msglen, "BVH8 collapse placed %u of %llu primitives", prim_base, (unsigned long long)n);
+        return cudaErrorUnknown;
+    }
+
+    // ---- encodings and primitive records -----------------------------------------------------
+    NodeQ* qn;
+    HRT_CK(cudaMalloc(&qn, out.nnodes * sizeof(NodeQ)));
+    quantise_kernel<<<grid_for(out.nnodes, T), T, 0, s>>>(nodes_tmp, out.nnodes, qn);
+    NodeF* fnodes;
+    HRT_CK(cudaMalloc(&fnodes, out.nnodes * sizeof(NodeF)));
+    HRT_CK(cudaMemcpyAsync(fnodes, nodes_tmp, out.nnodes * sizeof(NodeF), cudaMemcpyDeviceToDevice, s));
+    if (in.precision == HRT_PRECISION_QUANTISED) { out.nodes = qn; out.qnodes_aux = fnodes; }
+    else { out.nodes = fnodes; out.qnodes_aux = qn; }
+    HRT_CK(cudaMalloc(&out.prim_ids, n * 4));
+    map_order_kernel<<<grid_for(n, T), T, 0, s>>>(porder, order, n, out.prim_ids);
+    HRT_CK(cudaMalloc(&out.prims, n * out.prim_bytes));
+    records_kernel<<<grid_for(n, T), T, 0, s>>>(in.type, in.precision, out.prim_ids, n, out.curves, in.lrad, out.geom,
+                                                chunk_incl, out.roots, out.prims);
+    HRT_CK(cudaGetLastError());
+
+    // bounds: union of all primitive boxes = root of the binary tree
+    float hb[6];
+    HRT_CK(cudaMemcpyAsync(hb, n >= 2 ? nboxes : sboxes, 24, cudaMemcpyDeviceToHost, s));
+    uint32_t h_err = 0;
+    HRT_CK(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, s));
+    HRT_CK(cudaStreamSynchronize(s));
+    memcpy(out.bounds, hb, sizeof(hb));
+    if (h_err) { snprintf(msg, msglen, "refit exceeded its depth bound"); return cudaErrorUnknown; }
+
+    if (in.keep_intermediate) {
+        out.morton_sorted = codes;
+        out.sorted_index = order;
+        out.bin_left = left;
+        out.bin_right = right;
+        out.bin_boxes = nboxes;
+        out.prim_order = nullptr;
+    } else {
+        cudaFree(codes);
+        cudaFree(order);
+        if (left) cudaFree(left);
+        if (right) cudaFree(right);
+        if (nboxes) cudaFree(nboxes);
+    }
+    void* tmps[] = {ob, err, sboxes, first, last, pint, pleaf, visits, nodes_tmp, lvl_a, lvl_b, kids, nk, nint,
+                    nprim, int_off, prim_off, totals, porder, dq, rad_for_boxes, chunk_incl, keys_tmp};
+    for (void* p : tmps)
+        if (p) cudaFreeAsync(p, s);
+    HRT_CK(cudaStreamSynchronize(s));
+    out.device_bytes = n * 6 * 4 + (out.curves ? n * 48 : 0) +
+                       (out.geom ? n * (in.type == HRT_BLAS_LSS ? 32 : 72) : 0) + out.nnodes * (sizeof(NodeF) + sizeof(NodeQ)) +
+                       n * 4 + n * out.prim_bytes + out.nroots * 16;
+    return cudaSuccess;
+}
+
+// Expands DOTS frames into the reference's 12 vertices per segment (inspection only).
+cudaError_t expand_dots(const float* geom, uint64_t n, float* out36, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    expand_dots_kernel<<<grid_for(n, 256), 256, 0, s>>>(geom, n, out36);
+    return cudaGetLastError();
+}
+
+}  // namespace hrt

@@ -1,0 +1,142 @@
+// hrt_internal.h -- layouts shared by the BVH build (build.cu), the trace kernels (trace.cu)
+// and the C ABI (api.cu). Device memory only; nothing here is part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hrt.h"
+
+namespace hrt {
+
+constexpr uint32_t kLeafFlag = 0x80000000u;
+constexpr int kStackSize = 64;          // traversal stack entries per ray
+constexpr uint32_t kMaxTraversalSteps = 1u << 16;  // per ray; exceeding it sets kErrTimeout
+
+// Device error word bits (read back by the host after a launch).
+constexpr uint32_t kErrStackOverflow = 1u;
+constexpr uint32_t kErrTimeout = 2u;
+
+// ---- BVH8 nodes -----------------------------------------------------------------------------
+// Both node formats describe the same tree (same children, same order):
+//   meta[k] == 0            empty slot
+//   meta[k] & 0x80          internal child, node index child_base + (meta & 7)
+//   otherwise               leaf: (meta >> 5) primitives from slot prim_base + (meta & 31)
+struct alignas(16) NodeF {  // 224 bytes, FP32 child boxes (structure of arrays)
+    float lo_x[8], hi_x[8], lo_y[8], hi_y[8], lo_z[8], hi_z[8];
+    uint32_t child_base, prim_base;
+    uint8_t meta[8];
+    uint32_t pad[4];
+};
+static_assert(sizeof(NodeF) == 224, "NodeF layout");
+
+struct alignas(16) NodeQ {  // 80 bytes, child boxes as 8-bit offsets on a per-axis 2^e grid
+    float px, py, pz;       // grid origin (min of the child boxes)
+    uint8_t ex, ey, ez;     // e + 127
+    uint8_t nchild;
+    uint32_t child_base, prim_base;
+    uint8_t meta[8];
+    uint8_t qlo_x[8], qhi_x[8], qlo_y[8], qhi_y[8], qlo_z[8], qhi_z[8];
+};
+static_assert(sizeof(NodeQ) == 80, "NodeQ layout");
+
+// ---- primitive records (leaf slot order) ----------------------------------------------------
+// Phantom FP32 (64 B): {start, r0} {cp1, r1} {cp2, id} {end, 0}
+// Phantom FP16 (32 B): 12 halves = control points minus the chunk root, halves r0 r1,
+//                      uint32 key = chunk << 8 | segment-in-chunk; roots[chunk] = {xyz, first id}
+// LSS (32 B): {p0, r0} {p1, r1}; id from prim_ids
+// DOTS (80 B): start, end, s*r0, t*r0, s*r1, t*r1 (18 floats), id, pad
+struct alignas(16) PrimPhantomF { float4 a, b, c, d; };
+struct alignas(16) PrimPhantomH { uint4 q0, q1; };
+struct alignas(16) PrimLss { float4 a, b; };
+struct alignas(16) PrimDots { float4 a, b, c, d, e; };
+
+struct DevBlas {
+    const void* nodes;        // NodeF or NodeQ
+    const void* prims;        // records in slot order
+    const float4* roots;      // quantised Phantom chunk roots
+    const uint32_t* prim_ids; // slot -> segment index
+    uint32_t type, precision, nprims, nnodes;
+    float lo[3], hi[3];
+};
+
+struct DevInstance {
+    DevBlas b;
+    float w2o[12];   // world -> object, rows of a 3x4 affine matrix
+    float nrm[9];    // object -> world normal matrix (inverse transpose, rows)
+    uint32_t identity;
+    float wlo[3], whi[3];  // world-space bounds
+};
+
+// One scene of a launch (a frame, or one scene of a batch).
+struct SceneLaunch {
+    const DevInstance* inst;
+    uint32_t ninst;
+    uint32_t width, height, spp;
+    uint32_t tiles_x;          // 8x4 pixel tiles per row
+    uint64_t work_begin;       // first global work item (a tile-ordered pixel) of the scene
+    uint64_t work_count;       // tiles * 32
+    float view_inv[16], proj_inv[16];
+    float4* fb;
+    hrt_hit* hits;
+};
+
+struct TraceCounters {
+    unsigned long long work;     // next work item
+    unsigned long long primary, shadow, nodes, prims, fp64_resolves, fp64_hits;
+    uint32_t error;
+    uint32_t pad;
+};
+
+struct TraceLaunch {
+    const SceneLaunch* scenes;
+    uint32_t nscenes;
+    uint64_t total_work;
+    float tmin, tmax, shadow_tmin;
+    uint32_t jitter, seed, shading, fp64_resolve, record_hits, count_stats;
+    TraceCounters* counters;
+};
+
+// ---- launch wrappers (trace.cu) --------------------------------------------------------------
+cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count);
+cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n,
+                              float tmin, float tmax, uint32_t fp64_resolve, hrt_hit* hits,
+                              TraceCounters* counters, bool quantised_nodes, cudaStream_t s, int sm_count);
+
+// ---- BVH build (build.cu) ----------------------------------------------------------------------
+struct BuildInput {
+    int type, precision, max_leaf;
+    uint32_t quant_chunk;
+    const float* lines;   // device, n x 6
+    const float* lrad;    // device, n x 2 (per line end)
+    uint64_t n;
+    bool keep_intermediate;
+};
+struct BuildOutput {
+    // owned device allocations (freed by the BLAS)
+    void* nodes = nullptr;        // NodeF or NodeQ (per precision)
+    void* qnodes_aux = nullptr;   // NodeQ copy when nodes are NodeF (inspection) or vice versa
+    void* prims = nullptr;
+    float4* roots = nullptr;
+    uint32_t* prim_ids = nullptr;
+    float* prim_boxes = nullptr;  // n x 6, segment order
+    float* curves = nullptr;      // Phantom n x 12 (FP32, segment order)
+    float* geom = nullptr;        // DOTS n x 18 / LSS n x 8 (segment order)
+    uint64_t* morton_sorted = nullptr;
+    uint32_t* sorted_index = nullptr;
+    uint32_t* bin_left = nullptr;
+    uint32_t* bin_right = nullptr;
+    float* bin_boxes = nullptr;
+    uint32_t* prim_order = nullptr;
+    uint64_t nnodes = 0, nroots = 0, node_bytes = 0, prim_bytes = 0, device_bytes = 0;
+    float bounds[6] = {0, 0, 0, 0, 0, 0};
+};
+// Runs the whole device build; returns a CUDA error or cudaSuccess; msg gets a reason.
+cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream_t s, char* msg, size_t msglen);
+void free_build_output(BuildOutput& out);
+cudaError_t expand_dots(const float* geom, uint64_t n, float* out36, cudaStream_t s);
+// Line generation from vertices (device pointers); see hrt_blas_input.
+cudaError_t make_lines(const float* verts, const float* vrad, float const_radius, const uint32_t* strand_line_off,
+                       const uint32_t* strand_vert_off, uint64_t nstrands, const uint32_t* line_idx, uint64_t nlines,
+                       float* lines, float* lrad, cudaStream_t s);
+
+}  // namespace hrt

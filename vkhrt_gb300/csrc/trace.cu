@@ -1,0 +1,780 @@
+// trace.cu -- the trace pass: ray generation, BVH8 traversal, the three hair intersectors,
+// closest-hit shading and the shadow ray, in one persistent kernel.
+//
+// Replaces ray_gen.rgen:16-48 -> traceRayEXT (RT-core traversal) -> hair_intersection.rint /
+// hardware LSS and triangle tests -> hair_closest_hit.rchit / triangle_closest_hit.rchit ->
+// miss.rmiss (constant black background, the payload's initial value ray_gen.rgen:30).
+//
+// Work: warps take 32 work items at a time from a global counter; 32 consecutive items are one
+// 8x4 pixel tile of one scene, so a warp's rays are coherent. Each thread traces all samples
+// of its pixel (primary ray, shading, shadow ray) and writes the averaged pixel.
+// Traversal: per-thread stack of (node or leaf reference, entry distance); at each BVH8 node
+// the eight child boxes are tested, the hits sorted by entry distance with a sorting network
+// in registers and pushed far to near. All waits are bounded: a full stack or more than
+// kMaxTraversalSteps steps ends the ray and sets a bit in the device error word.
+#include <cuda_fp16.h>
+
+#include "hrt_internal.h"
+
+namespace hrt {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kThreads = 128;
+
+// ---------------------------------------------------------------- small vector helpers
+template <class T> struct V3 { T x, y, z; };
+template <class T> __device__ __forceinline__ V3<T> mk(T x, T y, T z) { return {x, y, z}; }
+template <class T> __device__ __forceinline__ V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class T> __device__ __forceinline__ V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class T> __device__ __forceinline__ V3<T> operator*(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class T> __device__ __forceinline__ T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> __device__ __forceinline__ V3<T> cross(V3<T> x, V3<T> y) {
+    return {x.y * y.z - y.y * x.z, x.z * y.x - y.z * x.x, x.x * y.y - y.x * x.y};
+}
+__device__ __forceinline__ float rsq(float x) { return 1.0f / sqrtf(x); }
+__device__ __forceinline__ double rsq(double x) { return 1.0 / sqrt(x); }
+template <class T> __device__ __forceinline__ V3<T> normalize(V3<T> v) { return rsq(dot(v, v)) * v; }
+template <class T> __device__ __forceinline__ T length(V3<T> v) { return sqrt(dot(v, v)); }
+template <class T> __device__ __forceinline__ T gmin(T x, T y) { return (y < x) ? y : x; }  // glm order
+template <class T> __device__ __forceinline__ T gmax(T x, T y) { return (x < y) ? y : x; }
+template <class T> __device__ __forceinline__ T gabs(T x) { return x >= T(0) ? x : -x; }
+
+// ---------------------------------------------------------------- Phantom (Prhi)
+// curve.glsl:9-31
+template <class T> __device__ __forceinline__ V3<T> bez_point(const V3<T>* c, T t) {
+    T u = T(1) - t, tt = t * t, uu = u * u;
+    T uuu = uu * u, ttt = tt * t;
+    return uuu * c[0] + (T(3) * uu * t) * c[1] + (T(3) * u * tt) * c[2] + ttt * c[3];
+}
+template <class T> __device__ __forceinline__ V3<T> bez_axis(const V3<T>* c, T t) {
+    T u = T(1) - t;
+    return (T(-3) * u * u) * c[0] + (T(3) * (T(3) * t * t - T(4) * t + T(1))) * c[1] +
+           (T(3) * (T(2) - T(3) * t) * t) * c[2] + (T(3) * t * t) * c[3];
+}
+// cylinder.glsl:8-46 (capped cylinder, boolean; no range test on t)
+template <class T> __device__ __forceinline__ bool ray_cylinder(V3<T> o, V3<T> d, V3<T> p0, V3<T> p1, T r) {
+    V3<T> ba = p1 - p0, oc = o - p0;
+    T baba = dot(ba, ba), bard = dot(ba, d), baoc = dot(ba, oc);
+    T k2 = baba - bard * bard;
+    T k1 = baba * dot(oc, d) - baoc * bard;
+    T k0 = baba * dot(oc, oc) - baoc * baoc - r * r * baba;
+    T h = k1 * k1 - k2 * k0;
+    if (h < T(0)) return false;
+    h = sqrt(h);
+    T t = (-k1 - h) / k2;
+    T y = baoc + t * bard;
+    if (y > T(0) && y < baba) return true;
+    t = ((y < T(0) ? T(0) : baba) - baoc) / bard;
+    return gabs(k1 + k2 * t) < h;
+}
+
+enum { kMiss = 0, kHit = 1, kUnresolved = 2 };
+template <class T> struct PrhiOut { T s; T tc; int status; };
+
+// ray.glsl:13-17 MakeOrthonormalBasis; the RCC transform (ray.glsl:19-33) is the inverse of
+// [e1 e2 e3 | o], applied here as the transpose of the orthonormal frame after the translation.
+template <class T> struct Frame { V3<T> o, d, e1, e2, e3; };
+template <class T> __device__ __forceinline__ Frame<T> make_frame(V3<T> o, V3<T> d) {
+    Frame<T> f;
+    f.o = o;
+    f.d = d;
+    f.e3 = normalize(d);
+    V3<T> w = f.e3;
+    f.e2 = gabs(w.x) > gabs(w.y) ? normalize(mk(-w.z, T(0), w.x)) : normalize(mk(T(0), w.z, -w.y));
+    f.e1 = cross(f.e2, w);
+    return f;
+}
+
+// hair_intersection.rint:15-130 with the cone radius r0 + (r1 - r0) t (constant when equal).
+// status kUnresolved: no hit and some side used all 8 iterations inside [0, 1].
+template <class T>
+__device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T r0, T r1) {
+    PrhiOut<T> out{T(0), T(0), kMiss};
+    V3<T> mid = bez_point(P, T(0.5));
+    T rmax = length(cross(mid - P[0], mid - P[3])) / length(P[3] - P[0]) + gmax(r0, r1);
+    if (!ray_cylinder(F.o, F.d, P[0], P[3], rmax)) return out;
+    V3<T> Q[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        V3<T> w = P[k] - F.o;
+        Q[k] = mk(dot(F.e1, w), dot(F.e2, w), dot(F.e3, w));
+    }
+    T tStart = (Q[3].z - Q[0].z) > T(0) ? T(0) : T(1);
+    bool exhausted_any = false;
+    for (int side = 0; side < 2; ++side) {
+        T t = tStart, told = T(0), dt1 = T(0), dt2 = T(0);
+        bool exhausted = true;
+        for (int i = 0; i < 8; ++i) {
+            V3<T> c = bez_point(Q, t);
+            V3<T> ax = bez_axis(Q, t);
+            T rad = (r0 == r1) ? r0 : r0 + (r1 - r0) * t;
+            // cone.glsl:21-62 with slant 0
+            T ddd = ax.x * ax.x + ax.y * ax.y;
+            T dp = c.x * c.x + c.y * c.y;
+            T cdd = c.x * ax.x + c.y * ax.y;
+            T cxd = c.x * ax.y - c.y * ax.x;
+            T cc = ddd;
+            T b = ax.z * (-cdd);
+            T cdz2 = ax.z * ax.z;
+            ddd += cdz2;
+            T a = cxd * cxd - ddd * (rad * rad) + dp * cdz2;
+            T det = b * b - a * cc;
+            bool isect = det > T(0);
+            T s = (b - (isect ? sqrt(det) : T(0))) / cc;
+            T dt = (s * ax.z - cdd) / ddd;
+            if (isect && gabs(dt) < T(5e-5)) {
+                out.s = s + c.z;
+                out.tc = t;
+                exhausted = false;
+                break;
+            }
+            dt = gmin(dt, T(0.5));
+            dt = gmax(dt, T(-0.5));
+            dt1 = dt2;
+            dt2 = dt;
+            if (dt1 * dt2 < T(0)) {
+                T tnext = ((i & 3) == 0) ? T(0.5) * (told + t) : (dt2 * told - dt1 * t) / (dt2 - dt1);
+                told = t;
+                t = tnext;
+            } else {
+                told = t;
+                t += dt;
+            }
+            if (t < T(0) || t > T(1)) { exhausted = false; break; }
+        }
+        exhausted_any |= exhausted;
+        if (out.s > T(0)) break;
+        tStart = T(1) - tStart;
+    }
+    out.status = out.s > T(0) ? kHit : (exhausted_any ? kUnresolved : kMiss);
+    return out;
+}
+
+// FP64 re-solve of one candidate, kept out of line so the FP32 path keeps its registers.
+__device__ __noinline__ void prhi_fp64(float ox, float oy, float oz, float dx, float dy, float dz, const float* cp,
+                                       float r0, float r1, double* s_out, double* tc_out) {
+    Frame<double> F = make_frame(mk(double(ox), double(oy), double(oz)), mk(double(dx), double(dy), double(dz)));
+    V3<double> P[4];
+    for (int k = 0; k < 4; ++k) P[k] = mk(double(cp[3 * k]), double(cp[3 * k + 1]), double(cp[3 * k + 2]));
+    PrhiOut<double> r = prhi(F, P, double(r0), double(r1));
+    *s_out = r.status == kHit ? r.s : -1.0;
+    *tc_out = r.tc;
+}
+
+// ---------------------------------------------------------------- LSS (round cone)
+// Envelope of spheres a + u (b-a), radius ra + u (rb-ra): tangent-cone roots with u in [0,1]
+// and both end spheres; the least t >= tmin wins.
+__device__ __forceinline__ float sphere_hit(V3<float> o, V3<float> d, V3<float> c, float r, float tmin, float best) {
+    V3<float> oc = o - c;
+    float A = dot(d, d), B = dot(oc, d), C = dot(oc, oc) - r * r;
+    float h = B * B - A * C;
+    if (h < 0.0f) return best;
+    float sh = sqrtf(h);
+    float t0 = (-B - sh) / A, t1 = (-B + sh) / A;
+    if (t0 >= tmin && t0 < best) return t0;
+    if (t1 >= tmin && t1 < best) return t1;
+    return best;
+}
+__device__ __forceinline__ float lss_hit(V3<float> o, V3<float> d, V3<float> a, V3<float> b, float ra, float rb,
+                                         float tmin, float* u_out) {
+    const float kNone = __int_as_float(0x7f800000);
+    float best = kNone, bu = 0.0f;
+    V3<float> ba = b - a, oa = o - a;
+    float dr = rb - ra;
+    float m = dot(ba, ba) - dr * dr;
+    if (m > 0.0f) {
+        float yd = dot(ba, d);
+        float yo = dot(ba, oa) + ra * dr;
+        float A = m * dot(d, d) - yd * yd;
+        float B = m * dot(oa, d) - yo * yd;
+        float C = m * dot(oa, oa) - yo * yo - m * ra * ra;
+        float h = B * B - A * C;
+        if (h >= 0.0f && A != 0.0f) {
+            float sh = sqrtf(h);
+            float r0 = (-B - sh) / A, r1 = (-B + sh) / A;
+            float lo = gmin(r0, r1), hi = gmax(r0, r1);
+            float u = (yo + lo * yd) / m;
+            if (lo >= tmin && lo < best && u >= 0.0f && u <= 1.0f) { best = lo; bu = u; }
+            else {
+                u = (yo + hi * yd) / m;
+                if (hi >= tmin && hi < best && u >= 0.0f && u <= 1.0f) { best = hi; bu = u; }
+            }
+        }
+    }
+    float ta = sphere_hit(o, d, a, ra, tmin, best);
+    if (ta < best) { best = ta; bu = 0.0f; }
+    float tb = sphere_hit(o, d, b, rb, tmin, best);
+    if (tb < best) { best = tb; bu = 1.0f; }
+    if (best == kNone) return -1.0f;
+    *u_out = bu;
+    return best;
+}
+
+// ---------------------------------------------------------------- triangles (watertight)
+struct TriRay { int kx, ky, kz; float Sx, Sy, Sz; };
+__device__ __forceinline__ TriRay make_triray(V3<float> d) {
+    TriRay r;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    r.kz = 0;
+    if (ay > ax && ay >= az) r.kz = 1;
+    else if (az > ax && az > ay) r.kz = 2;
+    r.kx = r.kz == 2 ? 0 : r.kz + 1;
+    r.ky = r.kx == 2 ? 0 : r.kx + 1;
+    float dk[3] = {d.x, d.y, d.z};
+    if (dk[r.kz] < 0.0f) { int t = r.kx; r.kx = r.ky; r.ky = t; }
+    r.Sx = dk[r.kx] / dk[r.kz];
+    r.Sy = dk[r.ky] / dk[r.kz];
+    r.Sz = 1.0f / dk[r.kz];
+    return r;
+}
+__device__ __forceinline__ float comp(V3<float> v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+__device__ __forceinline__ float tri_hit(const TriRay& R, V3<float> o, V3<float> v0, V3<float> v1, V3<float> v2,
+                                         float tmin, float tmax) {
+    V3<float> A = v0 - o, B = v1 - o, C = v2 - o;
+    float Akz = comp(A, R.kz), Bkz = comp(B, R.kz), Ckz = comp(C, R.kz);
+    float Ax = comp(A, R.kx) - R.Sx * Akz, Ay = comp(A, R.ky) - R.Sy * Akz;
+    float Bx = comp(B, R.kx) - R.Sx * Bkz, By = comp(B, R.ky) - R.Sy * Bkz;
+    float Cx = comp(C, R.kx) - R.Sx * Ckz, Cy = comp(C, R.ky) - R.Sy * Ckz;
+    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return -1.0f;
+    float det = U + V + W;
+    if (det == 0.0f) return -1.0f;
+    float Tn = U * (R.Sz * Akz) + V * (R.Sz * Bkz) + W * (R.Sz * Ckz);
+    float t = Tn / det;
+    if (!(t >= tmin) || !(t <= tmax)) return -1.0f;
+    return t;
+}
+
+// ---------------------------------------------------------------- hit state
+struct Hit {
+    float t;
+    uint32_t id;    // reported primitive id
+    uint32_t inst;
+    uint32_t slot;  // leaf slot of the hit segment
+    float u;        // curve / segment parameter
+    uint32_t flags; // HRT_HIT_FP64
+};
+__device__ __forceinline__ bool beats(float t, uint32_t inst, uint32_t id, const Hit& h) {
+    if (t < h.t) return true;
+    if (t > h.t) return false;
+    return inst < h.inst || (inst == h.inst && id < h.id);
+}
+
+struct RayState {
+    V3<float> o, d, inv;
+    float tmin;
+    Frame<float> F;   // Phantom ray-centric frame
+    TriRay tr;
+};
+
+struct Stats { uint32_t nodes, prims, r64, h64; };
+
+// ---------------------------------------------------------------- leaves
+__device__ __forceinline__ void load_phantom(const DevBlas& B, uint32_t slot, V3<float>* P, float* r0, float* r1,
+                                             uint32_t* id) {
+    if (B.precision == HRT_PRECISION_QUANTISED) {
+        const PrimPhantomH* pr = static_cast<const PrimPhantomH*>(B.prims) + slot;
+        uint4 q0 = __ldg(&pr->q0), q1 = __ldg(&pr->q1);
+        uint32_t key = q1.w;
+        float4 rt = __ldg(&B.roots[key >> 8]);
+        uint32_t w[7] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z};
+        float h[14];
+#pragma unroll
+        for (int j = 0; j < 7; ++j) {
+            __half2 hh = *reinterpret_cast<const __half2*>(&w[j]);
+            float2 f = __half22float2(hh);
+            h[2 * j] = f.x;
+            h[2 * j + 1] = f.y;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            P[k] = mk(__fadd_rn(rt.x, h[3 * k]), __fadd_rn(rt.y, h[3 * k + 1]), __fadd_rn(rt.z, h[3 * k + 2]));
+        *r0 = h[12];
+        *r1 = h[13];
+        *id = __float_as_uint(rt.w) + (key & 0xffu);
+    } else {
+        const PrimPhantomF* pr = static_cast<const PrimPhantomF*>(B.prims) + slot;
+        float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c), d = __ldg(&pr->d);
+        P[0] = mk(a.x, a.y, a.z);
+        P[1] = mk(b.x, b.y, b.z);
+        P[2] = mk(c.x, c.y, c.z);
+        P[3] = mk(d.x, d.y, d.z);
+        *r0 = a.w;
+        *r1 = b.w;
+        *id = __float_as_uint(c.w);
+    }
+}
+
+// Tests one leaf slot; returns true if it produced an accepted hit.
+__device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint32_t inst, const RayState& R, Hit& h,
+                                          bool fp64_resolve, Stats& st) {
+    if (B.type == HRT_BLAS_PHANTOM) {
+        V3<float> P[4];
+        float r0, r1;
+        uint32_t id;
+        load_phantom(B, slot, P, &r0, &r1, &id);
+        PrhiOut<float> r = prhi(R.F, P, r0, r1);
+        if (r.status == kHit) {
+            if (r.s >= R.tmin && beats(r.s, inst, id, h)) {
+                h = Hit{r.s, id, inst, slot, r.tc, 0u};
+                return true;
+            }
+        } else if (r.status == kUnresolved && fp64_resolve) {
+            float cp[12];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { cp[3 * k] = P[k].x; cp[3 * k + 1] = P[k].y; cp[3 * k + 2] = P[k].z; }
+            double s64, tc64;
+            prhi_fp64(R.o.x, R.o.y, R.o.z, R.d.x, R.d.y, R.d.z, cp, r0, r1, &s64, &tc64);
+            ++st.r64;
+            if (s64 > 0.0) {
+                ++st.h64;
+                float s = float(s64);
+                if (s >= R.tmin && beats(s, inst, id, h)) {
+                    h = Hit{s, id, inst, slot, float(tc64), HRT_HIT_FP64};
+                    return true;
+                }
+            }
+        }
+        return false;
+    }
+    if (B.type == HRT_BLAS_LSS) {
+        const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + slot;
+        float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
+        float u;
+        float t = lss_hit(R.o, R.d, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, R.tmin, &u);
+        if (t >= 0.0f && t <= h.t) {
+            uint32_t id = __ldg(&B.prim_ids[slot]);
+            if (beats(t, inst, id, h)) { h = Hit{t, id, inst, slot, u, 0u}; return true; }
+        }
+        return false;
+    }
+    // DOTS: two orthogonal quads of the segment; triangle k has id 4 * segment + k
+    const PrimDots* pr = static_cast<const PrimDots*>(B.prims) + slot;
+    float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c), d = __ldg(&pr->d), e = __ldg(&pr->e);
+    V3<float> s0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y);
+    V3<float> va[2] = {mk(b.z, b.w, c.x), mk(c.y, c.z, c.w)};
+    V3<float> vb[2] = {mk(d.x, d.y, d.z), mk(d.w, e.x, e.y)};
+    uint32_t seg = __float_as_uint(e.z);
+    bool any = false;
+#pragma unroll
+    for (int face = 0; face < 2; ++face) {
+        V3<float> A0 = s0 + va[face], A1 = e0 - vb[face], A2 = e0 + vb[face];
+        V3<float> B1 = s0 - va[face];
+        // triangle 2 face: (start+v*ra, end-v*rb, end+v*rb); 2 face+1: (start+v*ra, start-v*ra, end-v*rb)
+        float t0 = tri_hit(R.tr, R.o, A0, A1, A2, R.tmin, h.t);
+        if (t0 >= 0.0f) {
+            uint32_t id = 4u * seg + 2u * face;
+            if (beats(t0, inst, id, h)) { h = Hit{t0, id, inst, slot, 0.0f, 0u}; any = true; }
+        }
+        float t1 = tri_hit(R.tr, R.o, A0, B1, A1, R.tmin, h.t);
+        if (t1 >= 0.0f) {
+            uint32_t id = 4u * seg + 2u * face + 1u;
+            if (beats(t1, inst, id, h)) { h = Hit{t1, id, inst, slot, 0.0f, 0u}; any = true; }
+        }
+    }
+    return any;
+}
+
+// ---------------------------------------------------------------- nodes
+__device__ __forceinline__ float bytef(uint32_t w, int k) { return float((w >> (8 * k)) & 0xffu); }
+
+// Child entry distances of one node; returns a bit mask of hit children and fills tn[8].
+template <bool kQuant>
+__device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, const RayState& R, float tfar,
+                                              float* tn, uint32_t* base, uint32_t* pbase, uint32_t* m0, uint32_t* m1) {
+    uint32_t mask = 0;
+    const float kEps = 1.0f + 9.5367431640625e-07f;  // 1 + 2^-20: rounding can only admit more boxes
+    if (!kQuant) {
+        const float4* p = reinterpret_cast<const float4*>(static_cast<const NodeF*>(nodes) + ni);
+        float4 L[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) L[k] = __ldg(p + k);
+        float4 tail = __ldg(p + 12);
+        *base = __float_as_uint(tail.x);
+        *pbase = __float_as_uint(tail.y);
+        *m0 = __float_as_uint(tail.z);
+        *m1 = __float_as_uint(tail.w);
+        const float* f = reinterpret_cast<const float*>(L);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            float x0 = (f[q] - R.o.x) * R.inv.x, x1 = (f[8 + q] - R.o.x) * R.inv.x;
+            float y0 = (f[16 + q] - R.o.y) * R.inv.y, y1 = (f[24 + q] - R.o.y) * R.inv.y;
+            float z0 = (f[32 + q] - R.o.z) * R.inv.z, z1 = (f[40 + q] - R.o.z) * R.inv.z;
+            float a = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), R.tmin));
+            float b = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tfar));
+            tn[q] = a;
+            if (a <= b * kEps) mask |= 1u << q;
+        }
+    } else {
+        const uint4* p = reinterpret_cast<const uint4*>(static_cast<const NodeQ*>(nodes) + ni);
+        uint4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
+        float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+        float sx = __uint_as_float((w0.w & 0xffu) << 23);
+        float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+        float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+        *base = w1.x;
+        *pbase = w1.y;
+        *m0 = w1.z;
+        *m1 = w1.w;
+        uint32_t qlx[2] = {w2.x, w2.y}, qhx[2] = {w2.z, w2.w};
+        uint32_t qly[2] = {w3.x, w3.y}, qhy[2] = {w3.z, w3.w};
+        uint32_t qlz[2] = {w4.x, w4.y}, qhz[2] = {w4.z, w4.w};
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            int wd = q >> 2, by = q & 3;
+            float lx = fmaf(bytef(qlx[wd], by), sx, px), hx = fmaf(bytef(qhx[wd], by), sx, px);
+            float ly = fmaf(bytef(qly[wd], by), sy, py), hy = fmaf(bytef(qhy[wd], by), sy, py);
+            float lz = fmaf(bytef(qlz[wd], by), sz, pz), hz = fmaf(bytef(qhz[wd], by), sz, pz);
+            float x0 = (lx - R.o.x) * R.inv.x, x1 = (hx - R.o.x) * R.inv.x;
+            float y0 = (ly - R.o.y) * R.inv.y, y1 = (hy - R.o.y) * R.inv.y;
+            float z0 = (lz - R.o.z) * R.inv.z, z1 = (hz - R.o.z) * R.inv.z;
+            float a = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), R.tmin));
+            float b = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tfar));
+            tn[q] = a;
+            if (a <= b * kEps) mask |= 1u << q;
+        }
+    }
+    // empty slots never count
+    uint32_t valid = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        uint32_t m = ((q < 4 ? *m0 : *m1) >> (8 * (q & 3))) & 0xffu;
+        valid |= (m ? 1u : 0u) << q;
+    }
+    return mask & valid;
+}
+
+__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
+    uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
+// Traverses one BLAS. any_hit: stop at the first accepted hit (shadow rays), skipping slot
+// `skip_slot` of instance `skip_inst`.
+template <bool kQuant>
+__device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit& h, bool any_hit, uint32_t skip_inst,
+                         uint32_t skip_slot, bool fp64_resolve, Stats& st, uint32_t& err) {
+    if (B.nnodes == 0) return false;
+    uint2 stack[kStackSize];
+    int sp = 0;
+    stack[sp++] = make_uint2(0u, __float_as_uint(R.tmin));
+    bool found = false;
+    uint32_t steps = 0;
+    while (sp > 0) {
+        if (++steps > kMaxTraversalSteps) { err |= kErrTimeout; break; }
+        uint2 e = stack[--sp];
+        if (__uint_as_float(e.y) > h.t) continue;
+        if (e.x & kLeafFlag) {
+            uint32_t first = (e.x & ~kLeafFlag) >> 2, cnt = (e.x & 3u) + 1u;
+            for (uint32_t j = 0; j < cnt; ++j) {
+                uint32_t slot = first + j;
+                if (any_hit && inst == skip_inst && slot == skip_slot) continue;
+                ++st.prims;
+                if (leaf_test(B, slot, inst, R, h, fp64_resolve, st)) {
+                    found = true;
+                    if (any_hit) return true;
+                }
+            }
+            continue;
+        }
+        ++st.nodes;
+        float tn[8];
+        uint32_t base, pbase, m0, m1;
+        uint32_t mask = test_node<kQuant>(B.nodes, e.x, R, h.t, tn, &base, &pbase, &m0, &m1);
+        if (!mask) continue;
+        uint32_t key[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            key[q] = (mask >> q) & 1u ? ((__float_as_uint(fmaxf(tn[q], 0.0f)) & ~7u) | uint32_t(q)) : 0xffffffffu;
+        // 19-comparator sorting network for 8 keys (ascending)
+        cswap(key[0], key[2]); cswap(key[1], key[3]); cswap(key[4], key[6]); cswap(key[5], key[7]);
+        cswap(key[0], key[4]); cswap(key[1], key[5]); cswap(key[2], key[6]); cswap(key[3], key[7]);
+        cswap(key[0], key[1]); cswap(key[2], key[3]); cswap(key[4], key[5]); cswap(key[6], key[7]);
+        cswap(key[2], key[4]); cswap(key[3], key[5]);
+        cswap(key[1], key[4]); cswap(key[3], key[6]);
+        cswap(key[1], key[2]); cswap(key[3], key[4]); cswap(key[5], key[6]);
+        int npush = __popc(mask);
+        if (sp + npush > kStackSize) { err |= kErrStackOverflow; break; }
+#pragma unroll
+        for (int k = 7; k >= 0; --k) {
+            if (k >= npush) continue;
+            uint32_t q = key[k] & 7u;
+            uint32_t m = ((q < 4 ? m0 : m1) >> (8 * (q & 3))) & 0xffu;
+            uint32_t ref = (m & 0x80u) ? base + (m & 7u)
+                                       : (kLeafFlag | ((pbase + (m & 31u)) << 2) | ((m >> 5) - 1u));
+            stack[sp++] = make_uint2(ref, key[k] & ~7u);
+        }
+    }
+    return found;
+}
+
+// World-space ray through every instance of a scene.
+template <bool kQuant>
+__device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> wo, V3<float> wd, float tmin, float tmax,
+                            Hit& h, bool any_hit, uint32_t skip_inst, uint32_t skip_slot, bool fp64_resolve, Stats& st,
+                            uint32_t& err) {
+    h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0u};
+    bool found = false;
+    for (uint32_t i = 0; i < ninst; ++i) {
+        const DevInstance& I = insts[i];
+        RayState R;
+        if (I.identity) { R.o = wo; R.d = wd; }
+        else {
+            const float* m = I.w2o;
+            R.o = mk(m[0] * wo.x + m[1] * wo.y + m[2] * wo.z + m[3], m[4] * wo.x + m[5] * wo.y + m[6] * wo.z + m[7],
+                     m[8] * wo.x + m[9] * wo.y + m[10] * wo.z + m[11]);
+            R.d = mk(m[0] * wd.x + m[1] * wd.y + m[2] * wd.z, m[4] * wd.x + m[5] * wd.y + m[6] * wd.z,
+                     m[8] * wd.x + m[9] * wd.y + m[10] * wd.z);
+        }
+        R.inv = mk(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
+        R.tmin = tmin;
+        // instance bounds (object space) against the current closest distance
+        {
+            const DevBlas& B = I.b;
+            float x0 = (B.lo[0] - R.o.x) * R.inv.x, x1 = (B.hi[0] - R.o.x) * R.inv.x;
+            float y0 = (B.lo[1] - R.o.y) * R.inv.y, y1 = (B.hi[1] - R.o.y) * R.inv.y;
+            float z0 = (B.lo[2] - R.o.z) * R.inv.z, z1 = (B.hi[2] - R.o.z) * R.inv.z;
+            float a = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
+            float b = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), h.t));
+            if (!(a <= b * (1.0f + 9.5367431640625e-07f))) continue;
+        }
+        if (I.b.type == HRT_BLAS_PHANTOM) R.F = make_frame(R.o, R.d);
+        else if (I.b.type == HRT_BLAS_DOTS) R.tr = make_triray(R.d);
+        if (traverse<kQuant>(I.b, i, R, h, any_hit, skip_inst, skip_slot, fp64_resolve, st, err)) {
+            found = true;
+            if (any_hit) return true;
+        }
+    }
+    return found;
+}
+
+// Object-space normal of the final hit (closest-hit stage).
+__device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo, V3<float> wd) {
+    const DevBlas& B = I.b;
+    V3<float> o = wo, d = wd;
+    if (!I.identity) {
+        const float* m = I.w2o;
+        o = mk(m[0] * wo.x + m[1] * wo.y + m[2] * wo.z + m[3], m[4] * wo.x + m[5] * wo.y + m[6] * wo.z + m[7],
+               m[8] * wo.x + m[9] * wo.y + m[10] * wo.z + m[11]);
+        d = mk(m[0] * wd.x + m[1] * wd.y + m[2] * wd.z, m[4] * wd.x + m[5] * wd.y + m[6] * wd.z,
+               m[8] * wd.x + m[9] * wd.y + m[10] * wd.z);
+    }
+    V3<float> n;
+    V3<float> hp = o + h.t * d;
+    if (B.type == HRT_BLAS_PHANTOM) {
+        // hair_intersection.rint:74-76: normalize(hit - curve(t))
+        V3<float> P[4];
+        float r0, r1;
+        uint32_t id;
+        load_phantom(B, h.slot, P, &r0, &r1, &id);
+        n = normalize(hp - bez_point(P, h.u));
+    } else if (B.type == HRT_BLAS_LSS) {
+        // triangle_closest_hit.rchit:43-58: hit - mix(p0, p1, u)
+        const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + h.slot;
+        float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
+        V3<float> p0 = mk(a.x, a.y, a.z), p1 = mk(b.x, b.y, b.z);
+        n = normalize(hp - (p0 + h.u * (p1 - p0)));
+    } else {
+        // DOTS vertices carry no normals (geometry_processor.cpp:259-264): the face normal
+        const PrimDots* pr = static_cast<const PrimDots*>(B.prims) + h.slot;
+        float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c), dd = __ldg(&pr->d), e = __ldg(&pr->e);
+        V3<float> s0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y);
+        uint32_t k = h.id & 3u, face = k >> 1;
+        V3<float> va = face ? mk(c.y, c.z, c.w) : mk(b.z, b.w, c.x);
+        V3<float> vb = face ? mk(dd.w, e.x, e.y) : mk(dd.x, dd.y, dd.z);
+        V3<float> A0 = s0 + va, A1 = e0 - vb;
+        V3<float> third = (k & 1u) ? (s0 - va) : (e0 + vb);
+        V3<float> v1 = (k & 1u) ? third : A1, v2 = (k & 1u) ? A1 : third;
+        n = normalize(cross(v1 - A0, v2 - A0));
+    }
+    if (!I.identity) {
+        const float* q = I.nrm;
+        n = normalize(mk(q[0] * n.x + q[1] * n.y + q[2] * n.z, q[3] * n.x + q[4] * n.y + q[5] * n.z,
+                         q[6] * n.x + q[7] * n.y + q[8] * n.z));
+    }
+    return n;
+}
+
+// ray_gen.rgen:18-24, every operation rounded separately (matches the CPU restatement).
+__device__ void raygen(const float* V, const float* P, uint32_t px, uint32_t py, uint32_t w, uint32_t hgt, float jx,
+                       float jy, V3<float>* o, V3<float>* d) {
+    float cx = __fadd_rn(float(px), jx), cy = __fadd_rn(float(py), jy);
+    float ux = __fdiv_rn(cx, float(w)), uy = __fdiv_rn(cy, float(hgt));
+    float dx = __fsub_rn(__fmul_rn(ux, 2.0f), 1.0f), dy = __fsub_rn(__fmul_rn(uy, 2.0f), 1.0f);
+    float org[3], tgt[3], dir[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        org[k] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(V[k], 0.0f), __fmul_rn(V[4 + k], 0.0f)), __fmul_rn(V[8 + k], 0.0f)),
+                           __fmul_rn(V[12 + k], 1.0f));
+        tgt[k] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(P[k], dx), __fmul_rn(P[4 + k], dy)), __fmul_rn(P[8 + k], 1.0f)),
+                           __fmul_rn(P[12 + k], 1.0f));
+    }
+    float dd = __fadd_rn(__fadd_rn(__fmul_rn(tgt[0], tgt[0]), __fmul_rn(tgt[1], tgt[1])), __fmul_rn(tgt[2], tgt[2]));
+    float inv = __fdiv_rn(1.0f, __fsqrt_rn(dd));
+    float n[3] = {__fmul_rn(tgt[0], inv), __fmul_rn(tgt[1], inv), __fmul_rn(tgt[2], inv)};
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        dir[k] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(V[k], n[0]), __fmul_rn(V[4 + k], n[1])), __fmul_rn(V[8 + k], n[2])),
+                           __fmul_rn(V[12 + k], 0.0f));
+    *o = mk(org[0], org[1], org[2]);
+    *d = mk(dir[0], dir[1], dir[2]);
+}
+
+__device__ __forceinline__ uint32_t hash_u32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+
+__constant__ float kPalette[6][3] = {{1.0f, 0.0f, 0.3f}, {0.8f, 0.2f, 0.3f}, {0.6f, 0.4f, 0.3f},
+                                     {0.4f, 0.6f, 0.3f}, {0.2f, 0.8f, 0.3f}, {0.0f, 1.0f, 0.3f}};
+
+__device__ __forceinline__ void warp_add(unsigned long long* ctr, uint32_t v) {
+    // one atomic per warp
+    uint32_t s = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(ctr, (unsigned long long)s);
+}
+
+template <bool kQuant>
+__global__ void __launch_bounds__(kThreads) trace_kernel(TraceLaunch L) {
+    const int lane = threadIdx.x & 31;
+    Stats st{0, 0, 0, 0};
+    uint32_t shadow_rays = 0;
+    uint32_t err = 0;
+    const volatile uint32_t* errword = &L.counters->error;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = *errword ? L.total_work : atomicAdd(&L.counters->work, 32ull);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= L.total_work) break;
+        uint64_t g = base + lane;
+        // scene of this tile (scenes are few; linear scan)
+        uint32_t si = 0;
+        while (si + 1 < L.nscenes && L.scenes[si + 1].work_begin <= g) ++si;
+        const SceneLaunch& S = L.scenes[si];
+        uint64_t local = g - S.work_begin;
+        uint64_t tile = local >> 5;
+        uint32_t within = uint32_t(local & 31u);
+        uint32_t px = uint32_t(tile % S.tiles_x) * 8u + (within & 7u);
+        uint32_t py = uint32_t(tile / S.tiles_x) * 4u + (within >> 3);
+        if (err && lane == 0) atomicOr(&L.counters->error, err);  // stop every warp early
+        if (px >= S.width || py >= S.height || err) continue;
+        uint64_t pix = uint64_t(py) * S.width + px;
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        for (uint32_t k = 0; k < S.spp; ++k) {
+            float jx = 0.5f, jy = 0.5f;
+            if (L.jitter || S.spp > 1) {
+                uint32_t h1 = hash_u32(L.seed ^ hash_u32(uint32_t(pix) * S.spp + k));
+                uint32_t h2 = hash_u32(h1);
+                jx = float(h1 >> 8) * 5.9604644775390625e-08f;
+                jy = float(h2 >> 8) * 5.9604644775390625e-08f;
+            }
+            V3<float> o, d;
+            raygen(S.view_inv, S.proj_inv, px, py, S.width, S.height, jx, jy, &o, &d);
+            Hit h;
+            bool found = trace_scene<kQuant>(S.inst, S.ninst, o, d, L.tmin, L.tmax, h, false, 0, 0, L.fp64_resolve != 0,
+                                             st, err);
+            float col[3] = {0.0f, 0.0f, 0.0f};
+            uint32_t flags = h.flags;
+            if (found) {
+                if (L.shading == HRT_SHADE_DEBUG) {
+                    uint32_t c = h.id % 6u;
+                    col[0] = kPalette[c][0]; col[1] = kPalette[c][1]; col[2] = kPalette[c][2];
+                } else {
+                    V3<float> n = hit_normal(S.inst[h.inst], h, o, d);
+                    bool lit = true;
+                    if (L.shading == HRT_SHADE_LAMBERT_SHADOW) {
+                        V3<float> hp = o + h.t * d;
+                        Hit hs;
+                        ++shadow_rays;
+                        lit = !trace_scene<kQuant>(S.inst, S.ninst, hp, mk(0.0f, 1.0f, 0.0f), L.shadow_tmin, L.tmax, hs,
+                                                   true, h.inst, h.slot, L.fp64_resolve != 0, st, err);
+                        if (!lit) flags |= HRT_HIT_SHADOWED;
+                    }
+                    // shading.glsl:1-10 with light direction (0,-1,0): |dot(n, L)| = |n.y|
+                    float ndl = lit ? fabsf(n.y) : 0.0f;
+                    col[0] = ndl * 0.4f + 0.3f;
+                    col[1] = ndl * 0.2f + 0.3f;
+                    col[2] = ndl * 0.1f + 0.3f;
+                }
+            }
+            acc[0] += col[0]; acc[1] += col[1]; acc[2] += col[2];
+            if (L.record_hits && S.hits) {
+                hrt_hit r;
+                r.t = found ? h.t : -1.0f;
+                r.prim = found ? h.id : 0xffffffffu;
+                r.inst = found ? h.inst : 0xffffffffu;
+                r.flags = found ? flags : 0u;
+                S.hits[pix * S.spp + k] = r;
+            }
+        }
+        float inv = 1.0f / float(S.spp);
+        S.fb[pix] = make_float4(acc[0] * inv, acc[1] * inv, acc[2] * inv, 1.0f);
+    }
+    warp_add(&L.counters->shadow, shadow_rays);
+    if (L.count_stats) {
+        warp_add(&L.counters->nodes, st.nodes);
+        warp_add(&L.counters->prims, st.prims);
+    }
+    warp_add(&L.counters->fp64_resolves, st.r64);
+    warp_add(&L.counters->fp64_hits, st.h64);
+    if (err) atomicOr(&L.counters->error, err);
+}
+
+template <bool kQuant>
+__global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance* inst, uint32_t ninst, const float* rays,
+                                                              uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
+                                                              hrt_hit* hits, TraceCounters* ctr) {
+    Stats st{0, 0, 0, 0};
+    uint32_t err = 0;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
+        const float* r = rays + 6 * i;
+        Hit h;
+        bool f = trace_scene<kQuant>(inst, ninst, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), tmin, tmax, h, false, 0, 0,
+                                     fp64_resolve != 0, st, err);
+        hrt_hit o;
+        o.t = f ? h.t : -1.0f;
+        o.prim = f ? h.id : 0xffffffffu;
+        o.inst = f ? h.inst : 0xffffffffu;
+        o.flags = f ? h.flags : 0u;
+        hits[i] = o;
+    }
+    warp_add(&ctr->fp64_resolves, st.r64);
+    warp_add(&ctr->fp64_hits, st.h64);
+    if (err) atomicOr(&ctr->error, err);
+}
+
+}  // namespace
+
+cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count) {
+    int per_sm = 0;
+    cudaError_t e = quantised_nodes
+                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<true>, kThreads, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<false>, kThreads, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    unsigned grid = unsigned(sm_count * per_sm);
+    uint64_t max_blocks = (L.total_work + kThreads - 1) / kThreads;
+    if (grid > max_blocks) grid = unsigned(max_blocks ? max_blocks : 1);
+    if (quantised_nodes) trace_kernel<true><<<grid, kThreads, 0, s>>>(L);
+    else trace_kernel<false><<<grid, kThreads, 0, s>>>(L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n, float tmin,
+                              float tmax, uint32_t fp64_resolve, hrt_hit* hits, TraceCounters* counters,
+                              bool quantised_nodes, cudaStream_t s, int sm_count) {
+    if (n == 0) return cudaSuccess;
+    uint64_t blocks = (n + kThreads - 1) / kThreads;
+    unsigned grid = unsigned(blocks < uint64_t(sm_count) * 16 ? blocks : uint64_t(sm_count) * 16);
+    if (quantised_nodes)
+        trace_rays_kernel<true><<<grid, kThreads, 0, s>>>(inst, ninst, rays, n, tmin, tmax, fp64_resolve, hits, counters);
+    else
+        trace_rays_kernel<false><<<grid, kThreads, 0, s>>>(inst, ninst, rays, n, tmin, tmax, fp64_resolve, hits, counters);
+    return cudaGetLastError();
+}
+
+}  // namespace hrt
