@@ -146,11 +146,23 @@ static const float kPalette[6][3] = {{1.0f, 0.0f, 0.3f}, {0.8f, 0.2f, 0.3f}, {0.
 // r0 + (r1 - r0) t along the segment (taper), which is exactly the constant when r0 == r1;
 // the bounding-cylinder pad is max(r0, r1).
 // status: 0 miss, 1 hit, 2 unresolved (a side used all 8 iterations inside [0,1]).
+// shift: evaluate from the ray point nearest the chord midpoint instead of the ray origin
+// (the bounding-cylinder test is on the infinite line and the cone step is translation
+// invariant along the ray, so the result is the same in exact arithmetic; in FP32 this removes
+// the cancellation of the world-space test, hair_intersection.rint:29). The reference-literal
+// form is shift = false.
 enum { kMiss = 0, kHit = 1, kUnresolved = 2 };
 template <class T>
-T prhi(const Ray<T>& ray, const Curve<T>& curve, T r0, T r1, tvec3<T>* normal, int* status) {
+T prhi(const Ray<T>& ray_in, const Curve<T>& curve, T r0, T r1, tvec3<T>* normal, int* status, bool shift = false) {
     T result = T(0);
     *status = kMiss;
+    Ray<T> ray = ray_in;
+    T tshift = T(0);
+    if (shift) {
+        tvec3<T> mid = (curve.start + curve.end) * T(0.5);
+        tshift = shim::dot(mid - ray_in.origin, ray_in.direction) / shim::dot(ray_in.direction, ray_in.direction);
+        ray.origin = ray_in.origin + tshift * ray_in.direction;
+    }
     T rmax = curve_distance_to_cylinder(curve, sample_point(curve, T(0.5)));
     rmax += gmax(r0, r1);
     Cylinder<T> cyl{curve.start, curve.end, rmax};
@@ -175,8 +187,8 @@ T prhi(const Ray<T>& ray, const Curve<T>& curve, T r0, T r1, tvec3<T>* normal, i
             ConeHit<T> rci = ray_cone_rcc(cone);
             if (rci.isIntersection && gabs(rci.dt) < T(5e-5)) {
                 rci.s += cone.center.z;
-                result = rci.s;
-                tvec3<T> hitPosition = ray.origin + result * ray.direction;
+                result = rci.s + tshift;
+                tvec3<T> hitPosition = ray_in.origin + result * ray_in.direction;
                 tvec3<T> curvePosition = sample_point(curve, t);
                 if (normal) *normal = shim::normalize(hitPosition - curvePosition);
                 exhausted = false;
@@ -228,9 +240,14 @@ template <class T> T sphere_roots(tvec3<T> o, tvec3<T> d, tvec3<T> c, T r, T tmi
     if (t1 >= tmin && t1 < best) return t1;
     return best;
 }
+// Solved from the ray point nearest the segment midpoint (t = tshift + t'), so the quadratic's
+// terms are of the segment's size rather than the camera distance.
 template <class T>
-T lss_intersect(tvec3<T> o, tvec3<T> d, tvec3<T> a, tvec3<T> b, T ra, T rb, T tmin, T* u_out) {
+T lss_intersect(tvec3<T> o_in, tvec3<T> d, tvec3<T> a, tvec3<T> b, T ra, T rb, T tmin_in, T* u_out) {
     const T kNone = T(INFINITY);
+    T tshift = shim::dot((a + b) * T(0.5) - o_in, d) / shim::dot(d, d);
+    tvec3<T> o = o_in + tshift * d;
+    T tmin = tmin_in - tshift;
     T best = kNone, bu = T(0);
     tvec3<T> ba = b - a;
     tvec3<T> oa = o - a;
@@ -262,7 +279,7 @@ T lss_intersect(tvec3<T> o, tvec3<T> d, tvec3<T> a, tvec3<T> b, T ra, T rb, T tm
     if (tb < best) { best = tb; bu = T(1); }
     if (best == kNone) return T(-1);
     *u_out = bu;
-    return best;
+    return best + tshift;
 }
 
 // ---- watertight ray/triangle (Woop, Benthin and Wald, JCGT 2013) --------------------------
@@ -757,15 +774,16 @@ static bool intersect_prim(const Blas& b, uint32_t inst, uint32_t s, const tvec3
         Ray<T> ray{o, d};
         int st;
         tvec3<T> nrm;
-        T t = prhi(ray, cv, T(b.radius[2 * s]), T(b.radius[2 * s + 1]), &nrm, &st);
+        bool shift = (resolve64 & 2) != 0;
+        T t = prhi(ray, cv, T(b.radius[2 * s]), T(b.radius[2 * s + 1]), &nrm, &st, shift);
         if (st == kHit) { take(t, s, T(0), 0); if (better) h->n = nrm; }
-        else if (st == kUnresolved && resolve64) {
+        else if (st == kUnresolved && (resolve64 & 1)) {
             Curve<double> cd{tvec3<double>(c[0], c[1], c[2]), tvec3<double>(c[3], c[4], c[5]),
                              tvec3<double>(c[6], c[7], c[8]), tvec3<double>(c[9], c[10], c[11])};
             Ray<double> rd{tvec3<double>(o.x, o.y, o.z), tvec3<double>(d.x, d.y, d.z)};
             int st2;
             tvec3<double> n2;
-            double t2 = prhi(rd, cd, double(b.radius[2 * s]), double(b.radius[2 * s + 1]), &n2, &st2);
+            double t2 = prhi(rd, cd, double(b.radius[2 * s]), double(b.radius[2 * s + 1]), &n2, &st2, shift);
             if (st2 == kHit) {
                 take(T(t2), s, T(0), 1);
                 if (better) h->n = tvec3<T>(T(n2.x), T(n2.y), T(n2.z));
@@ -868,6 +886,11 @@ static bool trace_one(const Scene& sc, const tvec3<T>& wo, const tvec3<T>& wd, T
 using namespace orc;
 
 namespace {
+// FP32 variants: 32 the reference-literal algorithm, 3264 with FP64 re-solve of unresolved
+// Phantom candidates, 33 / 3364 the same evaluated from the shifted origin (see prhi).
+int fp32_mode(int precision) {
+    return (precision == 3264 || precision == 3364 ? 1 : 0) | (precision == 33 || precision == 3364 ? 2 : 0);
+}
 template <class F> void parallel_for(int64_t n, int nthreads, F f) {
     if (nthreads <= 1 || n < 256) { for (int64_t i = 0; i < n; ++i) f(i); return; }
     std::atomic<int64_t> next{0};
@@ -1121,7 +1144,7 @@ void orc_trace_rays(void* s, const float* rays, int64_t n, float tmin, float tma
         } else {
             HitT<float> h;
             bool f = trace_one<float>(sc, v3f(r[0], r[1], r[2]), v3f(r[3], r[4], r[5]), tmin, tmax, false, 0, 0,
-                                      precision == 3264 ? 1 : 0, &h);
+                                      fp32_mode(precision), &h);
             t_out[i] = f ? double(h.t) : -1.0;
             prim_out[i] = f ? h.prim : 0xffffffffu;
             inst_out[i] = f ? h.inst : 0xffffffffu;
@@ -1189,7 +1212,7 @@ void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t 
             } else {
                 HitT<float> hh;
                 v3f od(o[0], o[1], o[2]), dd(d[0], d[1], d[2]);
-                found = trace_one<float>(sc, od, dd, tmin, tmax, false, 0, 0, precision == 3264 ? 1 : 0, &hh);
+                found = trace_one<float>(sc, od, dd, tmin, tmax, false, 0, 0, fp32_mode(precision), &hh);
                 t_out[si] = found ? double(hh.t) : -1.0;
                 prim_out[si] = found ? hh.prim : 0xffffffffu;
                 inst_out[si] = found ? hh.inst : 0xffffffffu;
@@ -1202,7 +1225,7 @@ void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t 
                             v3f hp = od + hh.t * dd;
                             HitT<float> sh2;
                             lit = !trace_one<float>(sc, hp, v3f(0.f, 1.f, 0.f), shadow_tmin, tmax, true, hh.inst, hh.seg,
-                                                    precision == 3264 ? 1 : 0, &sh2);
+                                                    fp32_mode(precision), &sh2);
                         }
                         sh = lit ? 0 : 1;
                         v3f c3 = lit ? shade(hh.n) : v3f(0.3f, 0.3f, 0.3f);

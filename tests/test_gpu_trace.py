@@ -50,11 +50,12 @@ def test_trace_rays_vs_fp64_oracle(ctx, orc, gtype, precision):
 
 
 def test_trace_rays_fp32_resolve_off_vs_fp32_oracle(ctx, orc):
-    """Without the FP64 re-solve the GPU's FP32 Phantom is the oracle's FP32 algorithm."""
+    """Without the FP64 re-solve the GPU's FP32 Phantom is the oracle's FP32 algorithm evaluated
+    from the shifted origin (oracle mode 33)."""
     blas, tlas, osc, lines = make_scene(ctx, orc, PHANTOM, 0, seed=22)
     rays = aimed_rays(np.random.default_rng(5), lines, 20000, spread=0.006)
     g = H.trace_rays(ctx, tlas, rays, H.trace_params(fp64_resolve=0))
-    o_t, o_prim, o_inst, _ = osc.trace_rays(rays, precision=32)
+    o_t, o_prim, o_inst, _ = osc.trace_rays(rays, precision=33)
     g_t = np.where(g["t"] >= 0, g["t"].astype(np.float64), -1.0)
     st = compare_hits(g_t, g["prim"], g["inst"], o_t, o_prim, o_inst)
     assert st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL

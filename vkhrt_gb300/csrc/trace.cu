@@ -74,11 +74,12 @@ template <class T> struct PrhiOut { T s; T tc; int status; };
 
 // ray.glsl:13-17 MakeOrthonormalBasis; the RCC transform (ray.glsl:19-33) is the inverse of
 // [e1 e2 e3 | o], applied here as the transpose of the orthonormal frame after the translation.
-template <class T> struct Frame { V3<T> o, d, e1, e2, e3; };
+template <class T> struct Frame { V3<T> o, d, e1, e2, e3; T inv_dd; };
 template <class T> __device__ __forceinline__ Frame<T> make_frame(V3<T> o, V3<T> d) {
     Frame<T> f;
     f.o = o;
     f.d = d;
+    f.inv_dd = T(1) / dot(d, d);
     f.e3 = normalize(d);
     V3<T> w = f.e3;
     f.e2 = gabs(w.x) > gabs(w.y) ? normalize(mk(-w.z, T(0), w.x)) : normalize(mk(T(0), w.z, -w.y));
@@ -88,16 +89,23 @@ template <class T> __device__ __forceinline__ Frame<T> make_frame(V3<T> o, V3<T>
 
 // hair_intersection.rint:15-130 with the cone radius r0 + (r1 - r0) t (constant when equal).
 // status kUnresolved: no hit and some side used all 8 iterations inside [0, 1].
+// The bounding-cylinder test (on the infinite line) and the ray-centric transform are taken
+// from the ray point nearest the chord midpoint, o' = o + ts d, and ts is added back to the
+// distance: the same result in exact arithmetic, without the FP32 cancellation of a world-space
+// test from a distant origin (hair_intersection.rint:29).
 template <class T>
 __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T r0, T r1) {
     PrhiOut<T> out{T(0), T(0), kMiss};
+    V3<T> cm = T(0.5) * (P[0] + P[3]);
+    T ts = dot(cm - F.o, F.d) * F.inv_dd;
+    V3<T> o = F.o + ts * F.d;
     V3<T> mid = bez_point(P, T(0.5));
     T rmax = length(cross(mid - P[0], mid - P[3])) / length(P[3] - P[0]) + gmax(r0, r1);
-    if (!ray_cylinder(F.o, F.d, P[0], P[3], rmax)) return out;
+    if (!ray_cylinder(o, F.d, P[0], P[3], rmax)) return out;
     V3<T> Q[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        V3<T> w = P[k] - F.o;
+        V3<T> w = P[k] - o;
         Q[k] = mk(dot(F.e1, w), dot(F.e2, w), dot(F.e3, w));
     }
     T tStart = (Q[3].z - Q[0].z) > T(0) ? T(0) : T(1);
@@ -124,7 +132,7 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T 
             T s = (b - (isect ? sqrt(det) : T(0))) / cc;
             T dt = (s * ax.z - cdd) / ddd;
             if (isect && gabs(dt) < T(5e-5)) {
-                out.s = s + c.z;
+                out.s = (s + c.z) + ts;
                 out.tc = t;
                 exhausted = false;
                 break;
@@ -176,9 +184,13 @@ __device__ __forceinline__ float sphere_hit(V3<float> o, V3<float> d, V3<float> 
     if (t1 >= tmin && t1 < best) return t1;
     return best;
 }
-__device__ __forceinline__ float lss_hit(V3<float> o, V3<float> d, V3<float> a, V3<float> b, float ra, float rb,
-                                         float tmin, float* u_out) {
+// Solved from the ray point nearest the segment midpoint (t = ts + t').
+__device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> a, V3<float> b, float ra, float rb,
+                                         float tmin_in, float* u_out) {
     const float kNone = __int_as_float(0x7f800000);
+    float ts = dot(0.5f * (a + b) - o_in, d) / dot(d, d);
+    V3<float> o = o_in + ts * d;
+    float tmin = tmin_in - ts;
     float best = kNone, bu = 0.0f;
     V3<float> ba = b - a, oa = o - a;
     float dr = rb - ra;
@@ -208,7 +220,7 @@ __device__ __forceinline__ float lss_hit(V3<float> o, V3<float> d, V3<float> a, 
     if (tb < best) { best = tb; bu = 1.0f; }
     if (best == kNone) return -1.0f;
     *u_out = bu;
-    return best;
+    return best + ts;
 }
 
 // ---------------------------------------------------------------- triangles (watertight)
