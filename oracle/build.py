@@ -82,6 +82,7 @@ def load() -> ctypes.CDLL:
         "orc_render": (None, [P, P, P, u32, u32, u32, i32, u32, f32, f32, i32, f32, i32, i32, i64, i64,
                               P, P, P, P, P, P]),
         "orc_hardware_threads": (i32, []),
+        "orc_resolve_stats": (None, [P, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

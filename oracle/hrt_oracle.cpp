@@ -145,39 +145,54 @@ static const float kPalette[6][3] = {{1.0f, 0.0f, 0.3f}, {0.8f, 0.2f, 0.3f}, {0.
 // Radius: the reference hard-codes 0.02 (hair_intersection.rint:18). Here the cone radius is
 // r0 + (r1 - r0) t along the segment (taper), which is exactly the constant when r0 == r1;
 // the bounding-cylinder pad is max(r0, r1).
-// status: 0 miss, 1 hit, 2 unresolved (a side used all 8 iterations inside [0,1]).
+// status: 0 miss, 1 hit, 2 unresolved (a side used all 8 iterations inside [0,1]), 3 unresolved
+// with a real cone intersection at the last step of such a side (the run had not converged).
 // shift: evaluate from the ray point nearest the chord midpoint instead of the ray origin
 // (the bounding-cylinder test is on the infinite line and the cone step is translation
 // invariant along the ray, so the result is the same in exact arithmetic; in FP32 this removes
 // the cancellation of the world-space test, hair_intersection.rint:29). The reference-literal
 // form is shift = false.
-enum { kMiss = 0, kHit = 1, kUnresolved = 2 };
+enum { kMiss = 0, kHit = 1, kUnresolved = 2, kUnresolvedNear = 3 };
 template <class T>
-T prhi(const Ray<T>& ray_in, const Curve<T>& curve, T r0, T r1, tvec3<T>* normal, int* status, bool shift = false) {
+T prhi(const Ray<T>& ray_in, const Curve<T>& curve, T r0, T r1, tvec3<T>* normal, int* status, bool shift = false,
+       bool polish = false) {
     T result = T(0);
     *status = kMiss;
     Ray<T> ray = ray_in;
     T tshift = T(0);
+    Curve<T> local = curve;  // the curve in the coordinates the solve runs in
     if (shift) {
+        // o' = o + tshift d is never rounded: each P - o' is P - o exactly (TwoSum) minus
+        // tshift d in one fused operation, so the relative vectors keep full precision.
         tvec3<T> mid = (curve.start + curve.end) * T(0.5);
         tshift = shim::dot(mid - ray_in.origin, ray_in.direction) / shim::dot(ray_in.direction, ray_in.direction);
-        ray.origin = ray_in.origin + tshift * ray_in.direction;
+        auto rel = [&](const tvec3<T>& p) {
+            tvec3<T> r;
+            for (int k = 0; k < 3; ++k) {
+                T a = p[k], c = -ray_in.origin[k];
+                T sum = a + c, cc = sum - a, err = (a - (sum - cc)) + (c - cc);
+                r[k] = std::fma(-tshift, ray_in.direction[k], sum) + err;
+            }
+            return r;
+        };
+        local = Curve<T>{rel(curve.start), rel(curve.cp1), rel(curve.cp2), rel(curve.end)};
+        ray.origin = tvec3<T>(T(0), T(0), T(0));
     }
     T rmax = curve_distance_to_cylinder(curve, sample_point(curve, T(0.5)));
     rmax += gmax(r0, r1);
-    Cylinder<T> cyl{curve.start, curve.end, rmax};
+    Cylinder<T> cyl{local.start, local.end, rmax};
     if (!ray_cylinder(ray, cyl)) return result;
     tmat4<T> rcc = rcc_matrix(ray);
-    Curve<T> rc = transform_curve(curve, rcc);
+    Curve<T> rc = transform_curve(local, rcc);
     const tvec3<T> rayDirection(T(0), T(0), T(1));
     tvec3<T> curveDirection = shim::normalize(rc.end - rc.start);
     T tStart = shim::dot(curveDirection, rayDirection) > T(0) ? T(0) : T(1);
-    bool exhausted_any = false;
+    bool exhausted_any = false, exhausted_isect = false;
     for (uint32_t side = 0; side < 2; ++side) {
         const uint32_t maxIterations = 8;
         T t = tStart;
         T told = T(0), dt1 = T(0), dt2 = T(0);
-        bool exhausted = true;
+        bool exhausted = true, last_isect = false;
         for (uint32_t i = 0; i < maxIterations; ++i) {
             Cone<T> cone;
             cone.center = sample_point(rc, t);
@@ -185,7 +200,20 @@ T prhi(const Ray<T>& ray_in, const Curve<T>& curve, T r0, T r1, tvec3<T>* normal
             cone.axis = sample_axis(rc, t);
             cone.slant = T(0);
             ConeHit<T> rci = ray_cone_rcc(cone);
+            last_isect = rci.isIntersection;
             if (rci.isIntersection && gabs(rci.dt) < T(5e-5)) {
+                if (polish) {  // one more cone step from the converged parameter
+                    T tp = t + rci.dt;
+                    if (tp >= T(0) && tp <= T(1)) {
+                        Cone<T> c2;
+                        c2.center = sample_point(rc, tp);
+                        c2.radius = (r0 == r1) ? r0 : r0 + (r1 - r0) * tp;
+                        c2.axis = sample_axis(rc, tp);
+                        c2.slant = T(0);
+                        ConeHit<T> r2 = ray_cone_rcc(c2);
+                        if (r2.isIntersection) { t = tp; rci = r2; cone = c2; }
+                    }
+                }
                 rci.s += cone.center.z;
                 result = rci.s + tshift;
                 tvec3<T> hitPosition = ray_in.origin + result * ray_in.direction;
@@ -211,10 +239,11 @@ T prhi(const Ray<T>& ray_in, const Curve<T>& curve, T r0, T r1, tvec3<T>* normal
             if (t < T(0) || t > T(1)) { exhausted = false; break; }
         }
         exhausted_any |= exhausted;
+        exhausted_isect |= exhausted && last_isect;
         if (result > T(0)) break;
         tStart = T(1) - tStart;
     }
-    *status = result > T(0) ? kHit : (exhausted_any ? kUnresolved : kMiss);
+    *status = result > T(0) ? kHit : (exhausted_isect ? kUnresolvedNear : (exhausted_any ? kUnresolved : kMiss));
     return result;
 }
 
@@ -756,6 +785,9 @@ static inline double xf_dir(const double* m, const double* p, int k) {
 
 // Intersect one BVH primitive; returns true and fills *h when it beats (t, prim) of *h.
 // mode64: 0 = precision T only; 1 = T then FP64 re-solve of unresolved Phantom candidates.
+// Diagnostics: FP32 unresolved candidates (far / near) and how many the FP64 re-solve turned
+// into hits (far / near).
+static std::atomic<int64_t> g_stat[4];
 // Closest-hit order: smaller t, then smaller instance, then smaller primitive id.
 template <class T>
 static bool intersect_prim(const Blas& b, uint32_t inst, uint32_t s, const tvec3<T>& o, const tvec3<T>& d, T tmin,
@@ -774,17 +806,19 @@ static bool intersect_prim(const Blas& b, uint32_t inst, uint32_t s, const tvec3
         Ray<T> ray{o, d};
         int st;
         tvec3<T> nrm;
-        bool shift = (resolve64 & 2) != 0;
-        T t = prhi(ray, cv, T(b.radius[2 * s]), T(b.radius[2 * s + 1]), &nrm, &st, shift);
+        bool shift = (resolve64 & 2) != 0, polish = (resolve64 & 4) != 0;
+        T t = prhi(ray, cv, T(b.radius[2 * s]), T(b.radius[2 * s + 1]), &nrm, &st, shift, polish);
+        if (st == kUnresolved || st == kUnresolvedNear) g_stat[st == kUnresolved ? 0 : 1]++;
         if (st == kHit) { take(t, s, T(0), 0); if (better) h->n = nrm; }
-        else if (st == kUnresolved && (resolve64 & 1)) {
+        else if (st == kUnresolvedNear && (resolve64 & 1)) {  // failed convergence test only
             Curve<double> cd{tvec3<double>(c[0], c[1], c[2]), tvec3<double>(c[3], c[4], c[5]),
                              tvec3<double>(c[6], c[7], c[8]), tvec3<double>(c[9], c[10], c[11])};
             Ray<double> rd{tvec3<double>(o.x, o.y, o.z), tvec3<double>(d.x, d.y, d.z)};
             int st2;
             tvec3<double> n2;
-            double t2 = prhi(rd, cd, double(b.radius[2 * s]), double(b.radius[2 * s + 1]), &n2, &st2, shift);
+            double t2 = prhi(rd, cd, double(b.radius[2 * s]), double(b.radius[2 * s + 1]), &n2, &st2, shift, polish);
             if (st2 == kHit) {
+                g_stat[st == kUnresolved ? 2 : 3]++;
                 take(T(t2), s, T(0), 1);
                 if (better) h->n = tvec3<T>(T(n2.x), T(n2.y), T(n2.z));
             }
@@ -886,11 +920,22 @@ static bool trace_one(const Scene& sc, const tvec3<T>& wo, const tvec3<T>& wd, T
 using namespace orc;
 
 namespace {
-// FP32 variants: 32 the reference-literal algorithm, 3264 with FP64 re-solve of unresolved
-// Phantom candidates, 33 / 3364 the same evaluated from the shifted origin (see prhi).
+// Precision codes of the tracing entry points.
+//   64    FP64, Phantom evaluated from the shifted origin (the oracle of record)
+//   6400  FP64, the reference-literal evaluation from the ray origin
+//   32    FP32, reference-literal; 3264 the same with FP64 re-solve of unresolved candidates
+//   33    FP32 from the shifted origin; 3364 the same with FP64 re-solve
+// The literal world-space bounding-cylinder test (cylinder.glsl:8-46) assumes a unit direction;
+// with a float-normalised direction its error grows with the squared distance of the ray
+// origin from the segment, so from a camera a few units away it misjudges rays in roughly the
+// outer tenth of the bounding radius even in exact arithmetic. The shifted evaluation is the
+// same formula on the same line, with that term made negligible.
 int fp32_mode(int precision) {
-    return (precision == 3264 || precision == 3364 ? 1 : 0) | (precision == 33 || precision == 3364 ? 2 : 0);
+    int p = precision % 1000000;
+    int m = (p == 3264 || p == 3364 ? 1 : 0) | (p == 33 || p == 3364 ? 2 : 0);
+    return m | (precision >= 1000000 ? 4 : 0);
 }
+int fp64_mode(int precision) { return (precision % 1000000 == 6400 ? 0 : 2) | (precision >= 1000000 ? 4 : 0); }
 template <class F> void parallel_for(int64_t n, int nthreads, F f) {
     if (nthreads <= 1 || n < 256) { for (int64_t i = 0; i < n; ++i) f(i); return; }
     std::atomic<int64_t> next{0};
@@ -1133,10 +1178,10 @@ void orc_trace_rays(void* s, const float* rays, int64_t n, float tmin, float tma
     const Scene& sc = *static_cast<Scene*>(s);
     parallel_for(n, nthreads, [&](int64_t i) {
         const float* r = rays + 6 * i;
-        if (precision == 64) {
+        if (precision % 1000000 == 64 || precision % 1000000 == 6400) {
             HitT<double> h;
             bool f = trace_one<double>(sc, tvec3<double>(r[0], r[1], r[2]), tvec3<double>(r[3], r[4], r[5]), double(tmin),
-                                       double(tmax), false, 0, 0, 0, &h);
+                                       double(tmax), false, 0, 0, fp64_mode(precision), &h);
             t_out[i] = f ? h.t : -1.0;
             prim_out[i] = f ? h.prim : 0xffffffffu;
             inst_out[i] = f ? h.inst : 0xffffffffu;
@@ -1186,10 +1231,10 @@ void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t 
             double col[3] = {0, 0, 0};
             bool found;
             uint32_t sh = 0;
-            if (precision == 64) {
+            if (precision % 1000000 == 64 || precision % 1000000 == 6400) {
                 HitT<double> hh;
                 tvec3<double> od(o[0], o[1], o[2]), dd(d[0], d[1], d[2]);
-                found = trace_one<double>(sc, od, dd, tmin, tmax, false, 0, 0, 0, &hh);
+                found = trace_one<double>(sc, od, dd, tmin, tmax, false, 0, 0, fp64_mode(precision), &hh);
                 t_out[si] = found ? hh.t : -1.0;
                 prim_out[si] = found ? hh.prim : 0xffffffffu;
                 inst_out[si] = found ? hh.inst : 0xffffffffu;
@@ -1201,7 +1246,7 @@ void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t 
                             tvec3<double> hp = od + hh.t * dd;
                             HitT<double> sh2;
                             lit = !trace_one<double>(sc, hp, tvec3<double>(0.0, 1.0, 0.0), double(shadow_tmin), double(tmax),
-                                                     true, hh.inst, hh.seg, 0, &sh2);
+                                                     true, hh.inst, hh.seg, fp64_mode(precision), &sh2);
                         }
                         sh = lit ? 0 : 1;
                         tvec3<double> c3 = lit ? shade(hh.n) : tvec3<double>(0.3f, 0.3f, 0.3f);
@@ -1237,12 +1282,15 @@ void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t 
             shadow_out[si] = uint8_t(sh);
         }
         float* px4 = fb + 4 * pi;
-        if (precision == 64) for (int c = 0; c < 3; ++c) px4[c] = float(acc[c] / double(spp));
+        if (precision % 1000000 == 64 || precision % 1000000 == 6400) for (int c = 0; c < 3; ++c) px4[c] = float(acc[c] / double(spp));
         else for (int c = 0; c < 3; ++c) px4[c] = accf[c] * (1.0f / float(spp));
         px4[3] = 1.0f;
     });
 }
 
 int orc_hardware_threads() { return int(std::thread::hardware_concurrency()); }
+void orc_resolve_stats(int64_t* out4, int reset) {
+    for (int k = 0; k < 4; ++k) { out4[k] = g_stat[k].load(); if (reset) g_stat[k] = 0; }
+}
 
 }  // extern "C"

@@ -69,8 +69,11 @@ template <class T> __device__ __forceinline__ bool ray_cylinder(V3<T> o, V3<T> d
     return gabs(k1 + k2 * t) < h;
 }
 
+// kUnresolved: no hit, and a side used all 8 iterations inside [0, 1] with a real cone
+// intersection at its last step (det > 0 but |dt| >= 5e-5): the FP32 run failed its
+// convergence test. Runs that exhaust without an intersection are misses.
 enum { kMiss = 0, kHit = 1, kUnresolved = 2 };
-template <class T> struct PrhiOut { T s; T tc; int status; };
+template <class T> struct PrhiOut { T s; T sl; T tc; int status; };  // s = ts + sl
 
 // ray.glsl:13-17 MakeOrthonormalBasis; the RCC transform (ray.glsl:19-33) is the inverse of
 // [e1 e2 e3 | o], applied here as the transpose of the orthonormal frame after the translation.
@@ -87,32 +90,41 @@ template <class T> __device__ __forceinline__ Frame<T> make_frame(V3<T> o, V3<T>
     return f;
 }
 
+// a - b - ts * d to full precision: a - b exactly by TwoSum, then one fused multiply-add.
+template <class T> __device__ __forceinline__ T rel_coord(T a, T b, T ts, T d) {
+    T c = -b;
+    T sum = a + c;
+    T cc = sum - a;
+    T err = (a - (sum - cc)) + (c - cc);
+    return fma(-ts, d, sum) + err;
+}
+
 // hair_intersection.rint:15-130 with the cone radius r0 + (r1 - r0) t (constant when equal).
-// status kUnresolved: no hit and some side used all 8 iterations inside [0, 1].
-// The bounding-cylinder test (on the infinite line) and the ray-centric transform are taken
-// from the ray point nearest the chord midpoint, o' = o + ts d, and ts is added back to the
-// distance: the same result in exact arithmetic, without the FP32 cancellation of a world-space
-// test from a distant origin (hair_intersection.rint:29).
+// The solve runs from o' = o + ts d, the ray point nearest the chord midpoint, on the vectors
+// P - o' kept at full precision (o' itself is never rounded); ts is added back to the
+// distance. The result is the same in exact arithmetic; in FP32 it removes the cancellation of
+// the world-space bounding-cylinder test from a distant origin (hair_intersection.rint:29).
 template <class T>
 __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T r0, T r1) {
-    PrhiOut<T> out{T(0), T(0), kMiss};
+    PrhiOut<T> out{T(0), T(0), T(0), kMiss};
     V3<T> cm = T(0.5) * (P[0] + P[3]);
     T ts = dot(cm - F.o, F.d) * F.inv_dd;
-    V3<T> o = F.o + ts * F.d;
+    V3<T> W[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        W[k] = mk(rel_coord(P[k].x, F.o.x, ts, F.d.x), rel_coord(P[k].y, F.o.y, ts, F.d.y),
+                  rel_coord(P[k].z, F.o.z, ts, F.d.z));
     V3<T> mid = bez_point(P, T(0.5));
     T rmax = length(cross(mid - P[0], mid - P[3])) / length(P[3] - P[0]) + gmax(r0, r1);
-    if (!ray_cylinder(o, F.d, P[0], P[3], rmax)) return out;
+    if (!ray_cylinder(mk(T(0), T(0), T(0)), F.d, W[0], W[3], rmax)) return out;
     V3<T> Q[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        V3<T> w = P[k] - o;
-        Q[k] = mk(dot(F.e1, w), dot(F.e2, w), dot(F.e3, w));
-    }
+    for (int k = 0; k < 4; ++k) Q[k] = mk(dot(F.e1, W[k]), dot(F.e2, W[k]), dot(F.e3, W[k]));
     T tStart = (Q[3].z - Q[0].z) > T(0) ? T(0) : T(1);
-    bool exhausted_any = false;
+    bool unresolved = false;
     for (int side = 0; side < 2; ++side) {
         T t = tStart, told = T(0), dt1 = T(0), dt2 = T(0);
-        bool exhausted = true;
+        bool exhausted = true, last_isect = false;
         for (int i = 0; i < 8; ++i) {
             V3<T> c = bez_point(Q, t);
             V3<T> ax = bez_axis(Q, t);
@@ -129,10 +141,12 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T 
             T a = cxd * cxd - ddd * (rad * rad) + dp * cdz2;
             T det = b * b - a * cc;
             bool isect = det > T(0);
+            last_isect = isect;
             T s = (b - (isect ? sqrt(det) : T(0))) / cc;
             T dt = (s * ax.z - cdd) / ddd;
             if (isect && gabs(dt) < T(5e-5)) {
-                out.s = (s + c.z) + ts;
+                out.sl = s + c.z;
+                out.s = out.sl + ts;
                 out.tc = t;
                 exhausted = false;
                 break;
@@ -151,30 +165,31 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T 
             }
             if (t < T(0) || t > T(1)) { exhausted = false; break; }
         }
-        exhausted_any |= exhausted;
+        unresolved |= exhausted && last_isect;
         if (out.s > T(0)) break;
         tStart = T(1) - tStart;
     }
-    out.status = out.s > T(0) ? kHit : (exhausted_any ? kUnresolved : kMiss);
+    out.status = out.s > T(0) ? kHit : (unresolved ? kUnresolved : kMiss);
     return out;
 }
 
 // FP64 re-solve of one candidate, kept out of line so the FP32 path keeps its registers.
 __device__ __noinline__ void prhi_fp64(float ox, float oy, float oz, float dx, float dy, float dz, const float* cp,
-                                       float r0, float r1, double* s_out, double* tc_out) {
+                                       float r0, float r1, double* s_out, double* sl_out, double* tc_out) {
     Frame<double> F = make_frame(mk(double(ox), double(oy), double(oz)), mk(double(dx), double(dy), double(dz)));
     V3<double> P[4];
     for (int k = 0; k < 4; ++k) P[k] = mk(double(cp[3 * k]), double(cp[3 * k + 1]), double(cp[3 * k + 2]));
     PrhiOut<double> r = prhi(F, P, double(r0), double(r1));
     *s_out = r.status == kHit ? r.s : -1.0;
+    *sl_out = r.sl;
     *tc_out = r.tc;
 }
 
 // ---------------------------------------------------------------- LSS (round cone)
 // Envelope of spheres a + u (b-a), radius ra + u (rb-ra): tangent-cone roots with u in [0,1]
-// and both end spheres; the least t >= tmin wins.
-__device__ __forceinline__ float sphere_hit(V3<float> o, V3<float> d, V3<float> c, float r, float tmin, float best) {
-    V3<float> oc = o - c;
+// and both end spheres; the least t >= tmin wins. Solved from o' = o + ts d (the ray point
+// nearest the segment midpoint) on the full-precision vectors a - o', b - o'; t = ts + t'.
+__device__ __forceinline__ float sphere_hit(V3<float> oc, V3<float> d, float r, float tmin, float best) {
     float A = dot(d, d), B = dot(oc, d), C = dot(oc, oc) - r * r;
     float h = B * B - A * C;
     if (h < 0.0f) return best;
@@ -184,15 +199,16 @@ __device__ __forceinline__ float sphere_hit(V3<float> o, V3<float> d, V3<float> 
     if (t1 >= tmin && t1 < best) return t1;
     return best;
 }
-// Solved from the ray point nearest the segment midpoint (t = ts + t').
 __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> a, V3<float> b, float ra, float rb,
-                                         float tmin_in, float* u_out) {
+                                         float tmin_in, float* u_out, float* tl_out) {
     const float kNone = __int_as_float(0x7f800000);
     float ts = dot(0.5f * (a + b) - o_in, d) / dot(d, d);
-    V3<float> o = o_in + ts * d;
+    V3<float> wa = mk(rel_coord(a.x, o_in.x, ts, d.x), rel_coord(a.y, o_in.y, ts, d.y), rel_coord(a.z, o_in.z, ts, d.z));
+    V3<float> wb = mk(rel_coord(b.x, o_in.x, ts, d.x), rel_coord(b.y, o_in.y, ts, d.y), rel_coord(b.z, o_in.z, ts, d.z));
+    V3<float> oa = mk(-wa.x, -wa.y, -wa.z);
     float tmin = tmin_in - ts;
     float best = kNone, bu = 0.0f;
-    V3<float> ba = b - a, oa = o - a;
+    V3<float> ba = b - a;
     float dr = rb - ra;
     float m = dot(ba, ba) - dr * dr;
     if (m > 0.0f) {
@@ -214,12 +230,13 @@ __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> 
             }
         }
     }
-    float ta = sphere_hit(o, d, a, ra, tmin, best);
+    float ta = sphere_hit(oa, d, ra, tmin, best);
     if (ta < best) { best = ta; bu = 0.0f; }
-    float tb = sphere_hit(o, d, b, rb, tmin, best);
+    float tb = sphere_hit(mk(-wb.x, -wb.y, -wb.z), d, rb, tmin, best);
     if (tb < best) { best = tb; bu = 1.0f; }
     if (best == kNone) return -1.0f;
     *u_out = bu;
+    *tl_out = best;
     return best + ts;
 }
 
@@ -265,6 +282,7 @@ struct Hit {
     uint32_t inst;
     uint32_t slot;  // leaf slot of the hit segment
     float u;        // curve / segment parameter
+    float sl;       // distance from the primitive's reference point o + ts d (normals)
     uint32_t flags; // HRT_HIT_FP64
 };
 __device__ __forceinline__ bool beats(float t, uint32_t inst, uint32_t id, const Hit& h) {
@@ -329,21 +347,21 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         PrhiOut<float> r = prhi(R.F, P, r0, r1);
         if (r.status == kHit) {
             if (r.s >= R.tmin && beats(r.s, inst, id, h)) {
-                h = Hit{r.s, id, inst, slot, r.tc, 0u};
+                h = Hit{r.s, id, inst, slot, r.tc, r.sl, 0u};
                 return true;
             }
         } else if (r.status == kUnresolved && fp64_resolve) {
             float cp[12];
 #pragma unroll
             for (int k = 0; k < 4; ++k) { cp[3 * k] = P[k].x; cp[3 * k + 1] = P[k].y; cp[3 * k + 2] = P[k].z; }
-            double s64, tc64;
-            prhi_fp64(R.o.x, R.o.y, R.o.z, R.d.x, R.d.y, R.d.z, cp, r0, r1, &s64, &tc64);
+            double s64, sl64, tc64;
+            prhi_fp64(R.o.x, R.o.y, R.o.z, R.d.x, R.d.y, R.d.z, cp, r0, r1, &s64, &sl64, &tc64);
             ++st.r64;
             if (s64 > 0.0) {
                 ++st.h64;
                 float s = float(s64);
                 if (s >= R.tmin && beats(s, inst, id, h)) {
-                    h = Hit{s, id, inst, slot, float(tc64), HRT_HIT_FP64};
+                    h = Hit{s, id, inst, slot, float(tc64), float(sl64), HRT_HIT_FP64};
                     return true;
                 }
             }
@@ -353,11 +371,11 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
     if (B.type == HRT_BLAS_LSS) {
         const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + slot;
         float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
-        float u;
-        float t = lss_hit(R.o, R.d, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, R.tmin, &u);
+        float u, tl;
+        float t = lss_hit(R.o, R.d, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, R.tmin, &u, &tl);
         if (t >= 0.0f && t <= h.t) {
             uint32_t id = __ldg(&B.prim_ids[slot]);
-            if (beats(t, inst, id, h)) { h = Hit{t, id, inst, slot, u, 0u}; return true; }
+            if (beats(t, inst, id, h)) { h = Hit{t, id, inst, slot, u, tl, 0u}; return true; }
         }
         return false;
     }
@@ -377,12 +395,12 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         float t0 = tri_hit(R.tr, R.o, A0, A1, A2, R.tmin, h.t);
         if (t0 >= 0.0f) {
             uint32_t id = 4u * seg + 2u * face;
-            if (beats(t0, inst, id, h)) { h = Hit{t0, id, inst, slot, 0.0f, 0u}; any = true; }
+            if (beats(t0, inst, id, h)) { h = Hit{t0, id, inst, slot, 0.0f, 0.0f, 0u}; any = true; }
         }
         float t1 = tri_hit(R.tr, R.o, A0, B1, A1, R.tmin, h.t);
         if (t1 >= 0.0f) {
             uint32_t id = 4u * seg + 2u * face + 1u;
-            if (beats(t1, inst, id, h)) { h = Hit{t1, id, inst, slot, 0.0f, 0u}; any = true; }
+            if (beats(t1, inst, id, h)) { h = Hit{t1, id, inst, slot, 0.0f, 0.0f, 0u}; any = true; }
         }
     }
     return any;
@@ -527,7 +545,7 @@ template <bool kQuant>
 __device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> wo, V3<float> wd, float tmin, float tmax,
                             Hit& h, bool any_hit, uint32_t skip_inst, uint32_t skip_slot, bool fp64_resolve, Stats& st,
                             uint32_t& err) {
-    h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0u};
+    h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0u};
     bool found = false;
     for (uint32_t i = 0; i < ninst; ++i) {
         const DevInstance& I = insts[i];
@@ -573,21 +591,28 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         d = mk(m[0] * wd.x + m[1] * wd.y + m[2] * wd.z, m[4] * wd.x + m[5] * wd.y + m[6] * wd.z,
                m[8] * wd.x + m[9] * wd.y + m[10] * wd.z);
     }
+    // Normals are differences of points a hair radius apart; they are formed from the
+    // full-precision vectors relative to the primitive's reference point o' = o + ts d.
     V3<float> n;
-    V3<float> hp = o + h.t * d;
     if (B.type == HRT_BLAS_PHANTOM) {
         // hair_intersection.rint:74-76: normalize(hit - curve(t))
         V3<float> P[4];
         float r0, r1;
         uint32_t id;
         load_phantom(B, h.slot, P, &r0, &r1, &id);
-        n = normalize(hp - bez_point(P, h.u));
+        float ts = dot(0.5f * (P[0] + P[3]) - o, d) / dot(d, d);
+        V3<float> W[4];
+        for (int k = 0; k < 4; ++k)
+            W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
+        n = normalize(h.sl * d - bez_point(W, h.u));
     } else if (B.type == HRT_BLAS_LSS) {
         // triangle_closest_hit.rchit:43-58: hit - mix(p0, p1, u)
         const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + h.slot;
         float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
         V3<float> p0 = mk(a.x, a.y, a.z), p1 = mk(b.x, b.y, b.z);
-        n = normalize(hp - (p0 + h.u * (p1 - p0)));
+        float ts = dot(0.5f * (p0 + p1) - o, d) / dot(d, d);
+        V3<float> w0 = mk(rel_coord(p0.x, o.x, ts, d.x), rel_coord(p0.y, o.y, ts, d.y), rel_coord(p0.z, o.z, ts, d.z));
+        n = normalize(h.sl * d - w0 - h.u * (p1 - p0));
     } else {
         // DOTS vertices carry no normals (geometry_processor.cpp:259-264): the face normal
         const PrimDots* pr = static_cast<const PrimDots*>(B.prims) + h.slot;
