@@ -129,9 +129,13 @@ def load_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+_OVERRIDE = {}
+
+
 def workload(name: str):
     import vkhrt_gb300 as H
     cfg = dict(H.CONFIGS[name])
+    cfg.update(_OVERRIDE)
     sp = H.StrandParams(seed=cfg["seed"], nstrands=cfg["nstrands"], nverts=cfg["nverts"], r_root=cfg["r_root"],
                         r_tip=cfg["r_tip"])
     return cfg, sp
@@ -291,6 +295,11 @@ def run_ours(args, dist):
                 "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
                 "bytes_per_launch": int(alg_bytes), "nodes_visited": int(st["nodes_visited"]),
                 "prims_tested": int(st["prims_tested"]), "node_bytes": int(node_b), "prim_bytes": int(prim_b)}
+    if args.profile:
+        print(json.dumps({"profile": True, "ms_per_step": round(ms, 3), "rays_per_step": int(rays_per_step),
+                          "value": round(value, 3), "roofline": roofline}), flush=True)
+        dist.close()
+        return
     # ---- e2e: C ABI per frame, camera in, framebuffer to pinned host memory ----
     lib = ctx.lib
     pinned = torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True)
@@ -369,8 +378,18 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle agreement and CPU baseline")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-pixels", type=int, default=4096)
+    ap.add_argument("--width", type=int, default=0, help="override the image width (profiling)")
+    ap.add_argument("--height", type=int, default=0, help="override the image height (profiling)")
+    ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling)")
+    ap.add_argument("--profile", action="store_true",
+                    help="one warm-up and the timed steps only: no e2e, FP32 comparison or CPU legs")
     args = ap.parse_args()
-    if args.warmup < 3:
+    for k in ("width", "height", "spp"):
+        if getattr(args, k):
+            _OVERRIDE[k] = getattr(args, k)
+    if args.profile:
+        args.quick = args.no_cpu = True
+    if args.warmup < 3 and not args.profile:
         args.warmup = 3
     dist = Dist()
     if args.impl == "reference":
