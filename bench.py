@@ -381,12 +381,17 @@ def main():
     ap.add_argument("--width", type=int, default=0, help="override the image width (profiling)")
     ap.add_argument("--height", type=int, default=0, help="override the image height (profiling)")
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling)")
+    ap.add_argument("--precision", choices=["fp32", "quantised"], default=None,
+                    help="override the workload's BVH/primitive precision (profiling)")
     ap.add_argument("--profile", action="store_true",
                     help="one warm-up and the timed steps only: no e2e, FP32 comparison or CPU legs")
     args = ap.parse_args()
     for k in ("width", "height", "spp"):
         if getattr(args, k):
             _OVERRIDE[k] = getattr(args, k)
+    if args.precision:
+        import vkhrt_gb300 as H
+        _OVERRIDE["precision"] = H.Precision.QUANTISED if args.precision == "quantised" else H.Precision.FP32
     if args.profile:
         args.quick = args.no_cpu = True
     if args.warmup < 3 and not args.profile:

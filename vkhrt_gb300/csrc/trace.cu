@@ -73,7 +73,7 @@ template <class T> __device__ __forceinline__ bool ray_cylinder(V3<T> o, V3<T> d
 // intersection at its last step (det > 0 but |dt| >= 5e-5): the FP32 run failed its
 // convergence test. Runs that exhaust without an intersection are misses.
 enum { kMiss = 0, kHit = 1, kUnresolved = 2 };
-template <class T> struct PrhiOut { T s; T sl; T tc; int status; };  // s = ts + sl
+template <class T> struct PrhiOut { T s; T sl; T ts; T tc; int status; };  // s = ts + sl
 
 // ray.glsl:13-17 MakeOrthonormalBasis; the RCC transform (ray.glsl:19-33) is the inverse of
 // [e1 e2 e3 | o], applied here as the transpose of the orthonormal frame after the translation.
@@ -106,9 +106,10 @@ template <class T> __device__ __forceinline__ T rel_coord(T a, T b, T ts, T d) {
 // the world-space bounding-cylinder test from a distant origin (hair_intersection.rint:29).
 template <class T>
 __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T r0, T r1) {
-    PrhiOut<T> out{T(0), T(0), T(0), kMiss};
+    PrhiOut<T> out{T(0), T(0), T(0), T(0), kMiss};
     V3<T> cm = T(0.5) * (P[0] + P[3]);
     T ts = dot(cm - F.o, F.d) * F.inv_dd;
+    out.ts = ts;
     V3<T> W[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
@@ -175,13 +176,15 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T 
 
 // FP64 re-solve of one candidate, kept out of line so the FP32 path keeps its registers.
 __device__ __noinline__ void prhi_fp64(float ox, float oy, float oz, float dx, float dy, float dz, const float* cp,
-                                       float r0, float r1, double* s_out, double* sl_out, double* tc_out) {
+                                       float r0, float r1, double* s_out, double* sl_out, double* ts_out,
+                                       double* tc_out) {
     Frame<double> F = make_frame(mk(double(ox), double(oy), double(oz)), mk(double(dx), double(dy), double(dz)));
     V3<double> P[4];
     for (int k = 0; k < 4; ++k) P[k] = mk(double(cp[3 * k]), double(cp[3 * k + 1]), double(cp[3 * k + 2]));
     PrhiOut<double> r = prhi(F, P, double(r0), double(r1));
     *s_out = r.status == kHit ? r.s : -1.0;
     *sl_out = r.sl;
+    *ts_out = r.ts;
     *tc_out = r.tc;
 }
 
@@ -200,7 +203,7 @@ __device__ __forceinline__ float sphere_hit(V3<float> oc, V3<float> d, float r, 
     return best;
 }
 __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> a, V3<float> b, float ra, float rb,
-                                         float tmin_in, float* u_out, float* tl_out) {
+                                         float tmin_in, float* u_out, float* tl_out, float* ts_out) {
     const float kNone = __int_as_float(0x7f800000);
     float ts = dot(0.5f * (a + b) - o_in, d) / dot(d, d);
     V3<float> wa = mk(rel_coord(a.x, o_in.x, ts, d.x), rel_coord(a.y, o_in.y, ts, d.y), rel_coord(a.z, o_in.z, ts, d.z));
@@ -237,6 +240,7 @@ __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> 
     if (best == kNone) return -1.0f;
     *u_out = bu;
     *tl_out = best;
+    *ts_out = ts;
     return best + ts;
 }
 
@@ -282,7 +286,7 @@ struct Hit {
     uint32_t inst;
     uint32_t slot;  // leaf slot of the hit segment
     float u;        // curve / segment parameter
-    float sl;       // distance from the primitive's reference point o + ts d (normals)
+    float ts, sl;   // t = ts + sl: the primitive's reference point o + ts d and the distance from it
     uint32_t flags; // HRT_HIT_FP64
 };
 __device__ __forceinline__ bool beats(float t, uint32_t inst, uint32_t id, const Hit& h) {
@@ -347,21 +351,21 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         PrhiOut<float> r = prhi(R.F, P, r0, r1);
         if (r.status == kHit) {
             if (r.s >= R.tmin && beats(r.s, inst, id, h)) {
-                h = Hit{r.s, id, inst, slot, r.tc, r.sl, 0u};
+                h = Hit{r.s, id, inst, slot, r.tc, r.ts, r.sl, 0u};
                 return true;
             }
         } else if (r.status == kUnresolved && fp64_resolve) {
             float cp[12];
 #pragma unroll
             for (int k = 0; k < 4; ++k) { cp[3 * k] = P[k].x; cp[3 * k + 1] = P[k].y; cp[3 * k + 2] = P[k].z; }
-            double s64, sl64, tc64;
-            prhi_fp64(R.o.x, R.o.y, R.o.z, R.d.x, R.d.y, R.d.z, cp, r0, r1, &s64, &sl64, &tc64);
+            double s64, sl64, tc64, ts64;
+            prhi_fp64(R.o.x, R.o.y, R.o.z, R.d.x, R.d.y, R.d.z, cp, r0, r1, &s64, &sl64, &ts64, &tc64);
             ++st.r64;
             if (s64 > 0.0) {
                 ++st.h64;
                 float s = float(s64);
                 if (s >= R.tmin && beats(s, inst, id, h)) {
-                    h = Hit{s, id, inst, slot, float(tc64), float(sl64), HRT_HIT_FP64};
+                    h = Hit{s, id, inst, slot, float(tc64), float(ts64), float(s64 - double(float(ts64))), HRT_HIT_FP64};
                     return true;
                 }
             }
@@ -371,11 +375,11 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
     if (B.type == HRT_BLAS_LSS) {
         const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + slot;
         float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
-        float u, tl;
-        float t = lss_hit(R.o, R.d, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, R.tmin, &u, &tl);
+        float u, tl, ts;
+        float t = lss_hit(R.o, R.d, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, R.tmin, &u, &tl, &ts);
         if (t >= 0.0f && t <= h.t) {
             uint32_t id = __ldg(&B.prim_ids[slot]);
-            if (beats(t, inst, id, h)) { h = Hit{t, id, inst, slot, u, tl, 0u}; return true; }
+            if (beats(t, inst, id, h)) { h = Hit{t, id, inst, slot, u, ts, tl, 0u}; return true; }
         }
         return false;
     }
@@ -395,12 +399,12 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         float t0 = tri_hit(R.tr, R.o, A0, A1, A2, R.tmin, h.t);
         if (t0 >= 0.0f) {
             uint32_t id = 4u * seg + 2u * face;
-            if (beats(t0, inst, id, h)) { h = Hit{t0, id, inst, slot, 0.0f, 0.0f, 0u}; any = true; }
+            if (beats(t0, inst, id, h)) { h = Hit{t0, id, inst, slot, 0.0f, 0.0f, 0.0f, 0u}; any = true; }
         }
         float t1 = tri_hit(R.tr, R.o, A0, B1, A1, R.tmin, h.t);
         if (t1 >= 0.0f) {
             uint32_t id = 4u * seg + 2u * face + 1u;
-            if (beats(t1, inst, id, h)) { h = Hit{t1, id, inst, slot, 0.0f, 0.0f, 0u}; any = true; }
+            if (beats(t1, inst, id, h)) { h = Hit{t1, id, inst, slot, 0.0f, 0.0f, 0.0f, 0u}; any = true; }
         }
     }
     return any;
@@ -545,7 +549,7 @@ template <bool kQuant>
 __device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> wo, V3<float> wd, float tmin, float tmax,
                             Hit& h, bool any_hit, uint32_t skip_inst, uint32_t skip_slot, bool fp64_resolve, Stats& st,
                             uint32_t& err) {
-    h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0u};
+    h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
     bool found = false;
     for (uint32_t i = 0; i < ninst; ++i) {
         const DevInstance& I = insts[i];
@@ -600,7 +604,7 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         float r0, r1;
         uint32_t id;
         load_phantom(B, h.slot, P, &r0, &r1, &id);
-        float ts = dot(0.5f * (P[0] + P[3]) - o, d) / dot(d, d);
+        float ts = h.ts;
         V3<float> W[4];
         for (int k = 0; k < 4; ++k)
             W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
@@ -610,7 +614,7 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + h.slot;
         float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
         V3<float> p0 = mk(a.x, a.y, a.z), p1 = mk(b.x, b.y, b.z);
-        float ts = dot(0.5f * (p0 + p1) - o, d) / dot(d, d);
+        float ts = h.ts;
         V3<float> w0 = mk(rel_coord(p0.x, o.x, ts, d.x), rel_coord(p0.y, o.y, ts, d.y), rel_coord(p0.z, o.z, ts, d.z));
         n = normalize(h.sl * d - w0 - h.u * (p1 - p0));
     } else {
