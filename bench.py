@@ -268,9 +268,10 @@ def run_ours(args, dist):
     build_wall = time.perf_counter() - t0
     cam = H.scene_camera(w, h)
     frame = H.Frame(ctx, w, h, spp, with_hits=True)
-    params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, **{"async": 1})
+    params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, kernel_variant=args.variant, **{"async": 1})
     # rays per step (deterministic: fixed camera, jitter seed)
-    H.trace(ctx, tlas, cam, frame, H.trace_params(spp=spp, jitter=1, seed=17, shading=2, count_stats=1))
+    H.trace(ctx, tlas, cam, frame, H.trace_params(spp=spp, jitter=1, seed=17, shading=2, count_stats=1,
+                                                  kernel_variant=args.variant))
     st = frame.stats()
     rays_per_step = st["primary_rays"] + st["shadow_rays"]
     # ---- timed region ----
@@ -303,7 +304,7 @@ def run_ours(args, dist):
     # ---- e2e: C ABI per frame, camera in, framebuffer to pinned host memory ----
     lib = ctx.lib
     pinned = torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True)
-    sync_params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2)
+    sync_params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, kernel_variant=args.variant)
     for _ in range(2):
         H.trace(ctx, tlas, cam, frame, sync_params)
         ctx.check(lib.hrt_frame_download(frame.handle, ctypes.c_void_p(pinned.data_ptr()), None, None))
@@ -333,7 +334,8 @@ def run_ours(args, dist):
             H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=H.Precision.FP32), ctx)
         tlas32 = H.TopLevelAccelerationStructure([blas32], ctx)
         f32 = H.Frame(ctx, w, h, spp, with_hits=False)
-        H.trace(ctx, tlas32, cam, f32, H.trace_params(spp=spp, jitter=1, seed=17, shading=2))
+        H.trace(ctx, tlas32, cam, f32, H.trace_params(spp=spp, jitter=1, seed=17, shading=2,
+                                                      kernel_variant=args.variant))
         s32 = f32.stats()
         ms32 = time_frames(ctx, tlas32, cam, f32, params, args.steps, args.warmup)
         line["plain_fp32"] = {"value": round((s32["primary_rays"] + s32["shadow_rays"]) / (ms32 * 1e-3) / 1e6, 3),
@@ -383,6 +385,7 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling)")
     ap.add_argument("--precision", choices=["fp32", "quantised"], default=None,
                     help="override the workload's BVH/primitive precision (profiling)")
+    ap.add_argument("--variant", type=int, default=0, help="trace kernel variant (0 default, 1, 2)")
     ap.add_argument("--profile", action="store_true",
                     help="one warm-up and the timed steps only: no e2e, FP32 comparison or CPU legs")
     args = ap.parse_args()

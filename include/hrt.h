@@ -148,7 +148,7 @@ typedef struct hrt_trace_params {
     uint32_t record_hits;  /* write per-sample hit records into the frame */
     uint32_t async;        /* 0: synchronise and check the device error word before returning */
     uint32_t count_stats;  /* accumulate traversal counters into the frame stats */
-    uint32_t reserved;
+    uint32_t kernel_variant; /* 0 default; 1: 4 resident blocks per SM; 2: 3 blocks with more registers */
 } hrt_trace_params;
 
 typedef struct hrt_hit {

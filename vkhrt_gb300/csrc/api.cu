@@ -36,6 +36,7 @@ struct hrt_tlas {
     DevInstance* dev = nullptr;
     uint32_t n = 0;
     bool quantised = false;
+    uint32_t type_mask = 0;  // bit per hrt_geometry_type present
 };
 
 struct hrt_frame {
@@ -171,8 +172,17 @@ void fill_scene(SceneLaunch& sl, const hrt_tlas* t, const hrt_camera* cam, hrt_f
     sl.hits = f->hits;
 }
 
-TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32_t n, uint64_t total, TraceCounters* c) {
+// The primitive type shared by every instance (selects a specialised kernel), or 3.
+uint32_t prim_kind(uint32_t type_mask) {
+    for (uint32_t k = 0; k < 3; ++k)
+        if (type_mask == (1u << k)) return k;
+    return 3;
+}
+
+TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32_t n, uint64_t total, TraceCounters* c,
+                        uint32_t type_mask) {
     TraceLaunch L;
+    L.prim_kind = prim_kind(type_mask);
     L.scenes = ds;
     L.nscenes = n;
     L.total_work = total;
@@ -185,6 +195,7 @@ TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32
     L.fp64_resolve = p->fp64_resolve;
     L.record_hits = p->record_hits;
     L.count_stats = p->count_stats;
+    L.variant = p->kernel_variant;
     L.counters = c;
     return L;
 }
@@ -476,6 +487,7 @@ hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint3
     DeviceSet ds(ctx->device);
     std::vector<DevInstance> inst(n);
     bool quant = false;
+    uint32_t type_mask = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const hrt_blas* b = blases[i];
         if (!b) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_tlas_build: null BLAS %u", i);
@@ -485,6 +497,7 @@ hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint3
             return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_tlas_build: FP32 and quantised BLASes cannot share a TLAS");
         DevInstance& d = inst[i];
         memset(&d, 0, sizeof(d));
+        type_mask |= 1u << b->type;
         d.b.nodes = b->out.nodes;
         d.b.prims = b->out.prims;
         d.b.roots = b->out.roots;
@@ -508,6 +521,7 @@ hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint3
     t->ctx = ctx;
     t->n = n;
     t->quantised = quant;
+    t->type_mask = type_mask;
     if (n) {
         cudaError_t e = cudaMalloc(&t->dev, n * sizeof(DevInstance));
         if (e == cudaSuccess)
@@ -669,7 +683,7 @@ hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* c
     fill_scene(sl, tlas, cam, f, 0);
     CK(ctx, cudaMemcpyAsync(f->dscene, &sl, sizeof(sl), cudaMemcpyHostToDevice, s), "upload scene");
     CK(ctx, cudaMemsetAsync(f->counters, 0, sizeof(TraceCounters), s), "reset counters");
-    TraceLaunch L = make_launch(p, f->dscene, 1, sl.work_count, f->counters);
+    TraceLaunch L = make_launch(p, f->dscene, 1, sl.work_count, f->counters, tlas->type_mask);
     CK(ctx, launch_trace(L, tlas->quantised, s, ctx->sm_count), "launch trace");
     f->pending_primary = uint64_t(f->w) * f->h * f->spp;
     f->stats_pending = true;
@@ -733,8 +747,10 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
     std::vector<SceneLaunch> sl(n);
     uint64_t work = 0, primary = 0;
     bool quant = false;
+    uint32_t type_mask = 0;
     for (uint32_t i = 0; i < n; ++i) {
         if (!scenes[i].tlas || !scenes[i].frame) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_create: scene %u incomplete", i);
+        type_mask |= scenes[i].tlas->type_mask;
         if (i == 0) quant = scenes[i].tlas->quantised;
         else if (scenes[i].tlas->quantised != quant)
             return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_batch_create: scenes mix FP32 and quantised BLASes");
@@ -761,7 +777,7 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         cudaError_t e1 = cudaMemsetAsync(b->counters, 0, sizeof(TraceCounters), cap);
-        TraceLaunch L = make_launch(p, b->dscenes, n, work, b->counters);
+        TraceLaunch L = make_launch(p, b->dscenes, n, work, b->counters, type_mask);
         cudaError_t e2 = e1 == cudaSuccess ? launch_trace(L, quant, cap, ctx->sm_count) : e1;
         cudaError_t e3 = cudaStreamEndCapture(cap, &b->graph);
         e = e2 != cudaSuccess ? e2 : e3;

@@ -93,6 +93,8 @@ struct TraceLaunch {
     uint64_t total_work;
     float tmin, tmax, shadow_tmin;
     uint32_t jitter, seed, shading, fp64_resolve, record_hits, count_stats;
+    uint32_t prim_kind;  // the primitive type of every instance, or 3 when they differ
+    uint32_t variant;    // kernel variant (occupancy / register split), 0 = default
     TraceCounters* counters;
 };
 

@@ -77,11 +77,9 @@ template <class T> struct PrhiOut { T s; T sl; T ts; T tc; int status; };  // s 
 
 // ray.glsl:13-17 MakeOrthonormalBasis; the RCC transform (ray.glsl:19-33) is the inverse of
 // [e1 e2 e3 | o], applied here as the transpose of the orthonormal frame after the translation.
-template <class T> struct Frame { V3<T> o, d, e1, e2, e3; T inv_dd; };
-template <class T> __device__ __forceinline__ Frame<T> make_frame(V3<T> o, V3<T> d) {
+template <class T> struct Frame { V3<T> e1, e2, e3; T inv_dd; };
+template <class T> __device__ __forceinline__ Frame<T> make_frame(V3<T> d) {
     Frame<T> f;
-    f.o = o;
-    f.d = d;
     f.inv_dd = T(1) / dot(d, d);
     f.e3 = normalize(d);
     V3<T> w = f.e3;
@@ -105,19 +103,18 @@ template <class T> __device__ __forceinline__ T rel_coord(T a, T b, T ts, T d) {
 // distance. The result is the same in exact arithmetic; in FP32 it removes the cancellation of
 // the world-space bounding-cylinder test from a distant origin (hair_intersection.rint:29).
 template <class T>
-__device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T r0, T r1) {
+__device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, const V3<T>* P, T r0, T r1) {
     PrhiOut<T> out{T(0), T(0), T(0), T(0), kMiss};
     V3<T> cm = T(0.5) * (P[0] + P[3]);
-    T ts = dot(cm - F.o, F.d) * F.inv_dd;
+    T ts = dot(cm - o, d) * F.inv_dd;
     out.ts = ts;
     V3<T> W[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        W[k] = mk(rel_coord(P[k].x, F.o.x, ts, F.d.x), rel_coord(P[k].y, F.o.y, ts, F.d.y),
-                  rel_coord(P[k].z, F.o.z, ts, F.d.z));
+        W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
     V3<T> mid = bez_point(P, T(0.5));
     T rmax = length(cross(mid - P[0], mid - P[3])) / length(P[3] - P[0]) + gmax(r0, r1);
-    if (!ray_cylinder(mk(T(0), T(0), T(0)), F.d, W[0], W[3], rmax)) return out;
+    if (!ray_cylinder(mk(T(0), T(0), T(0)), d, W[0], W[3], rmax)) return out;
     V3<T> Q[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) Q[k] = mk(dot(F.e1, W[k]), dot(F.e2, W[k]), dot(F.e3, W[k]));
@@ -178,10 +175,11 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, const V3<T>* P, T 
 __device__ __noinline__ void prhi_fp64(float ox, float oy, float oz, float dx, float dy, float dz, const float* cp,
                                        float r0, float r1, double* s_out, double* sl_out, double* ts_out,
                                        double* tc_out) {
-    Frame<double> F = make_frame(mk(double(ox), double(oy), double(oz)), mk(double(dx), double(dy), double(dz)));
+    V3<double> o = mk(double(ox), double(oy), double(oz)), d = mk(double(dx), double(dy), double(dz));
+    Frame<double> F = make_frame(d);
     V3<double> P[4];
     for (int k = 0; k < 4; ++k) P[k] = mk(double(cp[3 * k]), double(cp[3 * k + 1]), double(cp[3 * k + 2]));
-    PrhiOut<double> r = prhi(F, P, double(r0), double(r1));
+    PrhiOut<double> r = prhi(F, o, d, P, double(r0), double(r1));
     *s_out = r.status == kHit ? r.s : -1.0;
     *sl_out = r.sl;
     *ts_out = r.ts;
@@ -340,15 +338,19 @@ __device__ __forceinline__ void load_phantom(const DevBlas& B, uint32_t slot, V3
     }
 }
 
-// Tests one leaf slot; returns true if it produced an accepted hit.
+// Tests one leaf slot; returns true if it produced an accepted hit. kType is the primitive
+// type when every instance of the launch has the same one, kMixed to branch on the BLAS.
+constexpr int kMixed = 3;
+template <int kType = kMixed>
 __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint32_t inst, const RayState& R, Hit& h,
                                           bool fp64_resolve, Stats& st) {
-    if (B.type == HRT_BLAS_PHANTOM) {
+    const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
+    if (type == HRT_BLAS_PHANTOM) {
         V3<float> P[4];
         float r0, r1;
         uint32_t id;
         load_phantom(B, slot, P, &r0, &r1, &id);
-        PrhiOut<float> r = prhi(R.F, P, r0, r1);
+        PrhiOut<float> r = prhi(R.F, R.o, R.d, P, r0, r1);
         if (r.status == kHit) {
             if (r.s >= R.tmin && beats(r.s, inst, id, h)) {
                 h = Hit{r.s, id, inst, slot, r.tc, r.ts, r.sl, 0u};
@@ -372,7 +374,7 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         }
         return false;
     }
-    if (B.type == HRT_BLAS_LSS) {
+    if (type == HRT_BLAS_LSS) {
         const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + slot;
         float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
         float u, tl, ts;
@@ -574,7 +576,7 @@ __device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> 
             float b = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), h.t));
             if (!(a <= b * (1.0f + 9.5367431640625e-07f))) continue;
         }
-        if (I.b.type == HRT_BLAS_PHANTOM) R.F = make_frame(R.o, R.d);
+        if (I.b.type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
         else if (I.b.type == HRT_BLAS_DOTS) R.tr = make_triray(R.d);
         if (traverse<kQuant>(I.b, i, R, h, any_hit, skip_inst, skip_slot, fp64_resolve, st, err)) {
             found = true;
@@ -679,81 +681,274 @@ __device__ __forceinline__ void warp_add(unsigned long long* ctr, uint32_t v) {
     if ((threadIdx.x & 31) == 0 && s) atomicAdd(ctr, (unsigned long long)s);
 }
 
-template <bool kQuant>
-__global__ void __launch_bounds__(kThreads) trace_kernel(TraceLaunch L) {
-    const int lane = threadIdx.x & 31;
-    Stats st{0, 0, 0, 0};
-    uint32_t shadow_rays = 0;
-    uint32_t err = 0;
+// ---------------------------------------------------------------- the frame kernel
+// Persistent while-while traversal (Aila and Laine, HPG 2009): every lane owns a ray task (a
+// pixel: its samples, each a primary ray and, when shading with shadows, one shadow ray).
+//   refill     lanes without a task take pixels with one warp-aggregated atomic once enough
+//              lanes are idle (ballot + popc ranks), so finished rays do not idle the warp;
+//   node phase lanes pop and test nodes together until each holds a leaf or runs dry;
+//   leaf phase lanes with a leaf run its intersector together (the Phantom solve is long, so
+//              keeping it out of the node loop keeps the warp converged);
+//   completion a finished ray moves to the next instance, spawns its shadow ray, shades, or
+//              finishes the pixel.
+// The stack's top kShort entries live in shared memory (one column per thread), deeper ones
+// in local memory. Results do not depend on scheduling: one lane handles all samples of a
+// pixel in order and each ray's closest hit is the least (t, instance, id).
+constexpr int kShort = 16;
+constexpr int kRefill = 16;
+
+template <bool kQuant, int kType, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch L) {
+    __shared__ uint2 s_stack[kShort][kThreads];
+    uint2 l_stack[kStackSize - kShort];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     const volatile uint32_t* errword = &L.counters->error;
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = *errword ? L.total_work : atomicAdd(&L.counters->work, 32ull);
-        base = __shfl_sync(kFull, base, 0);
-        if (base >= L.total_work) break;
-        uint64_t g = base + lane;
-        // scene of this tile (scenes are few; linear scan)
-        uint32_t si = 0;
-        while (si + 1 < L.nscenes && L.scenes[si + 1].work_begin <= g) ++si;
+    Stats st{0, 0, 0, 0};
+    uint32_t shadow_rays = 0, err = 0;
+
+    bool has_ray = false, fetch_done = false;
+    uint32_t si = 0, px = 0, py = 0, sample = 0;
+    uint64_t pix = 0;
+    bool shadow = false, shadow_hit = false;
+    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, ndl = 0.0f;
+    uint32_t prim_flags = 0;
+    V3<float> wo = mk(0.0f, 0.0f, 0.0f), wd = mk(0.0f, 0.0f, 1.0f);
+    float cur_tmin = 0.0f;
+    RayState R;
+    Hit h{0.0f, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
+    uint32_t inst_cur = 0, skip_inst = 0xffffffffu, skip_slot = 0xffffffffu;
+    int sp = 0;
+    uint32_t leaf = 0, steps = 0;
+    bool have_leaf = false;
+
+    auto push = [&](uint2 e) {
+        if (sp < kShort) s_stack[sp][tid] = e;
+        else l_stack[sp - kShort] = e;
+        ++sp;
+    };
+    auto pop = [&]() -> uint2 {
+        --sp;
+        return sp < kShort ? s_stack[sp][tid] : l_stack[sp - kShort];
+    };
+    // Object-space ray for instance i; pushes its root when the instance box is hit.
+    auto setup_instance = [&](uint32_t i) -> bool {
+        const DevInstance& I = L.scenes[si].inst[i];
+        if (I.identity) { R.o = wo; R.d = wd; }
+        else {
+            const float* m = I.w2o;
+            R.o = mk(m[0] * wo.x + m[1] * wo.y + m[2] * wo.z + m[3], m[4] * wo.x + m[5] * wo.y + m[6] * wo.z + m[7],
+                     m[8] * wo.x + m[9] * wo.y + m[10] * wo.z + m[11]);
+            R.d = mk(m[0] * wd.x + m[1] * wd.y + m[2] * wd.z, m[4] * wd.x + m[5] * wd.y + m[6] * wd.z,
+                     m[8] * wd.x + m[9] * wd.y + m[10] * wd.z);
+        }
+        R.inv = mk(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
+        R.tmin = cur_tmin;
+        const DevBlas& B = I.b;
+        if (B.nnodes == 0) return false;
+        float x0 = (B.lo[0] - R.o.x) * R.inv.x, x1 = (B.hi[0] - R.o.x) * R.inv.x;
+        float y0 = (B.lo[1] - R.o.y) * R.inv.y, y1 = (B.hi[1] - R.o.y) * R.inv.y;
+        float z0 = (B.lo[2] - R.o.z) * R.inv.z, z1 = (B.hi[2] - R.o.z) * R.inv.z;
+        float a = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), cur_tmin));
+        float b = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), h.t));
+        if (!(a <= b * (1.0f + 9.5367431640625e-07f))) return false;
+        const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
+        if (type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
+        else if (type == HRT_BLAS_DOTS) R.tr = make_triray(R.d);
+        push(make_uint2(0u, __float_as_uint(cur_tmin)));
+        return true;
+    };
+    auto start_ray = [&](V3<float> o, V3<float> d, float tmin, float tmax) {
+        wo = o;
+        wd = d;
+        cur_tmin = tmin;
+        h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
+        sp = 0;
+        steps = 0;
+        const uint32_t n = L.scenes[si].ninst;
+        for (inst_cur = 0; inst_cur < n; ++inst_cur)
+            if (setup_instance(inst_cur)) break;
+    };
+    auto start_primary = [&]() {
         const SceneLaunch& S = L.scenes[si];
-        uint64_t local = g - S.work_begin;
-        uint64_t tile = local >> 5;
-        uint32_t within = uint32_t(local & 31u);
-        uint32_t px = uint32_t(tile % S.tiles_x) * 8u + (within & 7u);
-        uint32_t py = uint32_t(tile / S.tiles_x) * 4u + (within >> 3);
-        if (err && lane == 0) atomicOr(&L.counters->error, err);  // stop every warp early
-        if (px >= S.width || py >= S.height || err) continue;
-        uint64_t pix = uint64_t(py) * S.width + px;
-        float acc[3] = {0.0f, 0.0f, 0.0f};
-        for (uint32_t k = 0; k < S.spp; ++k) {
-            float jx = 0.5f, jy = 0.5f;
-            if (L.jitter || S.spp > 1) {
-                uint32_t h1 = hash_u32(L.seed ^ hash_u32(uint32_t(pix) * S.spp + k));
-                uint32_t h2 = hash_u32(h1);
-                jx = float(h1 >> 8) * 5.9604644775390625e-08f;
-                jy = float(h2 >> 8) * 5.9604644775390625e-08f;
-            }
-            V3<float> o, d;
-            raygen(S.view_inv, S.proj_inv, px, py, S.width, S.height, jx, jy, &o, &d);
-            Hit h;
-            bool found = trace_scene<kQuant>(S.inst, S.ninst, o, d, L.tmin, L.tmax, h, false, 0, 0, L.fp64_resolve != 0,
-                                             st, err);
-            float col[3] = {0.0f, 0.0f, 0.0f};
-            uint32_t flags = h.flags;
-            if (found) {
-                if (L.shading == HRT_SHADE_DEBUG) {
-                    uint32_t c = h.id % 6u;
-                    col[0] = kPalette[c][0]; col[1] = kPalette[c][1]; col[2] = kPalette[c][2];
-                } else {
-                    V3<float> n = hit_normal(S.inst[h.inst], h, o, d);
-                    bool lit = true;
-                    if (L.shading == HRT_SHADE_LAMBERT_SHADOW) {
-                        V3<float> hp = o + h.t * d;
-                        Hit hs;
-                        ++shadow_rays;
-                        lit = !trace_scene<kQuant>(S.inst, S.ninst, hp, mk(0.0f, 1.0f, 0.0f), L.shadow_tmin, L.tmax, hs,
-                                                   true, h.inst, h.slot, L.fp64_resolve != 0, st, err);
-                        if (!lit) flags |= HRT_HIT_SHADOWED;
-                    }
-                    // shading.glsl:1-10 with light direction (0,-1,0): |dot(n, L)| = |n.y|
-                    float ndl = lit ? fabsf(n.y) : 0.0f;
-                    col[0] = ndl * 0.4f + 0.3f;
-                    col[1] = ndl * 0.2f + 0.3f;
-                    col[2] = ndl * 0.1f + 0.3f;
-                }
-            }
-            acc[0] += col[0]; acc[1] += col[1]; acc[2] += col[2];
+        float jx = 0.5f, jy = 0.5f;
+        if (L.jitter || S.spp > 1) {
+            uint32_t h1 = hash_u32(L.seed ^ hash_u32(uint32_t(pix) * S.spp + sample));
+            uint32_t h2 = hash_u32(h1);
+            jx = float(h1 >> 8) * 5.9604644775390625e-08f;
+            jy = float(h2 >> 8) * 5.9604644775390625e-08f;
+        }
+        V3<float> o, d;
+        raygen(S.view_inv, S.proj_inv, px, py, S.width, S.height, jx, jy, &o, &d);
+        shadow = false;
+        start_ray(o, d, L.tmin, L.tmax);
+    };
+    auto next_sample = [&]() {
+        const SceneLaunch& S = L.scenes[si];
+        ++sample;
+        if (sample < S.spp) { start_primary(); return; }
+        float inv = 1.0f / float(S.spp);
+        S.fb[pix] = make_float4(acc0 * inv, acc1 * inv, acc2 * inv, 1.0f);
+        has_ray = false;
+    };
+    auto finish_phase = [&]() {
+        const SceneLaunch& S = L.scenes[si];
+        uint64_t rec = pix * S.spp + sample;
+        if (!shadow) {
+            bool found = h.id != 0xffffffffu;
+            prim_flags = h.flags;
             if (L.record_hits && S.hits) {
                 hrt_hit r;
                 r.t = found ? h.t : -1.0f;
-                r.prim = found ? h.id : 0xffffffffu;
-                r.inst = found ? h.inst : 0xffffffffu;
-                r.flags = found ? flags : 0u;
-                S.hits[pix * S.spp + k] = r;
+                r.prim = h.id;
+                r.inst = h.inst;
+                r.flags = found ? h.flags : 0u;
+                S.hits[rec] = r;
+            }
+            if (!found) { next_sample(); return; }
+            if (L.shading == HRT_SHADE_DEBUG) {
+                uint32_t c = h.id % 6u;
+                acc0 += kPalette[c][0]; acc1 += kPalette[c][1]; acc2 += kPalette[c][2];
+                next_sample();
+                return;
+            }
+            V3<float> n = hit_normal(S.inst[h.inst], h, wo, wd);
+            ndl = fabsf(n.y);  // shading.glsl: |dot(n, (0,-1,0))|
+            if (L.shading == HRT_SHADE_LAMBERT_SHADOW) {
+                skip_inst = h.inst;
+                skip_slot = h.slot;
+                shadow_hit = false;
+                shadow = true;
+                ++shadow_rays;
+                V3<float> hp = wo + h.t * wd;
+                start_ray(hp, mk(0.0f, 1.0f, 0.0f), L.shadow_tmin, L.tmax);
+                return;
+            }
+            acc0 += ndl * 0.4f + 0.3f; acc1 += ndl * 0.2f + 0.3f; acc2 += ndl * 0.1f + 0.3f;
+            next_sample();
+            return;
+        }
+        float lit = shadow_hit ? 0.0f : ndl;
+        acc0 += lit * 0.4f + 0.3f; acc1 += lit * 0.2f + 0.3f; acc2 += lit * 0.1f + 0.3f;
+        if (shadow_hit && L.record_hits && S.hits) S.hits[rec].flags = prim_flags | HRT_HIT_SHADOWED;
+        shadow = false;
+        next_sample();
+    };
+
+    for (;;) {
+        // ---- refill idle lanes
+        uint32_t idle = __ballot_sync(kFull, !has_ray);
+        if (idle && !fetch_done && (__popc(idle) >= kRefill || idle == kFull)) {
+            int n = __popc(idle), leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = *errword ? L.total_work : atomicAdd(&L.counters->work, (unsigned long long)n);
+            base = __shfl_sync(kFull, base, leader);
+            if (base + uint64_t(n) >= L.total_work) fetch_done = true;
+            if (!has_ray) {
+                uint64_t g = base + __popc(idle & lt_mask);
+                if (g < L.total_work) {
+                    si = 0;
+                    while (si + 1 < L.nscenes && L.scenes[si + 1].work_begin <= g) ++si;
+                    const SceneLaunch& S = L.scenes[si];
+                    uint64_t local = g - S.work_begin, tile = local >> 5;
+                    uint32_t within = uint32_t(local & 31u);
+                    px = uint32_t(tile % S.tiles_x) * 8u + (within & 7u);
+                    py = uint32_t(tile / S.tiles_x) * 4u + (within >> 3);
+                    if (px < S.width && py < S.height) {
+                        pix = uint64_t(py) * S.width + px;
+                        has_ray = true;
+                        sample = 0;
+                        acc0 = acc1 = acc2 = 0.0f;
+                        start_primary();
+                    }
+                }
             }
         }
-        float inv = 1.0f / float(S.spp);
-        S.fb[pix] = make_float4(acc[0] * inv, acc[1] * inv, acc[2] * inv, 1.0f);
+        if (!__any_sync(kFull, has_ray)) {
+            if (fetch_done) break;
+            continue;
+        }
+        // ---- node phase
+        for (;;) {
+            bool want = has_ray && !have_leaf && sp > 0;
+            if (!__any_sync(kFull, want)) break;
+            if (!want) continue;
+            if (++steps > kMaxTraversalSteps) {
+                err |= kErrTimeout;
+                sp = 0;
+                continue;
+            }
+            uint2 e = pop();
+            if (__uint_as_float(e.y) > h.t) continue;
+            if (e.x & kLeafFlag) {
+                leaf = e.x;
+                have_leaf = true;
+                continue;
+            }
+            ++st.nodes;
+            const DevBlas& B = L.scenes[si].inst[inst_cur].b;
+            float tn[8];
+            uint32_t base, pbase, m0, m1;
+            uint32_t mask = test_node<kQuant>(B.nodes, e.x, R, h.t, tn, &base, &pbase, &m0, &m1);
+            if (!mask) continue;
+            uint32_t key[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                key[q] = (mask >> q) & 1u ? ((__float_as_uint(fmaxf(tn[q], 0.0f)) & ~7u) | uint32_t(q)) : 0xffffffffu;
+            cswap(key[0], key[2]); cswap(key[1], key[3]); cswap(key[4], key[6]); cswap(key[5], key[7]);
+            cswap(key[0], key[4]); cswap(key[1], key[5]); cswap(key[2], key[6]); cswap(key[3], key[7]);
+            cswap(key[0], key[1]); cswap(key[2], key[3]); cswap(key[4], key[5]); cswap(key[6], key[7]);
+            cswap(key[2], key[4]); cswap(key[3], key[5]);
+            cswap(key[1], key[4]); cswap(key[3], key[6]);
+            cswap(key[1], key[2]); cswap(key[3], key[4]); cswap(key[5], key[6]);
+            int npush = __popc(mask);
+            if (sp + npush > kStackSize) {
+                err |= kErrStackOverflow;
+                sp = 0;
+                continue;
+            }
+#pragma unroll
+            for (int k = 7; k >= 0; --k) {
+                if (k >= npush) continue;
+                uint32_t q = key[k] & 7u;
+                uint32_t m = ((q < 4 ? m0 : m1) >> (8 * (q & 3))) & 0xffu;
+                uint32_t ref = (m & 0x80u) ? base + (m & 7u)
+                                           : (kLeafFlag | ((pbase + (m & 31u)) << 2) | ((m >> 5) - 1u));
+                push(make_uint2(ref, key[k] & ~7u));
+            }
+        }
+        // ---- leaf phase
+        if (have_leaf) {
+            have_leaf = false;
+            const DevBlas& B = L.scenes[si].inst[inst_cur].b;
+            uint32_t first = (leaf & ~kLeafFlag) >> 2, cnt = (leaf & 3u) + 1u;
+            for (uint32_t j = 0; j < cnt; ++j) {
+                uint32_t slot = first + j;
+                if (shadow && inst_cur == skip_inst && slot == skip_slot) continue;
+                ++st.prims;
+                if (leaf_test<kType>(B, slot, inst_cur, R, h, L.fp64_resolve != 0, st) && shadow) {
+                    shadow_hit = true;
+                    sp = 0;
+                    break;
+                }
+            }
+        }
+        // ---- completion
+        if (has_ray && !have_leaf && sp == 0) {
+            if (err) {  // a bounded loop gave up: drop the task and stop taking work
+                atomicOr(&L.counters->error, err);
+                has_ray = false;
+                fetch_done = true;
+                continue;
+            }
+            bool more = false;
+            if (!(shadow && shadow_hit)) {
+                const uint32_t n = L.scenes[si].ninst;
+                while (++inst_cur < n)
+                    if (setup_instance(inst_cur)) { more = true; break; }
+            }
+            if (!more) finish_phase();
+        }
     }
     warp_add(&L.counters->shadow, shadow_rays);
     if (L.count_stats) {
@@ -788,21 +983,37 @@ __global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance*
     if (err) atomicOr(&ctr->error, err);
 }
 
-}  // namespace
-
-cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count) {
+template <bool kQuant, int kType, int kMinBlocks>
+cudaError_t launch_frame(const TraceLaunch& L, cudaStream_t s, int sm_count) {
     int per_sm = 0;
-    cudaError_t e = quantised_nodes
-                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<true>, kThreads, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<false>, kThreads, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_kernel<kQuant, kType, kMinBlocks>,
+                                                                  kThreads, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     unsigned grid = unsigned(sm_count * per_sm);
     uint64_t max_blocks = (L.total_work + kThreads - 1) / kThreads;
     if (grid > max_blocks) grid = unsigned(max_blocks ? max_blocks : 1);
-    if (quantised_nodes) trace_kernel<true><<<grid, kThreads, 0, s>>>(L);
-    else trace_kernel<false><<<grid, kThreads, 0, s>>>(L);
+    frame_kernel<kQuant, kType, kMinBlocks><<<grid, kThreads, 0, s>>>(L);
     return cudaGetLastError();
+}
+
+template <bool kQuant, int kMinBlocks>
+cudaError_t launch_kind(const TraceLaunch& L, cudaStream_t s, int sm_count) {
+    switch (L.prim_kind) {  // one primitive type in every instance -> the specialised kernel
+        case HRT_BLAS_PHANTOM: return launch_frame<kQuant, HRT_BLAS_PHANTOM, kMinBlocks>(L, s, sm_count);
+        case HRT_BLAS_LSS: return launch_frame<kQuant, HRT_BLAS_LSS, kMinBlocks>(L, s, sm_count);
+        case HRT_BLAS_DOTS: return launch_frame<kQuant, HRT_BLAS_DOTS, kMinBlocks>(L, s, sm_count);
+        default: return launch_frame<kQuant, kMixed, kMinBlocks>(L, s, sm_count);
+    }
+}
+
+}  // namespace
+
+// variant: 0 default (4 resident blocks per SM), 1 = 4, 2 = 3 (more registers per thread).
+cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count) {
+    bool three = L.variant == 2;
+    if (quantised_nodes) return three ? launch_kind<true, 3>(L, s, sm_count) : launch_kind<true, 4>(L, s, sm_count);
+    return three ? launch_kind<false, 3>(L, s, sm_count) : launch_kind<false, 4>(L, s, sm_count);
 }
 
 cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n, float tmin,
