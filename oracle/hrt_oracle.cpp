@@ -259,8 +259,8 @@ template <class T> T sphere_roots(tvec3<T> o, tvec3<T> d, tvec3<T> c, T r, T tmi
     tvec3<T> oc = o - c;
     T A = shim::dot(d, d);
     T B = shim::dot(oc, d);
-    T C = shim::dot(oc, oc) - r * r;
-    T h = B * B - A * C;
+    tvec3<T> cx = shim::cross(oc, d);
+    T h = r * r * A - shim::dot(cx, cx);  // = B^2 - A (|oc|^2 - r^2) by Lagrange's identity
     if (h < T(0)) return best;
     T sh = std::sqrt(h);
     T t0 = (-B - sh) / A;
@@ -284,12 +284,15 @@ T lss_intersect(tvec3<T> o_in, tvec3<T> d, tvec3<T> a, tvec3<T> b, T ra, T rb, T
     T dr = rb - ra;
     T m = L2 - dr * dr;
     if (m > T(0)) {
-        T dd = shim::dot(d, d);
+        // coefficients through c1 = ba x oa, c2 = ba x d (Lagrange's identity), free of the
+        // cancellation of m |oa|^2 - yo^2
+        tvec3<T> c1 = shim::cross(ba, oa), c2 = shim::cross(ba, d);
         T yd = shim::dot(ba, d);
-        T yo = shim::dot(ba, oa) + ra * dr;
-        T A = m * dd - yd * yd;
-        T B = m * shim::dot(oa, d) - yo * yd;
-        T C = m * shim::dot(oa, oa) - yo * yo - m * ra * ra;
+        T ybo = shim::dot(ba, oa);
+        T yo = ybo + ra * dr;
+        T A = shim::dot(c2, c2) - dr * dr * shim::dot(d, d);
+        T B = shim::dot(c1, c2) - dr * dr * shim::dot(oa, d) - ra * dr * yd;
+        T C = shim::dot(c1, c1) - dr * dr * shim::dot(oa, oa) - T(2) * ra * dr * ybo - ra * ra * L2;
         T h = B * B - A * C;
         if (h >= T(0) && A != T(0)) {
             T sh = std::sqrt(h);

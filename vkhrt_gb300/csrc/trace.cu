@@ -190,9 +190,12 @@ __device__ __noinline__ void prhi_fp64(float ox, float oy, float oz, float dx, f
 // Envelope of spheres a + u (b-a), radius ra + u (rb-ra): tangent-cone roots with u in [0,1]
 // and both end spheres; the least t >= tmin wins. Solved from o' = o + ts d (the ray point
 // nearest the segment midpoint) on the full-precision vectors a - o', b - o'; t = ts + t'.
+// Quadratic coefficients are formed with cross products (Lagrange's identity) so that no term
+// is the small difference of two large ones: for the sphere, h = r^2 |d|^2 - |oc x d|^2.
 __device__ __forceinline__ float sphere_hit(V3<float> oc, V3<float> d, float r, float tmin, float best) {
-    float A = dot(d, d), B = dot(oc, d), C = dot(oc, oc) - r * r;
-    float h = B * B - A * C;
+    float A = dot(d, d), B = dot(oc, d);
+    V3<float> c = cross(oc, d);
+    float h = r * r * A - dot(c, c);
     if (h < 0.0f) return best;
     float sh = sqrtf(h);
     float t0 = (-B - sh) / A, t1 = (-B + sh) / A;
@@ -200,6 +203,10 @@ __device__ __forceinline__ float sphere_hit(V3<float> oc, V3<float> d, float r, 
     if (t1 >= tmin && t1 < best) return t1;
     return best;
 }
+// Tangent cone: m |P-a|^2 - (y + ra dr)^2 - m ra^2 = 0 with y = (b-a).(P-a), m = L^2 - dr^2;
+// with c1 = ba x oa and c2 = ba x d the quadratic A t^2 + 2 B t + C has
+//   A = |c2|^2 - dr^2 |d|^2,  B = c1.c2 - dr^2 (oa.d) - ra dr (ba.d),
+//   C = |c1|^2 - dr^2 |oa|^2 - 2 ra dr (ba.oa) - ra^2 L^2.
 __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> a, V3<float> b, float ra, float rb,
                                          float tmin_in, float* u_out, float* tl_out, float* ts_out) {
     const float kNone = __int_as_float(0x7f800000);
@@ -211,13 +218,15 @@ __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> 
     float best = kNone, bu = 0.0f;
     V3<float> ba = b - a;
     float dr = rb - ra;
-    float m = dot(ba, ba) - dr * dr;
+    float L2 = dot(ba, ba);
+    float m = L2 - dr * dr;
     if (m > 0.0f) {
-        float yd = dot(ba, d);
-        float yo = dot(ba, oa) + ra * dr;
-        float A = m * dot(d, d) - yd * yd;
-        float B = m * dot(oa, d) - yo * yd;
-        float C = m * dot(oa, oa) - yo * yo - m * ra * ra;
+        V3<float> c1 = cross(ba, oa), c2 = cross(ba, d);
+        float yd = dot(ba, d), ybo = dot(ba, oa);
+        float yo = ybo + ra * dr;
+        float A = dot(c2, c2) - dr * dr * dot(d, d);
+        float B = dot(c1, c2) - dr * dr * dot(oa, d) - ra * dr * yd;
+        float C = dot(c1, c1) - dr * dr * dot(oa, oa) - 2.0f * ra * dr * ybo - ra * ra * L2;
         float h = B * B - A * C;
         if (h >= 0.0f && A != 0.0f) {
             float sh = sqrtf(h);
