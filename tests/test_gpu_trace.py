@@ -213,3 +213,20 @@ def test_generator_checksum_on_this_host():
     from test_abi import C1_CHECKSUM
     v, r, _ = H.generate_strands(H.StrandParams())
     assert H.checksum(v, r) == C1_CHECKSUM
+
+
+def test_quantised_node_visits_close_to_fp32(ctx):
+    """The 8-bit boxes are the FP32 boxes rounded outward: same tree, a few more visits at most.
+    Shadow rays run along +y, so some slab distances use the clamped reciprocal of a zero."""
+    v, r, off = H.generate_strands(H.StrandParams(seed=35, nstrands=3000, nverts=48))
+    stats = {}
+    for prec in (H.Precision.FP32, H.Precision.QUANTISED):
+        b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r,
+                                                           strand_offsets=off, precision=prec), ctx)
+        t = H.TopLevelAccelerationStructure([b], ctx)
+        fr = H.Frame(ctx, 192, 128, 1)
+        H.trace(ctx, t, H.scene_camera(192, 128), fr, H.trace_params(shading=2, count_stats=1))
+        stats[int(prec)] = fr.stats()
+    f, q = stats[0], stats[1]
+    assert f["shadow_rays"] == q["shadow_rays"] > 1000
+    assert f["nodes_visited"] <= q["nodes_visited"] <= 1.3 * f["nodes_visited"]

@@ -424,60 +424,93 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
 // ---------------------------------------------------------------- nodes
 __device__ __forceinline__ float bytef(uint32_t w, int k) { return float((w >> (8 * k)) & 0xffu); }
 
+// Reciprocal direction with zero components replaced by +-1e20, so slab distances stay finite
+// (a ray inside a slab gets -huge..+huge, one outside a pair of equal signs).
+__device__ __forceinline__ V3<float> safe_inv(V3<float> d) {
+    auto r = [](float x) { return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
+    return mk(r(d.x), r(d.y), r(d.z));
+}
+// float of byte k of w: the byte placed under the exponent of 2^23, then 2^23 subtracted.
+__device__ __forceinline__ float byte_to_float(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(k))) - 8388608.0f;
+}
+
 // Child entry distances of one node; returns a bit mask of hit children and fills tn[8].
+// Near and far planes are chosen per axis by the sign of the direction (octant), so a child
+// needs three maxima and three minima. FP32 boxes: t = (plane - o) inv, accepted when
+// tnear <= tfar (1 + 2^-20). 8-bit boxes: t = q (2^e inv) + (p - o) inv, one fused operation
+// per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 255 2^e |inv|), and that
+// bound is subtracted from the axis's near planes and added to its far planes, so a box is
+// never lost to rounding (a near-parallel axis widens only its own planes).
 template <bool kQuant>
 __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, const RayState& R, float tfar,
                                               float* tn, uint32_t* base, uint32_t* pbase, uint32_t* m0, uint32_t* m1) {
     uint32_t mask = 0;
-    const float kEps = 1.0f + 9.5367431640625e-07f;  // 1 + 2^-20: rounding can only admit more boxes
+    const bool nx = R.inv.x < 0.0f, ny = R.inv.y < 0.0f, nz = R.inv.z < 0.0f;
     if (!kQuant) {
+        const float kEps = 1.0f + 9.5367431640625e-07f;  // 1 + 2^-20
         const float4* p = reinterpret_cast<const float4*>(static_cast<const NodeF*>(nodes) + ni);
-        float4 L[12];
-#pragma unroll
-        for (int k = 0; k < 12; ++k) L[k] = __ldg(p + k);
+        // float4 index of lo_x, hi_x, lo_y, hi_y, lo_z, hi_z: 0, 2, 4, 6, 8, 10
+        const int ax = nx ? 2 : 0, ay = ny ? 6 : 4, az = nz ? 10 : 8;
+        float4 n0 = __ldg(p + ax), n1 = __ldg(p + ax + 1), f0 = __ldg(p + (2 - ax)), f1 = __ldg(p + (3 - ax));
+        float4 n2 = __ldg(p + ay), n3 = __ldg(p + ay + 1), f2 = __ldg(p + (10 - ay)), f3 = __ldg(p + (11 - ay));
+        float4 n4 = __ldg(p + az), n5 = __ldg(p + az + 1), f4 = __ldg(p + (18 - az)), f5 = __ldg(p + (19 - az));
         float4 tail = __ldg(p + 12);
         *base = __float_as_uint(tail.x);
         *pbase = __float_as_uint(tail.y);
         *m0 = __float_as_uint(tail.z);
         *m1 = __float_as_uint(tail.w);
-        const float* f = reinterpret_cast<const float*>(L);
+        const float NX[8] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, n1.z, n1.w};
+        const float FX[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
+        const float NY[8] = {n2.x, n2.y, n2.z, n2.w, n3.x, n3.y, n3.z, n3.w};
+        const float FY[8] = {f2.x, f2.y, f2.z, f2.w, f3.x, f3.y, f3.z, f3.w};
+        const float NZ[8] = {n4.x, n4.y, n4.z, n4.w, n5.x, n5.y, n5.z, n5.w};
+        const float FZ[8] = {f4.x, f4.y, f4.z, f4.w, f5.x, f5.y, f5.z, f5.w};
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            float x0 = (f[q] - R.o.x) * R.inv.x, x1 = (f[8 + q] - R.o.x) * R.inv.x;
-            float y0 = (f[16 + q] - R.o.y) * R.inv.y, y1 = (f[24 + q] - R.o.y) * R.inv.y;
-            float z0 = (f[32 + q] - R.o.z) * R.inv.z, z1 = (f[40 + q] - R.o.z) * R.inv.z;
-            float a = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), R.tmin));
-            float b = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tfar));
+            float a = fmaxf(fmaxf((NX[q] - R.o.x) * R.inv.x, (NY[q] - R.o.y) * R.inv.y),
+                            fmaxf((NZ[q] - R.o.z) * R.inv.z, R.tmin));
+            float b = fminf(fminf((FX[q] - R.o.x) * R.inv.x, (FY[q] - R.o.y) * R.inv.y),
+                            fminf((FZ[q] - R.o.z) * R.inv.z, tfar));
             tn[q] = a;
             if (a <= b * kEps) mask |= 1u << q;
         }
     } else {
         const uint4* p = reinterpret_cast<const uint4*>(static_cast<const NodeQ*>(nodes) + ni);
         uint4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
-        float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
-        float sx = __uint_as_float((w0.w & 0xffu) << 23);
-        float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
-        float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+        // per node: s = 2^e inv, b = (p - o) inv
+        float sx = __uint_as_float((w0.w & 0xffu) << 23) * R.inv.x;
+        float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * R.inv.y;
+        float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * R.inv.z;
+        float bx = (__uint_as_float(w0.x) - R.o.x) * R.inv.x;
+        float by = (__uint_as_float(w0.y) - R.o.y) * R.inv.y;
+        float bz = (__uint_as_float(w0.z) - R.o.z) * R.inv.z;
+        // per-axis rounding bound, folded into the offsets: near planes move down, far planes up
+        const float kS = 9.5367431640625e-07f;  // 2^-20
+        float ex = kS * fmaf(255.0f, fabsf(sx), fabsf(bx));
+        float ey = kS * fmaf(255.0f, fabsf(sy), fabsf(by));
+        float ez = kS * fmaf(255.0f, fabsf(sz), fabsf(bz));
+        const float bxn = bx - ex, bxf = bx + ex, byn = by - ey, byf = by + ey, bzn = bz - ez, bzf = bz + ez;
         *base = w1.x;
         *pbase = w1.y;
         *m0 = w1.z;
         *m1 = w1.w;
-        uint32_t qlx[2] = {w2.x, w2.y}, qhx[2] = {w2.z, w2.w};
-        uint32_t qly[2] = {w3.x, w3.y}, qhy[2] = {w3.z, w3.w};
-        uint32_t qlz[2] = {w4.x, w4.y}, qhz[2] = {w4.z, w4.w};
+        // near / far byte words per axis (qlo = .x .y, qhi = .z .w)
+        const uint32_t nxw0 = nx ? w2.z : w2.x, nxw1 = nx ? w2.w : w2.y, fxw0 = nx ? w2.x : w2.z, fxw1 = nx ? w2.y : w2.w;
+        const uint32_t nyw0 = ny ? w3.z : w3.x, nyw1 = ny ? w3.w : w3.y, fyw0 = ny ? w3.x : w3.z, fyw1 = ny ? w3.y : w3.w;
+        const uint32_t nzw0 = nz ? w4.z : w4.x, nzw1 = nz ? w4.w : w4.y, fzw0 = nz ? w4.x : w4.z, fzw1 = nz ? w4.y : w4.w;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            int wd = q >> 2, by = q & 3;
-            float lx = fmaf(bytef(qlx[wd], by), sx, px), hx = fmaf(bytef(qhx[wd], by), sx, px);
-            float ly = fmaf(bytef(qly[wd], by), sy, py), hy = fmaf(bytef(qhy[wd], by), sy, py);
-            float lz = fmaf(bytef(qlz[wd], by), sz, pz), hz = fmaf(bytef(qhz[wd], by), sz, pz);
-            float x0 = (lx - R.o.x) * R.inv.x, x1 = (hx - R.o.x) * R.inv.x;
-            float y0 = (ly - R.o.y) * R.inv.y, y1 = (hy - R.o.y) * R.inv.y;
-            float z0 = (lz - R.o.z) * R.inv.z, z1 = (hz - R.o.z) * R.inv.z;
-            float a = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), R.tmin));
-            float b = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tfar));
+            const int by_ = q & 3;
+            const uint32_t wnx = q < 4 ? nxw0 : nxw1, wfx = q < 4 ? fxw0 : fxw1;
+            const uint32_t wny = q < 4 ? nyw0 : nyw1, wfy = q < 4 ? fyw0 : fyw1;
+            const uint32_t wnz = q < 4 ? nzw0 : nzw1, wfz = q < 4 ? fzw0 : fzw1;
+            float a = fmaxf(fmaxf(fmaf(byte_to_float(wnx, by_), sx, bxn), fmaf(byte_to_float(wny, by_), sy, byn)),
+                            fmaxf(fmaf(byte_to_float(wnz, by_), sz, bzn), R.tmin));
+            float b = fminf(fminf(fmaf(byte_to_float(wfx, by_), sx, bxf), fmaf(byte_to_float(wfy, by_), sy, byf)),
+                            fminf(fmaf(byte_to_float(wfz, by_), sz, bzf), tfar));
             tn[q] = a;
-            if (a <= b * kEps) mask |= 1u << q;
+            if (a <= b) mask |= 1u << q;
         }
     }
     // empty slots never count
@@ -573,7 +606,7 @@ __device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> 
             R.d = mk(m[0] * wd.x + m[1] * wd.y + m[2] * wd.z, m[4] * wd.x + m[5] * wd.y + m[6] * wd.z,
                      m[8] * wd.x + m[9] * wd.y + m[10] * wd.z);
         }
-        R.inv = mk(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
+        R.inv = safe_inv(R.d);
         R.tmin = tmin;
         // instance bounds (object space) against the current closest distance
         {
@@ -751,7 +784,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             R.d = mk(m[0] * wd.x + m[1] * wd.y + m[2] * wd.z, m[4] * wd.x + m[5] * wd.y + m[6] * wd.z,
                      m[8] * wd.x + m[9] * wd.y + m[10] * wd.z);
         }
-        R.inv = mk(1.0f / R.d.x, 1.0f / R.d.y, 1.0f / R.d.z);
+        R.inv = safe_inv(R.d);
         R.tmin = cur_tmin;
         const DevBlas& B = I.b;
         if (B.nnodes == 0) return false;
