@@ -220,6 +220,23 @@ hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* c
 hrt_status hrt_trace_rays(hrt_context* ctx, const hrt_tlas* tlas, const float* rays, uint64_t n,
                           const hrt_trace_params* p, hrt_hit* hits, int32_t memory, void* stream);
 
+/* ---- closest hit without any device allocation -----------------------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device memory: a picking or
+ * probing query issued from an interactive loop, where cudaFree's implicit device-wide
+ * synchronisation would stall frames in flight, or an integration that runs under a fixed
+ * device-memory budget. Same closest-hit kernel and results as hrt_trace_rays, with rays and
+ * hits in HOST memory (n x {ox, oy, oz, dx, dy, dz} floats in, n hrt_hit out); the device
+ * staging for both and the kernel's counters live in one static device array of
+ * HRT_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until the process exits.
+ * n above HRT_NOALLOC_MAX_RAYS is rejected with HRT_ERR_INVALID_ARG. The first call on a device
+ * looks up the array's device address (make that call before any stream capture). Every call
+ * shares the array: calls that overlap on the GPU (other streams, other host threads) race, so
+ * serialise them; each call synchronises `stream` before it returns. */
+#define HRT_NOALLOC_MAX_RAYS 65536u
+#define HRT_NOALLOC_SCRATCH_BYTES (256u + HRT_NOALLOC_MAX_RAYS * 40u)
+hrt_status hrt_trace_rays_noalloc(hrt_context* ctx, const hrt_tlas* tlas, const float* rays, uint64_t n,
+                                  const hrt_trace_params* p, hrt_hit* hits, void* stream);
+
 /* ---- batched multi-scene rendering ---------------------------------------------------------
  * All scenes are traced by one persistent launch, captured once in a CUDA graph by
  * hrt_batch_create and replayed by hrt_batch_launch. */

@@ -90,6 +90,7 @@ SIGNATURES = {
     "hrt_frame_get_stats": (c_i32, [c_p, ctypes.POINTER(FrameStatsC)]),
     "hrt_trace": (c_i32, [c_p, c_p, ctypes.POINTER(CameraC), ctypes.POINTER(TraceParamsC), c_p, c_p]),
     "hrt_trace_rays": (c_i32, [c_p, c_p, c_p, c_u64, ctypes.POINTER(TraceParamsC), c_p, c_i32, c_p]),
+    "hrt_trace_rays_noalloc": (c_i32, [c_p, c_p, c_p, c_u64, ctypes.POINTER(TraceParamsC), c_p, c_p]),
     "hrt_batch_create": (c_i32, [c_p, ctypes.POINTER(SceneDescC), c_u32, ctypes.POINTER(TraceParamsC), c_p,
                                  ctypes.POINTER(c_p)]),
     "hrt_batch_launch": (c_i32, [c_p, c_p]),
@@ -381,6 +382,21 @@ def trace_rays(ctx: Context, tlas: TopLevelAccelerationStructure, rays: np.ndarr
     hits = np.zeros(r.shape[0], HIT_DTYPE)
     p = params if params is not None else trace_params()
     ctx.check(ctx.lib.hrt_trace_rays(ctx.handle, tlas.handle, _ptr(r), r.shape[0], ctypes.byref(p), _ptr(hits), 0, None))
+    return hits
+
+
+NOALLOC_MAX_RAYS = 65536
+
+
+def trace_rays_noalloc(ctx: Context, tlas: TopLevelAccelerationStructure, rays: np.ndarray,
+                       params: TraceParamsC | None = None) -> np.ndarray:
+    """hrt_trace_rays_noalloc: closest hit for at most NOALLOC_MAX_RAYS host rays without any
+    device allocation (for callers that cannot call cudaMalloc/cudaFree; see include/hrt.h)."""
+    r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    hits = np.zeros(r.shape[0], HIT_DTYPE)
+    p = params if params is not None else trace_params()
+    ctx.check(ctx.lib.hrt_trace_rays_noalloc(ctx.handle, tlas.handle, _ptr(r), r.shape[0], ctypes.byref(p), _ptr(hits),
+                                             None))
     return hits
 
 

@@ -738,6 +738,24 @@ hrt_status hrt_trace_rays(hrt_context* ctx, const hrt_tlas* tlas, const float* r
     return st;
 }
 
+hrt_status hrt_trace_rays_noalloc(hrt_context* ctx, const hrt_tlas* tlas, const float* rays, uint64_t n,
+                                  const hrt_trace_params* p, hrt_hit* hits, void* stream) {
+    if (!ctx) return HRT_ERR_INVALID_ARG;
+    if (!tlas || !p || (n && (!rays || !hits))) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays_noalloc: null argument");
+    if (n > HRT_NOALLOC_MAX_RAYS)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays_noalloc: %llu rays; at most %u per call",
+                    (unsigned long long)n, HRT_NOALLOC_MAX_RAYS);
+    DeviceSet ds(ctx->device);
+    uint32_t err = 0;
+    cudaError_t e = trace_rays_noalloc(ctx->device, tlas->dev, tlas->n, tlas->quantised, rays, n, p->tmin, p->tmax,
+                                       p->fp64_resolve, hits, static_cast<cudaStream_t>(stream), ctx->sm_count, &err);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "hrt_trace_rays_noalloc");
+    if (err & kErrStackOverflow)
+        return fail(ctx, HRT_ERR_STACK_OVERFLOW, "traversal stack of %d entries overflowed", kStackSize);
+    if (err & kErrTimeout) return fail(ctx, HRT_ERR_TIMEOUT, "a traversal exceeded %u steps", kMaxTraversalSteps);
+    return HRT_OK;
+}
+
 hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* p,
                             void* stream, hrt_batch** out) {
     if (!ctx) return HRT_ERR_INVALID_ARG;

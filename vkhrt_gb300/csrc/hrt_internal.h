@@ -104,6 +104,12 @@ cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const flo
                               float tmin, float tmax, uint32_t fp64_resolve, hrt_hit* hits,
                               TraceCounters* counters, bool quantised_nodes, cudaStream_t s, int sm_count);
 
+// Closest hit for host rays through the static scratch array of trace.cu (no allocation);
+// error_word receives the device error bits.
+cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, uint32_t ninst, bool quantised_nodes,
+                               const float* host_rays, uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
+                               hrt_hit* host_hits, cudaStream_t s, int sm_count, uint32_t* error_word);
+
 // ---- BVH build (build.cu) ----------------------------------------------------------------------
 struct BuildInput {
     int type, precision, max_leaf;
