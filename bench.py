@@ -263,7 +263,8 @@ def run_ours(args, dist):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     blas = H.BottomLevelAccelerationStructure(
-        H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=cfg["precision"]), ctx)
+        H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=cfg["precision"],
+                    max_leaf=args.max_leaf), ctx)
     tlas = H.TopLevelAccelerationStructure([blas], ctx)
     build_wall = time.perf_counter() - t0
     cam = H.scene_camera(w, h)
@@ -296,9 +297,11 @@ def run_ours(args, dist):
                 "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
                 "bytes_per_launch": int(alg_bytes), "nodes_visited": int(st["nodes_visited"]),
                 "prims_tested": int(st["prims_tested"]), "node_bytes": int(node_b), "prim_bytes": int(prim_b)}
+    tot = st["warp_cycles_node"] + st["warp_cycles_leaf"] + st["warp_cycles_other"]
+    phase = {k: round(st["warp_cycles_" + k] / tot, 4) for k in ("node", "leaf", "other")} if tot else None
     if args.profile:
         print(json.dumps({"profile": True, "ms_per_step": round(ms, 3), "rays_per_step": int(rays_per_step),
-                          "value": round(value, 3), "roofline": roofline}), flush=True)
+                          "value": round(value, 3), "roofline": roofline, "phase_share": phase}), flush=True)
         dist.close()
         return
     # ---- e2e: C ABI per frame, camera in, framebuffer to pinned host memory ----
@@ -324,14 +327,15 @@ def run_ours(args, dist):
             "config": config_block(cfg, args.config), "rays_per_step": int(rays_per_step),
             "primary_rays_per_step": int(st["primary_rays"]), "shadow_rays_per_step": int(st["shadow_rays"]),
             "fp64_resolves_per_step": int(st["fp64_resolves"]), "gpu_launches": args.steps,
-            "roofline": roofline, "e2e": e2e, "clocks": clk,
+            "roofline": roofline, "phase_share": phase, "e2e": e2e, "clocks": clk,
             "build": {"blas_build_ms": round(info["build_ms"], 2), "build_wall_s": round(build_wall, 3),
                       "strand_generation_s": round(t_gen, 3), "nodes": int(info["nnodes"]),
                       "device_bytes": int(info["device_bytes"])}}
     # ---- plain FP32 tracer on the same strands (the comparison the metric names) ----
     if not args.quick and int(cfg["precision"]) == 1:
         blas32 = H.BottomLevelAccelerationStructure(
-            H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=H.Precision.FP32), ctx)
+            H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=H.Precision.FP32,
+                        max_leaf=args.max_leaf), ctx)
         tlas32 = H.TopLevelAccelerationStructure([blas32], ctx)
         f32 = H.Frame(ctx, w, h, spp, with_hits=False)
         H.trace(ctx, tlas32, cam, f32, H.trace_params(spp=spp, jitter=1, seed=17, shading=2,
@@ -386,6 +390,7 @@ def main():
     ap.add_argument("--precision", choices=["fp32", "quantised"], default=None,
                     help="override the workload's BVH/primitive precision (profiling)")
     ap.add_argument("--variant", type=int, default=0, help="trace kernel variant (0 default, 1, 2)")
+    ap.add_argument("--max-leaf", type=int, default=1, help="primitives per BVH8 leaf (1..3)")
     ap.add_argument("--profile", action="store_true",
                     help="one warm-up and the timed steps only: no e2e, FP32 comparison or CPU legs")
     args = ap.parse_args()

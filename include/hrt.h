@@ -168,6 +168,9 @@ typedef struct hrt_frame_stats {
     uint64_t prims_tested;    /* with count_stats */
     uint64_t fp64_resolves;   /* FP64 re-solves run */
     uint64_t fp64_hits;       /* re-solves that produced a hit */
+    uint64_t warp_cycles_node;  /* with count_stats: summed per-warp SM clocks in the node phase, */
+    uint64_t warp_cycles_leaf;  /* the intersector (leaf) phase */
+    uint64_t warp_cycles_other; /* and ray setup, shading and work fetch */
 } hrt_frame_stats;
 
 /* ---- context ------------------------------------------------------------------------- */

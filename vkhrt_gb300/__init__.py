@@ -50,7 +50,8 @@ class TraceParamsC(ctypes.Structure):
 
 class FrameStatsC(ctypes.Structure):
     _fields_ = [("primary_rays", c_u64), ("shadow_rays", c_u64), ("nodes_visited", c_u64),
-                ("prims_tested", c_u64), ("fp64_resolves", c_u64), ("fp64_hits", c_u64)]
+                ("prims_tested", c_u64), ("fp64_resolves", c_u64), ("fp64_hits", c_u64),
+                ("warp_cycles_node", c_u64), ("warp_cycles_leaf", c_u64), ("warp_cycles_other", c_u64)]
 
 
 class SceneDescC(ctypes.Structure):

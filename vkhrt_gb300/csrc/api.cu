@@ -154,6 +154,9 @@ void counters_to_stats(const TraceCounters& c, uint64_t primary, hrt_frame_stats
     st->prims_tested = c.prims;
     st->fp64_resolves = c.fp64_resolves;
     st->fp64_hits = c.fp64_hits;
+    st->warp_cycles_node = c.cycles_node;
+    st->warp_cycles_leaf = c.cycles_leaf;
+    st->warp_cycles_other = c.cycles_other;
 }
 
 void fill_scene(SceneLaunch& sl, const hrt_tlas* t, const hrt_camera* cam, hrt_frame* f, uint64_t work_begin) {

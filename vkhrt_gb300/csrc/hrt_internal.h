@@ -83,6 +83,7 @@ struct SceneLaunch {
 struct TraceCounters {
     unsigned long long work;     // next work item
     unsigned long long primary, shadow, nodes, prims, fp64_resolves, fp64_hits;
+    unsigned long long cycles_node, cycles_leaf, cycles_other;  // per-warp clock, with count_stats
     uint32_t error;
     uint32_t pad;
 };

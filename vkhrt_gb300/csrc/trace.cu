@@ -879,6 +879,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         next_sample();
     };
 
+    unsigned long long cyc_node = 0, cyc_leaf = 0, cyc_other = 0;
+    long long clk = clock64();
     for (;;) {
         // ---- refill idle lanes
         uint32_t idle = __ballot_sync(kFull, !has_ray);
@@ -912,6 +914,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             if (fetch_done) break;
             continue;
         }
+        if (L.count_stats) { long long c = clock64(); cyc_other += c - clk; clk = c; }
         // ---- node phase
         for (;;) {
             bool want = has_ray && !have_leaf && sp > 0;
@@ -961,6 +964,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 push(make_uint2(ref, key[k] & ~7u));
             }
         }
+        if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_node += c - clk; clk = c; }
         // ---- leaf phase
         if (have_leaf) {
             have_leaf = false;
@@ -977,6 +981,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 }
             }
         }
+        if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_leaf += c - clk; clk = c; }
         // ---- completion
         if (has_ray && !have_leaf && sp == 0) {
             if (err) {  // a bounded loop gave up: drop the task and stop taking work
@@ -998,6 +1003,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     if (L.count_stats) {
         warp_add(&L.counters->nodes, st.nodes);
         warp_add(&L.counters->prims, st.prims);
+        cyc_other += clock64() - clk;
+        if (lane == 0) {  // warp-level phase clocks
+            atomicAdd(&L.counters->cycles_node, cyc_node);
+            atomicAdd(&L.counters->cycles_leaf, cyc_leaf);
+            atomicAdd(&L.counters->cycles_other, cyc_other);
+        }
     }
     warp_add(&L.counters->fp64_resolves, st.r64);
     warp_add(&L.counters->fp64_hits, st.h64);
