@@ -199,6 +199,8 @@ TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32
     L.record_hits = p->record_hits;
     L.count_stats = p->count_stats;
     L.variant = p->kernel_variant;
+    L.refill = p->refill > 32 ? 32 : p->refill;
+    L.speculative = p->speculative;
     L.counters = c;
     return L;
 }

@@ -96,6 +96,8 @@ struct TraceLaunch {
     uint32_t jitter, seed, shading, fp64_resolve, record_hits, count_stats;
     uint32_t prim_kind;  // the primitive type of every instance, or 3 when they differ
     uint32_t variant;    // kernel variant (occupancy / register split), 0 = default
+    uint32_t refill;     // idle lanes of a warp that trigger a work fetch (0 = 16)
+    uint32_t speculative;  // lanes holding a leaf keep traversing while others search
     TraceCounters* counters;
 };
 

@@ -879,12 +879,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         next_sample();
     };
 
+    const int refill = L.refill ? int(L.refill) : kRefill;  // idle lanes that trigger a fetch
+    const bool spec = L.speculative != 0;
     unsigned long long cyc_node = 0, cyc_leaf = 0, cyc_other = 0;
     long long clk = clock64();
     for (;;) {
         // ---- refill idle lanes
         uint32_t idle = __ballot_sync(kFull, !has_ray);
-        if (idle && !fetch_done && (__popc(idle) >= kRefill || idle == kFull)) {
+        if (idle && !fetch_done && (__popc(idle) >= refill || idle == kFull)) {
             int n = __popc(idle), leader = __ffs(idle) - 1;
             unsigned long long base = 0;
             if (lane == leader) base = *errword ? L.total_work : atomicAdd(&L.counters->work, (unsigned long long)n);
@@ -915,10 +917,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             continue;
         }
         if (L.count_stats) { long long c = clock64(); cyc_other += c - clk; clk = c; }
-        // ---- node phase
+        // ---- node phase: runs while some lane still searches for a leaf; with speculation,
+        // lanes that already hold one keep walking nodes (a second leaf goes back on the stack)
+        bool stalled = false;
         for (;;) {
-            bool want = has_ray && !have_leaf && sp > 0;
-            if (!__any_sync(kFull, want)) break;
+            bool searching = has_ray && !have_leaf && sp > 0;
+            if (!__any_sync(kFull, searching)) break;
+            bool want = searching || (spec && has_ray && have_leaf && !stalled && sp > 0);
             if (!want) continue;
             if (++steps > kMaxTraversalSteps) {
                 err |= kErrTimeout;
@@ -928,8 +933,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             uint2 e = pop();
             if (__uint_as_float(e.y) > h.t) continue;
             if (e.x & kLeafFlag) {
-                leaf = e.x;
-                have_leaf = true;
+                if (have_leaf) {  // speculative lane found a second leaf: keep it for later
+                    push(e);
+                    stalled = true;
+                } else {
+                    leaf = e.x;
+                    have_leaf = true;
+                }
                 continue;
             }
             ++st.nodes;
