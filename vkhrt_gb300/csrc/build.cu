@@ -605,7 +605,8 @@ __global__ void collapse_emit_kernel(BinView bv, const uint32_t* level, uint32_t
         nd.lo_x[q] = nd.hi_x[q] = nd.lo_y[q] = nd.hi_y[q] = nd.lo_z[q] = nd.hi_z[q] = 0.0f;
         nd.meta[q] = 0;
     }
-    for (int q = 0; q < 4; ++q) nd.pad[q] = 0;
+    nd.valid = 0;
+    for (int q = 0; q < 3; ++q) nd.pad[q] = 0;
     nd.child_base = next_node_base + int_off[w];
     nd.prim_base = prim_base_g + prim_off[w];
     uint32_t rank = 0, poff = 0;
@@ -616,6 +617,7 @@ __global__ void collapse_emit_kernel(BinView bv, const uint32_t* level, uint32_t
         nd.lo_x[q] = bx[0]; nd.lo_y[q] = bx[1]; nd.lo_z[q] = bx[2];
         nd.hi_x[q] = bx[3]; nd.hi_y[q] = bx[4]; nd.hi_z[q] = bx[5];
         uint32_t cnt = bcount(bv, c);
+        nd.valid |= 1u << q;
         if (!(c & kLeafFlag) && cnt > uint32_t(max_leaf)) {
             nd.meta[q] = uint8_t(0x80u | rank);
             next_level[int_off[w] + rank] = c;
@@ -645,7 +647,7 @@ __global__ void quantise_kernel(const NodeF* in, uint64_t nn, NodeQ* out) {
     float pp[3];
     uint8_t ee[3];
     uint32_t nc = 0;
-    for (int c = 0; c < 8; ++c) nc += a.meta[c] ? 1u : 0u;
+    for (int c = 0; c < 8; ++c) nc |= (a.meta[c] ? 1u : 0u) << c;
     for (int k = 0; k < 3; ++k) {
         float p = __int_as_float(0x7f800000), P = -__int_as_float(0x7f800000);
         for (int c = 0; c < 8; ++c) {
@@ -677,7 +679,7 @@ __global__ void quantise_kernel(const NodeF* in, uint64_t nn, NodeQ* out) {
     }
     q.px = pp[0]; q.py = pp[1]; q.pz = pp[2];
     q.ex = ee[0]; q.ey = ee[1]; q.ez = ee[2];
-    q.nchild = uint8_t(nc);
+    q.valid = uint8_t(nc);
     q.child_base = a.child_base;
     q.prim_base = a.prim_base;
     for (int c = 0; c < 8; ++c) q.meta[c] = a.meta[c];

@@ -25,14 +25,15 @@ struct alignas(16) NodeF {  // 224 bytes, FP32 child boxes (structure of arrays)
     float lo_x[8], hi_x[8], lo_y[8], hi_y[8], lo_z[8], hi_z[8];
     uint32_t child_base, prim_base;
     uint8_t meta[8];
-    uint32_t pad[4];
+    uint32_t valid;  // bit q set when slot q holds a child
+    uint32_t pad[3];
 };
 static_assert(sizeof(NodeF) == 224, "NodeF layout");
 
 struct alignas(16) NodeQ {  // 80 bytes, child boxes as 8-bit offsets on a per-axis 2^e grid
     float px, py, pz;       // grid origin (min of the child boxes)
     uint8_t ex, ey, ez;     // e + 127
-    uint8_t nchild;
+    uint8_t valid;          // bit q set when slot q holds a child
     uint32_t child_base, prim_base;
     uint8_t meta[8];
     uint8_t qlo_x[8], qhi_x[8], qlo_y[8], qhi_y[8], qlo_z[8], qhi_z[8];

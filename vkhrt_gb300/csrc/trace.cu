@@ -432,9 +432,9 @@ __device__ __forceinline__ V3<float> safe_inv(V3<float> d) {
     auto r = [](float x) { return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
     return mk(r(d.x), r(d.y), r(d.z));
 }
-// float of byte k of w: the byte placed under the exponent of 2^23, then 2^23 subtracted.
-__device__ __forceinline__ float byte_to_float(uint32_t w, int k) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(k))) - 8388608.0f;
+// 2^23 + (byte k of w) as a float: the byte placed under the exponent of 2^23.
+__device__ __forceinline__ float biased_byte(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(k)));
 }
 
 // Child entry distances of one node; returns a bit mask of hit children and fills tn[8].
@@ -462,6 +462,7 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         *pbase = __float_as_uint(tail.y);
         *m0 = __float_as_uint(tail.z);
         *m1 = __float_as_uint(tail.w);
+        const uint32_t valid = __float_as_uint(__ldg(reinterpret_cast<const float*>(p + 13)));
         const float NX[8] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, n1.z, n1.w};
         const float FX[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
         const float NY[8] = {n2.x, n2.y, n2.z, n2.w, n3.x, n3.y, n3.z, n3.w};
@@ -477,6 +478,7 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
             tn[q] = a;
             if (a <= b * kEps) mask |= 1u << q;
         }
+        return mask & valid;
     } else {
         const uint4* p = reinterpret_cast<const uint4*>(static_cast<const NodeQ*>(nodes) + ni);
         uint4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
@@ -487,12 +489,18 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         float bx = (__uint_as_float(w0.x) - R.o.x) * R.inv.x;
         float by = (__uint_as_float(w0.y) - R.o.y) * R.inv.y;
         float bz = (__uint_as_float(w0.z) - R.o.z) * R.inv.z;
-        // per-axis rounding bound, folded into the offsets: near planes move down, far planes up
+        // The byte q is read as the float 2^23 + q (byte permute under the exponent of 2^23), and
+        // the 2^23 is folded into the offset: t = (2^23 + q) s + (b - 2^23 s), one fused
+        // multiply-add per plane. Rounding of the offset costs at most |s| / 2; with the rest it
+        // is bounded by E = 2^-20 (|b| + 255 |s|) + |s| per axis, subtracted from the near planes
+        // and added to the far planes, so a box is never lost to rounding.
         const float kS = 9.5367431640625e-07f;  // 2^-20
-        float ex = kS * fmaf(255.0f, fabsf(sx), fabsf(bx));
-        float ey = kS * fmaf(255.0f, fabsf(sy), fabsf(by));
-        float ez = kS * fmaf(255.0f, fabsf(sz), fabsf(bz));
-        const float bxn = bx - ex, bxf = bx + ex, byn = by - ey, byf = by + ey, bzn = bz - ez, bzf = bz + ez;
+        float ex = fmaf(kS, fmaf(255.0f, fabsf(sx), fabsf(bx)), fabsf(sx));
+        float ey = fmaf(kS, fmaf(255.0f, fabsf(sy), fabsf(by)), fabsf(sy));
+        float ez = fmaf(kS, fmaf(255.0f, fabsf(sz), fabsf(bz)), fabsf(sz));
+        const float cx = fmaf(-8388608.0f, sx, bx), cy = fmaf(-8388608.0f, sy, by), cz = fmaf(-8388608.0f, sz, bz);
+        const float bxn = cx - ex, bxf = cx + ex, byn = cy - ey, byf = cy + ey, bzn = cz - ez, bzf = cz + ez;
+        const uint32_t valid = (w0.w >> 24) & 0xffu;
         *base = w1.x;
         *pbase = w1.y;
         *m0 = w1.z;
@@ -507,22 +515,15 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
             const uint32_t wnx = q < 4 ? nxw0 : nxw1, wfx = q < 4 ? fxw0 : fxw1;
             const uint32_t wny = q < 4 ? nyw0 : nyw1, wfy = q < 4 ? fyw0 : fyw1;
             const uint32_t wnz = q < 4 ? nzw0 : nzw1, wfz = q < 4 ? fzw0 : fzw1;
-            float a = fmaxf(fmaxf(fmaf(byte_to_float(wnx, by_), sx, bxn), fmaf(byte_to_float(wny, by_), sy, byn)),
-                            fmaxf(fmaf(byte_to_float(wnz, by_), sz, bzn), R.tmin));
-            float b = fminf(fminf(fmaf(byte_to_float(wfx, by_), sx, bxf), fmaf(byte_to_float(wfy, by_), sy, byf)),
-                            fminf(fmaf(byte_to_float(wfz, by_), sz, bzf), tfar));
+            float a = fmaxf(fmaxf(fmaf(biased_byte(wnx, by_), sx, bxn), fmaf(biased_byte(wny, by_), sy, byn)),
+                            fmaxf(fmaf(biased_byte(wnz, by_), sz, bzn), R.tmin));
+            float b = fminf(fminf(fmaf(biased_byte(wfx, by_), sx, bxf), fmaf(biased_byte(wfy, by_), sy, byf)),
+                            fminf(fmaf(biased_byte(wfz, by_), sz, bzf), tfar));
             tn[q] = a;
             if (a <= b) mask |= 1u << q;
         }
+        return mask & valid;
     }
-    // empty slots never count
-    uint32_t valid = 0;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        uint32_t m = ((q < 4 ? *m0 : *m1) >> (8 * (q & 3))) & 0xffu;
-        valid |= (m ? 1u : 0u) << q;
-    }
-    return mask & valid;
 }
 
 __device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
@@ -950,8 +951,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             if (!mask) continue;
             uint32_t key[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q)
-                key[q] = (mask >> q) & 1u ? ((__float_as_uint(fmaxf(tn[q], 0.0f)) & ~7u) | uint32_t(q)) : 0xffffffffu;
+            for (int q = 0; q < 8; ++q)  // tn >= tmin >= 0, so its bits order as unsigned integers
+                key[q] = (mask >> q) & 1u ? ((__float_as_uint(tn[q]) & ~7u) | uint32_t(q)) : 0xffffffffu;
             cswap(key[0], key[2]); cswap(key[1], key[3]); cswap(key[4], key[6]); cswap(key[5], key[7]);
             cswap(key[0], key[4]); cswap(key[1], key[5]); cswap(key[2], key[6]); cswap(key[3], key[7]);
             cswap(key[0], key[1]); cswap(key[2], key[3]); cswap(key[4], key[5]); cswap(key[6], key[7]);
