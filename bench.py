@@ -186,6 +186,8 @@ def run_reference(args, dist):
     """CPU restatement of the reference's trace path (FP32 Prhi, all host threads)."""
     if dist.rank != 0:
         return
+    if args.config == BATCH_CONFIG:
+        return run_reference_batched(args)
     import vkhrt_gb300 as H
     cfg, sp = workload(args.config)
     v, r, off = H.generate_strands(sp)
@@ -216,6 +218,48 @@ def run_reference(args, dist):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
             "config": config_block(cfg, args.config),
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_batched(args):
+    """The oracle's FP32 tracer over every scene of the batched workload, a bounded pixel sample of
+    each scene per step (all host threads)."""
+    import vkhrt_gb300 as H
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from hairscene import OracleScene, load_oracle, oracle_geometry
+    orc = load_oracle()
+    threads = orc.orc_hardware_threads()
+    models = batch_models(args)
+    scenes = []
+    for m, v, r, off in models:
+        lines, lrad = uniform_lines(v, r, m["nstrands"], m["nverts"])
+        data, rad = oracle_geometry(orc, int(m["type"]), lines, lrad, quantised=(int(m["type"]) == 0))
+        cam = H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"])
+        scenes.append((m, OracleScene(orc, [(int(m["type"]), data, rad)]), H.camera_arrays(cam)))
+    npx = max(16, args.ref_pixels // len(models))
+    total_t = 0.0
+    total_rays = 0
+    for step in range(args.warmup + args.steps):
+        for m, osc, (vi, pi) in scenes:
+            w, h, spp = m["width"], m["height"], m["spp"]
+            px = sample_pixels(w, h, max(4, npx // spp), seed=1000 + step)
+            t0 = time.perf_counter()
+            o = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=px,
+                           threads=threads)
+            dt = time.perf_counter() - t0
+            if step >= args.warmup:
+                total_t += dt
+                total_rays += len(px) * spp + int((o["t"] >= 0).sum())
+    value = total_rays / total_t / 1e6
+    sample = f"about {npx} random samples of each of the {len(models)} scenes per step (+ shadow rays)"
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_t / max(args.steps, 1), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
+            "config": batch_config_block(models),
             "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -373,6 +417,227 @@ def run_ours(args, dist):
     dist.close()
 
 
+BATCH_CONFIG = "c5_batched"
+
+
+def batch_models(args):
+    """The 16 models of the batched workload, with strands generated (host arrays)."""
+    import vkhrt_gb300 as H
+    models = []
+    for m in H.batch_workload():
+        sp = H.StrandParams(seed=m["seed"], nstrands=m["nstrands"], nverts=m["nverts"], r_root=m["r_root"],
+                            r_tip=m["r_tip"])
+        v, r, off = H.generate_strands(sp)
+        models.append((m, v, r, off))
+    return models
+
+
+def batch_config_block(models):
+    nseg = sum(m["nstrands"] * (m["nverts"] - 1) for m, *_ in models)
+    px = sum(m["width"] * m["height"] * m["spp"] for m, *_ in models)
+    return {"workload": f"{BATCH_CONFIG}: {len(models)} hair models (strands log-uniform in [2000, 200000], "
+                        f"{{16,32,64,128}} vertices, Phantom/LSS/DOTS in turn), {nseg} segments, own cameras, "
+                        f"256x256..1920x1080 at 1-4 spp ({px} primary samples), Shade + 1 shadow ray",
+            "segments": nseg, "scenes": len(models), "primary_samples": px,
+            "precision": "quantised (8-bit BVH8 boxes; FP16 control points for Phantom)",
+            "l2": "inputs larger than L2 (BVHs + primitives resident, no flush)", "parallelism": "replicas"}
+
+
+def run_batched(args, dist):
+    """All scenes in one CUDA-graph launch of the persistent kernel (autotuned) against 16
+    sequential plain FP32 launches and 16 sequential quantised launches of the same scenes."""
+    import torch
+    import vkhrt_gb300 as H
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    ctx = H.Context(dev)
+    t_gen = time.perf_counter()
+    models = batch_models(args)
+    t_gen = time.perf_counter() - t_gen
+
+    def build(precision):
+        out = []
+        for m, v, r, off in models:
+            b = H.BottomLevelAccelerationStructure(
+                H.BLASInput(type=m["type"], vertices=v, radius=r, strand_offsets=off, precision=precision,
+                            max_leaf=args.max_leaf), ctx)
+            t = H.TopLevelAccelerationStructure([b], ctx)
+            cam = H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"])
+            out.append((b, t, cam, H.Frame(ctx, m["width"], m["height"], m["spp"], with_hits=not args.no_cpu)))
+        return out
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    q = build(H.Precision.QUANTISED)
+    build_wall = time.perf_counter() - t0
+    f = build(H.Precision.FP32)
+    base = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1})
+    # ---- per-scene work counts (sequential, counted): rays and algorithmic bytes ----
+    rays_per_step = 0
+    alg_bytes = 0
+    per_scene = []
+    for (b, t, cam, fr), (m, *_r) in zip(q, models):
+        H.trace(ctx, t, cam, fr, H.trace_params(jitter=1, seed=17, shading=2, count_stats=1))
+        st = fr.stats()
+        info = b.info
+        prim_b = info["prim_bytes"] + (16 if int(m["type"]) == 0 else 0)
+        rays = st["primary_rays"] + st["shadow_rays"]
+        rays_per_step += rays
+        alg_bytes += st["nodes_visited"] * info["node_bytes"] + st["prims_tested"] * prim_b + \
+            m["width"] * m["height"] * 16
+        per_scene.append({"type": m["type"].name[1:], "segments": m["nstrands"] * (m["nverts"] - 1),
+                          "image": f"{m['width']}x{m['height']}", "spp": m["spp"], "rays": int(rays)})
+    # ---- autotune the batch (untimed) ----
+    scenes_q = [(t, cam, fr) for (_, t, cam, fr) in q]
+    tuned, tune_ms = H.autotune(ctx, scenes_q, base, reps=2)
+    batch = H.Batch(ctx, scenes_q, tuned)
+    dist.barrier()
+    clocks = Clocks(dev)
+    clocks.start()
+    for _ in range(args.warmup):
+        batch.launch()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        batch.launch()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms_max = dist.max(ms)
+    value = dist.world * rays_per_step / (ms_max * 1e-3) / 1e6
+
+    def sequential(sc, params):
+        """Mean over steps of the sum of per-scene launch times (each launch bracketed by events)."""
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in sc]
+        for _ in range(args.warmup):
+            for (_, t, cam, fr) in sc:
+                H.trace(ctx, t, cam, fr, params)
+        torch.cuda.synchronize()
+        lat = np.zeros(len(sc))
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        total = 0.0
+        for _ in range(args.steps):
+            s0.record()
+            for (a, z), (_, t, cam, fr) in zip(ev, sc):
+                a.record()
+                H.trace(ctx, t, cam, fr, params)
+                z.record()
+            s1.record()
+            torch.cuda.synchronize()
+            lat += [a.elapsed_time(z) for a, z in ev]
+            total += s0.elapsed_time(s1)
+        return total / args.steps, lat / args.steps
+
+    plain_params = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1})
+    ms_f32, lat_f32 = sequential(f, plain_params)
+    ms_q, lat_q = sequential(q, tuned)
+    if dist.rank != 0:
+        dist.close()
+        return
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    for d, a, b2 in zip(per_scene, lat_f32, lat_q):
+        d["plain_fp32_ms"] = round(float(a), 3)
+        d["quantised_ms"] = round(float(b2), 3)
+    # ---- e2e: graph launch through the C ABI, every framebuffer to pinned host memory ----
+    pins = [torch.empty((m["height"], m["width"], 4), dtype=torch.float32, pin_memory=True) for m, *_ in models]
+    sync_batch = H.Batch(ctx, scenes_q, H.trace_params(jitter=1, seed=17, shading=2,
+                                                       **{k: getattr(tuned, k) for k in H.TUNED_FIELDS}))
+
+    def e2e_step():
+        sync_batch.launch()
+        for (_, _, _, fr), pin in zip(q, pins):
+            ctx.check(ctx.lib.hrt_frame_download(fr.handle, ctypes.c_void_p(pin.data_ptr()), None, None))
+
+    for _ in range(2):
+        e2e_step()
+    te = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_step()
+    te = (time.perf_counter() - te) / e2e_steps
+    d2h = sum(m["width"] * m["height"] * 16 for m, *_ in models)
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32 (fp16 control-point storage, 8-bit node boxes)",
+            "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
+            "config": batch_config_block(models), "rays_per_step": int(rays_per_step), "gpu_launches": args.steps,
+            "autotuned": {k: int(getattr(tuned, k)) for k in H.TUNED_FIELDS} | {"mean_ms": round(tune_ms, 3)},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                         "bytes_per_launch": int(alg_bytes)},
+            "sequential_plain_fp32": {"value": round(rays_per_step / (ms_f32 * 1e-3) / 1e6, 3),
+                                      "ms_per_step": round(ms_f32, 3), "launches_per_step": len(models)},
+            "sequential_quantised": {"value": round(rays_per_step / (ms_q * 1e-3) / 1e6, 3),
+                                     "ms_per_step": round(ms_q, 3), "launches_per_step": len(models)},
+            "per_scene_latency_ms": {"batched_all_scenes": round(ms, 3),
+                                     "note": "a batched scene completes with the launch; sequential latencies "
+                                             "are per launch"},
+            "scenes": per_scene,
+            "e2e": {"value": round(rays_per_step / te / 1e6, 3), "unit": "Mrays/s",
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(d2h), "ms_per_step": round(te * 1e3, 3)},
+            "clocks": clk,
+            "build": {"build_wall_s_quantised": round(build_wall, 3), "strand_generation_s": round(t_gen, 3)}}
+    if not args.no_cpu:
+        line.update(batch_agreement_and_cpu(args, ctx, q, models))
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def batch_agreement_and_cpu(args, ctx, q, models):
+    """Per-scene FP64 oracle agreement on ~65,536 sampled rays in all, and the oracle's FP32 rate."""
+    import vkhrt_gb300 as H
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from hairscene import OracleScene, compare_hits, load_oracle, oracle_geometry
+    orc = load_oracle()
+    threads = orc.orc_hardware_threads()
+    n_t = n_mis = n_ties = 0
+    max_rel_t = 0.0
+    max_rgb = 0.0
+    cpu_rays = 0
+    cpu_s = 0.0
+    per = max(1, 65536 // len(models))
+    for (b, t, cam, fr), (m, v, r, off) in zip(q, models):
+        H.trace(ctx, t, cam, fr, H.trace_params(jitter=1, seed=17, shading=2, record_hits=1))
+        rgba, hits = fr.download(hits=True)
+        w, h, spp = m["width"], m["height"], m["spp"]
+        lines, lrad = uniform_lines(v, r, m["nstrands"], m["nverts"])
+        data, rad = oracle_geometry(orc, int(m["type"]), lines, lrad, quantised=(int(m["type"]) == 0))
+        del lines, lrad
+        osc = OracleScene(orc, [(int(m["type"]), data, rad)])
+        vi, pi = H.camera_arrays(cam)
+        px = sample_pixels(w, h, per // spp, seed=3)
+        o = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=64, pixel_list=px)
+        gh = hits.reshape(h * w, spp)[px].reshape(-1)
+        g_t = np.where(gh["t"] >= 0, gh["t"].astype(np.float64), -1.0)
+        cmp = compare_hits(g_t, gh["prim"], gh["inst"], o["t"], o["prim"], o["inst"])
+        n_t += cmp["n"]
+        n_mis += cmp["mismatches"]
+        n_ties += cmp["ties"]
+        max_rel_t = max(max_rel_t, cmp["max_rel_t"])
+        same = (gh["prim"] == o["prim"]) & (((gh["flags"] & H.HIT_SHADOWED) != 0) == (o["shadow"] != 0))
+        ok_px = same.reshape(-1, spp).all(axis=1)
+        if ok_px.any():
+            max_rgb = max(max_rgb, float(np.abs(rgba.reshape(-1, 4)[px] - o["fb"]).max(axis=1)[ok_px].max()))
+        cpx = sample_pixels(w, h, max(64, int(args.cpu_seconds * 2000 / len(models)) // spp), seed=11)
+        t0 = time.perf_counter()
+        oc = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=cpx,
+                        threads=threads)
+        cpu_s += time.perf_counter() - t0
+        cpu_rays += len(cpx) * spp + int((oc["t"] >= 0).sum())
+        del osc, data, rad
+    return {"agreement": {"rays": int(n_t), "hit_id": round(1.0 - n_mis / max(n_t - n_ties, 1), 6),
+                          "mismatches": int(n_mis),
+                          "ties": int(n_ties), "max_rel_t": max_rel_t, "max_rgb_err_agreeing": max_rgb,
+                          "oracle": "FP64 CPU restatement on the same (dequantised) geometry, per scene"},
+            "cpu_baseline": {"value": round(cpu_rays / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads,
+                             "kind": "port", "sample": f"random pixels of every scene, FP32 oracle, {cpu_s:.1f} s"}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -410,6 +675,9 @@ def main():
     if args.impl == "reference":
         run_reference(args, dist)
         dist.close()
+        return
+    if args.config == BATCH_CONFIG:
+        run_batched(args, dist)
         return
     run_ours(args, dist)
 

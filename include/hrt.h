@@ -255,6 +255,15 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
 hrt_status hrt_batch_launch(hrt_batch* b, void* stream);
 hrt_status hrt_batch_destroy(hrt_batch* b);
 
+/* ---- autotuner ------------------------------------------------------------------------------
+ * Times every candidate kernel configuration on the given scenes (occupancy variant x refill
+ * threshold x speculative traversal: HRT_AUTOTUNE_CANDIDATES in all), each `reps` times with
+ * plain launches after one warm-up, and writes the fastest into `best` (a copy of `base` with
+ * kernel_variant, refill and speculative replaced) and its mean frame time into `best_ms`. */
+#define HRT_AUTOTUNE_CANDIDATES 12u
+hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* base,
+                        uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms);
+
 /* ---- synthetic strands (stand-in for the reference's glTF hair assets) --------------------
  * Roots uniform on the unit-sphere cap of polar angle < cap_deg about +y; each strand grows
  * along the root normal in `step` increments, the direction of step k being

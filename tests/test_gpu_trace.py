@@ -232,3 +232,41 @@ def test_quantised_node_visits_close_to_fp32(ctx):
     assert f["shadow_rays"] > 1000 and q["shadow_rays"] > 1000
     per_ray = lambda s: s["nodes_visited"] / (s["primary_rays"] + s["shadow_rays"])
     assert 0.9 * per_ray(f) <= per_ray(q) <= 1.3 * per_ray(f)
+
+
+def test_kernel_variants_and_autotune_give_identical_frames(ctx, tmp_path):
+    """Every configuration the autotuner may pick renders the same hits and pixels, and the
+    autotuner's choice is one of its candidates (cached choices are reused)."""
+    scenes = []
+    for k, (gt, ns, w, h, spp) in enumerate([(PHANTOM, 300, 72, 40, 2), (LSS, 200, 48, 48, 1), (DOTS, 120, 40, 56, 3)]):
+        v, r, off = H.generate_strands(H.StrandParams(seed=90 + k, nstrands=ns, nverts=32))
+        b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType(gt), vertices=v, radius=r, strand_offsets=off,
+                                                           precision=H.Precision.QUANTISED), ctx)
+        t = H.TopLevelAccelerationStructure([b], ctx)
+        scenes.append((b, t, H.orbit_camera(w, h, 0.4 * k, 0.1), H.Frame(ctx, w, h, spp, with_hits=True)))
+    ref = None
+    for variant in (1, 2):
+        for refill in (4, 8, 16):
+            for spec in (0, 1):
+                p = H.trace_params(shading=2, record_hits=1, jitter=1, seed=5, kernel_variant=variant, refill=refill,
+                                   speculative=spec)
+                out = []
+                for (_, t, cam, fr) in scenes:
+                    H.trace(ctx, t, cam, fr, p)
+                    out.append(fr.download(hits=True))
+                if ref is None:
+                    ref = out
+                for (a, ha), (b2, hb) in zip(ref, out):
+                    assert np.array_equal(a, b2) and np.array_equal(ha, hb), (variant, refill, spec)
+    cache = str(tmp_path / "tune.json")
+    sc = [(t, cam, fr) for (_, t, cam, fr) in scenes]
+    best, ms = H.autotune(ctx, sc, H.trace_params(shading=2, jitter=1, seed=5), reps=1, cache=cache, key="three")
+    assert ms > 0 and best.kernel_variant in (1, 2) and best.refill in (4, 8, 16) and best.speculative in (0, 1)
+    again, ms2 = H.autotune(ctx, sc, H.trace_params(shading=2, jitter=1, seed=5), reps=1, cache=cache, key="three")
+    assert ms2 == -1.0 and all(getattr(again, f) == getattr(best, f) for f in H.TUNED_FIELDS)
+    p = H.trace_params(shading=2, record_hits=1, jitter=1, seed=5, **{f: getattr(best, f) for f in H.TUNED_FIELDS})
+    batch = H.Batch(ctx, sc, p)
+    batch.launch()
+    for (a, ha), (_, _, _, fr) in zip(ref, scenes):
+        b2, hb = fr.download(hits=True)
+        assert np.array_equal(a, b2) and np.array_equal(ha, hb)

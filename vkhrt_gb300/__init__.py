@@ -96,6 +96,8 @@ SIGNATURES = {
     "hrt_batch_create": (c_i32, [c_p, ctypes.POINTER(SceneDescC), c_u32, ctypes.POINTER(TraceParamsC), c_p,
                                  ctypes.POINTER(c_p)]),
     "hrt_batch_launch": (c_i32, [c_p, c_p]),
+    "hrt_autotune": (c_i32, [c_p, ctypes.POINTER(SceneDescC), c_u32, ctypes.POINTER(TraceParamsC), c_u32, c_p,
+                             ctypes.POINTER(TraceParamsC), ctypes.POINTER(c_f)]),
     "hrt_batch_destroy": (c_i32, [c_p]),
     "hrt_strand_params_default": (None, [ctypes.POINTER(StrandParamsC)]),
     "hrt_generate_strands": (c_i32, [ctypes.POINTER(StrandParamsC), c_p, c_p, c_p]),
@@ -402,6 +404,46 @@ def trace_rays_noalloc(ctx: Context, tlas: TopLevelAccelerationStructure, rays: 
     return hits
 
 
+TUNED_FIELDS = ("kernel_variant", "refill", "speculative")
+
+
+def autotune(ctx: Context, scenes: list[tuple[TopLevelAccelerationStructure, CameraC, Frame]],
+             params: TraceParamsC | None = None, reps: int = 3, cache: str | None = None,
+             key: str | None = None) -> tuple[TraceParamsC, float]:
+    """hrt_autotune on `scenes`; with `cache` (a JSON file) and `key`, a stored choice is reused
+    and a new one is stored. Returns (parameters, mean frame ms of the choice or -1 if cached)."""
+    import json
+    base = params if params is not None else trace_params()
+    if cache and key and os.path.exists(cache):
+        try:
+            stored = json.load(open(cache)).get(key)
+        except (OSError, ValueError):
+            stored = None
+        if stored:
+            best = TraceParamsC.from_buffer_copy(base)
+            for f in TUNED_FIELDS:
+                setattr(best, f, int(stored[f]))
+            return best, -1.0
+    descs = (SceneDescC * len(scenes))()
+    for i, (t, cam, fr) in enumerate(scenes):
+        descs[i].tlas = t.handle
+        descs[i].camera = cam
+        descs[i].frame = fr.handle
+    best = TraceParamsC()
+    ms = c_f()
+    ctx.check(ctx.lib.hrt_autotune(ctx.handle, descs, len(scenes), ctypes.byref(base), reps, None, ctypes.byref(best),
+                                   ctypes.byref(ms)))
+    if cache and key:
+        try:
+            data = json.load(open(cache)) if os.path.exists(cache) else {}
+        except (OSError, ValueError):
+            data = {}
+        data[key] = {f: int(getattr(best, f)) for f in TUNED_FIELDS} | {"ms": round(float(ms.value), 4)}
+        with open(cache, "w") as fh:
+            json.dump(data, fh, indent=1, sort_keys=True)
+    return best, float(ms.value)
+
+
 class Batch:
     """hrt_batch: many scenes in one persistent launch replayed from a CUDA graph."""
 
@@ -487,3 +529,33 @@ CONFIGS = {
 def scene_camera(width: int, height: int) -> CameraC:
     """Camera of the benchmark scenes: eye (0,0,3) looking at the origin, +y up, 40 deg FOV."""
     return look_at((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width / height, 0.1, 1000.0)
+
+
+def orbit_camera(width: int, height: int, azimuth: float, elevation: float, dist: float = 3.0) -> CameraC:
+    """scene_camera moved on the sphere of radius `dist` (angles in radians, azimuth 0 = +z)."""
+    import math
+    eye = (dist * math.cos(elevation) * math.sin(azimuth), dist * math.sin(elevation),
+           dist * math.cos(elevation) * math.cos(azimuth))
+    return look_at(eye, (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width / height, 0.1, 1000.0)
+
+
+def batch_workload(seed: int = 1005, nscenes: int = 16) -> list[dict]:
+    """The batched multi-scene workload: `nscenes` hair models with strand counts log-uniform in
+    [2,000, 200,000], vertices per strand uniform in {16, 32, 64, 128}, intersector modes in turn
+    Phantom, LSS, DOTS; each with its own orbit camera, a resolution log-uniform from 256x256 to
+    1920x1080 (width and height at the same fraction) and 1-4 samples per pixel."""
+    import math
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(nscenes):
+        ns = int(round(math.exp(rng.uniform(math.log(2000.0), math.log(200000.0)))))
+        nv = int(rng.choice([16, 32, 64, 128]))
+        f = float(rng.uniform())
+        w = int(round(256 * (1920 / 256) ** f))
+        h = int(round(256 * (1080 / 256) ** f))
+        spp = int(rng.integers(1, 5))
+        az = float(rng.uniform(0.0, 2.0 * math.pi))
+        el = float(rng.uniform(-0.2, 0.6))
+        out.append(dict(seed=seed * 1000 + i, nstrands=ns, nverts=nv, r_root=0.003, r_tip=0.0008,
+                        type=BLASType(i % 3), width=w, height=h, spp=spp, azimuth=az, elevation=el))
+    return out

@@ -833,6 +833,89 @@ hrt_status hrt_batch_launch(hrt_batch* b, void* stream) {
     return HRT_OK;
 }
 
+hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* base,
+                        uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms) {
+    if (!ctx) return HRT_ERR_INVALID_ARG;
+    if (!scenes || !n || !base || !best) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_autotune: null or empty argument");
+    if (reps == 0) reps = 3;
+    DeviceSet ds(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    std::vector<SceneLaunch> sl(n);
+    uint64_t work = 0;
+    bool quant = scenes[0].tlas ? scenes[0].tlas->quantised : false;
+    uint32_t type_mask = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!scenes[i].tlas || !scenes[i].frame) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_autotune: scene %u incomplete", i);
+        if (scenes[i].tlas->quantised != quant)
+            return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_autotune: scenes mix FP32 and quantised BLASes");
+        type_mask |= scenes[i].tlas->type_mask;
+        fill_scene(sl[i], scenes[i].tlas, &scenes[i].camera, scenes[i].frame, work);
+        work += sl[i].work_count;
+    }
+    SceneLaunch* ds_ = nullptr;
+    TraceCounters* ctr = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        if (ds_) cudaFree(ds_);
+        if (ctr) cudaFree(ctr);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    cudaError_t e = cudaMalloc(&ds_, n * sizeof(SceneLaunch));
+    if (e == cudaSuccess) e = cudaMalloc(&ctr, sizeof(TraceCounters));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ds_, sl.data(), n * sizeof(SceneLaunch), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(ctx, e, "hrt_autotune");
+    }
+    const uint32_t variants[2] = {1, 2}, refills[3] = {4, 8, 16}, specs[2] = {0, 1};
+    float best_t = -1.0f;
+    hrt_trace_params bp = *base;
+    for (uint32_t v : variants)
+        for (uint32_t r : refills)
+            for (uint32_t sp : specs) {
+                hrt_trace_params p = *base;
+                p.kernel_variant = v;
+                p.refill = r;
+                p.speculative = sp;
+                p.record_hits = 0;
+                p.count_stats = 0;
+                TraceLaunch L = make_launch(&p, ds_, n, work, ctr, type_mask);
+                float tot = 0.0f;
+                for (uint32_t k = 0; k <= reps && e == cudaSuccess; ++k) {
+                    e = cudaMemsetAsync(ctr, 0, sizeof(TraceCounters), s);
+                    if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+                    if (e == cudaSuccess) e = launch_trace(L, quant, s, ctx->sm_count);
+                    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                    float ms = 0.0f;
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                    if (k > 0) tot += ms;  // the first run warms up
+                }
+                if (e != cudaSuccess) break;
+                TraceCounters c;
+                hrt_status st = read_counters(ctx, ctr, &c, s);
+                if (st != HRT_OK) {
+                    cleanup();
+                    return st;
+                }
+                float mean = tot / float(reps);
+                if (best_t < 0.0f || mean < best_t) {
+                    best_t = mean;
+                    bp = p;
+                    bp.record_hits = base->record_hits;
+                    bp.count_stats = base->count_stats;
+                }
+            }
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "hrt_autotune");
+    *best = bp;
+    if (best_ms) *best_ms = best_t;
+    return HRT_OK;
+}
+
 hrt_status hrt_batch_destroy(hrt_batch* b) {
     if (!b) return HRT_OK;
     DeviceSet ds(b->ctx->device);

@@ -432,16 +432,16 @@ __device__ __forceinline__ V3<float> safe_inv(V3<float> d) {
     auto r = [](float x) { return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
     return mk(r(d.x), r(d.y), r(d.z));
 }
-// 2^23 + (byte k of w) as a float: the byte placed under the exponent of 2^23.
+// 1 + (byte k of w) 2^-15 as a float: the byte placed in mantissa bits 15..8 of 1.0.
 __device__ __forceinline__ float biased_byte(uint32_t w, int k) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | uint32_t(k)));
+    return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | (uint32_t(k) << 4)));
 }
 
 // Child entry distances of one node; returns a bit mask of hit children and fills tn[8].
 // Near and far planes are chosen per axis by the sign of the direction (octant), so a child
 // needs three maxima and three minima. FP32 boxes: t = (plane - o) inv, accepted when
 // tnear <= tfar (1 + 2^-20). 8-bit boxes: t = q (2^e inv) + (p - o) inv, one fused operation
-// per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 255 2^e |inv|), and that
+// per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 33023 2^e |inv|), and that
 // bound is subtracted from the axis's near planes and added to its far planes, so a box is
 // never lost to rounding (a near-parallel axis widens only its own planes).
 template <bool kQuant>
@@ -482,23 +482,27 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
     } else {
         const uint4* p = reinterpret_cast<const uint4*>(static_cast<const NodeQ*>(nodes) + ni);
         uint4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
-        // per node: s = 2^e inv, b = (p - o) inv
+        // per node: s = 2^e inv (scaled to 2^15 s below), b = (p - o) inv
         float sx = __uint_as_float((w0.w & 0xffu) << 23) * R.inv.x;
         float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * R.inv.y;
         float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * R.inv.z;
         float bx = (__uint_as_float(w0.x) - R.o.x) * R.inv.x;
         float by = (__uint_as_float(w0.y) - R.o.y) * R.inv.y;
         float bz = (__uint_as_float(w0.z) - R.o.z) * R.inv.z;
-        // The byte q is read as the float 2^23 + q (byte permute under the exponent of 2^23), and
-        // the 2^23 is folded into the offset: t = (2^23 + q) s + (b - 2^23 s), one fused
-        // multiply-add per plane. Rounding of the offset costs at most |s| / 2; with the rest it
-        // is bounded by E = 2^-20 (|b| + 255 |s|) + |s| per axis, subtracted from the near planes
-        // and added to the far planes, so a box is never lost to rounding.
+        // The byte q is read as the float v = 1 + q 2^-15 (byte permute into the mantissa of
+        // 1.0), and the 1 is folded into the offset: t = v S + (b - S) with S = 2^15 s, one
+        // fused multiply-add per plane. The three roundings (offset, slack, product-sum) are each
+        // below 2^-24 (|b| + (2^15 + 255) |s|), so E = 2^-20 (|b| + 33023 |s|) per axis, taken
+        // from the near planes and given to the far planes, never loses a box to rounding; it is
+        // about 1/32 of a grid step.
         const float kS = 9.5367431640625e-07f;  // 2^-20
-        float ex = fmaf(kS, fmaf(255.0f, fabsf(sx), fabsf(bx)), fabsf(sx));
-        float ey = fmaf(kS, fmaf(255.0f, fabsf(sy), fabsf(by)), fabsf(sy));
-        float ez = fmaf(kS, fmaf(255.0f, fabsf(sz), fabsf(bz)), fabsf(sz));
-        const float cx = fmaf(-8388608.0f, sx, bx), cy = fmaf(-8388608.0f, sy, by), cz = fmaf(-8388608.0f, sz, bz);
+        sx *= 32768.0f;
+        sy *= 32768.0f;
+        sz *= 32768.0f;
+        float ex = kS * fmaf(1.00775146484375f, fabsf(sx), fabsf(bx));  // 33023 / 32768
+        float ey = kS * fmaf(1.00775146484375f, fabsf(sy), fabsf(by));
+        float ez = kS * fmaf(1.00775146484375f, fabsf(sz), fabsf(bz));
+        const float cx = bx - sx, cy = by - sy, cz = bz - sz;
         const float bxn = cx - ex, bxf = cx + ex, byn = cy - ey, byf = cy + ey, bzn = cz - ez, bzf = cz + ez;
         const uint32_t valid = (w0.w >> 24) & 0xffu;
         *base = w1.x;
