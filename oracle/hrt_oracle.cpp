@@ -566,10 +566,12 @@ static void refit(Binary& bt, const Box* sorted_boxes, int64_t n) {
 // (dx*dy + dy*dz) + dz*dx that is an internal node holding more than max_leaf primitives is
 // replaced in place by its left child, and its right child is appended (ties: first in list).
 // A child holding at most max_leaf primitives becomes a leaf (a contiguous run of sorted
-// primitives). Nodes are numbered breadth first; a node's internal children take consecutive
-// indices from child_base in child order, and its leaf primitives are copied to consecutive
-// slots from prim_base in child order (the primitive order array).
-// meta byte per child: 0 empty, 0x80|rank internal, (count<<5)|offset leaf.
+// primitives). The children are then placed in the 8 slots by direction (octant_slots below).
+// Nodes are numbered breadth first; a node's internal children take consecutive indices from
+// child_base in slot order, and its leaf primitives are copied to consecutive slots from
+// prim_base in slot order (the primitive order array).
+// meta byte per slot: 0 empty, 0x80|rank internal, (count<<5)|offset leaf; an empty slot's box
+// is lo = +inf, hi = -inf.
 struct Wide {
     std::vector<uint32_t> child_base, prim_base;
     std::vector<uint8_t> meta;     // 8 per node
@@ -580,6 +582,34 @@ static float sa_measure(const Box& b) {
     float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
     return (dx * dy + dy * dz) + dz * dx;
 }
+// Slot of each child by direction: cost(c, s) = ((+-dx) + (+-dy)) + (+-dz) with
+// d = (lo + hi of the child) - (lo + hi of the node), the sign on an axis + when bit
+// (x 1, y 2, z 4) of s is set. The (child, slot) pair of largest cost is taken first,
+// repeatedly; ties go to the lower child, then the lower slot, and a NaN cost never replaces a
+// candidate already held. kid_in[s] = child index or -1. (A ray then visits slots in the order
+// i ^ octant, octant bit k set when the ray's direction is negative on axis k: nearest first.)
+static void octant_slots(const Box& parent, const Box* const* kid_box, int n, int* kid_in) {
+    const float pc[3] = {parent.lo[0] + parent.hi[0], parent.lo[1] + parent.hi[1], parent.lo[2] + parent.hi[2]};
+    int slot_of[8];
+    for (int q = 0; q < 8; ++q) { kid_in[q] = -1; slot_of[q] = -1; }
+    for (int r = 0; r < n; ++r) {
+        int bq = -1, bs = -1;
+        float bc = 0.0f;
+        for (int q = 0; q < n; ++q) {
+            if (slot_of[q] >= 0) continue;
+            const Box& b = *kid_box[q];
+            float d0 = (b.lo[0] + b.hi[0]) - pc[0], d1 = (b.lo[1] + b.hi[1]) - pc[1], d2 = (b.lo[2] + b.hi[2]) - pc[2];
+            for (int s2 = 0; s2 < 8; ++s2) {
+                if (kid_in[s2] >= 0) continue;
+                float c = ((s2 & 1 ? d0 : -d0) + (s2 & 2 ? d1 : -d1)) + (s2 & 4 ? d2 : -d2);
+                if (bq < 0 || c > bc) { bq = q; bs = s2; bc = c; }
+            }
+        }
+        slot_of[bq] = bs;
+        kid_in[bs] = bq;
+    }
+}
+
 static void collapse(const Binary& bt, const Box* sorted_boxes, int64_t n, int max_leaf, Wide& w) {
     w = Wide{};
     if (n <= 0) return;
@@ -616,12 +646,17 @@ static void collapse(const Binary& bt, const Box* sorted_boxes, int64_t n, int m
             }
             size_t base = w.meta.size();
             w.meta.resize(base + 8, 0);
-            w.cbox.resize(base + 8, Box{{0, 0, 0}, {0, 0, 0}});
+            w.cbox.resize(base + 8, Box{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}});
             w.child_base.push_back(next_node);
             w.prim_base.push_back(next_prim);
+            const Box* kb[8];
+            for (int q = 0; q < nk; ++q) kb[q] = &cbox(kids[q]);
+            int kid_in[8];
+            octant_slots(cbox(b), kb, nk, kid_in);
             uint32_t rank = 0, poff = 0;
-            for (int q = 0; q < nk; ++q) {
-                uint32_t c = kids[q];
+            for (int q = 0; q < 8; ++q) {
+                if (kid_in[q] < 0) continue;
+                uint32_t c = kids[kid_in[q]];
                 w.cbox[base + q] = cbox(c);
                 uint32_t cnt = count(c);
                 if (!(c & 0x80000000u) && cnt > uint32_t(max_leaf)) {

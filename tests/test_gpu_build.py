@@ -14,8 +14,8 @@ pytestmark = pytest.mark.gpu
 
 NODEF = np.dtype([("lo_x", "<f4", 8), ("hi_x", "<f4", 8), ("lo_y", "<f4", 8), ("hi_y", "<f4", 8),
                   ("lo_z", "<f4", 8), ("hi_z", "<f4", 8), ("child_base", "<u4"), ("prim_base", "<u4"),
-                  ("meta", "u1", 8), ("valid", "<u4"), ("pad", "<u4", 3)])
-NODEQ = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("valid", "u1"), ("child_base", "<u4"), ("prim_base", "<u4"),
+                  ("imask", "<u4"), ("pad0", "<u4"), ("meta", "u1", 8), ("pad", "<u4", 2)])
+NODEQ = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("imask", "u1"), ("child_base", "<u4"), ("prim_base", "<u4"),
                   ("meta", "u1", 8), ("qlo_x", "u1", 8), ("qhi_x", "u1", 8), ("qlo_y", "u1", 8), ("qhi_y", "u1", 8),
                   ("qlo_z", "u1", 8), ("qhi_z", "u1", 8)])
 PRIMH = np.dtype([("h", "<u2", 14), ("key", "<u4")])
@@ -85,8 +85,8 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
     qn = blas.get(H.Part.QNODES, np.uint8, nn * 80).view(NODEQ)
     assert np.array_equal(qn["child_base"], o["cb"][:nn]) and np.array_equal(qn["prim_base"], o["pb"][:nn])
     assert np.array_equal(qn["meta"], o["meta"][:nn])
-    valid = ((o["meta"][:nn] != 0).astype(np.uint32) << np.arange(8, dtype=np.uint32)).sum(axis=1)
-    assert np.array_equal(qn["valid"], valid.astype(np.uint8))
+    imask = (((o["meta"][:nn] & 0x80) != 0).astype(np.uint32) << np.arange(8, dtype=np.uint32)).sum(axis=1)
+    assert np.array_equal(qn["imask"], imask.astype(np.uint8))
     assert qn["p"].tobytes() == o["qp"][:nn].tobytes() and np.array_equal(qn["e"], o["qe"][:nn])
     for k, ax in enumerate("xyz"):
         assert np.array_equal(qn["qlo_" + ax], o["qlo"][:nn, k]) and np.array_equal(qn["qhi_" + ax], o["qhi"][:nn, k])
@@ -96,7 +96,7 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
             assert fn["lo_" + ax].tobytes() == np.ascontiguousarray(o["cbox"][:nn, :, k]).tobytes()
             assert fn["hi_" + ax].tobytes() == np.ascontiguousarray(o["cbox"][:nn, :, 3 + k]).tobytes()
         assert np.array_equal(fn["meta"], o["meta"][:nn])
-        assert np.array_equal(fn["valid"], valid)
+        assert np.array_equal(fn["imask"], imask)
     if quant_prims:
         recs = blas.get(H.Part.PRIMS, np.uint8, n * 32).view(PRIMH)
         halves = recs["h"].view(np.float16).astype(np.float32)

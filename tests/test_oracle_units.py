@@ -107,11 +107,15 @@ def test_bvh8_properties(orc, n, max_leaf):
     seen_nodes = {0}
     for i in range(nn):
         poff = 0
+        rank = 0
         for q in range(8):
             m = int(meta[i, q])
-            if m == 0:
+            if m == 0:  # an empty slot holds an empty box
+                assert np.all(cbox[i, q, :3] == np.inf) and np.all(cbox[i, q, 3:] == -np.inf)
                 continue
             if m & 0x80:
+                assert (m & 7) == rank  # internal children are numbered in slot order
+                rank += 1
                 child = int(cb[i]) + (m & 7)
                 assert child < nn and child not in seen_nodes
                 seen_nodes.add(child)
@@ -163,3 +167,27 @@ def test_karras_ranges(orc):
     assert F[0] == 0 and La[0] == n - 1
     # root box = union of all boxes
     assert np.array_equal(nb[0, :3], boxes[:, :3].min(0)) and np.array_equal(nb[0, 3:], boxes[:, 3:].max(0))
+
+
+def test_bvh8_slots_follow_direction(orc):
+    """Eight leaf boxes at the corners of a cube land in the slot of their octant."""
+    corners = [(x, y, z) for z in (0, 1) for y in (0, 1) for x in (0, 1)]
+    rng = np.random.default_rng(5)
+    perm = rng.permutation(8)
+    boxes = np.array([[10 * c[0], 10 * c[1], 10 * c[2], 10 * c[0] + 1, 10 * c[1] + 1, 10 * c[2] + 1]
+                      for c in np.array(corners)[perm]], np.float32)
+    mx = 8
+    cb = np.zeros(mx, np.uint32)
+    pb = np.zeros(mx, np.uint32)
+    meta = np.zeros((mx, 8), np.uint8)
+    cbox = np.zeros((mx, 8, 6), np.float32)
+    order = np.zeros(8, np.uint32)
+    qp = np.zeros((mx, 3), np.float32)
+    qe = np.zeros((mx, 3), np.uint8)
+    qlo = np.zeros((mx, 3, 8), np.uint8)
+    qhi = np.zeros((mx, 3, 8), np.uint8)
+    nn = orc.orc_bvh8(P(boxes), 8, 1, mx, P(cb), P(pb), P(meta), P(cbox), P(order), P(qp), P(qe), P(qlo), P(qhi))
+    assert nn == 1
+    for s in range(8):
+        lo = cbox[0, s, :3]
+        assert tuple(int(v > 5) for v in lo) == ((s & 1), (s >> 1) & 1, (s >> 2) & 1)

@@ -594,36 +594,69 @@ __global__ void collapse_expand_kernel(BinView bv, const uint32_t* level, uint32
     nprim[w] = np;
 }
 
+// Slot of each child by direction: cost(c, s) = ((+-dx) + (+-dy)) + (+-dz), d = (lo + hi of
+// the child) - (lo + hi of the node), the sign on an axis + when bit (x 1, y 2, z 4) of s is
+// set; the (child, slot) pair of largest cost is taken first, repeatedly (ties: lower child,
+// then lower slot; a NaN cost never wins over a taken candidate). kid_in[s] = child or -1.
+__device__ void octant_slots(const BinView& bv, uint32_t b, const uint32_t* kids, int n, int* kid_in) {
+    const float* pb = bbox(bv, b);
+    const float pc[3] = {pb[0] + pb[3], pb[1] + pb[4], pb[2] + pb[5]};
+    int slot_of[8];
+    for (int q = 0; q < 8; ++q) { kid_in[q] = -1; slot_of[q] = -1; }
+    for (int r = 0; r < n; ++r) {
+        int bq = -1, bs = -1;
+        float bc = 0.0f;
+        for (int q = 0; q < n; ++q) {
+            if (slot_of[q] >= 0) continue;
+            const float* bx = bbox(bv, kids[q]);
+            float d0 = (bx[0] + bx[3]) - pc[0], d1 = (bx[1] + bx[4]) - pc[1], d2 = (bx[2] + bx[5]) - pc[2];
+            for (int s2 = 0; s2 < 8; ++s2) {
+                if (kid_in[s2] >= 0) continue;
+                float c = ((s2 & 1 ? d0 : -d0) + (s2 & 2 ? d1 : -d1)) + (s2 & 4 ? d2 : -d2);
+                if (bq < 0 || c > bc) { bq = q; bs = s2; bc = c; }
+            }
+        }
+        slot_of[bq] = bs;
+        kid_in[bs] = bq;
+    }
+}
+
 __global__ void collapse_emit_kernel(BinView bv, const uint32_t* level, uint32_t count, int max_leaf,
                                      const uint32_t* kids, const uint32_t* nk, const uint32_t* int_off,
                                      const uint32_t* prim_off, uint32_t node_base, uint32_t next_node_base,
                                      uint32_t prim_base_g, NodeF* nodes, uint32_t* next_level, uint32_t* prim_order) {
     uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= count) return;
+    const float kInf = __int_as_float(0x7f800000);
     NodeF nd;
     for (int q = 0; q < 8; ++q) {
-        nd.lo_x[q] = nd.hi_x[q] = nd.lo_y[q] = nd.hi_y[q] = nd.lo_z[q] = nd.hi_z[q] = 0.0f;
+        nd.lo_x[q] = nd.lo_y[q] = nd.lo_z[q] = kInf;
+        nd.hi_x[q] = nd.hi_y[q] = nd.hi_z[q] = -kInf;
         nd.meta[q] = 0;
     }
-    nd.valid = 0;
-    for (int q = 0; q < 3; ++q) nd.pad[q] = 0;
+    nd.imask = 0;
+    nd.pad0 = 0;
+    nd.pad[0] = nd.pad[1] = 0;
     nd.child_base = next_node_base + int_off[w];
     nd.prim_base = prim_base_g + prim_off[w];
-    uint32_t rank = 0, poff = 0;
     int n = int(nk[w]);
-    for (int q = 0; q < n; ++q) {
-        uint32_t c = kids[8 * uint64_t(w) + q];
+    int kid_in[8];
+    octant_slots(bv, level[w], kids + 8 * uint64_t(w), n, kid_in);
+    uint32_t rank = 0, poff = 0;
+    for (int s2 = 0; s2 < 8; ++s2) {
+        if (kid_in[s2] < 0) continue;
+        uint32_t c = kids[8 * uint64_t(w) + kid_in[s2]];
         const float* bx = bbox(bv, c);
-        nd.lo_x[q] = bx[0]; nd.lo_y[q] = bx[1]; nd.lo_z[q] = bx[2];
-        nd.hi_x[q] = bx[3]; nd.hi_y[q] = bx[4]; nd.hi_z[q] = bx[5];
+        nd.lo_x[s2] = bx[0]; nd.lo_y[s2] = bx[1]; nd.lo_z[s2] = bx[2];
+        nd.hi_x[s2] = bx[3]; nd.hi_y[s2] = bx[4]; nd.hi_z[s2] = bx[5];
         uint32_t cnt = bcount(bv, c);
-        nd.valid |= 1u << q;
         if (!(c & kLeafFlag) && cnt > uint32_t(max_leaf)) {
-            nd.meta[q] = uint8_t(0x80u | rank);
+            nd.meta[s2] = uint8_t(0x80u | rank);
+            nd.imask |= 1u << s2;
             next_level[int_off[w] + rank] = c;
             ++rank;
         } else {
-            nd.meta[q] = uint8_t((cnt << 5) | poff);
+            nd.meta[s2] = uint8_t((cnt << 5) | poff);
             uint32_t f = bfirst(bv, c);
             for (uint32_t j = 0; j < cnt; ++j) prim_order[nd.prim_base + poff + j] = f + j;
             poff += cnt;
@@ -646,8 +679,8 @@ __global__ void quantise_kernel(const NodeF* in, uint64_t nn, NodeQ* out) {
     uint8_t* QH[3] = {q.qhi_x, q.qhi_y, q.qhi_z};
     float pp[3];
     uint8_t ee[3];
-    uint32_t nc = 0;
-    for (int c = 0; c < 8; ++c) nc |= (a.meta[c] ? 1u : 0u) << c;
+    uint32_t im = 0;
+    for (int c = 0; c < 8; ++c) im |= (a.meta[c] & 0x80u ? 1u : 0u) << c;
     for (int k = 0; k < 3; ++k) {
         float p = __int_as_float(0x7f800000), P = -__int_as_float(0x7f800000);
         for (int c = 0; c < 8; ++c) {
@@ -679,7 +712,7 @@ __global__ void quantise_kernel(const NodeF* in, uint64_t nn, NodeQ* out) {
     }
     q.px = pp[0]; q.py = pp[1]; q.pz = pp[2];
     q.ex = ee[0]; q.ey = ee[1]; q.ez = ee[2];
-    q.valid = uint8_t(nc);
+    q.imask = uint8_t(im);
     q.child_base = a.child_base;
     q.prim_base = a.prim_base;
     for (int c = 0; c < 8; ++c) q.meta[c] = a.meta[c];

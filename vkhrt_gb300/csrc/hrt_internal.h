@@ -21,19 +21,25 @@ constexpr uint32_t kErrTimeout = 2u;
 //   meta[k] == 0            empty slot
 //   meta[k] & 0x80          internal child, node index child_base + (meta & 7)
 //   otherwise               leaf: (meta >> 5) primitives from slot prim_base + (meta & 31)
+// Child slots: a node's children sit in the 8 slots by direction (slot s holds the child whose
+// centre lies furthest along (s&1 ? +x : -x, s&2 ? +y : -y, s&4 ? +z : -z) from the node's
+// centre), so a ray visits slots in the order i ^ octant(ray) roughly front to back. Internal
+// children are numbered from child_base in slot order, leaf primitives from prim_base in slot
+// order. Empty slots hold an empty box (FP32: lo = +inf, hi = -inf; 8-bit: qlo = 255, qhi = 0).
 struct alignas(16) NodeF {  // 224 bytes, FP32 child boxes (structure of arrays)
     float lo_x[8], hi_x[8], lo_y[8], hi_y[8], lo_z[8], hi_z[8];
     uint32_t child_base, prim_base;
+    uint32_t imask;  // bit s set when slot s holds an internal child
+    uint32_t pad0;
     uint8_t meta[8];
-    uint32_t valid;  // bit q set when slot q holds a child
-    uint32_t pad[3];
+    uint32_t pad[2];
 };
 static_assert(sizeof(NodeF) == 224, "NodeF layout");
 
 struct alignas(16) NodeQ {  // 80 bytes, child boxes as 8-bit offsets on a per-axis 2^e grid
     float px, py, pz;       // grid origin (min of the child boxes)
     uint8_t ex, ey, ez;     // e + 127
-    uint8_t valid;          // bit q set when slot q holds a child
+    uint8_t imask;          // bit s set when slot s holds an internal child
     uint32_t child_base, prim_base;
     uint8_t meta[8];
     uint8_t qlo_x[8], qhi_x[8], qlo_y[8], qhi_y[8], qlo_z[8], qhi_z[8];

@@ -8,10 +8,13 @@
 // Work: warps take 32 work items at a time from a global counter; 32 consecutive items are one
 // 8x4 pixel tile of one scene, so a warp's rays are coherent. Each thread traces all samples
 // of its pixel (primary ray, shading, shadow ray) and writes the averaged pixel.
-// Traversal: per-thread stack of (node or leaf reference, entry distance); at each BVH8 node
-// the eight child boxes are tested, the hits sorted by entry distance with a sorting network
-// in registers and pushed far to near. All waits are bounded: a full stack or more than
-// kMaxTraversalSteps steps ends the ray and sets a bit in the device error word.
+// Traversal (frame kernel): children sit in slots by direction, so a ray visits the hit
+// children of a node in the order i ^ octant(ray) without sorting; the stack holds node groups
+// (child_base, hit bits, internal-child mask) and parked leaf groups, one entry per visited
+// node at most. The explicit-ray kernel keeps a per-thread stack of (reference, entry
+// distance) with the hits of a node sorted by a sorting network. All waits are bounded: a full
+// stack or more than kMaxTraversalSteps steps ends the ray and sets a bit in the device error
+// word.
 #include <cuda_fp16.h>
 
 #include <mutex>
@@ -41,6 +44,27 @@ template <class T> __device__ __forceinline__ T length(V3<T> v) { return sqrt(do
 template <class T> __device__ __forceinline__ T gmin(T x, T y) { return (y < x) ? y : x; }  // glm order
 template <class T> __device__ __forceinline__ T gmax(T x, T y) { return (x < y) ? y : x; }
 template <class T> __device__ __forceinline__ T gabs(T x) { return x >= T(0) ? x : -x; }
+
+// Explicitly rounded forms (fixed fused multiply-adds, no contraction left to the compiler),
+// for values that must not depend on how a kernel variant is compiled: instance transforms,
+// normals, shading.
+__device__ __forceinline__ float dot_rn(V3<float> a, V3<float> b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, __fmul_rn(a.x, b.x))); }
+__device__ __forceinline__ V3<float> normalize_rn(V3<float> v) {
+    const float k = __fdiv_rn(1.0f, __fsqrt_rn(dot_rn(v, v)));
+    return mk(__fmul_rn(k, v.x), __fmul_rn(k, v.y), __fmul_rn(k, v.z));
+}
+__device__ __forceinline__ V3<float> cross_rn(V3<float> x, V3<float> y) {
+    return mk(fmaf(x.y, y.z, -__fmul_rn(y.y, x.z)), fmaf(x.z, y.x, -__fmul_rn(y.z, x.x)), fmaf(x.x, y.y, -__fmul_rn(y.x, x.y)));
+}
+// rows of a 3x4 affine matrix applied to a point / a direction
+__device__ __forceinline__ V3<float> xform_point(const float* m, V3<float> p) {
+    return mk(fmaf(m[2], p.z, fmaf(m[1], p.y, fmaf(m[0], p.x, m[3]))), fmaf(m[6], p.z, fmaf(m[5], p.y, fmaf(m[4], p.x, m[7]))),
+              fmaf(m[10], p.z, fmaf(m[9], p.y, fmaf(m[8], p.x, m[11]))));
+}
+__device__ __forceinline__ V3<float> xform_dir(const float* m, V3<float> v) {
+    return mk(fmaf(m[2], v.z, fmaf(m[1], v.y, __fmul_rn(m[0], v.x))), fmaf(m[6], v.z, fmaf(m[5], v.y, __fmul_rn(m[4], v.x))),
+              fmaf(m[10], v.z, fmaf(m[9], v.y, __fmul_rn(m[8], v.x))));
+}
 
 // ---------------------------------------------------------------- Phantom (Prhi)
 // curve.glsl:9-31
@@ -424,7 +448,6 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
 }
 
 // ---------------------------------------------------------------- nodes
-__device__ __forceinline__ float bytef(uint32_t w, int k) { return float((w >> (8 * k)) & 0xffu); }
 
 // Reciprocal direction with zero components replaced by +-1e20, so slab distances stay finite
 // (a ray inside a slab gets -huge..+huge, one outside a pair of equal signs).
@@ -444,9 +467,12 @@ __device__ __forceinline__ float biased_byte(uint32_t w, int k) {
 // per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 33023 2^e |inv|), and that
 // bound is subtracted from the axis's near planes and added to its far planes, so a box is
 // never lost to rounding (a near-parallel axis widens only its own planes).
-template <bool kQuant>
+// Empty slots hold empty boxes and fail the test. kWithT: also the entry distances tn[8] and
+// the meta words m0/m1 (sorted traversal); without it only the hit mask, child_base and imask.
+template <bool kQuant, bool kWithT = true>
 __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, const RayState& R, float tfar,
-                                              float* tn, uint32_t* base, uint32_t* pbase, uint32_t* m0, uint32_t* m1) {
+                                              float* tn, uint32_t* base, uint32_t* pbase, uint32_t* m0, uint32_t* m1,
+                                              uint32_t* imask = nullptr) {
     uint32_t mask = 0;
     const bool nx = R.inv.x < 0.0f, ny = R.inv.y < 0.0f, nz = R.inv.z < 0.0f;
     if (!kQuant) {
@@ -457,12 +483,15 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         float4 n0 = __ldg(p + ax), n1 = __ldg(p + ax + 1), f0 = __ldg(p + (2 - ax)), f1 = __ldg(p + (3 - ax));
         float4 n2 = __ldg(p + ay), n3 = __ldg(p + ay + 1), f2 = __ldg(p + (10 - ay)), f3 = __ldg(p + (11 - ay));
         float4 n4 = __ldg(p + az), n5 = __ldg(p + az + 1), f4 = __ldg(p + (18 - az)), f5 = __ldg(p + (19 - az));
-        float4 tail = __ldg(p + 12);
+        const float4 tail = __ldg(p + 12);  // child_base, prim_base, imask, pad
         *base = __float_as_uint(tail.x);
-        *pbase = __float_as_uint(tail.y);
-        *m0 = __float_as_uint(tail.z);
-        *m1 = __float_as_uint(tail.w);
-        const uint32_t valid = __float_as_uint(__ldg(reinterpret_cast<const float*>(p + 13)));
+        if (imask) *imask = __float_as_uint(tail.z);
+        if (kWithT) {
+            const float2 mw = __ldg(reinterpret_cast<const float2*>(p + 13));
+            *pbase = __float_as_uint(tail.y);
+            *m0 = __float_as_uint(mw.x);
+            *m1 = __float_as_uint(mw.y);
+        }
         const float NX[8] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, n1.z, n1.w};
         const float FX[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
         const float NY[8] = {n2.x, n2.y, n2.z, n2.w, n3.x, n3.y, n3.z, n3.w};
@@ -475,10 +504,10 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
                             fmaxf((NZ[q] - R.o.z) * R.inv.z, R.tmin));
             float b = fminf(fminf((FX[q] - R.o.x) * R.inv.x, (FY[q] - R.o.y) * R.inv.y),
                             fminf((FZ[q] - R.o.z) * R.inv.z, tfar));
-            tn[q] = a;
+            if (kWithT) tn[q] = a;
             if (a <= b * kEps) mask |= 1u << q;
         }
-        return mask & valid;
+        return mask;
     } else {
         const uint4* p = reinterpret_cast<const uint4*>(static_cast<const NodeQ*>(nodes) + ni);
         uint4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
@@ -504,11 +533,13 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         float ez = kS * fmaf(1.00775146484375f, fabsf(sz), fabsf(bz));
         const float cx = bx - sx, cy = by - sy, cz = bz - sz;
         const float bxn = cx - ex, bxf = cx + ex, byn = cy - ey, byf = cy + ey, bzn = cz - ez, bzf = cz + ez;
-        const uint32_t valid = (w0.w >> 24) & 0xffu;
+        if (imask) *imask = w0.w >> 24;
         *base = w1.x;
-        *pbase = w1.y;
-        *m0 = w1.z;
-        *m1 = w1.w;
+        if (kWithT) {
+            *pbase = w1.y;
+            *m0 = w1.z;
+            *m1 = w1.w;
+        }
         // near / far byte words per axis (qlo = .x .y, qhi = .z .w)
         const uint32_t nxw0 = nx ? w2.z : w2.x, nxw1 = nx ? w2.w : w2.y, fxw0 = nx ? w2.x : w2.z, fxw1 = nx ? w2.y : w2.w;
         const uint32_t nyw0 = ny ? w3.z : w3.x, nyw1 = ny ? w3.w : w3.y, fyw0 = ny ? w3.x : w3.z, fyw1 = ny ? w3.y : w3.w;
@@ -523,11 +554,29 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
                             fmaxf(fmaf(biased_byte(wnz, by_), sz, bzn), R.tmin));
             float b = fminf(fminf(fmaf(biased_byte(wfx, by_), sx, bxf), fmaf(biased_byte(wfy, by_), sy, byf)),
                             fminf(fmaf(biased_byte(wfz, by_), sz, bzf), tfar));
-            tn[q] = a;
+            if (kWithT) tn[q] = a;
             if (a <= b) mask |= 1u << q;
         }
-        return mask & valid;
+        return mask;
     }
+}
+
+// {child_base, prim_base, meta[0..3], meta[4..7]} of node ni.
+template <bool kQuant>
+__device__ __forceinline__ uint4 node_header(const void* nodes, uint32_t ni) {
+    if (kQuant) return __ldg(reinterpret_cast<const uint4*>(static_cast<const NodeQ*>(nodes) + ni) + 1);
+    const uint4* p = reinterpret_cast<const uint4*>(static_cast<const NodeF*>(nodes) + ni);
+    const uint4 t = __ldg(p + 12);
+    const uint2 m = __ldg(reinterpret_cast<const uint2*>(p + 13));
+    return make_uint4(t.x, t.y, m.x, m.y);
+}
+
+// Slot-order mask -> traversal order for a ray of direction octant oct: bit i <- bit i ^ oct.
+__device__ __forceinline__ uint32_t oct_permute(uint32_t m, uint32_t oct) {
+    if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (oct & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
+    return m;
 }
 
 __device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
@@ -587,6 +636,7 @@ __device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit
             if (k >= npush) continue;
             uint32_t q = key[k] & 7u;
             uint32_t m = ((q < 4 ? m0 : m1) >> (8 * (q & 3))) & 0xffu;
+            if (m == 0) continue;  // an empty slot (only a degenerate ray can pass its empty box)
             uint32_t ref = (m & 0x80u) ? base + (m & 7u)
                                        : (kLeafFlag | ((pbase + (m & 31u)) << 2) | ((m >> 5) - 1u));
             stack[sp++] = make_uint2(ref, key[k] & ~7u);
@@ -608,10 +658,8 @@ __device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> 
         if (I.identity) { R.o = wo; R.d = wd; }
         else {
             const float* m = I.w2o;
-            R.o = mk(m[0] * wo.x + m[1] * wo.y + m[2] * wo.z + m[3], m[4] * wo.x + m[5] * wo.y + m[6] * wo.z + m[7],
-                     m[8] * wo.x + m[9] * wo.y + m[10] * wo.z + m[11]);
-            R.d = mk(m[0] * wd.x + m[1] * wd.y + m[2] * wd.z, m[4] * wd.x + m[5] * wd.y + m[6] * wd.z,
-                     m[8] * wd.x + m[9] * wd.y + m[10] * wd.z);
+            R.o = xform_point(m, wo);
+            R.d = xform_dir(m, wd);
         }
         R.inv = safe_inv(R.d);
         R.tmin = tmin;
@@ -641,10 +689,8 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
     V3<float> o = wo, d = wd;
     if (!I.identity) {
         const float* m = I.w2o;
-        o = mk(m[0] * wo.x + m[1] * wo.y + m[2] * wo.z + m[3], m[4] * wo.x + m[5] * wo.y + m[6] * wo.z + m[7],
-               m[8] * wo.x + m[9] * wo.y + m[10] * wo.z + m[11]);
-        d = mk(m[0] * wd.x + m[1] * wd.y + m[2] * wd.z, m[4] * wd.x + m[5] * wd.y + m[6] * wd.z,
-               m[8] * wd.x + m[9] * wd.y + m[10] * wd.z);
+        o = xform_point(m, wo);
+        d = xform_dir(m, wd);
     }
     // Normals are differences of points a hair radius apart; they are formed from the
     // full-precision vectors relative to the primitive's reference point o' = o + ts d.
@@ -659,7 +705,15 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         V3<float> W[4];
         for (int k = 0; k < 4; ++k)
             W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
-        n = normalize(h.sl * d - bez_point(W, h.u));
+        // the curve point in Bernstein form with fixed fused operations
+        const float u = h.u, v = __fsub_rn(1.0f, u);
+        const float b0 = __fmul_rn(__fmul_rn(v, v), v), b1 = __fmul_rn(__fmul_rn(3.0f, __fmul_rn(v, v)), u);
+        const float b2 = __fmul_rn(__fmul_rn(3.0f, v), __fmul_rn(u, u)), b3 = __fmul_rn(__fmul_rn(u, u), u);
+        V3<float> c;
+        c.x = fmaf(b3, W[3].x, fmaf(b2, W[2].x, fmaf(b1, W[1].x, __fmul_rn(b0, W[0].x))));
+        c.y = fmaf(b3, W[3].y, fmaf(b2, W[2].y, fmaf(b1, W[1].y, __fmul_rn(b0, W[0].y))));
+        c.z = fmaf(b3, W[3].z, fmaf(b2, W[2].z, fmaf(b1, W[1].z, __fmul_rn(b0, W[0].z))));
+        n = normalize_rn(mk(fmaf(h.sl, d.x, -c.x), fmaf(h.sl, d.y, -c.y), fmaf(h.sl, d.z, -c.z)));
     } else if (B.type == HRT_BLAS_LSS) {
         // triangle_closest_hit.rchit:43-58: hit - mix(p0, p1, u)
         const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + h.slot;
@@ -667,7 +721,9 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         V3<float> p0 = mk(a.x, a.y, a.z), p1 = mk(b.x, b.y, b.z);
         float ts = h.ts;
         V3<float> w0 = mk(rel_coord(p0.x, o.x, ts, d.x), rel_coord(p0.y, o.y, ts, d.y), rel_coord(p0.z, o.z, ts, d.z));
-        n = normalize(h.sl * d - w0 - h.u * (p1 - p0));
+        const V3<float> ax = mk(__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z));
+        n = normalize_rn(mk(fmaf(-h.u, ax.x, fmaf(h.sl, d.x, -w0.x)), fmaf(-h.u, ax.y, fmaf(h.sl, d.y, -w0.y)),
+                            fmaf(-h.u, ax.z, fmaf(h.sl, d.z, -w0.z))));
     } else {
         // DOTS vertices carry no normals (geometry_processor.cpp:259-264): the face normal
         const PrimDots* pr = static_cast<const PrimDots*>(B.prims) + h.slot;
@@ -679,12 +735,13 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         V3<float> A0 = s0 + va, A1 = e0 - vb;
         V3<float> third = (k & 1u) ? (s0 - va) : (e0 + vb);
         V3<float> v1 = (k & 1u) ? third : A1, v2 = (k & 1u) ? A1 : third;
-        n = normalize(cross(v1 - A0, v2 - A0));
+        n = normalize_rn(cross_rn(v1 - A0, v2 - A0));
     }
     if (!I.identity) {
         const float* q = I.nrm;
-        n = normalize(mk(q[0] * n.x + q[1] * n.y + q[2] * n.z, q[3] * n.x + q[4] * n.y + q[5] * n.z,
-                         q[6] * n.x + q[7] * n.y + q[8] * n.z));
+        n = normalize_rn(mk(fmaf(q[2], n.z, fmaf(q[1], n.y, __fmul_rn(q[0], n.x))),
+                            fmaf(q[5], n.z, fmaf(q[4], n.y, __fmul_rn(q[3], n.x))),
+                            fmaf(q[8], n.z, fmaf(q[7], n.y, __fmul_rn(q[6], n.x)))));
     }
     return n;
 }
@@ -735,13 +792,14 @@ __device__ __forceinline__ void warp_add(unsigned long long* ctr, uint32_t v) {
 // pixel: its samples, each a primary ray and, when shading with shadows, one shadow ray).
 //   refill     lanes without a task take pixels with one warp-aggregated atomic once enough
 //              lanes are idle (ballot + popc ranks), so finished rays do not idle the warp;
-//   node phase lanes pop and test nodes together until each holds a leaf or runs dry;
-//   leaf phase lanes with a leaf run its intersector together (the Phantom solve is long, so
-//              keeping it out of the node loop keeps the warp converged);
+//   node phase lanes test the next child of their node group together until each holds
+//              leaf children or runs dry;
+//   leaf phase lanes with leaf children test one each (the Phantom solve is long, so keeping
+//              it out of the node loop keeps the warp converged);
 //   completion a finished ray moves to the next instance, spawns its shadow ray, shades, or
 //              finishes the pixel.
-// The stack's top kShort entries live in shared memory (one column per thread), deeper ones
-// in local memory. Results do not depend on scheduling: one lane handles all samples of a
+// The stack's bottom kShort entries live in shared memory (one column per thread), deeper
+// ones in local memory. Results do not depend on scheduling: one lane handles all samples of a
 // pixel in order and each ray's closest hit is the least (t, instance, id).
 constexpr int kShort = 16;
 constexpr int kRefill = 16;
@@ -768,8 +826,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     Hit h{0.0f, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
     uint32_t inst_cur = 0, skip_inst = 0xffffffffu, skip_slot = 0xffffffffu;
     int sp = 0;
-    uint32_t leaf = 0, steps = 0;
-    bool have_leaf = false;
+    uint32_t steps = 0;
+    const void* nodes = nullptr;                 // node array of the current instance's BLAS
+    uint32_t oct = 0;                            // direction octant of the object-space ray
+    uint32_t cur_base = 0, cur_bits = 0;         // node group: hits in visiting order (bits 0-7), imask (8-15)
+    uint32_t leaf_node = 0, leaf_bits = 0;       // leaf children (slot mask) of node leaf_node, untested
 
     auto push = [&](uint2 e) {
         if (sp < kShort) s_stack[sp][tid] = e;
@@ -786,10 +847,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         if (I.identity) { R.o = wo; R.d = wd; }
         else {
             const float* m = I.w2o;
-            R.o = mk(m[0] * wo.x + m[1] * wo.y + m[2] * wo.z + m[3], m[4] * wo.x + m[5] * wo.y + m[6] * wo.z + m[7],
-                     m[8] * wo.x + m[9] * wo.y + m[10] * wo.z + m[11]);
-            R.d = mk(m[0] * wd.x + m[1] * wd.y + m[2] * wd.z, m[4] * wd.x + m[5] * wd.y + m[6] * wd.z,
-                     m[8] * wd.x + m[9] * wd.y + m[10] * wd.z);
+            R.o = xform_point(m, wo);
+            R.d = xform_dir(m, wd);
         }
         R.inv = safe_inv(R.d);
         R.tmin = cur_tmin;
@@ -804,7 +863,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
         if (type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
         else if (type == HRT_BLAS_DOTS) R.tr = make_triray(R.d);
-        push(make_uint2(0u, __float_as_uint(cur_tmin)));
+        nodes = B.nodes;
+        oct = (R.inv.x < 0.0f ? 1u : 0u) | (R.inv.y < 0.0f ? 2u : 0u) | (R.inv.z < 0.0f ? 4u : 0u);
+        cur_base = 0;  // the root as a group of one internal child in slot 0
+        cur_bits = (1u << oct) | (1u << 8);
         return true;
     };
     auto start_ray = [&](V3<float> o, V3<float> d, float tmin, float tmax) {
@@ -813,6 +875,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         cur_tmin = tmin;
         h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
         sp = 0;
+        cur_bits = 0;
+        leaf_bits = 0;
         steps = 0;
         const uint32_t n = L.scenes[si].ninst;
         for (inst_cur = 0; inst_cur < n; ++inst_cur)
@@ -837,7 +901,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         ++sample;
         if (sample < S.spp) { start_primary(); return; }
         float inv = 1.0f / float(S.spp);
-        S.fb[pix] = make_float4(acc0 * inv, acc1 * inv, acc2 * inv, 1.0f);
+        S.fb[pix] = make_float4(__fmul_rn(acc0, inv), __fmul_rn(acc1, inv), __fmul_rn(acc2, inv), 1.0f);
         has_ray = false;
     };
     auto finish_phase = [&]() {
@@ -857,7 +921,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             if (!found) { next_sample(); return; }
             if (L.shading == HRT_SHADE_DEBUG) {
                 uint32_t c = h.id % 6u;
-                acc0 += kPalette[c][0]; acc1 += kPalette[c][1]; acc2 += kPalette[c][2];
+                acc0 = __fadd_rn(acc0, kPalette[c][0]);
+                acc1 = __fadd_rn(acc1, kPalette[c][1]);
+                acc2 = __fadd_rn(acc2, kPalette[c][2]);
                 next_sample();
                 return;
             }
@@ -869,16 +935,20 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 shadow_hit = false;
                 shadow = true;
                 ++shadow_rays;
-                V3<float> hp = wo + h.t * wd;
+                V3<float> hp = mk(fmaf(h.t, wd.x, wo.x), fmaf(h.t, wd.y, wo.y), fmaf(h.t, wd.z, wo.z));
                 start_ray(hp, mk(0.0f, 1.0f, 0.0f), L.shadow_tmin, L.tmax);
                 return;
             }
-            acc0 += ndl * 0.4f + 0.3f; acc1 += ndl * 0.2f + 0.3f; acc2 += ndl * 0.1f + 0.3f;
+            acc0 = __fadd_rn(acc0, fmaf(ndl, 0.4f, 0.3f));
+            acc1 = __fadd_rn(acc1, fmaf(ndl, 0.2f, 0.3f));
+            acc2 = __fadd_rn(acc2, fmaf(ndl, 0.1f, 0.3f));
             next_sample();
             return;
         }
         float lit = shadow_hit ? 0.0f : ndl;
-        acc0 += lit * 0.4f + 0.3f; acc1 += lit * 0.2f + 0.3f; acc2 += lit * 0.1f + 0.3f;
+        acc0 = __fadd_rn(acc0, fmaf(lit, 0.4f, 0.3f));
+        acc1 = __fadd_rn(acc1, fmaf(lit, 0.2f, 0.3f));
+        acc2 = __fadd_rn(acc2, fmaf(lit, 0.1f, 0.3f));
         if (shadow_hit && L.record_hits && S.hits) S.hits[rec].flags = prim_flags | HRT_HIT_SHADOWED;
         shadow = false;
         next_sample();
@@ -923,68 +993,78 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         }
         if (L.count_stats) { long long c = clock64(); cyc_other += c - clk; clk = c; }
         // ---- node phase: runs while some lane still searches for a leaf; with speculation,
-        // lanes that already hold one keep walking nodes (a second leaf goes back on the stack)
+        // lanes that already hold leaves keep walking nodes (further leaves go on the stack).
+        // A lane visits the children of its current node group in the order i ^ oct (slots are
+        // laid out by direction, so roughly near to far); a visited node's internal hits become
+        // the new group (the rest of the old one goes on the stack) and its leaf hits become
+        // the lane's pending leaves.
         bool stalled = false;
         for (;;) {
-            bool searching = has_ray && !have_leaf && sp > 0;
+            const bool more = (cur_bits & 0xffu) != 0u || sp > 0;
+            const bool searching = has_ray && !leaf_bits && more;
             if (!__any_sync(kFull, searching)) break;
-            bool want = searching || (spec && has_ray && have_leaf && !stalled && sp > 0);
+            const bool want = searching || (spec && has_ray && leaf_bits && !stalled && more);
             if (!want) continue;
             if (++steps > kMaxTraversalSteps) {
                 err |= kErrTimeout;
                 sp = 0;
+                cur_bits = leaf_bits = 0;
                 continue;
             }
-            uint2 e = pop();
-            if (__uint_as_float(e.y) > h.t) continue;
-            if (e.x & kLeafFlag) {
-                if (have_leaf) {  // speculative lane found a second leaf: keep it for later
-                    push(e);
-                    stalled = true;
-                } else {
-                    leaf = e.x;
-                    have_leaf = true;
+            if (!(cur_bits & 0xffu)) {
+                const uint2 e = pop();
+                if (e.x & kLeafFlag) {  // leaves parked by a speculating lane
+                    if (leaf_bits) {
+                        push(e);
+                        stalled = true;
+                    } else {
+                        leaf_node = e.x & ~kLeafFlag;
+                        leaf_bits = e.y;
+                    }
+                    continue;
                 }
-                continue;
+                cur_base = e.x;
+                cur_bits = e.y;
             }
+            const uint32_t i = __ffs(cur_bits & 0xffu) - 1;
+            cur_bits &= ~(1u << i);
+            const uint32_t slot = i ^ oct;
+            const uint32_t child = cur_base + __popc((cur_bits >> 8) & ((1u << slot) - 1u));
             ++st.nodes;
-            const DevBlas& B = L.scenes[si].inst[inst_cur].b;
-            float tn[8];
-            uint32_t base, pbase, m0, m1;
-            uint32_t mask = test_node<kQuant>(B.nodes, e.x, R, h.t, tn, &base, &pbase, &m0, &m1);
-            if (!mask) continue;
-            uint32_t key[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q)  // tn >= tmin >= 0, so its bits order as unsigned integers
-                key[q] = (mask >> q) & 1u ? ((__float_as_uint(tn[q]) & ~7u) | uint32_t(q)) : 0xffffffffu;
-            cswap(key[0], key[2]); cswap(key[1], key[3]); cswap(key[4], key[6]); cswap(key[5], key[7]);
-            cswap(key[0], key[4]); cswap(key[1], key[5]); cswap(key[2], key[6]); cswap(key[3], key[7]);
-            cswap(key[0], key[1]); cswap(key[2], key[3]); cswap(key[4], key[5]); cswap(key[6], key[7]);
-            cswap(key[2], key[4]); cswap(key[3], key[5]);
-            cswap(key[1], key[4]); cswap(key[3], key[6]);
-            cswap(key[1], key[2]); cswap(key[3], key[4]); cswap(key[5], key[6]);
-            int npush = __popc(mask);
-            if (sp + npush > kStackSize) {
+            uint32_t base, imask;
+            const uint32_t mask = test_node<kQuant, false>(nodes, child, R, h.t, nullptr, &base, nullptr, nullptr,
+                                                           nullptr, &imask);
+            const uint32_t ih = mask & imask, lh = mask & ~imask;
+            if (sp + 2 > kStackSize) {
                 err |= kErrStackOverflow;
                 sp = 0;
+                cur_bits = leaf_bits = 0;
                 continue;
             }
-#pragma unroll
-            for (int k = 7; k >= 0; --k) {
-                if (k >= npush) continue;
-                uint32_t q = key[k] & 7u;
-                uint32_t m = ((q < 4 ? m0 : m1) >> (8 * (q & 3))) & 0xffu;
-                uint32_t ref = (m & 0x80u) ? base + (m & 7u)
-                                           : (kLeafFlag | ((pbase + (m & 31u)) << 2) | ((m >> 5) - 1u));
-                push(make_uint2(ref, key[k] & ~7u));
+            if (lh) {
+                if (!leaf_bits) {
+                    leaf_node = child;
+                    leaf_bits = lh;
+                } else {
+                    push(make_uint2(kLeafFlag | child, lh));
+                    stalled = true;
+                }
+            }
+            if (ih) {
+                if (cur_bits & 0xffu) push(make_uint2(cur_base, cur_bits));
+                cur_base = base;
+                cur_bits = oct_permute(ih, oct) | (imask << 8);
             }
         }
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_node += c - clk; clk = c; }
-        // ---- leaf phase
-        if (have_leaf) {
-            have_leaf = false;
+        // ---- leaf phase: one leaf child per lane
+        if (leaf_bits) {
             const DevBlas& B = L.scenes[si].inst[inst_cur].b;
-            uint32_t first = (leaf & ~kLeafFlag) >> 2, cnt = (leaf & 3u) + 1u;
+            const uint32_t q = __ffs(leaf_bits) - 1;
+            leaf_bits &= leaf_bits - 1u;
+            const uint4 hd = node_header<kQuant>(nodes, leaf_node);
+            const uint32_t m = ((q < 4 ? hd.z : hd.w) >> (8 * (q & 3))) & 0xffu;
+            const uint32_t first = hd.y + (m & 31u), cnt = m >> 5;
             for (uint32_t j = 0; j < cnt; ++j) {
                 uint32_t slot = first + j;
                 if (shadow && inst_cur == skip_inst && slot == skip_slot) continue;
@@ -992,13 +1072,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 if (leaf_test<kType>(B, slot, inst_cur, R, h, L.fp64_resolve != 0, st) && shadow) {
                     shadow_hit = true;
                     sp = 0;
+                    cur_bits = leaf_bits = 0;
                     break;
                 }
             }
         }
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_leaf += c - clk; clk = c; }
         // ---- completion
-        if (has_ray && !have_leaf && sp == 0) {
+        if (has_ray && !leaf_bits && sp == 0 && !(cur_bits & 0xffu)) {
             if (err) {  // a bounded loop gave up: drop the task and stop taking work
                 atomicOr(&L.counters->error, err);
                 has_ray = false;
