@@ -467,8 +467,8 @@ __device__ __forceinline__ float biased_byte(uint32_t w, int k) {
 // per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 33023 2^e |inv|), and that
 // bound is subtracted from the axis's near planes and added to its far planes, so a box is
 // never lost to rounding (a near-parallel axis widens only its own planes).
-// Empty slots hold empty boxes and fail the test. kWithT: also the entry distances tn[8] and
-// the meta words m0/m1 (sorted traversal); without it only the hit mask, child_base and imask.
+// Empty slots hold empty boxes and fail the test. tn (when given) receives the entry distances;
+// kWithT: also prim_base and the meta words m0/m1 (sorted traversal).
 template <bool kQuant, bool kWithT = true>
 __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, const RayState& R, float tfar,
                                               float* tn, uint32_t* base, uint32_t* pbase, uint32_t* m0, uint32_t* m1,
@@ -504,7 +504,7 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
                             fmaxf((NZ[q] - R.o.z) * R.inv.z, R.tmin));
             float b = fminf(fminf((FX[q] - R.o.x) * R.inv.x, (FY[q] - R.o.y) * R.inv.y),
                             fminf((FZ[q] - R.o.z) * R.inv.z, tfar));
-            if (kWithT) tn[q] = a;
+            if (tn) tn[q] = a;
             if (a <= b * kEps) mask |= 1u << q;
         }
         return mask;
@@ -554,7 +554,7 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
                             fmaxf(fmaf(biased_byte(wnz, by_), sz, bzn), R.tmin));
             float b = fminf(fminf(fmaf(biased_byte(wfx, by_), sx, bxf), fmaf(biased_byte(wfy, by_), sy, byf)),
                             fminf(fmaf(biased_byte(wfz, by_), sz, bzf), tfar));
-            if (kWithT) tn[q] = a;
+            if (tn) tn[q] = a;
             if (a <= b) mask |= 1u << q;
         }
         return mask;
@@ -807,6 +807,7 @@ constexpr int kRefill = 16;
 template <bool kQuant, int kType, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch L) {
     __shared__ uint2 s_stack[kShort][kThreads];
+    __shared__ float s_leaf_t[8][kThreads];  // entry distances of the pending leaf children, by slot
     uint2 l_stack[kStackSize - kShort];
     const int tid = threadIdx.x, lane = tid & 31;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -830,7 +831,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     const void* nodes = nullptr;                 // node array of the current instance's BLAS
     uint32_t oct = 0;                            // direction octant of the object-space ray
     uint32_t cur_base = 0, cur_bits = 0;         // node group: hits in visiting order (bits 0-7), imask (8-15)
-    uint32_t leaf_node = 0, leaf_bits = 0;       // leaf children (slot mask) of node leaf_node, untested
+    uint32_t leaf_node = 0, leaf_bits = 0;       // untested leaf children of node leaf_node, visiting order
+    bool leaf_t = false;                         // s_leaf_t holds their entry distances
 
     auto push = [&](uint2 e) {
         if (sp < kShort) s_stack[sp][tid] = e;
@@ -1013,13 +1015,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             }
             if (!(cur_bits & 0xffu)) {
                 const uint2 e = pop();
-                if (e.x & kLeafFlag) {  // leaves parked by a speculating lane
+                if (e.x & kLeafFlag) {  // leaves parked by a speculating lane (no distances kept)
                     if (leaf_bits) {
                         push(e);
                         stalled = true;
                     } else {
                         leaf_node = e.x & ~kLeafFlag;
-                        leaf_bits = e.y;
+                        leaf_bits = oct_permute(e.y, oct);
+                        leaf_t = false;
                     }
                     continue;
                 }
@@ -1032,7 +1035,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             const uint32_t child = cur_base + __popc((cur_bits >> 8) & ((1u << slot) - 1u));
             ++st.nodes;
             uint32_t base, imask;
-            const uint32_t mask = test_node<kQuant, false>(nodes, child, R, h.t, nullptr, &base, nullptr, nullptr,
+            float tn[8];
+            const uint32_t mask = test_node<kQuant, false>(nodes, child, R, h.t, tn, &base, nullptr, nullptr,
                                                            nullptr, &imask);
             const uint32_t ih = mask & imask, lh = mask & ~imask;
             if (sp + 2 > kStackSize) {
@@ -1044,7 +1048,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             if (lh) {
                 if (!leaf_bits) {
                     leaf_node = child;
-                    leaf_bits = lh;
+                    leaf_bits = oct_permute(lh, oct);
+                    leaf_t = true;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) s_leaf_t[q][tid] = tn[q];
                 } else {
                     push(make_uint2(kLeafFlag | child, lh));
                     stalled = true;
@@ -1057,12 +1064,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             }
         }
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_node += c - clk; clk = c; }
-        // ---- leaf phase: one leaf child per lane
+        // ---- leaf phase: one leaf child per lane, nearest first; one whose box starts beyond
+        // the closest hit so far is skipped
         if (leaf_bits) {
             const DevBlas& B = L.scenes[si].inst[inst_cur].b;
-            const uint32_t q = __ffs(leaf_bits) - 1;
+            const uint32_t q = (__ffs(leaf_bits) - 1) ^ oct;
             leaf_bits &= leaf_bits - 1u;
-            const uint4 hd = node_header<kQuant>(nodes, leaf_node);
+            const bool beyond = leaf_t && s_leaf_t[q][tid] > h.t;
+            const uint4 hd = beyond ? make_uint4(0u, 0u, 0u, 0u) : node_header<kQuant>(nodes, leaf_node);
             const uint32_t m = ((q < 4 ? hd.z : hd.w) >> (8 * (q & 3))) & 0xffu;
             const uint32_t first = hd.y + (m & 31u), cnt = m >> 5;
             for (uint32_t j = 0; j < cnt; ++j) {
