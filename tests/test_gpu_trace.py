@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import vkhrt_gb300 as H
-from hairscene import DOTS, LSS, PHANTOM, OracleScene, aimed_rays, compare_hits, lines_from_strands, oracle_geometry
+from hairscene import DOTS, LSS, PHANTOM, P, OracleScene, aimed_rays, compare_hits, lines_from_strands, oracle_geometry
 
 pytestmark = pytest.mark.gpu
 
@@ -274,3 +274,38 @@ def test_kernel_variants_and_autotune_give_identical_frames(ctx, tmp_path):
     for (a, ha), (_, _, _, fr) in zip(ref, scenes):
         b2, hb = fr.download(hits=True)
         assert np.array_equal(ha, hb) and np.abs(a - b2).max() <= 1e-6
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_frame_primary_hits_equal_explicit_rays(ctx, orc, precision):
+    """A frame's primary hits (node-group traversal, FP64 re-solve as a second pass over the
+    listed pixels) equal hrt_trace_rays on the same rays (sorted traversal, FP64 re-solve
+    inline): same ids and flags, t within 1e-6 relative. The rays come from the oracle's ray
+    generation, which matches the GPU's bit for bit."""
+    w, h = 192, 160
+    v, r, off = H.generate_strands(H.StrandParams(seed=1001, nstrands=2000, nverts=32))
+    blas = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r, strand_offsets=off,
+                    precision=H.Precision(precision)), ctx)
+    tlas = H.TopLevelAccelerationStructure([blas], ctx)
+    cam = H.scene_camera(w, h)
+    vi, pi = H.camera_arrays(cam)
+    fr = H.Frame(ctx, w, h, 1, with_hits=True)
+    H.trace(ctx, tlas, cam, fr, H.trace_params(shading=2, record_hits=1, count_stats=1))
+    _, fh = fr.download(hits=True)
+    rays = np.zeros((h * w, 6), np.float32)
+    o3 = np.zeros(3, np.float32)
+    d3 = np.zeros(3, np.float32)
+    for py in range(h):
+        for px in range(w):
+            orc.orc_raygen_f32(P(vi), P(pi), px, py, w, h, 0.5, 0.5, P(o3), P(d3))
+            rays[py * w + px, :3] = o3
+            rays[py * w + px, 3:] = d3
+    rh = H.trace_rays(ctx, tlas, rays)
+    assert (fh["t"] >= 0).sum() > 1000
+    assert np.array_equal(fh["prim"], rh["prim"]) and np.array_equal(fh["inst"], rh["inst"])
+    assert np.array_equal(fh["flags"] & H.HIT_FP64, rh["flags"] & H.HIT_FP64)
+    hit = fh["t"] >= 0
+    assert np.array_equal(hit, rh["t"] >= 0)
+    assert np.max(np.abs(fh["t"][hit] - rh["t"][hit]) / rh["t"][hit]) <= 1e-6
+    print("fp64 resolves", fr.stats()["fp64_resolves"], "fp64 hits", int(((fh["flags"] & H.HIT_FP64) != 0).sum()))

@@ -108,16 +108,18 @@ _lib = None
 
 
 def load(build_if_missing: bool = True) -> ctypes.CDLL:
-    """Load libhrt.so (building it with nvcc if it is missing or stale)."""
+    """Load libhrt.so (building it with nvcc if it is missing or stale). The environment
+    variable HRT_LIBRARY names another build of the same library to load instead."""
     global _lib
     if _lib is not None:
         return _lib
-    if build_if_missing:
+    path = os.environ.get("HRT_LIBRARY") or LIB_PATH
+    if build_if_missing and path == LIB_PATH:
         from . import build as _build
         _build.build()
-    if not os.path.exists(LIB_PATH):
-        raise RuntimeError(f"{LIB_PATH} is missing: the CUDA library must be built (vkhrt_gb300.build.build())")
-    lib = ctypes.CDLL(LIB_PATH)
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: the CUDA library must be built (vkhrt_gb300.build.build())")
+    lib = ctypes.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)
         fn.restype = res

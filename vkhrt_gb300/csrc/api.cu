@@ -46,6 +46,7 @@ struct hrt_frame {
     hrt_hit* hits = nullptr;
     SceneLaunch* dscene = nullptr;
     TraceCounters* counters = nullptr;
+    uint32_t* resolve_list = nullptr;  // one entry per pixel (FP64 pass)
     hrt_frame_stats stats{};
     bool stats_pending = false;
     uint64_t pending_primary = 0;
@@ -55,6 +56,7 @@ struct hrt_batch {
     hrt_context* ctx = nullptr;
     SceneLaunch* dscenes = nullptr;
     TraceCounters* counters = nullptr;
+    uint32_t* resolve_list = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<hrt_frame*> frames;
@@ -183,7 +185,7 @@ uint32_t prim_kind(uint32_t type_mask) {
 }
 
 TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32_t n, uint64_t total, TraceCounters* c,
-                        uint32_t type_mask) {
+                        uint32_t type_mask, uint32_t* resolve_list, uint64_t resolve_cap) {
     TraceLaunch L;
     L.prim_kind = prim_kind(type_mask);
     L.scenes = ds;
@@ -202,6 +204,8 @@ TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32
     L.refill = p->refill > 32 ? 32 : p->refill;
     L.speculative = p->speculative;
     L.counters = c;
+    L.resolve_list = resolve_list;
+    L.resolve_cap = resolve_cap;
     return L;
 }
 
@@ -619,6 +623,7 @@ hrt_status hrt_frame_create(hrt_context* ctx, uint32_t w, uint32_t h, uint32_t s
     if (e == cudaSuccess && with_hits) e = cudaMalloc(&f->hits, uint64_t(w) * h * spp * sizeof(hrt_hit));
     if (e == cudaSuccess) e = cudaMalloc(&f->dscene, sizeof(SceneLaunch));
     if (e == cudaSuccess) e = cudaMalloc(&f->counters, sizeof(TraceCounters));
+    if (e == cudaSuccess) e = cudaMalloc(&f->resolve_list, uint64_t(w) * h * sizeof(uint32_t));
     if (e != cudaSuccess) {
         hrt_frame_destroy(f);
         return cuda_fail(ctx, e, "hrt_frame_create");
@@ -634,6 +639,7 @@ hrt_status hrt_frame_destroy(hrt_frame* f) {
     if (f->hits) cudaFree(f->hits);
     if (f->dscene) cudaFree(f->dscene);
     if (f->counters) cudaFree(f->counters);
+    if (f->resolve_list) cudaFree(f->resolve_list);
     delete f;
     return HRT_OK;
 }
@@ -688,7 +694,8 @@ hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* c
     fill_scene(sl, tlas, cam, f, 0);
     CK(ctx, cudaMemcpyAsync(f->dscene, &sl, sizeof(sl), cudaMemcpyHostToDevice, s), "upload scene");
     CK(ctx, cudaMemsetAsync(f->counters, 0, sizeof(TraceCounters), s), "reset counters");
-    TraceLaunch L = make_launch(p, f->dscene, 1, sl.work_count, f->counters, tlas->type_mask);
+    TraceLaunch L = make_launch(p, f->dscene, 1, sl.work_count, f->counters, tlas->type_mask, f->resolve_list,
+                                uint64_t(f->w) * f->h);
     CK(ctx, launch_trace(L, tlas->quantised, s, ctx->sm_count), "launch trace");
     f->pending_primary = uint64_t(f->w) * f->h * f->spp;
     f->stats_pending = true;
@@ -783,6 +790,7 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
         work += sl[i].work_count;
         primary += uint64_t(scenes[i].frame->w) * scenes[i].frame->h * scenes[i].frame->spp;
     }
+    if (work >= (1ull << 32)) return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_batch_create: more than 2^32 pixel work items");
     hrt_batch* b = new (std::nothrow) hrt_batch();
     if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_batch_create: host allocation");
     b->ctx = ctx;
@@ -790,8 +798,11 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
     b->async = p->async != 0;
     for (uint32_t i = 0; i < n; ++i) b->frames.push_back(scenes[i].frame);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint64_t npix = 0;
+    for (uint32_t i = 0; i < n; ++i) npix += uint64_t(scenes[i].frame->w) * scenes[i].frame->h;
     cudaError_t e = cudaMalloc(&b->dscenes, n * sizeof(SceneLaunch));
     if (e == cudaSuccess) e = cudaMalloc(&b->counters, sizeof(TraceCounters));
+    if (e == cudaSuccess) e = cudaMalloc(&b->resolve_list, npix * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->dscenes, sl.data(), n * sizeof(SceneLaunch), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     // capture: counter reset + the persistent trace launch
@@ -800,7 +811,7 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         cudaError_t e1 = cudaMemsetAsync(b->counters, 0, sizeof(TraceCounters), cap);
-        TraceLaunch L = make_launch(p, b->dscenes, n, work, b->counters, type_mask);
+        TraceLaunch L = make_launch(p, b->dscenes, n, work, b->counters, type_mask, b->resolve_list, npix);
         cudaError_t e2 = e1 == cudaSuccess ? launch_trace(L, quant, cap, ctx->sm_count) : e1;
         cudaError_t e3 = cudaStreamEndCapture(cap, &b->graph);
         e = e2 != cudaSuccess ? e2 : e3;
@@ -854,15 +865,20 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
     }
     SceneLaunch* ds_ = nullptr;
     TraceCounters* ctr = nullptr;
+    uint32_t* rlist = nullptr;
+    uint64_t npix = 0;
+    for (uint32_t i = 0; i < n; ++i) npix += uint64_t(scenes[i].frame->w) * scenes[i].frame->h;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto cleanup = [&]() {
         if (ds_) cudaFree(ds_);
         if (ctr) cudaFree(ctr);
+        if (rlist) cudaFree(rlist);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
     };
     cudaError_t e = cudaMalloc(&ds_, n * sizeof(SceneLaunch));
     if (e == cudaSuccess) e = cudaMalloc(&ctr, sizeof(TraceCounters));
+    if (e == cudaSuccess) e = cudaMalloc(&rlist, npix * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemcpyAsync(ds_, sl.data(), n * sizeof(SceneLaunch), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
@@ -882,7 +898,7 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
                 p.speculative = sp;
                 p.record_hits = 0;
                 p.count_stats = 0;
-                TraceLaunch L = make_launch(&p, ds_, n, work, ctr, type_mask);
+                TraceLaunch L = make_launch(&p, ds_, n, work, ctr, type_mask, rlist, npix);
                 float tot = 0.0f;
                 for (uint32_t k = 0; k <= reps && e == cudaSuccess; ++k) {
                     e = cudaMemsetAsync(ctr, 0, sizeof(TraceCounters), s);
@@ -923,6 +939,7 @@ hrt_status hrt_batch_destroy(hrt_batch* b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->dscenes) cudaFree(b->dscenes);
     if (b->counters) cudaFree(b->counters);
+    if (b->resolve_list) cudaFree(b->resolve_list);
     delete b;
     return HRT_OK;
 }

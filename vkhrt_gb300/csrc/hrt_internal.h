@@ -93,6 +93,8 @@ struct TraceCounters {
     unsigned long long cycles_node, cycles_leaf, cycles_other;  // per-warp clock, with count_stats
     uint32_t error;
     uint32_t pad;
+    unsigned long long resolve_n;  // pixels listed by the first pass for the FP64 pass
+    unsigned long long work2;      // next list entry of the FP64 pass
 };
 
 struct TraceLaunch {
@@ -106,6 +108,11 @@ struct TraceLaunch {
     uint32_t refill;     // idle lanes of a warp that trigger a work fetch (0 = 16)
     uint32_t speculative;  // lanes holding a leaf keep traversing while others search
     TraceCounters* counters;
+    // Two-pass FP64 re-solve: the first pass lists the work items (pixels) that met a Phantom
+    // candidate whose FP32 solve did not converge; the second re-renders just those with the
+    // FP64 re-solve inline. resolve_cap >= the number of pixels, so the list cannot overflow.
+    uint32_t* resolve_list;
+    uint64_t resolve_cap;
 };
 
 // ---- launch wrappers (trace.cu) --------------------------------------------------------------

@@ -335,7 +335,7 @@ struct RayState {
     TriRay tr;
 };
 
-struct Stats { uint32_t nodes, prims, r64, h64; };
+struct Stats { uint32_t nodes, prims, r64, h64, need64; };
 
 // ---------------------------------------------------------------- leaves
 __device__ __forceinline__ void load_phantom(const DevBlas& B, uint32_t slot, V3<float>* P, float* r0, float* r1,
@@ -375,8 +375,10 @@ __device__ __forceinline__ void load_phantom(const DevBlas& B, uint32_t slot, V3
 
 // Tests one leaf slot; returns true if it produced an accepted hit. kType is the primitive
 // type when every instance of the launch has the same one, kMixed to branch on the BLAS.
+// kFlag64: a non-converged Phantom candidate only sets st.need64 (the FP64 re-solve runs in a
+// later pass); otherwise it is re-solved here.
 constexpr int kMixed = 3;
-template <int kType = kMixed>
+template <int kType = kMixed, bool kFlag64 = false>
 __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint32_t inst, const RayState& R, Hit& h,
                                           bool fp64_resolve, Stats& st) {
     const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
@@ -391,7 +393,9 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
                 h = Hit{r.s, id, inst, slot, r.tc, r.ts, r.sl, 0u};
                 return true;
             }
-        } else if (r.status == kUnresolved && fp64_resolve) {
+        } else if (kFlag64 && r.status == kUnresolved && fp64_resolve) {
+            st.need64 = 1u;
+        } else if (!kFlag64 && r.status == kUnresolved && fp64_resolve) {
             float cp[12];
 #pragma unroll
             for (int k = 0; k < 4; ++k) { cp[3 * k] = P[k].x; cp[3 * k + 1] = P[k].y; cp[3 * k + 2] = P[k].z; }
@@ -804,19 +808,20 @@ __device__ __forceinline__ void warp_add(unsigned long long* ctr, uint32_t v) {
 constexpr int kShort = 16;
 constexpr int kRefill = 16;
 
-template <bool kQuant, int kType, int kMinBlocks>
+// kPass 1: the frame (non-converged Phantom candidates flag their pixel); kPass 2: the listed
+// pixels again, with the FP64 re-solve inline (adds only the FP64 counts).
+template <bool kQuant, int kType, int kMinBlocks, int kPass>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch L) {
     __shared__ uint2 s_stack[kShort][kThreads];
-    __shared__ float s_leaf_t[8][kThreads];  // entry distances of the pending leaf children, by slot
     uint2 l_stack[kStackSize - kShort];
     const int tid = threadIdx.x, lane = tid & 31;
     const uint32_t lt_mask = (1u << lane) - 1u;
     const volatile uint32_t* errword = &L.counters->error;
-    Stats st{0, 0, 0, 0};
+    Stats st{0, 0, 0, 0, 0};
     uint32_t shadow_rays = 0, err = 0;
 
     bool has_ray = false, fetch_done = false;
-    uint32_t si = 0, px = 0, py = 0, sample = 0;
+    uint32_t si = 0, px = 0, py = 0, sample = 0, g_cur = 0;
     uint64_t pix = 0;
     bool shadow = false, shadow_hit = false;
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, ndl = 0.0f;
@@ -832,7 +837,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     uint32_t oct = 0;                            // direction octant of the object-space ray
     uint32_t cur_base = 0, cur_bits = 0;         // node group: hits in visiting order (bits 0-7), imask (8-15)
     uint32_t leaf_node = 0, leaf_bits = 0;       // untested leaf children of node leaf_node, visiting order
-    bool leaf_t = false;                         // s_leaf_t holds their entry distances
 
     auto push = [&](uint2 e) {
         if (sp < kShort) s_stack[sp][tid] = e;
@@ -905,6 +909,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         float inv = 1.0f / float(S.spp);
         S.fb[pix] = make_float4(__fmul_rn(acc0, inv), __fmul_rn(acc1, inv), __fmul_rn(acc2, inv), 1.0f);
         has_ray = false;
+        if (kPass == 1 && st.need64) {  // list the pixel for the FP64 pass
+            st.need64 = 0;
+            unsigned long long k = atomicAdd(&L.counters->resolve_n, 1ull);
+            if (k < L.resolve_cap) L.resolve_list[k] = g_cur;
+        }
     };
     auto finish_phase = [&]() {
         const SceneLaunch& S = L.scenes[si];
@@ -958,6 +967,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
 
     const int refill = L.refill ? int(L.refill) : kRefill;  // idle lanes that trigger a fetch
     const bool spec = L.speculative != 0;
+    // work items: pass 1 every item; pass 2 the listed ones (all of them if the list overflowed)
+    unsigned long long* const work_ctr = kPass == 1 ? &L.counters->work : &L.counters->work2;
+    uint64_t total = L.total_work;
+    bool use_list = false;
+    if (kPass == 2) {
+        const unsigned long long nl = __ldcg(&L.counters->resolve_n);
+        if (nl <= L.resolve_cap) { total = nl; use_list = true; }
+    }
     unsigned long long cyc_node = 0, cyc_leaf = 0, cyc_other = 0;
     long long clk = clock64();
     for (;;) {
@@ -966,12 +983,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         if (idle && !fetch_done && (__popc(idle) >= refill || idle == kFull)) {
             int n = __popc(idle), leader = __ffs(idle) - 1;
             unsigned long long base = 0;
-            if (lane == leader) base = *errword ? L.total_work : atomicAdd(&L.counters->work, (unsigned long long)n);
+            if (lane == leader) base = *errword ? total : atomicAdd(work_ctr, (unsigned long long)n);
             base = __shfl_sync(kFull, base, leader);
-            if (base + uint64_t(n) >= L.total_work) fetch_done = true;
+            if (base + uint64_t(n) >= total) fetch_done = true;
             if (!has_ray) {
                 uint64_t g = base + __popc(idle & lt_mask);
-                if (g < L.total_work) {
+                if (g < total) {
+                    if (use_list) g = __ldcg(&L.resolve_list[g]);
+                    g_cur = uint32_t(g);
                     si = 0;
                     while (si + 1 < L.nscenes && L.scenes[si + 1].work_begin <= g) ++si;
                     const SceneLaunch& S = L.scenes[si];
@@ -1022,7 +1041,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                     } else {
                         leaf_node = e.x & ~kLeafFlag;
                         leaf_bits = oct_permute(e.y, oct);
-                        leaf_t = false;
                     }
                     continue;
                 }
@@ -1035,8 +1053,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             const uint32_t child = cur_base + __popc((cur_bits >> 8) & ((1u << slot) - 1u));
             ++st.nodes;
             uint32_t base, imask;
-            float tn[8];
-            const uint32_t mask = test_node<kQuant, false>(nodes, child, R, h.t, tn, &base, nullptr, nullptr,
+            const uint32_t mask = test_node<kQuant, false>(nodes, child, R, h.t, nullptr, &base, nullptr, nullptr,
                                                            nullptr, &imask);
             const uint32_t ih = mask & imask, lh = mask & ~imask;
             if (sp + 2 > kStackSize) {
@@ -1049,9 +1066,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 if (!leaf_bits) {
                     leaf_node = child;
                     leaf_bits = oct_permute(lh, oct);
-                    leaf_t = true;
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) s_leaf_t[q][tid] = tn[q];
                 } else {
                     push(make_uint2(kLeafFlag | child, lh));
                     stalled = true;
@@ -1064,21 +1078,19 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             }
         }
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_node += c - clk; clk = c; }
-        // ---- leaf phase: one leaf child per lane, nearest first; one whose box starts beyond
-        // the closest hit so far is skipped
+        // ---- leaf phase: one leaf child per lane, in visiting order
         if (leaf_bits) {
             const DevBlas& B = L.scenes[si].inst[inst_cur].b;
             const uint32_t q = (__ffs(leaf_bits) - 1) ^ oct;
             leaf_bits &= leaf_bits - 1u;
-            const bool beyond = leaf_t && s_leaf_t[q][tid] > h.t;
-            const uint4 hd = beyond ? make_uint4(0u, 0u, 0u, 0u) : node_header<kQuant>(nodes, leaf_node);
+            const uint4 hd = node_header<kQuant>(nodes, leaf_node);
             const uint32_t m = ((q < 4 ? hd.z : hd.w) >> (8 * (q & 3))) & 0xffu;
             const uint32_t first = hd.y + (m & 31u), cnt = m >> 5;
             for (uint32_t j = 0; j < cnt; ++j) {
                 uint32_t slot = first + j;
                 if (shadow && inst_cur == skip_inst && slot == skip_slot) continue;
                 ++st.prims;
-                if (leaf_test<kType>(B, slot, inst_cur, R, h, L.fp64_resolve != 0, st) && shadow) {
+                if (leaf_test<kType, kPass == 1>(B, slot, inst_cur, R, h, L.fp64_resolve != 0, st) && shadow) {
                     shadow_hit = true;
                     sp = 0;
                     cur_bits = leaf_bits = 0;
@@ -1104,8 +1116,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             if (!more) finish_phase();
         }
     }
-    warp_add(&L.counters->shadow, shadow_rays);
-    if (L.count_stats) {
+    if (kPass == 1) warp_add(&L.counters->shadow, shadow_rays);
+    if (kPass == 1 && L.count_stats) {
         warp_add(&L.counters->nodes, st.nodes);
         warp_add(&L.counters->prims, st.prims);
         cyc_other += clock64() - clk;
@@ -1124,7 +1136,7 @@ template <bool kQuant>
 __global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance* inst, uint32_t ninst, const float* rays,
                                                               uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
                                                               hrt_hit* hits, TraceCounters* ctr) {
-    Stats st{0, 0, 0, 0};
+    Stats st{0, 0, 0, 0, 0};
     uint32_t err = 0;
     for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
         const float* r = rays + 6 * i;
@@ -1143,37 +1155,50 @@ __global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance*
     if (err) atomicOr(&ctr->error, err);
 }
 
-template <bool kQuant, int kType, int kMinBlocks>
+template <bool kQuant, int kType, int kMinBlocks, int kPass>
 cudaError_t launch_frame(const TraceLaunch& L, cudaStream_t s, int sm_count) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_kernel<kQuant, kType, kMinBlocks>,
-                                                                  kThreads, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, frame_kernel<kQuant, kType, kMinBlocks, kPass>, kThreads, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     unsigned grid = unsigned(sm_count * per_sm);
     uint64_t max_blocks = (L.total_work + kThreads - 1) / kThreads;
     if (grid > max_blocks) grid = unsigned(max_blocks ? max_blocks : 1);
-    frame_kernel<kQuant, kType, kMinBlocks><<<grid, kThreads, 0, s>>>(L);
+    frame_kernel<kQuant, kType, kMinBlocks, kPass><<<grid, kThreads, 0, s>>>(L);
     return cudaGetLastError();
 }
 
 template <bool kQuant, int kMinBlocks>
 cudaError_t launch_kind(const TraceLaunch& L, cudaStream_t s, int sm_count) {
     switch (L.prim_kind) {  // one primitive type in every instance -> the specialised kernel
-        case HRT_BLAS_PHANTOM: return launch_frame<kQuant, HRT_BLAS_PHANTOM, kMinBlocks>(L, s, sm_count);
-        case HRT_BLAS_LSS: return launch_frame<kQuant, HRT_BLAS_LSS, kMinBlocks>(L, s, sm_count);
-        case HRT_BLAS_DOTS: return launch_frame<kQuant, HRT_BLAS_DOTS, kMinBlocks>(L, s, sm_count);
-        default: return launch_frame<kQuant, kMixed, kMinBlocks>(L, s, sm_count);
+        case HRT_BLAS_PHANTOM: return launch_frame<kQuant, HRT_BLAS_PHANTOM, kMinBlocks, 1>(L, s, sm_count);
+        case HRT_BLAS_LSS: return launch_frame<kQuant, HRT_BLAS_LSS, kMinBlocks, 1>(L, s, sm_count);
+        case HRT_BLAS_DOTS: return launch_frame<kQuant, HRT_BLAS_DOTS, kMinBlocks, 1>(L, s, sm_count);
+        default: return launch_frame<kQuant, kMixed, kMinBlocks, 1>(L, s, sm_count);
     }
+}
+
+// The FP64 pass: only launches that hold Phantom BLASes can list pixels.
+template <bool kQuant>
+cudaError_t launch_resolve(const TraceLaunch& L, cudaStream_t s, int sm_count) {
+    if (!L.fp64_resolve || !L.resolve_list) return cudaSuccess;
+    if (L.prim_kind == HRT_BLAS_PHANTOM) return launch_frame<kQuant, HRT_BLAS_PHANTOM, 1, 2>(L, s, sm_count);
+    if (L.prim_kind == kMixed) return launch_frame<kQuant, kMixed, 1, 2>(L, s, sm_count);
+    return cudaSuccess;
 }
 
 }  // namespace
 
 // variant: 0 default (4 resident blocks per SM), 1 = 4, 2 = 3 (more registers per thread).
+// Launches the frame pass and, when Phantom candidates may need it, the FP64 pass.
 cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count) {
     bool three = L.variant == 2;
-    if (quantised_nodes) return three ? launch_kind<true, 3>(L, s, sm_count) : launch_kind<true, 4>(L, s, sm_count);
-    return three ? launch_kind<false, 3>(L, s, sm_count) : launch_kind<false, 4>(L, s, sm_count);
+    cudaError_t e;
+    if (quantised_nodes) e = three ? launch_kind<true, 3>(L, s, sm_count) : launch_kind<true, 4>(L, s, sm_count);
+    else e = three ? launch_kind<false, 3>(L, s, sm_count) : launch_kind<false, 4>(L, s, sm_count);
+    if (e != cudaSuccess) return e;
+    return quantised_nodes ? launch_resolve<true>(L, s, sm_count) : launch_resolve<false>(L, s, sm_count);
 }
 
 cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n, float tmin,
