@@ -168,11 +168,14 @@ def test_batch_equals_single_launches(ctx, orc):
     for (rgba, hits), (_, _, _, fr, *_r) in zip(batch_out, scenes):
         rgba2, hits2 = fr.download(hits=True)
         assert np.array_equal(rgba, rgba2) and np.array_equal(hits, hits2)
+    # a mixed-type batch runs the kernel compiled for every primitive type; single launches run
+    # the per-type kernels: identical hits, pixels within 1e-6 (last-bit rounding of the
+    # separately compiled FP32 Phantom solve moves shaded normals by a few ulps)
     for (rgba, hits), (b, t, cam, _, w, h, spp) in zip(batch_out, scenes):
         fr = H.Frame(ctx, w, h, spp, with_hits=True)
         H.trace(ctx, t, cam, fr, p)
         rgba1, hits1 = fr.download(hits=True)
-        assert np.array_equal(rgba, rgba1) and np.array_equal(hits, hits1)
+        assert np.array_equal(hits, hits1) and np.abs(rgba - rgba1).max() <= 1e-6
 
 
 def test_empty_scene_and_misses(ctx):
