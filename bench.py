@@ -656,8 +656,8 @@ def main():
                     help="override the workload's BVH/primitive precision (profiling)")
     ap.add_argument("--variant", type=int, default=0, help="trace kernel variant (0 default, 1, 2)")
     ap.add_argument("--max-leaf", type=int, default=1, help="primitives per BVH8 leaf (1..3)")
-    ap.add_argument("--refill", type=int, default=0, help="idle lanes per warp that trigger a fetch (0 = 16)")
-    ap.add_argument("--speculative", type=int, default=0, help="speculative traversal (0/1)")
+    ap.add_argument("--refill", type=int, default=8, help="idle lanes per warp that trigger a fetch (0 = 16)")
+    ap.add_argument("--speculative", type=int, default=1, help="speculative traversal (0/1)")
     ap.add_argument("--profile", action="store_true",
                     help="one warm-up and the timed steps only: no e2e, FP32 comparison or CPU legs")
     args = ap.parse_args()

@@ -149,8 +149,8 @@ typedef struct hrt_trace_params {
     uint32_t async;        /* 0: synchronise and check the device error word before returning */
     uint32_t count_stats;  /* accumulate traversal counters into the frame stats */
     uint32_t kernel_variant; /* 0 default; 1: 4 resident blocks per SM; 2: 3 blocks with more registers */
-    uint32_t refill;         /* idle lanes of a warp that trigger a work fetch, 1..32 (0 = 16) */
-    uint32_t speculative;    /* lanes that hold a leaf keep traversing while others search (0/1) */
+    uint32_t refill;         /* idle lanes of a warp that trigger a work fetch, 1..32 (0 = 16; default 8) */
+    uint32_t speculative;    /* lanes that hold a leaf keep traversing while others search (0/1; default 1) */
 } hrt_trace_params;
 
 typedef struct hrt_hit {

@@ -604,6 +604,8 @@ void hrt_trace_params_default(hrt_trace_params* p) {
     p->shading = HRT_SHADE_DEBUG;
     p->shadow_tmin = 1e-4f;
     p->fp64_resolve = 1;
+    p->refill = 8;
+    p->speculative = 1;
 }
 
 hrt_status hrt_frame_create(hrt_context* ctx, uint32_t w, uint32_t h, uint32_t spp, int32_t with_hits, hrt_frame** out) {
