@@ -47,6 +47,8 @@ struct hrt_frame {
     SceneLaunch* dscene = nullptr;
     TraceCounters* counters = nullptr;
     uint32_t* resolve_list = nullptr;  // one entry per pixel (FP64 pass)
+    float4* resolve_scratch = nullptr; // per-sample colours of the FP64 pass
+    uint64_t scratch_cap = 0;
     hrt_frame_stats stats{};
     bool stats_pending = false;
     uint64_t pending_primary = 0;
@@ -57,6 +59,7 @@ struct hrt_batch {
     SceneLaunch* dscenes = nullptr;
     TraceCounters* counters = nullptr;
     uint32_t* resolve_list = nullptr;
+    float4* resolve_scratch = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<hrt_frame*> frames;
@@ -184,8 +187,12 @@ uint32_t prim_kind(uint32_t type_mask) {
     return 3;
 }
 
+// Samples the FP64 pass can run one per lane (beyond that it runs one pixel per lane).
+constexpr uint64_t kScratchSamples = 1ull << 18;
+
 TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32_t n, uint64_t total, TraceCounters* c,
-                        uint32_t type_mask, uint32_t* resolve_list, uint64_t resolve_cap) {
+                        uint32_t type_mask, uint32_t* resolve_list, uint64_t resolve_cap, float4* scratch,
+                        uint64_t scratch_cap, uint32_t max_spp) {
     TraceLaunch L;
     L.prim_kind = prim_kind(type_mask);
     L.scenes = ds;
@@ -206,6 +213,9 @@ TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32
     L.counters = c;
     L.resolve_list = resolve_list;
     L.resolve_cap = resolve_cap;
+    L.resolve_scratch = scratch;
+    L.scratch_cap = scratch ? scratch_cap : 0;
+    L.max_spp = max_spp ? max_spp : 1;
     return L;
 }
 
@@ -626,6 +636,8 @@ hrt_status hrt_frame_create(hrt_context* ctx, uint32_t w, uint32_t h, uint32_t s
     if (e == cudaSuccess) e = cudaMalloc(&f->dscene, sizeof(SceneLaunch));
     if (e == cudaSuccess) e = cudaMalloc(&f->counters, sizeof(TraceCounters));
     if (e == cudaSuccess) e = cudaMalloc(&f->resolve_list, uint64_t(w) * h * sizeof(uint32_t));
+    f->scratch_cap = std::min<uint64_t>(uint64_t(w) * h * spp, kScratchSamples);
+    if (e == cudaSuccess) e = cudaMalloc(&f->resolve_scratch, f->scratch_cap * sizeof(float4));
     if (e != cudaSuccess) {
         hrt_frame_destroy(f);
         return cuda_fail(ctx, e, "hrt_frame_create");
@@ -642,6 +654,7 @@ hrt_status hrt_frame_destroy(hrt_frame* f) {
     if (f->dscene) cudaFree(f->dscene);
     if (f->counters) cudaFree(f->counters);
     if (f->resolve_list) cudaFree(f->resolve_list);
+    if (f->resolve_scratch) cudaFree(f->resolve_scratch);
     delete f;
     return HRT_OK;
 }
@@ -697,7 +710,7 @@ hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* c
     CK(ctx, cudaMemcpyAsync(f->dscene, &sl, sizeof(sl), cudaMemcpyHostToDevice, s), "upload scene");
     CK(ctx, cudaMemsetAsync(f->counters, 0, sizeof(TraceCounters), s), "reset counters");
     TraceLaunch L = make_launch(p, f->dscene, 1, sl.work_count, f->counters, tlas->type_mask, f->resolve_list,
-                                uint64_t(f->w) * f->h);
+                                uint64_t(f->w) * f->h, f->resolve_scratch, f->scratch_cap, f->spp);
     CK(ctx, launch_trace(L, tlas->quantised, s, ctx->sm_count), "launch trace");
     f->pending_primary = uint64_t(f->w) * f->h * f->spp;
     f->stats_pending = true;
@@ -800,11 +813,18 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
     b->async = p->async != 0;
     for (uint32_t i = 0; i < n; ++i) b->frames.push_back(scenes[i].frame);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    uint64_t npix = 0;
-    for (uint32_t i = 0; i < n; ++i) npix += uint64_t(scenes[i].frame->w) * scenes[i].frame->h;
+    uint64_t npix = 0, nsamp = 0;
+    uint32_t max_spp = 1;
+    for (uint32_t i = 0; i < n; ++i) {
+        npix += uint64_t(scenes[i].frame->w) * scenes[i].frame->h;
+        nsamp += uint64_t(scenes[i].frame->w) * scenes[i].frame->h * scenes[i].frame->spp;
+        max_spp = std::max(max_spp, scenes[i].frame->spp);
+    }
+    const uint64_t scap = std::min<uint64_t>(nsamp, kScratchSamples);
     cudaError_t e = cudaMalloc(&b->dscenes, n * sizeof(SceneLaunch));
     if (e == cudaSuccess) e = cudaMalloc(&b->counters, sizeof(TraceCounters));
     if (e == cudaSuccess) e = cudaMalloc(&b->resolve_list, npix * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&b->resolve_scratch, scap * sizeof(float4));
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->dscenes, sl.data(), n * sizeof(SceneLaunch), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     // capture: counter reset + the persistent trace launch
@@ -813,7 +833,8 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         cudaError_t e1 = cudaMemsetAsync(b->counters, 0, sizeof(TraceCounters), cap);
-        TraceLaunch L = make_launch(p, b->dscenes, n, work, b->counters, type_mask, b->resolve_list, npix);
+        TraceLaunch L = make_launch(p, b->dscenes, n, work, b->counters, type_mask, b->resolve_list, npix,
+                                    b->resolve_scratch, scap, max_spp);
         cudaError_t e2 = e1 == cudaSuccess ? launch_trace(L, quant, cap, ctx->sm_count) : e1;
         cudaError_t e3 = cudaStreamEndCapture(cap, &b->graph);
         e = e2 != cudaSuccess ? e2 : e3;
@@ -868,19 +889,28 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
     SceneLaunch* ds_ = nullptr;
     TraceCounters* ctr = nullptr;
     uint32_t* rlist = nullptr;
-    uint64_t npix = 0;
-    for (uint32_t i = 0; i < n; ++i) npix += uint64_t(scenes[i].frame->w) * scenes[i].frame->h;
+    float4* rscr = nullptr;
+    uint64_t npix = 0, nsamp = 0;
+    uint32_t max_spp = 1;
+    for (uint32_t i = 0; i < n; ++i) {
+        npix += uint64_t(scenes[i].frame->w) * scenes[i].frame->h;
+        nsamp += uint64_t(scenes[i].frame->w) * scenes[i].frame->h * scenes[i].frame->spp;
+        max_spp = std::max(max_spp, scenes[i].frame->spp);
+    }
+    const uint64_t scap = std::min<uint64_t>(nsamp, kScratchSamples);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto cleanup = [&]() {
         if (ds_) cudaFree(ds_);
         if (ctr) cudaFree(ctr);
         if (rlist) cudaFree(rlist);
+        if (rscr) cudaFree(rscr);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
     };
     cudaError_t e = cudaMalloc(&ds_, n * sizeof(SceneLaunch));
     if (e == cudaSuccess) e = cudaMalloc(&ctr, sizeof(TraceCounters));
     if (e == cudaSuccess) e = cudaMalloc(&rlist, npix * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&rscr, scap * sizeof(float4));
     if (e == cudaSuccess) e = cudaMemcpyAsync(ds_, sl.data(), n * sizeof(SceneLaunch), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
@@ -900,7 +930,7 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
                 p.speculative = sp;
                 p.record_hits = 0;
                 p.count_stats = 0;
-                TraceLaunch L = make_launch(&p, ds_, n, work, ctr, type_mask, rlist, npix);
+                TraceLaunch L = make_launch(&p, ds_, n, work, ctr, type_mask, rlist, npix, rscr, scap, max_spp);
                 float tot = 0.0f;
                 for (uint32_t k = 0; k <= reps && e == cudaSuccess; ++k) {
                     e = cudaMemsetAsync(ctr, 0, sizeof(TraceCounters), s);
@@ -942,6 +972,7 @@ hrt_status hrt_batch_destroy(hrt_batch* b) {
     if (b->dscenes) cudaFree(b->dscenes);
     if (b->counters) cudaFree(b->counters);
     if (b->resolve_list) cudaFree(b->resolve_list);
+    if (b->resolve_scratch) cudaFree(b->resolve_scratch);
     delete b;
     return HRT_OK;
 }

@@ -113,6 +113,12 @@ struct TraceLaunch {
     // FP64 re-solve inline. resolve_cap >= the number of pixels, so the list cannot overflow.
     uint32_t* resolve_list;
     uint64_t resolve_cap;
+    // The FP64 pass takes one sample per lane when the listed pixels' samples fit the scratch
+    // (per-sample colours, averaged per pixel in sample order by a third launch); otherwise one
+    // pixel per lane.
+    float4* resolve_scratch;
+    uint64_t scratch_cap;  // samples
+    uint32_t max_spp;      // over the scenes of the launch
 };
 
 // ---- launch wrappers (trace.cu) --------------------------------------------------------------

@@ -455,6 +455,19 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
 
 // Reciprocal direction with zero components replaced by +-1e20, so slab distances stay finite
 // (a ray inside a slab gets -huge..+huge, one outside a pair of equal signs).
+// Three-input minimum and maximum (sm_100 and later); like fminf/fmaxf, a NaN input is ignored
+// unless all are NaN.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 __device__ __forceinline__ V3<float> safe_inv(V3<float> d) {
     auto r = [](float x) { return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
     return mk(r(d.x), r(d.y), r(d.z));
@@ -502,12 +515,18 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         const float FY[8] = {f2.x, f2.y, f2.z, f2.w, f3.x, f3.y, f3.z, f3.w};
         const float NZ[8] = {n4.x, n4.y, n4.z, n4.w, n5.x, n5.y, n5.z, n5.w};
         const float FZ[8] = {f4.x, f4.y, f4.z, f4.w, f5.x, f5.y, f5.z, f5.w};
+        // t = plane inv + (-o inv) in one fused operation. -o inv is rounded once (error below
+        // 2^-24 |o inv|), so each axis's near offsets take 2^-22 |o inv| off and its far offsets
+        // add it; the product-sum's own rounding and that of inv are relative to t and covered
+        // by the 2^-20 relative margin of the final test.
+        const float ox = -R.o.x * R.inv.x, oy = -R.o.y * R.inv.y, oz = -R.o.z * R.inv.z;
+        const float kO = 2.384185791015625e-07f;  // 2^-22
+        const float ex = kO * fabsf(ox), ey = kO * fabsf(oy), ez = kO * fabsf(oz);
+        const float oxn = ox - ex, oxf = ox + ex, oyn = oy - ey, oyf = oy + ey, ozn = oz - ez, ozf = oz + ez;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            float a = fmaxf(fmaxf((NX[q] - R.o.x) * R.inv.x, (NY[q] - R.o.y) * R.inv.y),
-                            fmaxf((NZ[q] - R.o.z) * R.inv.z, R.tmin));
-            float b = fminf(fminf((FX[q] - R.o.x) * R.inv.x, (FY[q] - R.o.y) * R.inv.y),
-                            fminf((FZ[q] - R.o.z) * R.inv.z, tfar));
+            float a = max3f(fmaf(NX[q], R.inv.x, oxn), fmaf(NY[q], R.inv.y, oyn), fmaxf(fmaf(NZ[q], R.inv.z, ozn), R.tmin));
+            float b = min3f(fmaf(FX[q], R.inv.x, oxf), fmaf(FY[q], R.inv.y, oyf), fminf(fmaf(FZ[q], R.inv.z, ozf), tfar));
             if (tn) tn[q] = a;
             if (a <= b * kEps) mask |= 1u << q;
         }
@@ -554,9 +573,9 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
             const uint32_t wnx = q < 4 ? nxw0 : nxw1, wfx = q < 4 ? fxw0 : fxw1;
             const uint32_t wny = q < 4 ? nyw0 : nyw1, wfy = q < 4 ? fyw0 : fyw1;
             const uint32_t wnz = q < 4 ? nzw0 : nzw1, wfz = q < 4 ? fzw0 : fzw1;
-            float a = fmaxf(fmaxf(fmaf(biased_byte(wnx, by_), sx, bxn), fmaf(biased_byte(wny, by_), sy, byn)),
+            float a = max3f(fmaf(biased_byte(wnx, by_), sx, bxn), fmaf(biased_byte(wny, by_), sy, byn),
                             fmaxf(fmaf(biased_byte(wnz, by_), sz, bzn), R.tmin));
-            float b = fminf(fminf(fmaf(biased_byte(wfx, by_), sx, bxf), fmaf(biased_byte(wfy, by_), sy, byf)),
+            float b = min3f(fmaf(biased_byte(wfx, by_), sx, bxf), fmaf(biased_byte(wfy, by_), sy, byf),
                             fminf(fmaf(biased_byte(wfz, by_), sz, bzf), tfar));
             if (tn) tn[q] = a;
             if (a <= b) mask |= 1u << q;
@@ -820,8 +839,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     Stats st{0, 0, 0, 0, 0};
     uint32_t shadow_rays = 0, err = 0;
 
-    bool has_ray = false, fetch_done = false;
+    bool has_ray = false, fetch_done = false, per_sample = false;
     uint32_t si = 0, px = 0, py = 0, sample = 0, g_cur = 0;
+    uint64_t item = 0;  // FP64 pass, one sample per lane: the scratch index of the sample
     uint64_t pix = 0;
     bool shadow = false, shadow_hit = false;
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, ndl = 0.0f;
@@ -905,6 +925,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     auto next_sample = [&]() {
         const SceneLaunch& S = L.scenes[si];
         ++sample;
+        if (kPass == 2 && per_sample) {  // this sample's colour; a later launch averages
+            L.resolve_scratch[item] = make_float4(acc0, acc1, acc2, 0.0f);
+            has_ray = false;
+            return;
+        }
         if (sample < S.spp) { start_primary(); return; }
         float inv = 1.0f / float(S.spp);
         S.fb[pix] = make_float4(__fmul_rn(acc0, inv), __fmul_rn(acc1, inv), __fmul_rn(acc2, inv), 1.0f);
@@ -967,13 +992,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
 
     const int refill = L.refill ? int(L.refill) : kRefill;  // idle lanes that trigger a fetch
     const bool spec = L.speculative != 0;
-    // work items: pass 1 every item; pass 2 the listed ones (all of them if the list overflowed)
+    // work items: pass 1 every item; pass 2 the samples of the listed pixels, or the listed
+    // pixels when their samples do not fit the scratch, or every item if the list overflowed
     unsigned long long* const work_ctr = kPass == 1 ? &L.counters->work : &L.counters->work2;
     uint64_t total = L.total_work;
     bool use_list = false;
     if (kPass == 2) {
         const unsigned long long nl = __ldcg(&L.counters->resolve_n);
         if (nl <= L.resolve_cap) { total = nl; use_list = true; }
+        if (use_list && nl * L.max_spp <= L.scratch_cap) { total = nl * L.max_spp; per_sample = true; }
     }
     unsigned long long cyc_node = 0, cyc_leaf = 0, cyc_other = 0;
     long long clk = clock64();
@@ -989,6 +1016,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             if (!has_ray) {
                 uint64_t g = base + __popc(idle & lt_mask);
                 if (g < total) {
+                    uint32_t s0 = 0;
+                    if (per_sample) {
+                        item = g;
+                        s0 = uint32_t(g % L.max_spp);
+                        g = g / L.max_spp;
+                    }
                     if (use_list) g = __ldcg(&L.resolve_list[g]);
                     g_cur = uint32_t(g);
                     si = 0;
@@ -998,10 +1031,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                     uint32_t within = uint32_t(local & 31u);
                     px = uint32_t(tile % S.tiles_x) * 8u + (within & 7u);
                     py = uint32_t(tile / S.tiles_x) * 4u + (within >> 3);
-                    if (px < S.width && py < S.height) {
+                    if (px < S.width && py < S.height && s0 < S.spp) {
                         pix = uint64_t(py) * S.width + px;
                         has_ray = true;
-                        sample = 0;
+                        sample = s0;
                         acc0 = acc1 = acc2 = 0.0f;
                         start_primary();
                     }
@@ -1179,13 +1212,43 @@ cudaError_t launch_kind(const TraceLaunch& L, cudaStream_t s, int sm_count) {
     }
 }
 
+// After a per-sample FP64 pass: each listed pixel's colour is the mean of its samples' colours,
+// summed in sample order from zero (the frame pass's own accumulation, bit for bit).
+__global__ void __launch_bounds__(kThreads) resolve_average_kernel(TraceLaunch L) {
+    const unsigned long long nl = __ldcg(&L.counters->resolve_n);
+    if (nl > L.resolve_cap || nl * L.max_spp > L.scratch_cap) return;  // the pass ran per pixel
+    for (uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < nl; k += uint64_t(gridDim.x) * blockDim.x) {
+        const uint32_t g = __ldcg(&L.resolve_list[k]);
+        uint32_t si = 0;
+        while (si + 1 < L.nscenes && L.scenes[si + 1].work_begin <= g) ++si;
+        const SceneLaunch& S = L.scenes[si];
+        const uint64_t local = g - S.work_begin, tile = local >> 5;
+        const uint32_t within = uint32_t(local & 31u);
+        const uint32_t px = uint32_t(tile % S.tiles_x) * 8u + (within & 7u);
+        const uint32_t py = uint32_t(tile / S.tiles_x) * 4u + (within >> 3);
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+        for (uint32_t s2 = 0; s2 < S.spp; ++s2) {
+            const float4 c = __ldcg(&L.resolve_scratch[k * L.max_spp + s2]);
+            a0 = __fadd_rn(a0, c.x);
+            a1 = __fadd_rn(a1, c.y);
+            a2 = __fadd_rn(a2, c.z);
+        }
+        const float inv = 1.0f / float(S.spp);
+        S.fb[uint64_t(py) * S.width + px] = make_float4(__fmul_rn(a0, inv), __fmul_rn(a1, inv), __fmul_rn(a2, inv), 1.0f);
+    }
+}
+
 // The FP64 pass: only launches that hold Phantom BLASes can list pixels.
 template <bool kQuant>
 cudaError_t launch_resolve(const TraceLaunch& L, cudaStream_t s, int sm_count) {
     if (!L.fp64_resolve || !L.resolve_list) return cudaSuccess;
-    if (L.prim_kind == HRT_BLAS_PHANTOM) return launch_frame<kQuant, HRT_BLAS_PHANTOM, 1, 2>(L, s, sm_count);
-    if (L.prim_kind == kMixed) return launch_frame<kQuant, kMixed, 1, 2>(L, s, sm_count);
-    return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    if (L.prim_kind == HRT_BLAS_PHANTOM) e = launch_frame<kQuant, HRT_BLAS_PHANTOM, 1, 2>(L, s, sm_count);
+    else if (L.prim_kind == kMixed) e = launch_frame<kQuant, kMixed, 1, 2>(L, s, sm_count);
+    else return cudaSuccess;
+    if (e != cudaSuccess || !L.resolve_scratch) return e;
+    resolve_average_kernel<<<unsigned(sm_count), kThreads, 0, s>>>(L);
+    return cudaGetLastError();
 }
 
 }  // namespace
