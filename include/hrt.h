@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HRT_ABI_VERSION 1
+#define HRT_ABI_VERSION 2
 
 typedef enum hrt_status {
     HRT_OK = 0,
@@ -151,6 +151,7 @@ typedef struct hrt_trace_params {
     uint32_t kernel_variant; /* 0 default; 1: 4 resident blocks per SM; 2: 3 blocks with more registers */
     uint32_t refill;         /* idle lanes of a warp that trigger a work fetch, 1..32 (0 = 16; default 8) */
     uint32_t speculative;    /* lanes that hold a leaf keep traversing while others search (0/1; default 1) */
+    uint32_t split_types;    /* batches: one persistent launch per primitive type instead of one for all (0/1) */
 } hrt_trace_params;
 
 typedef struct hrt_hit {
@@ -257,9 +258,10 @@ hrt_status hrt_batch_destroy(hrt_batch* b);
 
 /* ---- autotuner ------------------------------------------------------------------------------
  * Times every candidate kernel configuration on the given scenes (occupancy variant x refill
- * threshold x speculative traversal: HRT_AUTOTUNE_CANDIDATES in all), each `reps` times with
- * plain launches after one warm-up, and writes the fastest into `best` (a copy of `base` with
- * kernel_variant, refill and speculative replaced) and its mean frame time into `best_ms`. */
+ * threshold x speculative traversal, and for scenes of mixed primitive types x one launch or one
+ * per type: HRT_AUTOTUNE_CANDIDATES or twice that), each `reps` times with plain launches after
+ * one warm-up, and writes the fastest into `best` (a copy of `base` with kernel_variant, refill,
+ * speculative and split_types replaced) and its mean frame time into `best_ms`. */
 #define HRT_AUTOTUNE_CANDIDATES 12u
 hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* base,
                         uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms);

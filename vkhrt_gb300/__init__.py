@@ -46,7 +46,7 @@ class TraceParamsC(ctypes.Structure):
     _fields_ = [("tmin", c_f), ("tmax", c_f), ("spp", c_u32), ("jitter", c_u32), ("seed", c_u32),
                 ("shading", c_u32), ("shadow_tmin", c_f), ("fp64_resolve", c_u32), ("record_hits", c_u32),
                 ("async_", c_u32), ("count_stats", c_u32), ("kernel_variant", c_u32), ("refill", c_u32),
-                ("speculative", c_u32)]
+                ("speculative", c_u32), ("split_types", c_u32)]
 
 
 class FrameStatsC(ctypes.Structure):
@@ -406,7 +406,7 @@ def trace_rays_noalloc(ctx: Context, tlas: TopLevelAccelerationStructure, rays: 
     return hits
 
 
-TUNED_FIELDS = ("kernel_variant", "refill", "speculative")
+TUNED_FIELDS = ("kernel_variant", "refill", "speculative", "split_types")
 
 
 def autotune(ctx: Context, scenes: list[tuple[TopLevelAccelerationStructure, CameraC, Frame]],

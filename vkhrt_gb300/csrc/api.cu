@@ -54,16 +54,42 @@ struct hrt_frame {
     uint64_t pending_primary = 0;
 };
 
+// Scenes of one launch sequence, ordered by group (one group per primitive type when split),
+// with the device resources the launches share: the scene table, one counter block per
+// group, and the FP64 pass's pixel list and sample scratch (reused group after group, since
+// the groups run in stream order).
+struct ScenePlan {
+    struct Group {
+        uint32_t first = 0, count = 0, type_mask = 0;
+        uint64_t work = 0;
+    };
+    std::vector<SceneLaunch> table;
+    std::vector<Group> groups;
+    uint64_t primary = 0, npix = 0, nsamp = 0, scap = 0;
+    uint32_t max_spp = 1;
+    bool quant = false;
+    SceneLaunch* dtable = nullptr;
+    TraceCounters* counters = nullptr;
+    uint32_t* list = nullptr;
+    float4* scratch = nullptr;
+    void release() {
+        if (dtable) cudaFree(dtable);
+        if (counters) cudaFree(counters);
+        if (list) cudaFree(list);
+        if (scratch) cudaFree(scratch);
+        dtable = nullptr;
+        counters = nullptr;
+        list = nullptr;
+        scratch = nullptr;
+    }
+};
+
 struct hrt_batch {
     hrt_context* ctx = nullptr;
-    SceneLaunch* dscenes = nullptr;
-    TraceCounters* counters = nullptr;
-    uint32_t* resolve_list = nullptr;
-    float4* resolve_scratch = nullptr;
+    ScenePlan plan;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<hrt_frame*> frames;
-    uint64_t primary = 0;
     bool async = false;
 };
 
@@ -217,6 +243,94 @@ TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32
     L.scratch_cap = scratch ? scratch_cap : 0;
     L.max_spp = max_spp ? max_spp : 1;
     return L;
+}
+
+// Validates the scenes and builds the plan (host table and device resources). split: one
+// group (one persistent launch) per primitive type, scenes whose TLAS mixes types in a group
+// of their own; otherwise one group.
+hrt_status make_plan(hrt_context* ctx, const char* who, const hrt_scene_desc* scenes, uint32_t n, bool split,
+                     bool need_hits, cudaStream_t s, ScenePlan& P) {
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!scenes[i].tlas || !scenes[i].frame) return fail(ctx, HRT_ERR_INVALID_ARG, "%s: scene %u incomplete", who, i);
+        if (scenes[i].tlas->quantised != scenes[0].tlas->quantised)
+            return fail(ctx, HRT_ERR_UNSUPPORTED, "%s: scenes mix FP32 and quantised BLASes", who);
+        if (need_hits && !scenes[i].frame->hits)
+            return fail(ctx, HRT_ERR_INVALID_ARG, "%s: record_hits on a frame without hit records", who);
+    }
+    P.quant = scenes[0].tlas->quantised;
+    auto key = [&](uint32_t i) -> uint32_t { return split ? prim_kind(scenes[i].tlas->type_mask) : 0u; };
+    for (uint32_t k = 0; k < 4; ++k) {
+        ScenePlan::Group G;
+        G.first = uint32_t(P.table.size());
+        for (uint32_t i = 0; i < n; ++i) {
+            if (key(i) != k) continue;
+            SceneLaunch sl;
+            fill_scene(sl, scenes[i].tlas, &scenes[i].camera, scenes[i].frame, G.work);
+            G.work += sl.work_count;
+            G.type_mask |= scenes[i].tlas->type_mask;
+            P.table.push_back(sl);
+            const hrt_frame* f = scenes[i].frame;
+            P.primary += uint64_t(f->w) * f->h * f->spp;
+            P.npix += uint64_t(f->w) * f->h;
+            P.nsamp += uint64_t(f->w) * f->h * f->spp;
+            P.max_spp = std::max(P.max_spp, f->spp);
+        }
+        G.count = uint32_t(P.table.size()) - G.first;
+        if (G.count == 0) continue;
+        if (G.work >= (1ull << 32)) return fail(ctx, HRT_ERR_UNSUPPORTED, "%s: more than 2^32 pixel work items", who);
+        P.groups.push_back(G);
+    }
+    P.scap = std::min<uint64_t>(P.nsamp, kScratchSamples);
+    cudaError_t e = cudaMalloc(&P.dtable, P.table.size() * sizeof(SceneLaunch));
+    if (e == cudaSuccess) e = cudaMalloc(&P.counters, P.groups.size() * sizeof(TraceCounters));
+    if (e == cudaSuccess) e = cudaMalloc(&P.list, P.npix * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&P.scratch, P.scap * sizeof(float4));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(P.dtable, P.table.data(), P.table.size() * sizeof(SceneLaunch), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        P.release();
+        return cuda_fail(ctx, e, who);
+    }
+    return HRT_OK;
+}
+
+// Enqueues the plan's launches: per group, counter reset, frame pass, FP64 pass.
+cudaError_t enqueue_plan(const ScenePlan& P, const hrt_trace_params* p, cudaStream_t s, int sm_count) {
+    for (size_t g = 0; g < P.groups.size(); ++g) {
+        const ScenePlan::Group& G = P.groups[g];
+        cudaError_t e = cudaMemsetAsync(P.counters + g, 0, sizeof(TraceCounters), s);
+        if (e != cudaSuccess) return e;
+        TraceLaunch L = make_launch(p, P.dtable + G.first, G.count, G.work, P.counters + g, G.type_mask, P.list,
+                                    P.npix, P.scratch, P.scap, P.max_spp);
+        e = launch_trace(L, P.quant, s, sm_count);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// Sum of the groups' counters (error bits or-ed), with the device error checks.
+hrt_status read_plan_counters(hrt_context* ctx, const ScenePlan& P, TraceCounters* sum, cudaStream_t s) {
+    std::vector<TraceCounters> c(P.groups.size());
+    CK(ctx, cudaMemcpyAsync(c.data(), P.counters, c.size() * sizeof(TraceCounters), cudaMemcpyDeviceToHost, s),
+       "read counters");
+    CK(ctx, cudaStreamSynchronize(s), "synchronise trace");
+    memset(sum, 0, sizeof(*sum));
+    for (const TraceCounters& x : c) {
+        sum->shadow += x.shadow;
+        sum->nodes += x.nodes;
+        sum->prims += x.prims;
+        sum->fp64_resolves += x.fp64_resolves;
+        sum->fp64_hits += x.fp64_hits;
+        sum->cycles_node += x.cycles_node;
+        sum->cycles_leaf += x.cycles_leaf;
+        sum->cycles_other += x.cycles_other;
+        sum->error |= x.error;
+    }
+    if (sum->error & kErrStackOverflow)
+        return fail(ctx, HRT_ERR_STACK_OVERFLOW, "traversal stack of %d entries overflowed", kStackSize);
+    if (sum->error & kErrTimeout) return fail(ctx, HRT_ERR_TIMEOUT, "a traversal exceeded %u steps", kMaxTraversalSteps);
+    return HRT_OK;
 }
 
 }  // namespace
@@ -789,53 +903,23 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
     if (!scenes || !n || !p || !out) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_create: null or empty argument");
     *out = nullptr;
     DeviceSet ds(ctx->device);
-    std::vector<SceneLaunch> sl(n);
-    uint64_t work = 0, primary = 0;
-    bool quant = false;
-    uint32_t type_mask = 0;
-    for (uint32_t i = 0; i < n; ++i) {
-        if (!scenes[i].tlas || !scenes[i].frame) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_create: scene %u incomplete", i);
-        type_mask |= scenes[i].tlas->type_mask;
-        if (i == 0) quant = scenes[i].tlas->quantised;
-        else if (scenes[i].tlas->quantised != quant)
-            return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_batch_create: scenes mix FP32 and quantised BLASes");
-        if (p->record_hits && !scenes[i].frame->hits)
-            return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_create: record_hits on a frame without hit records");
-        fill_scene(sl[i], scenes[i].tlas, &scenes[i].camera, scenes[i].frame, work);
-        work += sl[i].work_count;
-        primary += uint64_t(scenes[i].frame->w) * scenes[i].frame->h * scenes[i].frame->spp;
-    }
-    if (work >= (1ull << 32)) return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_batch_create: more than 2^32 pixel work items");
     hrt_batch* b = new (std::nothrow) hrt_batch();
     if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_batch_create: host allocation");
     b->ctx = ctx;
-    b->primary = primary;
     b->async = p->async != 0;
     for (uint32_t i = 0; i < n; ++i) b->frames.push_back(scenes[i].frame);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    uint64_t npix = 0, nsamp = 0;
-    uint32_t max_spp = 1;
-    for (uint32_t i = 0; i < n; ++i) {
-        npix += uint64_t(scenes[i].frame->w) * scenes[i].frame->h;
-        nsamp += uint64_t(scenes[i].frame->w) * scenes[i].frame->h * scenes[i].frame->spp;
-        max_spp = std::max(max_spp, scenes[i].frame->spp);
+    hrt_status st = make_plan(ctx, "hrt_batch_create", scenes, n, p->split_types != 0, p->record_hits != 0, s, b->plan);
+    if (st != HRT_OK) {
+        hrt_batch_destroy(b);
+        return st;
     }
-    const uint64_t scap = std::min<uint64_t>(nsamp, kScratchSamples);
-    cudaError_t e = cudaMalloc(&b->dscenes, n * sizeof(SceneLaunch));
-    if (e == cudaSuccess) e = cudaMalloc(&b->counters, sizeof(TraceCounters));
-    if (e == cudaSuccess) e = cudaMalloc(&b->resolve_list, npix * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&b->resolve_scratch, scap * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b->dscenes, sl.data(), n * sizeof(SceneLaunch), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    // capture: counter reset + the persistent trace launch
+    // capture: per group, counter reset + the persistent trace launch (+ the FP64 pass)
     cudaStream_t cap = nullptr;
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaError_t e1 = cudaMemsetAsync(b->counters, 0, sizeof(TraceCounters), cap);
-        TraceLaunch L = make_launch(p, b->dscenes, n, work, b->counters, type_mask, b->resolve_list, npix,
-                                    b->resolve_scratch, scap, max_spp);
-        cudaError_t e2 = e1 == cudaSuccess ? launch_trace(L, quant, cap, ctx->sm_count) : e1;
+        cudaError_t e2 = enqueue_plan(b->plan, p, cap, ctx->sm_count);
         cudaError_t e3 = cudaStreamEndCapture(cap, &b->graph);
         e = e2 != cudaSuccess ? e2 : e3;
     }
@@ -857,11 +941,11 @@ hrt_status hrt_batch_launch(hrt_batch* b, void* stream) {
     CK(ctx, cudaGraphLaunch(b->exec, s), "hrt_batch_launch");
     if (b->async) return HRT_OK;
     TraceCounters c;
-    hrt_status st = read_counters(ctx, b->counters, &c, s);
+    hrt_status st = read_plan_counters(ctx, b->plan, &c, s);
     if (st != HRT_OK) return st;
     // the batch's counters are shared; report them on the first frame
     if (!b->frames.empty()) {
-        counters_to_stats(c, b->primary, &b->frames[0]->stats);
+        counters_to_stats(c, b->plan.primary, &b->frames[0]->stats);
         b->frames[0]->stats_pending = false;
     }
     return HRT_OK;
@@ -874,89 +958,70 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
     if (reps == 0) reps = 3;
     DeviceSet ds(ctx->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    std::vector<SceneLaunch> sl(n);
-    uint64_t work = 0;
-    bool quant = scenes[0].tlas ? scenes[0].tlas->quantised : false;
-    uint32_t type_mask = 0;
-    for (uint32_t i = 0; i < n; ++i) {
-        if (!scenes[i].tlas || !scenes[i].frame) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_autotune: scene %u incomplete", i);
-        if (scenes[i].tlas->quantised != quant)
-            return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_autotune: scenes mix FP32 and quantised BLASes");
-        type_mask |= scenes[i].tlas->type_mask;
-        fill_scene(sl[i], scenes[i].tlas, &scenes[i].camera, scenes[i].frame, work);
-        work += sl[i].work_count;
+    // one plan per grouping (split by type only matters when the scenes mix types)
+    ScenePlan plans[2];
+    hrt_status st = make_plan(ctx, "hrt_autotune", scenes, n, false, false, s, plans[0]);
+    uint32_t nplans = 1;
+    if (st == HRT_OK) {
+        uint32_t kinds = 0;
+        for (uint32_t i = 0; i < n; ++i) kinds |= scenes[i].tlas->type_mask;
+        if (prim_kind(kinds) == 3) {
+            st = make_plan(ctx, "hrt_autotune", scenes, n, true, false, s, plans[1]);
+            nplans = 2;
+        }
     }
-    SceneLaunch* ds_ = nullptr;
-    TraceCounters* ctr = nullptr;
-    uint32_t* rlist = nullptr;
-    float4* rscr = nullptr;
-    uint64_t npix = 0, nsamp = 0;
-    uint32_t max_spp = 1;
-    for (uint32_t i = 0; i < n; ++i) {
-        npix += uint64_t(scenes[i].frame->w) * scenes[i].frame->h;
-        nsamp += uint64_t(scenes[i].frame->w) * scenes[i].frame->h * scenes[i].frame->spp;
-        max_spp = std::max(max_spp, scenes[i].frame->spp);
-    }
-    const uint64_t scap = std::min<uint64_t>(nsamp, kScratchSamples);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto cleanup = [&]() {
-        if (ds_) cudaFree(ds_);
-        if (ctr) cudaFree(ctr);
-        if (rlist) cudaFree(rlist);
-        if (rscr) cudaFree(rscr);
+        plans[0].release();
+        plans[1].release();
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
     };
-    cudaError_t e = cudaMalloc(&ds_, n * sizeof(SceneLaunch));
-    if (e == cudaSuccess) e = cudaMalloc(&ctr, sizeof(TraceCounters));
-    if (e == cudaSuccess) e = cudaMalloc(&rlist, npix * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&rscr, scap * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ds_, sl.data(), n * sizeof(SceneLaunch), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaEventCreate(&e0);
-    if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    if (e != cudaSuccess) {
+    if (st != HRT_OK) {
         cleanup();
-        return cuda_fail(ctx, e, "hrt_autotune");
+        return st;
     }
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
     const uint32_t variants[2] = {1, 2}, refills[3] = {4, 8, 16}, specs[2] = {0, 1};
     float best_t = -1.0f;
     hrt_trace_params bp = *base;
-    for (uint32_t v : variants)
-        for (uint32_t r : refills)
-            for (uint32_t sp : specs) {
-                hrt_trace_params p = *base;
-                p.kernel_variant = v;
-                p.refill = r;
-                p.speculative = sp;
-                p.record_hits = 0;
-                p.count_stats = 0;
-                TraceLaunch L = make_launch(&p, ds_, n, work, ctr, type_mask, rlist, npix, rscr, scap, max_spp);
-                float tot = 0.0f;
-                for (uint32_t k = 0; k <= reps && e == cudaSuccess; ++k) {
-                    e = cudaMemsetAsync(ctr, 0, sizeof(TraceCounters), s);
-                    if (e == cudaSuccess) e = cudaEventRecord(e0, s);
-                    if (e == cudaSuccess) e = launch_trace(L, quant, s, ctx->sm_count);
-                    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
-                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                    float ms = 0.0f;
-                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-                    if (k > 0) tot += ms;  // the first run warms up
+    for (uint32_t split = 0; split < nplans && e == cudaSuccess; ++split)
+        for (uint32_t v : variants)
+            for (uint32_t r : refills)
+                for (uint32_t sp : specs) {
+                    hrt_trace_params p = *base;
+                    p.kernel_variant = v;
+                    p.refill = r;
+                    p.speculative = sp;
+                    p.split_types = split;
+                    p.record_hits = 0;
+                    p.count_stats = 0;
+                    float tot = 0.0f;
+                    for (uint32_t k = 0; k <= reps && e == cudaSuccess; ++k) {
+                        e = cudaEventRecord(e0, s);
+                        if (e == cudaSuccess) e = enqueue_plan(plans[split], &p, s, ctx->sm_count);
+                        if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+                        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                        float ms = 0.0f;
+                        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                        if (k > 0) tot += ms;  // the first run warms up
+                    }
+                    if (e != cudaSuccess) break;
+                    TraceCounters c;
+                    st = read_plan_counters(ctx, plans[split], &c, s);
+                    if (st != HRT_OK) {
+                        cleanup();
+                        return st;
+                    }
+                    float mean = tot / float(reps);
+                    if (best_t < 0.0f || mean < best_t) {
+                        best_t = mean;
+                        bp = p;
+                        bp.record_hits = base->record_hits;
+                        bp.count_stats = base->count_stats;
+                    }
                 }
-                if (e != cudaSuccess) break;
-                TraceCounters c;
-                hrt_status st = read_counters(ctx, ctr, &c, s);
-                if (st != HRT_OK) {
-                    cleanup();
-                    return st;
-                }
-                float mean = tot / float(reps);
-                if (best_t < 0.0f || mean < best_t) {
-                    best_t = mean;
-                    bp = p;
-                    bp.record_hits = base->record_hits;
-                    bp.count_stats = base->count_stats;
-                }
-            }
     cleanup();
     if (e != cudaSuccess) return cuda_fail(ctx, e, "hrt_autotune");
     *best = bp;
@@ -969,10 +1034,7 @@ hrt_status hrt_batch_destroy(hrt_batch* b) {
     DeviceSet ds(b->ctx->device);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->dscenes) cudaFree(b->dscenes);
-    if (b->counters) cudaFree(b->counters);
-    if (b->resolve_list) cudaFree(b->resolve_list);
-    if (b->resolve_scratch) cudaFree(b->resolve_scratch);
+    b->plan.release();
     delete b;
     return HRT_OK;
 }
