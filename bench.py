@@ -1,12 +1,16 @@
 #!/usr/bin/env python3
-"""Mrays/s of the GB300 hair ray tracer on the Phantom precision-pattern workload.
+"""Mrays/s of the GB300 hair ray tracer: quantised and batched against plain FP32.
 
-Workload (default): 150,000 seeded strands x 128 vertices -> 19,050,000 cubic Bezier segments,
-quantised BVH8 (8-bit child boxes) with FP16 control-point offsets from FP32 strand roots,
-1920x1080 at 4 jittered samples per pixel, Shade() plus one shadow ray per hit. A step is one
-frame. `value` counts primary + shadow rays per second with the BVH resident in HBM (the BVH
-and primitives, ~0.8 GB, exceed the 129 MB L2, so no flush is needed between steps); `e2e`
-goes through the C ABI per frame (camera in, framebuffer copied to pinned host memory).
+Default workload (c5_batched): 16 seeded hair models (strands log-uniform in [2,000, 200,000],
+16-128 vertices, Phantom / LSS / DOTS in turn, 47.9 M segments in all), each with its own camera,
+resolution (256x256 .. 1920x1080) and 1-4 jittered samples per pixel, Shade() plus one shadow ray
+per hit. Quantised BLASes (8-bit BVH8 boxes; FP16 control points for Phantom), all scenes in one
+CUDA-graph replay of the persistent trace kernel with autotuned settings. A step is one replay.
+`value` counts primary + shadow rays per second with the BVHs resident in HBM (several GB, far
+above the 129 MB L2, so no flush between steps); `plain_fp32` is the same scenes as 16
+sequential launches of the FP32 tracer; `e2e` goes through the C ABI per step (cameras in,
+every framebuffer copied to pinned host memory). `--config c4_phantom_quantised` is the single
+Phantom precision-pattern frame (19.05 M segments, 1920x1080 x 4 spp) next to its FP32 build.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
 
@@ -548,7 +552,10 @@ def run_batched(args, dist):
     sync_batch = H.Batch(ctx, scenes_q, H.trace_params(jitter=1, seed=17, shading=2,
                                                        **{k: getattr(tuned, k) for k in H.TUNED_FIELDS}))
 
-    def e2e_step():
+    cams = [cam for (_, _, cam, _) in q]
+
+    def e2e_step():  # cameras in (the scene table), one graph launch, every framebuffer out
+        sync_batch.set_cameras(cams)
         sync_batch.launch()
         for (_, _, _, fr), pin in zip(q, pins):
             ctx.check(ctx.lib.hrt_frame_download(fr.handle, ctypes.c_void_p(pin.data_ptr()), None, None))
@@ -570,8 +577,10 @@ def run_batched(args, dist):
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
                          "bytes_per_launch": int(alg_bytes)},
-            "sequential_plain_fp32": {"value": round(rays_per_step / (ms_f32 * 1e-3) / 1e6, 3),
-                                      "ms_per_step": round(ms_f32, 3), "launches_per_step": len(models)},
+            "plain_fp32": {"value": round(rays_per_step / (ms_f32 * 1e-3) / 1e6, 3),
+                           "ms_per_step": round(ms_f32, 3), "launches_per_step": len(models),
+                           "what": "the same 16 scenes as 16 sequential launches of the FP32 tracer (FP32 nodes "
+                                   "and records, no batching, no autotuning)"},
             "sequential_quantised": {"value": round(rays_per_step / (ms_q * 1e-3) / 1e6, 3),
                                      "ms_per_step": round(ms_q, 3), "launches_per_step": len(models)},
             "per_scene_latency_ms": {"batched_all_scenes": round(ms, 3),
@@ -579,13 +588,42 @@ def run_batched(args, dist):
                                              "are per launch"},
             "scenes": per_scene,
             "e2e": {"value": round(rays_per_step / te / 1e6, 3), "unit": "Mrays/s",
-                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(d2h), "ms_per_step": round(te * 1e3, 3)},
+                    "h2d_bytes_per_step": sync_batch.table_bytes, "d2h_bytes_per_step": int(d2h),
+                    "ms_per_step": round(te * 1e3, 3)},
             "clocks": clk,
             "build": {"build_wall_s_quantised": round(build_wall, 3), "strand_generation_s": round(t_gen, 3)}}
     if not args.no_cpu:
         line.update(batch_agreement_and_cpu(args, ctx, q, models))
+    del q, f, batch, sync_batch, scenes_q
+    if not args.quick:
+        line["c4_phantom_quantised"] = c4_summary(args, ctx)
     print(json.dumps(line), flush=True)
     dist.close()
+
+
+def c4_summary(args, ctx):
+    """The single Phantom precision-pattern frame (19.05 M segments, 1920x1080 x 4 spp): quantised
+    and FP32 frame rates (no oracle legs; `--config c4_phantom_quantised` has them)."""
+    import vkhrt_gb300 as H
+    cfg, sp = workload("c4_phantom_quantised")
+    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
+    v, r, off = H.generate_strands(sp)
+    cam = H.scene_camera(w, h)
+    out = {}
+    for name, prec in (("quantised", H.Precision.QUANTISED), ("plain_fp32", H.Precision.FP32)):
+        blas = H.BottomLevelAccelerationStructure(
+            H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=prec), ctx)
+        tlas = H.TopLevelAccelerationStructure([blas], ctx)
+        fr = H.Frame(ctx, w, h, spp)
+        H.trace(ctx, tlas, cam, fr, H.trace_params(spp=spp, jitter=1, seed=17, shading=2, count_stats=1))
+        st = fr.stats()
+        p = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, **{"async": 1})
+        ms = time_frames(ctx, tlas, cam, fr, p, max(8, args.steps // 2), args.warmup)
+        out[name] = {"value": round((st["primary_rays"] + st["shadow_rays"]) / (ms * 1e-3) / 1e6, 3),
+                     "ms_per_step": round(ms, 3), "nodes_visited": int(st["nodes_visited"]),
+                     "prims_tested": int(st["prims_tested"])}
+        del fr, tlas, blas
+    return out
 
 
 def batch_agreement_and_cpu(args, ctx, q, models):
@@ -644,7 +682,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", default="c4_phantom_quantised")
+    ap.add_argument("--config", default=BATCH_CONFIG)
     ap.add_argument("--quick", action="store_true", help="skip the plain FP32 comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle agreement and CPU baseline")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

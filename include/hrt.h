@@ -255,6 +255,11 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
                             void* stream, hrt_batch** out);
 hrt_status hrt_batch_launch(hrt_batch* b, void* stream);
 hrt_status hrt_batch_destroy(hrt_batch* b);
+/* New cameras for the batch's scenes (one per scene, in creation order), uploaded with the scene
+ * table on `stream` ahead of the next hrt_batch_launch; the captured graph is reused. */
+hrt_status hrt_batch_set_cameras(hrt_batch* b, const hrt_camera* cams, uint32_t n, void* stream);
+/* Bytes one hrt_batch_set_cameras uploads. */
+uint64_t hrt_batch_table_bytes(const hrt_batch* b);
 
 /* ---- autotuner ------------------------------------------------------------------------------
  * Times every candidate kernel configuration on the given scenes (occupancy variant x refill

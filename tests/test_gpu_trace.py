@@ -313,3 +313,29 @@ def test_frame_primary_hits_equal_explicit_rays(ctx, orc, precision):
     assert np.array_equal(hit, rh["t"] >= 0)
     assert np.max(np.abs(fh["t"][hit] - rh["t"][hit]) / rh["t"][hit]) <= 1e-6
     print("fp64 resolves", fr.stats()["fp64_resolves"], "fp64 hits", int(((fh["flags"] & H.HIT_FP64) != 0).sum()))
+
+
+def test_batch_set_cameras_matches_single_launch(ctx):
+    """New cameras reach a captured batch through its scene table: the replay equals single
+    launches with those cameras."""
+    scenes = []
+    for k, (gt, ns, w, h) in enumerate([(PHANTOM, 250, 64, 40), (DOTS, 200, 48, 48)]):
+        v, r, off = H.generate_strands(H.StrandParams(seed=70 + k, nstrands=ns, nverts=16))
+        b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType(gt), vertices=v, radius=r, strand_offsets=off), ctx)
+        t = H.TopLevelAccelerationStructure([b], ctx)
+        scenes.append((b, t, H.scene_camera(w, h), H.Frame(ctx, w, h, 1, with_hits=True), w, h))
+    p = H.trace_params(shading=2, record_hits=1, split_types=1)
+    batch = H.Batch(ctx, [(t, cam, fr) for (_, t, cam, fr, *_r) in scenes], p)
+    new = [H.orbit_camera(w, h, 0.7 + k, 0.2) for k, (*_a, w, h) in enumerate(scenes)]
+    batch.set_cameras(new)
+    batch.launch()
+    assert batch.table_bytes > 0
+    for (b, t, _, fr, w, h), cam in zip(scenes, new):
+        rgba, hits = fr.download(hits=True)
+        f1 = H.Frame(ctx, w, h, 1, with_hits=True)
+        H.trace(ctx, t, cam, f1, p)
+        rgba1, hits1 = f1.download(hits=True)
+        assert (hits["t"] >= 0).sum() > 50
+        assert np.array_equal(hits, hits1) and np.abs(rgba - rgba1).max() <= 1e-6
+    with pytest.raises(H.HrtError):
+        batch.set_cameras(new[:1])

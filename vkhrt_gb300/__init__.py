@@ -99,6 +99,8 @@ SIGNATURES = {
     "hrt_autotune": (c_i32, [c_p, ctypes.POINTER(SceneDescC), c_u32, ctypes.POINTER(TraceParamsC), c_u32, c_p,
                              ctypes.POINTER(TraceParamsC), ctypes.POINTER(c_f)]),
     "hrt_batch_destroy": (c_i32, [c_p]),
+    "hrt_batch_set_cameras": (c_i32, [c_p, ctypes.POINTER(CameraC), c_u32, c_p]),
+    "hrt_batch_table_bytes": (c_u64, [c_p]),
     "hrt_strand_params_default": (None, [ctypes.POINTER(StrandParamsC)]),
     "hrt_generate_strands": (c_i32, [ctypes.POINTER(StrandParamsC), c_p, c_p, c_p]),
     "hrt_checksum": (c_u64, [c_p, c_u64, c_p, c_u64]),
@@ -465,6 +467,14 @@ class Batch:
 
     def launch(self, stream: int | None = None):
         self.ctx.check(self.ctx.lib.hrt_batch_launch(self.handle, c_p(stream) if stream else None))
+
+    def set_cameras(self, cams: list[CameraC], stream: int | None = None):
+        arr = (CameraC * len(cams))(*cams)
+        self.ctx.check(self.ctx.lib.hrt_batch_set_cameras(self.handle, arr, len(cams), c_p(stream) if stream else None))
+
+    @property
+    def table_bytes(self) -> int:
+        return int(self.ctx.lib.hrt_batch_table_bytes(self.handle))
 
     def close(self):
         if getattr(self, "handle", None):

@@ -64,6 +64,7 @@ struct ScenePlan {
         uint64_t work = 0;
     };
     std::vector<SceneLaunch> table;
+    std::vector<uint32_t> pos;  // table position of input scene i
     std::vector<Group> groups;
     uint64_t primary = 0, npix = 0, nsamp = 0, scap = 0;
     uint32_t max_spp = 1;
@@ -258,6 +259,7 @@ hrt_status make_plan(hrt_context* ctx, const char* who, const hrt_scene_desc* sc
             return fail(ctx, HRT_ERR_INVALID_ARG, "%s: record_hits on a frame without hit records", who);
     }
     P.quant = scenes[0].tlas->quantised;
+    P.pos.assign(n, 0);
     auto key = [&](uint32_t i) -> uint32_t { return split ? prim_kind(scenes[i].tlas->type_mask) : 0u; };
     for (uint32_t k = 0; k < 4; ++k) {
         ScenePlan::Group G;
@@ -268,6 +270,7 @@ hrt_status make_plan(hrt_context* ctx, const char* who, const hrt_scene_desc* sc
             fill_scene(sl, scenes[i].tlas, &scenes[i].camera, scenes[i].frame, G.work);
             G.work += sl.work_count;
             G.type_mask |= scenes[i].tlas->type_mask;
+            P.pos[i] = uint32_t(P.table.size());
             P.table.push_back(sl);
             const hrt_frame* f = scenes[i].frame;
             P.primary += uint64_t(f->w) * f->h * f->spp;
@@ -950,6 +953,26 @@ hrt_status hrt_batch_launch(hrt_batch* b, void* stream) {
     }
     return HRT_OK;
 }
+
+hrt_status hrt_batch_set_cameras(hrt_batch* b, const hrt_camera* cams, uint32_t n, void* stream) {
+    if (!b) return HRT_ERR_INVALID_ARG;
+    hrt_context* ctx = b->ctx;
+    if (!cams || n != b->plan.pos.size())
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_set_cameras: need one camera per scene (%zu)", b->plan.pos.size());
+    DeviceSet ds(ctx->device);
+    for (uint32_t i = 0; i < n; ++i) {
+        SceneLaunch& sl = b->plan.table[b->plan.pos[i]];
+        memcpy(sl.view_inv, cams[i].view_inverse, sizeof(sl.view_inv));
+        memcpy(sl.proj_inv, cams[i].proj_inverse, sizeof(sl.proj_inv));
+    }
+    // from pageable memory: the copy is staged before the call returns, so the table may change again
+    CK(ctx, cudaMemcpyAsync(b->plan.dtable, b->plan.table.data(), b->plan.table.size() * sizeof(SceneLaunch),
+                            cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream)),
+       "hrt_batch_set_cameras");
+    return HRT_OK;
+}
+
+uint64_t hrt_batch_table_bytes(const hrt_batch* b) { return b ? b->plan.table.size() * sizeof(SceneLaunch) : 0; }
 
 hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* base,
                         uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms) {

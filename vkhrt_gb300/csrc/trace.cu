@@ -472,6 +472,9 @@ __device__ __forceinline__ V3<float> safe_inv(V3<float> d) {
     auto r = [](float x) { return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
     return mk(r(d.x), r(d.y), r(d.z));
 }
+#ifndef HRT_Q8_H2
+#define HRT_Q8_H2 0
+#endif
 // 1 + (byte k of w) 2^-15 as a float: the byte placed in mantissa bits 15..8 of 1.0.
 __device__ __forceinline__ float biased_byte(uint32_t w, int k) {
     return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | (uint32_t(k) << 4)));
@@ -567,6 +570,39 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         const uint32_t nxw0 = nx ? w2.z : w2.x, nxw1 = nx ? w2.w : w2.y, fxw0 = nx ? w2.x : w2.z, fxw1 = nx ? w2.y : w2.w;
         const uint32_t nyw0 = ny ? w3.z : w3.x, nyw1 = ny ? w3.w : w3.y, fyw0 = ny ? w3.x : w3.z, fyw1 = ny ? w3.y : w3.w;
         const uint32_t nzw0 = nz ? w4.z : w4.x, nzw1 = nz ? w4.w : w4.y, fzw0 = nz ? w4.x : w4.z, fzw1 = nz ? w4.y : w4.w;
+#if HRT_Q8_H2
+        // Two bytes at a time become the halves 1024 + q (one byte permute under the exponent
+        // of 1024), widened to FP32 exactly; t = (1024 + q) s + (b - 1024 s).
+        const float kS2 = 9.5367431640625e-07f;  // 2^-20
+        const float s2x = sx * (1.0f / 32768.0f), s2y = sy * (1.0f / 32768.0f), s2z = sz * (1.0f / 32768.0f);
+        const float hx = kS2 * fmaf(1279.0f, fabsf(s2x), fabsf(bx)), hy = kS2 * fmaf(1279.0f, fabsf(s2y), fabsf(by));
+        const float hz = kS2 * fmaf(1279.0f, fabsf(s2z), fabsf(bz));
+        const float dx = fmaf(-1024.0f, s2x, bx), dy = fmaf(-1024.0f, s2y, by), dz = fmaf(-1024.0f, s2z, bz);
+        const float dxn = dx - hx, dxf = dx + hx, dyn = dy - hy, dyf = dy + hy, dzn = dz - hz, dzf = dz + hz;
+        auto h2f = [](uint32_t w, uint32_t sel) -> float2 {
+            const uint32_t u = __byte_perm(w, 0x64646464u, sel);
+            return __half22float2(*reinterpret_cast<const __half2*>(&u));
+        };
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t sel = (j & 1) ? 0x4342u : 0x4140u;
+            const float2 nxv = h2f(j < 2 ? nxw0 : nxw1, sel), fxv = h2f(j < 2 ? fxw0 : fxw1, sel);
+            const float2 nyv = h2f(j < 2 ? nyw0 : nyw1, sel), fyv = h2f(j < 2 ? fyw0 : fyw1, sel);
+            const float2 nzv = h2f(j < 2 ? nzw0 : nzw1, sel), fzv = h2f(j < 2 ? fzw0 : fzw1, sel);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int q = 2 * j + k;
+                const float vnx = k ? nxv.y : nxv.x, vfx = k ? fxv.y : fxv.x;
+                const float vny = k ? nyv.y : nyv.x, vfy = k ? fyv.y : fyv.x;
+                const float vnz = k ? nzv.y : nzv.x, vfz = k ? fzv.y : fzv.x;
+                float a = max3f(fmaf(vnx, s2x, dxn), fmaf(vny, s2y, dyn), fmaxf(fmaf(vnz, s2z, dzn), R.tmin));
+                float b = min3f(fmaf(vfx, s2x, dxf), fmaf(vfy, s2y, dyf), fminf(fmaf(vfz, s2z, dzf), tfar));
+                if (tn) tn[q] = a;
+                if (a <= b) mask |= 1u << q;
+            }
+        }
+        (void)bxn; (void)bxf; (void)byn; (void)byf; (void)bzn; (void)bzf;
+#else
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int by_ = q & 3;
@@ -580,6 +616,7 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
             if (tn) tn[q] = a;
             if (a <= b) mask |= 1u << q;
         }
+#endif
         return mask;
     }
 }
