@@ -243,13 +243,13 @@ def run_reference_batched(args):
         data, rad = oracle_geometry(orc, int(m["type"]), lines, lrad, quantised=(int(m["type"]) == 0))
         cam = H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"])
         scenes.append((m, OracleScene(orc, [(int(m["type"]), data, rad)]), H.camera_arrays(cam)))
-    npx = max(16, args.ref_pixels // len(models))
+    npx = 16384  # per scene and step: one oracle call has a few ms of thread start-up
     total_t = 0.0
     total_rays = 0
     for step in range(args.warmup + args.steps):
         for m, osc, (vi, pi) in scenes:
             w, h, spp = m["width"], m["height"], m["spp"]
-            px = sample_pixels(w, h, max(4, npx // spp), seed=1000 + step)
+            px = sample_pixels(w, h, npx, seed=1000 + step)
             t0 = time.perf_counter()
             o = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=px,
                            threads=threads)
@@ -258,7 +258,7 @@ def run_reference_batched(args):
                 total_t += dt
                 total_rays += len(px) * spp + int((o["t"] >= 0).sum())
     value = total_rays / total_t / 1e6
-    sample = f"about {npx} random samples of each of the {len(models)} scenes per step (+ shadow rays)"
+    sample = f"{npx} random pixels (all their samples) of each of the {len(models)} scenes per step (+ shadow rays)"
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_t / max(args.steps, 1), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
@@ -637,6 +637,7 @@ def batch_agreement_and_cpu(args, ctx, q, models):
     max_rel_t = 0.0
     max_rgb = 0.0
     cpu_rays = 0
+    cpu_px = 0
     cpu_s = 0.0
     per = max(1, 65536 // len(models))
     for (b, t, cam, fr), (m, v, r, off) in zip(q, models):
@@ -661,19 +662,30 @@ def batch_agreement_and_cpu(args, ctx, q, models):
         ok_px = same.reshape(-1, spp).all(axis=1)
         if ok_px.any():
             max_rgb = max(max_rgb, float(np.abs(rgba.reshape(-1, 4)[px] - o["fb"]).max(axis=1)[ok_px].max()))
-        cpx = sample_pixels(w, h, max(64, int(args.cpu_seconds * 2000 / len(models)) // spp), seed=11)
-        t0 = time.perf_counter()
-        oc = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=cpx,
-                        threads=threads)
-        cpu_s += time.perf_counter() - t0
+        # the oracle's FP32 tracer on a pixel sample grown until it takes about cpu_seconds / 16
+        # (one call has a few ms of thread start-up, so small samples would understate it)
+        npx = 4096
+        while True:
+            cpx = sample_pixels(w, h, npx, seed=11)
+            t0 = time.perf_counter()
+            oc = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=cpx,
+                            threads=threads)
+            dt = time.perf_counter() - t0
+            if dt >= args.cpu_seconds / len(models) or npx >= w * h:
+                break
+            npx = min(w * h, npx * 4)
+        cpu_s += dt
         cpu_rays += len(cpx) * spp + int((oc["t"] >= 0).sum())
+        cpu_px += len(cpx)
         del osc, data, rad
     return {"agreement": {"rays": int(n_t), "hit_id": round(1.0 - n_mis / max(n_t - n_ties, 1), 6),
                           "mismatches": int(n_mis),
                           "ties": int(n_ties), "max_rel_t": max_rel_t, "max_rgb_err_agreeing": max_rgb,
                           "oracle": "FP64 CPU restatement on the same (dequantised) geometry, per scene"},
             "cpu_baseline": {"value": round(cpu_rays / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads,
-                             "kind": "port", "sample": f"random pixels of every scene, FP32 oracle, {cpu_s:.1f} s"}}
+                             "kind": "port",
+                             "sample": f"{cpu_px} random pixels over the {len(models)} scenes (all samples, "
+                                       f"{cpu_rays} rays), FP32 oracle, {cpu_s:.1f} s"}}
 
 
 def main():

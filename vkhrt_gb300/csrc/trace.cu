@@ -472,19 +472,12 @@ __device__ __forceinline__ V3<float> safe_inv(V3<float> d) {
     auto r = [](float x) { return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
     return mk(r(d.x), r(d.y), r(d.z));
 }
-#ifndef HRT_Q8_H2
-#define HRT_Q8_H2 0
-#endif
-// 1 + (byte k of w) 2^-15 as a float: the byte placed in mantissa bits 15..8 of 1.0.
-__device__ __forceinline__ float biased_byte(uint32_t w, int k) {
-    return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | (uint32_t(k) << 4)));
-}
 
 // Child entry distances of one node; returns a bit mask of hit children and fills tn[8].
 // Near and far planes are chosen per axis by the sign of the direction (octant), so a child
 // needs three maxima and three minima. FP32 boxes: t = (plane - o) inv, accepted when
 // tnear <= tfar (1 + 2^-20). 8-bit boxes: t = q (2^e inv) + (p - o) inv, one fused operation
-// per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 33023 2^e |inv|), and that
+// per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 1279 2^e |inv|), and that
 // bound is subtracted from the axis's near planes and added to its far planes, so a box is
 // never lost to rounding (a near-parallel axis widens only its own planes).
 // Empty slots hold empty boxes and fail the test. tn (when given) receives the entry distances;
@@ -537,28 +530,24 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
     } else {
         const uint4* p = reinterpret_cast<const uint4*>(static_cast<const NodeQ*>(nodes) + ni);
         uint4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
-        // per node: s = 2^e inv (scaled to 2^15 s below), b = (p - o) inv
-        float sx = __uint_as_float((w0.w & 0xffu) << 23) * R.inv.x;
-        float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * R.inv.y;
-        float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * R.inv.z;
-        float bx = (__uint_as_float(w0.x) - R.o.x) * R.inv.x;
-        float by = (__uint_as_float(w0.y) - R.o.y) * R.inv.y;
-        float bz = (__uint_as_float(w0.z) - R.o.z) * R.inv.z;
-        // The byte q is read as the float v = 1 + q 2^-15 (byte permute into the mantissa of
-        // 1.0), and the 1 is folded into the offset: t = v S + (b - S) with S = 2^15 s, one
-        // fused multiply-add per plane. The three roundings (offset, slack, product-sum) are each
-        // below 2^-24 (|b| + (2^15 + 255) |s|), so E = 2^-20 (|b| + 33023 |s|) per axis, taken
-        // from the near planes and given to the far planes, never loses a box to rounding; it is
-        // about 1/32 of a grid step.
+        // per node: s = 2^e inv (one grid step in t), b = (p - o) inv
+        const float sx = __uint_as_float((w0.w & 0xffu) << 23) * R.inv.x;
+        const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * R.inv.y;
+        const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * R.inv.z;
+        const float bx = (__uint_as_float(w0.x) - R.o.x) * R.inv.x;
+        const float by = (__uint_as_float(w0.y) - R.o.y) * R.inv.y;
+        const float bz = (__uint_as_float(w0.z) - R.o.z) * R.inv.z;
+        // Two bytes at a time become the halves 1024 + q0, 1024 + q1 (one byte permute under the
+        // exponent of 1024), widened to FP32 exactly, and t = (1024 + q) s + (b - 1024 s), one
+        // fused multiply-add per plane. The roundings (offset, slack, product-sum) are each below
+        // 2^-24 (|b| + 1279 |s|), so E = 2^-20 (|b| + 1279 |s|) per axis, taken from the near
+        // planes and given to the far planes, never loses a box to rounding (about 1/800 of a
+        // grid step at the scale of the node).
         const float kS = 9.5367431640625e-07f;  // 2^-20
-        sx *= 32768.0f;
-        sy *= 32768.0f;
-        sz *= 32768.0f;
-        float ex = kS * fmaf(1.00775146484375f, fabsf(sx), fabsf(bx));  // 33023 / 32768
-        float ey = kS * fmaf(1.00775146484375f, fabsf(sy), fabsf(by));
-        float ez = kS * fmaf(1.00775146484375f, fabsf(sz), fabsf(bz));
-        const float cx = bx - sx, cy = by - sy, cz = bz - sz;
-        const float bxn = cx - ex, bxf = cx + ex, byn = cy - ey, byf = cy + ey, bzn = cz - ez, bzf = cz + ez;
+        const float ex = kS * fmaf(1279.0f, fabsf(sx), fabsf(bx)), ey = kS * fmaf(1279.0f, fabsf(sy), fabsf(by));
+        const float ez = kS * fmaf(1279.0f, fabsf(sz), fabsf(bz));
+        const float cx = fmaf(-1024.0f, sx, bx), cy = fmaf(-1024.0f, sy, by), cz = fmaf(-1024.0f, sz, bz);
+        const float cxn = cx - ex, cxf = cx + ex, cyn = cy - ey, cyf = cy + ey, czn = cz - ez, czf = cz + ez;
         if (imask) *imask = w0.w >> 24;
         *base = w1.x;
         if (kWithT) {
@@ -570,15 +559,6 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         const uint32_t nxw0 = nx ? w2.z : w2.x, nxw1 = nx ? w2.w : w2.y, fxw0 = nx ? w2.x : w2.z, fxw1 = nx ? w2.y : w2.w;
         const uint32_t nyw0 = ny ? w3.z : w3.x, nyw1 = ny ? w3.w : w3.y, fyw0 = ny ? w3.x : w3.z, fyw1 = ny ? w3.y : w3.w;
         const uint32_t nzw0 = nz ? w4.z : w4.x, nzw1 = nz ? w4.w : w4.y, fzw0 = nz ? w4.x : w4.z, fzw1 = nz ? w4.y : w4.w;
-#if HRT_Q8_H2
-        // Two bytes at a time become the halves 1024 + q (one byte permute under the exponent
-        // of 1024), widened to FP32 exactly; t = (1024 + q) s + (b - 1024 s).
-        const float kS2 = 9.5367431640625e-07f;  // 2^-20
-        const float s2x = sx * (1.0f / 32768.0f), s2y = sy * (1.0f / 32768.0f), s2z = sz * (1.0f / 32768.0f);
-        const float hx = kS2 * fmaf(1279.0f, fabsf(s2x), fabsf(bx)), hy = kS2 * fmaf(1279.0f, fabsf(s2y), fabsf(by));
-        const float hz = kS2 * fmaf(1279.0f, fabsf(s2z), fabsf(bz));
-        const float dx = fmaf(-1024.0f, s2x, bx), dy = fmaf(-1024.0f, s2y, by), dz = fmaf(-1024.0f, s2z, bz);
-        const float dxn = dx - hx, dxf = dx + hx, dyn = dy - hy, dyf = dy + hy, dzn = dz - hz, dzf = dz + hz;
         auto h2f = [](uint32_t w, uint32_t sel) -> float2 {
             const uint32_t u = __byte_perm(w, 0x64646464u, sel);
             return __half22float2(*reinterpret_cast<const __half2*>(&u));
@@ -595,28 +575,12 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
                 const float vnx = k ? nxv.y : nxv.x, vfx = k ? fxv.y : fxv.x;
                 const float vny = k ? nyv.y : nyv.x, vfy = k ? fyv.y : fyv.x;
                 const float vnz = k ? nzv.y : nzv.x, vfz = k ? fzv.y : fzv.x;
-                float a = max3f(fmaf(vnx, s2x, dxn), fmaf(vny, s2y, dyn), fmaxf(fmaf(vnz, s2z, dzn), R.tmin));
-                float b = min3f(fmaf(vfx, s2x, dxf), fmaf(vfy, s2y, dyf), fminf(fmaf(vfz, s2z, dzf), tfar));
+                float a = max3f(fmaf(vnx, sx, cxn), fmaf(vny, sy, cyn), fmaxf(fmaf(vnz, sz, czn), R.tmin));
+                float b = min3f(fmaf(vfx, sx, cxf), fmaf(vfy, sy, cyf), fminf(fmaf(vfz, sz, czf), tfar));
                 if (tn) tn[q] = a;
                 if (a <= b) mask |= 1u << q;
             }
         }
-        (void)bxn; (void)bxf; (void)byn; (void)byf; (void)bzn; (void)bzf;
-#else
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int by_ = q & 3;
-            const uint32_t wnx = q < 4 ? nxw0 : nxw1, wfx = q < 4 ? fxw0 : fxw1;
-            const uint32_t wny = q < 4 ? nyw0 : nyw1, wfy = q < 4 ? fyw0 : fyw1;
-            const uint32_t wnz = q < 4 ? nzw0 : nzw1, wfz = q < 4 ? fzw0 : fzw1;
-            float a = max3f(fmaf(biased_byte(wnx, by_), sx, bxn), fmaf(biased_byte(wny, by_), sy, byn),
-                            fmaxf(fmaf(biased_byte(wnz, by_), sz, bzn), R.tmin));
-            float b = min3f(fmaf(biased_byte(wfx, by_), sx, bxf), fmaf(biased_byte(wfy, by_), sy, byf),
-                            fminf(fmaf(biased_byte(wfz, by_), sz, bzf), tfar));
-            if (tn) tn[q] = a;
-            if (a <= b) mask |= 1u << q;
-        }
-#endif
         return mask;
     }
 }
