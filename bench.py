@@ -704,7 +704,7 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling)")
     ap.add_argument("--precision", choices=["fp32", "quantised"], default=None,
                     help="override the workload's BVH/primitive precision (profiling)")
-    ap.add_argument("--variant", type=int, default=0, help="trace kernel variant (0 default, 1, 2)")
+    ap.add_argument("--variant", type=int, default=0, help="resident blocks per SM: 0/1 = 4, 2 = 3, 3 = 5")
     ap.add_argument("--max-leaf", type=int, default=1, help="primitives per BVH8 leaf (1..3)")
     ap.add_argument("--refill", type=int, default=8, help="idle lanes per warp that trigger a fetch (0 = 16)")
     ap.add_argument("--speculative", type=int, default=1, help="speculative traversal (0/1)")

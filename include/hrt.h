@@ -148,7 +148,8 @@ typedef struct hrt_trace_params {
     uint32_t record_hits;  /* write per-sample hit records into the frame */
     uint32_t async;        /* 0: synchronise and check the device error word before returning */
     uint32_t count_stats;  /* accumulate traversal counters into the frame stats */
-    uint32_t kernel_variant; /* 0 default; 1: 4 resident blocks per SM; 2: 3 blocks with more registers */
+    uint32_t kernel_variant; /* resident blocks per SM (the register split): 0, 1: 4; 2: 3 (more registers
+                                per thread); 3: 5 (fewer) */
     uint32_t refill;         /* idle lanes of a warp that trigger a work fetch, 1..32 (0 = 16; default 8) */
     uint32_t speculative;    /* lanes that hold a leaf keep traversing while others search (0/1; default 1) */
     uint32_t split_types;    /* batches: one persistent launch per primitive type instead of one for all (0/1) */
@@ -267,7 +268,7 @@ uint64_t hrt_batch_table_bytes(const hrt_batch* b);
  * per type: HRT_AUTOTUNE_CANDIDATES or twice that), each `reps` times with plain launches after
  * one warm-up, and writes the fastest into `best` (a copy of `base` with kernel_variant, refill,
  * speculative and split_types replaced) and its mean frame time into `best_ms`. */
-#define HRT_AUTOTUNE_CANDIDATES 12u
+#define HRT_AUTOTUNE_CANDIDATES 18u
 hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* base,
                         uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms);
 

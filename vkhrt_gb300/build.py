@@ -1,10 +1,11 @@
 """Builds vkhrt_gb300/libhrt.so (the C ABI of include/hrt.h) for sm_103a with nvcc.
 
 Translation units compile in parallel:
-  csrc/build.cu    --fmad=false (bit-exact BVH build)
-  csrc/trace.cu    trace kernels
-  csrc/api.cu      C ABI (host code)
-  csrc/strands.cpp synthetic strands (host, -ffp-contract=off)
+  csrc/build.cu         --fmad=false (bit-exact BVH build)
+  csrc/trace.cu         explicit-ray and no-allocation trace entry points
+  csrc/trace_frames.cu  frame kernels, once for FP32 nodes and once for 8-bit nodes
+  csrc/api.cu           C ABI (host code)
+  csrc/strands.cpp      synthetic strands (host, -ffp-contract=off)
 """
 from __future__ import annotations
 
@@ -29,11 +30,14 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+# object name -> (source, extra flags); trace_frames.cu is compiled once per node layout
 UNITS = {
-    "build.cu": ["--fmad=false"],
-    "trace.cu": [],
-    "api.cu": [],
-    "strands.cpp": ["-x", "c++", "-Xcompiler", "-ffp-contract=off"],
+    "build": ("build.cu", ["--fmad=false"]),
+    "trace": ("trace.cu", []),
+    "trace_frames_f": ("trace_frames.cu", ["-DHRT_FRAMES_QUANT=0"]),
+    "trace_frames_q": ("trace_frames.cu", ["-DHRT_FRAMES_QUANT=1"]),
+    "api": ("api.cu", []),
+    "strands": ("strands.cpp", ["-x", "c++", "-Xcompiler", "-ffp-contract=off"]),
 }
 
 
@@ -44,8 +48,8 @@ def _deps() -> list[str]:
     return out
 
 
-def _compile(nvcc: str, src: str, extra: list[str], verbose: bool) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(nvcc: str, name: str, src: str, extra: list[str], verbose: bool) -> str:
+    obj = os.path.join(BUILD, name + ".o")
     cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-I" + INCLUDE, "-I" + CSRC,
            "-Xcompiler", "-fPIC", *extra, "-c", src, "-o", obj]
     if verbose:
@@ -67,7 +71,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        futs = [ex.submit(_compile, nvcc, os.path.join(CSRC, f), extra, verbose) for f, extra in UNITS.items()]
+        futs = [ex.submit(_compile, nvcc, name, os.path.join(CSRC, f), extra, verbose)
+                for name, (f, extra) in UNITS.items()]
         objs = [f.result() for f in futs]
     tmp = LIB + ".tmp"
     r = subprocess.run([nvcc, *ARCH, "-shared", "-o", tmp, *objs], capture_output=True, text=True)

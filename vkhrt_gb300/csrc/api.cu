@@ -1006,7 +1006,7 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
     }
     cudaError_t e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    const uint32_t variants[2] = {1, 2}, refills[3] = {4, 8, 16}, specs[2] = {0, 1};
+    const uint32_t variants[3] = {1, 2, 3}, refills[3] = {4, 8, 16}, specs[2] = {0, 1};
     float best_t = -1.0f;
     hrt_trace_params bp = *base;
     for (uint32_t split = 0; split < nplans && e == cudaSuccess; ++split)

@@ -1,1268 +1,16 @@
-// trace.cu -- the trace pass: ray generation, BVH8 traversal, the three hair intersectors,
-// closest-hit shading and the shadow ray, in one persistent kernel.
-//
-// Replaces ray_gen.rgen:16-48 -> traceRayEXT (RT-core traversal) -> hair_intersection.rint /
-// hardware LSS and triangle tests -> hair_closest_hit.rchit / triangle_closest_hit.rchit ->
-// miss.rmiss (constant black background, the payload's initial value ray_gen.rgen:30).
-//
-// Work: warps take 32 work items at a time from a global counter; 32 consecutive items are one
-// 8x4 pixel tile of one scene, so a warp's rays are coherent. Each thread traces all samples
-// of its pixel (primary ray, shading, shadow ray) and writes the averaged pixel.
-// Traversal (frame kernel): children sit in slots by direction, so a ray visits the hit
-// children of a node in the order i ^ octant(ray) without sorting; the stack holds node groups
-// (child_base, hit bits, internal-child mask) and parked leaf groups, one entry per visited
-// node at most. The explicit-ray kernel keeps a per-thread stack of (reference, entry
-// distance) with the hits of a node sorted by a sorting network. All waits are bounded: a full
-// stack or more than kMaxTraversalSteps steps ends the ray and sets a bit in the device error
-// word.
-#include <cuda_fp16.h>
-
+// trace.cu -- the trace pass's host entry points: frame launches (kernels in trace_frames.cu),
+// closest hit for explicit rays, and the no-allocation variant with its static scratch.
 #include <mutex>
 
-#include "hrt_internal.h"
+#include "trace_device.cuh"
 
 namespace hrt {
-namespace {
 
-constexpr unsigned kFull = 0xffffffffu;
-constexpr int kThreads = 128;
+cudaError_t launch_frames_f(const TraceLaunch& L, cudaStream_t s, int sm_count);  // trace_frames.cu
+cudaError_t launch_frames_q(const TraceLaunch& L, cudaStream_t s, int sm_count);
 
-// ---------------------------------------------------------------- small vector helpers
-template <class T> struct V3 { T x, y, z; };
-template <class T> __device__ __forceinline__ V3<T> mk(T x, T y, T z) { return {x, y, z}; }
-template <class T> __device__ __forceinline__ V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-template <class T> __device__ __forceinline__ V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-template <class T> __device__ __forceinline__ V3<T> operator*(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
-template <class T> __device__ __forceinline__ T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-template <class T> __device__ __forceinline__ V3<T> cross(V3<T> x, V3<T> y) {
-    return {x.y * y.z - y.y * x.z, x.z * y.x - y.z * x.x, x.x * y.y - y.x * x.y};
-}
-__device__ __forceinline__ float rsq(float x) { return 1.0f / sqrtf(x); }
-__device__ __forceinline__ double rsq(double x) { return 1.0 / sqrt(x); }
-template <class T> __device__ __forceinline__ V3<T> normalize(V3<T> v) { return rsq(dot(v, v)) * v; }
-template <class T> __device__ __forceinline__ T length(V3<T> v) { return sqrt(dot(v, v)); }
-template <class T> __device__ __forceinline__ T gmin(T x, T y) { return (y < x) ? y : x; }  // glm order
-template <class T> __device__ __forceinline__ T gmax(T x, T y) { return (x < y) ? y : x; }
-template <class T> __device__ __forceinline__ T gabs(T x) { return x >= T(0) ? x : -x; }
-
-// Explicitly rounded forms (fixed fused multiply-adds, no contraction left to the compiler),
-// for values that must not depend on how a kernel variant is compiled: instance transforms,
-// normals, shading.
-__device__ __forceinline__ float dot_rn(V3<float> a, V3<float> b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, __fmul_rn(a.x, b.x))); }
-__device__ __forceinline__ V3<float> normalize_rn(V3<float> v) {
-    const float k = __fdiv_rn(1.0f, __fsqrt_rn(dot_rn(v, v)));
-    return mk(__fmul_rn(k, v.x), __fmul_rn(k, v.y), __fmul_rn(k, v.z));
-}
-__device__ __forceinline__ V3<float> cross_rn(V3<float> x, V3<float> y) {
-    return mk(fmaf(x.y, y.z, -__fmul_rn(y.y, x.z)), fmaf(x.z, y.x, -__fmul_rn(y.z, x.x)), fmaf(x.x, y.y, -__fmul_rn(y.x, x.y)));
-}
-// rows of a 3x4 affine matrix applied to a point / a direction
-__device__ __forceinline__ V3<float> xform_point(const float* m, V3<float> p) {
-    return mk(fmaf(m[2], p.z, fmaf(m[1], p.y, fmaf(m[0], p.x, m[3]))), fmaf(m[6], p.z, fmaf(m[5], p.y, fmaf(m[4], p.x, m[7]))),
-              fmaf(m[10], p.z, fmaf(m[9], p.y, fmaf(m[8], p.x, m[11]))));
-}
-__device__ __forceinline__ V3<float> xform_dir(const float* m, V3<float> v) {
-    return mk(fmaf(m[2], v.z, fmaf(m[1], v.y, __fmul_rn(m[0], v.x))), fmaf(m[6], v.z, fmaf(m[5], v.y, __fmul_rn(m[4], v.x))),
-              fmaf(m[10], v.z, fmaf(m[9], v.y, __fmul_rn(m[8], v.x))));
-}
-
-// ---------------------------------------------------------------- Phantom (Prhi)
-// curve.glsl:9-31
-template <class T> __device__ __forceinline__ V3<T> bez_point(const V3<T>* c, T t) {
-    T u = T(1) - t, tt = t * t, uu = u * u;
-    T uuu = uu * u, ttt = tt * t;
-    return uuu * c[0] + (T(3) * uu * t) * c[1] + (T(3) * u * tt) * c[2] + ttt * c[3];
-}
-template <class T> __device__ __forceinline__ V3<T> bez_axis(const V3<T>* c, T t) {
-    T u = T(1) - t;
-    return (T(-3) * u * u) * c[0] + (T(3) * (T(3) * t * t - T(4) * t + T(1))) * c[1] +
-           (T(3) * (T(2) - T(3) * t) * t) * c[2] + (T(3) * t * t) * c[3];
-}
-// cylinder.glsl:8-46 (capped cylinder, boolean; no range test on t)
-template <class T> __device__ __forceinline__ bool ray_cylinder(V3<T> o, V3<T> d, V3<T> p0, V3<T> p1, T r) {
-    V3<T> ba = p1 - p0, oc = o - p0;
-    T baba = dot(ba, ba), bard = dot(ba, d), baoc = dot(ba, oc);
-    T k2 = baba - bard * bard;
-    T k1 = baba * dot(oc, d) - baoc * bard;
-    T k0 = baba * dot(oc, oc) - baoc * baoc - r * r * baba;
-    T h = k1 * k1 - k2 * k0;
-    if (h < T(0)) return false;
-    h = sqrt(h);
-    T t = (-k1 - h) / k2;
-    T y = baoc + t * bard;
-    if (y > T(0) && y < baba) return true;
-    t = ((y < T(0) ? T(0) : baba) - baoc) / bard;
-    return gabs(k1 + k2 * t) < h;
-}
-
-// kUnresolved: no hit, and a side used all 8 iterations inside [0, 1] with a real cone
-// intersection at its last step (det > 0 but |dt| >= 5e-5): the FP32 run failed its
-// convergence test. Runs that exhaust without an intersection are misses.
-enum { kMiss = 0, kHit = 1, kUnresolved = 2 };
-template <class T> struct PrhiOut { T s; T sl; T ts; T tc; int status; };  // s = ts + sl
-
-// ray.glsl:13-17 MakeOrthonormalBasis; the RCC transform (ray.glsl:19-33) is the inverse of
-// [e1 e2 e3 | o], applied here as the transpose of the orthonormal frame after the translation.
-template <class T> struct Frame { V3<T> e1, e2, e3; T inv_dd; };
-template <class T> __device__ __forceinline__ Frame<T> make_frame(V3<T> d) {
-    Frame<T> f;
-    f.inv_dd = T(1) / dot(d, d);
-    f.e3 = normalize(d);
-    V3<T> w = f.e3;
-    f.e2 = gabs(w.x) > gabs(w.y) ? normalize(mk(-w.z, T(0), w.x)) : normalize(mk(T(0), w.z, -w.y));
-    f.e1 = cross(f.e2, w);
-    return f;
-}
-
-// a - b - ts * d to full precision: a - b exactly by TwoSum, then one fused multiply-add.
-template <class T> __device__ __forceinline__ T rel_coord(T a, T b, T ts, T d) {
-    T c = -b;
-    T sum = a + c;
-    T cc = sum - a;
-    T err = (a - (sum - cc)) + (c - cc);
-    return fma(-ts, d, sum) + err;
-}
-
-// hair_intersection.rint:15-130 with the cone radius r0 + (r1 - r0) t (constant when equal).
-// The solve runs from o' = o + ts d, the ray point nearest the chord midpoint, on the vectors
-// P - o' kept at full precision (o' itself is never rounded); ts is added back to the
-// distance. The result is the same in exact arithmetic; in FP32 it removes the cancellation of
-// the world-space bounding-cylinder test from a distant origin (hair_intersection.rint:29).
-template <class T>
-__device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, const V3<T>* P, T r0, T r1) {
-    PrhiOut<T> out{T(0), T(0), T(0), T(0), kMiss};
-    V3<T> cm = T(0.5) * (P[0] + P[3]);
-    T ts = dot(cm - o, d) * F.inv_dd;
-    out.ts = ts;
-    V3<T> W[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-        W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
-    V3<T> mid = bez_point(P, T(0.5));
-    T rmax = length(cross(mid - P[0], mid - P[3])) / length(P[3] - P[0]) + gmax(r0, r1);
-    if (!ray_cylinder(mk(T(0), T(0), T(0)), d, W[0], W[3], rmax)) return out;
-    V3<T> Q[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) Q[k] = mk(dot(F.e1, W[k]), dot(F.e2, W[k]), dot(F.e3, W[k]));
-    T tStart = (Q[3].z - Q[0].z) > T(0) ? T(0) : T(1);
-    bool unresolved = false;
-    for (int side = 0; side < 2; ++side) {
-        T t = tStart, told = T(0), dt1 = T(0), dt2 = T(0);
-        bool exhausted = true, last_isect = false;
-        for (int i = 0; i < 8; ++i) {
-            V3<T> c = bez_point(Q, t);
-            V3<T> ax = bez_axis(Q, t);
-            T rad = (r0 == r1) ? r0 : r0 + (r1 - r0) * t;
-            // cone.glsl:21-62 with slant 0
-            T ddd = ax.x * ax.x + ax.y * ax.y;
-            T dp = c.x * c.x + c.y * c.y;
-            T cdd = c.x * ax.x + c.y * ax.y;
-            T cxd = c.x * ax.y - c.y * ax.x;
-            T cc = ddd;
-            T b = ax.z * (-cdd);
-            T cdz2 = ax.z * ax.z;
-            ddd += cdz2;
-            T a = cxd * cxd - ddd * (rad * rad) + dp * cdz2;
-            T det = b * b - a * cc;
-            bool isect = det > T(0);
-            last_isect = isect;
-            T s = (b - (isect ? sqrt(det) : T(0))) / cc;
-            T dt = (s * ax.z - cdd) / ddd;
-            if (isect && gabs(dt) < T(5e-5)) {
-                out.sl = s + c.z;
-                out.s = out.sl + ts;
-                out.tc = t;
-                exhausted = false;
-                break;
-            }
-            dt = gmin(dt, T(0.5));
-            dt = gmax(dt, T(-0.5));
-            dt1 = dt2;
-            dt2 = dt;
-            if (dt1 * dt2 < T(0)) {
-                T tnext = ((i & 3) == 0) ? T(0.5) * (told + t) : (dt2 * told - dt1 * t) / (dt2 - dt1);
-                told = t;
-                t = tnext;
-            } else {
-                told = t;
-                t += dt;
-            }
-            if (t < T(0) || t > T(1)) { exhausted = false; break; }
-        }
-        unresolved |= exhausted && last_isect;
-        if (out.s > T(0)) break;
-        tStart = T(1) - tStart;
-    }
-    out.status = out.s > T(0) ? kHit : (unresolved ? kUnresolved : kMiss);
-    return out;
-}
-
-// FP64 re-solve of one candidate, kept out of line so the FP32 path keeps its registers.
-__device__ __noinline__ void prhi_fp64(float ox, float oy, float oz, float dx, float dy, float dz, const float* cp,
-                                       float r0, float r1, double* s_out, double* sl_out, double* ts_out,
-                                       double* tc_out) {
-    V3<double> o = mk(double(ox), double(oy), double(oz)), d = mk(double(dx), double(dy), double(dz));
-    Frame<double> F = make_frame(d);
-    V3<double> P[4];
-    for (int k = 0; k < 4; ++k) P[k] = mk(double(cp[3 * k]), double(cp[3 * k + 1]), double(cp[3 * k + 2]));
-    PrhiOut<double> r = prhi(F, o, d, P, double(r0), double(r1));
-    *s_out = r.status == kHit ? r.s : -1.0;
-    *sl_out = r.sl;
-    *ts_out = r.ts;
-    *tc_out = r.tc;
-}
-
-// ---------------------------------------------------------------- LSS (round cone)
-// Envelope of spheres a + u (b-a), radius ra + u (rb-ra): tangent-cone roots with u in [0,1]
-// and both end spheres; the least t >= tmin wins. Solved from o' = o + ts d (the ray point
-// nearest the segment midpoint) on the full-precision vectors a - o', b - o'; t = ts + t'.
-// Quadratic coefficients are formed with cross products (Lagrange's identity) so that no term
-// is the small difference of two large ones: for the sphere, h = r^2 |d|^2 - |oc x d|^2.
-__device__ __forceinline__ float sphere_hit(V3<float> oc, V3<float> d, float r, float tmin, float best) {
-    float A = dot(d, d), B = dot(oc, d);
-    V3<float> c = cross(oc, d);
-    float h = r * r * A - dot(c, c);
-    if (h < 0.0f) return best;
-    float sh = sqrtf(h);
-    float t0 = (-B - sh) / A, t1 = (-B + sh) / A;
-    if (t0 >= tmin && t0 < best) return t0;
-    if (t1 >= tmin && t1 < best) return t1;
-    return best;
-}
-// Tangent cone: m |P-a|^2 - (y + ra dr)^2 - m ra^2 = 0 with y = (b-a).(P-a), m = L^2 - dr^2;
-// with c1 = ba x oa and c2 = ba x d the quadratic A t^2 + 2 B t + C has
-//   A = |c2|^2 - dr^2 |d|^2,  B = c1.c2 - dr^2 (oa.d) - ra dr (ba.d),
-//   C = |c1|^2 - dr^2 |oa|^2 - 2 ra dr (ba.oa) - ra^2 L^2.
-__device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> a, V3<float> b, float ra, float rb,
-                                         float tmin_in, float* u_out, float* tl_out, float* ts_out) {
-    const float kNone = __int_as_float(0x7f800000);
-    float ts = dot(0.5f * (a + b) - o_in, d) / dot(d, d);
-    V3<float> wa = mk(rel_coord(a.x, o_in.x, ts, d.x), rel_coord(a.y, o_in.y, ts, d.y), rel_coord(a.z, o_in.z, ts, d.z));
-    V3<float> wb = mk(rel_coord(b.x, o_in.x, ts, d.x), rel_coord(b.y, o_in.y, ts, d.y), rel_coord(b.z, o_in.z, ts, d.z));
-    V3<float> oa = mk(-wa.x, -wa.y, -wa.z);
-    float tmin = tmin_in - ts;
-    float best = kNone, bu = 0.0f;
-    V3<float> ba = b - a;
-    float dr = rb - ra;
-    float L2 = dot(ba, ba);
-    float m = L2 - dr * dr;
-    if (m > 0.0f) {
-        V3<float> c1 = cross(ba, oa), c2 = cross(ba, d);
-        float yd = dot(ba, d), ybo = dot(ba, oa);
-        float yo = ybo + ra * dr;
-        float A = dot(c2, c2) - dr * dr * dot(d, d);
-        float B = dot(c1, c2) - dr * dr * dot(oa, d) - ra * dr * yd;
-        float C = dot(c1, c1) - dr * dr * dot(oa, oa) - 2.0f * ra * dr * ybo - ra * ra * L2;
-        float h = B * B - A * C;
-        if (h >= 0.0f && A != 0.0f) {
-            float sh = sqrtf(h);
-            float r0 = (-B - sh) / A, r1 = (-B + sh) / A;
-            float lo = gmin(r0, r1), hi = gmax(r0, r1);
-            float u = (yo + lo * yd) / m;
-            if (lo >= tmin && lo < best && u >= 0.0f && u <= 1.0f) { best = lo; bu = u; }
-            else {
-                u = (yo + hi * yd) / m;
-                if (hi >= tmin && hi < best && u >= 0.0f && u <= 1.0f) { best = hi; bu = u; }
-            }
-        }
-    }
-    float ta = sphere_hit(oa, d, ra, tmin, best);
-    if (ta < best) { best = ta; bu = 0.0f; }
-    float tb = sphere_hit(mk(-wb.x, -wb.y, -wb.z), d, rb, tmin, best);
-    if (tb < best) { best = tb; bu = 1.0f; }
-    if (best == kNone) return -1.0f;
-    *u_out = bu;
-    *tl_out = best;
-    *ts_out = ts;
-    return best + ts;
-}
-
-// ---------------------------------------------------------------- triangles (watertight)
-struct TriRay { int kx, ky, kz; float Sx, Sy, Sz; };
-__device__ __forceinline__ TriRay make_triray(V3<float> d) {
-    TriRay r;
-    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
-    r.kz = 0;
-    if (ay > ax && ay >= az) r.kz = 1;
-    else if (az > ax && az > ay) r.kz = 2;
-    r.kx = r.kz == 2 ? 0 : r.kz + 1;
-    r.ky = r.kx == 2 ? 0 : r.kx + 1;
-    float dk[3] = {d.x, d.y, d.z};
-    if (dk[r.kz] < 0.0f) { int t = r.kx; r.kx = r.ky; r.ky = t; }
-    r.Sx = dk[r.kx] / dk[r.kz];
-    r.Sy = dk[r.ky] / dk[r.kz];
-    r.Sz = 1.0f / dk[r.kz];
-    return r;
-}
-__device__ __forceinline__ float comp(V3<float> v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
-__device__ __forceinline__ float tri_hit(const TriRay& R, V3<float> o, V3<float> v0, V3<float> v1, V3<float> v2,
-                                         float tmin, float tmax) {
-    V3<float> A = v0 - o, B = v1 - o, C = v2 - o;
-    float Akz = comp(A, R.kz), Bkz = comp(B, R.kz), Ckz = comp(C, R.kz);
-    float Ax = comp(A, R.kx) - R.Sx * Akz, Ay = comp(A, R.ky) - R.Sy * Akz;
-    float Bx = comp(B, R.kx) - R.Sx * Bkz, By = comp(B, R.ky) - R.Sy * Bkz;
-    float Cx = comp(C, R.kx) - R.Sx * Ckz, Cy = comp(C, R.ky) - R.Sy * Ckz;
-    float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
-    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return -1.0f;
-    float det = U + V + W;
-    if (det == 0.0f) return -1.0f;
-    float Tn = U * (R.Sz * Akz) + V * (R.Sz * Bkz) + W * (R.Sz * Ckz);
-    float t = Tn / det;
-    if (!(t >= tmin) || !(t <= tmax)) return -1.0f;
-    return t;
-}
-
-// ---------------------------------------------------------------- hit state
-struct Hit {
-    float t;
-    uint32_t id;    // reported primitive id
-    uint32_t inst;
-    uint32_t slot;  // leaf slot of the hit segment
-    float u;        // curve / segment parameter
-    float ts, sl;   // t = ts + sl: the primitive's reference point o + ts d and the distance from it
-    uint32_t flags; // HRT_HIT_FP64
-};
-__device__ __forceinline__ bool beats(float t, uint32_t inst, uint32_t id, const Hit& h) {
-    if (t < h.t) return true;
-    if (t > h.t) return false;
-    return inst < h.inst || (inst == h.inst && id < h.id);
-}
-
-struct RayState {
-    V3<float> o, d, inv;
-    float tmin;
-    Frame<float> F;   // Phantom ray-centric frame
-    TriRay tr;
-};
-
-struct Stats { uint32_t nodes, prims, r64, h64, need64; };
-
-// ---------------------------------------------------------------- leaves
-__device__ __forceinline__ void load_phantom(const DevBlas& B, uint32_t slot, V3<float>* P, float* r0, float* r1,
-                                             uint32_t* id) {
-    if (B.precision == HRT_PRECISION_QUANTISED) {
-        const PrimPhantomH* pr = static_cast<const PrimPhantomH*>(B.prims) + slot;
-        uint4 q0 = __ldg(&pr->q0), q1 = __ldg(&pr->q1);
-        uint32_t key = q1.w;
-        float4 rt = __ldg(&B.roots[key >> 8]);
-        uint32_t w[7] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z};
-        float h[14];
-#pragma unroll
-        for (int j = 0; j < 7; ++j) {
-            __half2 hh = *reinterpret_cast<const __half2*>(&w[j]);
-            float2 f = __half22float2(hh);
-            h[2 * j] = f.x;
-            h[2 * j + 1] = f.y;
-        }
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            P[k] = mk(__fadd_rn(rt.x, h[3 * k]), __fadd_rn(rt.y, h[3 * k + 1]), __fadd_rn(rt.z, h[3 * k + 2]));
-        *r0 = h[12];
-        *r1 = h[13];
-        *id = __float_as_uint(rt.w) + (key & 0xffu);
-    } else {
-        const PrimPhantomF* pr = static_cast<const PrimPhantomF*>(B.prims) + slot;
-        float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c), d = __ldg(&pr->d);
-        P[0] = mk(a.x, a.y, a.z);
-        P[1] = mk(b.x, b.y, b.z);
-        P[2] = mk(c.x, c.y, c.z);
-        P[3] = mk(d.x, d.y, d.z);
-        *r0 = a.w;
-        *r1 = b.w;
-        *id = __float_as_uint(c.w);
-    }
-}
-
-// Tests one leaf slot; returns true if it produced an accepted hit. kType is the primitive
-// type when every instance of the launch has the same one, kMixed to branch on the BLAS.
-// kFlag64: a non-converged Phantom candidate only sets st.need64 (the FP64 re-solve runs in a
-// later pass); otherwise it is re-solved here.
-constexpr int kMixed = 3;
-template <int kType = kMixed, bool kFlag64 = false>
-__device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint32_t inst, const RayState& R, Hit& h,
-                                          bool fp64_resolve, Stats& st) {
-    const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
-    if (type == HRT_BLAS_PHANTOM) {
-        V3<float> P[4];
-        float r0, r1;
-        uint32_t id;
-        load_phantom(B, slot, P, &r0, &r1, &id);
-        PrhiOut<float> r = prhi(R.F, R.o, R.d, P, r0, r1);
-        if (r.status == kHit) {
-            if (r.s >= R.tmin && beats(r.s, inst, id, h)) {
-                h = Hit{r.s, id, inst, slot, r.tc, r.ts, r.sl, 0u};
-                return true;
-            }
-        } else if (kFlag64 && r.status == kUnresolved && fp64_resolve) {
-            st.need64 = 1u;
-        } else if (!kFlag64 && r.status == kUnresolved && fp64_resolve) {
-            float cp[12];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) { cp[3 * k] = P[k].x; cp[3 * k + 1] = P[k].y; cp[3 * k + 2] = P[k].z; }
-            double s64, sl64, tc64, ts64;
-            prhi_fp64(R.o.x, R.o.y, R.o.z, R.d.x, R.d.y, R.d.z, cp, r0, r1, &s64, &sl64, &ts64, &tc64);
-            ++st.r64;
-            if (s64 > 0.0) {
-                ++st.h64;
-                float s = float(s64);
-                if (s >= R.tmin && beats(s, inst, id, h)) {
-                    h = Hit{s, id, inst, slot, float(tc64), float(ts64), float(s64 - double(float(ts64))), HRT_HIT_FP64};
-                    return true;
-                }
-            }
-        }
-        return false;
-    }
-    if (type == HRT_BLAS_LSS) {
-        const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + slot;
-        float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
-        float u, tl, ts;
-        float t = lss_hit(R.o, R.d, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, R.tmin, &u, &tl, &ts);
-        if (t >= 0.0f && t <= h.t) {
-            uint32_t id = __ldg(&B.prim_ids[slot]);
-            if (beats(t, inst, id, h)) { h = Hit{t, id, inst, slot, u, ts, tl, 0u}; return true; }
-        }
-        return false;
-    }
-    // DOTS: two orthogonal quads of the segment; triangle k has id 4 * segment + k
-    const PrimDots* pr = static_cast<const PrimDots*>(B.prims) + slot;
-    float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c), d = __ldg(&pr->d), e = __ldg(&pr->e);
-    V3<float> s0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y);
-    V3<float> va[2] = {mk(b.z, b.w, c.x), mk(c.y, c.z, c.w)};
-    V3<float> vb[2] = {mk(d.x, d.y, d.z), mk(d.w, e.x, e.y)};
-    uint32_t seg = __float_as_uint(e.z);
-    bool any = false;
-#pragma unroll
-    for (int face = 0; face < 2; ++face) {
-        V3<float> A0 = s0 + va[face], A1 = e0 - vb[face], A2 = e0 + vb[face];
-        V3<float> B1 = s0 - va[face];
-        // triangle 2 face: (start+v*ra, end-v*rb, end+v*rb); 2 face+1: (start+v*ra, start-v*ra, end-v*rb)
-        float t0 = tri_hit(R.tr, R.o, A0, A1, A2, R.tmin, h.t);
-        if (t0 >= 0.0f) {
-            uint32_t id = 4u * seg + 2u * face;
-            if (beats(t0, inst, id, h)) { h = Hit{t0, id, inst, slot, 0.0f, 0.0f, 0.0f, 0u}; any = true; }
-        }
-        float t1 = tri_hit(R.tr, R.o, A0, B1, A1, R.tmin, h.t);
-        if (t1 >= 0.0f) {
-            uint32_t id = 4u * seg + 2u * face + 1u;
-            if (beats(t1, inst, id, h)) { h = Hit{t1, id, inst, slot, 0.0f, 0.0f, 0.0f, 0u}; any = true; }
-        }
-    }
-    return any;
-}
-
-// ---------------------------------------------------------------- nodes
-
-// Reciprocal direction with zero components replaced by +-1e20, so slab distances stay finite
-// (a ray inside a slab gets -huge..+huge, one outside a pair of equal signs).
-// Three-input minimum and maximum (sm_100 and later); like fminf/fmaxf, a NaN input is ignored
-// unless all are NaN.
-__device__ __forceinline__ float max3f(float a, float b, float c) {
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-__device__ __forceinline__ float min3f(float a, float b, float c) {
-    float r;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-
-__device__ __forceinline__ V3<float> safe_inv(V3<float> d) {
-    auto r = [](float x) { return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
-    return mk(r(d.x), r(d.y), r(d.z));
-}
-
-// Child entry distances of one node; returns a bit mask of hit children and fills tn[8].
-// Near and far planes are chosen per axis by the sign of the direction (octant), so a child
-// needs three maxima and three minima. FP32 boxes: t = (plane - o) inv, accepted when
-// tnear <= tfar (1 + 2^-20). 8-bit boxes: t = q (2^e inv) + (p - o) inv, one fused operation
-// per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 1279 2^e |inv|), and that
-// bound is subtracted from the axis's near planes and added to its far planes, so a box is
-// never lost to rounding (a near-parallel axis widens only its own planes).
-// Empty slots hold empty boxes and fail the test. tn (when given) receives the entry distances;
-// kWithT: also prim_base and the meta words m0/m1 (sorted traversal).
-template <bool kQuant, bool kWithT = true>
-__device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, const RayState& R, float tfar,
-                                              float* tn, uint32_t* base, uint32_t* pbase, uint32_t* m0, uint32_t* m1,
-                                              uint32_t* imask = nullptr) {
-    uint32_t mask = 0;
-    const bool nx = R.inv.x < 0.0f, ny = R.inv.y < 0.0f, nz = R.inv.z < 0.0f;
-    if (!kQuant) {
-        const float kEps = 1.0f + 9.5367431640625e-07f;  // 1 + 2^-20
-        const float4* p = reinterpret_cast<const float4*>(static_cast<const NodeF*>(nodes) + ni);
-        // float4 index of lo_x, hi_x, lo_y, hi_y, lo_z, hi_z: 0, 2, 4, 6, 8, 10
-        const int ax = nx ? 2 : 0, ay = ny ? 6 : 4, az = nz ? 10 : 8;
-        float4 n0 = __ldg(p + ax), n1 = __ldg(p + ax + 1), f0 = __ldg(p + (2 - ax)), f1 = __ldg(p + (3 - ax));
-        float4 n2 = __ldg(p + ay), n3 = __ldg(p + ay + 1), f2 = __ldg(p + (10 - ay)), f3 = __ldg(p + (11 - ay));
-        float4 n4 = __ldg(p + az), n5 = __ldg(p + az + 1), f4 = __ldg(p + (18 - az)), f5 = __ldg(p + (19 - az));
-        const float4 tail = __ldg(p + 12);  // child_base, prim_base, imask, pad
-        *base = __float_as_uint(tail.x);
-        if (imask) *imask = __float_as_uint(tail.z);
-        if (kWithT) {
-            const float2 mw = __ldg(reinterpret_cast<const float2*>(p + 13));
-            *pbase = __float_as_uint(tail.y);
-            *m0 = __float_as_uint(mw.x);
-            *m1 = __float_as_uint(mw.y);
-        }
-        const float NX[8] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, n1.z, n1.w};
-        const float FX[8] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
-        const float NY[8] = {n2.x, n2.y, n2.z, n2.w, n3.x, n3.y, n3.z, n3.w};
-        const float FY[8] = {f2.x, f2.y, f2.z, f2.w, f3.x, f3.y, f3.z, f3.w};
-        const float NZ[8] = {n4.x, n4.y, n4.z, n4.w, n5.x, n5.y, n5.z, n5.w};
-        const float FZ[8] = {f4.x, f4.y, f4.z, f4.w, f5.x, f5.y, f5.z, f5.w};
-        // t = plane inv + (-o inv) in one fused operation. -o inv is rounded once (error below
-        // 2^-24 |o inv|), so each axis's near offsets take 2^-22 |o inv| off and its far offsets
-        // add it; the product-sum's own rounding and that of inv are relative to t and covered
-        // by the 2^-20 relative margin of the final test.
-        const float ox = -R.o.x * R.inv.x, oy = -R.o.y * R.inv.y, oz = -R.o.z * R.inv.z;
-        const float kO = 2.384185791015625e-07f;  // 2^-22
-        const float ex = kO * fabsf(ox), ey = kO * fabsf(oy), ez = kO * fabsf(oz);
-        const float oxn = ox - ex, oxf = ox + ex, oyn = oy - ey, oyf = oy + ey, ozn = oz - ez, ozf = oz + ez;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            float a = max3f(fmaf(NX[q], R.inv.x, oxn), fmaf(NY[q], R.inv.y, oyn), fmaxf(fmaf(NZ[q], R.inv.z, ozn), R.tmin));
-            float b = min3f(fmaf(FX[q], R.inv.x, oxf), fmaf(FY[q], R.inv.y, oyf), fminf(fmaf(FZ[q], R.inv.z, ozf), tfar));
-            if (tn) tn[q] = a;
-            if (a <= b * kEps) mask |= 1u << q;
-        }
-        return mask;
-    } else {
-        const uint4* p = reinterpret_cast<const uint4*>(static_cast<const NodeQ*>(nodes) + ni);
-        uint4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
-        // per node: s = 2^e inv (one grid step in t), b = (p - o) inv
-        const float sx = __uint_as_float((w0.w & 0xffu) << 23) * R.inv.x;
-        const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * R.inv.y;
-        const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * R.inv.z;
-        const float bx = (__uint_as_float(w0.x) - R.o.x) * R.inv.x;
-        const float by = (__uint_as_float(w0.y) - R.o.y) * R.inv.y;
-        const float bz = (__uint_as_float(w0.z) - R.o.z) * R.inv.z;
-        // Two bytes at a time become the halves 1024 + q0, 1024 + q1 (one byte permute under the
-        // exponent of 1024), widened to FP32 exactly, and t = (1024 + q) s + (b - 1024 s), one
-        // fused multiply-add per plane. The roundings (offset, slack, product-sum) are each below
-        // 2^-24 (|b| + 1279 |s|), so E = 2^-20 (|b| + 1279 |s|) per axis, taken from the near
-        // planes and given to the far planes, never loses a box to rounding (about 1/800 of a
-        // grid step at the scale of the node).
-        const float kS = 9.5367431640625e-07f;  // 2^-20
-        const float ex = kS * fmaf(1279.0f, fabsf(sx), fabsf(bx)), ey = kS * fmaf(1279.0f, fabsf(sy), fabsf(by));
-        const float ez = kS * fmaf(1279.0f, fabsf(sz), fabsf(bz));
-        const float cx = fmaf(-1024.0f, sx, bx), cy = fmaf(-1024.0f, sy, by), cz = fmaf(-1024.0f, sz, bz);
-        const float cxn = cx - ex, cxf = cx + ex, cyn = cy - ey, cyf = cy + ey, czn = cz - ez, czf = cz + ez;
-        if (imask) *imask = w0.w >> 24;
-        *base = w1.x;
-        if (kWithT) {
-            *pbase = w1.y;
-            *m0 = w1.z;
-            *m1 = w1.w;
-        }
-        // near / far byte words per axis (qlo = .x .y, qhi = .z .w)
-        const uint32_t nxw0 = nx ? w2.z : w2.x, nxw1 = nx ? w2.w : w2.y, fxw0 = nx ? w2.x : w2.z, fxw1 = nx ? w2.y : w2.w;
-        const uint32_t nyw0 = ny ? w3.z : w3.x, nyw1 = ny ? w3.w : w3.y, fyw0 = ny ? w3.x : w3.z, fyw1 = ny ? w3.y : w3.w;
-        const uint32_t nzw0 = nz ? w4.z : w4.x, nzw1 = nz ? w4.w : w4.y, fzw0 = nz ? w4.x : w4.z, fzw1 = nz ? w4.y : w4.w;
-        auto h2f = [](uint32_t w, uint32_t sel) -> float2 {
-            const uint32_t u = __byte_perm(w, 0x64646464u, sel);
-            return __half22float2(*reinterpret_cast<const __half2*>(&u));
-        };
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t sel = (j & 1) ? 0x4342u : 0x4140u;
-            const float2 nxv = h2f(j < 2 ? nxw0 : nxw1, sel), fxv = h2f(j < 2 ? fxw0 : fxw1, sel);
-            const float2 nyv = h2f(j < 2 ? nyw0 : nyw1, sel), fyv = h2f(j < 2 ? fyw0 : fyw1, sel);
-            const float2 nzv = h2f(j < 2 ? nzw0 : nzw1, sel), fzv = h2f(j < 2 ? fzw0 : fzw1, sel);
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int q = 2 * j + k;
-                const float vnx = k ? nxv.y : nxv.x, vfx = k ? fxv.y : fxv.x;
-                const float vny = k ? nyv.y : nyv.x, vfy = k ? fyv.y : fyv.x;
-                const float vnz = k ? nzv.y : nzv.x, vfz = k ? fzv.y : fzv.x;
-                float a = max3f(fmaf(vnx, sx, cxn), fmaf(vny, sy, cyn), fmaxf(fmaf(vnz, sz, czn), R.tmin));
-                float b = min3f(fmaf(vfx, sx, cxf), fmaf(vfy, sy, cyf), fminf(fmaf(vfz, sz, czf), tfar));
-                if (tn) tn[q] = a;
-                if (a <= b) mask |= 1u << q;
-            }
-        }
-        return mask;
-    }
-}
-
-// {child_base, prim_base, meta[0..3], meta[4..7]} of node ni.
-template <bool kQuant>
-__device__ __forceinline__ uint4 node_header(const void* nodes, uint32_t ni) {
-    if (kQuant) return __ldg(reinterpret_cast<const uint4*>(static_cast<const NodeQ*>(nodes) + ni) + 1);
-    const uint4* p = reinterpret_cast<const uint4*>(static_cast<const NodeF*>(nodes) + ni);
-    const uint4 t = __ldg(p + 12);
-    const uint2 m = __ldg(reinterpret_cast<const uint2*>(p + 13));
-    return make_uint4(t.x, t.y, m.x, m.y);
-}
-
-// Slot-order mask -> traversal order for a ray of direction octant oct: bit i <- bit i ^ oct.
-__device__ __forceinline__ uint32_t oct_permute(uint32_t m, uint32_t oct) {
-    if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
-    if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
-    if (oct & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
-    return m;
-}
-
-__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
-    uint32_t lo = min(a, b), hi = max(a, b);
-    a = lo;
-    b = hi;
-}
-
-// Traverses one BLAS. any_hit: stop at the first accepted hit (shadow rays), skipping slot
-// `skip_slot` of instance `skip_inst`.
-template <bool kQuant>
-__device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit& h, bool any_hit, uint32_t skip_inst,
-                         uint32_t skip_slot, bool fp64_resolve, Stats& st, uint32_t& err) {
-    if (B.nnodes == 0) return false;
-    uint2 stack[kStackSize];
-    int sp = 0;
-    stack[sp++] = make_uint2(0u, __float_as_uint(R.tmin));
-    bool found = false;
-    uint32_t steps = 0;
-    while (sp > 0) {
-        if (++steps > kMaxTraversalSteps) { err |= kErrTimeout; break; }
-        uint2 e = stack[--sp];
-        if (__uint_as_float(e.y) > h.t) continue;
-        if (e.x & kLeafFlag) {
-            uint32_t first = (e.x & ~kLeafFlag) >> 2, cnt = (e.x & 3u) + 1u;
-            for (uint32_t j = 0; j < cnt; ++j) {
-                uint32_t slot = first + j;
-                if (any_hit && inst == skip_inst && slot == skip_slot) continue;
-                ++st.prims;
-                if (leaf_test(B, slot, inst, R, h, fp64_resolve, st)) {
-                    found = true;
-                    if (any_hit) return true;
-                }
-            }
-            continue;
-        }
-        ++st.nodes;
-        float tn[8];
-        uint32_t base, pbase, m0, m1;
-        uint32_t mask = test_node<kQuant>(B.nodes, e.x, R, h.t, tn, &base, &pbase, &m0, &m1);
-        if (!mask) continue;
-        uint32_t key[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-            key[q] = (mask >> q) & 1u ? ((__float_as_uint(fmaxf(tn[q], 0.0f)) & ~7u) | uint32_t(q)) : 0xffffffffu;
-        // 19-comparator sorting network for 8 keys (ascending)
-        cswap(key[0], key[2]); cswap(key[1], key[3]); cswap(key[4], key[6]); cswap(key[5], key[7]);
-        cswap(key[0], key[4]); cswap(key[1], key[5]); cswap(key[2], key[6]); cswap(key[3], key[7]);
-        cswap(key[0], key[1]); cswap(key[2], key[3]); cswap(key[4], key[5]); cswap(key[6], key[7]);
-        cswap(key[2], key[4]); cswap(key[3], key[5]);
-        cswap(key[1], key[4]); cswap(key[3], key[6]);
-        cswap(key[1], key[2]); cswap(key[3], key[4]); cswap(key[5], key[6]);
-        int npush = __popc(mask);
-        if (sp + npush > kStackSize) { err |= kErrStackOverflow; break; }
-#pragma unroll
-        for (int k = 7; k >= 0; --k) {
-            if (k >= npush) continue;
-            uint32_t q = key[k] & 7u;
-            uint32_t m = ((q < 4 ? m0 : m1) >> (8 * (q & 3))) & 0xffu;
-            if (m == 0) continue;  // an empty slot (only a degenerate ray can pass its empty box)
-            uint32_t ref = (m & 0x80u) ? base + (m & 7u)
-                                       : (kLeafFlag | ((pbase + (m & 31u)) << 2) | ((m >> 5) - 1u));
-            stack[sp++] = make_uint2(ref, key[k] & ~7u);
-        }
-    }
-    return found;
-}
-
-// World-space ray through every instance of a scene.
-template <bool kQuant>
-__device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> wo, V3<float> wd, float tmin, float tmax,
-                            Hit& h, bool any_hit, uint32_t skip_inst, uint32_t skip_slot, bool fp64_resolve, Stats& st,
-                            uint32_t& err) {
-    h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
-    bool found = false;
-    for (uint32_t i = 0; i < ninst; ++i) {
-        const DevInstance& I = insts[i];
-        RayState R;
-        if (I.identity) { R.o = wo; R.d = wd; }
-        else {
-            const float* m = I.w2o;
-            R.o = xform_point(m, wo);
-            R.d = xform_dir(m, wd);
-        }
-        R.inv = safe_inv(R.d);
-        R.tmin = tmin;
-        // instance bounds (object space) against the current closest distance
-        {
-            const DevBlas& B = I.b;
-            float x0 = (B.lo[0] - R.o.x) * R.inv.x, x1 = (B.hi[0] - R.o.x) * R.inv.x;
-            float y0 = (B.lo[1] - R.o.y) * R.inv.y, y1 = (B.hi[1] - R.o.y) * R.inv.y;
-            float z0 = (B.lo[2] - R.o.z) * R.inv.z, z1 = (B.hi[2] - R.o.z) * R.inv.z;
-            float a = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
-            float b = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), h.t));
-            if (!(a <= b * (1.0f + 9.5367431640625e-07f))) continue;
-        }
-        if (I.b.type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
-        else if (I.b.type == HRT_BLAS_DOTS) R.tr = make_triray(R.d);
-        if (traverse<kQuant>(I.b, i, R, h, any_hit, skip_inst, skip_slot, fp64_resolve, st, err)) {
-            found = true;
-            if (any_hit) return true;
-        }
-    }
-    return found;
-}
-
-// Object-space normal of the final hit (closest-hit stage).
-__device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo, V3<float> wd) {
-    const DevBlas& B = I.b;
-    V3<float> o = wo, d = wd;
-    if (!I.identity) {
-        const float* m = I.w2o;
-        o = xform_point(m, wo);
-        d = xform_dir(m, wd);
-    }
-    // Normals are differences of points a hair radius apart; they are formed from the
-    // full-precision vectors relative to the primitive's reference point o' = o + ts d.
-    V3<float> n;
-    if (B.type == HRT_BLAS_PHANTOM) {
-        // hair_intersection.rint:74-76: normalize(hit - curve(t))
-        V3<float> P[4];
-        float r0, r1;
-        uint32_t id;
-        load_phantom(B, h.slot, P, &r0, &r1, &id);
-        float ts = h.ts;
-        V3<float> W[4];
-        for (int k = 0; k < 4; ++k)
-            W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
-        // the curve point in Bernstein form with fixed fused operations
-        const float u = h.u, v = __fsub_rn(1.0f, u);
-        const float b0 = __fmul_rn(__fmul_rn(v, v), v), b1 = __fmul_rn(__fmul_rn(3.0f, __fmul_rn(v, v)), u);
-        const float b2 = __fmul_rn(__fmul_rn(3.0f, v), __fmul_rn(u, u)), b3 = __fmul_rn(__fmul_rn(u, u), u);
-        V3<float> c;
-        c.x = fmaf(b3, W[3].x, fmaf(b2, W[2].x, fmaf(b1, W[1].x, __fmul_rn(b0, W[0].x))));
-        c.y = fmaf(b3, W[3].y, fmaf(b2, W[2].y, fmaf(b1, W[1].y, __fmul_rn(b0, W[0].y))));
-        c.z = fmaf(b3, W[3].z, fmaf(b2, W[2].z, fmaf(b1, W[1].z, __fmul_rn(b0, W[0].z))));
-        n = normalize_rn(mk(fmaf(h.sl, d.x, -c.x), fmaf(h.sl, d.y, -c.y), fmaf(h.sl, d.z, -c.z)));
-    } else if (B.type == HRT_BLAS_LSS) {
-        // triangle_closest_hit.rchit:43-58: hit - mix(p0, p1, u)
-        const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + h.slot;
-        float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
-        V3<float> p0 = mk(a.x, a.y, a.z), p1 = mk(b.x, b.y, b.z);
-        float ts = h.ts;
-        V3<float> w0 = mk(rel_coord(p0.x, o.x, ts, d.x), rel_coord(p0.y, o.y, ts, d.y), rel_coord(p0.z, o.z, ts, d.z));
-        const V3<float> ax = mk(__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z));
-        n = normalize_rn(mk(fmaf(-h.u, ax.x, fmaf(h.sl, d.x, -w0.x)), fmaf(-h.u, ax.y, fmaf(h.sl, d.y, -w0.y)),
-                            fmaf(-h.u, ax.z, fmaf(h.sl, d.z, -w0.z))));
-    } else {
-        // DOTS vertices carry no normals (geometry_processor.cpp:259-264): the face normal
-        const PrimDots* pr = static_cast<const PrimDots*>(B.prims) + h.slot;
-        float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c), dd = __ldg(&pr->d), e = __ldg(&pr->e);
-        V3<float> s0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y);
-        uint32_t k = h.id & 3u, face = k >> 1;
-        V3<float> va = face ? mk(c.y, c.z, c.w) : mk(b.z, b.w, c.x);
-        V3<float> vb = face ? mk(dd.w, e.x, e.y) : mk(dd.x, dd.y, dd.z);
-        V3<float> A0 = s0 + va, A1 = e0 - vb;
-        V3<float> third = (k & 1u) ? (s0 - va) : (e0 + vb);
-        V3<float> v1 = (k & 1u) ? third : A1, v2 = (k & 1u) ? A1 : third;
-        n = normalize_rn(cross_rn(v1 - A0, v2 - A0));
-    }
-    if (!I.identity) {
-        const float* q = I.nrm;
-        n = normalize_rn(mk(fmaf(q[2], n.z, fmaf(q[1], n.y, __fmul_rn(q[0], n.x))),
-                            fmaf(q[5], n.z, fmaf(q[4], n.y, __fmul_rn(q[3], n.x))),
-                            fmaf(q[8], n.z, fmaf(q[7], n.y, __fmul_rn(q[6], n.x)))));
-    }
-    return n;
-}
-
-// ray_gen.rgen:18-24, every operation rounded separately (matches the CPU restatement).
-__device__ void raygen(const float* V, const float* P, uint32_t px, uint32_t py, uint32_t w, uint32_t hgt, float jx,
-                       float jy, V3<float>* o, V3<float>* d) {
-    float cx = __fadd_rn(float(px), jx), cy = __fadd_rn(float(py), jy);
-    float ux = __fdiv_rn(cx, float(w)), uy = __fdiv_rn(cy, float(hgt));
-    float dx = __fsub_rn(__fmul_rn(ux, 2.0f), 1.0f), dy = __fsub_rn(__fmul_rn(uy, 2.0f), 1.0f);
-    float org[3], tgt[3], dir[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        org[k] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(V[k], 0.0f), __fmul_rn(V[4 + k], 0.0f)), __fmul_rn(V[8 + k], 0.0f)),
-                           __fmul_rn(V[12 + k], 1.0f));
-        tgt[k] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(P[k], dx), __fmul_rn(P[4 + k], dy)), __fmul_rn(P[8 + k], 1.0f)),
-                           __fmul_rn(P[12 + k], 1.0f));
-    }
-    float dd = __fadd_rn(__fadd_rn(__fmul_rn(tgt[0], tgt[0]), __fmul_rn(tgt[1], tgt[1])), __fmul_rn(tgt[2], tgt[2]));
-    float inv = __fdiv_rn(1.0f, __fsqrt_rn(dd));
-    float n[3] = {__fmul_rn(tgt[0], inv), __fmul_rn(tgt[1], inv), __fmul_rn(tgt[2], inv)};
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        dir[k] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(V[k], n[0]), __fmul_rn(V[4 + k], n[1])), __fmul_rn(V[8 + k], n[2])),
-                           __fmul_rn(V[12 + k], 0.0f));
-    *o = mk(org[0], org[1], org[2]);
-    *d = mk(dir[0], dir[1], dir[2]);
-}
-
-__device__ __forceinline__ uint32_t hash_u32(uint32_t x) {
-    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
-    return x;
-}
-
-__constant__ float kPalette[6][3] = {{1.0f, 0.0f, 0.3f}, {0.8f, 0.2f, 0.3f}, {0.6f, 0.4f, 0.3f},
-                                     {0.4f, 0.6f, 0.3f}, {0.2f, 0.8f, 0.3f}, {0.0f, 1.0f, 0.3f}};
-
-__device__ __forceinline__ void warp_add(unsigned long long* ctr, uint32_t v) {
-    // one atomic per warp
-    uint32_t s = v;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
-    if ((threadIdx.x & 31) == 0 && s) atomicAdd(ctr, (unsigned long long)s);
-}
-
-// ---------------------------------------------------------------- the frame kernel
-// Persistent while-while traversal (Aila and Laine, HPG 2009): every lane owns a ray task (a
-// pixel: its samples, each a primary ray and, when shading with shadows, one shadow ray).
-//   refill     lanes without a task take pixels with one warp-aggregated atomic once enough
-//              lanes are idle (ballot + popc ranks), so finished rays do not idle the warp;
-//   node phase lanes test the next child of their node group together until each holds
-//              leaf children or runs dry;
-//   leaf phase lanes with leaf children test one each (the Phantom solve is long, so keeping
-//              it out of the node loop keeps the warp converged);
-//   completion a finished ray moves to the next instance, spawns its shadow ray, shades, or
-//              finishes the pixel.
-// The stack's bottom kShort entries live in shared memory (one column per thread), deeper
-// ones in local memory. Results do not depend on scheduling: one lane handles all samples of a
-// pixel in order and each ray's closest hit is the least (t, instance, id).
-constexpr int kShort = 16;
-constexpr int kRefill = 16;
-
-// kPass 1: the frame (non-converged Phantom candidates flag their pixel); kPass 2: the listed
-// pixels again, with the FP64 re-solve inline (adds only the FP64 counts).
-template <bool kQuant, int kType, int kMinBlocks, int kPass>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch L) {
-    __shared__ uint2 s_stack[kShort][kThreads];
-    uint2 l_stack[kStackSize - kShort];
-    const int tid = threadIdx.x, lane = tid & 31;
-    const uint32_t lt_mask = (1u << lane) - 1u;
-    const volatile uint32_t* errword = &L.counters->error;
-    Stats st{0, 0, 0, 0, 0};
-    uint32_t shadow_rays = 0, err = 0;
-
-    bool has_ray = false, fetch_done = false, per_sample = false;
-    uint32_t si = 0, px = 0, py = 0, sample = 0, g_cur = 0;
-    uint64_t item = 0;  // FP64 pass, one sample per lane: the scratch index of the sample
-    uint64_t pix = 0;
-    bool shadow = false, shadow_hit = false;
-    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, ndl = 0.0f;
-    uint32_t prim_flags = 0;
-    V3<float> wo = mk(0.0f, 0.0f, 0.0f), wd = mk(0.0f, 0.0f, 1.0f);
-    float cur_tmin = 0.0f;
-    RayState R;
-    Hit h{0.0f, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
-    uint32_t inst_cur = 0, skip_inst = 0xffffffffu, skip_slot = 0xffffffffu;
-    int sp = 0;
-    uint32_t steps = 0;
-    const void* nodes = nullptr;                 // node array of the current instance's BLAS
-    uint32_t oct = 0;                            // direction octant of the object-space ray
-    uint32_t cur_base = 0, cur_bits = 0;         // node group: hits in visiting order (bits 0-7), imask (8-15)
-    uint32_t leaf_node = 0, leaf_bits = 0;       // untested leaf children of node leaf_node, visiting order
-
-    auto push = [&](uint2 e) {
-        if (sp < kShort) s_stack[sp][tid] = e;
-        else l_stack[sp - kShort] = e;
-        ++sp;
-    };
-    auto pop = [&]() -> uint2 {
-        --sp;
-        return sp < kShort ? s_stack[sp][tid] : l_stack[sp - kShort];
-    };
-    // Object-space ray for instance i; pushes its root when the instance box is hit.
-    auto setup_instance = [&](uint32_t i) -> bool {
-        const DevInstance& I = L.scenes[si].inst[i];
-        if (I.identity) { R.o = wo; R.d = wd; }
-        else {
-            const float* m = I.w2o;
-            R.o = xform_point(m, wo);
-            R.d = xform_dir(m, wd);
-        }
-        R.inv = safe_inv(R.d);
-        R.tmin = cur_tmin;
-        const DevBlas& B = I.b;
-        if (B.nnodes == 0) return false;
-        float x0 = (B.lo[0] - R.o.x) * R.inv.x, x1 = (B.hi[0] - R.o.x) * R.inv.x;
-        float y0 = (B.lo[1] - R.o.y) * R.inv.y, y1 = (B.hi[1] - R.o.y) * R.inv.y;
-        float z0 = (B.lo[2] - R.o.z) * R.inv.z, z1 = (B.hi[2] - R.o.z) * R.inv.z;
-        float a = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), cur_tmin));
-        float b = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), h.t));
-        if (!(a <= b * (1.0f + 9.5367431640625e-07f))) return false;
-        const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
-        if (type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
-        else if (type == HRT_BLAS_DOTS) R.tr = make_triray(R.d);
-        nodes = B.nodes;
-        oct = (R.inv.x < 0.0f ? 1u : 0u) | (R.inv.y < 0.0f ? 2u : 0u) | (R.inv.z < 0.0f ? 4u : 0u);
-        cur_base = 0;  // the root as a group of one internal child in slot 0
-        cur_bits = (1u << oct) | (1u << 8);
-        return true;
-    };
-    auto start_ray = [&](V3<float> o, V3<float> d, float tmin, float tmax) {
-        wo = o;
-        wd = d;
-        cur_tmin = tmin;
-        h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
-        sp = 0;
-        cur_bits = 0;
-        leaf_bits = 0;
-        steps = 0;
-        const uint32_t n = L.scenes[si].ninst;
-        for (inst_cur = 0; inst_cur < n; ++inst_cur)
-            if (setup_instance(inst_cur)) break;
-    };
-    auto start_primary = [&]() {
-        const SceneLaunch& S = L.scenes[si];
-        float jx = 0.5f, jy = 0.5f;
-        if (L.jitter || S.spp > 1) {
-            uint32_t h1 = hash_u32(L.seed ^ hash_u32(uint32_t(pix) * S.spp + sample));
-            uint32_t h2 = hash_u32(h1);
-            jx = float(h1 >> 8) * 5.9604644775390625e-08f;
-            jy = float(h2 >> 8) * 5.9604644775390625e-08f;
-        }
-        V3<float> o, d;
-        raygen(S.view_inv, S.proj_inv, px, py, S.width, S.height, jx, jy, &o, &d);
-        shadow = false;
-        start_ray(o, d, L.tmin, L.tmax);
-    };
-    auto next_sample = [&]() {
-        const SceneLaunch& S = L.scenes[si];
-        ++sample;
-        if (kPass == 2 && per_sample) {  // this sample's colour; a later launch averages
-            L.resolve_scratch[item] = make_float4(acc0, acc1, acc2, 0.0f);
-            has_ray = false;
-            return;
-        }
-        if (sample < S.spp) { start_primary(); return; }
-        float inv = 1.0f / float(S.spp);
-        S.fb[pix] = make_float4(__fmul_rn(acc0, inv), __fmul_rn(acc1, inv), __fmul_rn(acc2, inv), 1.0f);
-        has_ray = false;
-        if (kPass == 1 && st.need64) {  // list the pixel for the FP64 pass
-            st.need64 = 0;
-            unsigned long long k = atomicAdd(&L.counters->resolve_n, 1ull);
-            if (k < L.resolve_cap) L.resolve_list[k] = g_cur;
-        }
-    };
-    auto finish_phase = [&]() {
-        const SceneLaunch& S = L.scenes[si];
-        uint64_t rec = pix * S.spp + sample;
-        if (!shadow) {
-            bool found = h.id != 0xffffffffu;
-            prim_flags = h.flags;
-            if (L.record_hits && S.hits) {
-                hrt_hit r;
-                r.t = found ? h.t : -1.0f;
-                r.prim = h.id;
-                r.inst = h.inst;
-                r.flags = found ? h.flags : 0u;
-                S.hits[rec] = r;
-            }
-            if (!found) { next_sample(); return; }
-            if (L.shading == HRT_SHADE_DEBUG) {
-                uint32_t c = h.id % 6u;
-                acc0 = __fadd_rn(acc0, kPalette[c][0]);
-                acc1 = __fadd_rn(acc1, kPalette[c][1]);
-                acc2 = __fadd_rn(acc2, kPalette[c][2]);
-                next_sample();
-                return;
-            }
-            V3<float> n = hit_normal(S.inst[h.inst], h, wo, wd);
-            ndl = fabsf(n.y);  // shading.glsl: |dot(n, (0,-1,0))|
-            if (L.shading == HRT_SHADE_LAMBERT_SHADOW) {
-                skip_inst = h.inst;
-                skip_slot = h.slot;
-                shadow_hit = false;
-                shadow = true;
-                ++shadow_rays;
-                V3<float> hp = mk(fmaf(h.t, wd.x, wo.x), fmaf(h.t, wd.y, wo.y), fmaf(h.t, wd.z, wo.z));
-                start_ray(hp, mk(0.0f, 1.0f, 0.0f), L.shadow_tmin, L.tmax);
-                return;
-            }
-            acc0 = __fadd_rn(acc0, fmaf(ndl, 0.4f, 0.3f));
-            acc1 = __fadd_rn(acc1, fmaf(ndl, 0.2f, 0.3f));
-            acc2 = __fadd_rn(acc2, fmaf(ndl, 0.1f, 0.3f));
-            next_sample();
-            return;
-        }
-        float lit = shadow_hit ? 0.0f : ndl;
-        acc0 = __fadd_rn(acc0, fmaf(lit, 0.4f, 0.3f));
-        acc1 = __fadd_rn(acc1, fmaf(lit, 0.2f, 0.3f));
-        acc2 = __fadd_rn(acc2, fmaf(lit, 0.1f, 0.3f));
-        if (shadow_hit && L.record_hits && S.hits) S.hits[rec].flags = prim_flags | HRT_HIT_SHADOWED;
-        shadow = false;
-        next_sample();
-    };
-
-    const int refill = L.refill ? int(L.refill) : kRefill;  // idle lanes that trigger a fetch
-    const bool spec = L.speculative != 0;
-    // work items: pass 1 every item; pass 2 the samples of the listed pixels, or the listed
-    // pixels when their samples do not fit the scratch, or every item if the list overflowed
-    unsigned long long* const work_ctr = kPass == 1 ? &L.counters->work : &L.counters->work2;
-    uint64_t total = L.total_work;
-    bool use_list = false;
-    if (kPass == 2) {
-        const unsigned long long nl = __ldcg(&L.counters->resolve_n);
-        if (nl <= L.resolve_cap) { total = nl; use_list = true; }
-        if (use_list && nl * L.max_spp <= L.scratch_cap) { total = nl * L.max_spp; per_sample = true; }
-    }
-    unsigned long long cyc_node = 0, cyc_leaf = 0, cyc_other = 0;
-    long long clk = clock64();
-    for (;;) {
-        // ---- refill idle lanes
-        uint32_t idle = __ballot_sync(kFull, !has_ray);
-        if (idle && !fetch_done && (__popc(idle) >= refill || idle == kFull)) {
-            int n = __popc(idle), leader = __ffs(idle) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = *errword ? total : atomicAdd(work_ctr, (unsigned long long)n);
-            base = __shfl_sync(kFull, base, leader);
-            if (base + uint64_t(n) >= total) fetch_done = true;
-            if (!has_ray) {
-                uint64_t g = base + __popc(idle & lt_mask);
-                if (g < total) {
-                    uint32_t s0 = 0;
-                    if (per_sample) {
-                        item = g;
-                        s0 = uint32_t(g % L.max_spp);
-                        g = g / L.max_spp;
-                    }
-                    if (use_list) g = __ldcg(&L.resolve_list[g]);
-                    g_cur = uint32_t(g);
-                    si = 0;
-                    while (si + 1 < L.nscenes && L.scenes[si + 1].work_begin <= g) ++si;
-                    const SceneLaunch& S = L.scenes[si];
-                    uint64_t local = g - S.work_begin, tile = local >> 5;
-                    uint32_t within = uint32_t(local & 31u);
-                    px = uint32_t(tile % S.tiles_x) * 8u + (within & 7u);
-                    py = uint32_t(tile / S.tiles_x) * 4u + (within >> 3);
-                    if (px < S.width && py < S.height && s0 < S.spp) {
-                        pix = uint64_t(py) * S.width + px;
-                        has_ray = true;
-                        sample = s0;
-                        acc0 = acc1 = acc2 = 0.0f;
-                        start_primary();
-                    }
-                }
-            }
-        }
-        if (!__any_sync(kFull, has_ray)) {
-            if (fetch_done) break;
-            continue;
-        }
-        if (L.count_stats) { long long c = clock64(); cyc_other += c - clk; clk = c; }
-        // ---- node phase: runs while some lane still searches for a leaf; with speculation,
-        // lanes that already hold leaves keep walking nodes (further leaves go on the stack).
-        // A lane visits the children of its current node group in the order i ^ oct (slots are
-        // laid out by direction, so roughly near to far); a visited node's internal hits become
-        // the new group (the rest of the old one goes on the stack) and its leaf hits become
-        // the lane's pending leaves.
-        bool stalled = false;
-        for (;;) {
-            const bool more = (cur_bits & 0xffu) != 0u || sp > 0;
-            const bool searching = has_ray && !leaf_bits && more;
-            if (!__any_sync(kFull, searching)) break;
-            const bool want = searching || (spec && has_ray && leaf_bits && !stalled && more);
-            if (!want) continue;
-            if (++steps > kMaxTraversalSteps) {
-                err |= kErrTimeout;
-                sp = 0;
-                cur_bits = leaf_bits = 0;
-                continue;
-            }
-            if (!(cur_bits & 0xffu)) {
-                const uint2 e = pop();
-                if (e.x & kLeafFlag) {  // leaves parked by a speculating lane (no distances kept)
-                    if (leaf_bits) {
-                        push(e);
-                        stalled = true;
-                    } else {
-                        leaf_node = e.x & ~kLeafFlag;
-                        leaf_bits = oct_permute(e.y, oct);
-                    }
-                    continue;
-                }
-                cur_base = e.x;
-                cur_bits = e.y;
-            }
-            const uint32_t i = __ffs(cur_bits & 0xffu) - 1;
-            cur_bits &= ~(1u << i);
-            const uint32_t slot = i ^ oct;
-            const uint32_t child = cur_base + __popc((cur_bits >> 8) & ((1u << slot) - 1u));
-            ++st.nodes;
-            uint32_t base, imask;
-            const uint32_t mask = test_node<kQuant, false>(nodes, child, R, h.t, nullptr, &base, nullptr, nullptr,
-                                                           nullptr, &imask);
-            const uint32_t ih = mask & imask, lh = mask & ~imask;
-            if (sp + 2 > kStackSize) {
-                err |= kErrStackOverflow;
-                sp = 0;
-                cur_bits = leaf_bits = 0;
-                continue;
-            }
-            if (lh) {
-                if (!leaf_bits) {
-                    leaf_node = child;
-                    leaf_bits = oct_permute(lh, oct);
-                } else {
-                    push(make_uint2(kLeafFlag | child, lh));
-                    stalled = true;
-                }
-            }
-            if (ih) {
-                if (cur_bits & 0xffu) push(make_uint2(cur_base, cur_bits));
-                cur_base = base;
-                cur_bits = oct_permute(ih, oct) | (imask << 8);
-            }
-        }
-        if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_node += c - clk; clk = c; }
-        // ---- leaf phase: one leaf child per lane, in visiting order
-        if (leaf_bits) {
-            const DevBlas& B = L.scenes[si].inst[inst_cur].b;
-            const uint32_t q = (__ffs(leaf_bits) - 1) ^ oct;
-            leaf_bits &= leaf_bits - 1u;
-            const uint4 hd = node_header<kQuant>(nodes, leaf_node);
-            const uint32_t m = ((q < 4 ? hd.z : hd.w) >> (8 * (q & 3))) & 0xffu;
-            const uint32_t first = hd.y + (m & 31u), cnt = m >> 5;
-            for (uint32_t j = 0; j < cnt; ++j) {
-                uint32_t slot = first + j;
-                if (shadow && inst_cur == skip_inst && slot == skip_slot) continue;
-                ++st.prims;
-                if (leaf_test<kType, kPass == 1>(B, slot, inst_cur, R, h, L.fp64_resolve != 0, st) && shadow) {
-                    shadow_hit = true;
-                    sp = 0;
-                    cur_bits = leaf_bits = 0;
-                    break;
-                }
-            }
-        }
-        if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_leaf += c - clk; clk = c; }
-        // ---- completion
-        if (has_ray && !leaf_bits && sp == 0 && !(cur_bits & 0xffu)) {
-            if (err) {  // a bounded loop gave up: drop the task and stop taking work
-                atomicOr(&L.counters->error, err);
-                has_ray = false;
-                fetch_done = true;
-                continue;
-            }
-            bool more = false;
-            if (!(shadow && shadow_hit)) {
-                const uint32_t n = L.scenes[si].ninst;
-                while (++inst_cur < n)
-                    if (setup_instance(inst_cur)) { more = true; break; }
-            }
-            if (!more) finish_phase();
-        }
-    }
-    if (kPass == 1) warp_add(&L.counters->shadow, shadow_rays);
-    if (kPass == 1 && L.count_stats) {
-        warp_add(&L.counters->nodes, st.nodes);
-        warp_add(&L.counters->prims, st.prims);
-        cyc_other += clock64() - clk;
-        if (lane == 0) {  // warp-level phase clocks
-            atomicAdd(&L.counters->cycles_node, cyc_node);
-            atomicAdd(&L.counters->cycles_leaf, cyc_leaf);
-            atomicAdd(&L.counters->cycles_other, cyc_other);
-        }
-    }
-    warp_add(&L.counters->fp64_resolves, st.r64);
-    warp_add(&L.counters->fp64_hits, st.h64);
-    if (err) atomicOr(&L.counters->error, err);
-}
-
-template <bool kQuant>
-__global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance* inst, uint32_t ninst, const float* rays,
-                                                              uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
-                                                              hrt_hit* hits, TraceCounters* ctr) {
-    Stats st{0, 0, 0, 0, 0};
-    uint32_t err = 0;
-    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
-        const float* r = rays + 6 * i;
-        Hit h;
-        bool f = trace_scene<kQuant>(inst, ninst, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), tmin, tmax, h, false, 0, 0,
-                                     fp64_resolve != 0, st, err);
-        hrt_hit o;
-        o.t = f ? h.t : -1.0f;
-        o.prim = f ? h.id : 0xffffffffu;
-        o.inst = f ? h.inst : 0xffffffffu;
-        o.flags = f ? h.flags : 0u;
-        hits[i] = o;
-    }
-    warp_add(&ctr->fp64_resolves, st.r64);
-    warp_add(&ctr->fp64_hits, st.h64);
-    if (err) atomicOr(&ctr->error, err);
-}
-
-template <bool kQuant, int kType, int kMinBlocks, int kPass>
-cudaError_t launch_frame(const TraceLaunch& L, cudaStream_t s, int sm_count) {
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, frame_kernel<kQuant, kType, kMinBlocks, kPass>, kThreads, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    unsigned grid = unsigned(sm_count * per_sm);
-    uint64_t max_blocks = (L.total_work + kThreads - 1) / kThreads;
-    if (grid > max_blocks) grid = unsigned(max_blocks ? max_blocks : 1);
-    frame_kernel<kQuant, kType, kMinBlocks, kPass><<<grid, kThreads, 0, s>>>(L);
-    return cudaGetLastError();
-}
-
-template <bool kQuant, int kMinBlocks>
-cudaError_t launch_kind(const TraceLaunch& L, cudaStream_t s, int sm_count) {
-    switch (L.prim_kind) {  // one primitive type in every instance -> the specialised kernel
-        case HRT_BLAS_PHANTOM: return launch_frame<kQuant, HRT_BLAS_PHANTOM, kMinBlocks, 1>(L, s, sm_count);
-        case HRT_BLAS_LSS: return launch_frame<kQuant, HRT_BLAS_LSS, kMinBlocks, 1>(L, s, sm_count);
-        case HRT_BLAS_DOTS: return launch_frame<kQuant, HRT_BLAS_DOTS, kMinBlocks, 1>(L, s, sm_count);
-        default: return launch_frame<kQuant, kMixed, kMinBlocks, 1>(L, s, sm_count);
-    }
-}
-
-// After a per-sample FP64 pass: each listed pixel's colour is the mean of its samples' colours,
-// summed in sample order from zero (the frame pass's own accumulation, bit for bit).
-__global__ void __launch_bounds__(kThreads) resolve_average_kernel(TraceLaunch L) {
-    const unsigned long long nl = __ldcg(&L.counters->resolve_n);
-    if (nl > L.resolve_cap || nl * L.max_spp > L.scratch_cap) return;  // the pass ran per pixel
-    for (uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < nl; k += uint64_t(gridDim.x) * blockDim.x) {
-        const uint32_t g = __ldcg(&L.resolve_list[k]);
-        uint32_t si = 0;
-        while (si + 1 < L.nscenes && L.scenes[si + 1].work_begin <= g) ++si;
-        const SceneLaunch& S = L.scenes[si];
-        const uint64_t local = g - S.work_begin, tile = local >> 5;
-        const uint32_t within = uint32_t(local & 31u);
-        const uint32_t px = uint32_t(tile % S.tiles_x) * 8u + (within & 7u);
-        const uint32_t py = uint32_t(tile / S.tiles_x) * 4u + (within >> 3);
-        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-        for (uint32_t s2 = 0; s2 < S.spp; ++s2) {
-            const float4 c = __ldcg(&L.resolve_scratch[k * L.max_spp + s2]);
-            a0 = __fadd_rn(a0, c.x);
-            a1 = __fadd_rn(a1, c.y);
-            a2 = __fadd_rn(a2, c.z);
-        }
-        const float inv = 1.0f / float(S.spp);
-        S.fb[uint64_t(py) * S.width + px] = make_float4(__fmul_rn(a0, inv), __fmul_rn(a1, inv), __fmul_rn(a2, inv), 1.0f);
-    }
-}
-
-// The FP64 pass: only launches that hold Phantom BLASes can list pixels.
-template <bool kQuant>
-cudaError_t launch_resolve(const TraceLaunch& L, cudaStream_t s, int sm_count) {
-    if (!L.fp64_resolve || !L.resolve_list) return cudaSuccess;
-    cudaError_t e = cudaSuccess;
-    if (L.prim_kind == HRT_BLAS_PHANTOM) e = launch_frame<kQuant, HRT_BLAS_PHANTOM, 1, 2>(L, s, sm_count);
-    else if (L.prim_kind == kMixed) e = launch_frame<kQuant, kMixed, 1, 2>(L, s, sm_count);
-    else return cudaSuccess;
-    if (e != cudaSuccess || !L.resolve_scratch) return e;
-    resolve_average_kernel<<<unsigned(sm_count), kThreads, 0, s>>>(L);
-    return cudaGetLastError();
-}
-
-}  // namespace
-
-// variant: 0 default (4 resident blocks per SM), 1 = 4, 2 = 3 (more registers per thread).
-// Launches the frame pass and, when Phantom candidates may need it, the FP64 pass.
 cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count) {
-    bool three = L.variant == 2;
-    cudaError_t e;
-    if (quantised_nodes) e = three ? launch_kind<true, 3>(L, s, sm_count) : launch_kind<true, 4>(L, s, sm_count);
-    else e = three ? launch_kind<false, 3>(L, s, sm_count) : launch_kind<false, 4>(L, s, sm_count);
-    if (e != cudaSuccess) return e;
-    return quantised_nodes ? launch_resolve<true>(L, s, sm_count) : launch_resolve<false>(L, s, sm_count);
+    return quantised_nodes ? launch_frames_q(L, s, sm_count) : launch_frames_f(L, s, sm_count);
 }
 
 cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n, float tmin,
