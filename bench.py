@@ -493,7 +493,7 @@ def run_batched(args, dist):
                           "image": f"{m['width']}x{m['height']}", "spp": m["spp"], "rays": int(rays)})
     # ---- autotune the batch (untimed) ----
     scenes_q = [(t, cam, fr) for (_, t, cam, fr) in q]
-    tuned, tune_ms = H.autotune(ctx, scenes_q, base, reps=2)
+    tuned, tune_ms = H.autotune(ctx, scenes_q, base, reps=2, cache=args.tune_cache, key=f"{BATCH_CONFIG}/quantised")
     batch = H.Batch(ctx, scenes_q, tuned)
     dist.barrier()
     clocks = Clocks(dev)
@@ -539,6 +539,21 @@ def run_batched(args, dist):
     plain_params = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1})
     ms_f32, lat_f32 = sequential(f, plain_params)
     ms_q, lat_q = sequential(q, tuned)
+    # the batching pattern on FP32 BLASes too, so that precision and batching can be told apart
+    scenes_f = [(t, cam, fr) for (_, t, cam, fr) in f]
+    tuned_f, _ = H.autotune(ctx, scenes_f, base, reps=2, cache=args.tune_cache, key=f"{BATCH_CONFIG}/fp32")
+    batch_f = H.Batch(ctx, scenes_f, tuned_f)
+    for _ in range(args.warmup):
+        batch_f.launch()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        batch_f.launch()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_bf = e0.elapsed_time(e1) / args.steps
+    mem_q = sum(int(b.info["device_bytes"]) for (b, *_r) in q)
+    mem_f = sum(int(b.info["device_bytes"]) for (b, *_r) in f)
     if dist.rank != 0:
         dist.close()
         return
@@ -583,6 +598,11 @@ def run_batched(args, dist):
                                    "and records, no batching, no autotuning)"},
             "sequential_quantised": {"value": round(rays_per_step / (ms_q * 1e-3) / 1e6, 3),
                                      "ms_per_step": round(ms_q, 3), "launches_per_step": len(models)},
+            "batched_fp32": {"value": round(rays_per_step / (ms_bf * 1e-3) / 1e6, 3), "ms_per_step": round(ms_bf, 3),
+                             "autotuned": {k: int(getattr(tuned_f, k)) for k in H.TUNED_FIELDS},
+                             "note": "the batching pattern on FP32 BLASes: on these coherent, L2-resident "
+                                     "workloads the 8-bit node decode costs more ALU than the bytes it saves"},
+            "device_bytes": {"quantised": mem_q, "fp32": mem_f},
             "per_scene_latency_ms": {"batched_all_scenes": round(ms, 3),
                                      "note": "a batched scene completes with the launch; sequential latencies "
                                              "are per launch"},
@@ -594,7 +614,7 @@ def run_batched(args, dist):
             "build": {"build_wall_s_quantised": round(build_wall, 3), "strand_generation_s": round(t_gen, 3)}}
     if not args.no_cpu:
         line.update(batch_agreement_and_cpu(args, ctx, q, models))
-    del q, f, batch, sync_batch, scenes_q
+    del q, f, batch, sync_batch, scenes_q, scenes_f, batch_f
     if not args.quick:
         line["c4_phantom_quantised"] = c4_summary(args, ctx)
     print(json.dumps(line), flush=True)
@@ -708,6 +728,7 @@ def main():
     ap.add_argument("--max-leaf", type=int, default=1, help="primitives per BVH8 leaf (1..3)")
     ap.add_argument("--refill", type=int, default=8, help="idle lanes per warp that trigger a fetch (0 = 16)")
     ap.add_argument("--speculative", type=int, default=1, help="speculative traversal (0/1)")
+    ap.add_argument("--tune-cache", default=None, help="JSON file that keeps autotuner choices between runs")
     ap.add_argument("--profile", action="store_true",
                     help="one warm-up and the timed steps only: no e2e, FP32 comparison or CPU legs")
     args = ap.parse_args()

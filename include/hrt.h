@@ -107,7 +107,9 @@ typedef struct hrt_blas_info {
     float build_ms;         /* device time of the last build */
 } hrt_blas_info;
 
-/* Parts of a built BLAS copied to the host for inspection (bit-exact tests). */
+/* Parts of a built BLAS copied to the host for inspection (bit-exact tests). A BLAS keeps only
+ * what tracing reads (NODES, PRIMS, PRIM_ORDER, ROOTS); the other parts need
+ * HRT_BUILD_KEEP_INTERMEDIATE (otherwise hrt_blas_get returns HRT_ERR_UNSUPPORTED). */
 typedef enum hrt_blas_part {
     HRT_PART_PRIM_BOXES = 0,    /* float[n][6], primitive (segment) order */
     HRT_PART_MORTON_SORTED = 1, /* uint64[n] (needs HRT_BUILD_KEEP_INTERMEDIATE) */
@@ -121,7 +123,7 @@ typedef enum hrt_blas_part {
     HRT_PART_CURVES = 9,        /* float[n][12] Bezier control points (Phantom, FP32) */
     HRT_PART_DOTS_VERTICES = 10,/* float[n][36] (DOTS), the reference's 12 vertices/segment */
     HRT_PART_LSS = 11,          /* float[n][8]: p0 xyz, p1 xyz, r0, r1 */
-    HRT_PART_QNODES = 12,       /* raw quantised nodes (80 B each), also built for FP32 BLASes */
+    HRT_PART_QNODES = 12,       /* raw quantised nodes (80 B each); of an FP32 BLAS only when kept */
     HRT_PART_ROOTS = 13         /* float[nchunks][4] quantised Phantom roots */
 } hrt_blas_part;
 

@@ -174,3 +174,20 @@ def test_build_rejects_bad_input(ctx):
     with pytest.raises(H.HrtError):
         H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v, max_leaf=4,
                                                        strand_offsets=np.array([0, 4], np.uint32)), ctx)
+
+
+def test_blas_keeps_only_what_tracing_reads(ctx):
+    """Without HRT_BUILD_KEEP_INTERMEDIATE a BLAS holds nodes, records, roots and the slot map
+    only: the quantised Phantom BLAS is 80 B per node + 32 B per segment + 4 B per segment + 16 B
+    per root, and inspection parts are refused."""
+    v, r, off = H.generate_strands(H.StrandParams(seed=5, nstrands=300, nverts=32))
+    n = 300 * 31
+    # strands of 31 segments: one FP16 root per strand
+    for prec, node_b, prim_b, nroots in ((H.Precision.QUANTISED, 80, 32, 300), (H.Precision.FP32, 224, 64, 0)):
+        blas = H.BottomLevelAccelerationStructure(
+            H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r, strand_offsets=off, precision=prec), ctx)
+        info = blas.info
+        assert info["device_bytes"] == info["nnodes"] * node_b + n * prim_b + n * 4 + nroots * 16
+        with pytest.raises(H.HrtError) as e:
+            blas.get(H.Part.CURVES, np.float32, (n, 12))
+        assert e.value.status == 6 or "not kept" in str(e.value)

@@ -597,6 +597,7 @@ hrt_status hrt_blas_get(const hrt_blas* b, int32_t part, void* dst, uint64_t byt
             need = n * 144;
             if (bytes != need) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_get: part needs %llu bytes", (unsigned long long)need);
             if (!n) return HRT_OK;
+            if (!o.geom) return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_get: part %d was not kept by this build", part);
             float* tmp = nullptr;
             CK(ctx, cudaMalloc(&tmp, need), "allocate DOTS vertices");
             cudaError_t e = expand_dots(o.geom, n, tmp, nullptr);

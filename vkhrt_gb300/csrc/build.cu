@@ -990,6 +990,18 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     memcpy(out.bounds, hb, sizeof(hb));
     if (h_err) { snprintf(msg, msglen, "refit exceeded its depth bound"); return cudaErrorUnknown; }
 
+    if (!in.keep_intermediate) {
+        // tracing reads nodes, records, roots and the slot -> segment map; the rest of the
+        // build's outputs (the other node encoding, primitive boxes, FP32 curves, LSS/DOTS
+        // geometry) are kept only for inspection
+        void* extra[] = {out.qnodes_aux, out.prim_boxes, out.curves, out.geom};
+        for (void* p : extra)
+            if (p) cudaFreeAsync(p, s);
+        out.qnodes_aux = nullptr;
+        out.prim_boxes = nullptr;
+        out.curves = nullptr;
+        out.geom = nullptr;
+    }
     if (in.keep_intermediate) {
         out.morton_sorted = codes;
         out.sorted_index = order;
@@ -1009,9 +1021,11 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     for (void* p : tmps)
         if (p) cudaFreeAsync(p, s);
     HRT_CK(cudaStreamSynchronize(s));
-    out.device_bytes = n * 6 * 4 + (out.curves ? n * 48 : 0) +
-                       (out.geom ? n * (in.type == HRT_BLAS_LSS ? 32 : 72) : 0) + out.nnodes * (sizeof(NodeF) + sizeof(NodeQ)) +
-                       n * 4 + n * out.prim_bytes + out.nroots * 16;
+    out.device_bytes = out.nnodes * out.node_bytes + n * out.prim_bytes + out.nroots * 16 + n * 4;
+    if (in.keep_intermediate)
+        out.device_bytes += n * 24 + (out.curves ? n * 48 : 0) + (out.geom ? n * (in.type == HRT_BLAS_LSS ? 32 : 72) : 0) +
+                            out.nnodes * (in.precision == HRT_PRECISION_QUANTISED ? sizeof(NodeF) : sizeof(NodeQ)) +
+                            n * 8 + n * 4 + (n ? (n - 1) * 32 : 0);
     return cudaSuccess;
 }
 
