@@ -243,13 +243,15 @@ def run_reference_batched(args):
         data, rad = oracle_geometry(orc, int(m["type"]), lines, lrad, quantised=(int(m["type"]) == 0))
         cam = H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"])
         scenes.append((m, OracleScene(orc, [(int(m["type"]), data, rad)]), H.camera_arrays(cam)))
-    npx = 16384  # per scene and step: one oracle call has a few ms of thread start-up
+    # per step the same fraction of every scene's pixels (all their samples), so the rate is that
+    # of the whole workload; 1/8 of the workload per step
+    frac = 0.125
     total_t = 0.0
     total_rays = 0
     for step in range(args.warmup + args.steps):
         for m, osc, (vi, pi) in scenes:
             w, h, spp = m["width"], m["height"], m["spp"]
-            px = sample_pixels(w, h, npx, seed=1000 + step)
+            px = sample_pixels(w, h, int(w * h * frac), seed=1000 + step)
             t0 = time.perf_counter()
             o = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=px,
                            threads=threads)
@@ -258,7 +260,8 @@ def run_reference_batched(args):
                 total_t += dt
                 total_rays += len(px) * spp + int((o["t"] >= 0).sum())
     value = total_rays / total_t / 1e6
-    sample = f"{npx} random pixels (all their samples) of each of the {len(models)} scenes per step (+ shadow rays)"
+    sample = (f"{frac:g} of the pixels of each of the {len(models)} scenes (all their samples, + shadow rays) per "
+              f"step: the workload's mix")
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_t / max(args.steps, 1), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
@@ -659,6 +662,7 @@ def batch_agreement_and_cpu(args, ctx, q, models):
     cpu_rays = 0
     cpu_px = 0
     cpu_s = 0.0
+    cpu_frac = 0.25
     per = max(1, 65536 // len(models))
     for (b, t, cam, fr), (m, v, r, off) in zip(q, models):
         H.trace(ctx, t, cam, fr, H.trace_params(jitter=1, seed=17, shading=2, record_hits=1))
@@ -682,18 +686,13 @@ def batch_agreement_and_cpu(args, ctx, q, models):
         ok_px = same.reshape(-1, spp).all(axis=1)
         if ok_px.any():
             max_rgb = max(max_rgb, float(np.abs(rgba.reshape(-1, 4)[px] - o["fb"]).max(axis=1)[ok_px].max()))
-        # the oracle's FP32 tracer on a pixel sample grown until it takes about cpu_seconds / 16
-        # (one call has a few ms of thread start-up, so small samples would understate it)
-        npx = 4096
-        while True:
-            cpx = sample_pixels(w, h, npx, seed=11)
-            t0 = time.perf_counter()
-            oc = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=cpx,
-                            threads=threads)
-            dt = time.perf_counter() - t0
-            if dt >= args.cpu_seconds / len(models) or npx >= w * h:
-                break
-            npx = min(w * h, npx * 4)
+        # the oracle's FP32 tracer on the same fraction of every scene's pixels (the workload's mix;
+        # at least 16,384 pixels per call, since a call has a few ms of thread start-up)
+        cpx = sample_pixels(w, h, int(w * h * cpu_frac), seed=11)
+        t0 = time.perf_counter()
+        oc = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=cpx,
+                        threads=threads)
+        dt = time.perf_counter() - t0
         cpu_s += dt
         cpu_rays += len(cpx) * spp + int((oc["t"] >= 0).sum())
         cpu_px += len(cpx)
@@ -704,8 +703,8 @@ def batch_agreement_and_cpu(args, ctx, q, models):
                           "oracle": "FP64 CPU restatement on the same (dequantised) geometry, per scene"},
             "cpu_baseline": {"value": round(cpu_rays / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads,
                              "kind": "port",
-                             "sample": f"{cpu_px} random pixels over the {len(models)} scenes (all samples, "
-                                       f"{cpu_rays} rays), FP32 oracle, {cpu_s:.1f} s"}}
+                             "sample": f"{cpu_frac:g} of the pixels of every scene ({cpu_px} pixels, all their "
+                                       f"samples, {cpu_rays} rays), FP32 oracle, {cpu_s:.1f} s"}}
 
 
 def main():
