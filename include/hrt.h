@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HRT_ABI_VERSION 2
+#define HRT_ABI_VERSION 3
 
 typedef enum hrt_status {
     HRT_OK = 0,
@@ -58,7 +58,8 @@ typedef struct hrt_batch hrt_batch;
 typedef enum hrt_geometry_type {
     HRT_BLAS_PHANTOM = 0, /* cubic Bezier segments, Phantom ray-hair intersector */
     HRT_BLAS_LSS = 1,     /* linear swept spheres (round cones, both end caps) */
-    HRT_BLAS_DOTS = 2     /* disjoint orthogonal triangle strips, 4 triangles per segment */
+    HRT_BLAS_DOTS = 2,    /* disjoint orthogonal triangle strips, 4 triangles per segment */
+    HRT_BLAS_MESH = 3     /* indexed triangle mesh (BLASType::eMesh), optional per-vertex normals */
 } hrt_geometry_type;
 
 typedef enum hrt_precision {
@@ -93,6 +94,11 @@ typedef struct hrt_blas_input {
     float transform[16];            /* object to world, column major (glm::mat4) */
     uint32_t quant_chunk;           /* quantised Phantom: max segments per FP32 root (0 = 256) */
     uint32_t flags;                 /* HRT_BUILD_* */
+    /* HRT_BLAS_MESH (renderer.cpp:543-582): 3 vertex indices per triangle; triangle i reports
+     * primitive id i. strand_offsets and line_indices must be NULL. */
+    const uint32_t* tri_indices;
+    uint64_t ntris;
+    const float* normals;           /* 3 floats per vertex (interpolated at the hit), or NULL (face normal) */
 } hrt_blas_input;
 
 #define HRT_BUILD_KEEP_INTERMEDIATE 1u /* keep Morton codes, binary tree, boxes (hrt_blas_get) */

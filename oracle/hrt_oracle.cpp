@@ -318,7 +318,8 @@ T lss_intersect(tvec3<T> o_in, tvec3<T> d, tvec3<T> a, tvec3<T> b, T ra, T rb, T
 // Not in the reference's source: DOTS triangles are intersected by RT hardware with facing
 // culling disabled (top_level_acceleration_structure.cpp:28). Returns t or -1.
 template <class T>
-T tri_intersect(tvec3<T> o, tvec3<T> d, tvec3<T> v0, tvec3<T> v1, tvec3<T> v2, T tmin, T tmax) {
+T tri_intersect(tvec3<T> o, tvec3<T> d, tvec3<T> v0, tvec3<T> v1, tvec3<T> v2, T tmin, T tmax, T* b1 = nullptr,
+                T* b2 = nullptr) {
     int kz = 0;
     T ax = gabs(d.x), ay = gabs(d.y), az = gabs(d.z);
     if (ay > ax && ay >= az) kz = 1;
@@ -340,6 +341,7 @@ T tri_intersect(tvec3<T> o, tvec3<T> d, tvec3<T> v0, tvec3<T> v1, tvec3<T> v2, T
     T Tn = U * Az + V * Bz + W * Cz;
     T t = Tn / det;
     if (!(t >= tmin) || !(t <= tmax)) return T(-1);
+    if (b1) { *b1 = V / det; *b2 = W / det; }  // barycentric weights of v1 and v2
     return t;
 }
 
@@ -413,7 +415,8 @@ static inline float fmax_t(float a, float b) { return (a < b) ? b : a; }
 //   Phantom: control hull +- max(r0, r1)  (GenerateAABBs geometry_processor.cpp:431-432)
 //   LSS:     min/max of (p0 -+ r0, p1 -+ r1)
 //   DOTS:    min/max over the segment's 12 vertices, in vertex order
-enum { kPhantom = 0, kLss = 1, kDots = 2 };
+//   mesh:    min/max over the triangle's 3 vertices, in vertex order
+enum { kPhantom = 0, kLss = 1, kDots = 2, kMesh = 3 };
 static Box prim_box(int type, const float* data, const float* radius, int64_t i) {
     Box b;
     if (type == kPhantom) {
@@ -429,6 +432,12 @@ static Box prim_box(int type, const float* data, const float* radius, int64_t i)
         for (int k = 0; k < 3; ++k) {
             b.lo[k] = fmin_t(p[k] - ra, p[3 + k] - rb);
             b.hi[k] = fmax_t(p[k] + ra, p[3 + k] + rb);
+        }
+    } else if (type == kMesh) {
+        const float* v = data + 9 * i;
+        for (int k = 0; k < 3; ++k) {
+            b.lo[k] = fmin_t(fmin_t(v[k], v[3 + k]), v[6 + k]);
+            b.hi[k] = fmax_t(fmax_t(v[k], v[3 + k]), v[6 + k]);
         }
     } else {
         const float* v = data + 36 * i;
@@ -873,6 +882,27 @@ static bool intersect_prim(const Blas& b, uint32_t inst, uint32_t s, const tvec3
                 h->n = shim::normalize(hp - (a + u * (e - a)));
             }
         }
+    } else if (b.type == kMesh) {
+        // triangle i reports primitive id i; the normal interpolates the vertex normals with the
+        // hit's barycentrics (triangle_closest_hit.rchit:19-41), else it is the face normal
+        const float* q = b.data.data() + 9 * s;
+        tvec3<T> v0 = tvec3<T>{T(q[0]), T(q[1]), T(q[2])}, v1 = tvec3<T>{T(q[3]), T(q[4]), T(q[5])},
+                 v2 = tvec3<T>{T(q[6]), T(q[7]), T(q[8])};
+        T b1, b2;
+        T t = tri_intersect(o, d, v0, v1, v2, tmin, h->t, &b1, &b2);
+        if (t >= T(0)) {
+            take(t, s, b1, 0);
+            if (better) {
+                if (!b.radius.empty()) {
+                    const float* m = b.radius.data() + 9 * s;
+                    T w = T(1) - b1 - b2;
+                    tvec3<T> n0{T(m[0]), T(m[1]), T(m[2])}, n1{T(m[3]), T(m[4]), T(m[5])}, n2{T(m[6]), T(m[7]), T(m[8])};
+                    h->n = shim::normalize(w * n0 + b1 * n1 + b2 * n2);
+                } else {
+                    h->n = shim::normalize(shim::cross(v1 - v0, v2 - v0));
+                }
+            }
+        }
     } else {
         const float* v = b.data.data() + 36 * s;
         for (int k = 0; k < 4; ++k) {
@@ -1177,16 +1207,21 @@ int64_t orc_bvh8(const float* boxes, int64_t n, int max_leaf, int64_t max_nodes,
 // ---- scenes and tracing -----------------------------------------------------------------
 void* orc_scene_create() { return new Scene(); }
 void orc_scene_destroy(void* s) { delete static_cast<Scene*>(s); }
-// type: 0 Phantom (data 12 floats/prim, radius 2/prim), 1 LSS (6, 2), 2 DOTS (36, unused).
+// type: 0 Phantom (data 12 floats/prim, radius 2/prim), 1 LSS (6, 2), 2 DOTS (36, unused),
+// 3 mesh (9 floats/triangle; "radius" = 9 vertex-normal floats per triangle, or null).
 // Returns the BLAS index.
 int orc_scene_add_blas(void* s, int type, int64_t nprim, const float* data, const float* radius) {
     Scene* sc = static_cast<Scene*>(s);
     Blas b;
     b.type = type;
     b.nprim = nprim;
-    int per = type == kPhantom ? 12 : (type == kLss ? 6 : 36);
+    int per = type == kPhantom ? 12 : (type == kLss ? 6 : (type == kMesh ? 9 : 36));
     b.data.assign(data, data + per * nprim);
-    if (type != kDots) b.radius.assign(radius, radius + 2 * nprim);
+    if (type == kMesh) {
+        if (radius) b.radius.assign(radius, radius + 9 * nprim);  // vertex normals per triangle
+    } else if (type != kDots) {
+        b.radius.assign(radius, radius + 2 * nprim);
+    }
     build_blas(b);
     sc->blas.push_back(std::move(b));
     return int(sc->blas.size() - 1);

@@ -75,7 +75,7 @@ class OracleScene:
         self._keep = []
         for i, (gt, data, rad) in enumerate(blases):
             d = np.ascontiguousarray(data, np.float32)
-            r = np.ascontiguousarray(rad, np.float32)
+            r = None if rad is None else np.ascontiguousarray(rad, np.float32)
             self._keep += [d, r]
             b = orc.orc_scene_add_blas(self.h, gt, d.shape[0], P(d), P(r))
             xf = None if transforms is None or transforms[i] is None else \
@@ -151,3 +151,34 @@ def aimed_rays(rng, lines: np.ndarray, n: int, spread: float = 0.01, dist: float
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     org = tgt - d * dist
     return np.concatenate([org, d], axis=1).astype(np.float32)
+
+
+MESH = 3
+
+
+def sphere_mesh(rng, nu=48, nv=24, radius=0.35, bump=0.04, centre=(0.0, 0.3, 0.0)):
+    """A bumpy UV sphere: vertices (nv+1)*(nu+1), triangles 2*nu*nv, smooth vertex normals
+    (normalised offsets from the centre). Returns (vertices, triangle indices, normals)."""
+    th = np.linspace(0.0, np.pi, nv + 1)
+    ph = np.linspace(0.0, 2.0 * np.pi, nu + 1)
+    T, Ph = np.meshgrid(th, ph, indexing="ij")
+    rr = radius * (1.0 + bump * rng.standard_normal(T.shape))
+    pts = np.stack([rr * np.sin(T) * np.cos(Ph), rr * np.cos(T), rr * np.sin(T) * np.sin(Ph)], axis=-1)
+    v = (pts.reshape(-1, 3) + np.asarray(centre)).astype(np.float32)
+    n = pts.reshape(-1, 3)
+    n = (n / np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-12)).astype(np.float32)
+    idx = []
+    for i in range(nv):
+        for j in range(nu):
+            a, b = i * (nu + 1) + j, i * (nu + 1) + j + 1
+            c, d = (i + 1) * (nu + 1) + j, (i + 1) * (nu + 1) + j + 1
+            idx.append((a, c, b))
+            idx.append((b, c, d))
+    return v, np.asarray(idx, np.uint32), n
+
+
+def mesh_oracle_data(v, tri, nrm=None):
+    """Oracle BLAS data of a mesh: 9 floats per triangle, and 9 vertex-normal floats or None."""
+    data = np.ascontiguousarray(v[tri].reshape(-1, 9), np.float32)
+    nd = None if nrm is None else np.ascontiguousarray(nrm[tri].reshape(-1, 9), np.float32)
+    return data, nd

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import vkhrt_gb300 as H
-from hairscene import DOTS, LSS, PHANTOM, P, lines_from_strands, oracle_geometry
+from hairscene import DOTS, LSS, MESH, PHANTOM, P, lines_from_strands, mesh_oracle_data, oracle_geometry, sphere_mesh
 
 pytestmark = pytest.mark.gpu
 
@@ -71,6 +71,27 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
         assert blas.get(H.Part.DOTS_VERTICES, np.float32, (n, 36)).tobytes() == data.tobytes()
     ref_boxes = np.zeros((n, 6), np.float32)
     orc.orc_prim_boxes(gtype, P(np.ascontiguousarray(data)), P(np.ascontiguousarray(rad)), n, P(ref_boxes))
+    o = check_tree(blas, orc, ref_boxes, max_leaf, precision)
+    if quant_prims:
+        recs = blas.get(H.Part.PRIMS, np.uint8, n * 32).view(PRIMH)
+        halves = recs["h"].view(np.float16).astype(np.float32)
+        key = recs["key"]
+        nroots = int(key.max() >> 8) + 1
+        roots = blas.get(H.Part.ROOTS, np.float32, (nroots, 4))
+        rt = roots[key >> 8, :3]
+        deq = (np.repeat(rt, 4, axis=0).reshape(n, 4, 3) + halves[:, :12].reshape(n, 4, 3)).astype(np.float32)
+        order = o["order"]
+        assert deq.reshape(n, 12).tobytes() == np.ascontiguousarray(data[order]).tobytes()
+        assert np.ascontiguousarray(halves[:, 12:14]).tobytes() == np.ascontiguousarray(rad[order]).tobytes()
+        first = roots[key >> 8, 3].view(np.uint32)
+        assert np.array_equal(first + (key & 0xff), order)
+    return blas
+
+
+def check_tree(blas, orc, ref_boxes, max_leaf, precision):
+    """Primitive boxes, Morton codes, sort, binary tree, BVH8 nodes (both encodings) and leaf
+    order of a BLAS against the oracle built from the same boxes; returns the oracle's tree."""
+    n = len(ref_boxes)
     assert blas.get(H.Part.PRIM_BOXES, np.float32, (n, 6)).tobytes() == ref_boxes.tobytes()
     o = oracle_bvh(orc, ref_boxes, max_leaf)
     assert np.array_equal(blas.get(H.Part.MORTON_SORTED, np.uint64, n), o["codes"])
@@ -97,20 +118,7 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
             assert fn["hi_" + ax].tobytes() == np.ascontiguousarray(o["cbox"][:nn, :, 3 + k]).tobytes()
         assert np.array_equal(fn["meta"], o["meta"][:nn])
         assert np.array_equal(fn["imask"], imask)
-    if quant_prims:
-        recs = blas.get(H.Part.PRIMS, np.uint8, n * 32).view(PRIMH)
-        halves = recs["h"].view(np.float16).astype(np.float32)
-        key = recs["key"]
-        nroots = int(key.max() >> 8) + 1
-        roots = blas.get(H.Part.ROOTS, np.float32, (nroots, 4))
-        rt = roots[key >> 8, :3]
-        deq = (np.repeat(rt, 4, axis=0).reshape(n, 4, 3) + halves[:, :12].reshape(n, 4, 3)).astype(np.float32)
-        order = o["order"]
-        assert deq.reshape(n, 12).tobytes() == np.ascontiguousarray(data[order]).tobytes()
-        assert np.ascontiguousarray(halves[:, 12:14]).tobytes() == np.ascontiguousarray(rad[order]).tobytes()
-        first = roots[key >> 8, 3].view(np.uint32)
-        assert np.array_equal(first + (key & 0xff), order)
-    return blas
+    return o
 
 
 @pytest.mark.parametrize("gtype", [PHANTOM, LSS, DOTS])
@@ -191,3 +199,32 @@ def test_blas_keeps_only_what_tracing_reads(ctx):
         with pytest.raises(H.HrtError) as e:
             blas.get(H.Part.CURVES, np.float32, (n, 12))
         assert e.value.status == 6 or "not kept" in str(e.value)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("with_normals", [True, False])
+def test_mesh_build_bit_exact(ctx, orc, precision, with_normals):
+    """Triangle-mesh BLAS: boxes, tree and nodes bit for bit against the oracle; records hold the
+    triangle's vertices, its vertex normals (or none) and its index as the primitive id."""
+    rng = np.random.default_rng(41)
+    v, tri, nrm = sphere_mesh(rng)
+    blas = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=H.BLASType.eMesh, vertices=v, tri_indices=tri, normals=nrm if with_normals else None,
+                    precision=H.Precision(precision), keep_intermediate=True), ctx)
+    n = len(tri)
+    assert blas.info["nprims"] == n and blas.info["prim_bytes"] == 80
+    data, nd = mesh_oracle_data(v, tri, nrm)
+    ref_boxes = np.zeros((n, 6), np.float32)
+    orc.orc_prim_boxes(MESH, P(data), None, n, P(ref_boxes))
+    o = check_tree(blas, orc, ref_boxes, 1, precision)
+    rec = blas.get(H.Part.PRIMS, np.float32, (n, 20))
+    order = o["order"]
+    assert rec[:, [0, 1, 2, 4, 5, 6, 8, 9, 10]].tobytes() == np.ascontiguousarray(data[order]).tobytes()
+    assert np.array_equal(rec[:, 3].view(np.uint32), order)
+    if with_normals:
+        assert rec[:, [7, 11, 12, 13, 14, 15, 16, 17, 18]].tobytes() == np.ascontiguousarray(nd[order]).tobytes()
+        assert np.all(rec[:, 19].view(np.uint32) == 1)
+    else:
+        assert np.all(rec[:, 19].view(np.uint32) == 0)
+    with pytest.raises(H.HrtError):  # indices past the vertices
+        H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.eMesh, vertices=v[:10], tri_indices=tri), ctx)

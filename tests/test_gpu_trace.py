@@ -339,3 +339,52 @@ def test_batch_set_cameras_matches_single_launch(ctx):
         assert np.array_equal(hits, hits1) and np.abs(rgba - rgba1).max() <= 1e-6
     with pytest.raises(H.HrtError):
         batch.set_cameras(new[:1])
+
+
+def _mesh_scene(ctx, orc, precision, with_normals, hair=False):
+    from hairscene import MESH, mesh_oracle_data, sphere_mesh
+    rng = np.random.default_rng(43)
+    v, tri, nrm = sphere_mesh(rng)
+    mb = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=H.BLASType.eMesh, vertices=v, tri_indices=tri, normals=nrm if with_normals else None,
+                    precision=H.Precision(precision)), ctx)
+    data, nd = mesh_oracle_data(v, tri, nrm if with_normals else None)
+    blases, obl = [mb], [(MESH, data, nd)]
+    if hair:
+        hv, hr, hoff = H.generate_strands(H.StrandParams(seed=44, nstrands=800, nverts=24))
+        hb = H.BottomLevelAccelerationStructure(
+            H.BLASInput(type=H.BLASType.ePhantom, vertices=hv, radius=hr, strand_offsets=hoff,
+                        precision=H.Precision(precision)), ctx)
+        lines, lrad = lines_from_strands(hv, hr, hoff)
+        hd, hrad = oracle_geometry(orc, PHANTOM, lines, lrad, quantised=precision == 1)
+        blases.append(hb)
+        obl.append((PHANTOM, hd, hrad))
+    tlas = H.TopLevelAccelerationStructure(blases, ctx)
+    return blases, tlas, OracleScene(orc, obl), v, tri
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_mesh_trace_rays_vs_fp64_oracle(ctx, orc, precision):
+    _, tlas, osc, v, tri = _mesh_scene(ctx, orc, precision, True)
+    rng = np.random.default_rng(45)
+    c = v[tri].mean(axis=1)
+    tgt = c[rng.integers(0, len(c), 20000)] + rng.normal(size=(20000, 3)) * 0.01
+    d = rng.normal(size=(20000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([tgt - 3.0 * d, d], axis=1).astype(np.float32)
+    g = H.trace_rays(ctx, tlas, rays)
+    o_t, o_p, o_i, _ = osc.trace_rays(rays, precision=64)
+    st = compare_hits(np.where(g["t"] >= 0, g["t"].astype(np.float64), -1.0), g["prim"], g["inst"], o_t, o_p, o_i)
+    assert st["hits"] > 10000 and st["agreement"] >= AGREE and st["max_rel_t"] <= T_REL
+
+
+@pytest.mark.parametrize("with_normals", [True, False])
+def test_mesh_frame_shaded_vs_oracle(ctx, orc, with_normals):
+    """Interpolated vertex normals (or face normals), Shade() and the shadow ray, with a Phantom
+    hair BLAS in the same TLAS (the mixed-type kernel)."""
+    _, tlas, osc, *_ = _mesh_scene(ctx, orc, 0, with_normals, hair=True)
+    fr, rgba, hits, o = render_both(ctx, tlas, osc, 160, 120, spp=1, shading=2)
+    st, px_ok, diff = frame_checks(rgba, hits, o, 1)
+    assert (hits["inst"] == 0).sum() > 1000 and (hits["inst"] == 1).sum() > 500  # both instances are seen
+    assert st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
+    assert px_ok.mean() >= 0.999 and diff[px_ok].max() <= RGB_ABS

@@ -191,3 +191,23 @@ def test_bvh8_slots_follow_direction(orc):
     for s in range(8):
         lo = cbox[0, s, :3]
         assert tuple(int(v > 5) for v in lo) == ((s & 1), (s >> 1) & 1, (s >> 2) & 1)
+
+
+def test_mesh_triangle_known_answer(orc):
+    """One triangle in the z = 1 plane, a ray down -z through a known point: t, id and the
+    barycentric interpolation of its vertex normals (triangle_closest_hit.rchit:19-41)."""
+    from hairscene import OracleScene
+    tri = np.array([[0, 0, 1, 1, 0, 1, 0, 1, 1]], np.float32)
+    nrm = np.array([[0, 0, 1, 1, 0, 0, 0, 1, 0]], np.float32)  # n0 = +z, n1 = +x, n2 = +y
+    osc = OracleScene(orc, [(3, tri, nrm)])
+    rays = np.array([[0.25, 0.5, 3.0, 0.0, 0.0, -1.0]], np.float32)  # hits at (0.25, 0.5, 1): b1 0.25, b2 0.5
+    t, prim, inst, n = osc.trace_rays(rays, precision=64)
+    assert abs(t[0] - 2.0) < 1e-12 and prim[0] == 0 and inst[0] == 0
+    expect = np.array([0.25, 0.5, 0.25])  # w n0 + b1 n1 + b2 n2 with w = 0.25
+    assert np.allclose(n[0], expect / np.linalg.norm(expect), atol=1e-12)
+    osc2 = OracleScene(orc, [(3, tri, None)])  # no normals: the face normal
+    t2, _, _, n2 = osc2.trace_rays(rays, precision=64)
+    assert abs(t2[0] - 2.0) < 1e-12 and np.allclose(np.abs(n2[0]), [0, 0, 1])
+    boxes = np.zeros((1, 6), np.float32)
+    orc.orc_prim_boxes(3, P(tri), None, 1, P(boxes))
+    assert boxes.tolist() == [[0, 0, 1, 1, 1, 1]]

@@ -30,7 +30,8 @@ class BLASInputC(ctypes.Structure):
     _fields_ = [("type", c_i32), ("precision", c_i32), ("memory", c_i32), ("max_leaf", c_u32),
                 ("vertices", c_p), ("radius", c_p), ("strand_offsets", c_p), ("line_indices", c_p),
                 ("nvertices", c_u64), ("nstrands", c_u64), ("nlines", c_u64), ("const_radius", c_f),
-                ("transform", c_f * 16), ("quant_chunk", c_u32), ("flags", c_u32)]
+                ("transform", c_f * 16), ("quant_chunk", c_u32), ("flags", c_u32), ("tri_indices", c_p),
+                ("ntris", c_u64), ("normals", c_p)]
 
 
 class BLASInfoC(ctypes.Structure):
@@ -145,6 +146,7 @@ class BLASType(enum.IntEnum):
     ePhantom = 0   # cubic Bezier curves, Phantom ray-hair intersector (BLASType::eHair)
     eLSS = 1       # linear swept spheres (BLASType::eMesh with LSS geometry)
     eDOTS = 2      # disjoint orthogonal triangle strips (BLASType::eMesh triangles)
+    eMesh = 3      # indexed triangle mesh (BLASType::eMesh), optional vertex normals
 
 
 class Precision(enum.IntEnum):
@@ -177,12 +179,15 @@ class Part(enum.IntEnum):
 
 @dataclass
 class BLASInput:
-    """Hair geometry of one BLAS (hrt_blas_input). Either strand_offsets or line_indices."""
+    """Geometry of one BLAS (hrt_blas_input): hair (strand_offsets or line_indices) or, for
+    BLASType.eMesh, indexed triangles (tri_indices, optional per-vertex normals)."""
     type: BLASType
     vertices: np.ndarray                      # (nv, 3) float32
     radius: np.ndarray | None = None          # (nv,) float32 per vertex
     strand_offsets: np.ndarray | None = None  # (ns + 1,) uint32
     line_indices: np.ndarray | None = None    # (nl, 2) uint32
+    tri_indices: np.ndarray | None = None     # (nt, 3) uint32 (mesh)
+    normals: np.ndarray | None = None         # (nv, 3) float32 (mesh)
     const_radius: float = 0.02
     transform: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))  # object->world
     precision: Precision = Precision.FP32
@@ -249,6 +254,15 @@ class BottomLevelAccelerationStructure:
             self._keep.append(li)
             c.line_indices = _ptr(li)
             c.nlines = li.shape[0]
+        if inp.tri_indices is not None:
+            ti = np.ascontiguousarray(inp.tri_indices, dtype=np.uint32).reshape(-1, 3)
+            self._keep.append(ti)
+            c.tri_indices = _ptr(ti)
+            c.ntris = ti.shape[0]
+        if inp.normals is not None:
+            nm = np.ascontiguousarray(inp.normals, dtype=np.float32).reshape(-1, 3)
+            self._keep.append(nm)
+            c.normals = _ptr(nm)
         c.const_radius = inp.const_radius
         xf = np.asarray(inp.transform, dtype=np.float32).reshape(4, 4)
         for i, val in enumerate(xf.T.reshape(-1)):  # column major

@@ -391,16 +391,114 @@ void hrt_blas_input_default(hrt_blas_input* in) {
     for (int k = 0; k < 4; ++k) in->transform[5 * k] = 1.0f;
 }
 
+// Builds a triangle-mesh BLAS: gathers the indexed triangles (and vertex normals) on the device
+// and runs the common BVH build over them.
+static hrt_status build_mesh(hrt_context* ctx, const hrt_blas_input* in, cudaStream_t s, hrt_blas** out) {
+    if (in->strand_offsets || in->line_indices)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: a mesh takes tri_indices, not strands or lines");
+    if (in->ntris && !in->tri_indices) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: null tri_indices");
+    if (in->nvertices > 0 && !in->vertices) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: null vertices");
+    if (in->nvertices >= (1ull << 32))
+        return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_build: more than 2^32 - 1 vertices");
+    if (in->ntris >= (1ull << 29))
+        return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_build: %llu triangles; the limit is 2^29",
+                    (unsigned long long)in->ntris);
+    const uint32_t max_leaf = in->max_leaf ? in->max_leaf : 1;
+    if (max_leaf > 3) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: max_leaf must be 1..3");
+    if (in->memory == HRT_MEMORY_HOST)
+        for (uint64_t i = 0; i < 3 * in->ntris; ++i)
+            if (in->tri_indices[i] >= in->nvertices)
+                return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: triangle index %llu out of range",
+                            (unsigned long long)i);
+    const uint64_t n = in->ntris;
+    hrt_blas* b = new (std::nothrow) hrt_blas();
+    if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_blas_build: host allocation");
+    b->ctx = ctx;
+    b->type = in->type;
+    b->precision = in->precision;
+    b->nprims = n;
+    b->keep = (in->flags & HRT_BUILD_KEEP_INTERMEDIATE) != 0;
+    memcpy(b->transform, in->transform, sizeof(b->transform));
+    float *dv = nullptr, *dn = nullptr, *tris = nullptr, *tnrm = nullptr;
+    uint32_t* didx = nullptr;
+    const bool host = in->memory == HRT_MEMORY_HOST;
+    auto cleanup = [&]() {
+        if (host) {
+            if (dv) cudaFree(dv);
+            if (dn) cudaFree(dn);
+            if (didx) cudaFree(didx);
+        }
+        if (tris) cudaFree(tris);
+        if (tnrm) cudaFree(tnrm);
+    };
+    auto bail = [&](cudaError_t e, const char* what) {
+        cleanup();
+        free_build_output(b->out);
+        delete b;
+        return cuda_fail(ctx, e, what);
+    };
+    cudaError_t e = cudaSuccess;
+    if (host && n) {
+        if ((e = cudaMalloc(&dv, in->nvertices * 12)) != cudaSuccess) return bail(e, "allocate vertices");
+        if ((e = cudaMemcpyAsync(dv, in->vertices, in->nvertices * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return bail(e, "copy vertices");
+        if (in->normals) {
+            if ((e = cudaMalloc(&dn, in->nvertices * 12)) != cudaSuccess) return bail(e, "allocate normals");
+            if ((e = cudaMemcpyAsync(dn, in->normals, in->nvertices * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+                return bail(e, "copy normals");
+        }
+        if ((e = cudaMalloc(&didx, n * 12)) != cudaSuccess) return bail(e, "allocate indices");
+        if ((e = cudaMemcpyAsync(didx, in->tri_indices, n * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return bail(e, "copy indices");
+    } else if (!host) {
+        dv = const_cast<float*>(in->vertices);
+        dn = const_cast<float*>(in->normals);
+        didx = const_cast<uint32_t*>(in->tri_indices);
+    }
+    if (n) {
+        if ((e = cudaMalloc(&tris, n * 36)) != cudaSuccess) return bail(e, "allocate triangles");
+        if (in->normals && (e = cudaMalloc(&tnrm, n * 36)) != cudaSuccess) return bail(e, "allocate normals");
+        if ((e = make_tris(dv, dn, didx, n, tris, tnrm, s)) != cudaSuccess) return bail(e, "gather triangles");
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    BuildInput bi{in->type, in->precision, int(max_leaf), in->quant_chunk, nullptr, nullptr, n, b->keep, tris, tnrm};
+    char msg[256] = {0};
+    e = build_blas_device(bi, b->out, s, msg, sizeof(msg));
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&b->build_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) {
+        std::string m = msg;
+        cleanup();
+        free_build_output(b->out);
+        delete b;
+        if (e == cudaErrorMemoryAllocation) return fail(ctx, HRT_ERR_OOM, "BVH build: %s", m.c_str());
+        return fail(ctx, HRT_ERR_CUDA, "BVH build: %s", m.empty() ? cudaGetErrorString(e) : m.c_str());
+    }
+    cleanup();
+    *out = b;
+    return HRT_OK;
+}
+
 hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stream, hrt_blas** out) {
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!in || !out) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: null input or output");
     *out = nullptr;
-    if (in->type < HRT_BLAS_PHANTOM || in->type > HRT_BLAS_DOTS)
+    if (in->type < HRT_BLAS_PHANTOM || in->type > HRT_BLAS_MESH)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: unknown geometry type %d", in->type);
     if (in->precision != HRT_PRECISION_FP32 && in->precision != HRT_PRECISION_QUANTISED)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: unknown precision %d", in->precision);
     if (in->memory != HRT_MEMORY_HOST && in->memory != HRT_MEMORY_DEVICE)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: unknown memory kind %d", in->memory);
+    if (in->type == HRT_BLAS_MESH) {
+        DeviceSet dset(ctx->device);
+        return build_mesh(ctx, in, static_cast<cudaStream_t>(stream), out);
+    }
     if (!!in->strand_offsets == !!in->line_indices)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: give exactly one of strand_offsets and line_indices");
     if (in->nvertices > 0 && !in->vertices)

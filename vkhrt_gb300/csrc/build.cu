@@ -321,6 +321,28 @@ __global__ void boxes_dots_kernel(const float* geom, uint64_t n, float* boxes) {
         boxes[6 * i + 3 + k] = hi;
     }
 }
+// Mesh triangle box: min/max of the three vertices, in vertex order.
+__global__ void boxes_tri_kernel(const float* tris, uint64_t n, float* boxes) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* v = tris + 9 * i;
+    for (int k = 0; k < 3; ++k) {
+        boxes[6 * i + k] = fmin_t(fmin_t(v[k], v[3 + k]), v[6 + k]);
+        boxes[6 * i + 3 + k] = fmax_t(fmax_t(v[k], v[3 + k]), v[6 + k]);
+    }
+}
+__global__ void tris_kernel(const float* verts, const float* vnrm, const uint32_t* idx, uint64_t n, float* tris,
+                            float* tri_nrm) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int j = 0; j < 3; ++j) {
+        const uint64_t v = idx[3 * i + j];
+        for (int k = 0; k < 3; ++k) {
+            tris[9 * i + 3 * j + k] = verts[3 * v + k];
+            if (tri_nrm) tri_nrm[9 * i + 3 * j + k] = vnrm[3 * v + k];
+        }
+    }
+}
 __global__ void expand_dots_kernel(const float* geom, uint64_t n, float* out36) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -728,7 +750,7 @@ __global__ void map_order_kernel(const uint32_t* sorted_pos, const uint32_t* sor
 // Primitive records in slot order.
 __global__ void records_kernel(int type, int precision, const uint32_t* ids, uint64_t n, const float* curves,
                                const float* lrad, const float* geom, const uint32_t* chunk_incl, const float4* roots,
-                               void* prims) {
+                               const float* tri_nrm, void* prims) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t s = ids[i];
@@ -764,6 +786,18 @@ __global__ void records_kernel(int type, int precision, const uint32_t* ids, uin
         r.a = make_float4(g[0], g[1], g[2], g[6]);
         r.b = make_float4(g[3], g[4], g[5], g[7]);
         static_cast<PrimLss*>(prims)[i] = r;
+    } else if (type == HRT_BLAS_MESH) {
+        const float* v = geom + 9 * uint64_t(s);
+        const float* m = tri_nrm ? tri_nrm + 9 * uint64_t(s) : nullptr;
+        float nn[9];
+        for (int k = 0; k < 9; ++k) nn[k] = m ? m[k] : 0.0f;
+        PrimTri r;
+        r.a = make_float4(v[0], v[1], v[2], __uint_as_float(s));
+        r.b = make_float4(v[3], v[4], v[5], nn[0]);
+        r.c = make_float4(v[6], v[7], v[8], nn[1]);
+        r.d = make_float4(nn[2], nn[3], nn[4], nn[5]);
+        r.e = make_float4(nn[6], nn[7], nn[8], __uint_as_float(m ? 1u : 0u));
+        static_cast<PrimTri*>(prims)[i] = r;
     } else {
         const float* g = geom + 18 * uint64_t(s);
         PrimDots r;
@@ -783,6 +817,13 @@ template <class T> cudaError_t dalloc(T** p, uint64_t count, cudaStream_t s) {
 }  // namespace
 
 // =================================================================================================
+cudaError_t make_tris(const float* verts, const float* vnrm, const uint32_t* idx, uint64_t ntris, float* tris,
+                      float* tri_nrm, cudaStream_t s) {
+    if (ntris == 0) return cudaSuccess;
+    tris_kernel<<<grid_for(ntris, 256), 256, 0, s>>>(verts, vnrm, idx, ntris, tris, tri_nrm);
+    return cudaGetLastError();
+}
+
 cudaError_t make_lines(const float* verts, const float* vrad, float const_radius, const uint32_t* strand_line_off,
                        const uint32_t* strand_vert_off, uint64_t nstrands, const uint32_t* line_idx, uint64_t nlines,
                        float* lines, float* lrad, cudaStream_t s) {
@@ -817,7 +858,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     const unsigned T = 256;
     out.node_bytes = in.precision == HRT_PRECISION_QUANTISED ? sizeof(NodeQ) : sizeof(NodeF);
     if (in.type == HRT_BLAS_PHANTOM) out.prim_bytes = in.precision == HRT_PRECISION_QUANTISED ? 32 : 64;
-    else out.prim_bytes = in.type == HRT_BLAS_LSS ? 32 : 80;
+    else out.prim_bytes = in.type == HRT_BLAS_LSS ? 32 : 80;  // DOTS and mesh triangles: 80
     if (n == 0) return cudaSuccess;
 
     // ---- geometry processing -> per-segment boxes (and the intersected geometry) ----------------
@@ -874,6 +915,8 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
         HRT_CK(cudaMalloc(&out.geom, n * 8 * sizeof(float)));
         lss_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, out.geom);
         boxes_lss_kernel<<<grid_for(n, T), T, 0, s>>>(out.geom, n, out.prim_boxes);
+    } else if (in.type == HRT_BLAS_MESH) {
+        boxes_tri_kernel<<<grid_for(n, T), T, 0, s>>>(in.tris, n, out.prim_boxes);
     } else {
         HRT_CK(cudaMalloc(&out.geom, n * 18 * sizeof(float)));
         dots_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, out.geom);
@@ -977,8 +1020,9 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     HRT_CK(cudaMalloc(&out.prim_ids, n * 4));
     map_order_kernel<<<grid_for(n, T), T, 0, s>>>(porder, order, n, out.prim_ids);
     HRT_CK(cudaMalloc(&out.prims, n * out.prim_bytes));
-    records_kernel<<<grid_for(n, T), T, 0, s>>>(in.type, in.precision, out.prim_ids, n, out.curves, in.lrad, out.geom,
-                                                chunk_incl, out.roots, out.prims);
+    records_kernel<<<grid_for(n, T), T, 0, s>>>(in.type, in.precision, out.prim_ids, n, out.curves, in.lrad,
+                                                in.type == HRT_BLAS_MESH ? in.tris : out.geom, chunk_incl, out.roots,
+                                                in.tri_normals, out.prims);
     HRT_CK(cudaGetLastError());
 
     // bounds: union of all primitive boxes = root of the binary tree

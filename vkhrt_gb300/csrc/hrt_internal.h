@@ -56,6 +56,8 @@ struct alignas(16) PrimPhantomF { float4 a, b, c, d; };
 struct alignas(16) PrimPhantomH { uint4 q0, q1; };
 struct alignas(16) PrimLss { float4 a, b; };
 struct alignas(16) PrimDots { float4 a, b, c, d, e; };
+// Mesh triangle (80 B): {v0, id} {v1, n0.x} {v2, n0.y} {n0.z, n1} {n2, has normals (0/1 bits)}
+struct alignas(16) PrimTri { float4 a, b, c, d, e; };
 
 struct DevBlas {
     const void* nodes;        // NodeF or NodeQ
@@ -141,6 +143,8 @@ struct BuildInput {
     const float* lrad;    // device, n x 2 (per line end)
     uint64_t n;
     bool keep_intermediate;
+    const float* tris = nullptr;         // mesh: device, n x 9 (triangle vertices)
+    const float* tri_normals = nullptr;  // mesh: device, n x 9 (vertex normals), or null
 };
 struct BuildOutput {
     // owned device allocations (freed by the BLAS)
@@ -166,6 +170,9 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
 void free_build_output(BuildOutput& out);
 cudaError_t expand_dots(const float* geom, uint64_t n, float* out36, cudaStream_t s);
 // Line generation from vertices (device pointers); see hrt_blas_input.
+// Gathers mesh triangles (and their vertex normals when given) into n x 9 arrays.
+cudaError_t make_tris(const float* verts, const float* vnrm, const uint32_t* idx, uint64_t ntris, float* tris,
+                      float* tri_nrm, cudaStream_t s);
 cudaError_t make_lines(const float* verts, const float* vrad, float const_radius, const uint32_t* strand_line_off,
                        const uint32_t* strand_vert_off, uint64_t nstrands, const uint32_t* line_idx, uint64_t nlines,
                        float* lines, float* lrad, cudaStream_t s);

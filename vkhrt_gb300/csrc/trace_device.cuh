@@ -299,8 +299,9 @@ __device__ __forceinline__ TriRay make_triray(V3<float> d) {
     return r;
 }
 __device__ __forceinline__ float comp(V3<float> v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+// b1, b2 (when given): barycentric weights of v1 and v2 at the hit (v0's is 1 - b1 - b2).
 __device__ __forceinline__ float tri_hit(const TriRay& R, V3<float> o, V3<float> v0, V3<float> v1, V3<float> v2,
-                                         float tmin, float tmax) {
+                                         float tmin, float tmax, float* b1 = nullptr, float* b2 = nullptr) {
     V3<float> A = v0 - o, B = v1 - o, C = v2 - o;
     float Akz = comp(A, R.kz), Bkz = comp(B, R.kz), Ckz = comp(C, R.kz);
     float Ax = comp(A, R.kx) - R.Sx * Akz, Ay = comp(A, R.ky) - R.Sy * Akz;
@@ -313,6 +314,11 @@ __device__ __forceinline__ float tri_hit(const TriRay& R, V3<float> o, V3<float>
     float Tn = U * (R.Sz * Akz) + V * (R.Sz * Bkz) + W * (R.Sz * Ckz);
     float t = Tn / det;
     if (!(t >= tmin) || !(t <= tmax)) return -1.0f;
+    if (b1) {
+        const float inv = 1.0f / det;
+        *b1 = V * inv;
+        *b2 = W * inv;
+    }
     return t;
 }
 
@@ -425,6 +431,17 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         if (t >= 0.0f && t <= h.t) {
             uint32_t id = __ldg(&B.prim_ids[slot]);
             if (beats(t, inst, id, h)) { h = Hit{t, id, inst, slot, u, ts, tl, 0u}; return true; }
+        }
+        return false;
+    }
+    if (type == HRT_BLAS_MESH) {  // renderer.cpp:543-582: one triangle per slot, id = triangle index
+        const PrimTri* pr = static_cast<const PrimTri*>(B.prims) + slot;
+        const float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c);
+        float b1, b2;
+        const float t = tri_hit(R.tr, R.o, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), R.tmin, h.t, &b1, &b2);
+        if (t >= 0.0f) {
+            const uint32_t id = __float_as_uint(a.w);
+            if (beats(t, inst, id, h)) { h = Hit{t, id, inst, slot, b1, b2, 0.0f, 0u}; return true; }
         }
         return false;
     }
@@ -702,7 +719,7 @@ __device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> 
             if (!(a <= b * (1.0f + 9.5367431640625e-07f))) continue;
         }
         if (I.b.type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
-        else if (I.b.type == HRT_BLAS_DOTS) R.tr = make_triray(R.d);
+        else if (I.b.type == HRT_BLAS_DOTS || I.b.type == HRT_BLAS_MESH) R.tr = make_triray(R.d);
         if (traverse<kQuant>(I.b, i, R, h, any_hit, skip_inst, skip_slot, fp64_resolve, st, err)) {
             found = true;
             if (any_hit) return true;
@@ -752,6 +769,20 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         const V3<float> ax = mk(__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z));
         n = normalize_rn(mk(fmaf(-h.u, ax.x, fmaf(h.sl, d.x, -w0.x)), fmaf(-h.u, ax.y, fmaf(h.sl, d.y, -w0.y)),
                             fmaf(-h.u, ax.z, fmaf(h.sl, d.z, -w0.z))));
+    } else if (B.type == HRT_BLAS_MESH) {
+        // triangle_closest_hit.rchit:19-41: vertex normals interpolated with the hit's
+        // barycentrics (1 - u - v, u, v); without normals, the face normal
+        const PrimTri* pr = static_cast<const PrimTri*>(B.prims) + h.slot;
+        const float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c), d4 = __ldg(&pr->d), e4 = __ldg(&pr->e);
+        if (__float_as_uint(e4.w)) {  // n0 = (b.w, c.w, d.x), n1 = d.yzw, n2 = e.xyz
+            const float u = h.u, v = h.ts, w = __fsub_rn(__fsub_rn(1.0f, u), v);
+            n = normalize_rn(mk(fmaf(v, e4.x, fmaf(u, d4.y, __fmul_rn(w, b.w))),
+                                fmaf(v, e4.y, fmaf(u, d4.z, __fmul_rn(w, c.w))),
+                                fmaf(v, e4.z, fmaf(u, d4.w, __fmul_rn(w, d4.x)))));
+        } else {
+            const V3<float> v0 = mk(a.x, a.y, a.z), v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+            n = normalize_rn(cross_rn(v1 - v0, v2 - v0));
+        }
     } else {
         // DOTS vertices carry no normals (geometry_processor.cpp:259-264): the face normal
         const PrimDots* pr = static_cast<const PrimDots*>(B.prims) + h.slot;
@@ -893,7 +924,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         if (!(a <= b * (1.0f + 9.5367431640625e-07f))) return false;
         const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
         if (type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
-        else if (type == HRT_BLAS_DOTS) R.tr = make_triray(R.d);
+        else if (type == HRT_BLAS_DOTS || type == HRT_BLAS_MESH) R.tr = make_triray(R.d);
         nodes = B.nodes;
         oct = (R.inv.x < 0.0f ? 1u : 0u) | (R.inv.y < 0.0f ? 2u : 0u) | (R.inv.z < 0.0f ? 4u : 0u);
         cur_base = 0;  // the root as a group of one internal child in slot 0
