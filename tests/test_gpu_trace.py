@@ -383,8 +383,8 @@ def test_mesh_frame_shaded_vs_oracle(ctx, orc, with_normals):
     """Interpolated vertex normals (or face normals), Shade() and the shadow ray, with a Phantom
     hair BLAS in the same TLAS (the mixed-type kernel)."""
     _, tlas, osc, *_ = _mesh_scene(ctx, orc, 0, with_normals, hair=True)
-    fr, rgba, hits, o = render_both(ctx, tlas, osc, 160, 120, spp=1, shading=2)
+    fr, rgba, hits, o = render_both(ctx, tlas, osc, 200, 150, spp=1, shading=2)
     st, px_ok, diff = frame_checks(rgba, hits, o, 1)
-    assert (hits["inst"] == 0).sum() > 1000 and (hits["inst"] == 1).sum() > 500  # both instances are seen
+    assert (hits["inst"] == 0).sum() > 500 and (hits["inst"] == 1).sum() > 500  # both instances are seen
     assert st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
     assert px_ok.mean() >= 0.999 and diff[px_ok].max() <= RGB_ABS
