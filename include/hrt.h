@@ -110,7 +110,7 @@ typedef struct hrt_blas_info {
     uint64_t prim_bytes;    /* bytes per primitive record */
     uint64_t device_bytes;  /* total device memory held */
     float bounds[6];        /* object-space lo xyz, hi xyz */
-    float build_ms;         /* device time of the last build */
+    float build_ms;         /* device time of the last build or refit */
 } hrt_blas_info;
 
 /* Parts of a built BLAS copied to the host for inspection (bit-exact tests). A BLAS keeps only
@@ -196,6 +196,13 @@ int hrt_abi_version(void);
 void hrt_blas_input_default(hrt_blas_input* in);
 hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stream, hrt_blas** out);
 hrt_status hrt_blas_destroy(hrt_blas* blas);
+/* Moves the primitives of a built BLAS (animated strands): new vertex positions, and per-vertex
+ * radii (hair) or normals (mesh) exactly when the build had them, for the same vertex count and
+ * topology. Geometry, primitive boxes and records are recomputed and the BVH8 boxes refitted
+ * bottom-up; the tree's topology and leaf order are kept, so its quality falls with large
+ * motions (build anew then). TLASes that hold the BLAS must be built again afterwards (they
+ * copy its bounds). No counterpart in the reference (it builds once). */
+hrt_status hrt_blas_refit(hrt_blas* blas, const float* vertices, const float* per_vertex, int32_t memory, void* stream);
 int32_t hrt_blas_type(const hrt_blas* blas);
 hrt_status hrt_blas_transform(const hrt_blas* blas, float out[16]);
 hrt_status hrt_blas_get_info(const hrt_blas* blas, hrt_blas_info* out);

@@ -228,3 +228,51 @@ def test_mesh_build_bit_exact(ctx, orc, precision, with_normals):
         assert np.all(rec[:, 19].view(np.uint32) == 0)
     with pytest.raises(H.HrtError):  # indices past the vertices
         H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.eMesh, vertices=v[:10], tri_indices=tri), ctx)
+
+
+def _numpy_refit(nodes, prim_order, boxes):
+    """Slot boxes of a BVH8 after a refit, from its structure and new primitive boxes: a leaf
+    slot is the union of its primitives' boxes, an internal slot its child's union (exact)."""
+    nn = len(nodes)
+    lo = np.full((nn, 8, 3), np.inf, np.float32)
+    hi = np.full((nn, 8, 3), -np.inf, np.float32)
+    nb = np.zeros((nn, 6), np.float32)
+    for i in range(nn - 1, -1, -1):
+        for q in range(8):
+            m = int(nodes["meta"][i, q])
+            if m & 0x80:
+                c = int(nodes["child_base"][i]) + (m & 7)
+                lo[i, q], hi[i, q] = nb[c, :3], nb[c, 3:]
+            elif m:
+                s = [int(prim_order[int(nodes["prim_base"][i]) + (m & 31) + j]) for j in range(m >> 5)]
+                lo[i, q], hi[i, q] = boxes[s, :3].min(axis=0), boxes[s, 3:].max(axis=0)
+        used = nodes["meta"][i] != 0
+        nb[i, :3], nb[i, 3:] = lo[i, used].min(axis=0), hi[i, used].max(axis=0)
+    return lo, hi, nb
+
+
+@pytest.mark.parametrize("gtype", [PHANTOM, LSS, DOTS])
+def test_refit_boxes_exact(ctx, orc, gtype):
+    """hrt_blas_refit on moved strands: primitive boxes equal the oracle's for the new geometry
+    and every node's slot boxes are the exact unions over the kept tree."""
+    v, r, off = H.generate_strands(H.StrandParams(seed=8, nstrands=300, nverts=17))
+    blas = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=H.BLASType(gtype), vertices=v, radius=r, strand_offsets=off, keep_intermediate=True), ctx)
+    rng = np.random.default_rng(9)
+    v2 = (v + 0.05 * np.sin(3.0 * v[:, [1, 2, 0]] + rng.uniform(0, 6.28, 3))).astype(np.float32)
+    blas.refit(v2, r)
+    n = blas.info["nprims"]
+    lines, lrad = lines_from_strands(v2, r, off)
+    data, rad = oracle_geometry(orc, gtype, lines, lrad)
+    ref_boxes = np.zeros((n, 6), np.float32)
+    orc.orc_prim_boxes(gtype, P(np.ascontiguousarray(data)), P(np.ascontiguousarray(rad)), n, P(ref_boxes))
+    assert blas.get(H.Part.PRIM_BOXES, np.float32, (n, 6)).tobytes() == ref_boxes.tobytes()
+    nn = blas.info["nnodes"]
+    fn = blas.get(H.Part.NODES, np.uint8, nn * 224).view(NODEF)
+    lo, hi, nb = _numpy_refit(fn, blas.get(H.Part.PRIM_ORDER, np.uint32, n), ref_boxes)
+    for k, ax in enumerate("xyz"):
+        assert fn["lo_" + ax].tobytes() == np.ascontiguousarray(lo[:, :, k]).tobytes()
+        assert fn["hi_" + ax].tobytes() == np.ascontiguousarray(hi[:, :, k]).tobytes()
+    assert np.array_equal(np.array(blas.info["bounds"], np.float32), nb[0])
+    with pytest.raises(H.HrtError):  # radii were given at the build
+        blas.refit(v2, None)

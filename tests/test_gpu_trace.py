@@ -388,3 +388,38 @@ def test_mesh_frame_shaded_vs_oracle(ctx, orc, with_normals):
     assert (hits["inst"] == 0).sum() > 500 and (hits["inst"] == 1).sum() > 500  # both instances are seen
     assert st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
     assert px_ok.mean() >= 0.999 and diff[px_ok].max() <= RGB_ABS
+
+
+@pytest.mark.parametrize("gtype,precision", [(PHANTOM, 0), (PHANTOM, 1), (LSS, 1), (DOTS, 0)])
+def test_refit_trace_vs_fp64_oracle(ctx, orc, gtype, precision):
+    """Trace a refitted BLAS (moved strands, topology kept) against the oracle on the moved
+    geometry: the same agreement bar as a fresh build."""
+    v, r, off = H.generate_strands(H.StrandParams(seed=12, nstrands=600, nverts=24))
+    blas = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType(gtype), vertices=v, radius=r,
+                                                          strand_offsets=off, precision=H.Precision(precision)), ctx)
+    v2 = (v + 0.04 * np.sin(2.0 * v[:, [2, 0, 1]])).astype(np.float32)
+    blas.refit(v2, r)
+    tlas = H.TopLevelAccelerationStructure([blas], ctx)  # TLASes copy the bounds: build after a refit
+    lines, lrad = lines_from_strands(v2, r, off)
+    data, rad = oracle_geometry(orc, gtype, lines, lrad, quantised=(precision == 1 and gtype == PHANTOM))
+    osc = OracleScene(orc, [(gtype, data, rad)])
+    rays = aimed_rays(np.random.default_rng(13), lines, 20000, spread=0.006)
+    g = H.trace_rays(ctx, tlas, rays)
+    o_t, o_p, o_i, _ = osc.trace_rays(rays, precision=64)
+    st = compare_hits(np.where(g["t"] >= 0, g["t"].astype(np.float64), -1.0), g["prim"], g["inst"], o_t, o_p, o_i)
+    assert st["hits"] > 5000 and st["agreement"] >= AGREE and st["max_rel_t"] <= T_REL
+
+
+def test_mesh_refit_trace(ctx, orc):
+    from hairscene import MESH, mesh_oracle_data, sphere_mesh
+    v, tri, nrm = sphere_mesh(np.random.default_rng(14))
+    blas = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.eMesh, vertices=v, tri_indices=tri,
+                                                          normals=nrm), ctx)
+    v2 = (v * np.float32(1.2) + np.float32(0.05)).astype(np.float32)
+    blas.refit(v2, nrm)
+    tlas = H.TopLevelAccelerationStructure([blas], ctx)
+    data, nd = mesh_oracle_data(v2, tri, nrm)
+    osc = OracleScene(orc, [(MESH, data, nd)])
+    fr, rgba, hits, o = render_both(ctx, tlas, osc, 128, 96, spp=1, shading=2)
+    st, px_ok, diff = frame_checks(rgba, hits, o, 1)
+    assert st["hits"] > 1000 and st["agreement"] >= AGREE and diff[px_ok].max() <= RGB_ABS

@@ -78,6 +78,7 @@ SIGNATURES = {
     "hrt_blas_input_default": (None, [ctypes.POINTER(BLASInputC)]),
     "hrt_blas_build": (c_i32, [c_p, ctypes.POINTER(BLASInputC), c_p, ctypes.POINTER(c_p)]),
     "hrt_blas_destroy": (c_i32, [c_p]),
+    "hrt_blas_refit": (c_i32, [c_p, c_p, c_p, c_i32, c_p]),
     "hrt_blas_type": (c_i32, [c_p]),
     "hrt_blas_transform": (c_i32, [c_p, c_p]),
     "hrt_blas_get_info": (c_i32, [c_p, ctypes.POINTER(BLASInfoC)]),
@@ -280,6 +281,16 @@ class BottomLevelAccelerationStructure:
 
     def Structure(self):
         return self.handle
+
+    def refit(self, vertices: np.ndarray, per_vertex: np.ndarray | None = None, stream: int | None = None):
+        """hrt_blas_refit: new vertex positions (and radii or normals when the build had them)."""
+        v = np.ascontiguousarray(vertices, dtype=np.float32)
+        pv = None if per_vertex is None else np.ascontiguousarray(per_vertex, dtype=np.float32)
+        self.ctx.check(self.ctx.lib.hrt_blas_refit(self.handle, _ptr(v), _ptr(pv), 0, c_p(stream) if stream else None))
+        info = BLASInfoC()
+        self.ctx.check(self.ctx.lib.hrt_blas_get_info(self.handle, ctypes.byref(info)))
+        self.info = {k: getattr(info, k) for k, _ in BLASInfoC._fields_}
+        self.info["bounds"] = list(info.bounds)
 
     def Type(self) -> BLASType:
         return BLASType(self.ctx.lib.hrt_blas_type(self.handle))

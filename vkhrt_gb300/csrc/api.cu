@@ -29,7 +29,26 @@ struct hrt_blas {
     float build_ms = 0.0f;
     bool keep = false;
     BuildOutput out;
+    // the topology, kept on the host for hrt_blas_refit
+    uint32_t max_leaf = 1, quant_chunk = 0;
+    uint64_t nvertices = 0, nstrands = 0;
+    float const_radius = 0.0f;
+    bool has_radius = false, has_normals = false;
+    std::vector<uint32_t> line_off, vert_off, line_idx, tri_idx;
 };
+
+namespace {
+// Host copy of n uint32 values from host or device memory.
+bool copy_u32(const uint32_t* src, uint64_t n, int32_t memory, std::vector<uint32_t>& dst) {
+    dst.resize(n);
+    if (!n) return true;
+    if (memory == HRT_MEMORY_HOST) {
+        memcpy(dst.data(), src, n * 4);
+        return true;
+    }
+    return cudaMemcpy(dst.data(), src, n * 4, cudaMemcpyDeviceToHost) == cudaSuccess;
+}
+}  // namespace
 
 struct hrt_tlas {
     hrt_context* ctx = nullptr;
@@ -419,6 +438,13 @@ static hrt_status build_mesh(hrt_context* ctx, const hrt_blas_input* in, cudaStr
     b->nprims = n;
     b->keep = (in->flags & HRT_BUILD_KEEP_INTERMEDIATE) != 0;
     memcpy(b->transform, in->transform, sizeof(b->transform));
+    b->max_leaf = max_leaf;
+    b->nvertices = in->nvertices;
+    b->has_normals = in->normals != nullptr;
+    if (!copy_u32(in->tri_indices, 3 * n, in->memory, b->tri_idx)) {
+        delete b;
+        return fail(ctx, HRT_ERR_CUDA, "hrt_blas_build: read triangle indices");
+    }
     float *dv = nullptr, *dn = nullptr, *tris = nullptr, *tnrm = nullptr;
     uint32_t* didx = nullptr;
     const bool host = in->memory == HRT_MEMORY_HOST;
@@ -551,6 +577,18 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
     b->nprims = nlines;
     b->keep = (in->flags & HRT_BUILD_KEEP_INTERMEDIATE) != 0;
     memcpy(b->transform, in->transform, sizeof(b->transform));
+    b->max_leaf = max_leaf;
+    b->quant_chunk = in->quant_chunk;
+    b->nvertices = in->nvertices;
+    b->nstrands = in->nstrands;
+    b->const_radius = in->const_radius;
+    b->has_radius = in->radius != nullptr;
+    b->line_off = line_off;
+    b->vert_off = vert_off;
+    if (in->line_indices && !copy_u32(in->line_indices, 2 * nlines, in->memory, b->line_idx)) {
+        delete b;
+        return fail(ctx, HRT_ERR_CUDA, "hrt_blas_build: read line indices");
+    }
 
     // ---- device copies of the inputs ------------------------------------------------------------
     float *dv = nullptr, *dr = nullptr, *lines = nullptr, *lrad = nullptr;
@@ -634,6 +672,94 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
     cudaEventDestroy(e1);
     cleanup();
     *out = b;
+    return HRT_OK;
+}
+
+hrt_status hrt_blas_refit(hrt_blas* b, const float* vertices, const float* per_vertex, int32_t memory, void* stream) {
+    if (!b) return HRT_ERR_INVALID_ARG;
+    hrt_context* ctx = b->ctx;
+    const bool mesh = b->type == HRT_BLAS_MESH;
+    const bool want = mesh ? b->has_normals : b->has_radius;
+    if (b->nvertices && !vertices) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_refit: null vertices");
+    if (want != (per_vertex != nullptr))
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_refit: %s %s as at the build", mesh ? "normals" : "radii",
+                    want ? "are required" : "must be null");
+    if (memory != HRT_MEMORY_HOST && memory != HRT_MEMORY_DEVICE)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_refit: unknown memory kind %d", memory);
+    if (b->nprims == 0) return HRT_OK;
+    DeviceSet ds(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const uint64_t n = b->nprims, nv = b->nvertices;
+    const int per = mesh ? 3 : 1;  // floats per vertex of per_vertex
+    float *dv = nullptr, *dp = nullptr, *g0 = nullptr, *g1 = nullptr;
+    uint32_t *d0 = nullptr, *d1 = nullptr;
+    const bool host = memory == HRT_MEMORY_HOST;
+    auto cleanup = [&]() {
+        if (host) {
+            if (dv) cudaFree(dv);
+            if (dp) cudaFree(dp);
+        }
+        void* p[] = {g0, g1, d0, d1};
+        for (void* q : p)
+            if (q) cudaFree(q);
+    };
+    cudaError_t e = cudaSuccess;
+    if (host) {
+        e = cudaMalloc(&dv, nv * 12);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dv, vertices, nv * 12, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && per_vertex) e = cudaMalloc(&dp, nv * 4 * per);
+        if (e == cudaSuccess && per_vertex) e = cudaMemcpyAsync(dp, per_vertex, nv * 4 * per, cudaMemcpyHostToDevice, s);
+    } else {
+        dv = const_cast<float*>(vertices);
+        dp = const_cast<float*>(per_vertex);
+    }
+    BuildInput bi{b->type, b->precision, int(b->max_leaf), b->quant_chunk, nullptr, nullptr, n, b->keep};
+    if (mesh) {
+        if (e == cudaSuccess) e = cudaMalloc(&d0, n * 12);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d0, b->tri_idx.data(), n * 12, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMalloc(&g0, n * 36);
+        if (e == cudaSuccess && dp) e = cudaMalloc(&g1, n * 36);
+        if (e == cudaSuccess) e = make_tris(dv, dp, d0, n, g0, g1, s);
+        bi.tris = g0;
+        bi.tri_normals = g1;
+    } else {
+        if (b->line_idx.empty()) {
+            if (e == cudaSuccess) e = cudaMalloc(&d0, b->line_off.size() * 4);
+            if (e == cudaSuccess) e = cudaMalloc(&d1, b->vert_off.size() * 4);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d0, b->line_off.data(), b->line_off.size() * 4, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d1, b->vert_off.data(), b->vert_off.size() * 4, cudaMemcpyHostToDevice, s);
+        } else {
+            if (e == cudaSuccess) e = cudaMalloc(&d0, n * 8);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(d0, b->line_idx.data(), n * 8, cudaMemcpyHostToDevice, s);
+        }
+        if (e == cudaSuccess) e = cudaMalloc(&g0, n * 24);
+        if (e == cudaSuccess) e = cudaMalloc(&g1, n * 8);
+        if (e == cudaSuccess)
+            e = b->line_idx.empty() ? make_lines(dv, dp, b->const_radius, d0, d1, b->nstrands, nullptr, n, g0, g1, s)
+                                    : make_lines(dv, dp, b->const_radius, nullptr, nullptr, 0, d0, n, g0, g1, s);
+        bi.lines = g0;
+        bi.lrad = g1;
+    }
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(ctx, e, "hrt_blas_refit");
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    char msg[256] = {0};
+    e = refit_blas_device(bi, b->out, s, msg, sizeof(msg));
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&b->build_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cleanup();
+    if (e == cudaErrorInvalidValue) return fail(ctx, HRT_ERR_UNSUPPORTED, "%s", msg);
+    if (e != cudaSuccess) return fail(ctx, HRT_ERR_CUDA, "%s", msg[0] ? msg : cudaGetErrorString(e));
     return HRT_OK;
 }
 

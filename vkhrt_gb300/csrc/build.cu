@@ -853,6 +853,89 @@ void free_build_output(BuildOutput& o) {
         }                                                                                      \
     } while (0)
 
+// Geometry processing shared by build and refit: per-segment boxes into `boxes`, the
+// intersected geometry into out.curves / out.geom and, for quantised Phantom, the chunk roots
+// into out.roots (each allocated when null; a refit reuses them) with the chunk map in g.
+struct GeomTmp {
+    float* rad_for_boxes = nullptr;  // Phantom radii used for the boxes
+    float* dq = nullptr;             // dequantised curves (quantised Phantom)
+    uint32_t* chunk_incl = nullptr;
+    uint32_t* keys_tmp = nullptr;
+    void release(cudaStream_t s) {
+        void* p[] = {rad_for_boxes, dq, chunk_incl, keys_tmp};
+        for (void* q : p)
+            if (q) cudaFreeAsync(q, s);
+        *this = GeomTmp{};
+    }
+};
+cudaError_t geometry_stage(const BuildInput& in, BuildOutput& out, float* boxes, GeomTmp& g, cudaStream_t s,
+                           char* msg, size_t msglen) {
+    const uint64_t n = in.n;
+    const unsigned T = 256;
+    uint64_t nchunks = 0;
+    if (in.type == HRT_BLAS_PHANTOM) {
+        if (!out.curves) HRT_CK(cudaMalloc(&out.curves, n * 12 * sizeof(float)));
+        curves_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, n, out.curves);
+        HRT_CK(cudaGetLastError());
+        if (in.precision == HRT_PRECISION_QUANTISED) {
+            uint32_t chunk = in.quant_chunk ? in.quant_chunk : 256u;
+            if (chunk > 256u) chunk = 256u;
+            uint32_t *runpos, *runstart, *flags, *total;
+            HRT_CK(dalloc(&runpos, n, s));
+            HRT_CK(dalloc(&runstart, n, s));
+            HRT_CK(dalloc(&flags, n, s));
+            HRT_CK(dalloc(&g.chunk_incl, n, s));
+            HRT_CK(dalloc(&total, 1, s));
+            run_flags_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, n, runpos);
+            HRT_CK(device_scan<MaxOp>(runpos, runstart, n, true, nullptr, s));
+            chunk_flags_kernel<<<grid_for(n, T), T, 0, s>>>(runstart, n, chunk, flags);
+            HRT_CK(device_scan<SumOp>(flags, g.chunk_incl, n, true, total, s));
+            uint32_t h_total = 0;
+            HRT_CK(cudaMemcpyAsync(&h_total, total, 4, cudaMemcpyDeviceToHost, s));
+            HRT_CK(cudaStreamSynchronize(s));
+            nchunks = h_total;
+            if (nchunks >= (1ull << 24)) {
+                snprintf(msg, msglen, "quantised Phantom BLAS needs %llu chunk roots; the limit is 2^24",
+                         (unsigned long long)nchunks);
+                return cudaErrorInvalidValue;
+            }
+            if (out.roots && nchunks != out.nroots) {
+                snprintf(msg, msglen, "refit: the strands' chunks changed (%llu roots, built with %llu)",
+                         (unsigned long long)nchunks, (unsigned long long)out.nroots);
+                return cudaErrorInvalidValue;
+            }
+            if (!out.roots) HRT_CK(cudaMalloc(&out.roots, nchunks * sizeof(float4)));
+            out.nroots = nchunks;
+            chunk_roots_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, flags, g.chunk_incl, n, out.roots);
+            HRT_CK(dalloc(&g.dq, n * 12, s));
+            HRT_CK(dalloc(&g.rad_for_boxes, n * 2, s));
+            HRT_CK(dalloc(&g.keys_tmp, n, s));
+            dequant_curves_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, in.lrad, g.chunk_incl, out.roots, n, g.dq,
+                                                                g.rad_for_boxes, g.keys_tmp);
+            HRT_CK(cudaGetLastError());
+            boxes_phantom_kernel<<<grid_for(n, T), T, 0, s>>>(g.dq, g.rad_for_boxes, n, boxes);
+            cudaFreeAsync(runpos, s);
+            cudaFreeAsync(runstart, s);
+            cudaFreeAsync(flags, s);
+            cudaFreeAsync(total, s);
+        } else {
+            boxes_phantom_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, in.lrad, n, boxes);
+        }
+    } else if (in.type == HRT_BLAS_LSS) {
+        if (!out.geom) HRT_CK(cudaMalloc(&out.geom, n * 8 * sizeof(float)));
+        lss_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, out.geom);
+        boxes_lss_kernel<<<grid_for(n, T), T, 0, s>>>(out.geom, n, boxes);
+    } else if (in.type == HRT_BLAS_MESH) {
+        boxes_tri_kernel<<<grid_for(n, T), T, 0, s>>>(in.tris, n, boxes);
+    } else {
+        if (!out.geom) HRT_CK(cudaMalloc(&out.geom, n * 18 * sizeof(float)));
+        dots_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, out.geom);
+        boxes_dots_kernel<<<grid_for(n, T), T, 0, s>>>(out.geom, n, boxes);
+    }
+    HRT_CK(cudaGetLastError());
+    return cudaSuccess;
+}
+
 cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream_t s, char* msg, size_t msglen) {
     const uint64_t n = in.n;
     const unsigned T = 256;
@@ -863,66 +946,18 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
 
     // ---- geometry processing -> per-segment boxes (and the intersected geometry) ----------------
     HRT_CK(cudaMalloc(&out.prim_boxes, n * 6 * sizeof(float)));
-    float* rad_for_boxes = nullptr;   // Phantom radii used for the boxes
-    float* dq = nullptr;              // dequantised curves (quantised Phantom)
-    uint32_t* chunk_incl = nullptr;
-    uint32_t* keys_tmp = nullptr;
-    uint64_t nchunks = 0;
-    if (in.type == HRT_BLAS_PHANTOM) {
-        HRT_CK(cudaMalloc(&out.curves, n * 12 * sizeof(float)));
-        curves_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, n, out.curves);
-        HRT_CK(cudaGetLastError());
-        if (in.precision == HRT_PRECISION_QUANTISED) {
-            uint32_t chunk = in.quant_chunk ? in.quant_chunk : 256u;
-            if (chunk > 256u) chunk = 256u;
-            uint32_t *runpos, *runstart, *flags, *total;
-            HRT_CK(dalloc(&runpos, n, s));
-            HRT_CK(dalloc(&runstart, n, s));
-            HRT_CK(dalloc(&flags, n, s));
-            HRT_CK(dalloc(&chunk_incl, n, s));
-            HRT_CK(dalloc(&total, 1, s));
-            run_flags_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, n, runpos);
-            HRT_CK(device_scan<MaxOp>(runpos, runstart, n, true, nullptr, s));
-            chunk_flags_kernel<<<grid_for(n, T), T, 0, s>>>(runstart, n, chunk, flags);
-            HRT_CK(device_scan<SumOp>(flags, chunk_incl, n, true, total, s));
-            uint32_t h_total = 0;
-            HRT_CK(cudaMemcpyAsync(&h_total, total, 4, cudaMemcpyDeviceToHost, s));
-            HRT_CK(cudaStreamSynchronize(s));
-            nchunks = h_total;
-            if (nchunks >= (1ull << 24)) {
-                snprintf(msg, msglen, "quantised Phantom BLAS needs %llu chunk roots; the limit is 2^24",
-                         (unsigned long long)nchunks);
-                return cudaErrorInvalidValue;
-            }
-            HRT_CK(cudaMalloc(&out.roots, nchunks * sizeof(float4)));
-            out.nroots = nchunks;
-            chunk_roots_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, flags, chunk_incl, n, out.roots);
-            HRT_CK(dalloc(&dq, n * 12, s));
-            HRT_CK(dalloc(&rad_for_boxes, n * 2, s));
-            HRT_CK(dalloc(&keys_tmp, n, s));
-            dequant_curves_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, in.lrad, chunk_incl, out.roots, n, dq,
-                                                                rad_for_boxes, keys_tmp);
-            HRT_CK(cudaGetLastError());
-            boxes_phantom_kernel<<<grid_for(n, T), T, 0, s>>>(dq, rad_for_boxes, n, out.prim_boxes);
-            cudaFreeAsync(runpos, s);
-            cudaFreeAsync(runstart, s);
-            cudaFreeAsync(flags, s);
-            cudaFreeAsync(total, s);
-        } else {
-            boxes_phantom_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, in.lrad, n, out.prim_boxes);
+    GeomTmp gt;
+    {
+        cudaError_t ge = geometry_stage(in, out, out.prim_boxes, gt, s, msg, msglen);
+        if (ge != cudaSuccess) {
+            gt.release(s);
+            return ge;
         }
-    } else if (in.type == HRT_BLAS_LSS) {
-        HRT_CK(cudaMalloc(&out.geom, n * 8 * sizeof(float)));
-        lss_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, out.geom);
-        boxes_lss_kernel<<<grid_for(n, T), T, 0, s>>>(out.geom, n, out.prim_boxes);
-    } else if (in.type == HRT_BLAS_MESH) {
-        boxes_tri_kernel<<<grid_for(n, T), T, 0, s>>>(in.tris, n, out.prim_boxes);
-    } else {
-        HRT_CK(cudaMalloc(&out.geom, n * 18 * sizeof(float)));
-        dots_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, out.geom);
-        boxes_dots_kernel<<<grid_for(n, T), T, 0, s>>>(out.geom, n, out.prim_boxes);
     }
-    HRT_CK(cudaGetLastError());
+    float* rad_for_boxes = gt.rad_for_boxes;
+    float* dq = gt.dq;
+    uint32_t* chunk_incl = gt.chunk_incl;
+    uint32_t* keys_tmp = gt.keys_tmp;
 
     // ---- Morton codes + sort ----------------------------------------------------------------
     uint32_t* ob;
@@ -983,8 +1018,10 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     uint32_t root = n == 1 ? kLeafFlag : 0u;
     HRT_CK(cudaMemcpyAsync(lvl_a, &root, 4, cudaMemcpyHostToDevice, s));
     uint32_t count = 1, node_base = 0, next_node_base = 1, prim_base = 0;
+    out.level_start.clear();
     for (int level = 0; count > 0; ++level) {
         if (level > 4096) { snprintf(msg, msglen, "BVH8 collapse did not terminate"); return cudaErrorUnknown; }
+        out.level_start.push_back(node_base);
         collapse_expand_kernel<<<grid_for(count, T), T, 0, s>>>(bv, lvl_a, count, in.max_leaf, kids, nk, nint, nprim);
         HRT_CK(cudaGetLastError());
         HRT_CK(device_scan<SumOp>(nint, int_off, count, false, totals, s));
@@ -1003,6 +1040,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
         std::swap(lvl_a, lvl_b);
     }
     out.nnodes = node_base;
+    out.level_start.push_back(node_base);
     if (prim_base != n) {
         snprintf(msg, msglen, "BVH8 collapse placed %u of %llu primitives", prim_base, (unsigned long long)n);
         return cudaErrorUnknown;
@@ -1071,6 +1109,117 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
                             out.nnodes * (in.precision == HRT_PRECISION_QUANTISED ? sizeof(NodeF) : sizeof(NodeQ)) +
                             n * 8 + n * 4 + (n ? (n - 1) * 32 : 0);
     return cudaSuccess;
+}
+
+// ============================ refit ===============================================================
+// One breadth-first level of the BVH8, deepest first: each slot's box is the union of its leaf
+// primitives' boxes or its child node's box (nbox, written by the level below); the node's own
+// box is the union of its slots. The header (child_base, prim_base, imask, meta) is read from
+// either encoding and copied into the FP32 node written to `outf`.
+__global__ void refit_level_kernel(const void* nodes, int quant, uint32_t first, uint32_t count, const uint32_t* prim_ids,
+                                   const float* boxes, float* nbox, NodeF* outf) {
+    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= count) return;
+    const uint32_t i = first + w;
+    uint32_t cb, pb, im;
+    uint8_t meta[8];
+    if (quant) {
+        const NodeQ& q = static_cast<const NodeQ*>(nodes)[i];
+        cb = q.child_base;
+        pb = q.prim_base;
+        im = q.imask;
+        for (int k = 0; k < 8; ++k) meta[k] = q.meta[k];
+    } else {
+        const NodeF& f = static_cast<const NodeF*>(nodes)[i];
+        cb = f.child_base;
+        pb = f.prim_base;
+        im = f.imask;
+        for (int k = 0; k < 8; ++k) meta[k] = f.meta[k];
+    }
+    const float kInf = __int_as_float(0x7f800000);
+    NodeF nd;
+    float nb[6] = {kInf, kInf, kInf, -kInf, -kInf, -kInf};
+    for (int q = 0; q < 8; ++q) {
+        float b[6] = {kInf, kInf, kInf, -kInf, -kInf, -kInf};
+        const uint32_t m = meta[q];
+        if (m & 0x80u) {
+            const float* c = nbox + 6 * uint64_t(cb + (m & 7u));
+            for (int k = 0; k < 6; ++k) b[k] = c[k];
+        } else if (m) {
+            for (uint32_t j = 0; j < (m >> 5); ++j) {
+                const float* c = boxes + 6 * uint64_t(prim_ids[pb + (m & 31u) + j]);
+                for (int k = 0; k < 3; ++k) { b[k] = fmin_t(b[k], c[k]); b[3 + k] = fmax_t(b[3 + k], c[3 + k]); }
+            }
+        }
+        nd.lo_x[q] = b[0]; nd.lo_y[q] = b[1]; nd.lo_z[q] = b[2];
+        nd.hi_x[q] = b[3]; nd.hi_y[q] = b[4]; nd.hi_z[q] = b[5];
+        nd.meta[q] = meta[q];
+        if (m) for (int k = 0; k < 3; ++k) { nb[k] = fmin_t(nb[k], b[k]); nb[3 + k] = fmax_t(nb[3 + k], b[3 + k]); }
+    }
+    nd.child_base = cb;
+    nd.prim_base = pb;
+    nd.imask = im;
+    nd.pad0 = 0;
+    nd.pad[0] = nd.pad[1] = 0;
+    outf[i] = nd;
+    for (int k = 0; k < 6; ++k) nbox[6 * uint64_t(i) + k] = nb[k];
+}
+
+cudaError_t refit_blas_device(const BuildInput& in, BuildOutput& out, cudaStream_t s, char* msg, size_t msglen) {
+    const uint64_t n = in.n;
+    const unsigned T = 256;
+    if (n == 0) return cudaSuccess;
+    const bool quant = in.precision == HRT_PRECISION_QUANTISED;
+    float* boxes = out.prim_boxes;  // kept for inspection, else a temporary
+    bool own_boxes = false, own_curves = !out.curves, own_geom = !out.geom;
+    if (!boxes) {
+        HRT_CK(dalloc(&boxes, n * 6, s));
+        own_boxes = true;
+    }
+    GeomTmp gt;
+    cudaError_t e = geometry_stage(in, out, boxes, gt, s, msg, msglen);
+    float* nbox = nullptr;
+    NodeF* fn = nullptr;
+    if (e == cudaSuccess) e = dalloc(&nbox, out.nnodes * 6, s);
+    if (e == cudaSuccess) {
+        // FP32 nodes are refitted in place; 8-bit nodes through an FP32 copy, then re-quantised
+        if (quant) e = dalloc(&fn, out.nnodes, s);
+        else fn = static_cast<NodeF*>(out.nodes);
+    }
+    for (size_t L = out.level_start.size() - 1; e == cudaSuccess && L-- > 0;) {
+        const uint32_t first = out.level_start[L], count = out.level_start[L + 1] - first;
+        refit_level_kernel<<<grid_for(count, T), T, 0, s>>>(out.nodes, quant ? 1 : 0, first, count, out.prim_ids, boxes,
+                                                            nbox, fn);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && quant) {
+        quantise_kernel<<<grid_for(out.nnodes, T), T, 0, s>>>(fn, out.nnodes, static_cast<NodeQ*>(out.nodes));
+        if (out.qnodes_aux) e = cudaMemcpyAsync(out.qnodes_aux, fn, out.nnodes * sizeof(NodeF), cudaMemcpyDeviceToDevice, s);
+    } else if (e == cudaSuccess && out.qnodes_aux) {
+        quantise_kernel<<<grid_for(out.nnodes, T), T, 0, s>>>(fn, out.nnodes, static_cast<NodeQ*>(out.qnodes_aux));
+    }
+    if (e == cudaSuccess) {
+        records_kernel<<<grid_for(n, T), T, 0, s>>>(in.type, in.precision, out.prim_ids, n, out.curves, in.lrad,
+                                                    in.type == HRT_BLAS_MESH ? in.tris : out.geom, gt.chunk_incl,
+                                                    out.roots, in.tri_normals, out.prims);
+        e = cudaGetLastError();
+    }
+    float hb[6];
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hb, nbox, 24, cudaMemcpyDeviceToHost, s);  // the root's box
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) memcpy(out.bounds, hb, sizeof(hb));
+    gt.release(s);
+    if (nbox) cudaFreeAsync(nbox, s);
+    if (quant && fn) cudaFreeAsync(fn, s);
+    if (own_boxes) cudaFreeAsync(boxes, s);
+    if (!in.keep_intermediate) {  // the geometry stage's outputs are kept only for inspection
+        if (own_curves && out.curves) { cudaFreeAsync(out.curves, s); out.curves = nullptr; }
+        if (own_geom && out.geom) { cudaFreeAsync(out.geom, s); out.geom = nullptr; }
+    }
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess && !msg[0]) snprintf(msg, msglen, "refit: %s", cudaGetErrorString(e));
+    return e;
 }
 
 // Expands DOTS frames into the reference's 12 vertices per segment (inspection only).

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "hrt.h"
 
 namespace hrt {
@@ -164,9 +166,14 @@ struct BuildOutput {
     uint32_t* prim_order = nullptr;
     uint64_t nnodes = 0, nroots = 0, node_bytes = 0, prim_bytes = 0, device_bytes = 0;
     float bounds[6] = {0, 0, 0, 0, 0, 0};
+    std::vector<uint32_t> level_start;  // first node of each breadth-first level, then nnodes
 };
 // Runs the whole device build; returns a CUDA error or cudaSuccess; msg gets a reason.
 cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream_t s, char* msg, size_t msglen);
+// Moves a built BLAS to new geometry of the same topology (in.n segments or triangles): boxes,
+// records and the BVH8 node boxes (refitted bottom-up, level by level) are recomputed; the
+// tree's topology and leaf order are kept.
+cudaError_t refit_blas_device(const BuildInput& in, BuildOutput& out, cudaStream_t s, char* msg, size_t msglen);
 void free_build_output(BuildOutput& out);
 cudaError_t expand_dots(const float* geom, uint64_t n, float* out36, cudaStream_t s);
 // Line generation from vertices (device pointers); see hrt_blas_input.
