@@ -644,7 +644,11 @@ def c4_summary(args, ctx):
         ms = time_frames(ctx, tlas, cam, fr, p, max(8, args.steps // 2), args.warmup)
         out[name] = {"value": round((st["primary_rays"] + st["shadow_rays"]) / (ms * 1e-3) / 1e6, 3),
                      "ms_per_step": round(ms, 3), "nodes_visited": int(st["nodes_visited"]),
-                     "prims_tested": int(st["prims_tested"])}
+                     "prims_tested": int(st["prims_tested"]), "blas_build_ms": round(blas.info["build_ms"], 2)}
+        # animated strands: the same BLAS refitted to moved vertices (topology kept)
+        v2 = (v + np.float32(0.01) * np.sin(np.float32(3.0) * v[:, [1, 2, 0]])).astype(np.float32)
+        blas.refit(v2, r)
+        out[name]["blas_refit_ms"] = round(blas.info["build_ms"], 2)
         del fr, tlas, blas
     return out
 
