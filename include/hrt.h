@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HRT_ABI_VERSION 3
+#define HRT_ABI_VERSION 4
 
 typedef enum hrt_status {
     HRT_OK = 0,
@@ -161,6 +161,12 @@ typedef struct hrt_trace_params {
     uint32_t refill;         /* idle lanes of a warp that trigger a work fetch, 1..32 (0 = 16; default 8) */
     uint32_t speculative;    /* lanes that hold a leaf keep traversing while others search (0/1; default 1) */
     uint32_t split_types;    /* batches: one persistent launch per primitive type instead of one for all (0/1) */
+    /* Environment map for primary rays that miss (miss.rmiss:17-37), or NULL for the constant black
+     * background: device float4 RGBA texels, env_height rows of env_width, equirectangular, row 0 at
+     * v = 0; sampled bilinearly (u repeats, v clamps to the edge rows), then 1 - exp(-c) and gamma
+     * 1/2.2 as the reference's miss shader. */
+    const float* env_map;
+    uint32_t env_width, env_height;
 } hrt_trace_params;
 
 typedef struct hrt_hit {

@@ -80,7 +80,7 @@ def load() -> ctypes.CDLL:
         "orc_scene_add_instance": (i32, [P, i32, P]),
         "orc_trace_rays": (None, [P, P, i64, f32, f32, i32, i32, P, P, P, P]),
         "orc_render": (None, [P, P, P, u32, u32, u32, i32, u32, f32, f32, i32, f32, i32, i32, i64, i64,
-                              P, P, P, P, P, P]),
+                              P, P, P, P, P, P, P, u32, u32]),
         "orc_hardware_threads": (i32, []),
         "orc_resolve_stats": (None, [P, i32]),
     }

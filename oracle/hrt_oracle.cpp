@@ -1280,10 +1280,37 @@ void orc_trace_rays(void* s, const float* rays, int64_t n, float tmin, float tma
 // Pixels: first_pixel .. first_pixel + npixels - 1, or pixel_list[0 .. npixels-1] when given.
 // Per-sample outputs (npixels*spp): t (double, -1 miss), prim, inst, shadow flag;
 // framebuffer npixels*4 floats (RGBA, A = 1), averaged over samples in sample order.
+// miss.rmiss:17-37: the environment along -d (equirectangular DirectionToUV), bilinear with u
+// repeating and v clamped to the edge rows (texel centres at (i + 0.5) / size), then
+// 1 - exp(-c) and gamma 1/2.2. env: RGBA float texels, ew x eh, row 0 at v = 0.
+extern "C++" template <class T>
+void env_color(const float* env, uint32_t ew, uint32_t eh, const T d[3], T out[3]) {
+    T n = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    T v[3] = {-d[0] / n, -d[1] / n, -d[2] / n};
+    const T k1OverPi = T(0.3183098861837);
+    T gamma = std::asin(std::min(std::max(v[1], T(-1)), T(1))), theta = std::atan2(v[0], -v[2]);
+    T u = theta * k1OverPi * T(0.5) + T(0.5), vv = gamma * k1OverPi + T(0.5);
+    T x = u * T(ew) - T(0.5), y = vv * T(eh) - T(0.5);
+    T fx = std::floor(x), fy = std::floor(y), ax = x - fx, ay = y - fy;
+    int64_t x0 = int64_t(fx) % int64_t(ew);
+    if (x0 < 0) x0 += ew;
+    int64_t x1 = (x0 + 1) % int64_t(ew);
+    int64_t y0 = std::min<int64_t>(std::max<int64_t>(int64_t(fy), 0), eh - 1);
+    int64_t y1 = std::min<int64_t>(std::max<int64_t>(int64_t(fy) + 1, 0), eh - 1);
+    for (int k = 0; k < 3; ++k) {
+        T c00 = env[4 * (y0 * ew + x0) + k], c10 = env[4 * (y0 * ew + x1) + k];
+        T c01 = env[4 * (y1 * ew + x0) + k], c11 = env[4 * (y1 * ew + x1) + k];
+        T a = c00 + ax * (c10 - c00), b = c01 + ax * (c11 - c01);
+        T c = a + ay * (b - a);
+        out[k] = std::pow(T(1) - std::exp(-c), T(1) / T(2.2));
+    }
+}
+
 void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t w, uint32_t h, uint32_t spp,
                 int jitter, uint32_t seed, float tmin, float tmax, int shading, float shadow_tmin, int precision,
                 int nthreads, int64_t first_pixel, int64_t npixels, const uint32_t* pixel_list, double* t_out,
-                uint32_t* prim_out, uint32_t* inst_out, uint8_t* shadow_out, float* fb) {
+                uint32_t* prim_out, uint32_t* inst_out, uint8_t* shadow_out, float* fb, const float* env,
+                uint32_t env_w, uint32_t env_h) {
     const Scene& sc = *static_cast<Scene*>(s);
     parallel_for(npixels, nthreads, [&](int64_t pi) {
         int64_t p = pixel_list ? int64_t(pixel_list[pi]) : first_pixel + pi;
@@ -1325,6 +1352,9 @@ void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t 
                         tvec3<double> c3 = lit ? shade(hh.n) : tvec3<double>(0.3f, 0.3f, 0.3f);
                         col[0] = c3.x; col[1] = c3.y; col[2] = c3.z;
                     }
+                } else if (env) {
+                    const double dv[3] = {double(d[0]), double(d[1]), double(d[2])};
+                    env_color(env, env_w, env_h, dv, col);
                 }
                 for (int c = 0; c < 3; ++c) acc[c] += col[c];
             } else {
@@ -1349,6 +1379,8 @@ void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t 
                         v3f c3 = lit ? shade(hh.n) : v3f(0.3f, 0.3f, 0.3f);
                         cf[0] = c3.x; cf[1] = c3.y; cf[2] = c3.z;
                     }
+                } else if (env) {
+                    env_color(env, env_w, env_h, d, cf);
                 }
                 for (int c = 0; c < 3; ++c) accf[c] += cf[c];
             }

@@ -95,7 +95,8 @@ class OracleScene:
         return t, prim, inst, nrm
 
     def render(self, view_inv, proj_inv, w, h, spp=1, jitter=0, seed=0, shading=2, precision=64, tmin=0.001,
-               tmax=10000.0, shadow_tmin=1e-4, threads: int = 0, first_pixel=0, npixels=None, pixel_list=None):
+               tmax=10000.0, shadow_tmin=1e-4, threads: int = 0, first_pixel=0, npixels=None, pixel_list=None,
+               env=None):
         if pixel_list is not None:
             pixel_list = np.ascontiguousarray(pixel_list, np.uint32)
             npixels = len(pixel_list)
@@ -108,8 +109,10 @@ class OracleScene:
         th = threads or max(1, self.orc.orc_hardware_threads())
         vi = np.ascontiguousarray(view_inv, np.float32)
         pi = np.ascontiguousarray(proj_inv, np.float32)
+        e = None if env is None else np.ascontiguousarray(env, np.float32)
+        eh, ew = (0, 0) if e is None else e.shape[:2]
         self.orc.orc_render(self.h, P(vi), P(pi), w, h, spp, jitter, seed, tmin, tmax, shading, shadow_tmin, precision,
-                            th, first_pixel, npx, P(pixel_list), P(t), P(prim), P(inst), P(sh), P(fb))
+                            th, first_pixel, npx, P(pixel_list), P(t), P(prim), P(inst), P(sh), P(fb), P(e), ew, eh)
         return dict(t=t, prim=prim, inst=inst, shadow=sh, fb=fb)
 
     def __del__(self):

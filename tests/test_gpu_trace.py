@@ -423,3 +423,26 @@ def test_mesh_refit_trace(ctx, orc):
     fr, rgba, hits, o = render_both(ctx, tlas, osc, 128, 96, spp=1, shading=2)
     st, px_ok, diff = frame_checks(rgba, hits, o, 1)
     assert st["hits"] > 1000 and st["agreement"] >= AGREE and diff[px_ok].max() <= RGB_ABS
+
+
+def test_environment_map_miss_shading(ctx, orc):
+    """Primary rays that miss take the environment map's colour (miss.rmiss:17-37): equal to the
+    oracle's within the RGB bar, with hits unchanged."""
+    import torch
+    blas, tlas, osc, _ = make_scene(ctx, orc, PHANTOM, 0, seed=34, ns=500, nv=24)
+    rng = np.random.default_rng(35)
+    env = rng.uniform(0.0, 3.0, (32, 64, 4)).astype(np.float32)
+    denv = torch.as_tensor(env).cuda()
+    w, h = 160, 120
+    cam = H.scene_camera(w, h)
+    vi, pi = H.camera_arrays(cam)
+    fr = H.Frame(ctx, w, h, 2, with_hits=True)
+    H.trace(ctx, tlas, cam, fr, H.trace_params(spp=2, shading=2, jitter=1, seed=3, record_hits=1,
+                                               env_map=denv.data_ptr(), env_width=64, env_height=32))
+    rgba, hits = fr.download(hits=True)
+    o = osc.render(vi, pi, w, h, spp=2, jitter=1, seed=3, shading=2, precision=64, env=env)
+    st, px_ok, diff = frame_checks(rgba, hits, o, 2)
+    miss_px = (hits["t"].reshape(-1, 2) < 0).all(axis=1)
+    assert miss_px.sum() > 1000 and st["agreement"] >= AGREE
+    assert diff[px_ok].max() <= RGB_ABS
+    assert rgba.reshape(-1, 4)[miss_px, :3].min() > 0.05  # the background is the map, not black

@@ -211,3 +211,24 @@ def test_mesh_triangle_known_answer(orc):
     boxes = np.zeros((1, 6), np.float32)
     orc.orc_prim_boxes(3, P(tri), None, 1, P(boxes))
     assert boxes.tolist() == [[0, 0, 1, 1, 1, 1]]
+
+
+def test_environment_map_miss(orc):
+    """miss.rmiss:17-37 on an empty scene: a constant map gives 1 - exp(-c) under gamma 1/2.2;
+    a map that varies only in u shows the direction -> (u, v) mapping and the bilinear blend."""
+    from hairscene import OracleScene
+    import vkhrt_gb300 as H
+    osc = OracleScene(orc, [(0, np.zeros((0, 12), np.float32), np.zeros((0, 2), np.float32))])
+    cam = H.scene_camera(8, 6)
+    vi, pi = H.camera_arrays(cam)
+    env = np.full((4, 8, 4), 0.7, np.float32)
+    o = osc.render(vi, pi, 8, 6, shading=2, precision=64, env=env)
+    expect = (1.0 - np.exp(-0.7)) ** (1.0 / 2.2)
+    assert np.allclose(o["fb"][:, :3], expect, atol=1e-6) and np.all(o["t"] == -1.0)
+    # the camera looks down -z, so -d points to +z: theta = atan2(x, -z) = +-pi -> u at the seam
+    ramp = np.zeros((4, 8, 4), np.float32)
+    ramp[:, :, 0] = np.arange(8)[None, :]
+    o2 = osc.render(vi, pi, 8, 6, shading=2, precision=64, env=ramp)
+    centre = o2["fb"].reshape(6, 8, 4)[3, 4, 0]
+    c_lin = -np.log(1.0 - centre ** 2.2)  # undo the tone map
+    assert 0.0 <= c_lin <= 7.0  # a blend of the ramp's texels around the seam (u = 0 / 1)

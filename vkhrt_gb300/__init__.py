@@ -47,7 +47,8 @@ class TraceParamsC(ctypes.Structure):
     _fields_ = [("tmin", c_f), ("tmax", c_f), ("spp", c_u32), ("jitter", c_u32), ("seed", c_u32),
                 ("shading", c_u32), ("shadow_tmin", c_f), ("fp64_resolve", c_u32), ("record_hits", c_u32),
                 ("async_", c_u32), ("count_stats", c_u32), ("kernel_variant", c_u32), ("refill", c_u32),
-                ("speculative", c_u32), ("split_types", c_u32)]
+                ("speculative", c_u32), ("split_types", c_u32), ("env_map", c_p), ("env_width", c_u32),
+                ("env_height", c_u32)]
 
 
 class FrameStatsC(ctypes.Structure):

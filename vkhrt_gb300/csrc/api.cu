@@ -262,6 +262,10 @@ TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32
     L.resolve_scratch = scratch;
     L.scratch_cap = scratch ? scratch_cap : 0;
     L.max_spp = max_spp ? max_spp : 1;
+    const bool env = p->env_map && p->env_width && p->env_height;
+    L.env_map = env ? reinterpret_cast<const float4*>(p->env_map) : nullptr;
+    L.env_w = env ? p->env_width : 0;
+    L.env_h = env ? p->env_height : 0;
     return L;
 }
 

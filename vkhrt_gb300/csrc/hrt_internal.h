@@ -123,6 +123,8 @@ struct TraceLaunch {
     float4* resolve_scratch;
     uint64_t scratch_cap;  // samples
     uint32_t max_spp;      // over the scenes of the launch
+    const float4* env_map; // miss shading (or null)
+    uint32_t env_w, env_h;
 };
 
 // ---- launch wrappers (trace.cu) --------------------------------------------------------------

@@ -805,6 +805,31 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
     return n;
 }
 
+// miss.rmiss:17-37: the environment seen along -d (the map is inverted), equirectangular
+// (DirectionToUV), bilinear with u repeating and v clamped, then 1 - exp(-c) and gamma 1/2.2.
+__device__ V3<float> env_color(const float4* env, uint32_t w, uint32_t h, V3<float> d) {
+    const V3<float> v = normalize_rn(mk(-d.x, -d.y, -d.z));
+    const float k1OverPi = 0.3183098861837f;  // M_1_OVER_PI of the shader
+    const float gamma = asinf(fminf(fmaxf(v.y, -1.0f), 1.0f)), theta = atan2f(v.x, -v.z);
+    const float u = fmaf(theta * k1OverPi, 0.5f, 0.5f), vv = fmaf(gamma, k1OverPi, 0.5f);
+    // texel centres at (i + 0.5) / w
+    const float x = fmaf(u, float(w), -0.5f), y = fmaf(vv, float(h), -0.5f);
+    const float fx = floorf(x), fy = floorf(y);
+    const float ax = x - fx, ay = y - fy;
+    int x0 = int(fx) % int(w);
+    if (x0 < 0) x0 += int(w);
+    const int x1 = (x0 + 1) % int(w);
+    const int y0 = min(max(int(fy), 0), int(h) - 1), y1 = min(max(int(fy) + 1, 0), int(h) - 1);
+    const float4 c00 = __ldg(env + size_t(y0) * w + x0), c10 = __ldg(env + size_t(y0) * w + x1);
+    const float4 c01 = __ldg(env + size_t(y1) * w + x0), c11 = __ldg(env + size_t(y1) * w + x1);
+    auto lerp = [](float a, float b, float t) { return fmaf(t, b - a, a); };
+    float c[3] = {lerp(lerp(c00.x, c10.x, ax), lerp(c01.x, c11.x, ax), ay),
+                  lerp(lerp(c00.y, c10.y, ax), lerp(c01.y, c11.y, ax), ay),
+                  lerp(lerp(c00.z, c10.z, ax), lerp(c01.z, c11.z, ax), ay)};
+    for (int k = 0; k < 3; ++k) c[k] = powf(1.0f - expf(-c[k]), 1.0f / 2.2f);
+    return mk(c[0], c[1], c[2]);
+}
+
 // ray_gen.rgen:18-24, every operation rounded separately (matches the CPU restatement).
 __device__ void raygen(const float* V, const float* P, uint32_t px, uint32_t py, uint32_t w, uint32_t hgt, float jx,
                        float jy, V3<float>* o, V3<float>* d) {
@@ -990,7 +1015,16 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 r.flags = found ? h.flags : 0u;
                 S.hits[rec] = r;
             }
-            if (!found) { next_sample(); return; }
+            if (!found) {
+                if (L.env_map) {
+                    const V3<float> c = env_color(L.env_map, L.env_w, L.env_h, wd);
+                    acc0 = __fadd_rn(acc0, c.x);
+                    acc1 = __fadd_rn(acc1, c.y);
+                    acc2 = __fadd_rn(acc2, c.z);
+                }
+                next_sample();
+                return;
+            }
             if (L.shading == HRT_SHADE_DEBUG) {
                 uint32_t c = h.id % 6u;
                 acc0 = __fadd_rn(acc0, kPalette[c][0]);
