@@ -446,3 +446,32 @@ def test_environment_map_miss_shading(ctx, orc):
     assert miss_px.sum() > 1000 and st["agreement"] >= AGREE
     assert diff[px_ok].max() <= RGB_ABS
     assert rgba.reshape(-1, 4)[miss_px, :3].min() > 0.05  # the background is the map, not black
+
+
+def test_gltf_model_builds_and_traces(ctx, tmp_path):
+    """Primitives read from a glTF file build BLASes (hair lines with their radii and node
+    transform, a triangle mesh) whose hits equal a build from the same arrays."""
+    import json
+    from test_gltf import _doc_and_blob
+    from vkhrt_gb300 import gltf
+    doc, blob, e = _doc_and_blob(False, True)
+    doc["buffers"][0]["uri"] = "m.bin"
+    (tmp_path / "m.bin").write_bytes(blob)
+    (tmp_path / "m.gltf").write_text(json.dumps(doc))
+    prims = gltf.load(str(tmp_path / "m.gltf"))
+    blases = [H.BottomLevelAccelerationStructure(p.blas_input(H.BLASType.ePhantom), ctx) for p in prims]
+    tlas = H.TopLevelAccelerationStructure(blases, ctx)
+    direct = [H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=e["sv"], radius=e["rad"],
+                                                             line_indices=e["pairs"][0], transform=e["hair_w"]), ctx),
+              H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.eMesh, vertices=e["mv"], tri_indices=e["tri"],
+                                                             normals=e["mn"], transform=e["mesh_w"]), ctx)]
+    tlas2 = H.TopLevelAccelerationStructure(direct, ctx)
+    rng = np.random.default_rng(21)
+    tgt = np.concatenate([(e["hair_w"] @ np.c_[e["sv"], np.ones(10)].T).T[:, :3],
+                          (e["mesh_w"] @ np.c_[e["mv"], np.ones(4)].T).T[:, :3]])
+    tgt = tgt[rng.integers(0, len(tgt), 4000)] + rng.normal(size=(4000, 3)) * 0.02
+    d = rng.normal(size=(4000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([tgt - 2.0 * d, d], axis=1).astype(np.float32)
+    a, b = H.trace_rays(ctx, tlas, rays), H.trace_rays(ctx, tlas2, rays)
+    assert (a["t"] >= 0).sum() > 200 and np.array_equal(a, b)
