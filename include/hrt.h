@@ -209,6 +209,13 @@ hrt_status hrt_blas_destroy(hrt_blas* blas);
  * motions (build anew then). TLASes that hold the BLAS must be built again afterwards (they
  * copy its bounds). No counterpart in the reference (it builds once). */
 hrt_status hrt_blas_refit(hrt_blas* blas, const float* vertices, const float* per_vertex, int32_t memory, void* stream);
+/* A built BLAS as bytes (host memory): tree, records, roots, slot map and the refit topology.
+ * hrt_blas_deserialize checks the image (header, sizes, every node's child and leaf ranges,
+ * record roots) before anything reaches the device and rejects a corrupt one with
+ * HRT_ERR_INVALID_ARG. No counterpart in the reference (it rebuilds at every start). */
+uint64_t hrt_blas_serialized_size(const hrt_blas* blas);
+hrt_status hrt_blas_serialize(const hrt_blas* blas, void* dst, uint64_t bytes);
+hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t bytes, void* stream, hrt_blas** out);
 int32_t hrt_blas_type(const hrt_blas* blas);
 hrt_status hrt_blas_transform(const hrt_blas* blas, float out[16]);
 hrt_status hrt_blas_get_info(const hrt_blas* blas, hrt_blas_info* out);

@@ -475,3 +475,30 @@ def test_gltf_model_builds_and_traces(ctx, tmp_path):
     rays = np.concatenate([tgt - 2.0 * d, d], axis=1).astype(np.float32)
     a, b = H.trace_rays(ctx, tlas, rays), H.trace_rays(ctx, tlas2, rays)
     assert (a["t"] >= 0).sum() > 200 and np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("gtype,precision", [(PHANTOM, 1), (PHANTOM, 0), (LSS, 1), (DOTS, 0)])
+def test_serialized_blas_traces_identically(ctx, gtype, precision):
+    """serialize -> load gives a BLAS whose hits equal the original's; a loaded BLAS refits; a
+    truncated or corrupt image is refused on the host (nothing reaches the device)."""
+    v, r, off = H.generate_strands(H.StrandParams(seed=15, nstrands=400, nverts=20))
+    blas = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType(gtype), vertices=v, radius=r,
+                                                          strand_offsets=off, precision=H.Precision(precision)), ctx)
+    data = blas.serialize()
+    b2 = H.BottomLevelAccelerationStructure.load(data, ctx)
+    assert b2.info["nnodes"] == blas.info["nnodes"] and b2.info["bounds"] == blas.info["bounds"]
+    lines, _ = lines_from_strands(v, r, off)
+    rays = aimed_rays(np.random.default_rng(16), lines, 8000, spread=0.006)
+    t1, t2 = H.TopLevelAccelerationStructure([blas], ctx), H.TopLevelAccelerationStructure([b2], ctx)
+    assert np.array_equal(H.trace_rays(ctx, t1, rays), H.trace_rays(ctx, t2, rays))
+    v2 = (v + 0.02 * np.sin(4.0 * v)).astype(np.float32)
+    blas.refit(v2, r)
+    b2.refit(v2, r)
+    t1, t2 = H.TopLevelAccelerationStructure([blas], ctx), H.TopLevelAccelerationStructure([b2], ctx)
+    assert np.array_equal(H.trace_rays(ctx, t1, rays), H.trace_rays(ctx, t2, rays))
+    with pytest.raises(H.HrtError):
+        H.BottomLevelAccelerationStructure.load(data[: len(data) // 2], ctx)
+    bad = bytearray(data)
+    bad[:4] = b"XXXX"
+    with pytest.raises(H.HrtError):
+        H.BottomLevelAccelerationStructure.load(bytes(bad), ctx)

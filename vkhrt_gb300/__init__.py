@@ -80,6 +80,9 @@ SIGNATURES = {
     "hrt_blas_build": (c_i32, [c_p, ctypes.POINTER(BLASInputC), c_p, ctypes.POINTER(c_p)]),
     "hrt_blas_destroy": (c_i32, [c_p]),
     "hrt_blas_refit": (c_i32, [c_p, c_p, c_p, c_i32, c_p]),
+    "hrt_blas_serialized_size": (c_u64, [c_p]),
+    "hrt_blas_serialize": (c_i32, [c_p, c_p, c_u64]),
+    "hrt_blas_deserialize": (c_i32, [c_p, c_p, c_u64, c_p, ctypes.POINTER(c_p)]),
     "hrt_blas_type": (c_i32, [c_p]),
     "hrt_blas_transform": (c_i32, [c_p, c_p]),
     "hrt_blas_get_info": (c_i32, [c_p, ctypes.POINTER(BLASInfoC)]),
@@ -282,6 +285,30 @@ class BottomLevelAccelerationStructure:
 
     def Structure(self):
         return self.handle
+
+    def serialize(self) -> bytes:
+        """hrt_blas_serialize: the BLAS as bytes (load with BottomLevelAccelerationStructure.load)."""
+        n = int(self.ctx.lib.hrt_blas_serialized_size(self.handle))
+        buf = np.zeros(n, np.uint8)
+        self.ctx.check(self.ctx.lib.hrt_blas_serialize(self.handle, _ptr(buf), n))
+        return buf.tobytes()
+
+    @classmethod
+    def load(cls, data: bytes, ctx: Context, stream: int | None = None) -> "BottomLevelAccelerationStructure":
+        """hrt_blas_deserialize: a BLAS from serialize()'s bytes (validated before use)."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self._keep = []
+        buf = np.frombuffer(data, np.uint8)
+        h = c_p()
+        ctx.check(ctx.lib.hrt_blas_deserialize(ctx.handle, _ptr(buf), len(buf), c_p(stream) if stream else None,
+                                               ctypes.byref(h)))
+        self.handle = h
+        info = BLASInfoC()
+        ctx.check(ctx.lib.hrt_blas_get_info(h, ctypes.byref(info)))
+        self.info = {k: getattr(info, k) for k, _ in BLASInfoC._fields_}
+        self.info["bounds"] = list(info.bounds)
+        return self
 
     def refit(self, vertices: np.ndarray, per_vertex: np.ndarray | None = None, stream: int | None = None):
         """hrt_blas_refit: new vertex positions (and radii or normals when the build had them)."""

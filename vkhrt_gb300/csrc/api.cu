@@ -783,6 +783,214 @@ hrt_status hrt_blas_transform(const hrt_blas* b, float out[16]) {
     return HRT_OK;
 }
 
+// ---- serialisation --------------------------------------------------------------------------
+// Layout (little-endian): the header below, then level starts (u32), the refit topology
+// (line offsets, vertex offsets, line indices, triangle indices: u32 each, lengths in the
+// header), then the device arrays: nodes, records, roots (float4), slot map (u32).
+namespace {
+struct SerialHeader {
+    char magic[4];  // "HRTB"
+    uint32_t version;
+    int32_t type, precision;
+    uint64_t nprims, nnodes, nroots, node_bytes, prim_bytes;
+    float bounds[6];
+    float transform[16];
+    uint32_t max_leaf, quant_chunk;
+    uint64_t nvertices, nstrands;
+    float const_radius;
+    uint32_t has_radius, has_normals;
+    uint64_t nlevels, n_line_off, n_vert_off, n_line_idx, n_tri_idx;
+};
+constexpr uint32_t kSerialVersion = 1;
+
+uint64_t serial_size(const hrt_blas* b) {
+    const BuildOutput& o = b->out;
+    return sizeof(SerialHeader) +
+           4 * (o.level_start.size() + b->line_off.size() + b->vert_off.size() + b->line_idx.size() + b->tri_idx.size()) +
+           o.nnodes * o.node_bytes + b->nprims * o.prim_bytes + o.nroots * 16 + b->nprims * 4;
+}
+
+// Reads a u32 array of n entries at *p, advancing it; false past the end.
+bool take_u32(const uint8_t*& p, const uint8_t* end, uint64_t n, std::vector<uint32_t>& v) {
+    if (n > uint64_t(end - p) / 4) return false;
+    v.resize(n);
+    if (n) memcpy(v.data(), p, n * 4);
+    p += n * 4;
+    return true;
+}
+
+// Host-side check of a deserialised tree, so that tracing it never reads outside its arrays:
+// internal children below nnodes, leaf runs inside the records, FP16 records' roots in range.
+const char* check_tree(int type, int precision, uint64_t nprims, uint64_t nnodes, uint64_t nroots, const uint8_t* nodes,
+                       const uint8_t* prims, const std::vector<uint32_t>& levels) {
+    const bool quant = precision == HRT_PRECISION_QUANTISED;
+    for (uint64_t i = 0; i < nnodes; ++i) {
+        uint32_t cb, pb;
+        const uint8_t* meta;
+        uint32_t imask;
+        if (quant) {
+            const NodeQ* q = reinterpret_cast<const NodeQ*>(nodes) + i;
+            cb = q->child_base; pb = q->prim_base; meta = q->meta; imask = q->imask;
+        } else {
+            const NodeF* f = reinterpret_cast<const NodeF*>(nodes) + i;
+            cb = f->child_base; pb = f->prim_base; meta = f->meta; imask = f->imask;
+        }
+        uint32_t rank = 0;
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t m = meta[k];
+            if (((imask >> k) & 1u) != ((m & 0x80u) ? 1u : 0u)) return "internal-child mask disagrees with meta";
+            if (m & 0x80u) {
+                if ((m & 0x78u) || (m & 7u) != rank) return "internal children are not ranked in slot order";
+                if (uint64_t(cb) + rank >= nnodes || uint64_t(cb) + rank <= i) return "child index out of range";
+                ++rank;
+            } else if (m) {
+                const uint32_t cnt = m >> 5, off = m & 31u;
+                if (cnt == 0 || cnt > 3 || uint64_t(pb) + off + cnt > nprims) return "leaf run out of range";
+            }
+        }
+    }
+    for (size_t k = 0; k + 1 < levels.size(); ++k)
+        if (levels[k] > levels[k + 1] || levels[k + 1] > nnodes) return "level starts out of order";
+    if (!levels.empty() && levels.back() != nnodes) return "level starts do not end at the node count";
+    if (type == HRT_BLAS_PHANTOM && quant)
+        for (uint64_t i = 0; i < nprims; ++i) {
+            const uint32_t key = reinterpret_cast<const PrimPhantomH*>(prims)[i].q1.w;
+            if ((key >> 8) >= nroots) return "record root out of range";
+        }
+    return nullptr;
+}
+}  // namespace
+
+uint64_t hrt_blas_serialized_size(const hrt_blas* b) { return b ? serial_size(b) : 0; }
+
+hrt_status hrt_blas_serialize(const hrt_blas* b, void* dst, uint64_t bytes) {
+    if (!b || !dst) return HRT_ERR_INVALID_ARG;
+    hrt_context* ctx = b->ctx;
+    const uint64_t need = serial_size(b);
+    if (bytes < need)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_serialize: needs %llu bytes, got %llu", (unsigned long long)need,
+                    (unsigned long long)bytes);
+    DeviceSet ds(ctx->device);
+    const BuildOutput& o = b->out;
+    SerialHeader h{};
+    memcpy(h.magic, "HRTB", 4);
+    h.version = kSerialVersion;
+    h.type = b->type;
+    h.precision = b->precision;
+    h.nprims = b->nprims;
+    h.nnodes = o.nnodes;
+    h.nroots = o.nroots;
+    h.node_bytes = o.node_bytes;
+    h.prim_bytes = o.prim_bytes;
+    memcpy(h.bounds, o.bounds, sizeof(h.bounds));
+    memcpy(h.transform, b->transform, sizeof(h.transform));
+    h.max_leaf = b->max_leaf;
+    h.quant_chunk = b->quant_chunk;
+    h.nvertices = b->nvertices;
+    h.nstrands = b->nstrands;
+    h.const_radius = b->const_radius;
+    h.has_radius = b->has_radius;
+    h.has_normals = b->has_normals;
+    h.nlevels = o.level_start.size();
+    h.n_line_off = b->line_off.size();
+    h.n_vert_off = b->vert_off.size();
+    h.n_line_idx = b->line_idx.size();
+    h.n_tri_idx = b->tri_idx.size();
+    uint8_t* p = static_cast<uint8_t*>(dst);
+    memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    for (const std::vector<uint32_t>* v : {&o.level_start, &b->line_off, &b->vert_off, &b->line_idx, &b->tri_idx}) {
+        if (!v->empty()) memcpy(p, v->data(), v->size() * 4);
+        p += v->size() * 4;
+    }
+    struct { const void* src; uint64_t n; } parts[] = {{o.nodes, o.nnodes * o.node_bytes},
+                                                      {o.prims, b->nprims * o.prim_bytes},
+                                                      {o.roots, o.nroots * 16},
+                                                      {o.prim_ids, b->nprims * 4}};
+    for (auto& q : parts) {
+        if (q.n) CK(ctx, cudaMemcpy(p, q.src, q.n, cudaMemcpyDeviceToHost), "hrt_blas_serialize");
+        p += q.n;
+    }
+    return HRT_OK;
+}
+
+hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t bytes, void* stream, hrt_blas** out) {
+    if (!ctx) return HRT_ERR_INVALID_ARG;
+    if (!src || !out) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: null argument");
+    *out = nullptr;
+    const uint8_t* p = static_cast<const uint8_t*>(src);
+    const uint8_t* end = p + bytes;
+    SerialHeader h;
+    if (bytes < sizeof(h)) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: truncated header");
+    memcpy(&h, p, sizeof(h));
+    p += sizeof(h);
+    if (memcmp(h.magic, "HRTB", 4) != 0 || h.version != kSerialVersion)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: not a version-%u BLAS image", kSerialVersion);
+    const bool quant = h.precision == HRT_PRECISION_QUANTISED;
+    const uint64_t want_node = quant ? sizeof(NodeQ) : sizeof(NodeF);
+    const uint64_t want_prim = h.type == HRT_BLAS_PHANTOM ? (quant ? 32 : 64) : (h.type == HRT_BLAS_LSS ? 32 : 80);
+    if (h.type < HRT_BLAS_PHANTOM || h.type > HRT_BLAS_MESH || (h.precision != HRT_PRECISION_FP32 && !quant) ||
+        h.node_bytes != want_node || h.prim_bytes != want_prim || h.nprims >= (1ull << 29) || h.nnodes > h.nprims + 1 ||
+        h.nroots > h.nprims || (h.nprims && !h.nnodes) || h.max_leaf < 1 || h.max_leaf > 3)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: inconsistent header");
+    hrt_blas* b = new (std::nothrow) hrt_blas();
+    if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_blas_deserialize: host allocation");
+    auto reject = [&](const char* why) {
+        free_build_output(b->out);
+        delete b;
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: %s", why);
+    };
+    b->ctx = ctx;
+    b->type = h.type;
+    b->precision = h.precision;
+    b->nprims = h.nprims;
+    memcpy(b->transform, h.transform, sizeof(h.transform));
+    b->max_leaf = h.max_leaf;
+    b->quant_chunk = h.quant_chunk;
+    b->nvertices = h.nvertices;
+    b->nstrands = h.nstrands;
+    b->const_radius = h.const_radius;
+    b->has_radius = h.has_radius != 0;
+    b->has_normals = h.has_normals != 0;
+    BuildOutput& o = b->out;
+    if (!take_u32(p, end, h.nlevels, o.level_start) || !take_u32(p, end, h.n_line_off, b->line_off) ||
+        !take_u32(p, end, h.n_vert_off, b->vert_off) || !take_u32(p, end, h.n_line_idx, b->line_idx) ||
+        !take_u32(p, end, h.n_tri_idx, b->tri_idx))
+        return reject("truncated tables");
+    const uint64_t nb = h.nnodes * h.node_bytes, pbytes = h.nprims * h.prim_bytes, rb = h.nroots * 16, ib = h.nprims * 4;
+    if (nb + pbytes + rb + ib > uint64_t(end - p)) return reject("truncated arrays");
+    const uint8_t* nodes = p;
+    const uint8_t* prims = p + nb;
+    if (const char* why = check_tree(h.type, h.precision, h.nprims, h.nnodes, h.nroots, nodes, prims, o.level_start))
+        return reject(why);
+    o.nnodes = h.nnodes;
+    o.nroots = h.nroots;
+    o.node_bytes = h.node_bytes;
+    o.prim_bytes = h.prim_bytes;
+    memcpy(o.bounds, h.bounds, sizeof(o.bounds));
+    DeviceSet ds(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaSuccess;
+    struct { void** dst; const uint8_t* src; uint64_t n; } parts[] = {{&o.nodes, nodes, nb},
+                                                                     {&o.prims, prims, pbytes},
+                                                                     {reinterpret_cast<void**>(&o.roots), prims + pbytes, rb},
+                                                                     {reinterpret_cast<void**>(&o.prim_ids), prims + pbytes + rb, ib}};
+    for (auto& q : parts) {
+        if (!q.n || e != cudaSuccess) continue;
+        e = cudaMalloc(q.dst, q.n);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(*q.dst, q.src, q.n, cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        free_build_output(b->out);
+        delete b;
+        return cuda_fail(ctx, e, "hrt_blas_deserialize");
+    }
+    o.device_bytes = nb + pbytes + rb + ib;
+    *out = b;
+    return HRT_OK;
+}
+
 hrt_status hrt_blas_get_info(const hrt_blas* b, hrt_blas_info* o) {
     if (!b || !o) return HRT_ERR_INVALID_ARG;
     o->nprims = b->nprims;
