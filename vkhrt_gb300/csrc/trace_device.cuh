@@ -887,9 +887,6 @@ __device__ __forceinline__ void warp_add(unsigned long long* ctr, uint32_t v) {
 // pixel in order and each ray's closest hit is the least (t, instance, id).
 constexpr int kShort = 16;
 constexpr int kRefill = 16;
-#ifndef HRT_PREFETCH
-#define HRT_PREFETCH 0
-#endif
 
 // kPass 1: the frame (non-converged Phantom candidates flag their pixel); kPass 2: the listed
 // pixels again, with the FP64 re-solve inline (adds only the FP64 counts).
@@ -1182,16 +1179,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 cur_base = base;
                 cur_bits = oct_permute(ih, oct) | (imask << 8);
             }
-#if HRT_PREFETCH
-            if (cur_bits & 0xffu) {  // the node this lane visits next: bring its lines into L1 now
-                const uint32_t ni = (__ffs(cur_bits & 0xffu) - 1) ^ oct;
-                const uint32_t nc = cur_base + __popc((cur_bits >> 8) & ((1u << ni) - 1u));
-                const char* na = static_cast<const char*>(nodes) + uint64_t(nc) * (kQuant ? sizeof(NodeQ) : sizeof(NodeF));
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(na));
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(na + (kQuant ? 64 : 128)));
-                if (!kQuant) asm volatile("prefetch.global.L1 [%0];" ::"l"(na + 208));
-            }
-#endif
         }
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_node += c - clk; clk = c; }
         // ---- leaf phase: one leaf child per lane, in visiting order
