@@ -138,13 +138,17 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
     V3<T> cm = T(0.5) * (P[0] + P[3]);
     T ts = dot(cm - o, d) * F.inv_dd;
     out.ts = ts;
+    // the end points first: the bounding-cylinder early-out needs only them
     V3<T> W[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 4; k += 3)
         W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
     V3<T> mid = bez_point(P, T(0.5));
     T rmax = length(cross(mid - P[0], mid - P[3])) / length(P[3] - P[0]) + gmax(r0, r1);
     if (!ray_cylinder(mk(T(0), T(0), T(0)), d, W[0], W[3], rmax)) return out;
+#pragma unroll
+    for (int k = 1; k < 3; ++k)
+        W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
     V3<T> Q[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) Q[k] = mk(dot(F.e1, W[k]), dot(F.e2, W[k]), dot(F.e3, W[k]));
