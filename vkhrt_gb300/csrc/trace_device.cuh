@@ -891,6 +891,9 @@ __device__ __forceinline__ void warp_add(unsigned long long* ctr, uint32_t v) {
 // pixel in order and each ray's closest hit is the least (t, instance, id).
 constexpr int kShort = 16;
 constexpr int kRefill = 16;
+#ifndef HRT_LEAF_AGAIN
+#define HRT_LEAF_AGAIN 0
+#endif
 
 // kPass 1: the frame (non-converged Phantom candidates flag their pixel); kPass 2: the listed
 // pixels again, with the FP64 re-solve inline (adds only the FP64 counts).
@@ -1185,7 +1188,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             }
         }
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_node += c - clk; clk = c; }
-        // ---- leaf phase: one leaf child per lane, in visiting order
+        // ---- leaf phase: one leaf child per lane, in visiting order (repeated while at least
+        // HRT_LEAF_AGAIN lanes still hold leaf children, when that option is set)
+#if HRT_LEAF_AGAIN
+        for (int round = 0;; ++round) {
+            if (round > 0 && __popc(__ballot_sync(kFull, leaf_bits != 0u)) < HRT_LEAF_AGAIN) break;
+            if (round >= 8) break;
+#endif
         if (leaf_bits) {
             const DevBlas& B = L.scenes[si].inst[inst_cur].b;
             const uint32_t q = (__ffs(leaf_bits) - 1) ^ oct;
@@ -1205,6 +1214,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 }
             }
         }
+#if HRT_LEAF_AGAIN
+        }
+#endif
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_leaf += c - clk; clk = c; }
         // ---- completion
         if (has_ray && !leaf_bits && sp == 0 && !(cur_bits & 0xffu)) {
