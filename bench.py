@@ -320,10 +320,10 @@ def run_ours(args, dist):
     build_wall = time.perf_counter() - t0
     cam = H.scene_camera(w, h)
     frame = H.Frame(ctx, w, h, spp, with_hits=True)
-    params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, kernel_variant=args.variant, refill=args.refill, speculative=args.speculative, **{"async": 1})
+    params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, kernel_variant=args.variant, refill=args.refill, speculative=args.speculative, leaf_again=args.leaf_again, **{"async": 1})
     # rays per step (deterministic: fixed camera, jitter seed)
     H.trace(ctx, tlas, cam, frame, H.trace_params(spp=spp, jitter=1, seed=17, shading=2, count_stats=1,
-                                                  kernel_variant=args.variant, refill=args.refill, speculative=args.speculative))
+                                                  kernel_variant=args.variant, refill=args.refill, speculative=args.speculative, leaf_again=args.leaf_again))
     st = frame.stats()
     rays_per_step = st["primary_rays"] + st["shadow_rays"]
     # ---- timed region ----
@@ -358,7 +358,7 @@ def run_ours(args, dist):
     # ---- e2e: C ABI per frame, camera in, framebuffer to pinned host memory ----
     lib = ctx.lib
     pinned = torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True)
-    sync_params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, kernel_variant=args.variant, refill=args.refill, speculative=args.speculative)
+    sync_params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, kernel_variant=args.variant, refill=args.refill, speculative=args.speculative, leaf_again=args.leaf_again)
     for _ in range(2):
         H.trace(ctx, tlas, cam, frame, sync_params)
         ctx.check(lib.hrt_frame_download(frame.handle, ctypes.c_void_p(pinned.data_ptr()), None, None))
@@ -390,7 +390,7 @@ def run_ours(args, dist):
         tlas32 = H.TopLevelAccelerationStructure([blas32], ctx)
         f32 = H.Frame(ctx, w, h, spp, with_hits=False)
         H.trace(ctx, tlas32, cam, f32, H.trace_params(spp=spp, jitter=1, seed=17, shading=2,
-                                                      kernel_variant=args.variant, refill=args.refill, speculative=args.speculative))
+                                                      kernel_variant=args.variant, refill=args.refill, speculative=args.speculative, leaf_again=args.leaf_again))
         s32 = f32.stats()
         ms32 = time_frames(ctx, tlas32, cam, f32, params, args.steps, args.warmup)
         line["plain_fp32"] = {"value": round((s32["primary_rays"] + s32["shadow_rays"]) / (ms32 * 1e-3) / 1e6, 3),
@@ -731,6 +731,8 @@ def main():
     ap.add_argument("--max-leaf", type=int, default=1, help="primitives per BVH8 leaf (1..3)")
     ap.add_argument("--refill", type=int, default=8, help="idle lanes per warp that trigger a fetch (0 = 16)")
     ap.add_argument("--speculative", type=int, default=1, help="speculative traversal (0/1)")
+    ap.add_argument("--leaf-again", type=int, default=8,
+                    help="repeat the leaf phase while this many lanes hold leaves (0 = once)")
     ap.add_argument("--tune-cache", default=None, help="JSON file that keeps autotuner choices between runs")
     ap.add_argument("--profile", action="store_true",
                     help="one warm-up and the timed steps only: no e2e, FP32 comparison or CPU legs")

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HRT_ABI_VERSION 4
+#define HRT_ABI_VERSION 5
 
 typedef enum hrt_status {
     HRT_OK = 0,
@@ -167,6 +167,8 @@ typedef struct hrt_trace_params {
      * 1/2.2 as the reference's miss shader. */
     const float* env_map;
     uint32_t env_width, env_height;
+    uint32_t leaf_again;     /* repeat the leaf phase while at least this many lanes of a warp hold untested
+                                leaf children (0 = one leaf per lane per phase; default 8) */
 } hrt_trace_params;
 
 typedef struct hrt_hit {
@@ -291,12 +293,13 @@ hrt_status hrt_batch_set_cameras(hrt_batch* b, const hrt_camera* cams, uint32_t 
 uint64_t hrt_batch_table_bytes(const hrt_batch* b);
 
 /* ---- autotuner ------------------------------------------------------------------------------
- * Times every candidate kernel configuration on the given scenes (occupancy variant x refill
- * threshold x speculative traversal, and for scenes of mixed primitive types x one launch or one
- * per type: HRT_AUTOTUNE_CANDIDATES or twice that), each `reps` times with plain launches after
- * one warm-up, and writes the fastest into `best` (a copy of `base` with kernel_variant, refill,
- * speculative and split_types replaced) and its mean frame time into `best_ms`. */
-#define HRT_AUTOTUNE_CANDIDATES 18u
+ * Times every candidate kernel configuration on the given scenes (occupancy variant 3/4/5 blocks
+ * per SM x refill threshold 8/16 x leaf repetition 0/8/16, speculative traversal on, and for
+ * scenes of mixed primitive types x one launch or one per type: HRT_AUTOTUNE_CANDIDATES or twice
+ * that), each `reps` times with plain launches after one warm-up, and writes the fastest into
+ * `best` (a copy of `base` with kernel_variant, refill, speculative, leaf_again and split_types
+ * replaced) and its mean frame time into `best_ms`. */
+#define HRT_AUTOTUNE_CANDIDATES 18u  /* 3 x 2 x 3 */
 hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* base,
                         uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms);
 

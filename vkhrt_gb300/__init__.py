@@ -48,7 +48,7 @@ class TraceParamsC(ctypes.Structure):
                 ("shading", c_u32), ("shadow_tmin", c_f), ("fp64_resolve", c_u32), ("record_hits", c_u32),
                 ("async_", c_u32), ("count_stats", c_u32), ("kernel_variant", c_u32), ("refill", c_u32),
                 ("speculative", c_u32), ("split_types", c_u32), ("env_map", c_p), ("env_width", c_u32),
-                ("env_height", c_u32)]
+                ("env_height", c_u32), ("leaf_again", c_u32)]
 
 
 class FrameStatsC(ctypes.Structure):
@@ -461,7 +461,7 @@ def trace_rays_noalloc(ctx: Context, tlas: TopLevelAccelerationStructure, rays: 
     return hits
 
 
-TUNED_FIELDS = ("kernel_variant", "refill", "speculative", "split_types")
+TUNED_FIELDS = ("kernel_variant", "refill", "speculative", "split_types", "leaf_again")
 
 
 def autotune(ctx: Context, scenes: list[tuple[TopLevelAccelerationStructure, CameraC, Frame]],

@@ -256,6 +256,7 @@ TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32
     L.variant = p->kernel_variant;
     L.refill = p->refill > 32 ? 32 : p->refill;
     L.speculative = p->speculative;
+    L.leaf_again = p->leaf_again > 32 ? 32 : p->leaf_again;
     L.counters = c;
     L.resolve_list = resolve_list;
     L.resolve_cap = resolve_cap;
@@ -1170,6 +1171,7 @@ void hrt_trace_params_default(hrt_trace_params* p) {
     p->fp64_resolve = 1;
     p->refill = 8;
     p->speculative = 1;
+    p->leaf_again = 8;
 }
 
 hrt_status hrt_frame_create(hrt_context* ctx, uint32_t w, uint32_t h, uint32_t spp, int32_t with_hits, hrt_frame** out) {
@@ -1443,17 +1445,18 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
     }
     cudaError_t e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    const uint32_t variants[3] = {1, 2, 3}, refills[3] = {4, 8, 16}, specs[2] = {0, 1};
+    const uint32_t variants[3] = {1, 2, 3}, refills[2] = {8, 16}, agains[3] = {0, 8, 16};
     float best_t = -1.0f;
     hrt_trace_params bp = *base;
     for (uint32_t split = 0; split < nplans && e == cudaSuccess; ++split)
         for (uint32_t v : variants)
             for (uint32_t r : refills)
-                for (uint32_t sp : specs) {
+                for (uint32_t la : agains) {
                     hrt_trace_params p = *base;
                     p.kernel_variant = v;
                     p.refill = r;
-                    p.speculative = sp;
+                    p.speculative = 1;
+                    p.leaf_again = la;
                     p.split_types = split;
                     p.record_hits = 0;
                     p.count_stats = 0;

@@ -111,6 +111,7 @@ struct TraceLaunch {
     uint32_t variant;    // kernel variant (occupancy / register split), 0 = default
     uint32_t refill;     // idle lanes of a warp that trigger a work fetch (0 = 16)
     uint32_t speculative;  // lanes holding a leaf keep traversing while others search
+    uint32_t leaf_again;   // repeat the leaf phase while this many lanes hold leaves (0 = once)
     TraceCounters* counters;
     // Two-pass FP64 re-solve: the first pass lists the work items (pixels) that met a Phantom
     // candidate whose FP32 solve did not converge; the second re-renders just those with the

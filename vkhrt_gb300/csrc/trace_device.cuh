@@ -891,9 +891,6 @@ __device__ __forceinline__ void warp_add(unsigned long long* ctr, uint32_t v) {
 // pixel in order and each ray's closest hit is the least (t, instance, id).
 constexpr int kShort = 16;
 constexpr int kRefill = 16;
-#ifndef HRT_LEAF_AGAIN
-#define HRT_LEAF_AGAIN 0
-#endif
 
 // kPass 1: the frame (non-converged Phantom candidates flag their pixel); kPass 2: the listed
 // pixels again, with the FP64 re-solve inline (adds only the FP64 counts).
@@ -1069,6 +1066,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
 
     const int refill = L.refill ? int(L.refill) : kRefill;  // idle lanes that trigger a fetch
     const bool spec = L.speculative != 0;
+    const int leaf_again = int(L.leaf_again);
     // work items: pass 1 every item; pass 2 the samples of the listed pixels, or the listed
     // pixels when their samples do not fit the scratch, or every item if the list overflowed
     unsigned long long* const work_ctr = kPass == 1 ? &L.counters->work : &L.counters->work2;
@@ -1188,13 +1186,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             }
         }
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_node += c - clk; clk = c; }
-        // ---- leaf phase: one leaf child per lane, in visiting order (repeated while at least
-        // HRT_LEAF_AGAIN lanes still hold leaf children, when that option is set)
-#if HRT_LEAF_AGAIN
-        for (int round = 0;; ++round) {
-            if (round > 0 && __popc(__ballot_sync(kFull, leaf_bits != 0u)) < HRT_LEAF_AGAIN) break;
-            if (round >= 8) break;
-#endif
+        // ---- leaf phase: one leaf child per lane, in visiting order; repeated (at most 8 rounds)
+        // while at least leaf_again lanes still hold leaf children, so lanes whose test ended
+        // early take their next leaf instead of idling
+        for (int round = 0; round < 8; ++round) {
+            if (round > 0 && (!leaf_again || __popc(__ballot_sync(kFull, leaf_bits != 0u)) < leaf_again)) break;
         if (leaf_bits) {
             const DevBlas& B = L.scenes[si].inst[inst_cur].b;
             const uint32_t q = (__ffs(leaf_bits) - 1) ^ oct;
@@ -1214,9 +1210,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 }
             }
         }
-#if HRT_LEAF_AGAIN
         }
-#endif
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_leaf += c - clk; clk = c; }
         // ---- completion
         if (has_ray && !leaf_bits && sp == 0 && !(cur_bits & 0xffu)) {
