@@ -494,7 +494,8 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 }
 
 __device__ __forceinline__ V3<float> safe_inv(V3<float> d) {
-    auto r = [](float x) { return 1.0f / (fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
+    // the IEEE reciprocal (round to nearest): the same value as 1 / x, without a full division
+    auto r = [](float x) { return __frcp_rn(fabsf(x) > 1e-20f ? x : copysignf(1e-20f, x)); };
     return mk(r(d.x), r(d.y), r(d.z));
 }
 
