@@ -731,7 +731,7 @@ def main():
     ap.add_argument("--max-leaf", type=int, default=1, help="primitives per BVH8 leaf (1..3)")
     ap.add_argument("--refill", type=int, default=8, help="idle lanes per warp that trigger a fetch (0 = 16)")
     ap.add_argument("--speculative", type=int, default=1, help="speculative traversal (0/1)")
-    ap.add_argument("--leaf-again", type=int, default=8,
+    ap.add_argument("--leaf-again", type=int, default=4,
                     help="repeat the leaf phase while this many lanes hold leaves (0 = once)")
     ap.add_argument("--tune-cache", default=None, help="JSON file that keeps autotuner choices between runs")
     ap.add_argument("--profile", action="store_true",

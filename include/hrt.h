@@ -168,7 +168,7 @@ typedef struct hrt_trace_params {
     const float* env_map;
     uint32_t env_width, env_height;
     uint32_t leaf_again;     /* repeat the leaf phase while at least this many lanes of a warp hold untested
-                                leaf children (0 = one leaf per lane per phase; default 8) */
+                                leaf children (0 = one leaf per lane per phase; default 4) */
 } hrt_trace_params;
 
 typedef struct hrt_hit {
@@ -294,7 +294,7 @@ uint64_t hrt_batch_table_bytes(const hrt_batch* b);
 
 /* ---- autotuner ------------------------------------------------------------------------------
  * Times every candidate kernel configuration on the given scenes (occupancy variant 3/4/5 blocks
- * per SM x refill threshold 8/16 x leaf repetition 0/8/16, speculative traversal on, and for
+ * per SM x refill threshold 8/16 x leaf repetition 2/4/8, speculative traversal on, and for
  * scenes of mixed primitive types x one launch or one per type: HRT_AUTOTUNE_CANDIDATES or twice
  * that), each `reps` times with plain launches after one warm-up, and writes the fastest into
  * `best` (a copy of `base` with kernel_variant, refill, speculative, leaf_again and split_types

@@ -1171,7 +1171,7 @@ void hrt_trace_params_default(hrt_trace_params* p) {
     p->fp64_resolve = 1;
     p->refill = 8;
     p->speculative = 1;
-    p->leaf_again = 8;
+    p->leaf_again = 4;
 }
 
 hrt_status hrt_frame_create(hrt_context* ctx, uint32_t w, uint32_t h, uint32_t spp, int32_t with_hits, hrt_frame** out) {
@@ -1445,7 +1445,7 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
     }
     cudaError_t e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    const uint32_t variants[3] = {1, 2, 3}, refills[2] = {8, 16}, agains[3] = {0, 8, 16};
+    const uint32_t variants[3] = {1, 2, 3}, refills[2] = {8, 16}, agains[3] = {2, 4, 8};
     float best_t = -1.0f;
     hrt_trace_params bp = *base;
     for (uint32_t split = 0; split < nplans && e == cudaSuccess; ++split)
