@@ -666,7 +666,7 @@ def batch_agreement_and_cpu(args, ctx, q, models):
     cpu_rays = 0
     cpu_px = 0
     cpu_s = 0.0
-    cpu_frac = 0.25
+    cpu_frac = 1.0  # every pixel of every scene: about 10 s of CPU work
     per = max(1, 65536 // len(models))
     for (b, t, cam, fr), (m, v, r, off) in zip(q, models):
         H.trace(ctx, t, cam, fr, H.trace_params(jitter=1, seed=17, shading=2, record_hits=1))
