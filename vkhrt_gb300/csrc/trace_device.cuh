@@ -82,6 +82,11 @@ template <class T> __device__ __forceinline__ V3<T> bez_axis(const V3<T>* c, T t
     return (T(-3) * u * u) * c[0] + (T(3) * (T(3) * t * t - T(4) * t + T(1))) * c[1] +
            (T(3) * (T(2) - T(3) * t) * t) * c[2] + (T(3) * t * t) * c[3];
 }
+// The quotients of the FP32 Phantom solve use the fast division (__fdividef, within 2 ulp):
+// the solve's results differ from the FP64 solve by far more than that, and the FP64 pass
+// re-solves the candidates whose FP32 iteration does not converge. FP64 divides exactly.
+template <class T> __device__ __forceinline__ T prhi_div(T a, T b) { return a / b; }
+template <> __device__ __forceinline__ float prhi_div<float>(float a, float b) { return __fdividef(a, b); }
 // cylinder.glsl:8-46 (capped cylinder, boolean; no range test on t)
 template <class T> __device__ __forceinline__ bool ray_cylinder(V3<T> o, V3<T> d, V3<T> p0, V3<T> p1, T r) {
     V3<T> ba = p1 - p0, oc = o - p0;
@@ -92,18 +97,41 @@ template <class T> __device__ __forceinline__ bool ray_cylinder(V3<T> o, V3<T> d
     T h = k1 * k1 - k2 * k0;
     if (h < T(0)) return false;
     h = sqrt(h);
-    T t = (-k1 - h) / k2;
+    T t = prhi_div(-k1 - h, k2);
     T y = baoc + t * bard;
     if (y > T(0) && y < baba) return true;
-    t = ((y < T(0) ? T(0) : baba) - baoc) / bard;
+    t = prhi_div((y < T(0) ? T(0) : baba) - baoc, bard);
     return gabs(k1 + k2 * t) < h;
+}
+
+// The cubic in power form, C3 t^3 + C2 t^2 + C1 t + C0, and its derivative
+// (3 C3 t + 2 C2) t + C1 = (C3 (1.5 t) + C2) (2 t) + C1, by Horner's rule.
+template <class T> __device__ __forceinline__ void power_eval(const V3<T>* C, T t, V3<T>& c, V3<T>& ax) {
+    const T t15 = T(1.5) * t, t2 = t + t;
+    c = mk(fma(fma(fma(C[3].x, t, C[2].x), t, C[1].x), t, C[0].x), fma(fma(fma(C[3].y, t, C[2].y), t, C[1].y), t, C[0].y),
+           fma(fma(fma(C[3].z, t, C[2].z), t, C[1].z), t, C[0].z));
+    ax = mk(fma(fma(C[3].x, t15, C[2].x), t2, C[1].x), fma(fma(C[3].y, t15, C[2].y), t2, C[1].y),
+            fma(fma(C[3].z, t15, C[2].z), t2, C[1].z));
+}
+// FP32: x and y in packed pairs (each half rounds exactly as fmaf, so the values are the same)
+__device__ __forceinline__ void power_eval(const V3<float>* C, float t, V3<float>& c, V3<float>& ax) {
+    const float t15 = 1.5f * t, t2 = t + t;
+    const float2 tt = make_float2(t, t), tt15 = make_float2(t15, t15), tt2 = make_float2(t2, t2);
+    const float2 c0 = make_float2(C[0].x, C[0].y), c1 = make_float2(C[1].x, C[1].y);
+    const float2 c2 = make_float2(C[2].x, C[2].y), c3 = make_float2(C[3].x, C[3].y);
+    const float2 pxy = __ffma2_rn(__ffma2_rn(__ffma2_rn(c3, tt, c2), tt, c1), tt, c0);
+    const float2 axy = __ffma2_rn(__ffma2_rn(c3, tt15, c2), tt2, c1);
+    c = mk(pxy.x, pxy.y, fmaf(fmaf(fmaf(C[3].z, t, C[2].z), t, C[1].z), t, C[0].z));
+    ax = mk(axy.x, axy.y, fmaf(fmaf(C[3].z, t15, C[2].z), t2, C[1].z));
 }
 
 // kUnresolved: no hit, and a side used all 8 iterations inside [0, 1] with a real cone
 // intersection at its last step (det > 0 but |dt| >= 5e-5): the FP32 run failed its
 // convergence test. Runs that exhaust without an intersection are misses.
 enum { kMiss = 0, kHit = 1, kUnresolved = 2 };
-template <class T> struct PrhiOut { T s; T sl; T ts; T tc; int status; };  // s = ts + sl
+template <class T> struct PrhiOut {  // s = ts + sl
+    T s; T sl; T ts; T tc; int status;
+};
 
 // ray.glsl:13-17 MakeOrthonormalBasis; the RCC transform (ray.glsl:19-33) is the inverse of
 // [e1 e2 e3 | o], applied here as the transpose of the orthonormal frame after the translation.
@@ -132,6 +160,10 @@ template <class T> __device__ __forceinline__ T rel_coord(T a, T b, T ts, T d) {
 // P - o' kept at full precision (o' itself is never rounded); ts is added back to the
 // distance. The result is the same in exact arithmetic; in FP32 it removes the cancellation of
 // the world-space bounding-cylinder test from a distant origin (hair_intersection.rint:29).
+// The bounding radius is sqrt(|cross|^2 / |chord|^2) (one root instead of two), and the Newton
+// iteration evaluates the Bezier point and tangent from the power form of the control points
+// (Horner's rule, power_eval) instead of the Bernstein weights of curve.glsl: the same
+// polynomials, in fewer operations.
 template <class T>
 __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, const V3<T>* P, T r0, T r1) {
     PrhiOut<T> out{T(0), T(0), T(0), T(0), kMiss};
@@ -144,7 +176,8 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
     for (int k = 0; k < 4; k += 3)
         W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
     V3<T> mid = bez_point(P, T(0.5));
-    T rmax = length(cross(mid - P[0], mid - P[3])) / length(P[3] - P[0]) + gmax(r0, r1);
+    const V3<T> cr = cross(mid - P[0], mid - P[3]), ch = P[3] - P[0];
+    T rmax = sqrt(prhi_div(dot(cr, cr), dot(ch, ch))) + gmax(r0, r1);
     if (!ray_cylinder(mk(T(0), T(0), T(0)), d, W[0], W[3], rmax)) return out;
 #pragma unroll
     for (int k = 1; k < 3; ++k)
@@ -152,14 +185,15 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
     V3<T> Q[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) Q[k] = mk(dot(F.e1, W[k]), dot(F.e2, W[k]), dot(F.e3, W[k]));
+    V3<T> PC[4] = {Q[0], T(3) * (Q[1] - Q[0]), T(3) * ((Q[0] - Q[1]) + (Q[2] - Q[1])), (Q[3] - Q[0]) + T(3) * (Q[1] - Q[2])};
     T tStart = (Q[3].z - Q[0].z) > T(0) ? T(0) : T(1);
     bool unresolved = false;
     for (int side = 0; side < 2; ++side) {
         T t = tStart, told = T(0), dt1 = T(0), dt2 = T(0);
         bool exhausted = true, last_isect = false;
         for (int i = 0; i < 8; ++i) {
-            V3<T> c = bez_point(Q, t);
-            V3<T> ax = bez_axis(Q, t);
+            V3<T> c, ax;
+            power_eval(PC, t, c, ax);
             T rad = (r0 == r1) ? r0 : r0 + (r1 - r0) * t;
             // cone.glsl:21-62 with slant 0
             T ddd = ax.x * ax.x + ax.y * ax.y;
@@ -174,8 +208,8 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
             T det = b * b - a * cc;
             bool isect = det > T(0);
             last_isect = isect;
-            T s = (b - (isect ? sqrt(det) : T(0))) / cc;
-            T dt = (s * ax.z - cdd) / ddd;
+            T s = prhi_div(b - (isect ? sqrt(det) : T(0)), cc);
+            T dt = prhi_div(s * ax.z - cdd, ddd);
             if (isect && gabs(dt) < T(5e-5)) {
                 out.sl = s + c.z;
                 out.s = out.sl + ts;
@@ -188,7 +222,7 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
             dt1 = dt2;
             dt2 = dt;
             if (dt1 * dt2 < T(0)) {
-                T tnext = ((i & 3) == 0) ? T(0.5) * (told + t) : (dt2 * told - dt1 * t) / (dt2 - dt1);
+                T tnext = ((i & 3) == 0) ? T(0.5) * (told + t) : prhi_div(dt2 * told - dt1 * t, dt2 - dt1);
                 told = t;
                 t = tnext;
             } else {
@@ -226,13 +260,17 @@ __device__ __noinline__ void prhi_fp64(float ox, float oy, float oz, float dx, f
 // nearest the segment midpoint) on the full-precision vectors a - o', b - o'; t = ts + t'.
 // Quadratic coefficients are formed with cross products (Lagrange's identity) so that no term
 // is the small difference of two large ones: for the sphere, h = r^2 |d|^2 - |oc x d|^2.
+// Quotients by a reciprocal from the fast division (within 2 ulp); the hit distances stay
+// within the FP32 tolerance of the FP64 round-cone solve.
+__device__ __forceinline__ float lss_rcp(float x) { return __fdividef(1.0f, x); }
 __device__ __forceinline__ float sphere_hit(V3<float> oc, V3<float> d, float r, float tmin, float best) {
     float A = dot(d, d), B = dot(oc, d);
     V3<float> c = cross(oc, d);
     float h = r * r * A - dot(c, c);
     if (h < 0.0f) return best;
     float sh = sqrtf(h);
-    float t0 = (-B - sh) / A, t1 = (-B + sh) / A;
+    const float iA = lss_rcp(A);
+    float t0 = (-B - sh) * iA, t1 = (-B + sh) * iA;
     if (t0 >= tmin && t0 < best) return t0;
     if (t1 >= tmin && t1 < best) return t1;
     return best;
@@ -244,7 +282,7 @@ __device__ __forceinline__ float sphere_hit(V3<float> oc, V3<float> d, float r, 
 __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> a, V3<float> b, float ra, float rb,
                                          float tmin_in, float* u_out, float* tl_out, float* ts_out) {
     const float kNone = __int_as_float(0x7f800000);
-    float ts = dot(0.5f * (a + b) - o_in, d) / dot(d, d);
+    float ts = dot(0.5f * (a + b) - o_in, d) * lss_rcp(dot(d, d));
     V3<float> wa = mk(rel_coord(a.x, o_in.x, ts, d.x), rel_coord(a.y, o_in.y, ts, d.y), rel_coord(a.z, o_in.z, ts, d.z));
     V3<float> wb = mk(rel_coord(b.x, o_in.x, ts, d.x), rel_coord(b.y, o_in.y, ts, d.y), rel_coord(b.z, o_in.z, ts, d.z));
     V3<float> oa = mk(-wa.x, -wa.y, -wa.z);
@@ -264,12 +302,13 @@ __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> 
         float h = B * B - A * C;
         if (h >= 0.0f && A != 0.0f) {
             float sh = sqrtf(h);
-            float r0 = (-B - sh) / A, r1 = (-B + sh) / A;
+            const float iA = lss_rcp(A), im = lss_rcp(m);
+            float r0 = (-B - sh) * iA, r1 = (-B + sh) * iA;
             float lo = gmin(r0, r1), hi = gmax(r0, r1);
-            float u = (yo + lo * yd) / m;
+            float u = (yo + lo * yd) * im;
             if (lo >= tmin && lo < best && u >= 0.0f && u <= 1.0f) { best = lo; bu = u; }
             else {
-                u = (yo + hi * yd) / m;
+                u = (yo + hi * yd) * im;
                 if (hi >= tmin && hi < best && u >= 0.0f && u <= 1.0f) { best = hi; bu = u; }
             }
         }
@@ -316,7 +355,11 @@ __device__ __forceinline__ float tri_hit(const TriRay& R, V3<float> o, V3<float>
     float det = U + V + W;
     if (det == 0.0f) return -1.0f;
     float Tn = U * (R.Sz * Akz) + V * (R.Sz * Bkz) + W * (R.Sz * Ckz);
+#if HRT_FAST_DIV_TRI
+    float t = __fdividef(Tn, det);
+#else
     float t = Tn / det;
+#endif
     if (!(t >= tmin) || !(t <= tmax)) return -1.0f;
     if (b1) {
         const float inv = 1.0f / det;
@@ -503,9 +546,10 @@ __device__ __forceinline__ V3<float> safe_inv(V3<float> d) {
 // Near and far planes are chosen per axis by the sign of the direction (octant), so a child
 // needs three maxima and three minima. FP32 boxes: t = (plane - o) inv, accepted when
 // tnear <= tfar (1 + 2^-20). 8-bit boxes: t = q (2^e inv) + (p - o) inv, one fused operation
-// per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 1279 2^e |inv|), and that
+// per plane; its rounding on an axis is below 2^-20 (|p - o| |inv| + 33023 2^e |inv|), and that
 // bound is subtracted from the axis's near planes and added to its far planes, so a box is
-// never lost to rounding (a near-parallel axis widens only its own planes).
+// never lost to rounding (a near-parallel axis widens only its own planes). The planes of two
+// children go through one packed fused multiply-add (__ffma2_rn, each half rounded as fmaf).
 // Empty slots hold empty boxes and fail the test. tn (when given) receives the entry distances;
 // kWithT: also prim_base and the meta words m0/m1 (sorted traversal).
 template <bool kQuant, bool kWithT = true>
@@ -545,12 +589,27 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         const float kO = 2.384185791015625e-07f;  // 2^-22
         const float ex = kO * fabsf(ox), ey = kO * fabsf(oy), ez = kO * fabsf(oz);
         const float oxn = ox - ex, oxf = ox + ex, oyn = oy - ey, oyf = oy + ey, ozn = oz - ez, ozf = oz + ez;
+        // two children per packed fused multiply-add (each half rounds exactly as fmaf)
+        const float2 ix = make_float2(R.inv.x, R.inv.x), iy = make_float2(R.inv.y, R.inv.y);
+        const float2 iz = make_float2(R.inv.z, R.inv.z);
+        const float2 oxn2 = make_float2(oxn, oxn), oxf2 = make_float2(oxf, oxf), oyn2 = make_float2(oyn, oyn);
+        const float2 oyf2 = make_float2(oyf, oyf), ozn2 = make_float2(ozn, ozn), ozf2 = make_float2(ozf, ozf);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            float a = max3f(fmaf(NX[q], R.inv.x, oxn), fmaf(NY[q], R.inv.y, oyn), fmaxf(fmaf(NZ[q], R.inv.z, ozn), R.tmin));
-            float b = min3f(fmaf(FX[q], R.inv.x, oxf), fmaf(FY[q], R.inv.y, oyf), fminf(fmaf(FZ[q], R.inv.z, ozf), tfar));
-            if (tn) tn[q] = a;
-            if (a <= b * kEps) mask |= 1u << q;
+        for (int j = 0; j < 4; ++j) {
+            const float2 tnx = __ffma2_rn(make_float2(NX[2 * j], NX[2 * j + 1]), ix, oxn2);
+            const float2 tfx = __ffma2_rn(make_float2(FX[2 * j], FX[2 * j + 1]), ix, oxf2);
+            const float2 tny = __ffma2_rn(make_float2(NY[2 * j], NY[2 * j + 1]), iy, oyn2);
+            const float2 tfy = __ffma2_rn(make_float2(FY[2 * j], FY[2 * j + 1]), iy, oyf2);
+            const float2 tnz = __ffma2_rn(make_float2(NZ[2 * j], NZ[2 * j + 1]), iz, ozn2);
+            const float2 tfz = __ffma2_rn(make_float2(FZ[2 * j], FZ[2 * j + 1]), iz, ozf2);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int q = 2 * j + k;
+                const float a = max3f(k ? tnx.y : tnx.x, k ? tny.y : tny.x, fmaxf(k ? tnz.y : tnz.x, R.tmin));
+                const float b = min3f(k ? tfx.y : tfx.x, k ? tfy.y : tfy.x, fminf(k ? tfz.y : tfz.x, tfar));
+                if (tn) tn[q] = a;
+                if (a <= b * kEps) mask |= 1u << q;
+            }
         }
         return mask;
     } else {
@@ -563,16 +622,17 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         const float bx = (__uint_as_float(w0.x) - R.o.x) * R.inv.x;
         const float by = (__uint_as_float(w0.y) - R.o.y) * R.inv.y;
         const float bz = (__uint_as_float(w0.z) - R.o.z) * R.inv.z;
-        // Two bytes at a time become the halves 1024 + q0, 1024 + q1 (one byte permute under the
-        // exponent of 1024), widened to FP32 exactly, and t = (1024 + q) s + (b - 1024 s), one
-        // fused multiply-add per plane. The roundings (offset, slack, product-sum) are each below
-        // 2^-24 (|b| + 1279 |s|), so E = 2^-20 (|b| + 1279 |s|) per axis, taken from the near
-        // planes and given to the far planes, never loses a box to rounding (about 1/800 of a
-        // grid step at the scale of the node).
+        // One byte permute per plane makes the float 0x3F80qq00 = 1 + q 2^-15 (q under the
+        // exponent of 1), and t = (1 + q 2^-15) S + (b - S) with S = 2^15 s: one packed fused
+        // multiply-add per plane pair of two children. The roundings (offset, slack, product-sum)
+        // are each below 2^-24 (|b| + 33023 |s|), so E = 2^-20 (|b| + 33023 |s|) per axis, taken
+        // from the near planes and given to the far planes, never loses a box to rounding (about
+        // 1/128 of a grid step at the scale of the node).
         const float kS = 9.5367431640625e-07f;  // 2^-20
-        const float ex = kS * fmaf(1279.0f, fabsf(sx), fabsf(bx)), ey = kS * fmaf(1279.0f, fabsf(sy), fabsf(by));
-        const float ez = kS * fmaf(1279.0f, fabsf(sz), fabsf(bz));
-        const float cx = fmaf(-1024.0f, sx, bx), cy = fmaf(-1024.0f, sy, by), cz = fmaf(-1024.0f, sz, bz);
+        const float ex = kS * fmaf(33023.0f, fabsf(sx), fabsf(bx)), ey = kS * fmaf(33023.0f, fabsf(sy), fabsf(by));
+        const float ez = kS * fmaf(33023.0f, fabsf(sz), fabsf(bz));
+        const float Sx = 32768.0f * sx, Sy = 32768.0f * sy, Sz = 32768.0f * sz;
+        const float cx = bx - Sx, cy = by - Sy, cz = bz - Sz;
         const float cxn = cx - ex, cxf = cx + ex, cyn = cy - ey, cyf = cy + ey, czn = cz - ez, czf = cz + ez;
         if (imask) *imask = w0.w >> 24;
         *base = w1.x;
@@ -585,26 +645,26 @@ __device__ __forceinline__ uint32_t test_node(const void* nodes, uint32_t ni, co
         const uint32_t nxw0 = nx ? w2.z : w2.x, nxw1 = nx ? w2.w : w2.y, fxw0 = nx ? w2.x : w2.z, fxw1 = nx ? w2.y : w2.w;
         const uint32_t nyw0 = ny ? w3.z : w3.x, nyw1 = ny ? w3.w : w3.y, fyw0 = ny ? w3.x : w3.z, fyw1 = ny ? w3.y : w3.w;
         const uint32_t nzw0 = nz ? w4.z : w4.x, nzw1 = nz ? w4.w : w4.y, fzw0 = nz ? w4.x : w4.z, fzw1 = nz ? w4.y : w4.w;
-        auto h2f = [](uint32_t w, uint32_t sel) -> float2 {
-            const uint32_t u = __byte_perm(w, 0x64646464u, sel);
-            return __half22float2(*reinterpret_cast<const __half2*>(&u));
-        };
+        auto q15 = [](uint32_t w, uint32_t sel) { return __uint_as_float(__byte_perm(w, 0x3F800000u, sel)); };
+        const float2 sx2 = make_float2(Sx, Sx), sy2 = make_float2(Sy, Sy), sz2 = make_float2(Sz, Sz);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const uint32_t sel = (j & 1) ? 0x4342u : 0x4140u;
-            const float2 nxv = h2f(j < 2 ? nxw0 : nxw1, sel), fxv = h2f(j < 2 ? fxw0 : fxw1, sel);
-            const float2 nyv = h2f(j < 2 ? nyw0 : nyw1, sel), fyv = h2f(j < 2 ? fyw0 : fyw1, sel);
-            const float2 nzv = h2f(j < 2 ? nzw0 : nzw1, sel), fzv = h2f(j < 2 ? fzw0 : fzw1, sel);
+            const uint32_t s0 = (j & 1) ? 0x7624u : 0x7604u, s1 = (j & 1) ? 0x7634u : 0x7614u;
+            const uint32_t a = j < 2 ? nxw0 : nxw1, b = j < 2 ? fxw0 : fxw1, c = j < 2 ? nyw0 : nyw1;
+            const uint32_t d = j < 2 ? fyw0 : fyw1, e = j < 2 ? nzw0 : nzw1, f = j < 2 ? fzw0 : fzw1;
+            const float2 tnx = __ffma2_rn(make_float2(q15(a, s0), q15(a, s1)), sx2, make_float2(cxn, cxn));
+            const float2 tfx = __ffma2_rn(make_float2(q15(b, s0), q15(b, s1)), sx2, make_float2(cxf, cxf));
+            const float2 tny = __ffma2_rn(make_float2(q15(c, s0), q15(c, s1)), sy2, make_float2(cyn, cyn));
+            const float2 tfy = __ffma2_rn(make_float2(q15(d, s0), q15(d, s1)), sy2, make_float2(cyf, cyf));
+            const float2 tnz = __ffma2_rn(make_float2(q15(e, s0), q15(e, s1)), sz2, make_float2(czn, czn));
+            const float2 tfz = __ffma2_rn(make_float2(q15(f, s0), q15(f, s1)), sz2, make_float2(czf, czf));
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
                 const int q = 2 * j + k;
-                const float vnx = k ? nxv.y : nxv.x, vfx = k ? fxv.y : fxv.x;
-                const float vny = k ? nyv.y : nyv.x, vfy = k ? fyv.y : fyv.x;
-                const float vnz = k ? nzv.y : nzv.x, vfz = k ? fzv.y : fzv.x;
-                float a = max3f(fmaf(vnx, sx, cxn), fmaf(vny, sy, cyn), fmaxf(fmaf(vnz, sz, czn), R.tmin));
-                float b = min3f(fmaf(vfx, sx, cxf), fmaf(vfy, sy, cyf), fminf(fmaf(vfz, sz, czf), tfar));
-                if (tn) tn[q] = a;
-                if (a <= b) mask |= 1u << q;
+                const float lo = max3f(k ? tnx.y : tnx.x, k ? tny.y : tny.x, fmaxf(k ? tnz.y : tnz.x, R.tmin));
+                const float hi = min3f(k ? tfx.y : tfx.x, k ? tfy.y : tfy.x, fminf(k ? tfz.y : tfz.x, tfar));
+                if (tn) tn[q] = lo;
+                if (lo <= hi) mask |= 1u << q;
             }
         }
         return mask;
