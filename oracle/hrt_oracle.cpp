@@ -570,12 +570,21 @@ static void refit(Binary& bt, const Box* sorted_boxes, int64_t n) {
 }
 
 // ---- collapse to an 8-wide BVH (breadth-first layout) ------------------------------------
-// Each wide node starts from a binary internal node with children [left, right]; while it has
-// fewer than 8 children, the child with the largest surface-area measure
-// (dx*dy + dy*dz) + dz*dx that is an internal node holding more than max_leaf primitives is
-// replaced in place by its left child, and its right child is appended (ties: first in list).
-// A child holding at most max_leaf primitives becomes a leaf (a contiguous run of sorted
-// primitives). The children are then placed in the 8 slots by direction (octant_slots below).
+// The binary tree's nodes are distributed over wide nodes by cost, a restatement of the
+// dynamic program of Ylitalo, Immonen and Karras (HPG 2017, "Efficient incoherent ray
+// traversal on GPUs through compressed wide BVHs", section 3): with A the surface-area measure
+// (dx*dy + dy*dz) + dz*dx, cost(x, k) is the least cost of x's subtree when it fills k slots
+// (k = 1..8) of its parent:
+//   a primitive: A for every k;
+//   dist(k) = min over j = 1..k-1 of cost(left, j) + cost(right, k - j)   (k >= 2);
+//   cost(x, 1) = A c when x holds c <= max_leaf primitives (a leaf slot), else A + dist(8);
+//   cost(x, k) = min(cost(x, k - 1), dist(k)).
+// Each wide node starts from a binary internal node b whose 8 slots go to its children as j and
+// 8 - j, j the least minimiser of cost(left, j) + cost(right, 8 - j); a child given k slots takes
+// the fewest k' <= k of the same cost and, with k' > 1, splits them again between its own
+// children, left before right. A child holding at most max_leaf primitives becomes a leaf (a
+// contiguous run of sorted primitives), a larger one a wide node of the next level. The
+// children are then placed in the 8 slots by direction (octant_slots below).
 // Nodes are numbered breadth first; a node's internal children take consecutive indices from
 // child_base in slot order, and its leaf primitives are copied to consecutive slots from
 // prim_base in slot order (the primitive order array).
@@ -629,6 +638,47 @@ static void collapse(const Binary& bt, const Box* sorted_boxes, int64_t n, int m
         return (c & 0x80000000u) ? sorted_boxes[c & 0x7fffffffu] : bt.box[c];
     };
     auto cfirst = [&](uint32_t c) -> uint32_t { return (c & 0x80000000u) ? (c & 0x7fffffffu) : bt.first[c]; };
+    // collapse costs, children before parents (reverse pre-order)
+    std::vector<float> dpc(n >= 2 ? 8 * size_t(n - 1) : 0);
+    auto cost = [&](uint32_t c, int k) -> float {
+        return (c & 0x80000000u) ? sa_measure(sorted_boxes[c & 0x7fffffffu]) : dpc[8 * size_t(c) + (k - 1)];
+    };
+    if (n >= 2) {
+        std::vector<uint32_t> pre, stk{0u};
+        while (!stk.empty()) {
+            uint32_t x = stk.back();
+            stk.pop_back();
+            pre.push_back(x);
+            if (!(bt.left[x] & 0x80000000u)) stk.push_back(bt.left[x]);
+            if (!(bt.right[x] & 0x80000000u)) stk.push_back(bt.right[x]);
+        }
+        for (size_t o = pre.size(); o-- > 0;) {
+            const uint32_t x = pre[o], l = bt.left[x], r = bt.right[x];
+            float dist[9];
+            for (int k = 2; k <= 8; ++k) {
+                float best = INFINITY;
+                for (int i = 1; i < k; ++i) {
+                    const float v = cost(l, i) + cost(r, k - i);
+                    if (v < best) best = v;
+                }
+                dist[k] = best;
+            }
+            const uint32_t cnt = count(x);
+            const float a = sa_measure(bt.box[x]);
+            float* c = &dpc[8 * size_t(x)];
+            c[0] = cnt <= uint32_t(max_leaf) ? a * float(cnt) : a + dist[8];
+            for (int k = 2; k <= 8; ++k) c[k - 1] = dist[k] < c[k - 2] ? dist[k] : c[k - 2];
+        }
+    }
+    auto split = [&](uint32_t x, int k) -> int {
+        int bj = 1;
+        float bv = INFINITY;
+        for (int j = 1; j < k; ++j) {
+            const float v = cost(bt.left[x], j) + cost(bt.right[x], k - j);
+            if (v < bv) { bv = v; bj = j; }
+        }
+        return bj;
+    };
     std::vector<uint32_t> level;  // binary node per wide node (0x80000000|p for a 1-prim root)
     level.push_back(n == 1 ? 0x80000000u : 0u);
     uint32_t next_node = 1, next_prim = 0;
@@ -638,20 +688,21 @@ static void collapse(const Binary& bt, const Box* sorted_boxes, int64_t n, int m
             uint32_t kids[8];
             int nk = 0;
             if (b & 0x80000000u) kids[nk++] = b;
-            else { kids[nk++] = bt.left[b]; kids[nk++] = bt.right[b]; }
-            while (nk < 8) {
-                int best = -1;
-                float bsa = -1.0f;
-                for (int q = 0; q < nk; ++q) {
-                    uint32_t c = kids[q];
-                    if ((c & 0x80000000u) || count(c) <= uint32_t(max_leaf)) continue;
-                    float s = sa_measure(cbox(c));
-                    if (best < 0 || s > bsa) { best = q; bsa = s; }
+            else {
+                std::vector<std::pair<uint32_t, int>> work;  // (binary node, slots), left on top
+                const int j = split(b, 8);
+                work.push_back({bt.right[b], 8 - j});
+                work.push_back({bt.left[b], j});
+                while (!work.empty()) {
+                    auto [x, k] = work.back();
+                    work.pop_back();
+                    if (x & 0x80000000u) { kids[nk++] = x; continue; }
+                    while (k > 1 && cost(x, k) == cost(x, k - 1)) --k;
+                    if (k == 1) { kids[nk++] = x; continue; }
+                    const int jj = split(x, k);
+                    work.push_back({bt.right[x], k - jj});
+                    work.push_back({bt.left[x], jj});
                 }
-                if (best < 0) break;
-                uint32_t c = kids[best];
-                kids[best] = bt.left[c];
-                kids[nk++] = bt.right[c];
             }
             size_t base = w.meta.size();
             w.meta.resize(base + 8, 0);

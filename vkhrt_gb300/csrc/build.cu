@@ -535,9 +535,21 @@ __global__ void gather_boxes_kernel(const float* boxes, const uint32_t* order, u
 }
 
 // Bottom-up refit: the second thread to reach a node computes union(left, right).
+__device__ __forceinline__ float sa_measure(const float* bx) {
+    float dx = bx[3] - bx[0], dy = bx[4] - bx[1], dz = bx[5] - bx[2];
+    return (dx * dy + dy * dz) + dz * dx;
+}
+
+// Bottom-up box refit; the second child to arrive computes its parent. With dpc, the node's
+// collapse costs as well (dpc[8 node + k - 1], k = 1..8 slots; see collapse_expand_kernel):
+//   dist(k) = min over j = 1..k-1 of cost(left, j) + cost(right, k - j)     (k >= 2)
+//   cost(node, 1) = A c if it holds c <= max_leaf primitives (a leaf slot), else A + dist(8)
+//   cost(node, k) = min(cost(node, k - 1), dist(k))
+// with A the node's surface-area measure; a primitive costs its own measure for every k.
+// Node visits and primitive tests are weighted alike.
 __global__ void refit_kernel(const uint32_t* parent_leaf, const uint32_t* parent_int, const uint32_t* left,
-                             const uint32_t* right, const float* sboxes, float* nboxes, uint32_t* visits,
-                             uint64_t n, uint32_t* err) {
+                             const uint32_t* right, const uint32_t* first, const uint32_t* last, const float* sboxes,
+                             float* nboxes, uint32_t* visits, uint64_t n, uint32_t* err, float* dpc, int max_leaf) {
     uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     uint32_t node = parent_leaf[j];
@@ -546,16 +558,41 @@ __global__ void refit_kernel(const uint32_t* parent_leaf, const uint32_t* parent
         __threadfence();
         if (atomicAdd(&visits[node], 1u) == 0u) return;
         __threadfence();
-        float b[6];
+        float b[6], v[2][6];
         uint32_t c[2] = {left[node], right[node]};
         for (int q = 0; q < 2; ++q) {
             const float* src = (c[q] & kLeafFlag) ? sboxes + 6 * uint64_t(c[q] & ~kLeafFlag) : nboxes + 6 * uint64_t(c[q]);
-            float v[6];
-            for (int k = 0; k < 6; ++k) v[k] = __ldcg(src + k);
-            if (q == 0) for (int k = 0; k < 6; ++k) b[k] = v[k];
-            else for (int k = 0; k < 3; ++k) { b[k] = fmin_t(b[k], v[k]); b[3 + k] = fmax_t(b[3 + k], v[3 + k]); }
+            for (int k = 0; k < 6; ++k) v[q][k] = __ldcg(src + k);
         }
+        for (int k = 0; k < 6; ++k) b[k] = v[0][k];
+        for (int k = 0; k < 3; ++k) { b[k] = fmin_t(b[k], v[1][k]); b[3 + k] = fmax_t(b[3 + k], v[1][3 + k]); }
         for (int k = 0; k < 6; ++k) __stcg(nboxes + 6 * uint64_t(node) + k, b[k]);
+        if (dpc) {
+            float cc[2][8];
+            for (int q = 0; q < 2; ++q) {
+                if (c[q] & kLeafFlag) {
+                    const float a = sa_measure(v[q]);
+                    for (int k = 0; k < 8; ++k) cc[q][k] = a;
+                } else {
+                    for (int k = 0; k < 8; ++k) cc[q][k] = __ldcg(dpc + 8 * uint64_t(c[q]) + k);
+                }
+            }
+            float dist[9];
+            for (int k = 2; k <= 8; ++k) {
+                float best = __int_as_float(0x7f800000);
+                for (int i = 1; i < k; ++i) {
+                    const float x = cc[0][i - 1] + cc[1][k - i - 1];
+                    if (x < best) best = x;
+                }
+                dist[k] = best;
+            }
+            const uint32_t cnt = last[node] - first[node] + 1u;
+            const float a = sa_measure(b);
+            float cost[8];
+            cost[0] = cnt <= uint32_t(max_leaf) ? a * float(cnt) : a + dist[8];
+            for (int k = 2; k <= 8; ++k) cost[k - 1] = dist[k] < cost[k - 2] ? dist[k] : cost[k - 2];
+            for (int k = 0; k < 8; ++k) __stcg(dpc + 8 * uint64_t(node) + k, cost[k]);
+        }
         node = parent_int[node];
     }
 }
@@ -565,6 +602,7 @@ struct BinView {
     const uint32_t *left, *right, *first, *last;
     const float* nboxes;  // internal node boxes
     const float* sboxes;  // sorted leaf boxes
+    const float* dpc;     // collapse costs, 8 per internal node
 };
 __device__ __forceinline__ uint32_t bcount(const BinView& b, uint32_t c) {
     return (c & kLeafFlag) ? 1u : b.last[c] - b.first[c] + 1u;
@@ -575,11 +613,28 @@ __device__ __forceinline__ const float* bbox(const BinView& b, uint32_t c) {
 __device__ __forceinline__ uint32_t bfirst(const BinView& b, uint32_t c) {
     return (c & kLeafFlag) ? (c & ~kLeafFlag) : b.first[c];
 }
-__device__ __forceinline__ float sa_measure(const float* bx) {
-    float dx = bx[3] - bx[0], dy = bx[4] - bx[1], dz = bx[5] - bx[2];
-    return (dx * dy + dy * dz) + dz * dx;
+// cost(c, k) of the collapse (refit_kernel): a primitive costs its measure for every k.
+__device__ __forceinline__ float dp_cost(const BinView& b, uint32_t c, int k) {
+    return (c & kLeafFlag) ? sa_measure(bbox(b, c)) : __ldg(b.dpc + 8 * uint64_t(c) + (k - 1));
+}
+// The k slots of internal node x go to its children as j and k - j slots, j the least of the
+// minimisers of cost(left, j) + cost(right, k - j).
+__device__ __forceinline__ int dp_split(const BinView& b, uint32_t x, int k) {
+    const uint32_t l = b.left[x], r = b.right[x];
+    int bj = 1;
+    float bv = __int_as_float(0x7f800000);
+    for (int j = 1; j < k; ++j) {
+        const float v = dp_cost(b, l, j) + dp_cost(b, r, k - j);
+        if (v < bv) { bv = v; bj = j; }
+    }
+    return bj;
 }
 
+// Children of the wide node made from binary node b, by the collapse costs: b's 8 slots are
+// split between its children; a child given k slots takes the fewest k' <= k of the same
+// cost, and with k' > 1 splits them again between its own children (left before right), so the
+// children come out in the binary tree's left-to-right order. A child holding at most max_leaf
+// primitives becomes a leaf slot; a larger one becomes a wide node of the next level.
 __global__ void collapse_expand_kernel(BinView bv, const uint32_t* level, uint32_t count, int max_leaf,
                                        uint32_t* kids, uint32_t* nk, uint32_t* nint, uint32_t* nprim) {
     uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
@@ -588,20 +643,22 @@ __global__ void collapse_expand_kernel(BinView bv, const uint32_t* level, uint32
     uint32_t k[8];
     int n = 0;
     if (b & kLeafFlag) k[n++] = b;
-    else { k[n++] = bv.left[b]; k[n++] = bv.right[b]; }
-    while (n < 8) {
-        int best = -1;
-        float bsa = -1.0f;
-        for (int q = 0; q < n; ++q) {
-            uint32_t c = k[q];
-            if ((c & kLeafFlag) || bcount(bv, c) <= uint32_t(max_leaf)) continue;
-            float s = sa_measure(bbox(bv, c));
-            if (best < 0 || s > bsa) { best = q; bsa = s; }
+    else {
+        uint32_t sx[8];
+        int sk[8], sp = 0;
+        const int j = dp_split(bv, b, 8);
+        sx[sp] = bv.right[b]; sk[sp++] = 8 - j;
+        sx[sp] = bv.left[b]; sk[sp++] = j;
+        while (sp > 0) {
+            const uint32_t x = sx[--sp];
+            int kk = sk[sp];
+            if (x & kLeafFlag) { k[n++] = x; continue; }
+            while (kk > 1 && dp_cost(bv, x, kk) == dp_cost(bv, x, kk - 1)) --kk;
+            if (kk == 1) { k[n++] = x; continue; }
+            const int jj = dp_split(bv, x, kk);
+            sx[sp] = bv.right[x]; sk[sp++] = kk - jj;
+            sx[sp] = bv.left[x]; sk[sp++] = jj;
         }
-        if (best < 0) break;
-        uint32_t c = k[best];
-        k[best] = bv.left[c];
-        k[n++] = bv.right[c];
     }
     uint32_t ni = 0, np = 0;
     for (int q = 0; q < n; ++q) {
@@ -984,6 +1041,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     uint32_t *left = nullptr, *right = nullptr, *first = nullptr, *last = nullptr, *pint = nullptr, *pleaf = nullptr,
              *visits = nullptr;
     float* nboxes = nullptr;
+    float* dpc = nullptr;
     if (n >= 2) {
         HRT_CK(cudaMalloc(&left, ni * 4));
         HRT_CK(cudaMalloc(&right, ni * 4));
@@ -993,15 +1051,17 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
         HRT_CK(dalloc(&pleaf, n, s));
         HRT_CK(dalloc(&visits, ni, s));
         HRT_CK(cudaMalloc(&nboxes, ni * 6 * sizeof(float)));
+        HRT_CK(dalloc(&dpc, ni * 8, s));
         HRT_CK(cudaMemsetAsync(pint, 0xff, ni * 4, s));
         HRT_CK(cudaMemsetAsync(visits, 0, ni * 4, s));
         karras_kernel<<<grid_for(ni, T), T, 0, s>>>(codes, int64_t(n), left, right, first, last, pint, pleaf);
-        refit_kernel<<<grid_for(n, T), T, 0, s>>>(pleaf, pint, left, right, sboxes, nboxes, visits, n, err);
+        refit_kernel<<<grid_for(n, T), T, 0, s>>>(pleaf, pint, left, right, first, last, sboxes, nboxes, visits, n, err,
+                                                  dpc, in.max_leaf);
         HRT_CK(cudaGetLastError());
     }
 
     // ---- collapse to BVH8, breadth first -----------------------------------------------------
-    BinView bv{left, right, first, last, nboxes, sboxes};
+    BinView bv{left, right, first, last, nboxes, sboxes, dpc};
     NodeF* nodes_tmp;
     HRT_CK(dalloc(&nodes_tmp, n, s));
     uint32_t *lvl_a, *lvl_b, *kids, *nk, *nint, *nprim, *int_off, *prim_off, *totals, *porder;
@@ -1098,7 +1158,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
         if (right) cudaFree(right);
         if (nboxes) cudaFree(nboxes);
     }
-    void* tmps[] = {ob, err, sboxes, first, last, pint, pleaf, visits, nodes_tmp, lvl_a, lvl_b, kids, nk, nint,
+    void* tmps[] = {ob, err, sboxes, first, last, pint, pleaf, visits, dpc, nodes_tmp, lvl_a, lvl_b, kids, nk, nint,
                     nprim, int_off, prim_off, totals, porder, dq, rad_for_boxes, chunk_incl, keys_tmp};
     for (void* p : tmps)
         if (p) cudaFreeAsync(p, s);

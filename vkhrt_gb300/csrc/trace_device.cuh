@@ -355,11 +355,7 @@ __device__ __forceinline__ float tri_hit(const TriRay& R, V3<float> o, V3<float>
     float det = U + V + W;
     if (det == 0.0f) return -1.0f;
     float Tn = U * (R.Sz * Akz) + V * (R.Sz * Bkz) + W * (R.Sz * Ckz);
-#if HRT_FAST_DIV_TRI
     float t = __fdividef(Tn, det);
-#else
-    float t = Tn / det;
-#endif
     if (!(t >= tmin) || !(t <= tmax)) return -1.0f;
     if (b1) {
         const float inv = 1.0f / det;
