@@ -169,6 +169,28 @@ def test_build_edge_cases(ctx, orc):
     check_blas(ctx, orc, PHANTOM, 1, v, r, np.array([0, 3, 6], np.uint32))         # zero-length line
 
 
+@pytest.mark.parametrize("nseg", [7, 8, 9, 16, 17, 63, 64, 65, 513])
+def test_build_collapse_sizes_bit_exact(ctx, orc, nseg):
+    # one strand of nseg segments: node fan-out boundaries of the collapse by cost
+    v, r, off = H.generate_strands(H.StrandParams(seed=nseg, nstrands=1, nverts=nseg + 1))
+    check_blas(ctx, orc, PHANTOM, 1, v, r, off)
+    check_blas(ctx, orc, LSS, 0, v, r, off)
+
+
+def test_build_collapse_ties_bit_exact(ctx, orc):
+    # 300 identical segments (every split of the collapse costs the same) and 300 segments on
+    # 30 distinct positions
+    a = np.array([[0.1, 0.2, 0.3], [0.4, 0.9, 0.3]], np.float32)
+    v = np.tile(a, (300, 1))
+    off = np.arange(0, 601, 2, dtype=np.uint32)
+    check_blas(ctx, orc, PHANTOM, 0, v, None, off)
+    rng = np.random.default_rng(4)
+    pos = rng.uniform(-1, 1, (30, 2, 3)).astype(np.float32)
+    v2 = np.ascontiguousarray(pos[rng.integers(0, 30, 300)].reshape(-1, 3))
+    check_blas(ctx, orc, DOTS, 0, v2, None, off)
+    check_blas(ctx, orc, PHANTOM, 1, v2, np.full(600, 0.01, np.float32), off)
+
+
 def test_build_rejects_bad_input(ctx):
     v = np.zeros((4, 3), np.float32)
     with pytest.raises(H.HrtError) as e:

@@ -232,3 +232,41 @@ def test_environment_map_miss(orc):
     centre = o2["fb"].reshape(6, 8, 4)[3, 4, 0]
     c_lin = -np.log(1.0 - centre ** 2.2)  # undo the tone map
     assert 0.0 <= c_lin <= 7.0  # a blend of the ramp's texels around the seam (u = 0 / 1)
+
+
+def _bvh8_nodes(orc, boxes, max_leaf=1):
+    n = len(boxes)
+    mx = max(n, 1)
+    arrs = [np.zeros(mx, np.uint32), np.zeros(mx, np.uint32), np.zeros((mx, 8), np.uint8),
+            np.zeros((mx, 8, 6), np.float32), np.zeros(n, np.uint32), np.zeros((mx, 3), np.float32),
+            np.zeros((mx, 3), np.uint8), np.zeros((mx, 3, 8), np.uint8), np.zeros((mx, 3, 8), np.uint8)]
+    nn = orc.orc_bvh8(P(np.ascontiguousarray(boxes, np.float32)), n, max_leaf, mx, *[P(a) for a in arrs])
+    return nn, arrs[2][:max(nn, 0)], arrs[4]
+
+
+@pytest.mark.parametrize("n", [2, 5, 8])
+def test_collapse_by_cost_one_node_up_to_eight(orc, n):
+    """Up to 8 primitives: one wide node with every primitive in a leaf slot (any extra node
+    adds its own surface area to the cost)."""
+    rng = np.random.default_rng(n)
+    lo = rng.uniform(0, 10, (n, 3)).astype(np.float32)
+    boxes = np.concatenate([lo, lo + rng.uniform(0.1, 1, (n, 3)).astype(np.float32)], axis=1)
+    nn, meta, order = _bvh8_nodes(orc, boxes)
+    assert nn == 1
+    assert np.count_nonzero(meta[0]) == n and not (meta[0] & 0x80).any()
+    assert np.array_equal(np.sort(order), np.arange(n))
+
+
+def test_collapse_by_cost_nine_and_ties(orc):
+    """Nine primitives need two wide nodes; identical boxes (every split costs the same) still
+    give a valid tree with every primitive once and full nodes."""
+    rng = np.random.default_rng(9)
+    lo = rng.uniform(0, 10, (9, 3)).astype(np.float32)
+    boxes = np.concatenate([lo, lo + 0.5], axis=1)
+    nn, meta, order = _bvh8_nodes(orc, boxes)
+    assert nn == 2 and np.count_nonzero(meta) == 9 + 1
+    same = np.tile(np.float32([[0, 0, 0, 1, 1, 1]]), (200, 1))
+    nn, meta, order = _bvh8_nodes(orc, same)
+    assert np.array_equal(np.sort(order), np.arange(200))
+    # 200 leaves in nodes of 8 slots: at least 29 nodes; ties must not degrade to tiny nodes
+    assert 29 <= nn <= 40
