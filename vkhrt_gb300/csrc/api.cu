@@ -322,18 +322,69 @@ hrt_status make_plan(hrt_context* ctx, const char* who, const hrt_scene_desc* sc
     return HRT_OK;
 }
 
-// Enqueues the plan's launches: per group, counter reset, frame pass, FP64 pass.
-cudaError_t enqueue_plan(const ScenePlan& P, const hrt_trace_params* p, cudaStream_t s, int sm_count) {
-    for (size_t g = 0; g < P.groups.size(); ++g) {
+// Side streams for a plan's groups: groups that cannot run the FP64 pass go on their own
+// branch (fork from and join back to the caller's stream), so the launches' tails overlap.
+struct Branches {
+    cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
+    cudaError_t create() {
+        cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+        for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+            e = cudaStreamCreateWithFlags(&aux[k], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join[k], cudaEventDisableTiming);
+        }
+        return e;
+    }
+    void destroy() {
+        for (int k = 0; k < 3; ++k) {
+            if (aux[k]) cudaStreamDestroy(aux[k]);
+            if (join[k]) cudaEventDestroy(join[k]);
+            aux[k] = nullptr;
+            join[k] = nullptr;
+        }
+        if (fork) cudaEventDestroy(fork);
+        fork = nullptr;
+    }
+};
+
+// Enqueues the plan's launches: per group, counter reset, frame pass, FP64 pass. With br, the
+// groups without Phantom BLASes (no FP64 pass, so no use of the shared resolve list) run on
+// side branches.
+cudaError_t enqueue_plan(const ScenePlan& P, const hrt_trace_params* p, cudaStream_t s, int sm_count,
+                         const Branches* br = nullptr) {
+    const size_t ng = P.groups.size();
+    std::vector<cudaStream_t> gs(ng, s);
+    int naux = 0;
+    if (br && ng > 1) {
+        bool main_taken = false;
+        for (size_t g = 0; g < ng; ++g)
+            if (P.groups[g].type_mask & (1u << HRT_BLAS_PHANTOM)) main_taken = true;
+        for (size_t g = 0; g < ng; ++g) {
+            if (P.groups[g].type_mask & (1u << HRT_BLAS_PHANTOM)) continue;
+            if (!main_taken) { main_taken = true; continue; }
+            if (naux < 3) gs[g] = br->aux[naux++];
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    if (naux) {
+        e = cudaEventRecord(br->fork, s);
+        for (int k = 0; k < naux && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(br->aux[k], br->fork, 0);
+        if (e != cudaSuccess) return e;
+    }
+    for (size_t g = 0; g < ng; ++g) {
         const ScenePlan::Group& G = P.groups[g];
-        cudaError_t e = cudaMemsetAsync(P.counters + g, 0, sizeof(TraceCounters), s);
+        e = cudaMemsetAsync(P.counters + g, 0, sizeof(TraceCounters), gs[g]);
         if (e != cudaSuccess) return e;
         TraceLaunch L = make_launch(p, P.dtable + G.first, G.count, G.work, P.counters + g, G.type_mask, P.list,
                                     P.npix, P.scratch, P.scap, P.max_spp);
-        e = launch_trace(L, P.quant, s, sm_count);
+        e = launch_trace(L, P.quant, gs[g], sm_count);
         if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    for (int k = 0; k < naux && e == cudaSuccess; ++k) {
+        e = cudaEventRecord(br->join[k], br->aux[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, br->join[k], 0);
+    }
+    return e;
 }
 
 // Sum of the groups' counters (error bits or-ed), with the device error checks.
@@ -1359,12 +1410,15 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
     // capture: per group, counter reset + the persistent trace launch (+ the FP64 pass)
     cudaStream_t cap = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    Branches br;
+    if (e == cudaSuccess) e = br.create();
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaError_t e2 = enqueue_plan(b->plan, p, cap, ctx->sm_count);
+        cudaError_t e2 = enqueue_plan(b->plan, p, cap, ctx->sm_count, &br);
         cudaError_t e3 = cudaStreamEndCapture(cap, &b->graph);
         e = e2 != cudaSuccess ? e2 : e3;
     }
+    br.destroy();
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
     if (cap) cudaStreamDestroy(cap);
     if (e != cudaSuccess) {
@@ -1433,11 +1487,13 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
         }
     }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    Branches br;
     auto cleanup = [&]() {
         plans[0].release();
         plans[1].release();
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
+        br.destroy();
     };
     if (st != HRT_OK) {
         cleanup();
@@ -1445,6 +1501,7 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
     }
     cudaError_t e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = br.create();
     const uint32_t variants[3] = {1, 2, 3}, refills[2] = {8, 16}, agains[3] = {2, 4, 8};
     float best_t = -1.0f;
     hrt_trace_params bp = *base;
@@ -1463,7 +1520,7 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
                     float tot = 0.0f;
                     for (uint32_t k = 0; k <= reps && e == cudaSuccess; ++k) {
                         e = cudaEventRecord(e0, s);
-                        if (e == cudaSuccess) e = enqueue_plan(plans[split], &p, s, ctx->sm_count);
+                        if (e == cudaSuccess) e = enqueue_plan(plans[split], &p, s, ctx->sm_count, &br);
                         if (e == cudaSuccess) e = cudaEventRecord(e1, s);
                         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
                         float ms = 0.0f;
