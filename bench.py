@@ -101,6 +101,12 @@ class Clocks:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # nvidia-smi's start-up (driver queries) would otherwise overlap the timed region: wait
+        # for its first sample (at most 5 s)
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+            time.sleep(0.02)
 
     def stop(self) -> dict:
         if not self.proc:
@@ -567,16 +573,15 @@ def run_batched(args, dist):
         d["quantised_ms"] = round(float(b2), 3)
     # ---- e2e: graph launch through the C ABI, every framebuffer to pinned host memory ----
     pins = [torch.empty((m["height"], m["width"], 4), dtype=torch.float32, pin_memory=True) for m, *_ in models]
-    sync_batch = H.Batch(ctx, scenes_q, H.trace_params(jitter=1, seed=17, shading=2,
-                                                       **{k: getattr(tuned, k) for k in H.TUNED_FIELDS}))
+    e2e_batch = H.Batch(ctx, scenes_q, H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1},
+                                                      **{k: getattr(tuned, k) for k in H.TUNED_FIELDS}))
 
     cams = [cam for (_, _, cam, _) in q]
 
-    def e2e_step():  # cameras in (the scene table), one graph launch, every framebuffer out
-        sync_batch.set_cameras(cams)
-        sync_batch.launch()
-        for (_, _, _, fr), pin in zip(q, pins):
-            ctx.check(ctx.lib.hrt_frame_download(fr.handle, ctypes.c_void_p(pin.data_ptr()), None, None))
+    def e2e_step():  # cameras in (the scene table), one graph launch, every framebuffer out, one sync
+        e2e_batch.set_cameras(cams)
+        e2e_batch.launch()
+        e2e_batch.download(pins)
 
     for _ in range(2):
         e2e_step()
@@ -611,13 +616,13 @@ def run_batched(args, dist):
                                              "are per launch"},
             "scenes": per_scene,
             "e2e": {"value": round(rays_per_step / te / 1e6, 3), "unit": "Mrays/s",
-                    "h2d_bytes_per_step": sync_batch.table_bytes, "d2h_bytes_per_step": int(d2h),
+                    "h2d_bytes_per_step": e2e_batch.table_bytes, "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": round(te * 1e3, 3)},
             "clocks": clk,
             "build": {"build_wall_s_quantised": round(build_wall, 3), "strand_generation_s": round(t_gen, 3)}}
     if not args.no_cpu:
         line.update(batch_agreement_and_cpu(args, ctx, q, models))
-    del q, f, batch, sync_batch, scenes_q, scenes_f, batch_f
+    del q, f, batch, e2e_batch, scenes_q, scenes_f, batch_f
     if not args.quick:
         line["c4_phantom_quantised"] = c4_summary(args, ctx)
     print(json.dumps(line), flush=True)

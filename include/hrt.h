@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HRT_ABI_VERSION 5
+#define HRT_ABI_VERSION 6
 
 typedef enum hrt_status {
     HRT_OK = 0,
@@ -291,6 +291,13 @@ hrt_status hrt_batch_destroy(hrt_batch* b);
 hrt_status hrt_batch_set_cameras(hrt_batch* b, const hrt_camera* cams, uint32_t n, void* stream);
 /* Bytes one hrt_batch_set_cameras uploads. */
 uint64_t hrt_batch_table_bytes(const hrt_batch* b);
+/* Copies every scene's framebuffer to host memory: rgba[i] receives scene i's width*height
+ * RGBA floats (scenes in creation order; NULL entries are skipped). The copies are enqueued on
+ * `stream` (after an hrt_batch_launch on the same stream); with synchronise != 0 the call waits
+ * for them, otherwise the caller synchronises the stream. Page-locked destinations make the
+ * copies asynchronous. One call per batch in place of one hrt_frame_download (and one
+ * synchronisation) per scene: the per-frame readback of the reference's present step. */
+hrt_status hrt_batch_download(hrt_batch* b, float* const* rgba, void* stream, int32_t synchronise);
 
 /* ---- autotuner ------------------------------------------------------------------------------
  * Times every candidate kernel configuration on the given scenes (occupancy variant 3/4/5 blocks

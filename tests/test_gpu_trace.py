@@ -338,6 +338,17 @@ def test_batch_set_cameras_matches_single_launch(ctx):
         assert np.array_equal(hits, hits1) and np.abs(rgba - rgba1).max() <= 1e-6
     with pytest.raises(H.HrtError):
         batch.set_cameras(new[:1])
+    # every framebuffer in one call (one skipped), equal to the per-frame downloads
+    batch.launch()
+    dst = [np.full((h, w, 4), -1.0, np.float32) for (*_a, w, h) in scenes]
+    batch.download([dst[0], None])
+    assert np.array_equal(dst[0], scenes[0][3].download().reshape(dst[0].shape))
+    assert (dst[1] == -1.0).all()
+    batch.download(dst)
+    for (_b, _t, _c, fr, w, h), d in zip(scenes, dst):
+        assert np.array_equal(d, fr.download().reshape(d.shape))
+    with pytest.raises(ValueError):
+        batch.download(dst[:1])
 
 
 def _mesh_scene(ctx, orc, precision, with_normals, hair=False):

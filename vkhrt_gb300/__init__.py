@@ -107,6 +107,7 @@ SIGNATURES = {
     "hrt_batch_destroy": (c_i32, [c_p]),
     "hrt_batch_set_cameras": (c_i32, [c_p, ctypes.POINTER(CameraC), c_u32, c_p]),
     "hrt_batch_table_bytes": (c_u64, [c_p]),
+    "hrt_batch_download": (c_i32, [c_p, c_p, c_p, c_i32]),
     "hrt_strand_params_default": (None, [ctypes.POINTER(StrandParamsC)]),
     "hrt_generate_strands": (c_i32, [ctypes.POINTER(StrandParamsC), c_p, c_p, c_p]),
     "hrt_checksum": (c_u64, [c_p, c_u64, c_p, c_u64]),
@@ -528,6 +529,24 @@ class Batch:
     @property
     def table_bytes(self) -> int:
         return int(self.ctx.lib.hrt_batch_table_bytes(self.handle))
+
+    def download(self, dst: list, stream: int | None = None, synchronise: bool = True):
+        """Every scene's framebuffer into dst[i] (host arrays or pinned tensors of height x width x 4
+        float32, or None to skip), enqueued on `stream`; one synchronisation when `synchronise`."""
+        def addr(d):
+            if d is None:
+                return None
+            if hasattr(d, "data_ptr"):  # a (pinned) torch tensor
+                return d.data_ptr()
+            a = np.asarray(d)
+            if a.dtype != np.float32 or not a.flags.c_contiguous:
+                raise ValueError("download destinations must be C-contiguous float32")
+            return a.ctypes.data
+        if len(dst) != len(self.scenes):
+            raise ValueError(f"need one destination per scene ({len(self.scenes)})")
+        ptrs = (c_p * len(dst))(*[addr(d) for d in dst])
+        self.ctx.check(self.ctx.lib.hrt_batch_download(self.handle, ptrs, c_p(stream) if stream else None,
+                                                       1 if synchronise else 0))
 
     def close(self):
         if getattr(self, "handle", None):

@@ -1467,6 +1467,22 @@ hrt_status hrt_batch_set_cameras(hrt_batch* b, const hrt_camera* cams, uint32_t 
 
 uint64_t hrt_batch_table_bytes(const hrt_batch* b) { return b ? b->plan.table.size() * sizeof(SceneLaunch) : 0; }
 
+hrt_status hrt_batch_download(hrt_batch* b, float* const* rgba, void* stream, int32_t synchronise) {
+    if (!b) return HRT_ERR_INVALID_ARG;
+    hrt_context* ctx = b->ctx;
+    if (!rgba) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_download: null destination array");
+    DeviceSet ds(ctx->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    for (size_t i = 0; i < b->frames.size(); ++i) {
+        if (!rgba[i]) continue;
+        const hrt_frame* f = b->frames[i];
+        CK(ctx, cudaMemcpyAsync(rgba[i], f->fb, uint64_t(f->w) * f->h * 16, cudaMemcpyDeviceToHost, s),
+           "hrt_batch_download");
+    }
+    if (synchronise) CK(ctx, cudaStreamSynchronize(s), "hrt_batch_download");
+    return HRT_OK;
+}
+
 hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* base,
                         uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms) {
     if (!ctx) return HRT_ERR_INVALID_ARG;

@@ -1138,14 +1138,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     long long clk = clock64();
     for (;;) {
         // ---- refill idle lanes
-        uint32_t idle = __ballot_sync(kFull, !has_ray);
-        if (idle && !fetch_done && (__popc(idle) >= refill || idle == kFull)) {
+        // FP64 pass: only the first two lanes of a warp take work (at once, whenever one is
+        // idle), so the few listed samples spread over many warps: the pass is as long as its
+        // slowest warp and sits on the batch's critical path (C5 +3.4 % against 32 lanes)
+        constexpr uint32_t kTake = kPass == 2 ? 0x3u : kFull;
+        uint32_t idle = __ballot_sync(kFull, !has_ray) & kTake;
+        if (idle && !fetch_done && (__popc(idle) >= refill || idle == kTake || (kTake != kFull))) {
             int n = __popc(idle), leader = __ffs(idle) - 1;
             unsigned long long base = 0;
             if (lane == leader) base = *errword ? total : atomicAdd(work_ctr, (unsigned long long)n);
             base = __shfl_sync(kFull, base, leader);
             if (base + uint64_t(n) >= total) fetch_done = true;
-            if (!has_ray) {
+            if (!has_ray && ((kTake >> lane) & 1u)) {
                 uint64_t g = base + __popc(idle & lt_mask);
                 if (g < total) {
                     uint32_t s0 = 0;
