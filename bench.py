@@ -507,14 +507,24 @@ def run_batched(args, dist):
     dist.barrier()
     clocks = Clocks(dev)
     clocks.start()
-    for _ in range(args.warmup):
-        batch.launch()
+    cams = [cam for (_, _, cam, _) in q]
+
+    def paced(b, nsteps):
+        # A step renders every scene from its cameras (their 3 KB scene-table upload starts the
+        # step, as in an interactive renderer) and ends when the replay has finished, as the
+        # sequential comparison's steps do. Replays queued back to back without this pacing ran
+        # about 4 % slower each on GB300 (cause not found).
+        for _ in range(nsteps):
+            b.set_cameras(cams)
+            b.launch()
+            torch.cuda.current_stream().synchronize()
+
+    paced(batch, args.warmup)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record()
-    for _ in range(args.steps):
-        batch.launch()
+    paced(batch, args.steps)
     e1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -552,12 +562,10 @@ def run_batched(args, dist):
     scenes_f = [(t, cam, fr) for (_, t, cam, fr) in f]
     tuned_f, _ = H.autotune(ctx, scenes_f, base, reps=2, cache=args.tune_cache, key=f"{BATCH_CONFIG}/fp32")
     batch_f = H.Batch(ctx, scenes_f, tuned_f)
-    for _ in range(args.warmup):
-        batch_f.launch()
+    paced(batch_f, args.warmup)
     torch.cuda.synchronize()
     e0.record()
-    for _ in range(args.steps):
-        batch_f.launch()
+    paced(batch_f, args.steps)
     e1.record()
     torch.cuda.synchronize()
     ms_bf = e0.elapsed_time(e1) / args.steps
@@ -582,7 +590,6 @@ def run_batched(args, dist):
             for _ in range(2)]
     streams = [torch.cuda.Stream(), torch.cuda.Stream()]
     rendered = [torch.cuda.Event(), torch.cuda.Event()]
-    cams = [cam for (_, _, cam, _) in q]
 
     def e2e_run(nsteps):
         prev = None
