@@ -441,7 +441,8 @@ hrt_status hrt_context_create(int device, hrt_context** out) {
     if (!c) return HRT_ERR_OOM;
     c->device = device;
     DeviceSet ds(device);
-    if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        prepare_frames() != cudaSuccess) {
         delete c;
         return HRT_ERR_CUDA;
     }

@@ -130,6 +130,7 @@ struct TraceLaunch {
 
 // ---- launch wrappers (trace.cu) --------------------------------------------------------------
 cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count);
+cudaError_t prepare_frames();  // frame kernels' attributes (shared memory / L1 split), once per context
 cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n,
                               float tmin, float tmax, uint32_t fp64_resolve, hrt_hit* hits,
                               TraceCounters* counters, bool quantised_nodes, cudaStream_t s, int sm_count);

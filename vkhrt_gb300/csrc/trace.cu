@@ -8,6 +8,12 @@ namespace hrt {
 
 cudaError_t launch_frames_f(const TraceLaunch& L, cudaStream_t s, int sm_count);  // trace_frames.cu
 cudaError_t launch_frames_q(const TraceLaunch& L, cudaStream_t s, int sm_count);
+cudaError_t prepare_frames_f();  // trace_frames.cu: kernel attributes, once per context
+cudaError_t prepare_frames_q();
+cudaError_t prepare_frames() {
+    cudaError_t e = prepare_frames_f();
+    return e == cudaSuccess ? prepare_frames_q() : e;
+}
 
 cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count) {
     return quantised_nodes ? launch_frames_q(L, s, sm_count) : launch_frames_f(L, s, sm_count);

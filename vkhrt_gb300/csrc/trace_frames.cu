@@ -27,4 +27,10 @@ cudaError_t launch_frames_f(const TraceLaunch& L, cudaStream_t s, int sm_count) 
     return launch_resolve<kQ>(L, s, sm_count);
 }
 
+#if HRT_FRAMES_QUANT
+cudaError_t prepare_frames_q() { return prepare_frame_kernels<true>(); }
+#else
+cudaError_t prepare_frames_f() { return prepare_frame_kernels<false>(); }
+#endif
+
 }  // namespace hrt
