@@ -1135,22 +1135,29 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         if (nl <= L.resolve_cap) { total = nl; use_list = true; }
         if (use_list && nl * L.max_spp <= L.scratch_cap) { total = nl * L.max_spp; per_sample = true; }
     }
+    // FP64 pass: only the first lanes of a warp take work (at once, whenever one is idle), two
+    // while the listed items fit two per warp of the grid, more when there are more: the few
+    // listed samples then spread over many warps instead of packing 32 divergent FP64 solves into
+    // one (the pass is as long as its slowest warp and sits on the batch's critical path; C5
+    // +3.4 % against 32 lanes)
+    uint32_t take = kFull;
+    if (kPass == 2) {
+        const uint64_t warps = uint64_t(gridDim.x) * (blockDim.x / 32);
+        const uint64_t per = (total + warps - 1) / warps;
+        take = per <= 2 ? 0x3u : (per >= 32 ? kFull : ((1u << uint32_t(per)) - 1u));
+    }
     unsigned long long cyc_node = 0, cyc_leaf = 0, cyc_other = 0;
     long long clk = clock64();
     for (;;) {
         // ---- refill idle lanes
-        // FP64 pass: only the first two lanes of a warp take work (at once, whenever one is
-        // idle), so the few listed samples spread over many warps: the pass is as long as its
-        // slowest warp and sits on the batch's critical path (C5 +3.4 % against 32 lanes)
-        constexpr uint32_t kTake = kPass == 2 ? 0x3u : kFull;
-        uint32_t idle = __ballot_sync(kFull, !has_ray) & kTake;
-        if (idle && !fetch_done && (__popc(idle) >= refill || idle == kTake || (kTake != kFull))) {
+        uint32_t idle = __ballot_sync(kFull, !has_ray) & take;
+        if (idle && !fetch_done && (__popc(idle) >= refill || idle == take || (kPass == 2))) {
             int n = __popc(idle), leader = __ffs(idle) - 1;
             unsigned long long base = 0;
             if (lane == leader) base = *errword ? total : atomicAdd(work_ctr, (unsigned long long)n);
             base = __shfl_sync(kFull, base, leader);
             if (base + uint64_t(n) >= total) fetch_done = true;
-            if (!has_ray && ((kTake >> lane) & 1u)) {
+            if (!has_ray && ((take >> lane) & 1u)) {
                 uint64_t g = base + __popc(idle & lt_mask);
                 if (g < total) {
                     uint32_t s0 = 0;
