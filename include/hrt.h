@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HRT_ABI_VERSION 6
+#define HRT_ABI_VERSION 7
 
 typedef enum hrt_status {
     HRT_OK = 0,
@@ -59,7 +59,8 @@ typedef enum hrt_geometry_type {
     HRT_BLAS_PHANTOM = 0, /* cubic Bezier segments, Phantom ray-hair intersector */
     HRT_BLAS_LSS = 1,     /* linear swept spheres (round cones, both end caps) */
     HRT_BLAS_DOTS = 2,    /* disjoint orthogonal triangle strips, 4 triangles per segment */
-    HRT_BLAS_MESH = 3     /* indexed triangle mesh (BLASType::eMesh), optional per-vertex normals */
+    HRT_BLAS_MESH = 3,    /* indexed triangle mesh (BLASType::eMesh), optional per-vertex normals */
+    HRT_BLAS_VOXELS = 4   /* hair voxelised into boxes (BLASType::eVoxels), ray-box hits */
 } hrt_geometry_type;
 
 typedef enum hrt_precision {
@@ -99,6 +100,11 @@ typedef struct hrt_blas_input {
     const uint32_t* tri_indices;
     uint64_t ntris;
     const float* normals;           /* 3 floats per vertex (interpolated at the hit), or NULL (face normal) */
+    /* HRT_BLAS_VOXELS (GenerateVoxelMesh, geometry_processor.cpp:515-602): the strands' lines are
+     * voxelised as capsules of radius const_radius on a grid of voxel_size cubes (0 = 0.1, the
+     * reference's); every filled voxel is a box primitive reporting its grid index
+     * x + y res_x + z res_x res_y as primitive id. Per-vertex radii are not used. */
+    float voxel_size;
 } hrt_blas_input;
 
 #define HRT_BUILD_KEEP_INTERMEDIATE 1u /* keep Morton codes, binary tree, boxes (hrt_blas_get) */

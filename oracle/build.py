@@ -74,6 +74,7 @@ def load() -> ctypes.CDLL:
         "orc_morton": (None, [P, i64, P]),
         "orc_lbvh": (None, [P, i64, P, P, P, P, P, P, P, P, P]),
         "orc_bvh8": (i64, [P, i64, i32, i64, P, P, P, P, P, P, P, P, P]),
+        "orc_voxelize": (i64, [P, i64, f32, f32, P, P, i64]),
         "orc_scene_create": (P, []),
         "orc_scene_destroy": (None, [P]),
         "orc_scene_add_blas": (i32, [P, i32, i64, P, P]),

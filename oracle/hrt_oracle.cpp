@@ -416,7 +416,7 @@ static inline float fmax_t(float a, float b) { return (a < b) ? b : a; }
 //   LSS:     min/max of (p0 -+ r0, p1 -+ r1)
 //   DOTS:    min/max over the segment's 12 vertices, in vertex order
 //   mesh:    min/max over the triangle's 3 vertices, in vertex order
-enum { kPhantom = 0, kLss = 1, kDots = 2, kMesh = 3 };
+enum { kPhantom = 0, kLss = 1, kDots = 2, kMesh = 3, kVoxel = 4 };
 static Box prim_box(int type, const float* data, const float* radius, int64_t i) {
     Box b;
     if (type == kPhantom) {
@@ -439,6 +439,9 @@ static Box prim_box(int type, const float* data, const float* radius, int64_t i)
             b.lo[k] = fmin_t(fmin_t(v[k], v[3 + k]), v[6 + k]);
             b.hi[k] = fmax_t(fmax_t(v[k], v[3 + k]), v[6 + k]);
         }
+    } else if (type == kVoxel) {  // lo xyz, hi xyz, grid index (bits)
+        const float* v = data + 7 * i;
+        for (int k = 0; k < 3; ++k) { b.lo[k] = v[k]; b.hi[k] = v[3 + k]; }
     } else {
         const float* v = data + 36 * i;
         for (int k = 0; k < 3; ++k) {
@@ -814,6 +817,105 @@ static float f16_to_f32(uint16_t h) {
     return f;
 }
 
+// ---- voxel hair ------------------------------------------------------------------------------
+// Restated from GenerateVoxelMesh (geometry_processor.cpp:515-602), the capsule voxelisation of
+// "Real-Time Rendering of Dynamic Line Sets using Voxel Ray Tracing" that it follows, with what
+// the reference leaves unfinished defined here:
+//   grid: origin = min over the line end points (coordinates + 0, so no -0) minus r; extent =
+//     (max + r) - origin; res = max(1, ceil(extent / size)) per axis (the reference starts at the
+//     mesh bounds and has no room for the capsules' radius);
+//   per line, d = end - start; the axes sorted by |d| descending (ties: lower axis first) are
+//     a0 (major), a1, a2; a line with |d[a0]| = 0 fills nothing. v0, v1 = the end points ordered
+//     along +a0; s = d / d[a0]; vr0 = v0 - s r, vr1 = v1 + s r; dn = sqrt((dx dx + dy dy) + dz dz);
+//     r1 = r / sqrt(1 - (d[a1]/dn)^2), r2 likewise with a2. From t0 = tmin = vr0[a0] while
+//     t0 < tmax = vr1[a0]: t1 = min(tmax, t0 + size), p1 = vr0 + s (t1 - tmin), the box from
+//     min(p0, p1) - (r1 on a1, r2 on a2) to max(p0, p1) + (r1, r2) fills every voxel of its index
+//     range floor((corner - origin) / size), clamped to the grid (the reference fills only the
+//     cells at the range's lowest x, geometry_processor.cpp:586-592); t0 = t1, p0 = p1;
+//   the filled voxels in ascending grid index i = x + y res_x + z res_x res_y become boxes
+//     lo = origin + float(x, y, z) size, hi = lo + size, reporting primitive id i (the reference
+//     gives every grid cell an AABB, geometry_processor.cpp:452-471, and its intersection shader
+//     reports t = 1 for all of them, voxel_intersection.rint:14: here a ray-box hit).
+struct VoxelGrid {
+    float origin[3], size;
+    int32_t res[3];
+};
+static VoxelGrid voxel_grid(const float* lines, int64_t n, float r, float size) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = 0; i < n; ++i)
+        for (int e = 0; e < 2; ++e)
+            for (int k = 0; k < 3; ++k) {
+                const float v = lines[6 * i + 3 * e + k] + 0.0f;
+                lo[k] = fmin_t(lo[k], v);
+                hi[k] = fmax_t(hi[k], v);
+            }
+    VoxelGrid g;
+    g.size = size;
+    for (int k = 0; k < 3; ++k) {
+        g.origin[k] = lo[k] - r;
+        const float ext = (hi[k] + r) - g.origin[k];
+        const float c = std::ceil(ext / size);
+        g.res[k] = c >= 1.0f ? int32_t(c) : 1;
+    }
+    return g;
+}
+static void voxel_axes(const float* d, int* a) {
+    a[0] = 0; a[1] = 1; a[2] = 2;
+    for (int i = 1; i < 3; ++i)  // insertion sort by |d| descending, ties keep the lower axis first
+        for (int j = i; j > 0 && std::fabs(d[a[j]]) > std::fabs(d[a[j - 1]]); --j) std::swap(a[j], a[j - 1]);
+}
+// Fills the voxels of one line (grid indices into `filled`); returns false past 2^20 steps.
+static bool voxel_line(const float* line, float r, const VoxelGrid& g, std::vector<uint8_t>& filled) {
+    const float* p = line;
+    const float* q = line + 3;
+    float d[3] = {q[0] - p[0], q[1] - p[1], q[2] - p[2]};
+    int a[3];
+    voxel_axes(d, a);
+    if (!(std::fabs(d[a[0]]) > 0.0f)) return true;
+    const float* v0 = d[a[0]] < 0.0f ? q : p;
+    const float* v1 = d[a[0]] < 0.0f ? p : q;
+    float sv[3], vr0[3], vr1[3];
+    for (int k = 0; k < 3; ++k) {
+        sv[k] = d[k] / d[a[0]];
+        const float sr = sv[k] * r;
+        vr0[k] = v0[k] - sr;
+        vr1[k] = v1[k] + sr;
+    }
+    const float dn = std::sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+    const float q1 = d[a[1]] / dn, q2 = d[a[2]] / dn;
+    const float r1 = r / std::sqrt(1.0f - q1 * q1), r2 = r / std::sqrt(1.0f - q2 * q2);
+    const float tmin = vr0[a[0]], tmax = vr1[a[0]];
+    float t0 = tmin, p0[3] = {vr0[0], vr0[1], vr0[2]};
+    const int64_t rx = g.res[0], rxy = int64_t(g.res[0]) * g.res[1];
+    for (int step = 0; t0 < tmax; ++step) {
+        if (step >= (1 << 20)) return false;
+        const float tn = t0 + g.size;
+        const float t1 = tn < tmax ? tn : tmax;
+        float p1[3], wmin[3], wmax[3];
+        for (int k = 0; k < 3; ++k) {
+            p1[k] = vr0[k] + sv[k] * (t1 - tmin);
+            wmin[k] = fmin_t(p0[k], p1[k]);
+            wmax[k] = fmax_t(p0[k], p1[k]);
+        }
+        wmin[a[1]] -= r1;
+        wmin[a[2]] -= r2;
+        wmax[a[1]] += r1;
+        wmax[a[2]] += r2;
+        int32_t mi[3], ma[3];
+        for (int k = 0; k < 3; ++k) {
+            const float f0 = std::floor((wmin[k] - g.origin[k]) / g.size), f1 = std::floor((wmax[k] - g.origin[k]) / g.size);
+            mi[k] = f0 < 0.0f ? 0 : (f0 > float(g.res[k] - 1) ? g.res[k] - 1 : int32_t(f0));
+            ma[k] = f1 < 0.0f ? 0 : (f1 > float(g.res[k] - 1) ? g.res[k] - 1 : int32_t(f1));
+        }
+        for (int32_t z = mi[2]; z <= ma[2]; ++z)
+            for (int32_t y = mi[1]; y <= ma[1]; ++y)
+                for (int32_t x = mi[0]; x <= ma[0]; ++x) filled[size_t(x + y * rx + z * rxy)] = 1;
+        t0 = t1;
+        for (int k = 0; k < 3; ++k) p0[k] = p1[k];
+    }
+    return true;
+}
+
 // ---- tracer ---------------------------------------------------------------------------------
 struct Blas {
     int type = kPhantom;
@@ -951,6 +1053,38 @@ static bool intersect_prim(const Blas& b, uint32_t inst, uint32_t s, const tvec3
                     h->n = shim::normalize(w * n0 + b1 * n1 + b2 * n2);
                 } else {
                     h->n = shim::normalize(shim::cross(v1 - v0, v2 - v0));
+                }
+            }
+        }
+    } else if (b.type == kVoxel) {
+        // ray-box: per axis the slab's entry and exit (an axis the ray runs parallel to only
+        // rejects an origin outside the slab); hit at the entry distance, or at tmin when the
+        // ray starts inside; the normal is the entry face's (the axis of the latest entry, the
+        // lower axis on ties), facing the ray
+        const float* v = b.data.data() + 7 * s;
+        T tn = -T(INFINITY), tf = T(INFINITY);
+        int ax = 0;
+        bool miss = false;
+        for (int k = 0; k < 3; ++k) {
+            if (d[k] == T(0)) {
+                if (o[k] < T(v[k]) || o[k] > T(v[3 + k])) miss = true;
+                continue;
+            }
+            T a0 = (T(v[k]) - o[k]) / d[k], a1 = (T(v[3 + k]) - o[k]) / d[k];
+            if (a0 > a1) std::swap(a0, a1);
+            if (a0 > tn) { tn = a0; ax = k; }
+            if (a1 < tf) tf = a1;
+        }
+        if (!miss && tn <= tf) {
+            const T t = tn >= tmin ? tn : (tf >= tmin ? tmin : T(-1));
+            uint32_t id;
+            std::memcpy(&id, v + 6, 4);
+            if (t >= tmin) {
+                take(t, id, T(ax), 0);
+                if (better) {
+                    tvec3<T> nn(T(0), T(0), T(0));
+                    nn[ax] = d[ax] > T(0) ? T(-1) : T(1);
+                    h->n = nn;
                 }
             }
         }
@@ -1221,6 +1355,39 @@ void orc_lbvh(const float* boxes, int64_t n, uint64_t* codes_sorted, uint32_t* s
     }
     for (int64_t i = 0; i < n; ++i) parent_leaf[i] = bt.parent_leaf[i];
 }
+// Voxelises n lines (6 floats each) as capsules of radius r on voxel_size cubes: grid_out gets
+// origin xyz, size, res xyz (as floats); out receives 7 floats per filled voxel (lo xyz, hi xyz,
+// grid index as bits) in ascending grid index, at most max_out. Returns the number of filled
+// voxels, -1 when the grid exceeds 2^31 voxels or a line needs more than 2^20 steps.
+int64_t orc_voxelize(const float* lines, int64_t n, float r, float voxel_size, float* grid_out, float* out,
+                     int64_t max_out) {
+    const VoxelGrid g = voxel_grid(lines, n, r, voxel_size);
+    for (int k = 0; k < 3; ++k) { grid_out[k] = g.origin[k]; grid_out[4 + k] = float(g.res[k]); }
+    grid_out[3] = g.size;
+    const int64_t total = int64_t(g.res[0]) * g.res[1] * g.res[2];
+    if (n == 0) return 0;
+    if (total > (int64_t(1) << 31)) return -1;
+    std::vector<uint8_t> filled(size_t(total), 0);
+    for (int64_t i = 0; i < n; ++i)
+        if (!voxel_line(lines + 6 * i, r, g, filled)) return -1;
+    int64_t m = 0;
+    const int64_t rx = g.res[0], rxy = int64_t(g.res[0]) * g.res[1];
+    for (int64_t i = 0; i < total; ++i) {
+        if (!filled[size_t(i)]) continue;
+        if (m < max_out) {
+            const int64_t xyz[3] = {i % rx, (i / rx) % g.res[1], i / rxy};
+            float* o = out + 7 * m;
+            for (int k = 0; k < 3; ++k) {
+                o[k] = g.origin[k] + float(xyz[k]) * g.size;
+                o[3 + k] = o[k] + g.size;
+            }
+            const uint32_t id = uint32_t(i);
+            std::memcpy(o + 6, &id, 4);
+        }
+        ++m;
+    }
+    return m;
+}
 // Collapse; returns the number of wide nodes. Outputs must hold max_nodes entries
 // (child_base, prim_base: max_nodes; meta: 8 max_nodes; cbox: 48 max_nodes floats;
 // prim_order: n). Quantised fields: qp (3 per node), qe (3), qlo/qhi (24 each).
@@ -1266,11 +1433,11 @@ int orc_scene_add_blas(void* s, int type, int64_t nprim, const float* data, cons
     Blas b;
     b.type = type;
     b.nprim = nprim;
-    int per = type == kPhantom ? 12 : (type == kLss ? 6 : (type == kMesh ? 9 : 36));
+    int per = type == kPhantom ? 12 : (type == kLss ? 6 : (type == kMesh ? 9 : (type == kVoxel ? 7 : 36)));
     b.data.assign(data, data + per * nprim);
     if (type == kMesh) {
         if (radius) b.radius.assign(radius, radius + 9 * nprim);  // vertex normals per triangle
-    } else if (type != kDots) {
+    } else if (type != kDots && type != kVoxel) {
         b.radius.assign(radius, radius + 2 * nprim);
     }
     build_blas(b);

@@ -185,3 +185,16 @@ def mesh_oracle_data(v, tri, nrm=None):
     data = np.ascontiguousarray(v[tri].reshape(-1, 9), np.float32)
     nd = None if nrm is None else np.ascontiguousarray(nrm[tri].reshape(-1, 9), np.float32)
     return data, nd
+
+
+VOXELS = 4
+
+
+def oracle_voxels(orc, lines: np.ndarray, r: float, size: float, max_out: int = 1 << 21):
+    """The oracle's capsule voxelisation: (count, grid [origin xyz, size, res xyz], voxels (m, 7))."""
+    lines = np.ascontiguousarray(lines, np.float32).reshape(-1, 6)
+    g = np.zeros(8, np.float32)
+    out = np.zeros((max_out, 7), np.float32)
+    m = orc.orc_voxelize(P(lines), len(lines), ctypes.c_float(r), ctypes.c_float(size), P(g), P(out), max_out)
+    assert 0 <= m <= max_out
+    return m, g, np.ascontiguousarray(out[:m])

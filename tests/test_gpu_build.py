@@ -8,7 +8,8 @@ import numpy as np
 import pytest
 
 import vkhrt_gb300 as H
-from hairscene import DOTS, LSS, MESH, PHANTOM, P, lines_from_strands, mesh_oracle_data, oracle_geometry, sphere_mesh
+from hairscene import (DOTS, LSS, MESH, PHANTOM, P, lines_from_strands, mesh_oracle_data, oracle_geometry, oracle_voxels,
+                       sphere_mesh)
 
 pytestmark = pytest.mark.gpu
 
@@ -189,6 +190,25 @@ def test_build_collapse_ties_bit_exact(ctx, orc):
     v2 = np.ascontiguousarray(pos[rng.integers(0, 30, 300)].reshape(-1, 3))
     check_blas(ctx, orc, DOTS, 0, v2, None, off)
     check_blas(ctx, orc, PHANTOM, 1, v2, np.full(600, 0.01, np.float32), off)
+
+
+@pytest.mark.parametrize("size", [0.04, 0.1])
+def test_voxel_build_bit_exact(ctx, orc, size):
+    """Voxel hair: the filled voxels (boxes in grid order), the BVH over them and the records
+    (box and grid index per slot) equal the oracle's."""
+    v, _, off = H.generate_strands(H.StrandParams(seed=21, nstrands=80, nverts=16))
+    blas = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=H.BLASType.eVoxels, vertices=v, strand_offsets=off, const_radius=0.02, voxel_size=size,
+                    keep_intermediate=True), ctx)
+    lines, _ = lines_from_strands(v, None, off)
+    m, g, vox = oracle_voxels(orc, lines, 0.02, size)
+    assert blas.info["nprims"] == m and m > 100
+    o = check_tree(blas, orc, np.ascontiguousarray(vox[:, :6]), 1, 0)
+    recs = blas.get(H.Part.PRIMS, np.float32, (m, 8))
+    assert np.array_equal(recs[:, 3].view(np.uint32), vox[o["order"], 6].view(np.uint32))
+    assert np.ascontiguousarray(recs[:, :3]).tobytes() == np.ascontiguousarray(vox[o["order"], :3]).tobytes()
+    with pytest.raises(H.HrtError):
+        blas.refit(v)  # moved strands fill other voxels: a voxel BLAS is rebuilt
 
 
 def test_build_rejects_bad_input(ctx):

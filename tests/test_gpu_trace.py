@@ -8,7 +8,8 @@ import numpy as np
 import pytest
 
 import vkhrt_gb300 as H
-from hairscene import DOTS, LSS, PHANTOM, P, OracleScene, aimed_rays, compare_hits, lines_from_strands, oracle_geometry
+from hairscene import (DOTS, LSS, PHANTOM, VOXELS, P, OracleScene, aimed_rays, compare_hits, lines_from_strands,
+                       oracle_geometry, oracle_voxels)
 
 pytestmark = pytest.mark.gpu
 
@@ -521,3 +522,29 @@ def test_serialized_blas_traces_identically(ctx, gtype, precision):
     with pytest.raises(H.HrtError) as e:
         H.BottomLevelAccelerationStructure.load(bytes(bad), ctx)
     assert "out of range" in str(e.value)
+
+
+@pytest.mark.parametrize("size", [0.03, 0.1])
+def test_voxel_frame_vs_oracle(ctx, orc, size):
+    """Voxel hair: box hits (grid index ids, entry distances, face normals) against the FP64
+    oracle on the same voxels. Shadow rays start on a voxel face and run along the plane it
+    shares with its neighbours, so whether they start inside a neighbour depends on the hit
+    point's last bits: colours are compared where the shadow flags agree, and every pixel of the
+    unshadowed debug shading must match."""
+    v, _, off = H.generate_strands(H.StrandParams(seed=23, nstrands=300, nverts=24))
+    blas = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=H.BLASType.eVoxels, vertices=v, strand_offsets=off, const_radius=0.01, voxel_size=size), ctx)
+    tlas = H.TopLevelAccelerationStructure([blas], ctx)
+    lines, _ = lines_from_strands(v, None, off)
+    m, g, vox = oracle_voxels(orc, lines, 0.01, size)
+    assert blas.info["nprims"] == m
+    osc = OracleScene(orc, [(VOXELS, vox, None)])
+    fr, rgba, hits, o = render_both(ctx, tlas, osc, 128, 96, spp=1, shading=2)
+    st, px_ok, diff = frame_checks(rgba, hits, o, 1)
+    print(size, {k: v for k, v in st.items() if k != "mism_idx"}, "pixels agreeing", px_ok.mean())
+    assert st["hits"] > 1000
+    assert st["mismatches"] == 0 and st["max_rel_t"] < 1e-5
+    assert px_ok.mean() > 0.98 and diff[px_ok].max() <= 1e-4
+    fr, rgba, hits, o = render_both(ctx, tlas, osc, 128, 96, spp=1, shading=1)
+    st, px_ok, diff = frame_checks(rgba, hits, o, 1)
+    assert st["mismatches"] == 0 and px_ok.all() and diff.max() <= 1e-6

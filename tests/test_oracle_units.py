@@ -270,3 +270,38 @@ def test_collapse_by_cost_nine_and_ties(orc):
     assert np.array_equal(np.sort(order), np.arange(200))
     # 200 leaves in nodes of 8 slots: at least 29 nodes; ties must not degrade to tiny nodes
     assert 29 <= nn <= 40
+
+
+def _voxelize(orc, lines, r=0.02, size=0.1, mx=200000):
+    lines = np.ascontiguousarray(lines, np.float32).reshape(-1, 6)
+    g = np.zeros(8, np.float32)
+    out = np.zeros((mx, 7), np.float32)
+    m = orc.orc_voxelize(P(lines), len(lines), ctypes.c_float(r), ctypes.c_float(size), P(g), P(out), mx)
+    return m, g, out[:max(m, 0)]
+
+
+def test_voxelize_known_answers(orc):
+    """Capsule voxelisation: an axis-aligned segment fills its row; a zero-length one fills
+    nothing; a diagonal one covers every point along it and its radius across the minor axes."""
+    m, g, v = _voxelize(orc, [0.05, 0.05, 0.05, 0.95, 0.05, 0.05])
+    assert m == 10 and tuple(g[4:7]) == (10, 1, 1)
+    assert np.array_equal(v[:, 6].view(np.uint32), np.arange(10, dtype=np.uint32))
+    assert np.allclose(v[:, 0], 0.03 + 0.1 * np.arange(10), atol=1e-6) and np.allclose(v[:, 3] - v[:, 0], 0.1)
+    m, g, v = _voxelize(orc, [0.3, 0.3, 0.3, 0.3, 0.3, 0.3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.05])
+    ids = set(v[:, 6].view(np.uint32).tolist())
+    assert all(i < 4 for i in ids)  # only the short segment's cells (grid 4 x 4 x 4 from the first point)
+    p0, p1 = np.array([0.0, 0.0, 0.0]), np.array([1.0, 1.0, 0.5])
+    m, g, v = _voxelize(orc, np.concatenate([p0, p1]), r=0.04)
+    res = g[4:7].astype(int)
+    ids = set(v[:, 6].view(np.uint32).tolist())
+    axis = (p1 - p0) / np.linalg.norm(p1 - p0)
+    perp = np.cross(axis, [0, 0, 1.0])
+    perp /= np.linalg.norm(perp)
+    for t in np.linspace(0, 1, 101):
+        for off in (0.0, 0.039, -0.039):
+            pt = p0 + t * (p1 - p0) + off * perp
+            ijk = np.floor((pt - g[:3]) / g[3]).astype(int)
+            assert int(ijk[0] + ijk[1] * res[0] + ijk[2] * res[0] * res[1]) in ids, (t, off)
+    # boxes come in ascending grid index and tile the grid exactly
+    gi = v[:, 6].view(np.uint32)
+    assert np.all(np.diff(gi.astype(np.int64)) > 0)

@@ -31,7 +31,7 @@ class BLASInputC(ctypes.Structure):
                 ("vertices", c_p), ("radius", c_p), ("strand_offsets", c_p), ("line_indices", c_p),
                 ("nvertices", c_u64), ("nstrands", c_u64), ("nlines", c_u64), ("const_radius", c_f),
                 ("transform", c_f * 16), ("quant_chunk", c_u32), ("flags", c_u32), ("tri_indices", c_p),
-                ("ntris", c_u64), ("normals", c_p)]
+                ("ntris", c_u64), ("normals", c_p), ("voxel_size", c_f)]
 
 
 class BLASInfoC(ctypes.Structure):
@@ -153,6 +153,7 @@ class BLASType(enum.IntEnum):
     eLSS = 1       # linear swept spheres (BLASType::eMesh with LSS geometry)
     eDOTS = 2      # disjoint orthogonal triangle strips (BLASType::eMesh triangles)
     eMesh = 3      # indexed triangle mesh (BLASType::eMesh), optional vertex normals
+    eVoxels = 4    # strands voxelised as capsules into box primitives (BLASType::eVoxels)
 
 
 class Precision(enum.IntEnum):
@@ -186,7 +187,9 @@ class Part(enum.IntEnum):
 @dataclass
 class BLASInput:
     """Geometry of one BLAS (hrt_blas_input): hair (strand_offsets or line_indices) or, for
-    BLASType.eMesh, indexed triangles (tri_indices, optional per-vertex normals)."""
+    BLASType.eMesh, indexed triangles (tri_indices, optional per-vertex normals). BLASType.eVoxels
+    voxelises the strands' lines as capsules of radius const_radius on cubes of voxel_size (0 =
+    0.1); each filled voxel reports its grid index as primitive id."""
     type: BLASType
     vertices: np.ndarray                      # (nv, 3) float32
     radius: np.ndarray | None = None          # (nv,) float32 per vertex
@@ -200,6 +203,7 @@ class BLASInput:
     max_leaf: int = 1
     quant_chunk: int = 0
     keep_intermediate: bool = False
+    voxel_size: float = 0.0
 
 
 class Context:
@@ -244,6 +248,7 @@ class BottomLevelAccelerationStructure:
         c.precision = int(inp.precision)
         c.memory = 0
         c.max_leaf = inp.max_leaf
+        c.voxel_size = inp.voxel_size
         c.vertices = _ptr(v)
         c.nvertices = v.shape[0]
         if inp.radius is not None:

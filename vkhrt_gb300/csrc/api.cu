@@ -28,6 +28,7 @@ struct hrt_blas {
     uint64_t nprims = 0;
     float build_ms = 0.0f;
     bool keep = false;
+    float voxel_grid[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // voxels: origin xyz, size, res xyz
     BuildOutput out;
     // the topology, kept on the host for hrt_blas_refit
     uint32_t max_leaf = 1, quant_chunk = 0;
@@ -572,8 +573,11 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!in || !out) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: null input or output");
     *out = nullptr;
-    if (in->type < HRT_BLAS_PHANTOM || in->type > HRT_BLAS_MESH)
+    if (in->type < HRT_BLAS_PHANTOM || in->type > HRT_BLAS_VOXELS)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: unknown geometry type %d", in->type);
+    const float voxel_size = in->voxel_size == 0.0f ? 0.1f : in->voxel_size;
+    if (in->type == HRT_BLAS_VOXELS && !(voxel_size > 0.0f && voxel_size < 1e30f))
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: voxel_size must be > 0");
     if (in->precision != HRT_PRECISION_FP32 && in->precision != HRT_PRECISION_QUANTISED)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: unknown precision %d", in->precision);
     if (in->memory != HRT_MEMORY_HOST && in->memory != HRT_MEMORY_DEVICE)
@@ -710,12 +714,23 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
     cudaEventRecord(e0, s);
     BuildInput bi{in->type, in->precision, int(max_leaf), in->quant_chunk, lines, lrad, nlines, b->keep};
     char msg[256] = {0};
-    e = build_blas_device(bi, b->out, s, msg, sizeof(msg));
+    float* vox = nullptr;
+    if (in->type == HRT_BLAS_VOXELS) {  // the lines become voxel boxes, the BVH primitives
+        uint64_t nvox = 0;
+        e = voxelize_device(lines, nlines, in->const_radius, voxel_size, &vox, &nvox, b->voxel_grid, s, msg,
+                            sizeof(msg));
+        bi.n = nvox;
+        bi.voxels = vox;
+        b->nprims = nvox;
+    }
+    if (e == cudaSuccess) e = build_blas_device(bi, b->out, s, msg, sizeof(msg));
     cudaEventRecord(e1, s);
     if (e != cudaSuccess) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         std::string m = msg;
+        cudaStreamSynchronize(s);
+        if (vox) cudaFree(vox);
         cleanup();
         free_build_output(b->out);
         delete b;
@@ -727,6 +742,7 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
     cudaEventElapsedTime(&b->build_ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (vox) cudaFree(vox);
     cleanup();
     *out = b;
     return HRT_OK;
@@ -735,6 +751,8 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
 hrt_status hrt_blas_refit(hrt_blas* b, const float* vertices, const float* per_vertex, int32_t memory, void* stream) {
     if (!b) return HRT_ERR_INVALID_ARG;
     hrt_context* ctx = b->ctx;
+    if (b->type == HRT_BLAS_VOXELS)
+        return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_refit: moved strands fill other voxels (rebuild the voxel BLAS)");
     const bool mesh = b->type == HRT_BLAS_MESH;
     const bool want = mesh ? b->has_normals : b->has_radius;
     if (b->nvertices && !vertices) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_refit: null vertices");
@@ -981,8 +999,9 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: not a version-%u BLAS image", kSerialVersion);
     const bool quant = h.precision == HRT_PRECISION_QUANTISED;
     const uint64_t want_node = quant ? sizeof(NodeQ) : sizeof(NodeF);
-    const uint64_t want_prim = h.type == HRT_BLAS_PHANTOM ? (quant ? 32 : 64) : (h.type == HRT_BLAS_LSS ? 32 : 80);
-    if (h.type < HRT_BLAS_PHANTOM || h.type > HRT_BLAS_MESH || (h.precision != HRT_PRECISION_FP32 && !quant) ||
+    const uint64_t want_prim = h.type == HRT_BLAS_PHANTOM ? (quant ? 32 : 64)
+                               : ((h.type == HRT_BLAS_LSS || h.type == HRT_BLAS_VOXELS) ? 32 : 80);
+    if (h.type < HRT_BLAS_PHANTOM || h.type > HRT_BLAS_VOXELS || (h.precision != HRT_PRECISION_FP32 && !quant) ||
         h.node_bytes != want_node || h.prim_bytes != want_prim || h.nprims >= (1ull << 29) || h.nnodes > h.nprims + 1 ||
         h.nroots > h.nprims || (h.nprims && !h.nnodes) || h.max_leaf < 1 || h.max_leaf > 3)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: inconsistent header");

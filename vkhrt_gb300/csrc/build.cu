@@ -13,6 +13,7 @@
 //   records in leaf-slot order.
 #include <cuda_fp16.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -843,6 +844,12 @@ __global__ void records_kernel(int type, int precision, const uint32_t* ids, uin
         r.a = make_float4(g[0], g[1], g[2], g[6]);
         r.b = make_float4(g[3], g[4], g[5], g[7]);
         static_cast<PrimLss*>(prims)[i] = r;
+    } else if (type == HRT_BLAS_VOXELS) {
+        const float* v = geom + 7 * uint64_t(s);
+        PrimVoxel r;
+        r.lo_id = make_float4(v[0], v[1], v[2], v[6]);
+        r.hi = make_float4(v[3], v[4], v[5], 0.0f);
+        static_cast<PrimVoxel*>(prims)[i] = r;
     } else if (type == HRT_BLAS_MESH) {
         const float* v = geom + 9 * uint64_t(s);
         const float* m = tri_nrm ? tri_nrm + 9 * uint64_t(s) : nullptr;
@@ -865,6 +872,117 @@ __global__ void records_kernel(int type, int precision, const uint32_t* ids, uin
         r.e = make_float4(g[16], g[17], __uint_as_float(s), 0.0f);
         static_cast<PrimDots*>(prims)[i] = r;
     }
+}
+
+// ============================ voxel hair ==========================================================
+// The voxeliser of the oracle's voxel_line (capsule walk along the major axis, every voxel of
+// each step's index range, clamped to the grid), one thread per line, filled voxels as bits.
+struct VoxGrid {
+    float origin[3], size;
+    int32_t res[3];
+};
+__global__ void voxel_bounds_kernel(const float* lines, uint64_t n, uint32_t* ob /*6: min xyz, max xyz*/) {
+    __shared__ uint32_t sm[6];
+    if (threadIdx.x < 3) sm[threadIdx.x] = 0xffffffffu;
+    else if (threadIdx.x < 6) sm[threadIdx.x] = 0u;
+    __syncthreads();
+    uint32_t lmin[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, lmax[3] = {0, 0, 0};
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x)
+        for (int e = 0; e < 2; ++e)
+            for (int k = 0; k < 3; ++k) {
+                const float v = lines[6 * i + 3 * e + k] + 0.0f;
+                if (!(v == v)) continue;
+                const uint32_t c = f2ord(v);
+                lmin[k] = min(lmin[k], c);
+                lmax[k] = max(lmax[k], c);
+            }
+    for (int k = 0; k < 3; ++k) { atomicMin(&sm[k], lmin[k]); atomicMax(&sm[3 + k], lmax[k]); }
+    __syncthreads();
+    if (threadIdx.x < 3) atomicMin(&ob[threadIdx.x], sm[threadIdx.x]);
+    else if (threadIdx.x < 6) atomicMax(&ob[threadIdx.x], sm[threadIdx.x]);
+}
+__global__ void voxel_fill_kernel(const float* lines, uint64_t n, float r, VoxGrid g, uint32_t* bits, uint32_t* err) {
+    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = lines + 6 * i;
+    const float* q = p + 3;
+    const float d[3] = {q[0] - p[0], q[1] - p[1], q[2] - p[2]};
+    int a[3] = {0, 1, 2};
+    for (int u = 1; u < 3; ++u)
+        for (int j = u; j > 0 && fabsf(d[a[j]]) > fabsf(d[a[j - 1]]); --j) { const int t = a[j]; a[j] = a[j - 1]; a[j - 1] = t; }
+    if (!(fabsf(d[a[0]]) > 0.0f)) return;
+    const float* v0 = d[a[0]] < 0.0f ? q : p;
+    const float* v1 = d[a[0]] < 0.0f ? p : q;
+    float sv[3], vr0[3], vr1[3];
+    for (int k = 0; k < 3; ++k) {
+        sv[k] = __fdiv_rn(d[k], d[a[0]]);
+        const float sr = sv[k] * r;
+        vr0[k] = v0[k] - sr;
+        vr1[k] = v1[k] + sr;
+    }
+    const float dn = __fsqrt_rn((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+    const float q1 = __fdiv_rn(d[a[1]], dn), q2 = __fdiv_rn(d[a[2]], dn);
+    const float r1 = __fdiv_rn(r, __fsqrt_rn(1.0f - q1 * q1)), r2 = __fdiv_rn(r, __fsqrt_rn(1.0f - q2 * q2));
+    const float tmin = vr0[a[0]], tmax = vr1[a[0]];
+    float t0 = tmin, p0[3] = {vr0[0], vr0[1], vr0[2]};
+    const int64_t rx = g.res[0], rxy = int64_t(g.res[0]) * g.res[1];
+    for (int step = 0; t0 < tmax; ++step) {
+        if (step >= (1 << 20)) { atomicOr(err, 1u); return; }
+        const float tn = t0 + g.size;
+        const float t1 = tn < tmax ? tn : tmax;
+        float p1[3], wmin[3], wmax[3];
+        for (int k = 0; k < 3; ++k) {
+            p1[k] = vr0[k] + sv[k] * (t1 - tmin);
+            wmin[k] = fmin_t(p0[k], p1[k]);
+            wmax[k] = fmax_t(p0[k], p1[k]);
+        }
+        wmin[a[1]] -= r1;
+        wmin[a[2]] -= r2;
+        wmax[a[1]] += r1;
+        wmax[a[2]] += r2;
+        int32_t mi[3], ma[3];
+        for (int k = 0; k < 3; ++k) {
+            const float f0 = floorf(__fdiv_rn(wmin[k] - g.origin[k], g.size));
+            const float f1 = floorf(__fdiv_rn(wmax[k] - g.origin[k], g.size));
+            mi[k] = f0 < 0.0f ? 0 : (f0 > float(g.res[k] - 1) ? g.res[k] - 1 : int32_t(f0));
+            ma[k] = f1 < 0.0f ? 0 : (f1 > float(g.res[k] - 1) ? g.res[k] - 1 : int32_t(f1));
+        }
+        for (int32_t z = mi[2]; z <= ma[2]; ++z)
+            for (int32_t y = mi[1]; y <= ma[1]; ++y)
+                for (int32_t x = mi[0]; x <= ma[0]; ++x) {
+                    const uint64_t v = uint64_t(x + y * rx + z * rxy);
+                    atomicOr(&bits[v >> 5], 1u << (v & 31u));
+                }
+        t0 = t1;
+        for (int k = 0; k < 3; ++k) p0[k] = p1[k];
+    }
+}
+__global__ void popc_kernel(const uint32_t* bits, uint64_t nw, uint32_t* cnt) {
+    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < nw) cnt[i] = __popc(bits[i]);
+}
+__global__ void voxel_emit_kernel(const uint32_t* bits, const uint32_t* off, uint64_t nw, VoxGrid g, float* vox) {
+    const uint64_t w = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (w >= nw) return;
+    uint32_t b = bits[w], o = off[w];
+    const int64_t rx = g.res[0], rxy = int64_t(g.res[0]) * g.res[1];
+    while (b) {
+        const uint32_t j = __ffs(b) - 1;
+        b &= b - 1u;
+        const int64_t idx = int64_t(w) * 32 + j;
+        const int64_t xyz[3] = {idx % rx, (idx / rx) % g.res[1], idx / rxy};
+        float* v = vox + 7 * uint64_t(o++);
+        for (int k = 0; k < 3; ++k) {
+            v[k] = g.origin[k] + float(xyz[k]) * g.size;
+            v[3 + k] = v[k] + g.size;
+        }
+        v[6] = __uint_as_float(uint32_t(idx));
+    }
+}
+__global__ void boxes_voxel_kernel(const float* vox, uint64_t n, float* boxes) {
+    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = 0; k < 6; ++k) boxes[6 * i + k] = vox[7 * i + k];
 }
 
 template <class T> cudaError_t dalloc(T** p, uint64_t count, cudaStream_t s) {
@@ -909,6 +1027,84 @@ void free_build_output(BuildOutput& o) {
             return e_;                                                                         \
         }                                                                                      \
     } while (0)
+
+static float ord2f_host(uint32_t u) {
+    const uint32_t b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+cudaError_t voxelize_device(const float* lines, uint64_t nlines, float r, float size, float** vox, uint64_t* nvox,
+                            float grid[8], cudaStream_t s, char* msg, size_t msglen) {
+    *vox = nullptr;
+    *nvox = 0;
+    const unsigned T = 256;
+    uint32_t* ob = nullptr;
+    HRT_CK(dalloc(&ob, 6, s));
+    const uint32_t init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+    HRT_CK(cudaMemcpyAsync(ob, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    if (nlines)
+        voxel_bounds_kernel<<<unsigned(grid_for(nlines, T) < 1024 ? grid_for(nlines, T) : 1024), T, 0, s>>>(lines, nlines, ob);
+    uint32_t hob[6];
+    HRT_CK(cudaMemcpyAsync(hob, ob, sizeof(hob), cudaMemcpyDeviceToHost, s));
+    HRT_CK(cudaStreamSynchronize(s));
+    cudaFreeAsync(ob, s);
+    // grid (the oracle's voxel_grid: adds, one division and a ceiling per axis)
+    VoxGrid g;
+    g.size = size;
+    uint64_t total = 1;
+    for (int k = 0; k < 3; ++k) {
+        const float lo = ord2f_host(hob[k]), hi = ord2f_host(hob[3 + k]);
+        g.origin[k] = lo - r;
+        const float ext = (hi + r) - g.origin[k];
+        const float c = std::ceil(ext / size);
+        g.res[k] = c >= 1.0f ? int32_t(c) : 1;
+        if (!(c < 2147483648.0f)) g.res[k] = 0x7fffffff;
+        total *= uint64_t(g.res[k]);
+        grid[k] = g.origin[k];
+        grid[4 + k] = float(g.res[k]);
+    }
+    grid[3] = size;
+    if (nlines == 0) return cudaSuccess;
+    if (total > (1ull << 31)) {
+        snprintf(msg, msglen, "voxel grid of %llu cells; the limit is 2^31 (raise voxel_size)", (unsigned long long)total);
+        return cudaErrorInvalidValue;
+    }
+    const uint64_t nw = (total + 31) / 32;
+    uint32_t *bits = nullptr, *cnt = nullptr, *off = nullptr, *tot = nullptr, *err = nullptr;
+    HRT_CK(dalloc(&bits, nw, s));
+    HRT_CK(dalloc(&cnt, nw, s));
+    HRT_CK(dalloc(&off, nw, s));
+    HRT_CK(dalloc(&tot, 1, s));
+    HRT_CK(dalloc(&err, 1, s));
+    HRT_CK(cudaMemsetAsync(bits, 0, nw * 4, s));
+    HRT_CK(cudaMemsetAsync(err, 0, 4, s));
+    voxel_fill_kernel<<<grid_for(nlines, T), T, 0, s>>>(lines, nlines, r, g, bits, err);
+    popc_kernel<<<grid_for(nw, T), T, 0, s>>>(bits, nw, cnt);
+    HRT_CK(cudaGetLastError());
+    HRT_CK(device_scan<SumOp>(cnt, off, nw, false, tot, s));
+    uint32_t h[2];
+    HRT_CK(cudaMemcpyAsync(&h[0], tot, 4, cudaMemcpyDeviceToHost, s));
+    HRT_CK(cudaMemcpyAsync(&h[1], err, 4, cudaMemcpyDeviceToHost, s));
+    HRT_CK(cudaStreamSynchronize(s));
+    if (h[1]) {
+        snprintf(msg, msglen, "a line needs more than 2^20 voxel steps (raise voxel_size)");
+        cudaFreeAsync(bits, s); cudaFreeAsync(cnt, s); cudaFreeAsync(off, s); cudaFreeAsync(tot, s); cudaFreeAsync(err, s);
+        return cudaErrorInvalidValue;
+    }
+    *nvox = h[0];
+    if (h[0]) {
+        HRT_CK(cudaMalloc(vox, uint64_t(h[0]) * 7 * sizeof(float)));
+        voxel_emit_kernel<<<grid_for(nw, T), T, 0, s>>>(bits, off, nw, g, *vox);
+        HRT_CK(cudaGetLastError());
+    }
+    cudaFreeAsync(bits, s);
+    cudaFreeAsync(cnt, s);
+    cudaFreeAsync(off, s);
+    cudaFreeAsync(tot, s);
+    cudaFreeAsync(err, s);
+    return cudaSuccess;
+}
 
 // Geometry processing shared by build and refit: per-segment boxes into `boxes`, the
 // intersected geometry into out.curves / out.geom and, for quantised Phantom, the chunk roots
@@ -984,6 +1180,8 @@ cudaError_t geometry_stage(const BuildInput& in, BuildOutput& out, float* boxes,
         boxes_lss_kernel<<<grid_for(n, T), T, 0, s>>>(out.geom, n, boxes);
     } else if (in.type == HRT_BLAS_MESH) {
         boxes_tri_kernel<<<grid_for(n, T), T, 0, s>>>(in.tris, n, boxes);
+    } else if (in.type == HRT_BLAS_VOXELS) {
+        boxes_voxel_kernel<<<grid_for(n, T), T, 0, s>>>(in.voxels, n, boxes);
     } else {
         if (!out.geom) HRT_CK(cudaMalloc(&out.geom, n * 18 * sizeof(float)));
         dots_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, out.geom);
@@ -998,7 +1196,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     const unsigned T = 256;
     out.node_bytes = in.precision == HRT_PRECISION_QUANTISED ? sizeof(NodeQ) : sizeof(NodeF);
     if (in.type == HRT_BLAS_PHANTOM) out.prim_bytes = in.precision == HRT_PRECISION_QUANTISED ? 32 : 64;
-    else out.prim_bytes = in.type == HRT_BLAS_LSS ? 32 : 80;  // DOTS and mesh triangles: 80
+    else out.prim_bytes = (in.type == HRT_BLAS_LSS || in.type == HRT_BLAS_VOXELS) ? 32 : 80;  // DOTS, mesh: 80
     if (n == 0) return cudaSuccess;
 
     // ---- geometry processing -> per-segment boxes (and the intersected geometry) ----------------
@@ -1119,7 +1317,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     map_order_kernel<<<grid_for(n, T), T, 0, s>>>(porder, order, n, out.prim_ids);
     HRT_CK(cudaMalloc(&out.prims, n * out.prim_bytes));
     records_kernel<<<grid_for(n, T), T, 0, s>>>(in.type, in.precision, out.prim_ids, n, out.curves, in.lrad,
-                                                in.type == HRT_BLAS_MESH ? in.tris : out.geom, chunk_incl, out.roots,
+                                                in.type == HRT_BLAS_MESH ? in.tris : (in.type == HRT_BLAS_VOXELS ? in.voxels : out.geom), chunk_incl, out.roots,
                                                 in.tri_normals, out.prims);
     HRT_CK(cudaGetLastError());
 

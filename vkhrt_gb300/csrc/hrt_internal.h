@@ -142,6 +142,10 @@ cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, uint32_t nin
                                hrt_hit* host_hits, cudaStream_t s, int sm_count, uint32_t* error_word);
 
 // ---- BVH build (build.cu) ----------------------------------------------------------------------
+// Voxel primitive record (HRT_BLAS_VOXELS): box lo + grid index (bits), box hi.
+struct PrimVoxel {
+    float4 lo_id, hi;
+};
 struct BuildInput {
     int type, precision, max_leaf;
     uint32_t quant_chunk;
@@ -151,7 +155,13 @@ struct BuildInput {
     bool keep_intermediate;
     const float* tris = nullptr;         // mesh: device, n x 9 (triangle vertices)
     const float* tri_normals = nullptr;  // mesh: device, n x 9 (vertex normals), or null
+    const float* voxels = nullptr;       // voxels: device, n x 7 (box lo xyz, hi xyz, grid index bits)
 };
+// Voxelises nlines device lines (6 floats each) as capsules of radius r on cubes of `size`:
+// allocates *vox (7 floats per filled voxel, ascending grid index), sets *nvox and grid
+// (origin xyz, size, res xyz as floats).
+cudaError_t voxelize_device(const float* lines, uint64_t nlines, float r, float size, float** vox, uint64_t* nvox,
+                            float grid[8], cudaStream_t s, char* msg, size_t msglen);
 struct BuildOutput {
     // owned device allocations (freed by the BLAS)
     void* nodes = nullptr;        // NodeF or NodeQ (per precision)

@@ -478,6 +478,37 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         }
         return false;
     }
+    if (type == HRT_BLAS_VOXELS) {
+        // a voxel box: per axis the slab's entry and exit (an axis the ray runs parallel to only
+        // rejects an origin outside the slab); hit at the entry distance, or at tmin when the ray
+        // starts inside; the entry face is the axis of the latest entry (the lower axis on ties)
+        const PrimVoxel* pr = static_cast<const PrimVoxel*>(B.prims) + slot;
+        const float4 lo = __ldg(&pr->lo_id), hi = __ldg(&pr->hi);
+        const float L3[3] = {lo.x, lo.y, lo.z}, H3[3] = {hi.x, hi.y, hi.z};
+        const float O3[3] = {R.o.x, R.o.y, R.o.z}, D3[3] = {R.d.x, R.d.y, R.d.z};
+        float tn = -__int_as_float(0x7f800000), tf = __int_as_float(0x7f800000);
+        int ax = 0;
+        bool miss = false;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (D3[k] == 0.0f) {
+                if (O3[k] < L3[k] || O3[k] > H3[k]) miss = true;
+                continue;
+            }
+            float a0 = __fdiv_rn(L3[k] - O3[k], D3[k]), a1 = __fdiv_rn(H3[k] - O3[k], D3[k]);
+            if (a0 > a1) { const float t = a0; a0 = a1; a1 = t; }
+            if (a0 > tn) { tn = a0; ax = k; }
+            if (a1 < tf) tf = a1;
+        }
+        if (miss || !(tn <= tf)) return false;
+        const float t = tn >= R.tmin ? tn : (tf >= R.tmin ? R.tmin : -1.0f);
+        if (!(t >= R.tmin) || !(t <= h.t)) return false;
+        const uint32_t id = __float_as_uint(lo.w);
+        if (!beats(t, inst, id, h)) return false;
+        const float face = float(ax + 1) * (D3[ax] > 0.0f ? -1.0f : 1.0f);
+        h = Hit{t, id, inst, slot, face, 0.0f, 0.0f, 0u};
+        return true;
+    }
     if (type == HRT_BLAS_MESH) {  // renderer.cpp:543-582: one triangle per slot, id = triangle index
         const PrimTri* pr = static_cast<const PrimTri*>(B.prims) + slot;
         const float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c);
@@ -831,6 +862,13 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         const V3<float> ax = mk(__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z));
         n = normalize_rn(mk(fmaf(-h.u, ax.x, fmaf(h.sl, d.x, -w0.x)), fmaf(-h.u, ax.y, fmaf(h.sl, d.y, -w0.y)),
                             fmaf(-h.u, ax.z, fmaf(h.sl, d.z, -w0.z))));
+    } else if (B.type == HRT_BLAS_VOXELS) {
+        // the entry face's normal, facing the ray; h.u = +-(axis + 1), negative when the ray
+        // runs along +axis
+        const float u = h.u;
+        const int ax = int(fabsf(u)) - 1;
+        const float sg = u < 0.0f ? -1.0f : 1.0f;
+        n = mk(ax == 0 ? sg : 0.0f, ax == 1 ? sg : 0.0f, ax == 2 ? sg : 0.0f);
     } else if (B.type == HRT_BLAS_MESH) {
         // triangle_closest_hit.rchit:19-41: vertex normals interpolated with the hit's
         // barycentrics (1 - u - v, u, v); without normals, the face normal
