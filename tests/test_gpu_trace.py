@@ -548,3 +548,20 @@ def test_voxel_frame_vs_oracle(ctx, orc, size):
     fr, rgba, hits, o = render_both(ctx, tlas, osc, 128, 96, spp=1, shading=1)
     st, px_ok, diff = frame_checks(rgba, hits, o, 1)
     assert st["mismatches"] == 0 and px_ok.all() and diff.max() <= 1e-6
+
+
+def test_voxel_blas_serializes(ctx):
+    """A voxel BLAS round-trips through serialize/load (identical hits on explicit rays) and
+    stays non-refittable."""
+    v, _, off = H.generate_strands(H.StrandParams(seed=25, nstrands=200, nverts=16))
+    blas = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=H.BLASType.eVoxels, vertices=v, strand_offsets=off, voxel_size=0.05), ctx)
+    b2 = H.BottomLevelAccelerationStructure.load(blas.serialize(), ctx)
+    assert b2.info["nprims"] == blas.info["nprims"] and b2.info["nnodes"] == blas.info["nnodes"]
+    lines, _ = lines_from_strands(v, None, off)
+    rays = aimed_rays(np.random.default_rng(26), lines, 4000, spread=0.02)
+    t1, t2 = H.TopLevelAccelerationStructure([blas], ctx), H.TopLevelAccelerationStructure([b2], ctx)
+    h1 = H.trace_rays(ctx, t1, rays)
+    assert (h1["t"] >= 0).sum() > 1000 and np.array_equal(h1, H.trace_rays(ctx, t2, rays))
+    with pytest.raises(H.HrtError):
+        b2.refit(v)
