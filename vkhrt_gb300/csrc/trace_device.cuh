@@ -366,6 +366,39 @@ __device__ __forceinline__ float tri_hit(const TriRay& R, V3<float> o, V3<float>
     return t;
 }
 
+// The two triangles (A0, A1, A2) and (A0, B1, A1) of a quad, sharing the edge A0-A1: the shared
+// vertices are transformed once and the second triangle's edge function on A0-A1 is the exact
+// negation of the first's, so no ray passes between them. t0 / t1 as tri_hit returns them.
+__device__ __forceinline__ void quad_hit(const TriRay& R, V3<float> o, V3<float> A0, V3<float> A1, V3<float> A2,
+                                         V3<float> B1, float tmin, float tmax, float* t0, float* t1) {
+    auto xf = [&](V3<float> v, float* px, float* py, float* pz) {
+        const V3<float> q = v - o;
+        const float z = comp(q, R.kz);
+        *px = comp(q, R.kx) - R.Sx * z;
+        *py = comp(q, R.ky) - R.Sy * z;
+        *pz = z;
+    };
+    float ax, ay, az, bx, by, bz, cx, cy, cz, dx, dy, dz;
+    xf(A0, &ax, &ay, &az);
+    xf(A1, &bx, &by, &bz);
+    xf(A2, &cx, &cy, &cz);
+    xf(B1, &dx, &dy, &dz);
+    const float wab = bx * ay - by * ax;  // edge A0-A1 of the first triangle
+    auto finish = [&](float U, float V, float W, float az0, float bz0, float cz0) -> float {
+        if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return -1.0f;
+        const float det = U + V + W;
+        if (det == 0.0f) return -1.0f;
+        const float Tn = U * (R.Sz * az0) + V * (R.Sz * bz0) + W * (R.Sz * cz0);
+        const float t = __fdividef(Tn, det);
+        if (!(t >= tmin) || !(t <= tmax)) return -1.0f;
+        return t;
+    };
+    // (A0, A1, A2): U = E(A2, A1), V = E(A0, A2), W = E(A1, A0)
+    *t0 = finish(cx * by - cy * bx, ax * cy - ay * cx, wab, az, bz, cz);
+    // (A0, B1, A1): U = E(A1, B1), V = E(A0, A1) = -W of the first, W = E(B1, A0)
+    *t1 = finish(bx * dy - by * dx, -wab, dx * ay - dy * ax, az, dz, bz);
+}
+
 // ---------------------------------------------------------------- hit state
 struct Hit {
     float t;
@@ -533,12 +566,15 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         V3<float> A0 = s0 + va[face], A1 = e0 - vb[face], A2 = e0 + vb[face];
         V3<float> B1 = s0 - va[face];
         // triangle 2 face: (start+v*ra, end-v*rb, end+v*rb); 2 face+1: (start+v*ra, start-v*ra, end-v*rb)
-        float t0 = tri_hit(R.tr, R.o, A0, A1, A2, R.tmin, h.t);
+        float t0, t1;
+        quad_hit(R.tr, R.o, A0, A1, A2, B1, R.tmin, h.t, &t0, &t1);
         if (t0 >= 0.0f) {
             uint32_t id = 4u * seg + 2u * face;
             if (beats(t0, inst, id, h)) { h = Hit{t0, id, inst, slot, 0.0f, 0.0f, 0.0f, 0u}; any = true; }
         }
+#if !HRT_QUAD
         float t1 = tri_hit(R.tr, R.o, A0, B1, A1, R.tmin, h.t);
+#endif
         if (t1 >= 0.0f) {
             uint32_t id = 4u * seg + 2u * face + 1u;
             if (beats(t1, inst, id, h)) { h = Hit{t1, id, inst, slot, 0.0f, 0.0f, 0.0f, 0u}; any = true; }
