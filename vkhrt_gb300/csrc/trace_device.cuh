@@ -572,9 +572,6 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
             uint32_t id = 4u * seg + 2u * face;
             if (beats(t0, inst, id, h)) { h = Hit{t0, id, inst, slot, 0.0f, 0.0f, 0.0f, 0u}; any = true; }
         }
-#if !HRT_QUAD
-        float t1 = tri_hit(R.tr, R.o, A0, B1, A1, R.tmin, h.t);
-#endif
         if (t1 >= 0.0f) {
             uint32_t id = 4u * seg + 2u * face + 1u;
             if (beats(t1, inst, id, h)) { h = Hit{t1, id, inst, slot, 0.0f, 0.0f, 0.0f, 0u}; any = true; }
