@@ -157,9 +157,11 @@ def test_two_instances_ids(ctx, orc):
 @pytest.mark.parametrize("split", [0, 1])
 def test_batch_equals_single_launches(ctx, orc, split):
     scenes = []
-    for k, (gt, ns, w, h, spp) in enumerate([(PHANTOM, 200, 64, 48, 1), (LSS, 300, 80, 40, 2), (DOTS, 150, 40, 40, 3)]):
+    for k, (gt, ns, w, h, spp) in enumerate([(PHANTOM, 200, 64, 48, 1), (LSS, 300, 80, 40, 2), (DOTS, 150, 40, 40, 3),
+                                             (VOXELS, 250, 48, 40, 2)]):
         v, r, off = H.generate_strands(H.StrandParams(seed=50 + k, nstrands=ns, nverts=16))
-        b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType(gt), vertices=v, radius=r, strand_offsets=off), ctx)
+        b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType(gt), vertices=v, radius=r, strand_offsets=off,
+                                                           voxel_size=0.05), ctx)
         t = H.TopLevelAccelerationStructure([b], ctx)
         scenes.append((b, t, H.scene_camera(w, h), H.Frame(ctx, w, h, spp, with_hits=True), w, h, spp))
     p = H.trace_params(shading=2, record_hits=1, jitter=1, seed=4, split_types=split)
