@@ -88,6 +88,14 @@ template <class T> __device__ __forceinline__ V3<T> bez_axis(const V3<T>* c, T t
 // re-solves the candidates whose FP32 iteration does not converge. FP64 divides exactly.
 template <class T> __device__ __forceinline__ T prhi_div(T a, T b) { return a / b; }
 template <> __device__ __forceinline__ float prhi_div<float>(float a, float b) { return __fdividef(a, b); }
+// Square roots of the FP32 intersectors: the approximate root of PTX (sqrt.approx.f32, relative
+// error about 2^-23); FP64 takes the exact root.
+template <class T> __device__ __forceinline__ T prhi_sqrt(T x) { return sqrt(x); }
+template <> __device__ __forceinline__ float prhi_sqrt<float>(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 // cylinder.glsl:8-46 (capped cylinder, boolean; no range test on t)
 template <class T> __device__ __forceinline__ bool ray_cylinder(V3<T> o, V3<T> d, V3<T> p0, V3<T> p1, T r) {
     V3<T> ba = p1 - p0, oc = o - p0;
@@ -97,7 +105,7 @@ template <class T> __device__ __forceinline__ bool ray_cylinder(V3<T> o, V3<T> d
     T k0 = baba * dot(oc, oc) - baoc * baoc - r * r * baba;
     T h = k1 * k1 - k2 * k0;
     if (h < T(0)) return false;
-    h = sqrt(h);
+    h = prhi_sqrt(h);
     T t = prhi_div(-k1 - h, k2);
     T y = baoc + t * bard;
     if (y > T(0) && y < baba) return true;
@@ -158,8 +166,8 @@ template <class T> __device__ __forceinline__ T rel_coord(T a, T b, T ts, T d) {
 
 // hair_intersection.rint:15-130 with the cone radius r0 + (r1 - r0) t (constant when equal).
 // The solve runs from o' = o + ts d, the ray point nearest the chord midpoint, on the vectors
-// P - o' kept at full precision (o' itself is never rounded); ts is added back to the
-// distance. The result is the same in exact arithmetic; in FP32 it removes the cancellation of
+// P - o' (o' itself is never rounded: P0 - o' is exact, the others add the control-point
+// differences to it in FP32); ts is added back to the distance. The result is the same in exact arithmetic; in FP32 it removes the cancellation of
 // the world-space bounding-cylinder test from a distant origin (hair_intersection.rint:29).
 // The bounding radius is sqrt(|cross|^2 / |chord|^2) (one root instead of two), and the Newton
 // iteration evaluates the Bezier point and tangent from the power form of the control points
@@ -173,16 +181,27 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
     out.ts = ts;
     // the end points first: the bounding-cylinder early-out needs only them
     V3<T> W[4];
-#pragma unroll
-    for (int k = 0; k < 4; k += 3)
-        W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
     V3<T> mid = bez_point(P, T(0.5));
     const V3<T> cr = cross(mid - P[0], mid - P[3]), ch = P[3] - P[0];
-    T rmax = sqrt(prhi_div(dot(cr, cr), dot(ch, ch))) + gmax(r0, r1);
-    if (!ray_cylinder(mk(T(0), T(0), T(0)), d, W[0], W[3], rmax)) return out;
+    T rmax = prhi_sqrt(prhi_div(dot(cr, cr), dot(ch, ch))) + gmax(r0, r1);
+    if constexpr (std::is_same<T, float>::value) {
+        // FP32: P0 - o' exactly, the other points through the control-point differences
+        // (rounded once, an error of 2^-24 times a segment's extent rather than the camera
+        // distance): 3 exact relative coordinates instead of 12
+        W[0] = mk(rel_coord(P[0].x, o.x, ts, d.x), rel_coord(P[0].y, o.y, ts, d.y), rel_coord(P[0].z, o.z, ts, d.z));
+        W[3] = W[0] + ch;
+        if (!ray_cylinder(mk(0.0f, 0.0f, 0.0f), d, W[0], W[3], rmax)) return out;
+        W[1] = W[0] + (P[1] - P[0]);
+        W[2] = W[0] + (P[2] - P[0]);
+    } else {
 #pragma unroll
-    for (int k = 1; k < 3; ++k)
-        W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
+        for (int k = 0; k < 4; k += 3)
+            W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
+        if (!ray_cylinder(mk(T(0), T(0), T(0)), d, W[0], W[3], rmax)) return out;
+#pragma unroll
+        for (int k = 1; k < 3; ++k)
+            W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
+    }
     V3<T> Q[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) Q[k] = mk(dot(F.e1, W[k]), dot(F.e2, W[k]), dot(F.e3, W[k]));
@@ -209,7 +228,7 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
             T det = b * b - a * cc;
             bool isect = det > T(0);
             last_isect = isect;
-            T s = prhi_div(b - (isect ? sqrt(det) : T(0)), cc);
+            T s = prhi_div(b - (isect ? prhi_sqrt(det) : T(0)), cc);
             T dt = prhi_div(s * ax.z - cdd, ddd);
             if (isect && gabs(dt) < T(5e-5)) {
                 out.sl = s + c.z;
@@ -258,7 +277,8 @@ __device__ __noinline__ void prhi_fp64(float ox, float oy, float oz, float dx, f
 // ---------------------------------------------------------------- LSS (round cone)
 // Envelope of spheres a + u (b-a), radius ra + u (rb-ra): tangent-cone roots with u in [0,1]
 // and both end spheres; the least t >= tmin wins. Solved from o' = o + ts d (the ray point
-// nearest the segment midpoint) on the full-precision vectors a - o', b - o'; t = ts + t'.
+// nearest the segment midpoint) on a - o' at full precision and b - o' = (a - o') + (b - a);
+// t = ts + t'.
 // Quadratic coefficients are formed with cross products (Lagrange's identity) so that no term
 // is the small difference of two large ones: for the sphere, h = r^2 |d|^2 - |oc x d|^2.
 // Quotients by a reciprocal from the fast division (within 2 ulp); the hit distances stay
@@ -269,7 +289,7 @@ __device__ __forceinline__ float sphere_hit(V3<float> oc, V3<float> d, float r, 
     V3<float> c = cross(oc, d);
     float h = r * r * A - dot(c, c);
     if (h < 0.0f) return best;
-    float sh = sqrtf(h);
+    float sh = prhi_sqrt(h);
     const float iA = lss_rcp(A);
     float t0 = (-B - sh) * iA, t1 = (-B + sh) * iA;
     if (t0 >= tmin && t0 < best) return t0;
@@ -285,11 +305,11 @@ __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> 
     const float kNone = __int_as_float(0x7f800000);
     float ts = dot(0.5f * (a + b) - o_in, d) * lss_rcp(dot(d, d));
     V3<float> wa = mk(rel_coord(a.x, o_in.x, ts, d.x), rel_coord(a.y, o_in.y, ts, d.y), rel_coord(a.z, o_in.z, ts, d.z));
-    V3<float> wb = mk(rel_coord(b.x, o_in.x, ts, d.x), rel_coord(b.y, o_in.y, ts, d.y), rel_coord(b.z, o_in.z, ts, d.z));
+    V3<float> ba = b - a;
+    V3<float> wb = wa + ba;  // b - o' through the segment vector (rounded at its own scale)
     V3<float> oa = mk(-wa.x, -wa.y, -wa.z);
     float tmin = tmin_in - ts;
     float best = kNone, bu = 0.0f;
-    V3<float> ba = b - a;
     float dr = rb - ra;
     float L2 = dot(ba, ba);
     float m = L2 - dr * dr;
@@ -302,7 +322,7 @@ __device__ __forceinline__ float lss_hit(V3<float> o_in, V3<float> d, V3<float> 
         float C = dot(c1, c1) - dr * dr * dot(oa, oa) - 2.0f * ra * dr * ybo - ra * ra * L2;
         float h = B * B - A * C;
         if (h >= 0.0f && A != 0.0f) {
-            float sh = sqrtf(h);
+            float sh = prhi_sqrt(h);
             const float iA = lss_rcp(A), im = lss_rcp(m);
             float r0 = (-B - sh) * iA, r1 = (-B + sh) * iA;
             float lo = gmin(r0, r1), hi = gmax(r0, r1);
