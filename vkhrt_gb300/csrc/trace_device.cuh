@@ -113,6 +113,23 @@ template <class T> __device__ __forceinline__ bool ray_cylinder(V3<T> o, V3<T> d
     return gabs(k1 + k2 * t) < h;
 }
 
+// ray_cylinder for a ray through the origin and the cylinder p0 .. p0 + ba, with baba = |ba|^2
+// given (FP32 Phantom early-out, on coordinates relative to the ray's reference point)
+__device__ __forceinline__ bool ray_cylinder0(V3<float> d, V3<float> p0, V3<float> ba, float baba, float r) {
+    const float bard = dot(ba, d), baoc = -dot(ba, p0);
+    const float k2 = baba - bard * bard;
+    const float k1 = -baba * dot(p0, d) - baoc * bard;
+    const float k0 = baba * dot(p0, p0) - baoc * baoc - r * r * baba;
+    float h = k1 * k1 - k2 * k0;
+    if (h < 0.0f) return false;
+    h = prhi_sqrt(h);
+    float t = prhi_div(-k1 - h, k2);
+    const float y = baoc + t * bard;
+    if (y > 0.0f && y < baba) return true;
+    t = prhi_div((y < 0.0f ? 0.0f : baba) - baoc, bard);
+    return fabsf(k1 + k2 * t) < h;
+}
+
 // The cubic in power form, C3 t^3 + C2 t^2 + C1 t + C0, and its derivative
 // (3 C3 t + 2 C2) t + C1 = (C3 (1.5 t) + C2) (2 t) + C1, by Horner's rule.
 template <class T> __device__ __forceinline__ void power_eval(const V3<T>* C, T t, V3<T>& c, V3<T>& ax) {
@@ -181,19 +198,25 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
     out.ts = ts;
     // the end points first: the bounding-cylinder early-out needs only them
     V3<T> W[4];
-    V3<T> mid = bez_point(P, T(0.5));
-    const V3<T> cr = cross(mid - P[0], mid - P[3]), ch = P[3] - P[0];
-    T rmax = prhi_sqrt(prhi_div(dot(cr, cr), dot(ch, ch))) + gmax(r0, r1);
     if constexpr (std::is_same<T, float>::value) {
         // FP32: P0 - o' exactly, the other points through the control-point differences
         // (rounded once, an error of 2^-24 times a segment's extent rather than the camera
-        // distance): 3 exact relative coordinates instead of 12
+        // distance): 3 exact relative coordinates instead of 12. With D1 = P1 - P0 and
+        // D2 = P2 - P0, mid - P0 = (3 D1 + 3 D2 + ch) / 8, so the bounding radius's
+        // |(mid - P0) x (mid - P3)| = (3/8) |ch x (D1 + D2)|.
+        const V3<float> ch = P[3] - P[0], D1 = P[1] - P[0], D2 = P[2] - P[0];
+        const V3<float> cr = cross(ch, D1 + D2);
+        const float chch = dot(ch, ch);
+        const float rmax = 0.375f * prhi_sqrt(prhi_div(dot(cr, cr), chch)) + gmax(r0, r1);
         W[0] = mk(rel_coord(P[0].x, o.x, ts, d.x), rel_coord(P[0].y, o.y, ts, d.y), rel_coord(P[0].z, o.z, ts, d.z));
+        if (!ray_cylinder0(d, W[0], ch, chch, rmax)) return out;
+        W[1] = W[0] + D1;
+        W[2] = W[0] + D2;
         W[3] = W[0] + ch;
-        if (!ray_cylinder(mk(0.0f, 0.0f, 0.0f), d, W[0], W[3], rmax)) return out;
-        W[1] = W[0] + (P[1] - P[0]);
-        W[2] = W[0] + (P[2] - P[0]);
     } else {
+        V3<T> mid = bez_point(P, T(0.5));
+        const V3<T> cr = cross(mid - P[0], mid - P[3]), ch = P[3] - P[0];
+        T rmax = prhi_sqrt(prhi_div(dot(cr, cr), dot(ch, ch))) + gmax(r0, r1);
 #pragma unroll
         for (int k = 0; k < 4; k += 3)
             W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
