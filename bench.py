@@ -266,7 +266,7 @@ def run_reference_batched(args):
                 total_t += dt
                 total_rays += len(px) * spp + int((o["t"] >= 0).sum())
     value = total_rays / total_t / 1e6
-    sample = (f"{frac:g} of the pixels of each of the {len(models)} scenes (all their samples, + shadow rays) per "
+    sample = (f"{pixel_share(frac)} of each of the {len(models)} scenes (all their samples, + shadow rays) per "
               f"step: the workload's mix")
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_t / max(args.steps, 1), 3),
@@ -735,8 +735,13 @@ def batch_agreement_and_cpu(args, ctx, q, models):
                           "oracle": "FP64 CPU restatement on the same (dequantised) geometry, per scene"},
             "cpu_baseline": {"value": round(cpu_rays / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads,
                              "kind": "port",
-                             "sample": f"{cpu_frac:g} of the pixels of every scene ({cpu_px} pixels, all their "
+                             "sample": f"{pixel_share(cpu_frac)} of every scene ({cpu_px} pixels, all their "
                                        f"samples, {cpu_rays} rays), FP32 oracle, {cpu_s:.1f} s"}}
+
+
+def pixel_share(frac: float) -> str:
+    """'every pixel' or '<frac> of the pixels' for a CPU sample description."""
+    return "every pixel" if frac >= 1.0 else f"{frac:g} of the pixels"
 
 
 def main():

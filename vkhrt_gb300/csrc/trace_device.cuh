@@ -183,48 +183,16 @@ template <class T> __device__ __forceinline__ T rel_coord(T a, T b, T ts, T d) {
 
 // hair_intersection.rint:15-130 with the cone radius r0 + (r1 - r0) t (constant when equal).
 // The solve runs from o' = o + ts d, the ray point nearest the chord midpoint, on the vectors
-// P - o' (o' itself is never rounded: P0 - o' is exact, the others add the control-point
-// differences to it in FP32); ts is added back to the distance. The result is the same in exact arithmetic; in FP32 it removes the cancellation of
-// the world-space bounding-cylinder test from a distant origin (hair_intersection.rint:29).
-// The bounding radius is sqrt(|cross|^2 / |chord|^2) (one root instead of two), and the Newton
-// iteration evaluates the Bezier point and tangent from the power form of the control points
-// (Horner's rule, power_eval) instead of the Bernstein weights of curve.glsl: the same
-// polynomials, in fewer operations.
+// P - o' (o' itself is never rounded); ts is added back to the distance. The result is the
+// same in exact arithmetic; in FP32 it removes the cancellation of the world-space
+// bounding-cylinder test from a distant origin (hair_intersection.rint:29). The bounding radius
+// is sqrt(|cross|^2 / |chord|^2) (one root instead of two), and the Newton iteration evaluates
+// the Bezier point and tangent from the power form of the control points (Horner's rule,
+// power_eval) instead of the Bernstein weights of curve.glsl: the same polynomials, in fewer
+// operations. prhi_solve is the iteration on the control points relative to o' (W), with
+// out.ts holding the distance of o' along the ray.
 template <class T>
-__device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, const V3<T>* P, T r0, T r1) {
-    PrhiOut<T> out{T(0), T(0), T(0), T(0), kMiss};
-    V3<T> cm = T(0.5) * (P[0] + P[3]);
-    T ts = dot(cm - o, d) * F.inv_dd;
-    out.ts = ts;
-    // the end points first: the bounding-cylinder early-out needs only them
-    V3<T> W[4];
-    if constexpr (std::is_same<T, float>::value) {
-        // FP32: P0 - o' exactly, the other points through the control-point differences
-        // (rounded once, an error of 2^-24 times a segment's extent rather than the camera
-        // distance): 3 exact relative coordinates instead of 12. With D1 = P1 - P0 and
-        // D2 = P2 - P0, mid - P0 = (3 D1 + 3 D2 + ch) / 8, so the bounding radius's
-        // |(mid - P0) x (mid - P3)| = (3/8) |ch x (D1 + D2)|.
-        const V3<float> ch = P[3] - P[0], D1 = P[1] - P[0], D2 = P[2] - P[0];
-        const V3<float> cr = cross(ch, D1 + D2);
-        const float chch = dot(ch, ch);
-        const float rmax = 0.375f * prhi_sqrt(prhi_div(dot(cr, cr), chch)) + gmax(r0, r1);
-        W[0] = mk(rel_coord(P[0].x, o.x, ts, d.x), rel_coord(P[0].y, o.y, ts, d.y), rel_coord(P[0].z, o.z, ts, d.z));
-        if (!ray_cylinder0(d, W[0], ch, chch, rmax)) return out;
-        W[1] = W[0] + D1;
-        W[2] = W[0] + D2;
-        W[3] = W[0] + ch;
-    } else {
-        V3<T> mid = bez_point(P, T(0.5));
-        const V3<T> cr = cross(mid - P[0], mid - P[3]), ch = P[3] - P[0];
-        T rmax = prhi_sqrt(prhi_div(dot(cr, cr), dot(ch, ch))) + gmax(r0, r1);
-#pragma unroll
-        for (int k = 0; k < 4; k += 3)
-            W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
-        if (!ray_cylinder(mk(T(0), T(0), T(0)), d, W[0], W[3], rmax)) return out;
-#pragma unroll
-        for (int k = 1; k < 3; ++k)
-            W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
-    }
+__device__ __forceinline__ PrhiOut<T> prhi_solve(const Frame<T>& F, const V3<T>* W, T r0, T r1, PrhiOut<T> out) {
     V3<T> Q[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) Q[k] = mk(dot(F.e1, W[k]), dot(F.e2, W[k]), dot(F.e3, W[k]));
@@ -255,7 +223,7 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
             T dt = prhi_div(s * ax.z - cdd, ddd);
             if (isect && gabs(dt) < T(5e-5)) {
                 out.sl = s + c.z;
-                out.s = out.sl + ts;
+                out.s = out.sl + out.ts;
                 out.tc = t;
                 exhausted = false;
                 break;
@@ -280,6 +248,56 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
     }
     out.status = out.s > T(0) ? kHit : (unresolved ? kUnresolved : kMiss);
     return out;
+}
+
+// FP32 prhi from P0 and the control-point differences D1 = P1 - P0, D2 = P2 - P0, ch = P3 - P0:
+// P0 - o' exactly, the other points as (P0 - o') + D (rounded at the scale of a segment, not of
+// the camera distance: 3 exact relative coordinates instead of 12). With
+// mid - P0 = (3 D1 + 3 D2 + ch) / 8 the bounding radius's |(mid - P0) x (mid - P3)| is
+// (3/8) |ch x (D1 + D2)|.
+__device__ __forceinline__ PrhiOut<float> prhi_diff(const Frame<float>& F, V3<float> o, V3<float> d, V3<float> P0,
+                                                    V3<float> D1, V3<float> D2, V3<float> ch, float r0, float r1) {
+    PrhiOut<float> out{0.0f, 0.0f, 0.0f, 0.0f, kMiss};
+    const V3<float> cm = mk(fmaf(0.5f, ch.x, P0.x), fmaf(0.5f, ch.y, P0.y), fmaf(0.5f, ch.z, P0.z));
+    const float ts = dot(cm - o, d) * F.inv_dd;
+    out.ts = ts;
+    const V3<float> cr = cross(ch, D1 + D2);
+    const float chch = dot(ch, ch);
+    const float rmax = 0.375f * prhi_sqrt(prhi_div(dot(cr, cr), chch)) + gmax(r0, r1);
+    V3<float> W[4];
+    W[0] = mk(rel_coord(P0.x, o.x, ts, d.x), rel_coord(P0.y, o.y, ts, d.y), rel_coord(P0.z, o.z, ts, d.z));
+    if (!ray_cylinder0(d, W[0], ch, chch, rmax)) return out;
+    W[1] = W[0] + D1;
+    W[2] = W[0] + D2;
+    W[3] = W[0] + ch;
+    return prhi_solve(F, W, r0, r1, out);
+}
+
+// hair_intersection.rint:15-130 on the four control points (FP64: every relative coordinate
+// exact; FP32: prhi_diff)
+template <class T>
+__device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, const V3<T>* P, T r0, T r1) {
+    if constexpr (std::is_same<T, float>::value) {
+        return prhi_diff(F, o, d, P[0], P[1] - P[0], P[2] - P[0], P[3] - P[0], r0, r1);
+    } else {
+        PrhiOut<T> out{T(0), T(0), T(0), T(0), kMiss};
+        V3<T> cm = T(0.5) * (P[0] + P[3]);
+        T ts = dot(cm - o, d) * F.inv_dd;
+        out.ts = ts;
+        // the end points first: the bounding-cylinder early-out needs only them
+        V3<T> W[4];
+        V3<T> mid = bez_point(P, T(0.5));
+        const V3<T> cr = cross(mid - P[0], mid - P[3]), ch = P[3] - P[0];
+        T rmax = prhi_sqrt(prhi_div(dot(cr, cr), dot(ch, ch))) + gmax(r0, r1);
+#pragma unroll
+        for (int k = 0; k < 4; k += 3)
+            W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
+        if (!ray_cylinder(mk(T(0), T(0), T(0)), d, W[0], W[3], rmax)) return out;
+#pragma unroll
+        for (int k = 1; k < 3; ++k)
+            W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
+        return prhi_solve(F, W, r0, r1, out);
+    }
 }
 
 // FP64 re-solve of one candidate, kept out of line so the FP32 path keeps its registers.
