@@ -71,6 +71,7 @@ def load() -> ctypes.CDLL:
         "orc_quantise_phantom": (i64, [P, P, P, i64, u32, P, P, P, P]),
         "orc_f16_to_f32": (f32, [ctypes.c_uint16]),
         "orc_prim_boxes": (None, [i32, P, P, i64, P]),
+        "orc_ref_boxes": (i64, [i32, P, P, i64, P]),
         "orc_morton": (None, [P, i64, P]),
         "orc_lbvh": (None, [P, i64, P, P, P, P, P, P, P, P, P]),
         "orc_bvh8": (i64, [P, i64, i32, i64, P, P, P, P, P, P, P, P, P]),

@@ -456,6 +456,48 @@ static Box prim_box(int type, const float* data, const float* radius, int64_t i)
     return b;
 }
 
+// BVH references of a BLAS's primitives, the boxes its LBVH sorts: one per primitive, or for LSS
+// and DOTS two per segment, the boxes of its halves (reference 2 i + h), as the device build forms
+// them. LSS: the half u <= 1/2 of the round cone lies in the hull of the sphere at a and the
+// sphere at the midpoint m with radius (ra + rb) / 2. DOTS: each quad is a trapezoid, s0 +- va
+// at the start (vertices 0 and 4 of its six) and e0 +- vb at the end (vertices 2 and 1), so its
+// first half is the hull of the start edge and the edge midpoints, its second half the hull of
+// the midpoints and the end edge.
+static int ref_shift_of(int type) { return (type == kLss || type == kDots) ? 1 : 0; }
+static void ref_boxes(int type, const float* data, const float* radius, int64_t i, Box* out) {
+    if (type == kLss) {
+        const float* p = data + 6 * i;
+        const float ra = radius[2 * i], rb = radius[2 * i + 1], rm = 0.5f * (ra + rb);
+        for (int k = 0; k < 3; ++k) {
+            const float m = 0.5f * (p[k] + p[3 + k]);
+            out[0].lo[k] = fmin_t(p[k] - ra, m - rm);
+            out[0].hi[k] = fmax_t(p[k] + ra, m + rm);
+            out[1].lo[k] = fmin_t(m - rm, p[3 + k] - rb);
+            out[1].hi[k] = fmax_t(m + rm, p[3 + k] + rb);
+        }
+    } else if (type == kDots) {
+        const float* v = data + 36 * i;
+        for (int k = 0; k < 3; ++k) {
+            float lo0 = INFINITY, hi0 = -INFINITY, lo1 = INFINITY, hi1 = -INFINITY;
+            for (int face = 0; face < 2; ++face) {
+                const float* f = v + 18 * face;
+                const float a = f[k], b = f[12 + k], c = f[6 + k], d = f[3 + k];
+                const float mp = 0.5f * (a + c), mm = 0.5f * (b + d);
+                lo0 = fmin_t(lo0, fmin_t(fmin_t(a, b), fmin_t(mp, mm)));
+                hi0 = fmax_t(hi0, fmax_t(fmax_t(a, b), fmax_t(mp, mm)));
+                lo1 = fmin_t(lo1, fmin_t(fmin_t(mp, mm), fmin_t(c, d)));
+                hi1 = fmax_t(hi1, fmax_t(fmax_t(mp, mm), fmax_t(c, d)));
+            }
+            out[0].lo[k] = lo0;
+            out[0].hi[k] = hi0;
+            out[1].lo[k] = lo1;
+            out[1].hi[k] = hi1;
+        }
+    } else {
+        out[0] = prim_box(type, data, radius, i);
+    }
+}
+
 // ---- LBVH: Morton codes, stable sort, Karras hierarchy, refit ----------------------------
 // Centroid c = (lo + hi) * 0.5; per axis q = (c - cmin) * (2^21 / (cmax - cmin)) truncated
 // to [0, 2^21 - 1] (0 when the extent is 0). Code = interleave with x in bit 3i+2, y in
@@ -1327,6 +1369,16 @@ void orc_prim_boxes(int type, const float* data, const float* radius, int64_t n,
         Box b = prim_box(type, data, radius, i);
         std::memcpy(boxes_out + 6 * i, &b, sizeof(Box));
     }
+}
+// The BVH references' boxes (n << ref_shift_of(type) of them, see ref_boxes); returns their count.
+int64_t orc_ref_boxes(int type, const float* data, const float* radius, int64_t n, float* boxes_out) {
+    const int sh = ref_shift_of(type);
+    for (int64_t i = 0; i < n; ++i) {
+        Box b[2];
+        ref_boxes(type, data, radius, i, b);
+        std::memcpy(boxes_out + (6 << sh) * i, b, sizeof(Box) << sh);
+    }
+    return n << sh;
 }
 void orc_morton(const float* boxes, int64_t n, uint64_t* codes) {
     morton_codes(reinterpret_cast<const Box*>(boxes), n, codes);

@@ -190,6 +190,15 @@ def mesh_oracle_data(v, tri, nrm=None):
 VOXELS = 4
 
 
+def ref_boxes(orc, gtype: int, data: np.ndarray, rad: np.ndarray, n: int) -> np.ndarray:
+    """The BVH reference boxes of a hair BLAS as the oracle forms them: one per segment, two (the
+    segment's halves, reference 2 i + h) for LSS and DOTS."""
+    out = np.zeros((n << (1 if gtype in (LSS, DOTS) else 0), 6), np.float32)
+    m = orc.orc_ref_boxes(gtype, P(np.ascontiguousarray(data)), P(np.ascontiguousarray(rad)), n, P(out))
+    assert m == len(out)
+    return out
+
+
 def oracle_voxels(orc, lines: np.ndarray, r: float, size: float, max_out: int = 1 << 21):
     """The oracle's capsule voxelisation: (count, grid [origin xyz, size, res xyz], voxels (m, 7))."""
     lines = np.ascontiguousarray(lines, np.float32).reshape(-1, 6)

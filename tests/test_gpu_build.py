@@ -9,7 +9,7 @@ import pytest
 
 import vkhrt_gb300 as H
 from hairscene import (DOTS, LSS, MESH, PHANTOM, P, lines_from_strands, mesh_oracle_data, oracle_geometry, oracle_voxels,
-                       sphere_mesh)
+                       ref_boxes, sphere_mesh)
 
 pytestmark = pytest.mark.gpu
 
@@ -70,9 +70,7 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
         assert np.ascontiguousarray(g[:, 6:]).tobytes() == rad.tobytes()
     else:
         assert blas.get(H.Part.DOTS_VERTICES, np.float32, (n, 36)).tobytes() == data.tobytes()
-    ref_boxes = np.zeros((n, 6), np.float32)
-    orc.orc_prim_boxes(gtype, P(np.ascontiguousarray(data)), P(np.ascontiguousarray(rad)), n, P(ref_boxes))
-    o = check_tree(blas, orc, ref_boxes, max_leaf, precision)
+    o = check_tree(blas, orc, ref_boxes(orc, gtype, data, rad, n), max_leaf, precision)
     if quant_prims:
         recs = blas.get(H.Part.PRIMS, np.uint8, n * 32).view(PRIMH)
         halves = recs["h"].view(np.float16).astype(np.float32)
@@ -306,12 +304,11 @@ def test_refit_boxes_exact(ctx, orc, gtype):
     n = blas.info["nprims"]
     lines, lrad = lines_from_strands(v2, r, off)
     data, rad = oracle_geometry(orc, gtype, lines, lrad)
-    ref_boxes = np.zeros((n, 6), np.float32)
-    orc.orc_prim_boxes(gtype, P(np.ascontiguousarray(data)), P(np.ascontiguousarray(rad)), n, P(ref_boxes))
-    assert blas.get(H.Part.PRIM_BOXES, np.float32, (n, 6)).tobytes() == ref_boxes.tobytes()
+    rb = ref_boxes(orc, gtype, data, rad, n)
+    assert blas.get(H.Part.PRIM_BOXES, np.float32, rb.shape).tobytes() == rb.tobytes()
     nn = blas.info["nnodes"]
     fn = blas.get(H.Part.NODES, np.uint8, nn * 224).view(NODEF)
-    lo, hi, nb = _numpy_refit(fn, blas.get(H.Part.PRIM_ORDER, np.uint32, n), ref_boxes)
+    lo, hi, nb = _numpy_refit(fn, blas.get(H.Part.PRIM_ORDER, np.uint32, len(rb)), rb)
     for k, ax in enumerate("xyz"):
         assert fn["lo_" + ax].tobytes() == np.ascontiguousarray(lo[:, :, k]).tobytes()
         assert fn["hi_" + ax].tobytes() == np.ascontiguousarray(hi[:, :, k]).tobytes()

@@ -627,8 +627,9 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
                     return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: line index %llu out of range",
                                 (unsigned long long)i);
     }
-    if (nlines >= (1ull << 29))
-        return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_build: %llu segments; the limit is 2^29", (unsigned long long)nlines);
+    if ((nlines << ref_shift(in->type)) >= (1ull << 29))
+        return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_build: %llu segments; the limit is 2^29 BVH references",
+                    (unsigned long long)nlines);
 
     hrt_blas* b = new (std::nothrow) hrt_blas();
     if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_blas_build: host allocation");
@@ -857,7 +858,9 @@ hrt_status hrt_blas_transform(const hrt_blas* b, float out[16]) {
 // ---- serialisation --------------------------------------------------------------------------
 // Layout (little-endian): the header below, then level starts (u32), the refit topology
 // (line offsets, vertex offsets, line indices, triangle indices: u32 each, lengths in the
-// header), then the device arrays: nodes, records, roots (float4), slot map (u32).
+// header), then the device arrays: nodes, records, roots (float4), slot map (u32). Records and
+// the slot map have one entry per BVH reference (two per LSS or DOTS segment); the partner map
+// of those two-reference types is rebuilt from the slot map when an image is read.
 namespace {
 struct SerialHeader {
     char magic[4];  // "HRTB"
@@ -872,13 +875,13 @@ struct SerialHeader {
     uint32_t has_radius, has_normals;
     uint64_t nlevels, n_line_off, n_vert_off, n_line_idx, n_tri_idx;
 };
-constexpr uint32_t kSerialVersion = 1;
+constexpr uint32_t kSerialVersion = 2;
 
 uint64_t serial_size(const hrt_blas* b) {
     const BuildOutput& o = b->out;
     return sizeof(SerialHeader) +
            4 * (o.level_start.size() + b->line_off.size() + b->vert_off.size() + b->line_idx.size() + b->tri_idx.size()) +
-           o.nnodes * o.node_bytes + b->nprims * o.prim_bytes + o.nroots * 16 + b->nprims * 4;
+           o.nnodes * o.node_bytes + o.nslots * o.prim_bytes + o.nroots * 16 + o.nslots * 4;
 }
 
 // Reads a u32 array of n entries at *p, advancing it; false past the end.
@@ -975,9 +978,9 @@ hrt_status hrt_blas_serialize(const hrt_blas* b, void* dst, uint64_t bytes) {
         p += v->size() * 4;
     }
     struct { const void* src; uint64_t n; } parts[] = {{o.nodes, o.nnodes * o.node_bytes},
-                                                      {o.prims, b->nprims * o.prim_bytes},
+                                                      {o.prims, o.nslots * o.prim_bytes},
                                                       {o.roots, o.nroots * 16},
-                                                      {o.prim_ids, b->nprims * 4}};
+                                                      {o.prim_ids, o.nslots * 4}};
     for (auto& q : parts) {
         if (q.n) CK(ctx, cudaMemcpy(p, q.src, q.n, cudaMemcpyDeviceToHost), "hrt_blas_serialize");
         p += q.n;
@@ -1002,7 +1005,8 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
     const uint64_t want_prim = h.type == HRT_BLAS_PHANTOM ? (quant ? 32 : 64)
                                : ((h.type == HRT_BLAS_LSS || h.type == HRT_BLAS_VOXELS) ? 32 : 80);
     if (h.type < HRT_BLAS_PHANTOM || h.type > HRT_BLAS_VOXELS || (h.precision != HRT_PRECISION_FP32 && !quant) ||
-        h.node_bytes != want_node || h.prim_bytes != want_prim || h.nprims >= (1ull << 29) || h.nnodes > h.nprims + 1 ||
+        h.node_bytes != want_node || h.prim_bytes != want_prim || h.nprims >= (1ull << 29) || (h.nprims << ref_shift(h.type)) >= (1ull << 29) ||
+        h.nnodes > (h.nprims << ref_shift(h.type)) + 1 ||
         h.nroots > h.nprims || (h.nprims && !h.nnodes) || h.max_leaf < 1 || h.max_leaf > 3)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: inconsistent header");
     hrt_blas* b = new (std::nothrow) hrt_blas();
@@ -1029,12 +1033,27 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
         !take_u32(p, end, h.n_vert_off, b->vert_off) || !take_u32(p, end, h.n_line_idx, b->line_idx) ||
         !take_u32(p, end, h.n_tri_idx, b->tri_idx))
         return reject("truncated tables");
-    const uint64_t nb = h.nnodes * h.node_bytes, pbytes = h.nprims * h.prim_bytes, rb = h.nroots * 16, ib = h.nprims * 4;
+    const uint32_t shift = ref_shift(h.type);
+    const uint64_t nslots = h.nprims << shift;
+    const uint64_t nb = h.nnodes * h.node_bytes, pbytes = nslots * h.prim_bytes, rb = h.nroots * 16, ib = nslots * 4;
     if (nb + pbytes + rb + ib > uint64_t(end - p)) return reject("truncated arrays");
     const uint8_t* nodes = p;
     const uint8_t* prims = p + nb;
-    if (const char* why = check_tree(h.type, h.precision, h.nprims, h.nnodes, h.nroots, nodes, prims, o.level_start))
+    if (const char* why = check_tree(h.type, h.precision, nslots, h.nnodes, h.nroots, nodes, prims, o.level_start))
         return reject(why);
+    // two references per segment: the slot map must be a permutation of the reference ids, and
+    // the partner map follows from it
+    std::vector<uint32_t> partner;
+    if (shift) {
+        std::vector<uint32_t> ids(nslots), slot_of(nslots, 0xffffffffu);
+        if (nslots) memcpy(ids.data(), prims + pbytes + rb, ib);
+        for (uint64_t i = 0; i < nslots; ++i) {
+            if (ids[i] >= nslots || slot_of[ids[i]] != 0xffffffffu) return reject("slot map is not a permutation");
+            slot_of[ids[i]] = uint32_t(i);
+        }
+        partner.resize(nslots);
+        for (uint64_t i = 0; i < nslots; ++i) partner[i] = slot_of[ids[i] ^ 1u];
+    }
     o.nnodes = h.nnodes;
     o.nroots = h.nroots;
     o.node_bytes = h.node_bytes;
@@ -1046,7 +1065,10 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
     struct { void** dst; const uint8_t* src; uint64_t n; } parts[] = {{&o.nodes, nodes, nb},
                                                                      {&o.prims, prims, pbytes},
                                                                      {reinterpret_cast<void**>(&o.roots), prims + pbytes, rb},
-                                                                     {reinterpret_cast<void**>(&o.prim_ids), prims + pbytes + rb, ib}};
+                                                                     {reinterpret_cast<void**>(&o.prim_ids), prims + pbytes + rb, ib},
+                                                                     {reinterpret_cast<void**>(&o.partner),
+                                                                      reinterpret_cast<const uint8_t*>(partner.data()),
+                                                                      partner.size() * 4}};
     for (auto& q : parts) {
         if (!q.n || e != cudaSuccess) continue;
         e = cudaMalloc(q.dst, q.n);
@@ -1058,7 +1080,8 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
         delete b;
         return cuda_fail(ctx, e, "hrt_blas_deserialize");
     }
-    o.device_bytes = nb + pbytes + rb + ib;
+    o.nslots = nslots;
+    o.device_bytes = nb + pbytes + rb + ib + partner.size() * 4;
     *out = b;
     return HRT_OK;
 }
@@ -1079,24 +1102,25 @@ hrt_status hrt_blas_get(const hrt_blas* b, int32_t part, void* dst, uint64_t byt
     if (!b || !dst) return HRT_ERR_INVALID_ARG;
     hrt_context* ctx = b->ctx;
     DeviceSet ds(ctx->device);
-    const uint64_t n = b->nprims;
+    const uint64_t n = b->nprims;  // segments (triangles, voxels)
+    const BuildOutput& o = b->out;
+    const uint64_t ns = o.nslots;   // BVH references: the parts of the tree and its leaves
     const void* src = nullptr;
     uint64_t need = 0;
-    const BuildOutput& o = b->out;
     switch (part) {
-        case HRT_PART_PRIM_BOXES: src = o.prim_boxes; need = n * 24; break;
-        case HRT_PART_MORTON_SORTED: src = o.morton_sorted; need = n * 8; break;
-        case HRT_PART_SORTED_INDEX: src = o.sorted_index; need = n * 4; break;
-        case HRT_PART_BIN_LEFT: src = o.bin_left; need = n ? (n - 1) * 4 : 0; break;
-        case HRT_PART_BIN_RIGHT: src = o.bin_right; need = n ? (n - 1) * 4 : 0; break;
-        case HRT_PART_BIN_BOXES: src = o.bin_boxes; need = n ? (n - 1) * 24 : 0; break;
+        case HRT_PART_PRIM_BOXES: src = o.prim_boxes; need = ns * 24; break;
+        case HRT_PART_MORTON_SORTED: src = o.morton_sorted; need = ns * 8; break;
+        case HRT_PART_SORTED_INDEX: src = o.sorted_index; need = ns * 4; break;
+        case HRT_PART_BIN_LEFT: src = o.bin_left; need = ns ? (ns - 1) * 4 : 0; break;
+        case HRT_PART_BIN_RIGHT: src = o.bin_right; need = ns ? (ns - 1) * 4 : 0; break;
+        case HRT_PART_BIN_BOXES: src = o.bin_boxes; need = ns ? (ns - 1) * 24 : 0; break;
         case HRT_PART_NODES: src = o.nodes; need = o.nnodes * o.node_bytes; break;
         case HRT_PART_QNODES:
             src = b->precision == HRT_PRECISION_QUANTISED ? o.nodes : o.qnodes_aux;
             need = o.nnodes * sizeof(NodeQ);
             break;
-        case HRT_PART_PRIM_ORDER: src = o.prim_ids; need = n * 4; break;
-        case HRT_PART_PRIMS: src = o.prims; need = n * o.prim_bytes; break;
+        case HRT_PART_PRIM_ORDER: src = o.prim_ids; need = ns * 4; break;
+        case HRT_PART_PRIMS: src = o.prims; need = ns * o.prim_bytes; break;
         case HRT_PART_CURVES: src = o.curves; need = n * 48; break;
         case HRT_PART_LSS: src = b->type == HRT_BLAS_LSS ? o.geom : nullptr; need = n * 32; break;
         case HRT_PART_ROOTS: src = o.roots; need = o.nroots * 16; break;
@@ -1147,6 +1171,8 @@ hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint3
         d.b.prims = b->out.prims;
         d.b.roots = b->out.roots;
         d.b.prim_ids = b->out.prim_ids;
+        d.b.partner = b->out.partner;
+        d.b.ref_shift = ref_shift(b->type);
         d.b.type = uint32_t(b->type);
         d.b.precision = uint32_t(b->precision);
         d.b.nprims = uint32_t(b->nprims);

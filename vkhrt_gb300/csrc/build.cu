@@ -287,14 +287,21 @@ __global__ void boxes_phantom_kernel(const float* curves, const float* rad, uint
         boxes[6 * i + 3 + k] = fmax_t(fmax_t(c[k], c[9 + k]), fmax_t(c[3 + k], c[6 + k])) + r;
     }
 }
+// LSS: two references per segment (see ref_shift). The round cone is the union of the spheres
+// a + u (b - a) with radius ra + u (rb - ra), so its half u <= 1/2 lies in the hull of the end
+// sphere at a and the sphere at the midpoint m, radius rm = (ra + rb) / 2; m and rm are computed
+// once and bound both halves, so the two boxes meet without a gap.
 __global__ void boxes_lss_kernel(const float* geom, uint64_t n, float* boxes) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* g = geom + 8 * i;
-    float ra = g[6], rb = g[7];
+    const float ra = g[6], rb = g[7], rm = 0.5f * (ra + rb);
     for (int k = 0; k < 3; ++k) {
-        boxes[6 * i + k] = fmin_t(g[k] - ra, g[3 + k] - rb);
-        boxes[6 * i + 3 + k] = fmax_t(g[k] + ra, g[3 + k] + rb);
+        const float m = 0.5f * (g[k] + g[3 + k]);
+        boxes[12 * i + k] = fmin_t(g[k] - ra, m - rm);
+        boxes[12 * i + 3 + k] = fmax_t(g[k] + ra, m + rm);
+        boxes[12 * i + 6 + k] = fmin_t(m - rm, g[3 + k] - rb);
+        boxes[12 * i + 9 + k] = fmax_t(m + rm, g[3 + k] + rb);
     }
 }
 __device__ void dots_vertices(const float* g, float* v36) {
@@ -310,16 +317,31 @@ __device__ void dots_vertices(const float* g, float* v36) {
         st3(o + 15, e0 - vb);
     }
 }
+// DOTS: two references per segment (see ref_shift). Each quad is a trapezoid, s0 +- va at the
+// start and e0 +- vb at the end (vertices 0, 4 and 2, 1 of its six), whose width is linear
+// along the segment, so its first half is the hull of the start edge and the edge midpoints
+// (v0 + v2) / 2, (v4 + v1) / 2, and its second half the hull of those midpoints and the end
+// edge; the midpoints are shared by both halves.
 __global__ void boxes_dots_kernel(const float* geom, uint64_t n, float* boxes) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float v[36];
     dots_vertices(geom + 18 * i, v);
     for (int k = 0; k < 3; ++k) {
-        float lo = v[k], hi = v[k];
-        for (int j = 1; j < 12; ++j) { lo = fmin_t(lo, v[3 * j + k]); hi = fmax_t(hi, v[3 * j + k]); }
-        boxes[6 * i + k] = lo;
-        boxes[6 * i + 3 + k] = hi;
+        float lo0 = __int_as_float(0x7f800000), hi0 = -lo0, lo1 = lo0, hi1 = hi0;
+        for (int face = 0; face < 2; ++face) {
+            const float* f = v + 18 * face;
+            const float a = f[k], b = f[12 + k], c = f[6 + k], d = f[3 + k];  // v0, v4, v2, v1
+            const float mp = 0.5f * (a + c), mm = 0.5f * (b + d);
+            lo0 = fmin_t(lo0, fmin_t(fmin_t(a, b), fmin_t(mp, mm)));
+            hi0 = fmax_t(hi0, fmax_t(fmax_t(a, b), fmax_t(mp, mm)));
+            lo1 = fmin_t(lo1, fmin_t(fmin_t(mp, mm), fmin_t(c, d)));
+            hi1 = fmax_t(hi1, fmax_t(fmax_t(mp, mm), fmax_t(c, d)));
+        }
+        boxes[12 * i + k] = lo0;
+        boxes[12 * i + 3 + k] = hi0;
+        boxes[12 * i + 6 + k] = lo1;
+        boxes[12 * i + 9 + k] = hi1;
     }
 }
 // Mesh triangle box: min/max of the three vertices, in vertex order.
@@ -799,6 +821,16 @@ __global__ void quantise_kernel(const NodeF* in, uint64_t nn, NodeQ* out) {
     out[i] = q;
 }
 
+// Two references per segment: slot_of[reference] = slot, then partner[slot] = the slot of the
+// same segment's other reference (reference id ^ 1).
+__global__ void slot_of_kernel(const uint32_t* ids, uint64_t n, uint32_t* slot_of) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) slot_of[ids[i]] = uint32_t(i);
+}
+__global__ void partner_kernel(const uint32_t* ids, const uint32_t* slot_of, uint64_t n, uint32_t* partner) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) partner[i] = slot_of[ids[i] ^ 1u];
+}
 __global__ void map_order_kernel(const uint32_t* sorted_pos, const uint32_t* sorted_index, uint64_t n, uint32_t* out) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -806,12 +838,12 @@ __global__ void map_order_kernel(const uint32_t* sorted_pos, const uint32_t* sor
 }
 
 // Primitive records in slot order.
-__global__ void records_kernel(int type, int precision, const uint32_t* ids, uint64_t n, const float* curves,
+__global__ void records_kernel(int type, int precision, uint32_t shift, const uint32_t* ids, uint64_t n, const float* curves,
                                const float* lrad, const float* geom, const uint32_t* chunk_incl, const float4* roots,
                                const float* tri_nrm, void* prims) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t s = ids[i];
+    uint32_t s = ids[i] >> shift;  // the slot's segment
     if (type == HRT_BLAS_PHANTOM && precision == HRT_PRECISION_FP32) {
         const float* c = curves + 12 * uint64_t(s);
         PrimPhantomF r;
@@ -1012,7 +1044,7 @@ cudaError_t make_lines(const float* verts, const float* vrad, float const_radius
 }
 
 void free_build_output(BuildOutput& o) {
-    void* ptrs[] = {o.nodes, o.qnodes_aux, o.prims, o.roots, o.prim_ids, o.prim_boxes, o.curves, o.geom,
+    void* ptrs[] = {o.nodes, o.qnodes_aux, o.prims, o.roots, o.prim_ids, o.partner, o.prim_boxes, o.curves, o.geom,
                     o.morton_sorted, o.sorted_index, o.bin_left, o.bin_right, o.bin_boxes, o.prim_order};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -1192,7 +1224,10 @@ cudaError_t geometry_stage(const BuildInput& in, BuildOutput& out, float* boxes,
 }
 
 cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream_t s, char* msg, size_t msglen) {
-    const uint64_t n = in.n;
+    // n: BVH references (leaf slots, records); the geometry stage works on the in.n segments
+    const uint32_t shift = ref_shift(in.type);
+    const uint64_t n = in.n << shift;
+    out.nslots = n;
     const unsigned T = 256;
     out.node_bytes = in.precision == HRT_PRECISION_QUANTISED ? sizeof(NodeQ) : sizeof(NodeF);
     if (in.type == HRT_BLAS_PHANTOM) out.prim_bytes = in.precision == HRT_PRECISION_QUANTISED ? 32 : 64;
@@ -1315,8 +1350,18 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     else { out.nodes = fnodes; out.qnodes_aux = qn; }
     HRT_CK(cudaMalloc(&out.prim_ids, n * 4));
     map_order_kernel<<<grid_for(n, T), T, 0, s>>>(porder, order, n, out.prim_ids);
+    if (shift) {
+        // the slot of each slot's partner reference: slot_of[reference] first, then a gather
+        uint32_t* slot_of;
+        HRT_CK(dalloc(&slot_of, n, s));
+        HRT_CK(cudaMalloc(&out.partner, n * 4));
+        slot_of_kernel<<<grid_for(n, T), T, 0, s>>>(out.prim_ids, n, slot_of);
+        partner_kernel<<<grid_for(n, T), T, 0, s>>>(out.prim_ids, slot_of, n, out.partner);
+        HRT_CK(cudaGetLastError());
+        cudaFreeAsync(slot_of, s);
+    }
     HRT_CK(cudaMalloc(&out.prims, n * out.prim_bytes));
-    records_kernel<<<grid_for(n, T), T, 0, s>>>(in.type, in.precision, out.prim_ids, n, out.curves, in.lrad,
+    records_kernel<<<grid_for(n, T), T, 0, s>>>(in.type, in.precision, shift, out.prim_ids, n, out.curves, in.lrad,
                                                 in.type == HRT_BLAS_MESH ? in.tris : (in.type == HRT_BLAS_VOXELS ? in.voxels : out.geom), chunk_incl, out.roots,
                                                 in.tri_normals, out.prims);
     HRT_CK(cudaGetLastError());
@@ -1331,7 +1376,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     if (h_err) { snprintf(msg, msglen, "refit exceeded its depth bound"); return cudaErrorUnknown; }
 
     if (!in.keep_intermediate) {
-        // tracing reads nodes, records, roots and the slot -> segment map; the rest of the
+        // tracing reads nodes, records, roots and the slot maps; the rest of the
         // build's outputs (the other node encoding, primitive boxes, FP32 curves, LSS/DOTS
         // geometry) are kept only for inspection
         void* extra[] = {out.qnodes_aux, out.prim_boxes, out.curves, out.geom};
@@ -1361,9 +1406,11 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     for (void* p : tmps)
         if (p) cudaFreeAsync(p, s);
     HRT_CK(cudaStreamSynchronize(s));
-    out.device_bytes = out.nnodes * out.node_bytes + n * out.prim_bytes + out.nroots * 16 + n * 4;
+    // n references: records, slot map, partner map; in.n segments: curves and LSS/DOTS geometry
+    out.device_bytes = out.nnodes * out.node_bytes + n * out.prim_bytes + out.nroots * 16 + n * 4 + (shift ? n * 4 : 0);
     if (in.keep_intermediate)
-        out.device_bytes += n * 24 + (out.curves ? n * 48 : 0) + (out.geom ? n * (in.type == HRT_BLAS_LSS ? 32 : 72) : 0) +
+        out.device_bytes += n * 24 + (out.curves ? in.n * 48 : 0) +
+                            (out.geom ? in.n * (in.type == HRT_BLAS_LSS ? 32 : 72) : 0) +
                             out.nnodes * (in.precision == HRT_PRECISION_QUANTISED ? sizeof(NodeF) : sizeof(NodeQ)) +
                             n * 8 + n * 4 + (n ? (n - 1) * 32 : 0);
     return cudaSuccess;
@@ -1427,11 +1474,13 @@ cudaError_t refit_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     const uint64_t n = in.n;
     const unsigned T = 256;
     if (n == 0) return cudaSuccess;
+    const uint32_t shift = ref_shift(in.type);
+    const uint64_t nslots = n << shift;  // BVH references (two per LSS or DOTS segment)
     const bool quant = in.precision == HRT_PRECISION_QUANTISED;
     float* boxes = out.prim_boxes;  // kept for inspection, else a temporary
     bool own_boxes = false, own_curves = !out.curves, own_geom = !out.geom;
     if (!boxes) {
-        HRT_CK(dalloc(&boxes, n * 6, s));
+        HRT_CK(dalloc(&boxes, nslots * 6, s));
         own_boxes = true;
     }
     GeomTmp gt;
@@ -1457,7 +1506,7 @@ cudaError_t refit_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
         quantise_kernel<<<grid_for(out.nnodes, T), T, 0, s>>>(fn, out.nnodes, static_cast<NodeQ*>(out.qnodes_aux));
     }
     if (e == cudaSuccess) {
-        records_kernel<<<grid_for(n, T), T, 0, s>>>(in.type, in.precision, out.prim_ids, n, out.curves, in.lrad,
+        records_kernel<<<grid_for(nslots, T), T, 0, s>>>(in.type, in.precision, shift, out.prim_ids, nslots, out.curves, in.lrad,
                                                     in.type == HRT_BLAS_MESH ? in.tris : out.geom, gt.chunk_incl,
                                                     out.roots, in.tri_normals, out.prims);
         e = cudaGetLastError();

@@ -61,12 +61,20 @@ struct alignas(16) PrimDots { float4 a, b, c, d, e; };
 // Mesh triangle (80 B): {v0, id} {v1, n0.x} {v2, n0.y} {n0.z, n1} {n2, has normals (0/1 bits)}
 struct alignas(16) PrimTri { float4 a, b, c, d, e; };
 
+// LSS and DOTS segments enter the BVH as two references, the boxes of the segment's halves (a
+// long, thin segment's box holds far more empty space than its two halves' boxes); each
+// reference's leaf slot holds a copy of the segment's record, and the slot map gives reference
+// ids 2 s + h. Phantom segments stay single: their leaf test is long however tight the box,
+// so halving buys fewer tests only of the kind that ends early.
+inline constexpr uint32_t ref_shift(int type) { return (type == HRT_BLAS_LSS || type == HRT_BLAS_DOTS) ? 1u : 0u; }
+
 struct DevBlas {
     const void* nodes;        // NodeF or NodeQ
     const void* prims;        // records in slot order
     const float4* roots;      // quantised Phantom chunk roots
-    const uint32_t* prim_ids; // slot -> segment index
-    uint32_t type, precision, nprims, nnodes;
+    const uint32_t* prim_ids; // slot -> reference id (segment index << ref_shift | half)
+    const uint32_t* partner;  // slot -> the slot of the same segment's other reference (LSS, DOTS)
+    uint32_t type, precision, nprims, nnodes, ref_shift;
     float lo[3], hi[3];
 };
 
@@ -168,8 +176,9 @@ struct BuildOutput {
     void* qnodes_aux = nullptr;   // NodeQ copy when nodes are NodeF (inspection) or vice versa
     void* prims = nullptr;
     float4* roots = nullptr;
-    uint32_t* prim_ids = nullptr;
-    float* prim_boxes = nullptr;  // n x 6, segment order
+    uint32_t* prim_ids = nullptr;  // slot -> reference id
+    uint32_t* partner = nullptr;   // slot -> partner slot (two references per segment only)
+    float* prim_boxes = nullptr;  // nslots x 6, reference order
     float* curves = nullptr;      // Phantom n x 12 (FP32, segment order)
     float* geom = nullptr;        // DOTS n x 18 / LSS n x 8 (segment order)
     uint64_t* morton_sorted = nullptr;
@@ -179,6 +188,7 @@ struct BuildOutput {
     float* bin_boxes = nullptr;
     uint32_t* prim_order = nullptr;
     uint64_t nnodes = 0, nroots = 0, node_bytes = 0, prim_bytes = 0, device_bytes = 0;
+    uint64_t nslots = 0;  // BVH references = leaf slots = records
     float bounds[6] = {0, 0, 0, 0, 0, 0};
     std::vector<uint32_t> level_start;  // first node of each breadth-first level, then nnodes
 };

@@ -567,7 +567,7 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         float u, tl, ts;
         float t = lss_hit(R.o, R.d, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, R.tmin, &u, &tl, &ts);
         if (t >= 0.0f && t <= h.t) {
-            uint32_t id = __ldg(&B.prim_ids[slot]);
+            uint32_t id = __ldg(&B.prim_ids[slot]) >> B.ref_shift;
             if (beats(t, inst, id, h)) { h = Hit{t, id, inst, slot, u, ts, tl, 0u}; return true; }
         }
         return false;
@@ -1105,7 +1105,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     float cur_tmin = 0.0f;
     RayState R;
     Hit h{0.0f, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
-    uint32_t inst_cur = 0, skip_inst = 0xffffffffu, skip_slot = 0xffffffffu;
+    uint32_t inst_cur = 0, skip_inst = 0xffffffffu, skip_slot = 0xffffffffu, skip_slot2 = 0xffffffffu;
     int sp = 0;
     uint32_t steps = 0;
     const void* nodes = nullptr;                 // node array of the current instance's BLAS
@@ -1231,7 +1231,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             ndl = fabsf(n.y);  // shading.glsl: |dot(n, (0,-1,0))|
             if (L.shading == HRT_SHADE_LAMBERT_SHADOW) {
                 skip_inst = h.inst;
+                // the hit segment's slots: its own and, for two-reference BLASes, its partner's
                 skip_slot = h.slot;
+                skip_slot2 = S.inst[h.inst].b.partner ? __ldg(&S.inst[h.inst].b.partner[h.slot]) : h.slot;
                 shadow_hit = false;
                 shadow = true;
                 ++shadow_rays;
@@ -1401,7 +1403,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             const uint32_t first = hd.y + (m & 31u), cnt = m >> 5;
             for (uint32_t j = 0; j < cnt; ++j) {
                 uint32_t slot = first + j;
-                if (shadow && inst_cur == skip_inst && slot == skip_slot) continue;
+                if (shadow && inst_cur == skip_inst && (slot == skip_slot || slot == skip_slot2)) continue;
                 ++st.prims;
                 if (leaf_test<kType, kPass == 1>(B, slot, inst_cur, R, h, L.fp64_resolve != 0, st) && shadow) {
                     shadow_hit = true;
