@@ -110,7 +110,7 @@ typedef struct hrt_blas_input {
 #define HRT_BUILD_KEEP_INTERMEDIATE 1u /* keep Morton codes, binary tree, boxes (hrt_blas_get) */
 
 typedef struct hrt_blas_info {
-    uint64_t nprims;        /* BVH primitives = line segments */
+    uint64_t nprims;        /* primitives: line segments (LSS, DOTS: two BVH references each), triangles, voxels */
     uint64_t nnodes;        /* BVH8 nodes */
     uint64_t node_bytes;    /* bytes per node (224 FP32, 80 quantised) */
     uint64_t prim_bytes;    /* bytes per primitive record */
@@ -217,10 +217,12 @@ hrt_status hrt_blas_destroy(hrt_blas* blas);
  * motions (build anew then). TLASes that hold the BLAS must be built again afterwards (they
  * copy its bounds). No counterpart in the reference (it builds once). */
 hrt_status hrt_blas_refit(hrt_blas* blas, const float* vertices, const float* per_vertex, int32_t memory, void* stream);
-/* A built BLAS as bytes (host memory): tree, records, roots, slot map and the refit topology.
- * hrt_blas_deserialize checks the image (header, sizes, every node's child and leaf ranges,
- * record roots) before anything reaches the device and rejects a corrupt one with
- * HRT_ERR_INVALID_ARG. No counterpart in the reference (it rebuilds at every start). */
+/* A built BLAS as bytes (host memory): tree, records, roots, slot map and the refit topology
+ * (image version 2: LSS and DOTS records and slot-map entries are per BVH reference, two per
+ * segment). hrt_blas_deserialize checks the image (header, sizes, every node's child and leaf
+ * ranges, record roots, the slot map of two-reference BLASes) before anything reaches the device
+ * and rejects a corrupt one, or one of another version, with HRT_ERR_INVALID_ARG. No counterpart
+ * in the reference (it rebuilds at every start). */
 uint64_t hrt_blas_serialized_size(const hrt_blas* blas);
 hrt_status hrt_blas_serialize(const hrt_blas* blas, void* dst, uint64_t bytes);
 hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t bytes, void* stream, hrt_blas** out);
