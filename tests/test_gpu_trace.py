@@ -524,6 +524,17 @@ def test_serialized_blas_traces_identically(ctx, gtype, precision):
     with pytest.raises(H.HrtError) as e:
         H.BottomLevelAccelerationStructure.load(bytes(bad), ctx)
     assert "out of range" in str(e.value)
+    if gtype in (LSS, DOTS):
+        # two references per segment: the image ends with the slot map (2 x nprims reference
+        # ids), from which the loader rebuilds the partner map; a repeated id is refused
+        nslots = 2 * blas.info["nprims"]
+        ids = np.frombuffer(data, np.uint32, nslots, len(data) - 4 * nslots)
+        assert np.array_equal(np.sort(ids), np.arange(nslots))
+        bad = bytearray(data)
+        struct.pack_into("<I", bad, len(data) - 4 * nslots + 4, int(ids[0]))
+        with pytest.raises(H.HrtError) as e:
+            H.BottomLevelAccelerationStructure.load(bytes(bad), ctx)
+        assert "permutation" in str(e.value)
 
 
 @pytest.mark.parametrize("size", [0.03, 0.1])
