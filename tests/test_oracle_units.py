@@ -305,3 +305,33 @@ def test_voxelize_known_answers(orc):
     # boxes come in ascending grid index and tile the grid exactly
     gi = v[:, 6].view(np.uint32)
     assert np.all(np.diff(gi.astype(np.int64)) > 0)
+
+
+@pytest.mark.parametrize("gtype", [LSS, DOTS])
+def test_two_reference_boxes_cover_each_segment(orc, gtype):
+    """LSS and DOTS segments enter the BVH as two references: the boxes of the segment's halves
+    (reference 2 i + h). Their union is the segment's own box bit for bit, the two halves share
+    their midpoint face, and their surface area is smaller; Phantom keeps one reference."""
+    import vkhrt_gb300 as H
+    from hairscene import lines_from_strands, oracle_geometry, ref_boxes
+    v, r, off = H.generate_strands(H.StrandParams(seed=31, nstrands=120, nverts=17))
+    lines, lrad = lines_from_strands(v, r, off)
+    n = len(lines)
+    data, rad = oracle_geometry(orc, gtype, lines, lrad)
+    seg = np.zeros((n, 6), np.float32)
+    orc.orc_prim_boxes(gtype, P(np.ascontiguousarray(data)), P(np.ascontiguousarray(rad)), n, P(seg))
+    h = ref_boxes(orc, gtype, data, rad, n).reshape(n, 2, 6)
+    union = np.concatenate([np.minimum(h[:, 0, :3], h[:, 1, :3]), np.maximum(h[:, 0, 3:], h[:, 1, 3:])], axis=1)
+    assert union.tobytes() == seg.tobytes()
+    assert np.all(h[:, :, :3] <= h[:, :, 3:])
+    # the halves overlap in a slab through the midpoint (no gap between them on any axis)
+    assert np.all(np.maximum(h[:, 0, :3], h[:, 1, :3]) <= np.minimum(h[:, 0, 3:], h[:, 1, 3:]))
+
+    def area(b):
+        d = b[..., 3:] - b[..., :3]
+        return d[..., 0] * d[..., 1] + d[..., 1] * d[..., 2] + d[..., 0] * d[..., 2]
+    assert area(h).sum() < 0.8 * area(seg).sum()
+    ph_data, ph_rad = oracle_geometry(orc, PHANTOM, lines, lrad)
+    ph_seg = np.zeros((n, 6), np.float32)
+    orc.orc_prim_boxes(PHANTOM, P(ph_data), P(ph_rad), n, P(ph_seg))
+    assert ref_boxes(orc, PHANTOM, ph_data, ph_rad, n).tobytes() == ph_seg.tobytes()
