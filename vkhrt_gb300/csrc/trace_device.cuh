@@ -817,8 +817,9 @@ __device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
     b = hi;
 }
 
-// Traverses one BLAS. any_hit: stop at the first accepted hit (shadow rays), skipping slot
-// `skip_slot` of instance `skip_inst`.
+// Traverses one BLAS. any_hit: stop at the first accepted hit (shadow rays), skipping the
+// segment in slot `skip_slot` of instance `skip_inst` (both of its slots in a two-reference
+// BLAS).
 template <bool kQuant>
 __device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit& h, bool any_hit, uint32_t skip_inst,
                          uint32_t skip_slot, bool fp64_resolve, Stats& st, uint32_t& err) {
@@ -836,7 +837,10 @@ __device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit
             uint32_t first = (e.x & ~kLeafFlag) >> 2, cnt = (e.x & 3u) + 1u;
             for (uint32_t j = 0; j < cnt; ++j) {
                 uint32_t slot = first + j;
-                if (any_hit && inst == skip_inst && slot == skip_slot) continue;
+                // the skipped segment's slots: its own and, with two references, its partner's
+                if (any_hit && inst == skip_inst &&
+                    (slot == skip_slot || (B.partner && slot == __ldg(&B.partner[skip_slot]))))
+                    continue;
                 ++st.prims;
                 if (leaf_test(B, slot, inst, R, h, fp64_resolve, st)) {
                     found = true;
