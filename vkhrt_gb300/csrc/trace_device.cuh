@@ -90,7 +90,8 @@ template <class T> __device__ __forceinline__ T prhi_div(T a, T b) { return a / 
 template <> __device__ __forceinline__ float prhi_div<float>(float a, float b) { return __fdividef(a, b); }
 // Square roots of the FP32 intersectors: the approximate root of PTX (sqrt.approx.f32), which
 // left the hit ids, distances and colours of the FP32 solves against the FP64 solve as they were
-// with the IEEE root (0 mismatches on the C2, C4 and C5 samples); FP64 takes the exact root.
+// with the IEEE root (0 mismatches on the sampled rays of a 3.15 M-segment LSS frame, a
+// 19 M-segment Phantom frame and a 16-scene batch); FP64 takes the exact root.
 template <class T> __device__ __forceinline__ T prhi_sqrt(T x) { return sqrt(x); }
 template <> __device__ __forceinline__ float prhi_sqrt<float>(float x) {
     float r;
@@ -1277,8 +1278,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     // FP64 pass: only the first lanes of a warp take work (at once, whenever one is idle), two
     // while the listed items fit two per warp of the grid, more when there are more: the few
     // listed samples then spread over many warps instead of packing 32 divergent FP64 solves into
-    // one (the pass is as long as its slowest warp and sits on the batch's critical path; C5
-    // +3.4 % against 32 lanes)
+    // one (the pass is as long as its slowest warp and sits on the batch's critical path; the
+    // 16-scene batch ran 3.4 % faster than with 32 lanes)
     uint32_t take = kFull;
     if (kPass == 2) {
         const uint64_t warps = uint64_t(gridDim.x) * (blockDim.x / 32);
