@@ -121,20 +121,23 @@ typedef struct hrt_blas_info {
 
 /* Parts of a built BLAS copied to the host for inspection (bit-exact tests). A BLAS keeps only
  * what tracing reads (NODES, PRIMS, PRIM_ORDER, ROOTS); the other parts need
- * HRT_BUILD_KEEP_INTERMEDIATE (otherwise hrt_blas_get returns HRT_ERR_UNSUPPORTED). */
+ * HRT_BUILD_KEEP_INTERMEDIATE (otherwise hrt_blas_get returns HRT_ERR_UNSUPPORTED).
+ * n below is the number of BVH references: nprims, or 2 nprims for LSS and DOTS BLASes, whose
+ * segments enter the BVH as the boxes of their two halves (reference id 2 segment + half).
+ * CURVES, DOTS_VERTICES and LSS have one row per segment. */
 typedef enum hrt_blas_part {
-    HRT_PART_PRIM_BOXES = 0,    /* float[n][6], primitive (segment) order */
+    HRT_PART_PRIM_BOXES = 0,    /* float[n][6], reference order */
     HRT_PART_MORTON_SORTED = 1, /* uint64[n] (needs HRT_BUILD_KEEP_INTERMEDIATE) */
     HRT_PART_SORTED_INDEX = 2,  /* uint32[n] (needs KEEP_INTERMEDIATE) */
     HRT_PART_BIN_LEFT = 3,      /* uint32[n-1] (needs KEEP_INTERMEDIATE) */
     HRT_PART_BIN_RIGHT = 4,
     HRT_PART_BIN_BOXES = 5,     /* float[n-1][6] */
     HRT_PART_NODES = 6,         /* raw BVH8 nodes, nnodes * node_bytes */
-    HRT_PART_PRIM_ORDER = 7,    /* uint32[n]: leaf slot -> segment index */
-    HRT_PART_PRIMS = 8,         /* raw primitive records, n * prim_bytes */
-    HRT_PART_CURVES = 9,        /* float[n][12] Bezier control points (Phantom, FP32) */
-    HRT_PART_DOTS_VERTICES = 10,/* float[n][36] (DOTS), the reference's 12 vertices/segment */
-    HRT_PART_LSS = 11,          /* float[n][8]: p0 xyz, p1 xyz, r0, r1 */
+    HRT_PART_PRIM_ORDER = 7,    /* uint32[n]: leaf slot -> reference id */
+    HRT_PART_PRIMS = 8,         /* raw primitive records in slot order, n * prim_bytes */
+    HRT_PART_CURVES = 9,        /* float[nprims][12] Bezier control points (Phantom, FP32) */
+    HRT_PART_DOTS_VERTICES = 10,/* float[nprims][36] (DOTS), the reference's 12 vertices/segment */
+    HRT_PART_LSS = 11,          /* float[nprims][8]: p0 xyz, p1 xyz, r0, r1 */
     HRT_PART_QNODES = 12,       /* raw quantised nodes (80 B each); of an FP32 BLAS only when kept */
     HRT_PART_ROOTS = 13         /* float[nchunks][4] quantised Phantom roots */
 } hrt_blas_part;
