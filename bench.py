@@ -4,7 +4,8 @@
 Default workload (c5_batched): 16 seeded hair models (strands log-uniform in [2,000, 200,000],
 16-128 vertices, Phantom / LSS / DOTS in turn, 47.9 M segments in all), each with its own camera,
 resolution (256x256 .. 1920x1080) and 1-4 jittered samples per pixel, Shade() plus one shadow ray
-per hit. Quantised BLASes (8-bit BVH8 boxes; FP16 control points for Phantom), all scenes in one
+per hit. Quantised BLASes (8-bit BVH8 boxes; Phantom segments rebuilt from the strand vertex
+stream), all scenes in one
 CUDA-graph replay of the persistent trace kernel with autotuned settings. A step is one replay.
 `value` counts primary + shadow rays per second with the BVHs resident in HBM (several GB, far
 above the 129 MB L2, so no flush between steps); `plain_fp32` is the same scenes as 16
@@ -37,6 +38,16 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Mrays/s on 1 GB300: quantized/batched vs plain FP32 at >=99.99% hit agreement"
 L2_BYTES = 129 * 1024 * 1024
+PRECISION_DESC = ("quantised (8-bit BVH8 boxes; Phantom segments as 4-byte indices into the strand vertex stream, "
+                  "control points rebuilt from the FP32 vertices in the leaf)")
+DTYPE_DESC = "fp32 (8-bit node boxes)"
+ORACLE_DESC = "FP64 CPU restatement on the original FP32 strands"
+
+
+def prim_test_bytes(info, gtype: int, precision: int) -> int:
+    """Bytes one primitive test reads: the record, and for quantised Phantom the four 16-byte
+    stream entries it indexes."""
+    return int(info["prim_bytes"]) + (64 if gtype == 0 and precision == 1 else 0)
 
 
 def env_int(name, default):
@@ -285,7 +296,7 @@ def config_block(cfg, name):
                         f"{'Bezier' if int(cfg['type']) == 0 else 'LSS' if int(cfg['type']) == 1 else 'DOTS'} segments, "
                         f"{cfg['width']}x{cfg['height']} x {cfg['spp']} spp, Shade + 1 shadow ray",
             "segments": nseg, "image": f"{cfg['width']}x{cfg['height']}", "spp": cfg["spp"],
-            "precision": "quantised (8-bit BVH8 boxes, FP16 control points)" if int(cfg["precision"]) else "fp32",
+            "precision": PRECISION_DESC if int(cfg["precision"]) else "fp32",
             "l2": "inputs larger than L2 (BVH + primitives resident, no flush)", "parallelism": "replicas"}
 
 
@@ -346,7 +357,7 @@ def run_ours(args, dist):
     info = blas.info
     # ---- roofline: algorithmic bytes per launch / launch time ----
     node_b = info["node_bytes"]
-    prim_b = info["prim_bytes"] + (16 if int(cfg["precision"]) == 1 and int(cfg["type"]) == 0 else 0)
+    prim_b = prim_test_bytes(info, int(cfg["type"]), int(cfg["precision"]))
     alg_bytes = st["nodes_visited"] * node_b + st["prims_tested"] * prim_b + w * h * 16
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (ms * 1e-3) / 1e9
@@ -379,7 +390,7 @@ def run_ours(args, dist):
            "d2h_bytes_per_step": w * h * 16, "ms_per_step": round(te * 1e3, 3)}
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp32 (fp16 control-point storage, 8-bit node boxes)",
+            "vs_baseline": None, "dtype": DTYPE_DESC,
             "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
             "config": config_block(cfg, args.config), "rays_per_step": int(rays_per_step),
             "primary_rays_per_step": int(st["primary_rays"]), "shadow_rays_per_step": int(st["shadow_rays"]),
@@ -422,7 +433,7 @@ def run_ours(args, dist):
                              "ties": cmp["ties"], "max_rel_t": cmp["max_rel_t"], "p9999_rel_t": cmp["p9999_rel_t"],
                              "pixels_agreeing": round(float(ok_px.mean()), 6),
                              "max_rgb_err_agreeing": float(dpx[ok_px].max()) if ok_px.any() else None,
-                             "oracle": "FP64 CPU restatement on the same (dequantised) geometry"}
+                             "oracle": ORACLE_DESC}
         rate, desc, secs = cpu_sample_rate(osc, (vi, pi), cfg, 32, target_s=args.cpu_seconds)
         line["cpu_baseline"] = {"value": round(rate, 4), "unit": "Mrays/s", "cores": orc.orc_hardware_threads(),
                                 "kind": "port", "sample": f"{desc}, FP32 oracle, {secs:.1f} s"}
@@ -452,7 +463,7 @@ def batch_config_block(models):
                         f"{{16,32,64,128}} vertices, Phantom/LSS/DOTS in turn), {nseg} segments, own cameras, "
                         f"256x256..1920x1080 at 1-4 spp ({px} primary samples), Shade + 1 shadow ray",
             "segments": nseg, "scenes": len(models), "primary_samples": px,
-            "precision": "quantised (8-bit BVH8 boxes; FP16 control points for Phantom)",
+            "precision": PRECISION_DESC,
             "l2": "inputs larger than L2 (BVHs + primitives resident, no flush)", "parallelism": "replicas"}
 
 
@@ -493,7 +504,7 @@ def run_batched(args, dist):
         H.trace(ctx, t, cam, fr, H.trace_params(jitter=1, seed=17, shading=2, count_stats=1))
         st = fr.stats()
         info = b.info
-        prim_b = info["prim_bytes"] + (16 if int(m["type"]) == 0 else 0)
+        prim_b = prim_test_bytes(info, int(m["type"]), 1)
         rays = st["primary_rays"] + st["shadow_rays"]
         rays_per_step += rays
         alg_bytes += st["nodes_visited"] * info["node_bytes"] + st["prims_tested"] * prim_b + \
@@ -616,7 +627,7 @@ def run_batched(args, dist):
     d2h = sum(m["width"] * m["height"] * 16 for m, *_ in models)
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp32 (fp16 control-point storage, 8-bit node boxes)",
+            "vs_baseline": None, "dtype": DTYPE_DESC,
             "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
             "config": batch_config_block(models), "rays_per_step": int(rays_per_step), "gpu_launches": args.steps,
             "autotuned": {k: int(getattr(tuned, k)) for k in H.TUNED_FIELDS} | {"mean_ms": round(tune_ms, 3)},
@@ -732,7 +743,7 @@ def batch_agreement_and_cpu(args, ctx, q, models):
     return {"agreement": {"rays": int(n_t), "hit_id": round(1.0 - n_mis / max(n_t - n_ties, 1), 6),
                           "mismatches": int(n_mis),
                           "ties": int(n_ties), "max_rel_t": max_rel_t, "max_rgb_err_agreeing": max_rgb,
-                          "oracle": "FP64 CPU restatement on the same (dequantised) geometry, per scene"},
+                          "oracle": ORACLE_DESC + ", per scene"},
             "cpu_baseline": {"value": round(cpu_rays / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads,
                              "kind": "port",
                              "sample": f"{pixel_share(cpu_frac)} of every scene ({cpu_px} pixels, all their "

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HRT_ABI_VERSION 7
+#define HRT_ABI_VERSION 8
 
 typedef enum hrt_status {
     HRT_OK = 0,
@@ -65,8 +65,11 @@ typedef enum hrt_geometry_type {
 
 typedef enum hrt_precision {
     HRT_PRECISION_FP32 = 0,      /* FP32 BVH8 boxes, FP32 primitives */
-    HRT_PRECISION_QUANTISED = 1  /* 8-bit BVH8 child boxes; Phantom control points as FP16
-                                    offsets from the strand's FP32 root */
+    HRT_PRECISION_QUANTISED = 1  /* 8-bit BVH8 child boxes; Phantom segments as a 4-byte index
+                                    into the BLAS's strand vertex stream (the strands' FP32
+                                    vertices and radii, 16 B each, shared by the two segments
+                                    that meet there), from which the leaf test rebuilds the
+                                    Bezier control points bit for bit */
 } hrt_precision;
 
 typedef enum hrt_memory {
@@ -93,7 +96,7 @@ typedef struct hrt_blas_input {
     uint64_t nlines;                /* with line_indices */
     float const_radius;
     float transform[16];            /* object to world, column major (glm::mat4) */
-    uint32_t quant_chunk;           /* quantised Phantom: max segments per FP32 root (0 = 256) */
+    uint32_t quant_chunk;           /* reserved, ignored (0) */
     uint32_t flags;                 /* HRT_BUILD_* */
     /* HRT_BLAS_MESH (renderer.cpp:543-582): 3 vertex indices per triangle; triangle i reports
      * primitive id i. strand_offsets and line_indices must be NULL. */
@@ -120,7 +123,7 @@ typedef struct hrt_blas_info {
 } hrt_blas_info;
 
 /* Parts of a built BLAS copied to the host for inspection (bit-exact tests). A BLAS keeps only
- * what tracing reads (NODES, PRIMS, PRIM_ORDER, ROOTS); the other parts need
+ * what tracing reads (NODES, PRIMS, PRIM_ORDER, STRAND_VERTICES); the other parts need
  * HRT_BUILD_KEEP_INTERMEDIATE (otherwise hrt_blas_get returns HRT_ERR_UNSUPPORTED).
  * n below is the number of BVH references: nprims, or 2 nprims for LSS and DOTS BLASes, whose
  * segments enter the BVH as the boxes of their two halves (reference id 2 segment + half).
@@ -139,7 +142,10 @@ typedef enum hrt_blas_part {
     HRT_PART_DOTS_VERTICES = 10,/* float[nprims][36] (DOTS), the reference's 12 vertices/segment */
     HRT_PART_LSS = 11,          /* float[nprims][8]: p0 xyz, p1 xyz, r0, r1 */
     HRT_PART_QNODES = 12,       /* raw quantised nodes (80 B each); of an FP32 BLAS only when kept */
-    HRT_PART_ROOTS = 13         /* float[nchunks][4] quantised Phantom roots */
+    HRT_PART_STRAND_VERTICES = 13 /* float[nentries][4] quantised Phantom strand vertex stream:
+                                     per run of joined lines (each starting where the previous ends,
+                                     with the same radius there) the point before it, its start,
+                                     each line's end, the point after it; {x, y, z, radius} */
 } hrt_blas_part;
 
 typedef struct hrt_camera {

@@ -67,9 +67,7 @@ def load() -> ctypes.CDLL:
         "orc_generate_aabbs": (None, [P, i64, f32, P]),
         "orc_generate_dots": (None, [P, P, f32, i64, P]),
         "orc_generate_lss": (None, [P, i64, f32, P, P]),
-        "orc_f32_to_f16": (ctypes.c_uint16, [f32]),
-        "orc_quantise_phantom": (i64, [P, P, P, i64, u32, P, P, P, P]),
-        "orc_f16_to_f32": (f32, [ctypes.c_uint16]),
+        "orc_strand_stream": (i64, [P, P, i64, P, P]),
         "orc_prim_boxes": (None, [i32, P, P, i64, P]),
         "orc_ref_boxes": (i64, [i32, P, P, i64, P]),
         "orc_morton": (None, [P, i64, P]),

@@ -816,49 +816,6 @@ static void quantise_node(const Box* cb, const uint8_t* meta, float* p_out, uint
     }
 }
 
-// ---- FP16 (binary16) round-to-nearest-even conversion, written from the IEEE 754 format ---
-static uint16_t f32_to_f16(float f) {
-    uint32_t x;
-    std::memcpy(&x, &f, 4);
-    uint32_t sign = (x >> 16) & 0x8000u;
-    uint32_t absx = x & 0x7fffffffu;
-    if (absx >= 0x7f800000u) return uint16_t(sign | 0x7c00u | (absx > 0x7f800000u ? 0x200u : 0u));
-    if (absx >= 0x477ff000u) return uint16_t(sign | 0x7c00u);  // rounds to infinity
-    int32_t exp = int32_t(absx >> 23) - 127;
-    uint32_t mant = (absx & 0x7fffffu) | 0x800000u;
-    if (exp < -24) {  // below half the smallest subnormal: +-0 (or the subnormal by rounding)
-        if (exp == -25 && (absx & 0x7fffffu) != 0) return uint16_t(sign | 1u);
-        return uint16_t(sign);
-    }
-    uint32_t shift;
-    uint32_t hexp;
-    if (exp < -14) { shift = uint32_t(13 + (-14 - exp)); hexp = 0; }
-    else { shift = 13; hexp = uint32_t(exp + 15); mant &= 0x7fffffu; }
-    uint32_t keep = mant >> shift;
-    uint32_t rem = mant & ((1u << shift) - 1u);
-    uint32_t half = 1u << (shift - 1);
-    if (rem > half || (rem == half && (keep & 1u))) keep += 1;
-    uint32_t h = (hexp << 10) + keep;  // carries propagate into the exponent correctly
-    return uint16_t(sign | h);
-}
-static float f16_to_f32(uint16_t h) {
-    uint32_t sign = uint32_t(h & 0x8000u) << 16;
-    uint32_t e = (h >> 10) & 0x1fu, m = h & 0x3ffu;
-    uint32_t x;
-    if (e == 0) {
-        if (m == 0) x = sign;
-        else {  // subnormal: m * 2^-24 exactly
-            float v = float(m) * 5.9604644775390625e-08f;
-            std::memcpy(&x, &v, 4);
-            x |= sign;
-        }
-    } else if (e == 31) x = sign | 0x7f800000u | (m << 13);
-    else x = sign | ((e + 112) << 23) | (m << 13);
-    float f;
-    std::memcpy(&f, &x, 4);
-    return f;
-}
-
 // ---- voxel hair ------------------------------------------------------------------------------
 // Restated from GenerateVoxelMesh (geometry_processor.cpp:515-602), the capsule voxelisation of
 // "Real-Time Rendering of Dynamic Line Sets using Voxel Ray Tracing" that it follows, with what
@@ -1335,32 +1292,40 @@ void orc_generate_lss(const float* lines, int64_t n, float r, float* pos, float*
         rad[2 * i + 1] = lr;
     }
 }
-uint16_t orc_f32_to_f16(float f) { return f32_to_f16(f); }
-float orc_f16_to_f32(uint16_t h) { return f16_to_f32(h); }
 
-// Quantised Phantom geometry: a chunk is a run of connected lines (end == next start, exact)
-// of at most `chunk` lines; its root is the start of its first line. Control points become
-// root + float(half(cp - root)) and radii float(half(r)) (round to nearest even).
-// Outputs: dequantised curves (n x 12), radii (n x 2), chunk index and first line per line.
-int64_t orc_quantise_phantom(const float* lines, const float* curves, const float* lrad, int64_t n, uint32_t chunk,
-                             float* dq, float* dqr, uint32_t* chunk_id, uint32_t* chunk_first) {
-    if (chunk == 0 || chunk > 256) chunk = 256;
-    int64_t run_start = 0, nchunks = 0, first = 0;
+// Quantised Phantom geometry: the strand vertex stream. A run is a maximal range of lines in
+// which each line starts exactly where the previous one ends (the neighbour rule of
+// GenerateCurves, geometry_processor.cpp:140-141) with the same radius at the joint. Run r of
+// lines [a, b) fills the b - a + 3 entries from a + 3 r: the point before the run (the previous
+// line's start when that line ends where the run starts, else the run's own start), the run's
+// start, each line's end, and the point after the run (the next line's end when it starts where
+// the run ends, else the run's own end); an entry is {x, y, z, radius at the point}, and the two
+// outer entries carry the radius of the point beside them. Line i gets entry i + 3 r: entries
+// e .. e + 3 are its curve's neighbours p0, p1, p2, p3. Returns the number of entries; `entries`
+// holds 4 (n + 3 n) floats at most.
+int64_t orc_strand_stream(const float* lines, const float* lrad, int64_t n, float* entries, uint32_t* line_entry) {
+    int64_t run = -1;
+    auto put = [&](int64_t e, const float* p, float r) {
+        entries[4 * e] = p[0]; entries[4 * e + 1] = p[1]; entries[4 * e + 2] = p[2]; entries[4 * e + 3] = r;
+    };
+    auto joins = [&](int64_t i) {  // line i starts where line i - 1 ends
+        return i > 0 && i < n && ld3(lines + 6 * (i - 1) + 3) == ld3(lines + 6 * i);
+    };
     for (int64_t i = 0; i < n; ++i) {
-        bool start = i == 0 || !(ld3(lines + 6 * (i - 1) + 3) == ld3(lines + 6 * i));
-        if (start) run_start = i;
-        if ((i - run_start) % chunk == 0) { ++nchunks; first = i; }
-        chunk_id[i] = uint32_t(nchunks - 1);
-        chunk_first[i] = uint32_t(first);
-        const float* root = curves + 12 * first;
-        for (int j = 0; j < 12; ++j) {
-            float off = curves[12 * i + j] - root[j % 3];
-            dq[12 * i + j] = root[j % 3] + f16_to_f32(f32_to_f16(off));
+        const bool start = !(joins(i) && lrad[2 * i - 1] == lrad[2 * i]);
+        if (start) ++run;
+        const int64_t e = i + 3 * run;
+        line_entry[i] = uint32_t(e);
+        const float* L = lines + 6 * i;
+        if (start) {
+            put(e, joins(i) ? lines + 6 * (i - 1) : L, lrad[2 * i]);
+            put(e + 1, L, lrad[2 * i]);
         }
-        dqr[2 * i] = f16_to_f32(f32_to_f16(lrad[2 * i]));
-        dqr[2 * i + 1] = f16_to_f32(f32_to_f16(lrad[2 * i + 1]));
+        put(e + 2, L + 3, lrad[2 * i + 1]);
+        const bool last = i + 1 == n || !(joins(i + 1) && lrad[2 * i + 1] == lrad[2 * i + 2]);
+        if (last) put(e + 3, joins(i + 1) ? lines + 6 * (i + 1) + 3 : L + 3, lrad[2 * i + 1]);
     }
-    return nchunks;
+    return n + 3 * (run + 1);
 }
 
 // ---- LBVH pipeline (for bit-exact comparison with the device build) -------------------------

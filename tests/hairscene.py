@@ -24,6 +24,17 @@ def P(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
+def strand_stream(orc, lines: np.ndarray, lrad: np.ndarray):
+    """The oracle's strand vertex stream of quantised Phantom lines: (entries (m, 4), first entry
+    of each line)."""
+    n = lines.shape[0]
+    ent = np.zeros((n + 3 * n, 4), np.float32)
+    first = np.zeros(n, np.uint32)
+    m = orc.orc_strand_stream(P(np.ascontiguousarray(lines, np.float32)), P(np.ascontiguousarray(lrad, np.float32)),
+                              n, P(ent), P(first))
+    return np.ascontiguousarray(ent[:m]), first
+
+
 def lines_from_strands(v: np.ndarray, r: np.ndarray | None, off: np.ndarray, const_r: float = 0.02):
     """Consecutive vertices of each strand form lines (n x 6) with end radii (n x 2)."""
     ls, rs = [], []
@@ -44,21 +55,16 @@ def lines_from_strands(v: np.ndarray, r: np.ndarray | None, off: np.ndarray, con
             np.ascontiguousarray(np.concatenate(rs), np.float32))
 
 
-def oracle_geometry(orc, gtype: int, lines: np.ndarray, lrad: np.ndarray, quantised: bool = False, chunk: int = 0):
-    """Geometry as the oracle restates it: (data, radius) in the layout orc_scene_add_blas takes."""
+def oracle_geometry(orc, gtype: int, lines: np.ndarray, lrad: np.ndarray, quantised: bool = False):
+    """Geometry as the oracle restates it: (data, radius) in the layout orc_scene_add_blas takes.
+    A quantised BLAS holds the same geometry (its Phantom leaves rebuild the FP32 curves from the
+    strand vertex stream), so `quantised` changes nothing: the oracle always traces the strands'
+    FP32 curves."""
     n = lines.shape[0]
     if gtype == PHANTOM:
         curves = np.zeros((n, 12), np.float32)
         orc.orc_generate_curves(P(lines), n, P(curves))
-        rad = lrad.copy()
-        if quantised:
-            dq = np.zeros_like(curves)
-            dqr = np.zeros_like(rad)
-            cid = np.zeros(n, np.uint32)
-            cfirst = np.zeros(n, np.uint32)
-            orc.orc_quantise_phantom(P(lines), P(curves), P(lrad), n, chunk, P(dq), P(dqr), P(cid), P(cfirst))
-            return dq, dqr
-        return curves, rad
+        return curves, lrad.copy()
     if gtype == LSS:
         rad = np.where(lrad < np.float32(0.001), np.float32(0.001), lrad).astype(np.float32)
         return lines.copy(), np.ascontiguousarray(rad)

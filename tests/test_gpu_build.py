@@ -1,6 +1,6 @@
 """Device BVH build vs the CPU oracle: every integer and FP32 stage bit for bit.
 
-Geometry processing (GenerateCurves, DOTS vertices, LSS radii, FP16 chunk quantisation),
+Geometry processing (GenerateCurves, DOTS vertices, LSS radii, the quantised strand vertex stream),
 primitive boxes, Morton codes, the stable sort, the Karras hierarchy, the refit, the BVH8
 collapse (topology, child boxes, leaf order) and the 8-bit node quantisation.
 """
@@ -9,7 +9,7 @@ import pytest
 
 import vkhrt_gb300 as H
 from hairscene import (DOTS, LSS, MESH, PHANTOM, P, lines_from_strands, mesh_oracle_data, oracle_geometry, oracle_voxels,
-                       ref_boxes, sphere_mesh)
+                       ref_boxes, sphere_mesh, strand_stream)
 
 pytestmark = pytest.mark.gpu
 
@@ -19,8 +19,7 @@ NODEF = np.dtype([("lo_x", "<f4", 8), ("hi_x", "<f4", 8), ("lo_y", "<f4", 8), ("
 NODEQ = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("imask", "u1"), ("child_base", "<u4"), ("prim_base", "<u4"),
                   ("meta", "u1", 8), ("qlo_x", "u1", 8), ("qhi_x", "u1", 8), ("qlo_y", "u1", 8), ("qhi_y", "u1", 8),
                   ("qlo_z", "u1", 8), ("qhi_z", "u1", 8)])
-PRIMH = np.dtype([("h", "<u2", 14), ("key", "<u4")])
-assert NODEF.itemsize == 224 and NODEQ.itemsize == 80 and PRIMH.itemsize == 32
+assert NODEF.itemsize == 224 and NODEQ.itemsize == 80
 
 
 def oracle_bvh(orc, boxes, max_leaf):
@@ -41,10 +40,18 @@ def oracle_bvh(orc, boxes, max_leaf):
     return out
 
 
-def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=None, const_radius=0.02, chunk=0):
+def rebuild_curves(ent, first):
+    """The control points a quantised Phantom leaf rebuilds from stream entries first .. first + 3
+    (GenerateCurves, tension 1, every float32 operation rounded separately)."""
+    k = np.float32(1.0) / np.float32(6.0)
+    p0, p1, p2, p3 = (ent[first + j, :3] for j in range(4))
+    return np.ascontiguousarray(np.concatenate([p1, p1 + (p2 - p0) * k, p2 - (p3 - p1) * k, p2], axis=1), np.float32)
+
+
+def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=None, const_radius=0.02):
     inp = H.BLASInput(type=H.BLASType(gtype), vertices=v, radius=r, strand_offsets=None if line_indices is not None else off,
                       line_indices=line_indices, precision=H.Precision(precision), max_leaf=max_leaf,
-                      const_radius=const_radius, keep_intermediate=True, quant_chunk=chunk)
+                      const_radius=const_radius, keep_intermediate=True)
     blas = H.BottomLevelAccelerationStructure(inp, ctx)
     if line_indices is None:
         lines, lrad = lines_from_strands(v, r, off, const_radius)
@@ -56,7 +63,7 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
     n = len(lines)
     assert blas.info["nprims"] == n
     quant_prims = precision == 1 and gtype == PHANTOM
-    data, rad = oracle_geometry(orc, gtype, lines, lrad, quantised=quant_prims, chunk=chunk)
+    data, rad = oracle_geometry(orc, gtype, lines, lrad, quantised=quant_prims)
     if n == 0:
         assert blas.info["nnodes"] == 0
         return blas
@@ -72,18 +79,16 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
         assert blas.get(H.Part.DOTS_VERTICES, np.float32, (n, 36)).tobytes() == data.tobytes()
     o = check_tree(blas, orc, ref_boxes(orc, gtype, data, rad, n), max_leaf, precision)
     if quant_prims:
-        recs = blas.get(H.Part.PRIMS, np.uint8, n * 32).view(PRIMH)
-        halves = recs["h"].view(np.float16).astype(np.float32)
-        key = recs["key"]
-        nroots = int(key.max() >> 8) + 1
-        roots = blas.get(H.Part.ROOTS, np.float32, (nroots, 4))
-        rt = roots[key >> 8, :3]
-        deq = (np.repeat(rt, 4, axis=0).reshape(n, 4, 3) + halves[:, :12].reshape(n, 4, 3)).astype(np.float32)
+        # the strand vertex stream and each slot's first entry equal the oracle's, and the control
+        # points and radii rebuilt from them are the FP32 curves bit for bit
+        ent, first = strand_stream(orc, lines, lrad)
+        assert blas.get(H.Part.STRAND_VERTICES, np.float32, ent.shape).tobytes() == ent.tobytes()
+        recs = blas.get(H.Part.PRIMS, np.uint32, n)
         order = o["order"]
-        assert deq.reshape(n, 12).tobytes() == np.ascontiguousarray(data[order]).tobytes()
-        assert np.ascontiguousarray(halves[:, 12:14]).tobytes() == np.ascontiguousarray(rad[order]).tobytes()
-        first = roots[key >> 8, 3].view(np.uint32)
-        assert np.array_equal(first + (key & 0xff), order)
+        assert np.array_equal(recs, first[order])
+        assert rebuild_curves(ent, recs).tobytes() == np.ascontiguousarray(data[order]).tobytes()
+        assert np.ascontiguousarray(ent[recs + 1, 3]).tobytes() == np.ascontiguousarray(rad[order, 0]).tobytes()
+        assert np.ascontiguousarray(ent[recs + 2, 3]).tobytes() == np.ascontiguousarray(rad[order, 1]).tobytes()
     return blas
 
 
@@ -146,15 +151,15 @@ def test_build_reference_literal_radius(ctx, orc):
     check_blas(ctx, orc, DOTS, 0, v, None, off, const_radius=0.02)
 
 
-def test_build_line_indices_and_chunks(ctx, orc):
+def test_build_line_indices_and_runs(ctx, orc):
     # explicit index pairs (GenerateLines) in shuffled order: neighbours are only found when
-    # consecutive; quantised chunks of at most 5 segments
+    # consecutive, so the quantised strand stream has a run per joined stretch
     v, r, off = H.generate_strands(H.StrandParams(seed=10, nstrands=50, nverts=20))
     pairs = np.array([(i, i + 1) for s in range(50) for i in range(int(off[s]), int(off[s + 1]) - 1)], np.uint32)
     rng = np.random.default_rng(0)
     sh = pairs.copy()
     rng.shuffle(sh[: len(sh) // 2])
-    check_blas(ctx, orc, PHANTOM, 1, v, r, off, line_indices=sh, chunk=5)
+    check_blas(ctx, orc, PHANTOM, 1, v, r, off, line_indices=sh)
     check_blas(ctx, orc, LSS, 0, v, r, off, line_indices=sh)
 
 
@@ -166,6 +171,11 @@ def test_build_edge_cases(ctx, orc):
     check_blas(ctx, orc, PHANTOM, 0, v, r, np.array([0, 2], np.uint32))            # one line
     check_blas(ctx, orc, LSS, 0, v, r, np.array([0, 3], np.uint32))                # two lines
     check_blas(ctx, orc, PHANTOM, 1, v, r, np.array([0, 3, 6], np.uint32))         # zero-length line
+    # a joint whose two lines carry other radii (a duplicated vertex): the quantised strand
+    # stream starts a new run there, and the curves still see their geometric neighbours
+    v3 = np.array([[0, 0, 0], [0, 1, 0], [0, 1, 0], [0, 2, 0], [0, 3, 0]], np.float32)
+    r3 = np.array([0.01, 0.02, 0.03, 0.02, 0.01], np.float32)
+    check_blas(ctx, orc, PHANTOM, 1, v3, r3, None, line_indices=np.array([[0, 1], [2, 3], [3, 4]], np.uint32))
 
 
 @pytest.mark.parametrize("nseg", [7, 8, 9, 16, 17, 63, 64, 65, 513])
@@ -225,17 +235,18 @@ def test_build_rejects_bad_input(ctx):
 
 
 def test_blas_keeps_only_what_tracing_reads(ctx):
-    """Without HRT_BUILD_KEEP_INTERMEDIATE a BLAS holds nodes, records, roots and the slot map
-    only: the quantised Phantom BLAS is 80 B per node + 32 B per segment + 4 B per segment + 16 B
-    per root, and inspection parts are refused."""
+    """Without HRT_BUILD_KEEP_INTERMEDIATE a BLAS holds nodes, records, the strand vertex stream
+    and the slot map only: the quantised Phantom BLAS is 80 B per node + 4 B per segment (record)
+    + 4 B per segment (slot map) + 16 B per stream entry (segments + 3 per strand), and inspection
+    parts are refused."""
     v, r, off = H.generate_strands(H.StrandParams(seed=5, nstrands=300, nverts=32))
     n = 300 * 31
-    # strands of 31 segments: one FP16 root per strand
-    for prec, node_b, prim_b, nroots in ((H.Precision.QUANTISED, 80, 32, 300), (H.Precision.FP32, 224, 64, 0)):
+    # strands of 31 segments: 34 stream entries per strand
+    for prec, node_b, prim_b, nent in ((H.Precision.QUANTISED, 80, 4, 300 * 34), (H.Precision.FP32, 224, 64, 0)):
         blas = H.BottomLevelAccelerationStructure(
             H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r, strand_offsets=off, precision=prec), ctx)
         info = blas.info
-        assert info["device_bytes"] == info["nnodes"] * node_b + n * prim_b + n * 4 + nroots * 16
+        assert info["device_bytes"] == info["nnodes"] * node_b + n * prim_b + n * 4 + nent * 16
         with pytest.raises(H.HrtError) as e:
             blas.get(H.Part.CURVES, np.float32, (n, 12))
         assert e.value.status == 6 or "not kept" in str(e.value)

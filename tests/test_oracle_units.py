@@ -4,19 +4,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from hairscene import DOTS, LSS, PHANTOM, P, OracleScene
-
-
-def test_f16_round_trip_matches_ieee(orc):
-    rng = np.random.default_rng(3)
-    xs = np.concatenate([rng.normal(size=20000) * s for s in (1e-6, 1e-3, 1, 100, 6e4)]).astype(np.float32)
-    xs = np.concatenate([xs, np.float32([0.0, -0.0, 65504.0, 65520.0, 6.1e-5, 5.96e-8, 2.98e-8, 1e-9])])
-    with np.errstate(over="ignore"):
-        ref = np.float16(xs)
-    for x, hx in zip(xs, ref):
-        h = orc.orc_f32_to_f16(float(x))
-        assert h == int(hx.view(np.uint16)), x
-        assert np.float32(orc.orc_f16_to_f32(h)).tobytes() == np.float32(hx).tobytes()
+from hairscene import DOTS, LSS, PHANTOM, P, OracleScene, lines_from_strands, strand_stream
 
 
 def test_prhi_straight_curve_known_answer(orc):
@@ -335,3 +323,47 @@ def test_two_reference_boxes_cover_each_segment(orc, gtype):
     ph_seg = np.zeros((n, 6), np.float32)
     orc.orc_prim_boxes(PHANTOM, P(ph_data), P(ph_rad), n, P(ph_seg))
     assert ref_boxes(orc, PHANTOM, ph_data, ph_rad, n).tobytes() == ph_seg.tobytes()
+
+
+def _rebuild(ent, first):
+    k = np.float32(1.0) / np.float32(6.0)
+    p0, p1, p2, p3 = (ent[first + j, :3] for j in range(4))
+    return np.ascontiguousarray(np.concatenate([p1, p1 + (p2 - p0) * k, p2 - (p3 - p1) * k, p2], axis=1), np.float32)
+
+
+@pytest.mark.parametrize("case", ["strands", "shuffled", "radius_joint", "touching_strands", "single"])
+def test_strand_stream_rebuilds_the_curves(orc, case):
+    """The quantised Phantom format keeps the strands' FP32 vertices (the strand vertex stream);
+    the control points rebuilt from entries e .. e + 3 of each line equal GenerateCurves' output
+    bit for bit, and entries e + 1, e + 2 carry the line's end radii."""
+    rng = np.random.default_rng(11)
+    if case == "single":
+        lines = np.array([[0, 0, 0, 1, 0, 0]], np.float32)
+        lrad = np.array([[0.01, 0.02]], np.float32)
+    elif case == "radius_joint":  # joined lines whose radii differ at the joint
+        lines = np.array([[0, 0, 0, 0, 1, 0], [0, 1, 0, 0, 2, 0], [0, 2, 0, 0, 3, 0]], np.float32)
+        lrad = np.array([[0.01, 0.02], [0.03, 0.02], [0.02, 0.01]], np.float32)
+    elif case == "touching_strands":  # strand 2 starts where strand 1 ends: GenerateCurves joins them
+        v = np.array([[0, 0, 0], [1, 0, 0], [2, 0, 0], [2, 0, 0], [2, 1, 0], [2, 2, 0]], np.float32)
+        lines, lrad = lines_from_strands(v, np.full(6, 0.01, np.float32), np.array([0, 3, 6]))
+    else:
+        ns, nv = 40, 9
+        v = rng.normal(size=(ns * nv, 3)).astype(np.float32)
+        r = rng.uniform(0.001, 0.01, ns * nv).astype(np.float32)
+        lines, lrad = lines_from_strands(v, r, np.arange(0, ns * nv + 1, nv))
+        if case == "shuffled":
+            idx = np.arange(len(lines))
+            rng.shuffle(idx[: len(idx) // 2])
+            lines, lrad = np.ascontiguousarray(lines[idx]), np.ascontiguousarray(lrad[idx])
+    n = len(lines)
+    curves = np.zeros((n, 12), np.float32)
+    orc.orc_generate_curves(P(lines), n, P(curves))
+    ent, first = strand_stream(orc, lines, lrad)
+    assert _rebuild(ent, first).tobytes() == curves.tobytes()
+    assert np.ascontiguousarray(ent[first + 1, 3]).tobytes() == np.ascontiguousarray(lrad[:, 0]).tobytes()
+    assert np.ascontiguousarray(ent[first + 2, 3]).tobytes() == np.ascontiguousarray(lrad[:, 1]).tobytes()
+    # runs: 3 extra entries each; a joint with other radii on its two sides starts a run
+    if case == "radius_joint":
+        assert len(ent) == n + 3 * 2
+    if case == "touching_strands":
+        assert len(ent) == n + 3

@@ -181,7 +181,7 @@ class Part(enum.IntEnum):
     DOTS_VERTICES = 10
     LSS = 11
     QNODES = 12
-    ROOTS = 13
+    STRAND_VERTICES = 13
 
 
 @dataclass
@@ -201,7 +201,6 @@ class BLASInput:
     transform: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))  # object->world
     precision: Precision = Precision.FP32
     max_leaf: int = 1
-    quant_chunk: int = 0
     keep_intermediate: bool = False
     voxel_size: float = 0.0
 
@@ -278,7 +277,6 @@ class BottomLevelAccelerationStructure:
         xf = np.asarray(inp.transform, dtype=np.float32).reshape(4, 4)
         for i, val in enumerate(xf.T.reshape(-1)):  # column major
             c.transform[i] = float(val)
-        c.quant_chunk = inp.quant_chunk
         c.flags = 1 if inp.keep_intermediate else 0
         h = c_p()
         ctx.check(lib.hrt_blas_build(ctx.handle, ctypes.byref(c), c_p(stream) if stream else None, ctypes.byref(h)))

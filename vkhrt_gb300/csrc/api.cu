@@ -31,7 +31,7 @@ struct hrt_blas {
     float voxel_grid[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // voxels: origin xyz, size, res xyz
     BuildOutput out;
     // the topology, kept on the host for hrt_blas_refit
-    uint32_t max_leaf = 1, quant_chunk = 0;
+    uint32_t max_leaf = 1;
     uint64_t nvertices = 0, nstrands = 0;
     float const_radius = 0.0f;
     bool has_radius = false, has_normals = false;
@@ -548,7 +548,7 @@ static hrt_status build_mesh(hrt_context* ctx, const hrt_blas_input* in, cudaStr
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    BuildInput bi{in->type, in->precision, int(max_leaf), in->quant_chunk, nullptr, nullptr, n, b->keep, tris, tnrm};
+    BuildInput bi{in->type, in->precision, int(max_leaf), nullptr, nullptr, n, b->keep, tris, tnrm};
     char msg[256] = {0};
     e = build_blas_device(bi, b->out, s, msg, sizeof(msg));
     cudaEventRecord(e1, s);
@@ -640,7 +640,6 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
     b->keep = (in->flags & HRT_BUILD_KEEP_INTERMEDIATE) != 0;
     memcpy(b->transform, in->transform, sizeof(b->transform));
     b->max_leaf = max_leaf;
-    b->quant_chunk = in->quant_chunk;
     b->nvertices = in->nvertices;
     b->nstrands = in->nstrands;
     b->const_radius = in->const_radius;
@@ -713,7 +712,7 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    BuildInput bi{in->type, in->precision, int(max_leaf), in->quant_chunk, lines, lrad, nlines, b->keep};
+    BuildInput bi{in->type, in->precision, int(max_leaf), lines, lrad, nlines, b->keep};
     char msg[256] = {0};
     float* vox = nullptr;
     if (in->type == HRT_BLAS_VOXELS) {  // the lines become voxel boxes, the BVH primitives
@@ -789,7 +788,7 @@ hrt_status hrt_blas_refit(hrt_blas* b, const float* vertices, const float* per_v
         dv = const_cast<float*>(vertices);
         dp = const_cast<float*>(per_vertex);
     }
-    BuildInput bi{b->type, b->precision, int(b->max_leaf), b->quant_chunk, nullptr, nullptr, n, b->keep};
+    BuildInput bi{b->type, b->precision, int(b->max_leaf), nullptr, nullptr, n, b->keep};
     if (mesh) {
         if (e == cudaSuccess) e = cudaMalloc(&d0, n * 12);
         if (e == cudaSuccess) e = cudaMemcpyAsync(d0, b->tri_idx.data(), n * 12, cudaMemcpyHostToDevice, s);
@@ -858,7 +857,8 @@ hrt_status hrt_blas_transform(const hrt_blas* b, float out[16]) {
 // ---- serialisation --------------------------------------------------------------------------
 // Layout (little-endian): the header below, then level starts (u32), the refit topology
 // (line offsets, vertex offsets, line indices, triangle indices: u32 each, lengths in the
-// header), then the device arrays: nodes, records, roots (float4), slot map (u32). Records and
+// header), then the device arrays: nodes, records, the strand vertex stream (float4, quantised
+// Phantom), slot map (u32). Records and
 // the slot map have one entry per BVH reference (two per LSS or DOTS segment); the partner map
 // of those two-reference types is rebuilt from the slot map when an image is read.
 namespace {
@@ -866,22 +866,22 @@ struct SerialHeader {
     char magic[4];  // "HRTB"
     uint32_t version;
     int32_t type, precision;
-    uint64_t nprims, nnodes, nroots, node_bytes, prim_bytes;
+    uint64_t nprims, nnodes, nverts, node_bytes, prim_bytes;
     float bounds[6];
     float transform[16];
-    uint32_t max_leaf, quant_chunk;
+    uint32_t max_leaf, reserved;
     uint64_t nvertices, nstrands;
     float const_radius;
     uint32_t has_radius, has_normals;
     uint64_t nlevels, n_line_off, n_vert_off, n_line_idx, n_tri_idx;
 };
-constexpr uint32_t kSerialVersion = 2;
+constexpr uint32_t kSerialVersion = 3;
 
 uint64_t serial_size(const hrt_blas* b) {
     const BuildOutput& o = b->out;
     return sizeof(SerialHeader) +
            4 * (o.level_start.size() + b->line_off.size() + b->vert_off.size() + b->line_idx.size() + b->tri_idx.size()) +
-           o.nnodes * o.node_bytes + o.nslots * o.prim_bytes + o.nroots * 16 + o.nslots * 4;
+           o.nnodes * o.node_bytes + o.nslots * o.prim_bytes + o.nverts * 16 + o.nslots * 4;
 }
 
 // Reads a u32 array of n entries at *p, advancing it; false past the end.
@@ -894,8 +894,9 @@ bool take_u32(const uint8_t*& p, const uint8_t* end, uint64_t n, std::vector<uin
 }
 
 // Host-side check of a deserialised tree, so that tracing it never reads outside its arrays:
-// internal children below nnodes, leaf runs inside the records, FP16 records' roots in range.
-const char* check_tree(int type, int precision, uint64_t nprims, uint64_t nnodes, uint64_t nroots, const uint8_t* nodes,
+// internal children below nnodes, leaf runs inside the records, quantised Phantom records' four
+// stream entries inside the strand vertex stream.
+const char* check_tree(int type, int precision, uint64_t nprims, uint64_t nnodes, uint64_t nverts, const uint8_t* nodes,
                        const uint8_t* prims, const std::vector<uint32_t>& levels) {
     const bool quant = precision == HRT_PRECISION_QUANTISED;
     for (uint64_t i = 0; i < nnodes; ++i) {
@@ -928,8 +929,9 @@ const char* check_tree(int type, int precision, uint64_t nprims, uint64_t nnodes
     if (!levels.empty() && levels.back() != nnodes) return "level starts do not end at the node count";
     if (type == HRT_BLAS_PHANTOM && quant)
         for (uint64_t i = 0; i < nprims; ++i) {
-            const uint32_t key = reinterpret_cast<const PrimPhantomH*>(prims)[i].q1.w;
-            if ((key >> 8) >= nroots) return "record root out of range";
+            uint32_t e;
+            memcpy(&e, prims + 4 * i, 4);
+            if (uint64_t(e) + 4 > nverts) return "record outside the strand vertex stream";
         }
     return nullptr;
 }
@@ -953,13 +955,12 @@ hrt_status hrt_blas_serialize(const hrt_blas* b, void* dst, uint64_t bytes) {
     h.precision = b->precision;
     h.nprims = b->nprims;
     h.nnodes = o.nnodes;
-    h.nroots = o.nroots;
+    h.nverts = o.nverts;
     h.node_bytes = o.node_bytes;
     h.prim_bytes = o.prim_bytes;
     memcpy(h.bounds, o.bounds, sizeof(h.bounds));
     memcpy(h.transform, b->transform, sizeof(h.transform));
     h.max_leaf = b->max_leaf;
-    h.quant_chunk = b->quant_chunk;
     h.nvertices = b->nvertices;
     h.nstrands = b->nstrands;
     h.const_radius = b->const_radius;
@@ -979,7 +980,7 @@ hrt_status hrt_blas_serialize(const hrt_blas* b, void* dst, uint64_t bytes) {
     }
     struct { const void* src; uint64_t n; } parts[] = {{o.nodes, o.nnodes * o.node_bytes},
                                                       {o.prims, o.nslots * o.prim_bytes},
-                                                      {o.roots, o.nroots * 16},
+                                                      {o.verts, o.nverts * 16},
                                                       {o.prim_ids, o.nslots * 4}};
     for (auto& q : parts) {
         if (q.n) CK(ctx, cudaMemcpy(p, q.src, q.n, cudaMemcpyDeviceToHost), "hrt_blas_serialize");
@@ -1002,12 +1003,13 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: not a version-%u BLAS image", kSerialVersion);
     const bool quant = h.precision == HRT_PRECISION_QUANTISED;
     const uint64_t want_node = quant ? sizeof(NodeQ) : sizeof(NodeF);
-    const uint64_t want_prim = h.type == HRT_BLAS_PHANTOM ? (quant ? 32 : 64)
+    const uint64_t want_prim = h.type == HRT_BLAS_PHANTOM ? (quant ? 4 : 64)
                                : ((h.type == HRT_BLAS_LSS || h.type == HRT_BLAS_VOXELS) ? 32 : 80);
     if (h.type < HRT_BLAS_PHANTOM || h.type > HRT_BLAS_VOXELS || (h.precision != HRT_PRECISION_FP32 && !quant) ||
         h.node_bytes != want_node || h.prim_bytes != want_prim || h.nprims >= (1ull << 29) || (h.nprims << ref_shift(h.type)) >= (1ull << 29) ||
         h.nnodes > (h.nprims << ref_shift(h.type)) + 1 ||
-        h.nroots > h.nprims || (h.nprims && !h.nnodes) || h.max_leaf < 1 || h.max_leaf > 3)
+        h.nverts > 4 * h.nprims || (h.type == HRT_BLAS_PHANTOM && quant ? (h.nprims && h.nverts < h.nprims + 3) : h.nverts != 0) ||
+        (h.nprims && !h.nnodes) || h.max_leaf < 1 || h.max_leaf > 3)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: inconsistent header");
     hrt_blas* b = new (std::nothrow) hrt_blas();
     if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_blas_deserialize: host allocation");
@@ -1022,7 +1024,6 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
     b->nprims = h.nprims;
     memcpy(b->transform, h.transform, sizeof(h.transform));
     b->max_leaf = h.max_leaf;
-    b->quant_chunk = h.quant_chunk;
     b->nvertices = h.nvertices;
     b->nstrands = h.nstrands;
     b->const_radius = h.const_radius;
@@ -1035,11 +1036,11 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
         return reject("truncated tables");
     const uint32_t shift = ref_shift(h.type);
     const uint64_t nslots = h.nprims << shift;
-    const uint64_t nb = h.nnodes * h.node_bytes, pbytes = nslots * h.prim_bytes, rb = h.nroots * 16, ib = nslots * 4;
+    const uint64_t nb = h.nnodes * h.node_bytes, pbytes = nslots * h.prim_bytes, rb = h.nverts * 16, ib = nslots * 4;
     if (nb + pbytes + rb + ib > uint64_t(end - p)) return reject("truncated arrays");
     const uint8_t* nodes = p;
     const uint8_t* prims = p + nb;
-    if (const char* why = check_tree(h.type, h.precision, nslots, h.nnodes, h.nroots, nodes, prims, o.level_start))
+    if (const char* why = check_tree(h.type, h.precision, nslots, h.nnodes, h.nverts, nodes, prims, o.level_start))
         return reject(why);
     // two references per segment: the slot map must be a permutation of the reference ids, and
     // the partner map follows from it
@@ -1055,7 +1056,7 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
         for (uint64_t i = 0; i < nslots; ++i) partner[i] = slot_of[ids[i] ^ 1u];
     }
     o.nnodes = h.nnodes;
-    o.nroots = h.nroots;
+    o.nverts = h.nverts;
     o.node_bytes = h.node_bytes;
     o.prim_bytes = h.prim_bytes;
     memcpy(o.bounds, h.bounds, sizeof(o.bounds));
@@ -1064,7 +1065,7 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
     cudaError_t e = cudaSuccess;
     struct { void** dst; const uint8_t* src; uint64_t n; } parts[] = {{&o.nodes, nodes, nb},
                                                                      {&o.prims, prims, pbytes},
-                                                                     {reinterpret_cast<void**>(&o.roots), prims + pbytes, rb},
+                                                                     {reinterpret_cast<void**>(&o.verts), prims + pbytes, rb},
                                                                      {reinterpret_cast<void**>(&o.prim_ids), prims + pbytes + rb, ib},
                                                                      {reinterpret_cast<void**>(&o.partner),
                                                                       reinterpret_cast<const uint8_t*>(partner.data()),
@@ -1123,7 +1124,7 @@ hrt_status hrt_blas_get(const hrt_blas* b, int32_t part, void* dst, uint64_t byt
         case HRT_PART_PRIMS: src = o.prims; need = ns * o.prim_bytes; break;
         case HRT_PART_CURVES: src = o.curves; need = n * 48; break;
         case HRT_PART_LSS: src = b->type == HRT_BLAS_LSS ? o.geom : nullptr; need = n * 32; break;
-        case HRT_PART_ROOTS: src = o.roots; need = o.nroots * 16; break;
+        case HRT_PART_STRAND_VERTICES: src = o.verts; need = o.nverts * 16; break;
         case HRT_PART_DOTS_VERTICES: {
             if (b->type != HRT_BLAS_DOTS) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_get: not a DOTS BLAS");
             need = n * 144;
@@ -1169,7 +1170,7 @@ hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint3
         type_mask |= 1u << b->type;
         d.b.nodes = b->out.nodes;
         d.b.prims = b->out.prims;
-        d.b.roots = b->out.roots;
+        d.b.verts = b->out.verts;
         d.b.prim_ids = b->out.prim_ids;
         d.b.partner = b->out.partner;
         d.b.ref_shift = ref_shift(b->type);

@@ -6,7 +6,7 @@
 //
 // Pipeline (one stream, temporaries from the stream-ordered allocator):
 //   lines -> per type: Bezier curves (GenerateCurves, geometry_processor.cpp:123-156) and, for
-//   the quantised format, FP16 offsets from chunk roots | LSS spheres (:273-298) | DOTS frames
+//   the quantised format, the strand vertex stream | LSS spheres (:273-298) | DOTS frames
 //   (:201-271) -> primitive boxes -> centroid bounds -> 63-bit Morton codes -> stable LSD radix
 //   sort (8 passes of 8 bits) -> Karras hierarchy -> bottom-up refit -> greedy surface-area
 //   collapse to BVH8, breadth first -> FP32 and 8-bit quantised node encodings -> primitive
@@ -195,43 +195,42 @@ __global__ void curves_kernel(const float* lines, uint64_t n, float* curves) {
     st3(c + 9, p2);
 }
 
-// Quantised Phantom chunks: a chunk is a run of connected lines (end == next start) of at most
-// `chunk` lines; its root is the start point of its first line.
-__global__ void run_flags_kernel(const float* lines, uint64_t n, uint32_t* run_start_pos) {
+// Quantised Phantom geometry: the strand vertex stream. A stream run is a maximal range of
+// lines in which every line starts where the previous one ends (exact equality, the neighbour
+// rule of GenerateCurves) with the same radius at the joint. Run r of lines [a, b) occupies the
+// b - a + 3 entries from a + 3 r: the point before it (the previous line's start when that line
+// joins it geometrically, otherwise its own start), its start, the end of each of its lines, and
+// the point after it (the next line's end when that line joins it, otherwise its own end); each
+// entry is {x, y, z, radius at the point}. Line i of run r has entry e = i + 3 r, and its
+// GenerateCurves neighbours p0, p1, p2, p3 are entries e .. e + 3, so the leaf test rebuilds the
+// line's Bezier control points from the FP32 vertices with the curve kernel's operations, bit for
+// bit.
+__global__ void stream_flags_kernel(const float* lines, const float* lrad, uint64_t n, uint32_t* flags) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    bool start = i == 0 || !(ld3(lines + 6 * (i - 1) + 3) == ld3(lines + 6 * i));
-    run_start_pos[i] = start ? uint32_t(i) : 0u;
+    const bool joined = i > 0 && ld3(lines + 6 * (i - 1) + 3) == ld3(lines + 6 * i) && lrad[2 * i - 1] == lrad[2 * i];
+    flags[i] = joined ? 0u : 1u;
 }
-__global__ void chunk_flags_kernel(const uint32_t* run_start, uint64_t n, uint32_t chunk, uint32_t* flags) {
+// run_incl: inclusive scan of the flags (run index + 1); writes the entries and line_entry[i].
+__global__ void stream_kernel(const float* lines, const float* lrad, const uint32_t* flags, const uint32_t* run_incl,
+                              uint64_t n, float4* verts, uint32_t* line_entry) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t d = uint32_t(i) - run_start[i];
-    flags[i] = (d % chunk) == 0 ? 1u : 0u;
-}
-__global__ void chunk_roots_kernel(const float* curves, const uint32_t* flags, const uint32_t* chunk_incl, uint64_t n,
-                                   float4* roots) {
-    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n || !flags[i]) return;
-    uint32_t c = chunk_incl[i] - 1;
-    const float* p = curves + 12 * i;
-    roots[c] = make_float4(p[0], p[1], p[2], __uint_as_float(uint32_t(i)));
-}
-// Dequantised control points: root + float(half(cp - root)); radii float(half(r)).
-__global__ void dequant_curves_kernel(const float* curves, const float* lrad, const uint32_t* chunk_incl,
-                                      const float4* roots, uint64_t n, float* dq, float* dqr, uint32_t* keys) {
-    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t c = chunk_incl[i] - 1;
-    float4 r = roots[c];
-    float rt[3] = {r.x, r.y, r.z};
-    for (int j = 0; j < 12; ++j) {
-        float off = curves[12 * i + j] - rt[j % 3];
-        dq[12 * i + j] = rt[j % 3] + __half2float(__float2half_rn(off));
+    const uint64_t e = i + 3ull * (run_incl[i] - 1u);
+    line_entry[i] = uint32_t(e);
+    const float* L = lines + 6 * i;
+    if (flags[i]) {  // first line of its run: the point before it and its start
+        const bool geo_prev = i > 0 && ld3(lines + 6 * (i - 1) + 3) == ld3(L);
+        const float* q = geo_prev ? lines + 6 * (i - 1) : L;
+        verts[e] = make_float4(q[0], q[1], q[2], lrad[2 * i]);
+        verts[e + 1] = make_float4(L[0], L[1], L[2], lrad[2 * i]);
     }
-    dqr[2 * i] = __half2float(__float2half_rn(lrad[2 * i]));
-    dqr[2 * i + 1] = __half2float(__float2half_rn(lrad[2 * i + 1]));
-    keys[i] = (c << 8) | (uint32_t(i) - __float_as_uint(r.w));
+    verts[e + 2] = make_float4(L[3], L[4], L[5], lrad[2 * i + 1]);
+    if (i + 1 == n || flags[i + 1]) {  // last line of its run: the point after it
+        const bool geo_next = i + 1 < n && ld3(L + 3) == ld3(lines + 6 * (i + 1));
+        const float* q = geo_next ? lines + 6 * (i + 1) + 3 : L + 3;
+        verts[e + 3] = make_float4(q[0], q[1], q[2], lrad[2 * i + 1]);
+    }
 }
 
 // GenerateLinearSweptSpheres geometry_processor.cpp:273-298: radius glm::max(r, 0.001).
@@ -837,10 +836,10 @@ __global__ void map_order_kernel(const uint32_t* sorted_pos, const uint32_t* sor
     out[i] = sorted_index[sorted_pos[i]];
 }
 
-// Primitive records in slot order.
+// Primitive records in slot order. Quantised Phantom: the segment's first strand-stream entry.
 __global__ void records_kernel(int type, int precision, uint32_t shift, const uint32_t* ids, uint64_t n, const float* curves,
-                               const float* lrad, const float* geom, const uint32_t* chunk_incl, const float4* roots,
-                               const float* tri_nrm, void* prims) {
+                               const float* lrad, const float* geom, const uint32_t* line_entry, const float* tri_nrm,
+                               void* prims) {
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t s = ids[i] >> shift;  // the slot's segment
@@ -853,23 +852,7 @@ __global__ void records_kernel(int type, int precision, uint32_t shift, const ui
         r.d = make_float4(c[9], c[10], c[11], 0.0f);
         static_cast<PrimPhantomF*>(prims)[i] = r;
     } else if (type == HRT_BLAS_PHANTOM) {
-        const float* c = curves + 12 * uint64_t(s);
-        uint32_t ch = chunk_incl[s] - 1;
-        float4 rt = roots[ch];
-        float root[3] = {rt.x, rt.y, rt.z};
-        __half h[16];
-        for (int j = 0; j < 12; ++j) h[j] = __float2half_rn(c[j] - root[j % 3]);
-        h[12] = __float2half_rn(lrad[2 * uint64_t(s)]);
-        h[13] = __float2half_rn(lrad[2 * uint64_t(s) + 1]);
-        uint32_t key = (ch << 8) | (s - __float_as_uint(rt.w));
-        uint32_t w[8];
-        for (int j = 0; j < 7; ++j)
-            w[j] = uint32_t(__half_as_ushort(h[2 * j])) | (uint32_t(__half_as_ushort(h[2 * j + 1])) << 16);
-        w[7] = key;
-        PrimPhantomH r;
-        r.q0 = make_uint4(w[0], w[1], w[2], w[3]);
-        r.q1 = make_uint4(w[4], w[5], w[6], w[7]);
-        static_cast<PrimPhantomH*>(prims)[i] = r;
+        static_cast<uint32_t*>(prims)[i] = line_entry[s];
     } else if (type == HRT_BLAS_LSS) {
         const float* g = geom + 8 * uint64_t(s);
         PrimLss r;
@@ -1044,7 +1027,7 @@ cudaError_t make_lines(const float* verts, const float* vrad, float const_radius
 }
 
 void free_build_output(BuildOutput& o) {
-    void* ptrs[] = {o.nodes, o.qnodes_aux, o.prims, o.roots, o.prim_ids, o.partner, o.prim_boxes, o.curves, o.geom,
+    void* ptrs[] = {o.nodes, o.qnodes_aux, o.prims, o.verts, o.prim_ids, o.partner, o.prim_boxes, o.curves, o.geom,
                     o.morton_sorted, o.sorted_index, o.bin_left, o.bin_right, o.bin_boxes, o.prim_order};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -1139,17 +1122,13 @@ cudaError_t voxelize_device(const float* lines, uint64_t nlines, float r, float 
 }
 
 // Geometry processing shared by build and refit: per-segment boxes into `boxes`, the
-// intersected geometry into out.curves / out.geom and, for quantised Phantom, the chunk roots
-// into out.roots (each allocated when null; a refit reuses them) with the chunk map in g.
+// intersected geometry into out.curves / out.geom and, for quantised Phantom, the strand vertex
+// stream into out.verts (each allocated when null; a refit reuses them) with each line's first
+// stream entry in g.line_entry.
 struct GeomTmp {
-    float* rad_for_boxes = nullptr;  // Phantom radii used for the boxes
-    float* dq = nullptr;             // dequantised curves (quantised Phantom)
-    uint32_t* chunk_incl = nullptr;
-    uint32_t* keys_tmp = nullptr;
+    uint32_t* line_entry = nullptr;
     void release(cudaStream_t s) {
-        void* p[] = {rad_for_boxes, dq, chunk_incl, keys_tmp};
-        for (void* q : p)
-            if (q) cudaFreeAsync(q, s);
+        if (line_entry) cudaFreeAsync(line_entry, s);
         *this = GeomTmp{};
     }
 };
@@ -1157,54 +1136,39 @@ cudaError_t geometry_stage(const BuildInput& in, BuildOutput& out, float* boxes,
                            char* msg, size_t msglen) {
     const uint64_t n = in.n;
     const unsigned T = 256;
-    uint64_t nchunks = 0;
     if (in.type == HRT_BLAS_PHANTOM) {
         if (!out.curves) HRT_CK(cudaMalloc(&out.curves, n * 12 * sizeof(float)));
         curves_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, n, out.curves);
         HRT_CK(cudaGetLastError());
+        // boxes of the FP32 curves: the quantised format rebuilds exactly these curves
+        boxes_phantom_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, in.lrad, n, boxes);
         if (in.precision == HRT_PRECISION_QUANTISED) {
-            uint32_t chunk = in.quant_chunk ? in.quant_chunk : 256u;
-            if (chunk > 256u) chunk = 256u;
-            uint32_t *runpos, *runstart, *flags, *total;
-            HRT_CK(dalloc(&runpos, n, s));
-            HRT_CK(dalloc(&runstart, n, s));
+            uint32_t *flags, *run_incl, *total;
             HRT_CK(dalloc(&flags, n, s));
-            HRT_CK(dalloc(&g.chunk_incl, n, s));
+            HRT_CK(dalloc(&run_incl, n, s));
             HRT_CK(dalloc(&total, 1, s));
-            run_flags_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, n, runpos);
-            HRT_CK(device_scan<MaxOp>(runpos, runstart, n, true, nullptr, s));
-            chunk_flags_kernel<<<grid_for(n, T), T, 0, s>>>(runstart, n, chunk, flags);
-            HRT_CK(device_scan<SumOp>(flags, g.chunk_incl, n, true, total, s));
-            uint32_t h_total = 0;
-            HRT_CK(cudaMemcpyAsync(&h_total, total, 4, cudaMemcpyDeviceToHost, s));
+            HRT_CK(dalloc(&g.line_entry, n, s));
+            stream_flags_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, n, flags);
+            HRT_CK(device_scan<SumOp>(flags, run_incl, n, true, total, s));
+            uint32_t nruns = 0;
+            HRT_CK(cudaMemcpyAsync(&nruns, total, 4, cudaMemcpyDeviceToHost, s));
             HRT_CK(cudaStreamSynchronize(s));
-            nchunks = h_total;
-            if (nchunks >= (1ull << 24)) {
-                snprintf(msg, msglen, "quantised Phantom BLAS needs %llu chunk roots; the limit is 2^24",
-                         (unsigned long long)nchunks);
+            const uint64_t nverts = n + 3ull * nruns;
+            if (out.verts && nverts != out.nverts) {
+                snprintf(msg, msglen, "refit: the strands' runs changed (%llu stream entries, built with %llu)",
+                         (unsigned long long)nverts, (unsigned long long)out.nverts);
+                cudaFreeAsync(flags, s);
+                cudaFreeAsync(run_incl, s);
+                cudaFreeAsync(total, s);
                 return cudaErrorInvalidValue;
             }
-            if (out.roots && nchunks != out.nroots) {
-                snprintf(msg, msglen, "refit: the strands' chunks changed (%llu roots, built with %llu)",
-                         (unsigned long long)nchunks, (unsigned long long)out.nroots);
-                return cudaErrorInvalidValue;
-            }
-            if (!out.roots) HRT_CK(cudaMalloc(&out.roots, nchunks * sizeof(float4)));
-            out.nroots = nchunks;
-            chunk_roots_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, flags, g.chunk_incl, n, out.roots);
-            HRT_CK(dalloc(&g.dq, n * 12, s));
-            HRT_CK(dalloc(&g.rad_for_boxes, n * 2, s));
-            HRT_CK(dalloc(&g.keys_tmp, n, s));
-            dequant_curves_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, in.lrad, g.chunk_incl, out.roots, n, g.dq,
-                                                                g.rad_for_boxes, g.keys_tmp);
+            if (!out.verts) HRT_CK(cudaMalloc(&out.verts, nverts * sizeof(float4)));
+            out.nverts = nverts;
+            stream_kernel<<<grid_for(n, T), T, 0, s>>>(in.lines, in.lrad, flags, run_incl, n, out.verts, g.line_entry);
             HRT_CK(cudaGetLastError());
-            boxes_phantom_kernel<<<grid_for(n, T), T, 0, s>>>(g.dq, g.rad_for_boxes, n, boxes);
-            cudaFreeAsync(runpos, s);
-            cudaFreeAsync(runstart, s);
             cudaFreeAsync(flags, s);
+            cudaFreeAsync(run_incl, s);
             cudaFreeAsync(total, s);
-        } else {
-            boxes_phantom_kernel<<<grid_for(n, T), T, 0, s>>>(out.curves, in.lrad, n, boxes);
         }
     } else if (in.type == HRT_BLAS_LSS) {
         if (!out.geom) HRT_CK(cudaMalloc(&out.geom, n * 8 * sizeof(float)));
@@ -1230,7 +1194,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     out.nslots = n;
     const unsigned T = 256;
     out.node_bytes = in.precision == HRT_PRECISION_QUANTISED ? sizeof(NodeQ) : sizeof(NodeF);
-    if (in.type == HRT_BLAS_PHANTOM) out.prim_bytes = in.precision == HRT_PRECISION_QUANTISED ? 32 : 64;
+    if (in.type == HRT_BLAS_PHANTOM) out.prim_bytes = in.precision == HRT_PRECISION_QUANTISED ? 4 : 64;
     else out.prim_bytes = (in.type == HRT_BLAS_LSS || in.type == HRT_BLAS_VOXELS) ? 32 : 80;  // DOTS, mesh: 80
     if (n == 0) return cudaSuccess;
 
@@ -1244,10 +1208,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
             return ge;
         }
     }
-    float* rad_for_boxes = gt.rad_for_boxes;
-    float* dq = gt.dq;
-    uint32_t* chunk_incl = gt.chunk_incl;
-    uint32_t* keys_tmp = gt.keys_tmp;
+    uint32_t* line_entry = gt.line_entry;
 
     // ---- Morton codes + sort ----------------------------------------------------------------
     uint32_t* ob;
@@ -1362,7 +1323,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     }
     HRT_CK(cudaMalloc(&out.prims, n * out.prim_bytes));
     records_kernel<<<grid_for(n, T), T, 0, s>>>(in.type, in.precision, shift, out.prim_ids, n, out.curves, in.lrad,
-                                                in.type == HRT_BLAS_MESH ? in.tris : (in.type == HRT_BLAS_VOXELS ? in.voxels : out.geom), chunk_incl, out.roots,
+                                                in.type == HRT_BLAS_MESH ? in.tris : (in.type == HRT_BLAS_VOXELS ? in.voxels : out.geom), line_entry,
                                                 in.tri_normals, out.prims);
     HRT_CK(cudaGetLastError());
 
@@ -1376,7 +1337,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     if (h_err) { snprintf(msg, msglen, "refit exceeded its depth bound"); return cudaErrorUnknown; }
 
     if (!in.keep_intermediate) {
-        // tracing reads nodes, records, roots and the slot maps; the rest of the
+        // tracing reads nodes, records, the strand vertex stream and the slot maps; the rest of the
         // build's outputs (the other node encoding, primitive boxes, FP32 curves, LSS/DOTS
         // geometry) are kept only for inspection
         void* extra[] = {out.qnodes_aux, out.prim_boxes, out.curves, out.geom};
@@ -1402,12 +1363,12 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
         if (nboxes) cudaFree(nboxes);
     }
     void* tmps[] = {ob, err, sboxes, first, last, pint, pleaf, visits, dpc, nodes_tmp, lvl_a, lvl_b, kids, nk, nint,
-                    nprim, int_off, prim_off, totals, porder, dq, rad_for_boxes, chunk_incl, keys_tmp};
+                    nprim, int_off, prim_off, totals, porder, line_entry};
     for (void* p : tmps)
         if (p) cudaFreeAsync(p, s);
     HRT_CK(cudaStreamSynchronize(s));
     // n references: records, slot map, partner map; in.n segments: curves and LSS/DOTS geometry
-    out.device_bytes = out.nnodes * out.node_bytes + n * out.prim_bytes + out.nroots * 16 + n * 4 + (shift ? n * 4 : 0);
+    out.device_bytes = out.nnodes * out.node_bytes + n * out.prim_bytes + out.nverts * 16 + n * 4 + (shift ? n * 4 : 0);
     if (in.keep_intermediate)
         out.device_bytes += n * 24 + (out.curves ? in.n * 48 : 0) +
                             (out.geom ? in.n * (in.type == HRT_BLAS_LSS ? 32 : 72) : 0) +
@@ -1507,8 +1468,8 @@ cudaError_t refit_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     }
     if (e == cudaSuccess) {
         records_kernel<<<grid_for(nslots, T), T, 0, s>>>(in.type, in.precision, shift, out.prim_ids, nslots, out.curves, in.lrad,
-                                                    in.type == HRT_BLAS_MESH ? in.tris : out.geom, gt.chunk_incl,
-                                                    out.roots, in.tri_normals, out.prims);
+                                                    in.type == HRT_BLAS_MESH ? in.tris : out.geom, gt.line_entry,
+                                                    in.tri_normals, out.prims);
         e = cudaGetLastError();
     }
     float hb[6];

@@ -50,12 +50,13 @@ static_assert(sizeof(NodeQ) == 80, "NodeQ layout");
 
 // ---- primitive records (leaf slot order) ----------------------------------------------------
 // Phantom FP32 (64 B): {start, r0} {cp1, r1} {cp2, id} {end, 0}
-// Phantom FP16 (32 B): 12 halves = control points minus the chunk root, halves r0 r1,
-//                      uint32 key = chunk << 8 | segment-in-chunk; roots[chunk] = {xyz, first id}
+// Phantom quantised (4 B): the segment's first entry e in the strand vertex stream (float4
+//                      {x, y, z, radius} per entry): entries e .. e + 3 are the GenerateCurves
+//                      neighbours p0, p1, p2, p3, from which the leaf rebuilds the control points
+//                      exactly; the id comes from the slot map
 // LSS (32 B): {p0, r0} {p1, r1}; id from prim_ids
 // DOTS (80 B): start, end, s*r0, t*r0, s*r1, t*r1 (18 floats), id, pad
 struct alignas(16) PrimPhantomF { float4 a, b, c, d; };
-struct alignas(16) PrimPhantomH { uint4 q0, q1; };
 struct alignas(16) PrimLss { float4 a, b; };
 struct alignas(16) PrimDots { float4 a, b, c, d, e; };
 // Mesh triangle (80 B): {v0, id} {v1, n0.x} {v2, n0.y} {n0.z, n1} {n2, has normals (0/1 bits)}
@@ -71,7 +72,7 @@ inline constexpr uint32_t ref_shift(int type) { return (type == HRT_BLAS_LSS || 
 struct DevBlas {
     const void* nodes;        // NodeF or NodeQ
     const void* prims;        // records in slot order
-    const float4* roots;      // quantised Phantom chunk roots
+    const float4* verts;      // quantised Phantom: the strand vertex stream
     const uint32_t* prim_ids; // slot -> reference id (segment index << ref_shift | half)
     const uint32_t* partner;  // slot -> the slot of the same segment's other reference (LSS, DOTS)
     uint32_t type, precision, nprims, nnodes, ref_shift;
@@ -156,7 +157,6 @@ struct PrimVoxel {
 };
 struct BuildInput {
     int type, precision, max_leaf;
-    uint32_t quant_chunk;
     const float* lines;   // device, n x 6
     const float* lrad;    // device, n x 2 (per line end)
     uint64_t n;
@@ -175,7 +175,7 @@ struct BuildOutput {
     void* nodes = nullptr;        // NodeF or NodeQ (per precision)
     void* qnodes_aux = nullptr;   // NodeQ copy when nodes are NodeF (inspection) or vice versa
     void* prims = nullptr;
-    float4* roots = nullptr;
+    float4* verts = nullptr;      // quantised Phantom strand vertex stream
     uint32_t* prim_ids = nullptr;  // slot -> reference id
     uint32_t* partner = nullptr;   // slot -> partner slot (two references per segment only)
     float* prim_boxes = nullptr;  // nslots x 6, reference order
@@ -187,7 +187,7 @@ struct BuildOutput {
     uint32_t* bin_right = nullptr;
     float* bin_boxes = nullptr;
     uint32_t* prim_order = nullptr;
-    uint64_t nnodes = 0, nroots = 0, node_bytes = 0, prim_bytes = 0, device_bytes = 0;
+    uint64_t nnodes = 0, nverts = 0, node_bytes = 0, prim_bytes = 0, device_bytes = 0;
     uint64_t nslots = 0;  // BVH references = leaf slots = records
     float bounds[6] = {0, 0, 0, 0, 0, 0};
     std::vector<uint32_t> level_start;  // first node of each breadth-first level, then nnodes

@@ -488,28 +488,27 @@ struct RayState {
 struct Stats { uint32_t nodes, prims, r64, h64, need64; };
 
 // ---------------------------------------------------------------- leaves
+// The control points and radii of the Phantom segment in leaf slot `slot`. FP32 records hold
+// them (and the id); the quantised format rebuilds them from the strand vertex stream with the
+// operations of the curve kernel (GenerateCurves, tension 1: cp1 = p1 + (p2 - p0) / 6,
+// cp2 = p2 - (p3 - p1) / 6, each operation rounded separately), so they equal the FP32 curves bit
+// for bit, and its id is read from the slot map when a hit needs it (phantom_id).
 __device__ __forceinline__ void load_phantom(const DevBlas& B, uint32_t slot, V3<float>* P, float* r0, float* r1,
                                              uint32_t* id) {
     if (B.precision == HRT_PRECISION_QUANTISED) {
-        const PrimPhantomH* pr = static_cast<const PrimPhantomH*>(B.prims) + slot;
-        uint4 q0 = __ldg(&pr->q0), q1 = __ldg(&pr->q1);
-        uint32_t key = q1.w;
-        float4 rt = __ldg(&B.roots[key >> 8]);
-        uint32_t w[7] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z};
-        float h[14];
-#pragma unroll
-        for (int j = 0; j < 7; ++j) {
-            __half2 hh = *reinterpret_cast<const __half2*>(&w[j]);
-            float2 f = __half22float2(hh);
-            h[2 * j] = f.x;
-            h[2 * j + 1] = f.y;
-        }
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            P[k] = mk(__fadd_rn(rt.x, h[3 * k]), __fadd_rn(rt.y, h[3 * k + 1]), __fadd_rn(rt.z, h[3 * k + 2]));
-        *r0 = h[12];
-        *r1 = h[13];
-        *id = __float_as_uint(rt.w) + (key & 0xffu);
+        const uint32_t e = __ldg(static_cast<const uint32_t*>(B.prims) + slot);
+        const float4 v0 = __ldg(B.verts + e), v1 = __ldg(B.verts + e + 1), v2 = __ldg(B.verts + e + 2),
+                     v3 = __ldg(B.verts + e + 3);
+        const float k = 1.0f / 6.0f;
+        P[0] = mk(v1.x, v1.y, v1.z);
+        P[1] = mk(__fadd_rn(v1.x, __fmul_rn(__fsub_rn(v2.x, v0.x), k)), __fadd_rn(v1.y, __fmul_rn(__fsub_rn(v2.y, v0.y), k)),
+                  __fadd_rn(v1.z, __fmul_rn(__fsub_rn(v2.z, v0.z), k)));
+        P[2] = mk(__fsub_rn(v2.x, __fmul_rn(__fsub_rn(v3.x, v1.x), k)), __fsub_rn(v2.y, __fmul_rn(__fsub_rn(v3.y, v1.y), k)),
+                  __fsub_rn(v2.z, __fmul_rn(__fsub_rn(v3.z, v1.z), k)));
+        P[3] = mk(v2.x, v2.y, v2.z);
+        *r0 = v1.w;
+        *r1 = v2.w;
+        *id = 0xffffffffu;
     } else {
         const PrimPhantomF* pr = static_cast<const PrimPhantomF*>(B.prims) + slot;
         float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c), d = __ldg(&pr->d);
@@ -521,6 +520,10 @@ __device__ __forceinline__ void load_phantom(const DevBlas& B, uint32_t slot, V3
         *r1 = b.w;
         *id = __float_as_uint(c.w);
     }
+}
+// The reported id of the Phantom segment in `slot` (id_rec: what load_phantom returned).
+__device__ __forceinline__ uint32_t phantom_id(const DevBlas& B, uint32_t slot, uint32_t id_rec) {
+    return B.precision == HRT_PRECISION_QUANTISED ? __ldg(&B.prim_ids[slot]) : id_rec;
 }
 
 // Tests one leaf slot; returns true if it produced an accepted hit. kType is the primitive
@@ -539,7 +542,7 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         load_phantom(B, slot, P, &r0, &r1, &id);
         PrhiOut<float> r = prhi(R.F, R.o, R.d, P, r0, r1);
         if (r.status == kHit) {
-            if (r.s >= R.tmin && beats(r.s, inst, id, h)) {
+            if (r.s >= R.tmin && r.s <= h.t && beats(r.s, inst, id = phantom_id(B, slot, id), h)) {
                 h = Hit{r.s, id, inst, slot, r.tc, r.ts, r.sl, 0u};
                 return true;
             }
@@ -555,7 +558,7 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
             if (s64 > 0.0) {
                 ++st.h64;
                 float s = float(s64);
-                if (s >= R.tmin && beats(s, inst, id, h)) {
+                if (s >= R.tmin && s <= h.t && beats(s, inst, id = phantom_id(B, slot, id), h)) {
                     h = Hit{s, id, inst, slot, float(tc64), float(ts64), float(s64 - double(float(ts64))), HRT_HIT_FP64};
                     return true;
                 }
