@@ -4,25 +4,30 @@
 Default workload (c5_batched): 16 seeded hair models (strands log-uniform in [2,000, 200,000],
 16-128 vertices, Phantom / LSS / DOTS in turn, 47.9 M segments in all), each with its own camera,
 resolution (256x256 .. 1920x1080) and 1-4 jittered samples per pixel, Shade() plus one shadow ray
-per hit. Quantised BLASes (8-bit BVH8 boxes; Phantom segments rebuilt from the strand vertex
-stream), all scenes in one
-CUDA-graph replay of the persistent trace kernel with autotuned settings. A step is one replay.
-`value` counts primary + shadow rays per second with the BVHs resident in HBM (several GB, far
-above the 129 MB L2, so no flush between steps); `plain_fp32` is the same scenes as 16
-sequential launches of the FP32 tracer; `e2e` goes through the C ABI per step (cameras in,
-every framebuffer copied to pinned host memory). `--config c4_phantom_quantised` is the single
-Phantom precision-pattern frame (19.05 M segments, 1920x1080 x 4 spp) next to its FP32 build.
+per hit. Quantised BLASes (8-bit BVH8 boxes; Phantom segments as indices into the strand vertex
+stream), all scenes in one CUDA-graph replay of the persistent trace kernels with autotuned
+settings. A step is one replay. `value` counts primary + shadow rays per second with the BVHs
+resident in HBM (several GB, far above the 129 MB L2, so no flush between steps).
+
+The line also carries, for the same scenes: `plain_fp32` (16 sequential launches of the FP32
+tracer, the comparison the metric names), `sequential_quantised`, `batched_fp32`; `agreement`
+(the timed graph's framebuffers and hit records of the same graph against the FP64 CPU oracle on
+65,536 sampled rays, on the original FP32 strands); `e2e` through the C ABI (cameras in, every
+framebuffer to pinned host memory); `cpu_baseline` (the oracle's FP32 tracer on every pixel, and
+its FP64 tracer on a row sample); and `configs`: C1-C4 (Phantom FP32 512x512, LSS and DOTS
+1920x1080, the 19.05 M-segment Phantom frame at 4 spp), each with both precisions, agreement and
+roofline. Per-scene details go to stderr.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
 
-Under torchrun (N > 1) every rank renders its own full frame (replicas, weak scaling); rank 0
-prints one JSON line. `--impl reference` times the CPU restatement of the reference's trace
-path (oracle/, FP32, all host threads) on bounded samples of the same workload.
+Under torchrun (N > 1) every rank renders the full workload (replicas, weak scaling); rank 0
+prints the line. `--impl reference` times the CPU restatement of the reference's trace path
+(oracle/, FP32, all host threads; the oracle library alone, which also carries the workload
+generator) on one band of image rows of every scene per step.
 """
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
 import os
 import statistics
@@ -35,6 +40,7 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))  # hairscene: oracle scenes and hit comparison (the checker)
 
 METRIC = "Mrays/s on 1 GB300: quantized/batched vs plain FP32 at >=99.99% hit agreement"
 L2_BYTES = 129 * 1024 * 1024
@@ -42,12 +48,12 @@ PRECISION_DESC = ("quantised (8-bit BVH8 boxes; Phantom segments as 4-byte indic
                   "control points rebuilt from the FP32 vertices in the leaf)")
 DTYPE_DESC = "fp32 (8-bit node boxes)"
 ORACLE_DESC = "FP64 CPU restatement on the original FP32 strands"
-
-
-def prim_test_bytes(info, gtype: int, precision: int) -> int:
-    """Bytes one primitive test reads: the record, and for quantised Phantom the four 16-byte
-    stream entries it indexes."""
-    return int(info["prim_bytes"]) + (64 if gtype == 0 and precision == 1 else 0)
+DATA_DESC = "synthetic: seeded strands (the reference's glTF hair assets are not available)"
+BATCH_CONFIG = "c5_batched"
+SINGLE_CONFIGS = ("c1_phantom_fp32", "c2_lss_fp32", "c3_dots_fp32", "c4_phantom_quantised")
+AGREE_RAYS = 65536
+ROW_BANDS = 4       # CPU legs: a step renders one of every ROW_BANDS image rows (scanline order)
+FP64_BANDS = 16     # the FP64 CPU figure: one of every FP64_BANDS rows
 
 
 def env_int(name, default):
@@ -150,6 +156,13 @@ def load_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+def prim_test_bytes(info, gtype: int, precision: int) -> int:
+    """Bytes one primitive test reads: the record, and for quantised Phantom the four 16-byte
+    stream entries it indexes."""
+    return int(info["prim_bytes"]) + (64 if gtype == 0 and precision == 1 else 0)
+
+
+# ------------------------------------------------------------------------------ workload helpers
 _OVERRIDE = {}
 
 
@@ -162,6 +175,13 @@ def workload(name: str):
     return cfg, sp
 
 
+def oracle_lib():
+    """The CPU oracle's library with the workload generator's symbols declared."""
+    import vkhrt_gb300 as H
+    from hairscene import load_oracle
+    return H.bind_workload(load_oracle())
+
+
 def uniform_lines(v, r, ns, nv):
     vv = v.reshape(ns, nv, 3)
     rr = r.reshape(ns, nv)
@@ -170,15 +190,13 @@ def uniform_lines(v, r, ns, nv):
     return lines, lrad
 
 
-def oracle_scene(cfg, v, r, precision):
-    """CPU oracle scene for the workload (the checker and the CPU baseline)."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from hairscene import OracleScene, load_oracle, oracle_geometry
-    orc = load_oracle()
-    lines, lrad = uniform_lines(v, r, cfg["nstrands"], cfg["nverts"])
-    data, rad = oracle_geometry(orc, int(cfg["type"]), lines, lrad, quantised=(precision == 1 and int(cfg["type"]) == 0))
+def oracle_scene(orc, gtype: int, v, r, ns: int, nv: int):
+    """The oracle's scene of one hair model: its own geometry processing of the FP32 strands."""
+    from hairscene import OracleScene, oracle_geometry
+    lines, lrad = uniform_lines(v, r, ns, nv)
+    data, rad = oracle_geometry(orc, gtype, lines, lrad)
     del lines, lrad
-    return OracleScene(orc, [(int(cfg["type"]), data, rad)]), orc
+    return OracleScene(orc, [(gtype, data, rad)])
 
 
 def sample_pixels(w, h, n, seed=7):
@@ -186,118 +204,56 @@ def sample_pixels(w, h, n, seed=7):
     return np.sort(rng.choice(w * h, size=min(n, w * h), replace=False)).astype(np.uint32)
 
 
-def cpu_sample_rate(osc, cam_arrays, cfg, precision, target_s=12.0, threads=0):
-    """Rays/s of the oracle on a growing pixel sample until ~target_s of work; returns (Mrays/s, desc)."""
-    vi, pi = cam_arrays
-    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
-    npx = 512
-    while True:
-        px = sample_pixels(w, h, npx, seed=npx)
-        t0 = time.perf_counter()
-        o = osc.render(vi, pi, w, h, spp=spp, jitter=1 if spp > 1 else 0, seed=17, shading=2, precision=precision,
-                       pixel_list=px, threads=threads)
-        dt = time.perf_counter() - t0
-        rays = len(px) * spp + int((o["t"] >= 0).sum())
-        if dt >= target_s or npx >= w * h:
-            return rays / dt / 1e6, f"{len(px)} random pixels x {spp} spp (+{int((o['t'] >= 0).sum())} shadow rays)", dt
-        npx = min(w * h, int(npx * max(2.0, min(8.0, target_s / max(dt, 1e-3)))))
+def row_band(w: int, h: int, k: int, nbands: int) -> np.ndarray:
+    """Pixels of the rows y = k (mod nbands), in scanline order."""
+    ys = np.arange(k % nbands, h, nbands, dtype=np.uint32)
+    return (ys[:, None] * np.uint32(w) + np.arange(w, dtype=np.uint32)[None, :]).reshape(-1)
 
 
-def run_reference(args, dist):
-    """CPU restatement of the reference's trace path (FP32 Prhi, all host threads)."""
-    if dist.rank != 0:
-        return
-    if args.config == BATCH_CONFIG:
-        return run_reference_batched(args)
+def compare_frame(rgba, hits, o, px, spp):
+    """GPU hit records and pixels against the oracle's render of the pixels `px` (all samples)."""
     import vkhrt_gb300 as H
-    cfg, sp = workload(args.config)
-    v, r, off = H.generate_strands(sp)
-    osc, orc = oracle_scene(cfg, v, r, int(cfg["precision"]))
-    cam = H.scene_camera(cfg["width"], cfg["height"])
-    vi, pi = H.camera_arrays(cam)
-    threads = orc.orc_hardware_threads()
-    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
-    npx = args.ref_pixels
-    rates = []
-    total_t = 0.0
-    total_rays = 0
-    for step in range(args.warmup + args.steps):
-        px = sample_pixels(w, h, npx, seed=1000 + step)
-        t0 = time.perf_counter()
-        o = osc.render(vi, pi, w, h, spp=spp, jitter=1 if spp > 1 else 0, seed=17, shading=2, precision=32,
-                       pixel_list=px, threads=threads)
-        dt = time.perf_counter() - t0
-        rays = len(px) * spp + int((o["t"] >= 0).sum())
-        if step >= args.warmup:
-            total_t += dt
-            total_rays += rays
-            rates.append(rays / dt / 1e6)
-    value = total_rays / total_t / 1e6
-    sample = f"{npx} random pixels x {spp} spp per step (+ shadow rays)"
-    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_t / max(args.steps, 1), 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
-            "config": config_block(cfg, args.config),
-            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                             "sample": sample},
-            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    from hairscene import compare_hits
+    gh = hits.reshape(-1, spp)[px].reshape(-1)
+    g_t = np.where(gh["t"] >= 0, gh["t"].astype(np.float64), -1.0)
+    cmp = compare_hits(g_t, gh["prim"], gh["inst"], o["t"], o["prim"], o["inst"])
+    same = (gh["prim"] == o["prim"]) & (((gh["flags"] & H.HIT_SHADOWED) != 0) == (o["shadow"] != 0))
+    ok_px = same.reshape(-1, spp).all(axis=1)
+    dpx = np.abs(rgba.reshape(-1, 4)[px] - o["fb"]).max(axis=1)
+    return {"rays": int(cmp["n"]), "hits": int(cmp["hits"]), "mismatches": int(cmp["mismatches"]),
+            "ties": int(cmp["ties"]), "max_rel_t": float(cmp["max_rel_t"]), "p9999_rel_t": float(cmp["p9999_rel_t"]),
+            "pixels": int(len(px)), "pixels_agreeing": int(ok_px.sum()),
+            "max_rgb": float(dpx[ok_px].max()) if ok_px.any() else 0.0,
+            "rgb_over_1e-4": int((dpx[ok_px] > 1e-4).sum())}
 
 
-def run_reference_batched(args):
-    """The oracle's FP32 tracer over every scene of the batched workload, a bounded pixel sample of
-    each scene per step (all host threads)."""
-    import vkhrt_gb300 as H
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from hairscene import OracleScene, load_oracle, oracle_geometry
-    orc = load_oracle()
-    threads = orc.orc_hardware_threads()
-    models = batch_models(args)
-    scenes = []
-    for m, v, r, off in models:
-        lines, lrad = uniform_lines(v, r, m["nstrands"], m["nverts"])
-        data, rad = oracle_geometry(orc, int(m["type"]), lines, lrad, quantised=(int(m["type"]) == 0))
-        cam = H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"])
-        scenes.append((m, OracleScene(orc, [(int(m["type"]), data, rad)]), H.camera_arrays(cam)))
-    # per step the same fraction of every scene's pixels (all their samples), so the rate is that
-    # of the whole workload; 1/8 of the workload per step
-    frac = 0.125
-    total_t = 0.0
-    total_rays = 0
-    for step in range(args.warmup + args.steps):
-        for m, osc, (vi, pi) in scenes:
-            w, h, spp = m["width"], m["height"], m["spp"]
-            px = sample_pixels(w, h, int(w * h * frac), seed=1000 + step)
+def merge_compare(parts):
+    n = sum(p["rays"] for p in parts)
+    ties = sum(p["ties"] for p in parts)
+    mis = sum(p["mismatches"] for p in parts)
+    return {"rays": n, "hit_id": round(1.0 - mis / max(n - ties, 1), 6), "mismatches": mis, "ties": ties,
+            "max_rel_t": max((p["max_rel_t"] for p in parts), default=0.0),
+            "max_rgb_err_agreeing": max((p["max_rgb"] for p in parts), default=0.0),
+            "pixels_rgb_over_1e-4": sum(p["rgb_over_1e-4"] for p in parts),
+            "pixels_agreeing": round(sum(p["pixels_agreeing"] for p in parts) /
+                                     max(sum(p["pixels"] for p in parts), 1), 6)}
+
+
+def cpu_rate(scenes, precision: int, bands, nbands: int, threads: int, jitter: int):
+    """The oracle's tracer over the given row bands of every scene: (Mrays/s, rays, pixels, seconds).
+    scenes: (oracle scene, view_inv, proj_inv, width, height, spp)."""
+    rays = px_n = 0
+    secs = 0.0
+    for osc, vi, pi, w, h, spp in scenes:
+        for k in bands:
+            px = row_band(w, h, k, nbands)
             t0 = time.perf_counter()
-            o = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=px,
-                           threads=threads)
-            dt = time.perf_counter() - t0
-            if step >= args.warmup:
-                total_t += dt
-                total_rays += len(px) * spp + int((o["t"] >= 0).sum())
-    value = total_rays / total_t / 1e6
-    sample = (f"{pixel_share(frac)} of each of the {len(models)} scenes (all their samples, + shadow rays) per "
-              f"step: the workload's mix")
-    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_t / max(args.steps, 1), 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
-            "config": batch_config_block(models),
-            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                             "sample": sample},
-            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-
-
-def config_block(cfg, name):
-    nseg = cfg["nstrands"] * (cfg["nverts"] - 1)
-    return {"workload": f"{name}: {cfg['nstrands']} strands x {cfg['nverts']} vertices = {nseg} "
-                        f"{'Bezier' if int(cfg['type']) == 0 else 'LSS' if int(cfg['type']) == 1 else 'DOTS'} segments, "
-                        f"{cfg['width']}x{cfg['height']} x {cfg['spp']} spp, Shade + 1 shadow ray",
-            "segments": nseg, "image": f"{cfg['width']}x{cfg['height']}", "spp": cfg["spp"],
-            "precision": PRECISION_DESC if int(cfg["precision"]) else "fp32",
-            "l2": "inputs larger than L2 (BVH + primitives resident, no flush)", "parallelism": "replicas"}
+            o = osc.render(vi, pi, w, h, spp=spp, jitter=jitter, seed=17, shading=2, precision=precision,
+                           pixel_list=px, threads=threads)
+            secs += time.perf_counter() - t0
+            rays += len(px) * spp + int((o["t"] >= 0).sum())
+            px_n += len(px)
+    return rays / secs / 1e6, rays, px_n, secs
 
 
 def time_frames(ctx, tlas, cam, frame, params, steps, warmup):
@@ -316,135 +272,135 @@ def time_frames(ctx, tlas, cam, frame, params, steps, warmup):
     return e0.elapsed_time(e1) / steps
 
 
-def run_ours(args, dist):
-    import torch
-    import vkhrt_gb300 as H
-    dev = dist.local
-    torch.cuda.set_device(dev)
-    ctx = H.Context(dev)
-    cfg, sp = workload(args.config)
-    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
-    t_gen = time.perf_counter()
-    v, r, off = H.generate_strands(sp)
-    t_gen = time.perf_counter() - t_gen
-    # ---- build (untimed for `value`; reported) ----
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    blas = H.BottomLevelAccelerationStructure(
-        H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=cfg["precision"],
-                    max_leaf=args.max_leaf), ctx)
-    tlas = H.TopLevelAccelerationStructure([blas], ctx)
-    build_wall = time.perf_counter() - t0
-    cam = H.scene_camera(w, h)
-    frame = H.Frame(ctx, w, h, spp, with_hits=True)
-    params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, kernel_variant=args.variant, refill=args.refill, speculative=args.speculative, leaf_again=args.leaf_again, **{"async": 1})
-    # rays per step (deterministic: fixed camera, jitter seed)
-    H.trace(ctx, tlas, cam, frame, H.trace_params(spp=spp, jitter=1, seed=17, shading=2, count_stats=1,
-                                                  kernel_variant=args.variant, refill=args.refill, speculative=args.speculative, leaf_again=args.leaf_again))
-    st = frame.stats()
-    rays_per_step = st["primary_rays"] + st["shadow_rays"]
-    # ---- timed region ----
-    dist.barrier()
-    clocks = Clocks(dev)
-    clocks.start()
-    ms = time_frames(ctx, tlas, cam, frame, params, args.steps, args.warmup)
-    clk = clocks.stop()
-    ms_max = dist.max(ms)
-    value = dist.world * rays_per_step / (ms_max * 1e-3) / 1e6
+def jitter_of(spp: int) -> int:
+    """The batched scenes jitter every sample; single configurations jitter only with several
+    samples per pixel (one sample at the pixel centre, as ray_gen.rgen)."""
+    return 1 if spp > 1 else 0
+
+
+# ------------------------------------------------------------------------------ reference arm
+def run_reference(args, dist):
+    """CPU restatement of the reference's trace path (FP32 Prhi / LSS / DOTS, all host threads),
+    loading only the oracle's library (which carries the workload generator too): step s renders
+    the rows y = s (mod 4) of every scene, all samples plus shadow rays, in scanline order."""
     if dist.rank != 0:
-        dist.close()
         return
-    info = blas.info
-    # ---- roofline: algorithmic bytes per launch / launch time ----
-    node_b = info["node_bytes"]
-    prim_b = prim_test_bytes(info, int(cfg["type"]), int(cfg["precision"]))
-    alg_bytes = st["nodes_visited"] * node_b + st["prims_tested"] * prim_b + w * h * 16
-    peak, peak_kind = load_peaks()
-    achieved = alg_bytes / (ms * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
-                "bytes_per_launch": int(alg_bytes), "nodes_visited": int(st["nodes_visited"]),
-                "prims_tested": int(st["prims_tested"]), "node_bytes": int(node_b), "prim_bytes": int(prim_b)}
-    tot = st["warp_cycles_node"] + st["warp_cycles_leaf"] + st["warp_cycles_other"]
-    phase = {k: round(st["warp_cycles_" + k] / tot, 4) for k in ("node", "leaf", "other")} if tot else None
-    if args.profile:
-        print(json.dumps({"profile": True, "ms_per_step": round(ms, 3), "rays_per_step": int(rays_per_step),
-                          "value": round(value, 3), "roofline": roofline, "phase_share": phase}), flush=True)
-        dist.close()
-        return
-    # ---- e2e: C ABI per frame, camera in, framebuffer to pinned host memory ----
-    lib = ctx.lib
-    pinned = torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True)
-    sync_params = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, kernel_variant=args.variant, refill=args.refill, speculative=args.speculative, leaf_again=args.leaf_again)
-    for _ in range(2):
-        H.trace(ctx, tlas, cam, frame, sync_params)
-        ctx.check(lib.hrt_frame_download(frame.handle, ctypes.c_void_p(pinned.data_ptr()), None, None))
-    torch.cuda.synchronize()
-    te = time.perf_counter()
-    e2e_steps = max(3, args.steps // 2)
-    for _ in range(e2e_steps):
-        H.trace(ctx, tlas, cam, frame, sync_params)
-        ctx.check(lib.hrt_frame_download(frame.handle, ctypes.c_void_p(pinned.data_ptr()), None, None))
-    te = (time.perf_counter() - te) / e2e_steps
-    e2e = {"value": round(rays_per_step / te / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 128,
-           "d2h_bytes_per_step": w * h * 16, "ms_per_step": round(te * 1e3, 3)}
-    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": dist.world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": DTYPE_DESC,
-            "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
-            "config": config_block(cfg, args.config), "rays_per_step": int(rays_per_step),
-            "primary_rays_per_step": int(st["primary_rays"]), "shadow_rays_per_step": int(st["shadow_rays"]),
-            "fp64_resolves_per_step": int(st["fp64_resolves"]), "gpu_launches": args.steps,
-            "roofline": roofline, "phase_share": phase, "e2e": e2e, "clocks": clk,
-            "build": {"blas_build_ms": round(info["build_ms"], 2), "build_wall_s": round(build_wall, 3),
-                      "strand_generation_s": round(t_gen, 3), "nodes": int(info["nnodes"]),
-                      "device_bytes": int(info["device_bytes"])}}
-    # ---- plain FP32 tracer on the same strands (the comparison the metric names) ----
-    if not args.quick and int(cfg["precision"]) == 1:
-        blas32 = H.BottomLevelAccelerationStructure(
-            H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=H.Precision.FP32,
-                        max_leaf=args.max_leaf), ctx)
-        tlas32 = H.TopLevelAccelerationStructure([blas32], ctx)
-        f32 = H.Frame(ctx, w, h, spp, with_hits=False)
-        H.trace(ctx, tlas32, cam, f32, H.trace_params(spp=spp, jitter=1, seed=17, shading=2,
-                                                      kernel_variant=args.variant, refill=args.refill, speculative=args.speculative, leaf_again=args.leaf_again))
-        s32 = f32.stats()
-        ms32 = time_frames(ctx, tlas32, cam, f32, params, args.steps, args.warmup)
-        line["plain_fp32"] = {"value": round((s32["primary_rays"] + s32["shadow_rays"]) / (ms32 * 1e-3) / 1e6, 3),
-                              "ms_per_step": round(ms32, 3), "build_ms": round(blas32.info["build_ms"], 2)}
-        del f32, tlas32, blas32
-    # ---- agreement with the FP64 oracle on 65,536 sampled rays, and the CPU baseline ----
-    if not args.no_cpu:
-        H.trace(ctx, tlas, cam, frame, H.trace_params(spp=spp, jitter=1, seed=17, shading=2, record_hits=1))
-        rgba, hits = frame.download(hits=True)
-        osc, orc = oracle_scene(cfg, v, r, int(cfg["precision"]))
+    import vkhrt_gb300 as H
+    orc = oracle_lib()
+    threads = orc.orc_hardware_threads()
+    if args.config == BATCH_CONFIG:
+        models = [(m, *H.generate_strands(H.StrandParams(seed=m["seed"], nstrands=m["nstrands"], nverts=m["nverts"],
+                                                         r_root=m["r_root"], r_tip=m["r_tip"]), lib=orc))
+                  for m in H.batch_workload()]
+        cams = [H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"], lib=orc) for m, *_ in models]
+        config = batch_config_block([m for m, *_ in models])
+        jit = 1
+    else:
+        cfg, sp = workload(args.config)
+        models = [(cfg, *H.generate_strands(sp, lib=orc))]
+        cams = [H.scene_camera(cfg["width"], cfg["height"], lib=orc)]
+        config = single_config_block(cfg, args.config)
+        jit = jitter_of(cfg["spp"])
+    scenes = []
+    for (m, v, r, off), cam in zip(models, cams):
         vi, pi = H.camera_arrays(cam)
-        px = sample_pixels(w, h, 65536 // spp, seed=3)
-        o = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=64, pixel_list=px)
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
-        from hairscene import compare_hits
-        gh = hits.reshape(h * w, spp)[px].reshape(-1)
-        g_t = np.where(gh["t"] >= 0, gh["t"].astype(np.float64), -1.0)
-        cmp = compare_hits(g_t, gh["prim"], gh["inst"], o["t"], o["prim"], o["inst"])
-        same = (gh["prim"] == o["prim"]) & (((gh["flags"] & H.HIT_SHADOWED) != 0) == (o["shadow"] != 0))
-        ok_px = same.reshape(-1, spp).all(axis=1)
-        dpx = np.abs(rgba.reshape(-1, 4)[px] - o["fb"]).max(axis=1)
-        line["agreement"] = {"rays": int(cmp["n"]), "hit_id": round(cmp["agreement"], 6), "mismatches": cmp["mismatches"],
-                             "ties": cmp["ties"], "max_rel_t": cmp["max_rel_t"], "p9999_rel_t": cmp["p9999_rel_t"],
-                             "pixels_agreeing": round(float(ok_px.mean()), 6),
-                             "max_rgb_err_agreeing": float(dpx[ok_px].max()) if ok_px.any() else None,
-                             "oracle": ORACLE_DESC}
-        rate, desc, secs = cpu_sample_rate(osc, (vi, pi), cfg, 32, target_s=args.cpu_seconds)
-        line["cpu_baseline"] = {"value": round(rate, 4), "unit": "Mrays/s", "cores": orc.orc_hardware_threads(),
-                                "kind": "port", "sample": f"{desc}, FP32 oracle, {secs:.1f} s"}
+        scenes.append((oracle_scene(orc, int(m["type"]), v, r, m["nstrands"], m["nverts"]), vi, pi, m["width"],
+                       m["height"], m["spp"]))
+    del models
+    total_t = 0.0
+    total_rays = 0
+    for step in range(args.warmup + args.steps):
+        _, rays, _, secs = cpu_rate(scenes, 32, [step % ROW_BANDS], ROW_BANDS, threads, jit)
+        if step >= args.warmup:
+            total_t += secs
+            total_rays += rays
+    value = total_rays / total_t / 1e6
+    sample = (f"rows y = s (mod {ROW_BANDS}) of every scene at step s (all samples, + shadow rays, scanline order): "
+              f"every pixel over {ROW_BANDS} steps")
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total_t / max(args.steps, 1), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": DATA_DESC,
+            "config": config,
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
-    dist.close()
 
 
-BATCH_CONFIG = "c5_batched"
+def single_config_block(cfg, name):
+    nseg = cfg["nstrands"] * (cfg["nverts"] - 1)
+    kind = {0: "Bezier", 1: "LSS", 2: "DOTS"}[int(cfg["type"])]
+    return {"workload": f"{name}: {cfg['nstrands']} strands x {cfg['nverts']} vertices = {nseg} {kind} segments, "
+                        f"{cfg['width']}x{cfg['height']} x {cfg['spp']} spp, Shade + 1 shadow ray",
+            "segments": nseg, "image": f"{cfg['width']}x{cfg['height']}", "spp": cfg["spp"],
+            "precision": PRECISION_DESC if int(cfg["precision"]) else "fp32",
+            "l2": "inputs larger than L2 (BVH + primitives resident, no flush)", "parallelism": "replicas"}
 
 
-def batch_models(args):
+def batch_config_block(models):
+    nseg = sum(m["nstrands"] * (m["nverts"] - 1) for m in models)
+    px = sum(m["width"] * m["height"] * m["spp"] for m in models)
+    return {"workload": f"{BATCH_CONFIG}: {len(models)} hair models (strands log-uniform in [2000, 200000], "
+                        f"{{16,32,64,128}} vertices, Phantom/LSS/DOTS in turn), {nseg} segments, own cameras, "
+                        f"256x256..1920x1080 at 1-4 spp ({px} primary samples), Shade + 1 shadow ray",
+            "segments": nseg, "scenes": len(models), "primary_samples": px, "precision": PRECISION_DESC,
+            "l2": "inputs larger than L2 (BVHs + primitives resident, no flush)", "parallelism": "replicas"}
+
+
+# ------------------------------------------------------------------------------ C1-C4 blocks
+def run_config(ctx, name: str, args, orc) -> dict:
+    """One BASELINE configuration at full size: both precisions timed (frames in HBM, K launches
+    between CUDA events), per-sample hit records of each checked against the FP64 oracle on
+    65,536 sampled rays (pixels within 1e-4 where hits agree), and the roofline of the
+    configuration's own precision."""
+    import vkhrt_gb300 as H
+    cfg, sp = workload(name)
+    w, h, spp, gtype = cfg["width"], cfg["height"], cfg["spp"], int(cfg["type"])
+    v, r, off = H.generate_strands(sp)
+    cam = H.scene_camera(w, h)
+    vi, pi = H.camera_arrays(cam)
+    t0 = time.perf_counter()
+    osc = oracle_scene(orc, gtype, v, r, cfg["nstrands"], cfg["nverts"])
+    px = sample_pixels(w, h, AGREE_RAYS // spp, seed=3)
+    o = osc.render(vi, pi, w, h, spp=spp, jitter=jitter_of(spp), seed=17, shading=2, precision=64, pixel_list=px)
+    oracle_s = time.perf_counter() - t0
+    del osc
+    peak, _ = load_peaks()
+    out = {}
+    for prec in (H.Precision.FP32, H.Precision.QUANTISED):
+        blas = H.BottomLevelAccelerationStructure(
+            H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=prec), ctx)
+        tlas = H.TopLevelAccelerationStructure([blas], ctx)
+        fr = H.Frame(ctx, w, h, spp, with_hits=True)
+        base = dict(spp=spp, jitter=jitter_of(spp), seed=17, shading=2)
+        H.trace(ctx, tlas, cam, fr, H.trace_params(count_stats=1, **base))
+        st = fr.stats()
+        ms = time_frames(ctx, tlas, cam, fr, H.trace_params(**base, **{"async": 1}), args.config_steps, 3)
+        H.trace(ctx, tlas, cam, fr, H.trace_params(record_hits=1, **base))
+        rgba, hits = fr.download(hits=True)
+        cmp = compare_frame(rgba, hits, o, px, spp)
+        info = blas.info
+        rays = st["primary_rays"] + st["shadow_rays"]
+        alg = st["nodes_visited"] * info["node_bytes"] + st["prims_tested"] * prim_test_bytes(info, gtype, int(prec)) \
+            + w * h * 16
+        out[int(prec)] = {"value": round(rays / (ms * 1e-3) / 1e6, 1), "ms": round(ms, 3), "rays": int(rays),
+                          "cmp": cmp, "fp64_resolves": int(st["fp64_resolves"]),
+                          "frac": round(alg / (ms * 1e-3) / 1e9 / peak, 3)}
+        del fr, tlas, blas
+    own, other = out[int(cfg["precision"])], out[1 - int(cfg["precision"])]
+
+    def agree(c):
+        return round(1.0 - c["mismatches"] / max(c["rays"] - c["ties"], 1), 6)
+
+    c = own["cmp"]
+    return {"value": own["value"], "fp32": out[0]["value"], "quantised": out[1]["value"], "agree": agree(c),
+            "rays": c["rays"], "mis": c["mismatches"], "ties": c["ties"], "max_rel_t": float(f"{c['max_rel_t']:.2e}"),
+            "max_rgb": float(f"{c['max_rgb']:.2e}"), "rgb_over": c["rgb_over_1e-4"], "fp64": own["fp64_resolves"],
+            "agree_other": agree(other["cmp"]), "hbm_frac": own["frac"], "oracle_s": round(oracle_s, 1)}
+
+
+# ------------------------------------------------------------------------------ batched (default)
+def batch_models():
     """The 16 models of the batched workload, with strands generated (host arrays)."""
     import vkhrt_gb300 as H
     models = []
@@ -456,30 +412,31 @@ def batch_models(args):
     return models
 
 
-def batch_config_block(models):
-    nseg = sum(m["nstrands"] * (m["nverts"] - 1) for m, *_ in models)
-    px = sum(m["width"] * m["height"] * m["spp"] for m, *_ in models)
-    return {"workload": f"{BATCH_CONFIG}: {len(models)} hair models (strands log-uniform in [2000, 200000], "
-                        f"{{16,32,64,128}} vertices, Phantom/LSS/DOTS in turn), {nseg} segments, own cameras, "
-                        f"256x256..1920x1080 at 1-4 spp ({px} primary samples), Shade + 1 shadow ray",
-            "segments": nseg, "scenes": len(models), "primary_samples": px,
-            "precision": PRECISION_DESC,
-            "l2": "inputs larger than L2 (BVHs + primitives resident, no flush)", "parallelism": "replicas"}
+def kernels_per_replay(models, params) -> int:
+    """Our kernel launches in one replay of a batch graph: a frame kernel per group (one group per
+    primitive type when split), plus the FP64 pass and its averaging kernel for the group that
+    holds the Phantom scenes."""
+    types = {int(m["type"]) for m in models}
+    groups = len(types) if params.split_types else 1
+    return groups + (2 if 0 in types and params.fp64_resolve else 0)
 
 
 def run_batched(args, dist):
-    """All scenes in one CUDA-graph launch of the persistent kernel (autotuned) against 16
-    sequential plain FP32 launches and 16 sequential quantised launches of the same scenes."""
+    """All scenes in one CUDA-graph replay of the persistent kernels (autotuned) against 16
+    sequential plain FP32 launches, 16 sequential quantised launches, and the batch on FP32
+    BLASes; then the timed graph's output against the FP64 oracle, the CPU baseline and the
+    single configurations."""
     import torch
     import vkhrt_gb300 as H
     dev = dist.local
     torch.cuda.set_device(dev)
     ctx = H.Context(dev)
     t_gen = time.perf_counter()
-    models = batch_models(args)
+    models = batch_models()
     t_gen = time.perf_counter() - t_gen
+    mlist = [m for m, *_ in models]
 
-    def build(precision):
+    def build(precision, with_hits):
         out = []
         for m, v, r, off in models:
             b = H.BottomLevelAccelerationStructure(
@@ -487,40 +444,36 @@ def run_batched(args, dist):
                             max_leaf=args.max_leaf), ctx)
             t = H.TopLevelAccelerationStructure([b], ctx)
             cam = H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"])
-            out.append((b, t, cam, H.Frame(ctx, m["width"], m["height"], m["spp"], with_hits=not args.no_cpu)))
+            out.append((b, t, cam, H.Frame(ctx, m["width"], m["height"], m["spp"], with_hits=with_hits)))
         return out
 
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    q = build(H.Precision.QUANTISED)
+    q = build(H.Precision.QUANTISED, not args.no_cpu)
     build_wall = time.perf_counter() - t0
-    f = build(H.Precision.FP32)
+    f = build(H.Precision.FP32, False)
     base = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1})
     # ---- per-scene work counts (sequential, counted): rays and algorithmic bytes ----
     rays_per_step = 0
-    alg_bytes = 0
     per_scene = []
-    for (b, t, cam, fr), (m, *_r) in zip(q, models):
+    for (b, t, cam, fr), m in zip(q, mlist):
         H.trace(ctx, t, cam, fr, H.trace_params(jitter=1, seed=17, shading=2, count_stats=1))
         st = fr.stats()
         info = b.info
-        prim_b = prim_test_bytes(info, int(m["type"]), 1)
         rays = st["primary_rays"] + st["shadow_rays"]
         rays_per_step += rays
-        alg_bytes += st["nodes_visited"] * info["node_bytes"] + st["prims_tested"] * prim_b + \
-            m["width"] * m["height"] * 16
+        alg = st["nodes_visited"] * info["node_bytes"] + st["prims_tested"] * prim_test_bytes(info, int(m["type"]), 1) \
+            + m["width"] * m["height"] * 16
         per_scene.append({"type": m["type"].name[1:], "segments": m["nstrands"] * (m["nverts"] - 1),
-                          "image": f"{m['width']}x{m['height']}", "spp": m["spp"], "rays": int(rays)})
+                          "image": f"{m['width']}x{m['height']}", "spp": m["spp"], "rays": int(rays),
+                          "alg_bytes": int(alg), "fp64_resolves": int(st["fp64_resolves"])})
     # ---- autotune the batch (untimed) ----
     scenes_q = [(t, cam, fr) for (_, t, cam, fr) in q]
     tuned, tune_ms = H.autotune(ctx, scenes_q, base, reps=2, cache=args.tune_cache, key=f"{BATCH_CONFIG}/quantised")
     batch = H.Batch(ctx, scenes_q, tuned)
-    dist.barrier()
-    clocks = Clocks(dev)
-    clocks.start()
-    cams = [cam for (_, _, cam, _) in q]
+    cams_all = [cam for (_, _, cam, _) in q]
 
-    def paced(b, nsteps):
+    def paced(b, nsteps, cams):
         # A step renders every scene from its cameras (their 3 KB scene-table upload starts the
         # step, as in an interactive renderer) and ends when the replay has finished, as the
         # sequential comparison's steps do. Replays queued back to back without this pacing ran
@@ -530,18 +483,27 @@ def run_batched(args, dist):
             b.launch()
             torch.cuda.current_stream().synchronize()
 
-    paced(batch, args.warmup)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    paced(batch, args.steps)
-    e1.record()
-    torch.cuda.synchronize()
+    def timed(b, nsteps, cams):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        paced(b, nsteps, cams)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / nsteps
+
+    dist.barrier()
+    paced(batch, args.warmup, cams_all)
+    clocks = Clocks(dev)
+    clocks.start()
+    ms = timed(batch, args.steps, cams_all)
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
     ms_max = dist.max(ms)
     value = dist.world * rays_per_step / (ms_max * 1e-3) / 1e6
+    # the timed replay's framebuffers, checked below against the oracle
+    fb_timed = [np.zeros((m["height"], m["width"], 4), np.float32) for m in mlist]
+    batch.download(fb_timed)
 
     def sequential(sc, params):
         """Mean over steps of the sum of per-scene launch times (each launch bracketed by events)."""
@@ -573,20 +535,31 @@ def run_batched(args, dist):
     scenes_f = [(t, cam, fr) for (_, t, cam, fr) in f]
     tuned_f, _ = H.autotune(ctx, scenes_f, base, reps=2, cache=args.tune_cache, key=f"{BATCH_CONFIG}/fp32")
     batch_f = H.Batch(ctx, scenes_f, tuned_f)
-    paced(batch_f, args.warmup)
-    torch.cuda.synchronize()
-    e0.record()
-    paced(batch_f, args.steps)
-    e1.record()
-    torch.cuda.synchronize()
-    ms_bf = e0.elapsed_time(e1) / args.steps
+    paced(batch_f, args.warmup, cams_all)
+    ms_bf = timed(batch_f, args.steps, cams_all)
     mem_q = sum(int(b.info["device_bytes"]) for (b, *_r) in q)
     mem_f = sum(int(b.info["device_bytes"]) for (b, *_r) in f)
+    del batch_f, scenes_f, f
+    # ---- the dominant kernel alone, for the roofline: the quantised Phantom scenes as one batch
+    # (the Phantom group's frame launch and its FP64 pass) ----
+    ph = [i for i, m in enumerate(mlist) if int(m["type"]) == 0]
+    batch_ph = H.Batch(ctx, [scenes_q[i] for i in ph], tuned)
+    cams_ph = [cams_all[i] for i in ph]
+    paced(batch_ph, args.warmup, cams_ph)
+    ms_ph = timed(batch_ph, args.steps, cams_ph)
+    del batch_ph
     if dist.rank != 0:
         dist.close()
         return
     peak, peak_kind = load_peaks()
-    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    ph_bytes = sum(per_scene[i]["alg_bytes"] for i in ph)
+    ph_rays = sum(per_scene[i]["rays"] for i in ph)
+    achieved = ph_bytes / (ms_ph * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "kernel": "frame_kernel<8-bit nodes, Phantom>: the Phantom group of the batch, timed alone",
+                "bytes_per_launch": int(ph_bytes), "launch_ms": round(ms_ph, 3), "rays_per_launch": int(ph_rays)}
+    roofline.update(measured_bounds(ph_rays, ms_ph, clk))
     for d, a, b2 in zip(per_scene, lat_f32, lat_q):
         d["plain_fp32_ms"] = round(float(a), 3)
         d["quantised_ms"] = round(float(b2), 3)
@@ -595,9 +568,9 @@ def run_batched(args, dist):
     # (the renders themselves stay in order: each waits for the previous one) ----
     tparams = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1},
                              **{k: getattr(tuned, k) for k in H.TUNED_FIELDS})
-    fsets = [[fr for (_, _, _, fr) in q], [H.Frame(ctx, m["width"], m["height"], m["spp"]) for m, *_ in models]]
+    fsets = [[fr for (_, _, _, fr) in q], [H.Frame(ctx, m["width"], m["height"], m["spp"]) for m in mlist]]
     e2e_batches = [H.Batch(ctx, [(t, cam, fr) for (_, t, cam, _), fr in zip(q, fs)], tparams) for fs in fsets]
-    pins = [[torch.empty((m["height"], m["width"], 4), dtype=torch.float32, pin_memory=True) for m, *_ in models]
+    pins = [[torch.empty((m["height"], m["width"], 4), dtype=torch.float32, pin_memory=True) for m in mlist]
             for _ in range(2)]
     streams = [torch.cuda.Stream(), torch.cuda.Stream()]
     rendered = [torch.cuda.Event(), torch.cuda.Event()]
@@ -609,7 +582,7 @@ def run_batched(args, dist):
             st, b = streams[j], e2e_batches[j]
             if prev is not None:
                 st.wait_event(prev)
-            b.set_cameras(cams, stream=st.cuda_stream)
+            b.set_cameras(cams_all, stream=st.cuda_stream)
             b.launch(stream=st.cuda_stream)
             rendered[j].record(st)
             prev = rendered[j]
@@ -623,136 +596,162 @@ def run_batched(args, dist):
     e2e_run(e2e_steps)
     te = (time.perf_counter() - te) / e2e_steps
     assert all(torch.equal(a, b) for a, b in zip(pins[0], pins[1])), "the two frame sets must render alike"
-    e2e_batch = e2e_batches[0]
-    d2h = sum(m["width"] * m["height"] * 16 for m, *_ in models)
+    table_bytes = e2e_batches[0].table_bytes
+    del e2e_batches, fsets
+    d2h = sum(m["width"] * m["height"] * 16 for m in mlist)
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": DTYPE_DESC,
-            "data": "synthetic: seeded strands (the reference's glTF hair assets are not available)",
-            "config": batch_config_block(models), "rays_per_step": int(rays_per_step), "gpu_launches": args.steps,
+            "vs_baseline": None, "dtype": DTYPE_DESC, "data": DATA_DESC, "config": batch_config_block(mlist),
+            "rays_per_step": int(rays_per_step), "gpu_launches": args.steps * kernels_per_replay(mlist, tuned),
             "autotuned": {k: int(getattr(tuned, k)) for k in H.TUNED_FIELDS} | {"mean_ms": round(tune_ms, 3)},
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
-                         "bytes_per_launch": int(alg_bytes)},
-            "plain_fp32": {"value": round(rays_per_step / (ms_f32 * 1e-3) / 1e6, 3),
-                           "ms_per_step": round(ms_f32, 3), "launches_per_step": len(models),
-                           "what": "the same 16 scenes as 16 sequential launches of the FP32 tracer (FP32 nodes "
-                                   "and records, no batching, no autotuning)"},
-            "sequential_quantised": {"value": round(rays_per_step / (ms_q * 1e-3) / 1e6, 3),
-                                     "ms_per_step": round(ms_q, 3), "launches_per_step": len(models)},
-            "batched_fp32": {"value": round(rays_per_step / (ms_bf * 1e-3) / 1e6, 3), "ms_per_step": round(ms_bf, 3),
-                             "autotuned": {k: int(getattr(tuned_f, k)) for k in H.TUNED_FIELDS},
-                             "note": "the batching pattern on FP32 BLASes: on these coherent, L2-resident "
-                                     "workloads the 8-bit node decode costs more ALU than the bytes it saves"},
+            "clocks": clk,
+            "e2e": {"value": round(rays_per_step / te / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": table_bytes,
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(te * 1e3, 3)},
+            "roofline": roofline,
+            "build": {"build_wall_s_quantised": round(build_wall, 3), "strand_generation_s": round(t_gen, 3)},
             "device_bytes": {"quantised": mem_q, "fp32": mem_f},
             "per_scene_latency_ms": {"batched_all_scenes": round(ms, 3),
-                                     "note": "a batched scene completes with the launch; sequential latencies "
-                                             "are per launch"},
-            "scenes": per_scene,
-            "e2e": {"value": round(rays_per_step / te / 1e6, 3), "unit": "Mrays/s",
-                    "h2d_bytes_per_step": e2e_batch.table_bytes, "d2h_bytes_per_step": int(d2h),
-                    "ms_per_step": round(te * 1e3, 3)},
-            "clocks": clk,
-            "build": {"build_wall_s_quantised": round(build_wall, 3), "strand_generation_s": round(t_gen, 3)}}
+                                     "plain_fp32": [round(float(x), 2) for x in lat_f32]}}
     if not args.no_cpu:
-        line.update(batch_agreement_and_cpu(args, ctx, q, models))
-    del q, f, batch, e2e_batch, e2e_batches, fsets, scenes_q, scenes_f, batch_f
+        line.update(batch_agreement_and_cpu(ctx, q, models, tuned, fb_timed))
+    del q, batch, scenes_q
     if not args.quick:
-        line["c4_phantom_quantised"] = c4_summary(args, ctx)
+        orc = oracle_lib()
+        line["configs"] = {name.split("_")[0]: run_config(ctx, name, args, orc) for name in SINGLE_CONFIGS}
+    # the comparisons the metric names, last (the line is long; its end is what a log tail keeps)
+    line["sequential_quantised"] = {"value": round(rays_per_step / (ms_q * 1e-3) / 1e6, 3),
+                                    "ms_per_step": round(ms_q, 3)}
+    line["batched_fp32"] = {"value": round(rays_per_step / (ms_bf * 1e-3) / 1e6, 3), "ms_per_step": round(ms_bf, 3),
+                            "autotuned": {k: int(getattr(tuned_f, k)) for k in H.TUNED_FIELDS}}
+    line["plain_fp32"] = {"value": round(rays_per_step / (ms_f32 * 1e-3) / 1e6, 3), "ms_per_step": round(ms_f32, 3),
+                          "what": "the same 16 scenes as 16 sequential launches of the FP32 tracer (FP32 nodes and "
+                                  "records, no batching, no autotuning)"}
+    agreement = line.pop("agreement", None)
+    if agreement is not None:
+        line["agreement"] = agreement
+    print(json.dumps({"per_scene": per_scene}), file=sys.stderr, flush=True)
     print(json.dumps(line), flush=True)
     dist.close()
 
 
-def c4_summary(args, ctx):
-    """The single Phantom precision-pattern frame (19.05 M segments, 1920x1080 x 4 spp): quantised
-    and FP32 frame rates (no oracle legs; `--config c4_phantom_quantised` has them)."""
-    import vkhrt_gb300 as H
-    cfg, sp = workload("c4_phantom_quantised")
-    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
-    v, r, off = H.generate_strands(sp)
-    cam = H.scene_camera(w, h)
-    out = {}
-    for name, prec in (("quantised", H.Precision.QUANTISED), ("plain_fp32", H.Precision.FP32)):
-        blas = H.BottomLevelAccelerationStructure(
-            H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=prec), ctx)
-        tlas = H.TopLevelAccelerationStructure([blas], ctx)
-        fr = H.Frame(ctx, w, h, spp)
-        H.trace(ctx, tlas, cam, fr, H.trace_params(spp=spp, jitter=1, seed=17, shading=2, count_stats=1))
-        st = fr.stats()
-        p = H.trace_params(spp=spp, jitter=1, seed=17, shading=2, **{"async": 1})
-        ms = time_frames(ctx, tlas, cam, fr, p, max(8, args.steps // 2), args.warmup)
-        out[name] = {"value": round((st["primary_rays"] + st["shadow_rays"]) / (ms * 1e-3) / 1e6, 3),
-                     "ms_per_step": round(ms, 3), "nodes_visited": int(st["nodes_visited"]),
-                     "prims_tested": int(st["prims_tested"]), "blas_build_ms": round(blas.info["build_ms"], 2)}
-        # animated strands: the same BLAS refitted to moved vertices (topology kept)
-        v2 = (v + np.float32(0.01) * np.sin(np.float32(3.0) * v[:, [1, 2, 0]])).astype(np.float32)
-        blas.refit(v2, r)
-        out[name]["blas_refit_ms"] = round(blas.info["build_ms"], 2)
-        del fr, tlas, blas
-    return out
+# Per-ray counters of the dominant kernel from an ncu capture (profiles/): DRAM bytes, L2 bytes
+# and warp instructions. None until a capture of the current kernel is summarised there.
+NCU_PER_RAY = None
 
 
-def batch_agreement_and_cpu(args, ctx, q, models):
-    """Per-scene FP64 oracle agreement on ~65,536 sampled rays in all, and the oracle's FP32 rate."""
+def measured_bounds(rays: int, ms: float, clk: dict) -> dict:
+    """DRAM traffic, achieved L2 bandwidth and the issue-rate fraction of the dominant kernel,
+    scaled from its ncu capture's per-ray counters to this launch."""
+    if not NCU_PER_RAY:
+        return {}
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    dram = NCU_PER_RAY["dram_bytes"] * rays
+    l2 = NCU_PER_RAY["l2_bytes"] * rays
+    inst = NCU_PER_RAY["warp_inst"] * rays
+    issue_peak = 152 * 4 * sm_mhz * 1e6  # one warp instruction per scheduler per clock
+    return {"traffic": int(dram), "l2": {"bytes_per_launch": int(l2), "achieved_gbs": round(l2 / (ms * 1e-3) / 1e9, 1)},
+            "issue": {"warp_inst_per_launch": int(inst), "achieved_per_s": round(inst / (ms * 1e-3), 1),
+                      "peak_per_s": issue_peak, "frac": round(inst / (ms * 1e-3) / issue_peak, 4)},
+            "counters_from": NCU_PER_RAY["source"]}
+
+
+def batch_agreement_and_cpu(ctx, q, models, tuned, fb_timed):
+    """The timed graph's output against the FP64 oracle: the same scenes, cameras and tuned
+    parameters captured again with per-sample hit records, replayed once; its framebuffers must
+    equal the timed replay's bit for bit, and its hits and the timed replay's pixels are compared
+    with the oracle on about 65,536 sampled rays. Then the oracle's FP32 rate on every pixel of
+    every scene (in the reference arm's row bands) and its FP64 rate on one of every 16 rows."""
     import vkhrt_gb300 as H
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from hairscene import OracleScene, compare_hits, load_oracle, oracle_geometry
-    orc = load_oracle()
+    orc = oracle_lib()
     threads = orc.orc_hardware_threads()
-    n_t = n_mis = n_ties = 0
-    max_rel_t = 0.0
-    max_rgb = 0.0
-    cpu_rays = 0
-    cpu_px = 0
-    cpu_s = 0.0
-    cpu_frac = 1.0  # every pixel of every scene: about 10 s of CPU work
-    per = max(1, 65536 // len(models))
-    for (b, t, cam, fr), (m, v, r, off) in zip(q, models):
-        H.trace(ctx, t, cam, fr, H.trace_params(jitter=1, seed=17, shading=2, record_hits=1))
-        rgba, hits = fr.download(hits=True)
+    rec = H.trace_params(jitter=1, seed=17, shading=2, record_hits=1,
+                         **{k: getattr(tuned, k) for k in H.TUNED_FIELDS})
+    batch = H.Batch(ctx, [(t, cam, fr) for (_, t, cam, fr) in q], rec)
+    batch.launch()
+    fb_rec = [np.zeros_like(a) for a in fb_timed]
+    batch.download(fb_rec)
+    same_fb = all(np.array_equal(a, b) for a, b in zip(fb_timed, fb_rec))
+    parts = []
+    per = max(1, AGREE_RAYS // len(models))
+    scenes = []
+    for (b, t, cam, fr), (m, v, r, off), rgba in zip(q, models, fb_timed):
         w, h, spp = m["width"], m["height"], m["spp"]
-        lines, lrad = uniform_lines(v, r, m["nstrands"], m["nverts"])
-        data, rad = oracle_geometry(orc, int(m["type"]), lines, lrad, quantised=(int(m["type"]) == 0))
-        del lines, lrad
-        osc = OracleScene(orc, [(int(m["type"]), data, rad)])
+        _, hits = fr.download(hits=True)
+        osc = oracle_scene(orc, int(m["type"]), v, r, m["nstrands"], m["nverts"])
         vi, pi = H.camera_arrays(cam)
         px = sample_pixels(w, h, per // spp, seed=3)
         o = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=64, pixel_list=px)
-        gh = hits.reshape(h * w, spp)[px].reshape(-1)
-        g_t = np.where(gh["t"] >= 0, gh["t"].astype(np.float64), -1.0)
-        cmp = compare_hits(g_t, gh["prim"], gh["inst"], o["t"], o["prim"], o["inst"])
-        n_t += cmp["n"]
-        n_mis += cmp["mismatches"]
-        n_ties += cmp["ties"]
-        max_rel_t = max(max_rel_t, cmp["max_rel_t"])
-        same = (gh["prim"] == o["prim"]) & (((gh["flags"] & H.HIT_SHADOWED) != 0) == (o["shadow"] != 0))
-        ok_px = same.reshape(-1, spp).all(axis=1)
-        if ok_px.any():
-            max_rgb = max(max_rgb, float(np.abs(rgba.reshape(-1, 4)[px] - o["fb"]).max(axis=1)[ok_px].max()))
-        # the oracle's FP32 tracer on the same fraction of every scene's pixels (the workload's mix;
-        # at least 16,384 pixels per call, since a call has a few ms of thread start-up)
-        cpx = sample_pixels(w, h, int(w * h * cpu_frac), seed=11)
-        t0 = time.perf_counter()
-        oc = osc.render(vi, pi, w, h, spp=spp, jitter=1, seed=17, shading=2, precision=32, pixel_list=cpx,
-                        threads=threads)
-        dt = time.perf_counter() - t0
-        cpu_s += dt
-        cpu_rays += len(cpx) * spp + int((oc["t"] >= 0).sum())
-        cpu_px += len(cpx)
-        del osc, data, rad
-    return {"agreement": {"rays": int(n_t), "hit_id": round(1.0 - n_mis / max(n_t - n_ties, 1), 6),
-                          "mismatches": int(n_mis),
-                          "ties": int(n_ties), "max_rel_t": max_rel_t, "max_rgb_err_agreeing": max_rgb,
-                          "oracle": ORACLE_DESC + ", per scene"},
-            "cpu_baseline": {"value": round(cpu_rays / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads,
-                             "kind": "port",
-                             "sample": f"{pixel_share(cpu_frac)} of every scene ({cpu_px} pixels, all their "
-                                       f"samples, {cpu_rays} rays), FP32 oracle, {cpu_s:.1f} s"}}
+        parts.append(compare_frame(rgba, hits, o, px, spp))
+        scenes.append((osc, vi, pi, w, h, spp))
+    agreement = merge_compare(parts)
+    agreement["graph_framebuffers_match_timed_replay"] = same_fb
+    agreement["oracle"] = ORACLE_DESC + ", per scene; hits from the timed graph's parameters, pixels from the timed replay"
+    rate, rays, npx, secs = cpu_rate(scenes, 32, range(ROW_BANDS), ROW_BANDS, threads, 1)
+    rate64, rays64, _, secs64 = cpu_rate(scenes, 64, [0], FP64_BANDS, threads, 1)
+    return {"agreement": agreement,
+            "cpu_baseline": {"value": round(rate, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": f"every pixel of every scene ({npx} pixels, all samples, {rays} rays), FP32 "
+                                       f"oracle, {secs:.1f} s, in the reference arm's row bands",
+                             "fp64": {"value": round(rate64, 4),
+                                      "sample": f"one of every {FP64_BANDS} rows ({rays64} rays), {secs64:.1f} s"}}}
 
 
-def pixel_share(frac: float) -> str:
-    """'every pixel' or '<frac> of the pixels' for a CPU sample description."""
-    return "every pixel" if frac >= 1.0 else f"{frac:g} of the pixels"
+# ------------------------------------------------------------------------------ one configuration
+def run_single(args, dist):
+    """`--config NAME` (C1-C4): the configuration's frame timed in its own precision (or the
+    --precision override); with --profile only the timed launches (for ncu), otherwise also the
+    configuration's block (both precisions, agreement)."""
+    import torch
+    import vkhrt_gb300 as H
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    ctx = H.Context(dev)
+    cfg, sp = workload(args.config)
+    w, h, spp = cfg["width"], cfg["height"], cfg["spp"]
+    v, r, off = H.generate_strands(sp)
+    blas = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=cfg["precision"],
+                    max_leaf=args.max_leaf), ctx)
+    tlas = H.TopLevelAccelerationStructure([blas], ctx)
+    cam = H.scene_camera(w, h)
+    frame = H.Frame(ctx, w, h, spp)
+    knobs = dict(spp=spp, jitter=jitter_of(spp), seed=17, shading=2, kernel_variant=args.variant, refill=args.refill,
+                 speculative=args.speculative, leaf_again=args.leaf_again)
+    H.trace(ctx, tlas, cam, frame, H.trace_params(count_stats=1, **knobs))
+    st = frame.stats()
+    rays = st["primary_rays"] + st["shadow_rays"]
+    dist.barrier()
+    clocks = Clocks(dev)
+    clocks.start()
+    ms = time_frames(ctx, tlas, cam, frame, H.trace_params(**knobs, **{"async": 1}), args.steps, args.warmup)
+    clk = clocks.stop()
+    ms_max = dist.max(ms)
+    value = dist.world * rays / (ms_max * 1e-3) / 1e6
+    if dist.rank != 0:
+        dist.close()
+        return
+    info = blas.info
+    alg = st["nodes_visited"] * info["node_bytes"] + \
+        st["prims_tested"] * prim_test_bytes(info, int(cfg["type"]), int(cfg["precision"])) + w * h * 16
+    peak, peak_kind = load_peaks()
+    achieved = alg / (ms * 1e-3) / 1e9
+    tot = st["warp_cycles_node"] + st["warp_cycles_leaf"] + st["warp_cycles_other"]
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": DTYPE_DESC if int(cfg["precision"]) else "fp32", "data": DATA_DESC,
+            "config": single_config_block(cfg, args.config), "rays_per_step": int(rays),
+            "gpu_launches": args.steps * (3 if int(cfg["type"]) == 0 else 1),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                         "bytes_per_launch": int(alg), "nodes_visited": int(st["nodes_visited"]),
+                         "prims_tested": int(st["prims_tested"])},
+            "phase_share": {k: round(st["warp_cycles_" + k] / tot, 4) for k in ("node", "leaf", "other")} if tot else None,
+            "clocks": clk}
+    if not args.profile:
+        del frame, tlas, blas
+        line["block"] = run_config(ctx, args.config, args, oracle_lib())
+    print(json.dumps(line), flush=True)
+    dist.close()
 
 
 def main():
@@ -762,10 +761,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default=BATCH_CONFIG)
-    ap.add_argument("--quick", action="store_true", help="skip the plain FP32 comparison")
+    ap.add_argument("--quick", action="store_true", help="skip the C1-C4 configuration blocks")
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle agreement and CPU baseline")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--ref-pixels", type=int, default=4096)
+    ap.add_argument("--config-steps", type=int, default=10, help="timed frames per precision in each C1-C4 block")
     ap.add_argument("--width", type=int, default=0, help="override the image width (profiling)")
     ap.add_argument("--height", type=int, default=0, help="override the image height (profiling)")
     ap.add_argument("--spp", type=int, default=0, help="override samples per pixel (profiling)")
@@ -779,7 +777,7 @@ def main():
                     help="repeat the leaf phase while this many lanes hold leaves (0 = once)")
     ap.add_argument("--tune-cache", default=None, help="JSON file that keeps autotuner choices between runs")
     ap.add_argument("--profile", action="store_true",
-                    help="one warm-up and the timed steps only: no e2e, FP32 comparison or CPU legs")
+                    help="with --config: the timed launches only (no agreement or CPU legs)")
     args = ap.parse_args()
     for k in ("width", "height", "spp"):
         if getattr(args, k):
@@ -787,8 +785,6 @@ def main():
     if args.precision:
         import vkhrt_gb300 as H
         _OVERRIDE["precision"] = H.Precision.QUANTISED if args.precision == "quantised" else H.Precision.FP32
-    if args.profile:
-        args.quick = args.no_cpu = True
     if args.warmup < 3 and not args.profile:
         args.warmup = 3
     dist = Dist()
@@ -799,7 +795,7 @@ def main():
     if args.config == BATCH_CONFIG:
         run_batched(args, dist)
         return
-    run_ours(args, dist)
+    run_single(args, dist)
 
 
 if __name__ == "__main__":

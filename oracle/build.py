@@ -14,8 +14,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD_DIR, "libhrtoracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libhrtref.so")
-SRC = [os.path.join(HERE, "hrt_oracle.cpp")]
-DEPS = SRC + [os.path.join(HERE, "glsl_shim.hpp")]
+ROOT = os.path.dirname(HERE)
+# the workload generator (synthetic strands, camera matrices) is compiled from the GPU library's
+# own host source, so that CPU-only runs trace exactly the same inputs without loading libhrt.so
+WORKLOAD_SRC = os.path.join(ROOT, "vkhrt_gb300", "csrc", "workload.cpp")
+SRC = [os.path.join(HERE, "hrt_oracle.cpp"), WORKLOAD_SRC]
+DEPS = SRC + [os.path.join(HERE, "glsl_shim.hpp"), os.path.join(ROOT, "include", "hrt.h")]
 
 
 def _stale(target: str, deps: list[str]) -> bool:
@@ -30,7 +34,7 @@ def build(force: bool = False, with_ref: bool = True) -> str:
     os.makedirs(BUILD_DIR, exist_ok=True)
     if force or _stale(LIB, DEPS):
         cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-               "-pthread", "-I" + HERE] + SRC + ["-o", LIB + ".tmp"]
+               "-pthread", "-I" + HERE, "-I" + os.path.join(ROOT, "include")] + SRC + ["-o", LIB + ".tmp"]
         subprocess.run(cmd, check=True)
         os.replace(LIB + ".tmp", LIB)
     if with_ref:

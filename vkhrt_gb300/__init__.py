@@ -375,8 +375,24 @@ class TopLevelAccelerationStructure:
             pass
 
 
-def look_at(eye, center, up, fovy_deg: float, aspect: float, znear: float = 0.1, zfar: float = 1000.0) -> CameraC:
-    lib = load()
+# The workload generator (synthetic strands, camera matrices) is host code that the CPU oracle's
+# library compiles too; `lib` selects which library runs it (default libhrt.so).
+WORKLOAD_SYMBOLS = ("hrt_camera_look_at", "hrt_strand_params_default", "hrt_generate_strands", "hrt_checksum")
+
+
+def bind_workload(lib: ctypes.CDLL) -> ctypes.CDLL:
+    """Declares the workload generator's symbols on a library that exports them."""
+    for name in WORKLOAD_SYMBOLS:
+        res, args = SIGNATURES[name]
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def look_at(eye, center, up, fovy_deg: float, aspect: float, znear: float = 0.1, zfar: float = 1000.0,
+            lib: ctypes.CDLL | None = None) -> CameraC:
+    lib = lib or load()
     cam = CameraC()
     e = np.asarray(eye, np.float32)
     c = np.asarray(center, np.float32)
@@ -577,9 +593,9 @@ class StrandParams:
     cap_deg: float = 60.0
 
 
-def generate_strands(p: StrandParams) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+def generate_strands(p: StrandParams, lib: ctypes.CDLL | None = None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     """Seeded synthetic strands: (vertices (nv,3), radius (nv,), strand_offsets (ns+1,))."""
-    lib = load()
+    lib = lib or load()
     c = StrandParamsC()
     for k, _ in StrandParamsC._fields_:
         setattr(c, k, getattr(p, k))
@@ -593,8 +609,8 @@ def generate_strands(p: StrandParams) -> tuple[np.ndarray, np.ndarray, np.ndarra
     return v, r, o
 
 
-def checksum(*arrays: np.ndarray) -> int:
-    lib = load()
+def checksum(*arrays: np.ndarray, lib: ctypes.CDLL | None = None) -> int:
+    lib = lib or load()
     a = np.ascontiguousarray(arrays[0])
     b = np.ascontiguousarray(arrays[1]) if len(arrays) > 1 else None
     return int(lib.hrt_checksum(_ptr(a), a.nbytes, _ptr(b), 0 if b is None else b.nbytes))
@@ -613,17 +629,18 @@ CONFIGS = {
 }
 
 
-def scene_camera(width: int, height: int) -> CameraC:
+def scene_camera(width: int, height: int, lib: ctypes.CDLL | None = None) -> CameraC:
     """Camera of the benchmark scenes: eye (0,0,3) looking at the origin, +y up, 40 deg FOV."""
-    return look_at((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width / height, 0.1, 1000.0)
+    return look_at((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width / height, 0.1, 1000.0, lib)
 
 
-def orbit_camera(width: int, height: int, azimuth: float, elevation: float, dist: float = 3.0) -> CameraC:
+def orbit_camera(width: int, height: int, azimuth: float, elevation: float, dist: float = 3.0,
+                 lib: ctypes.CDLL | None = None) -> CameraC:
     """scene_camera moved on the sphere of radius `dist` (angles in radians, azimuth 0 = +z)."""
     import math
     eye = (dist * math.cos(elevation) * math.sin(azimuth), dist * math.sin(elevation),
            dist * math.cos(elevation) * math.cos(azimuth))
-    return look_at(eye, (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width / height, 0.1, 1000.0)
+    return look_at(eye, (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0, width / height, 0.1, 1000.0, lib)
 
 
 def batch_workload(seed: int = 1005, nscenes: int = 16) -> list[dict]:

@@ -5,7 +5,7 @@ Translation units compile in parallel:
   csrc/trace.cu         explicit-ray and no-allocation trace entry points
   csrc/trace_frames.cu  frame kernels, once for FP32 nodes and once for 8-bit nodes
   csrc/api.cu           C ABI (host code)
-  csrc/strands.cpp      synthetic strands (host, -ffp-contract=off)
+  csrc/workload.cpp     synthetic strands and camera matrices (host, -ffp-contract=off)
 """
 from __future__ import annotations
 
@@ -37,7 +37,7 @@ UNITS = {
     "trace_frames_f": ("trace_frames.cu", ["-DHRT_FRAMES_QUANT=0"]),
     "trace_frames_q": ("trace_frames.cu", ["-DHRT_FRAMES_QUANT=1"]),
     "api": ("api.cu", []),
-    "strands": ("strands.cpp", ["-x", "c++", "-Xcompiler", "-ffp-contract=off"]),
+    "workload": ("workload.cpp", ["-x", "c++", "-Xcompiler", "-ffp-contract=off"]),
 }
 
 

@@ -137,6 +137,10 @@ struct TraceLaunch {
     uint32_t env_w, env_h;
 };
 
+// ---- host helpers (workload.cpp) ------------------------------------------------------------
+// Inverse of a column-major 4x4 matrix in double (false when singular).
+bool invert4(const double* m, double* out);
+
 // ---- launch wrappers (trace.cu) --------------------------------------------------------------
 cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count);
 cudaError_t prepare_frames();  // frame kernels' attributes (shared memory / L1 split), once per context

@@ -1,10 +1,14 @@
-// strands.cpp -- seeded synthetic hair strands (the reference loads Claire's glTF hair through
-// assimp, source/resources/model/model_loader.cpp:274-336; those assets are not available, so
-// strands of the same kind are generated). Compiled with -ffp-contract=off and free of libm
-// transcendental calls, so the output is bit-identical on every host.
+// workload.cpp -- host code that defines a traced workload: seeded synthetic hair strands (the
+// reference loads Claire's glTF hair through assimp, source/resources/model/model_loader.cpp:274-336;
+// those assets are not available, so strands of the same kind are generated) and the camera
+// matrices (FlyCamera, source/fly_camera.cpp:25-35). Compiled with -ffp-contract=off; the strand
+// generator is free of libm transcendental calls, so its output is bit-identical on every host.
+// The CPU oracle's library compiles this same file, so that a CPU-only run traces exactly the
+// strands and cameras the GPU library would.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <utility>
 
 #include "hrt.h"
 
@@ -51,7 +55,79 @@ D3 nrm(D3 a) {
 
 }  // namespace
 
+namespace hrt {
+// Inverse of a column-major 4x4 matrix in double: Gauss-Jordan elimination with partial
+// pivoting on the row-major copy [A | I].
+bool invert4(const double* m, double* out) {
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            a[r][c] = m[4 * c + r];
+            a[r][4 + c] = r == c ? 1.0 : 0.0;
+        }
+    for (int col = 0; col < 4; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < 4; ++r)
+            if (std::fabs(a[r][col]) > std::fabs(a[piv][col])) piv = r;
+        if (!(std::fabs(a[piv][col]) > 0.0) || !std::isfinite(a[piv][col])) return false;
+        if (piv != col)
+            for (int c = 0; c < 8; ++c) std::swap(a[piv][c], a[col][c]);
+        double d = a[col][col];
+        for (int c = 0; c < 8; ++c) a[col][c] /= d;
+        for (int r = 0; r < 4; ++r) {
+            if (r == col || a[r][col] == 0.0) continue;
+            double f = a[r][col];
+            for (int c = 0; c < 8; ++c) a[r][c] -= f * a[col][c];
+        }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) out[4 * c + r] = a[r][4 + c];
+    return true;
+}
+}  // namespace hrt
+
 extern "C" {
+
+hrt_status hrt_camera_look_at(const float eye[3], const float center[3], const float up[3], float fovy_deg,
+                              float aspect, float znear, float zfar, hrt_camera* out) {
+    if (!eye || !center || !up || !out || !(aspect > 0.0f) || !(zfar > znear) || !(fovy_deg > 0.0f) ||
+        !(fovy_deg < 180.0f))
+        return HRT_ERR_INVALID_ARG;
+    // glm::lookAtRH: f = normalize(center - eye), s = normalize(cross(f, up)), u = cross(s, f)
+    double e[3] = {eye[0], eye[1], eye[2]}, c[3] = {center[0], center[1], center[2]}, u0[3] = {up[0], up[1], up[2]};
+    double f[3] = {c[0] - e[0], c[1] - e[1], c[2] - e[2]};
+    double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    if (!(fl > 0.0)) return HRT_ERR_INVALID_ARG;
+    for (double& x : f) x /= fl;
+    double s[3] = {f[1] * u0[2] - f[2] * u0[1], f[2] * u0[0] - f[0] * u0[2], f[0] * u0[1] - f[1] * u0[0]};
+    double sl = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    if (!(sl > 0.0)) return HRT_ERR_INVALID_ARG;
+    for (double& x : s) x /= sl;
+    double u[3] = {s[1] * f[2] - s[2] * f[1], s[2] * f[0] - s[0] * f[2], s[0] * f[1] - s[1] * f[0]};
+    double V[16] = {0};
+    V[0] = s[0]; V[4] = s[1]; V[8] = s[2];
+    V[1] = u[0]; V[5] = u[1]; V[9] = u[2];
+    V[2] = -f[0]; V[6] = -f[1]; V[10] = -f[2];
+    V[12] = -(s[0] * e[0] + s[1] * e[1] + s[2] * e[2]);
+    V[13] = -(u[0] * e[0] + u[1] * e[1] + u[2] * e[2]);
+    V[14] = f[0] * e[0] + f[1] * e[1] + f[2] * e[2];
+    V[15] = 1.0;
+    // glm::perspectiveRH_ZO, then [1][1] *= -1 (fly_camera.cpp:32-33)
+    double th = std::tan(double(fovy_deg) * 3.14159265358979323846 / 360.0);
+    double P[16] = {0};
+    P[0] = 1.0 / (double(aspect) * th);
+    P[5] = -(1.0 / th);
+    P[10] = double(zfar) / (double(znear) - double(zfar));
+    P[11] = -1.0;
+    P[14] = -(double(zfar) * double(znear)) / (double(zfar) - double(znear));
+    double Vi[16], Pi[16];
+    if (!hrt::invert4(V, Vi) || !hrt::invert4(P, Pi)) return HRT_ERR_INVALID_ARG;
+    for (int k = 0; k < 16; ++k) {
+        out->view_inverse[k] = float(Vi[k]);
+        out->proj_inverse[k] = float(Pi[k]);
+    }
+    return HRT_OK;
+}
 
 void hrt_strand_params_default(hrt_strand_params* p) {
     memset(p, 0, sizeof(*p));
