@@ -40,7 +40,7 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
-sys.path.insert(0, os.path.join(ROOT, "tests"))  # hairscene: oracle scenes and hit comparison (the checker)
+sys.path.insert(0, os.path.join(ROOT, "tests"))  # hairscene: oracle scenes and hit comparison
 
 METRIC = "Mrays/s on 1 GB300: quantized/batched vs plain FP32 at >=99.99% hit agreement"
 L2_BYTES = 129 * 1024 * 1024

@@ -184,6 +184,13 @@ typedef struct hrt_trace_params {
     uint32_t env_width, env_height;
     uint32_t leaf_again;     /* repeat the leaf phase while at least this many lanes of a warp hold untested
                                 leaf children (0 = one leaf per lane per phase; default 4) */
+    /* Bounds of every ray's traversal (0 = the defaults, 65536 steps and 64 stack entries; a
+     * depth above 64 is refused). A ray that exceeds one stops, the launch stops taking work, and
+     * the call (or the next call that reads the launch's status: hrt_frame_get_stats,
+     * hrt_frame_download, hrt_batch_download with synchronise, hrt_batch_launch without async)
+     * returns HRT_ERR_TIMEOUT or HRT_ERR_STACK_OVERFLOW; the context stays usable. */
+    uint32_t max_steps;
+    uint32_t max_depth;
 } hrt_trace_params;
 
 typedef struct hrt_hit {
@@ -283,9 +290,11 @@ hrt_status hrt_trace_rays(hrt_context* ctx, const hrt_tlas* tlas, const float* r
  * staging for both and the kernel's counters live in one static device array of
  * HRT_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until the process exits.
  * n above HRT_NOALLOC_MAX_RAYS is rejected with HRT_ERR_INVALID_ARG. The first call on a device
- * looks up the array's device address (make that call before any stream capture). Every call
- * shares the array: calls that overlap on the GPU (other streams, other host threads) race, so
- * serialise them; each call synchronises `stream` before it returns. */
+ * looks up the array's device address; make that first call before any stream capture begins.
+ * Each call copies the rays and hits through pageable host memory and synchronises `stream`
+ * before it returns, so a call on a stream that is being captured is refused with
+ * HRT_ERR_INVALID_ARG. Every call shares the array: calls that overlap on the GPU (other
+ * streams, other host threads) race, so serialise them. */
 #define HRT_NOALLOC_MAX_RAYS 65536u
 #define HRT_NOALLOC_SCRATCH_BYTES (256u + HRT_NOALLOC_MAX_RAYS * 40u)
 hrt_status hrt_trace_rays_noalloc(hrt_context* ctx, const hrt_tlas* tlas, const float* rays, uint64_t n,

@@ -1,7 +1,7 @@
 """oracle/build.py -- TEST INFRASTRUCTURE: builds the CPU oracle (and, where the reference
 checkout is present, oracle/_ref). Used by __graft_entry__.build() and the test fixtures.
 
-The oracle is the checker: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+The oracle is test infrastructure: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
 leg load it.
 """
 from __future__ import annotations
@@ -40,9 +40,11 @@ def build(force: bool = False, with_ref: bool = True) -> str:
     if with_ref:
         ref_deps = [os.path.join(HERE, "ref_harness.cpp"), os.path.join(HERE, "glsl_shim.hpp"),
                     os.path.join(HERE, "build_ref.sh")]
-        ref_root = os.environ.get("HRT_REFERENCE", "/root/reference")
+        # the reference checkout: HRT_REFERENCE, else a `reference` directory beside the repository
+        ref_root = os.environ.get("HRT_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
         if os.path.isdir(os.path.join(ref_root, "shaders")) and (force or _stale(REF_LIB, ref_deps)):
-            subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True)
+            subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True,
+                           env=dict(os.environ, HRT_REFERENCE=ref_root))
     return LIB
 
 

@@ -2,8 +2,8 @@
 # oracle/build_ref.sh -- TEST INFRASTRUCTURE: builds oracle/_ref/libhrtref.so, the reference's
 # own shader and geometry code compiled as host C++ through oracle/glsl_shim.hpp.
 #
-# Reads the reference checkout (default /root/reference, override with HRT_REFERENCE) where it
-# lies; writes only into oracle/_ref/ (git-ignored). Nothing from the reference is committed.
+# Reads the reference checkout (HRT_REFERENCE, else a `reference` directory beside the repository)
+# where it lies; writes only into oracle/_ref/ (git-ignored). Nothing from the reference is committed.
 #   * shaders/{ray,curve,cone,cylinder,shading}.glsl are included as they are. For the FP32
 #     build every unsuffixed floating literal gets an `f` suffix, because in GLSL `0.5` is a
 #     float while in C++ it is a double; the FP64 build includes them untouched with
@@ -13,10 +13,10 @@
 #   * GenerateCurves, PerpStark, BuildFrame, GenerateDisjointOrthogonalTriangleStrips,
 #     GenerateLinearSweptSpheres and GenerateAABBs(curves) are cut out of
 #     source/resources/model/geometry_processor.cpp (:123-156, :199-298, :422-436).
-# If the checkout is absent (the GPU machine) the script prints a note and exits 0.
+# If the checkout is absent the script prints a note and exits 0.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${HRT_REFERENCE:-/root/reference}"
+REF="${HRT_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/shaders" ]; then
     echo "build_ref: reference checkout not found at $REF; oracle/_ref not built"

@@ -1,6 +1,6 @@
 """Test helpers: seeded hair scenes for the GPU library and the CPU oracle, and hit comparison.
 
-The oracle (oracle/) is the checker; it receives the same strands and processes them with its
+The oracle (oracle/) checks the GPU results; it receives the same strands and processes them with its
 own restatement of the reference's geometry code.
 """
 from __future__ import annotations

@@ -367,3 +367,36 @@ def test_strand_stream_rebuilds_the_curves(orc, case):
         assert len(ent) == n + 3 * 2
     if case == "touching_strands":
         assert len(ent) == n + 3
+
+
+@pytest.mark.parametrize("spread", [0.01, 0.004])
+def test_shifted_origin_fp64_agrees_with_the_literal_fp64_prhi(orc, spread):
+    """The oracle of record (precision code 64) evaluates Prhi in FP64 from the ray point nearest
+    the chord midpoint; the golden vectors pin the literal FP64 evaluation (code 6400).
+    * From 0.3 units away the two give the same closest hit on every aimed ray.
+    * From 3 units away the literal form misses a few grazing hits (about 1 in 1,000): its
+      bounding-cylinder test (hair_intersection.rint:29) rounds in proportion to the squared
+      distance of the origin. Moved 0.3 units in front of the hair, the same rays give the literal
+      form the shifted form's hits on every one of them, so the two differ only in that rounding."""
+    import vkhrt_gb300 as H
+    from hairscene import aimed_rays, compare_hits, oracle_geometry
+    v, r, off = H.generate_strands(H.StrandParams(seed=1004, nstrands=400, nverts=64, r_root=0.003, r_tip=0.0008),
+                                   lib=H.bind_workload(orc))
+    lines, lrad = lines_from_strands(v, r, off)
+    sc = OracleScene(orc, [(PHANTOM, *oracle_geometry(orc, PHANTOM, lines, lrad))])
+    for dist in (0.3, 3.0):
+        rays = aimed_rays(np.random.default_rng(64), lines, 20000, spread=spread, dist=dist)
+        a = sc.trace_rays(rays, precision=64)
+        b = sc.trace_rays(rays, precision=6400)
+        st = compare_hits(a[0], a[1], a[2], b[0], b[1], b[2])
+        assert st["hits"] > 5000 and st["p9999_rel_t"] <= 1e-6, st
+        if dist < 1.0:
+            assert st["mismatches"] == 0, st
+            continue
+        assert st["agreement"] >= 0.999, st
+        idx = st["mism_idx"]
+        assert (a[0][idx] >= 0).all()  # the shifted form finds a hit on every disputed ray
+        near = rays[idx].copy()
+        near[:, :3] += near[:, 3:] * np.float32(dist - 0.3)
+        c = sc.trace_rays(near, precision=6400)
+        assert np.array_equal(c[1][c[0] >= 0], a[1][idx][c[0] >= 0]) and (c[0] >= 0).all()

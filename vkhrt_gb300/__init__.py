@@ -48,7 +48,7 @@ class TraceParamsC(ctypes.Structure):
                 ("shading", c_u32), ("shadow_tmin", c_f), ("fp64_resolve", c_u32), ("record_hits", c_u32),
                 ("async_", c_u32), ("count_stats", c_u32), ("kernel_variant", c_u32), ("refill", c_u32),
                 ("speculative", c_u32), ("split_types", c_u32), ("env_map", c_p), ("env_width", c_u32),
-                ("env_height", c_u32), ("leaf_again", c_u32)]
+                ("env_height", c_u32), ("leaf_again", c_u32), ("max_steps", c_u32), ("max_depth", c_u32)]
 
 
 class FrameStatsC(ctypes.Structure):
@@ -457,12 +457,13 @@ def trace(ctx: Context, tlas: TopLevelAccelerationStructure, cam: CameraC, frame
 
 
 def trace_rays(ctx: Context, tlas: TopLevelAccelerationStructure, rays: np.ndarray,
-               params: TraceParamsC | None = None) -> np.ndarray:
+               params: TraceParamsC | None = None, stream: int | None = None) -> np.ndarray:
     """Closest hit for explicit rays (n, 6) float32 = origin xyz, direction xyz."""
     r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
     hits = np.zeros(r.shape[0], HIT_DTYPE)
     p = params if params is not None else trace_params()
-    ctx.check(ctx.lib.hrt_trace_rays(ctx.handle, tlas.handle, _ptr(r), r.shape[0], ctypes.byref(p), _ptr(hits), 0, None))
+    ctx.check(ctx.lib.hrt_trace_rays(ctx.handle, tlas.handle, _ptr(r), r.shape[0], ctypes.byref(p), _ptr(hits), 0,
+                                     c_p(stream) if stream else None))
     return hits
 
 
@@ -470,14 +471,14 @@ NOALLOC_MAX_RAYS = 65536
 
 
 def trace_rays_noalloc(ctx: Context, tlas: TopLevelAccelerationStructure, rays: np.ndarray,
-                       params: TraceParamsC | None = None) -> np.ndarray:
+                       params: TraceParamsC | None = None, stream: int | None = None) -> np.ndarray:
     """hrt_trace_rays_noalloc: closest hit for at most NOALLOC_MAX_RAYS host rays without any
     device allocation (for callers that cannot call cudaMalloc/cudaFree; see include/hrt.h)."""
     r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
     hits = np.zeros(r.shape[0], HIT_DTYPE)
     p = params if params is not None else trace_params()
     ctx.check(ctx.lib.hrt_trace_rays_noalloc(ctx.handle, tlas.handle, _ptr(r), r.shape[0], ctypes.byref(p), _ptr(hits),
-                                             None))
+                                             c_p(stream) if stream else None))
     return hits
 
 

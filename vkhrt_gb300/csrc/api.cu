@@ -112,6 +112,12 @@ struct hrt_batch {
     cudaGraphExec_t exec = nullptr;
     std::vector<hrt_frame*> frames;
     bool async = false;
+    // the groups' counters as the last replay left them (page-locked; the graph ends with their
+    // copy), and an event recorded after each replay: async replays report a device error at
+    // the next synchronising download, or at the next launch once the replay has finished
+    TraceCounters* host_ctr = nullptr;
+    cudaEvent_t done = nullptr;
+    bool launched = false;
 };
 
 namespace {
@@ -160,13 +166,34 @@ bool is_identity(const float* m) {
     return true;
 }
 
+// The status a launch's device error word stands for.
+hrt_status error_status(hrt_context* ctx, uint32_t error) {
+    if (error & kErrStackOverflow)
+        return fail(ctx, HRT_ERR_STACK_OVERFLOW, "a traversal overflowed its stack (max_depth entries, at most %d)",
+                    kStackSize);
+    if (error & kErrTimeout) return fail(ctx, HRT_ERR_TIMEOUT, "a traversal exceeded its step bound (max_steps)");
+    return HRT_OK;
+}
+
 hrt_status read_counters(hrt_context* ctx, TraceCounters* dev, TraceCounters* host, cudaStream_t s) {
     CK(ctx, cudaMemcpyAsync(host, dev, sizeof(TraceCounters), cudaMemcpyDeviceToHost, s), "read counters");
     CK(ctx, cudaStreamSynchronize(s), "synchronise trace");
-    if (host->error & kErrStackOverflow)
-        return fail(ctx, HRT_ERR_STACK_OVERFLOW, "traversal stack of %d entries overflowed", kStackSize);
-    if (host->error & kErrTimeout)
-        return fail(ctx, HRT_ERR_TIMEOUT, "a traversal exceeded %u steps", kMaxTraversalSteps);
+    return error_status(ctx, host->error);
+}
+
+// Traversal bounds of a launch from the caller's parameters (0 = the defaults).
+RayBounds bounds_of(const hrt_trace_params* p) {
+    return RayBounds{p->max_steps ? p->max_steps : kMaxTraversalSteps,
+                     p->max_depth ? int32_t(p->max_depth) : int32_t(kStackSize)};
+}
+
+// Checks of the parameters every trace entry point shares.
+hrt_status check_params(hrt_context* ctx, const hrt_trace_params* p, const char* who) {
+    if (!(p->tmax > p->tmin)) return fail(ctx, HRT_ERR_INVALID_ARG, "%s: tmax must exceed tmin", who);
+    if (p->shading > HRT_SHADE_LAMBERT_SHADOW) return fail(ctx, HRT_ERR_INVALID_ARG, "%s: unknown shading %u", who, p->shading);
+    if (p->max_depth > uint32_t(kStackSize))
+        return fail(ctx, HRT_ERR_INVALID_ARG, "%s: max_depth %u exceeds the %d-entry traversal stack", who, p->max_depth,
+                    kStackSize);
     return HRT_OK;
 }
 
@@ -229,6 +256,9 @@ TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32
     L.refill = p->refill > 32 ? 32 : p->refill;
     L.speculative = p->speculative;
     L.leaf_again = p->leaf_again > 32 ? 32 : p->leaf_again;
+    const RayBounds rb = bounds_of(p);
+    L.max_steps = rb.max_steps;
+    L.max_depth = rb.max_depth;
     L.counters = c;
     L.resolve_list = resolve_list;
     L.resolve_cap = resolve_cap;
@@ -377,10 +407,7 @@ hrt_status read_plan_counters(hrt_context* ctx, const ScenePlan& P, TraceCounter
         sum->cycles_other += x.cycles_other;
         sum->error |= x.error;
     }
-    if (sum->error & kErrStackOverflow)
-        return fail(ctx, HRT_ERR_STACK_OVERFLOW, "traversal stack of %d entries overflowed", kStackSize);
-    if (sum->error & kErrTimeout) return fail(ctx, HRT_ERR_TIMEOUT, "a traversal exceeded %u steps", kMaxTraversalSteps);
-    return HRT_OK;
+    return error_status(ctx, sum->error);
 }
 
 }  // namespace
@@ -1101,7 +1128,7 @@ hrt_status hrt_blas_get(const hrt_blas* b, int32_t part, void* dst, uint64_t byt
             need = n * 144;
             if (bytes != need) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_get: part needs %llu bytes", (unsigned long long)need);
             if (!n) return HRT_OK;
-            if (!o.geom) return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_get: part %d was not kept by this build", part);
+            if (!o.geom) return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_get: part %d was not kept when the BLAS was built", part);
             float* tmp = nullptr;
             CK(ctx, cudaMalloc(&tmp, need), "allocate DOTS vertices");
             cudaError_t e = expand_dots(o.geom, n, tmp, nullptr);
@@ -1116,7 +1143,7 @@ hrt_status hrt_blas_get(const hrt_blas* b, int32_t part, void* dst, uint64_t byt
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_get: part %d needs %llu bytes, got %llu", part,
                     (unsigned long long)need, (unsigned long long)bytes);
     if (need == 0) return HRT_OK;
-    if (!src) return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_get: part %d was not kept by this build", part);
+    if (!src) return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_get: part %d was not kept when the BLAS was built", part);
     CK(ctx, cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost), "hrt_blas_get");
     return HRT_OK;
 }
@@ -1261,6 +1288,13 @@ hrt_status hrt_frame_download(hrt_frame* f, float* rgba, hrt_hit* hits, void* st
         CK(ctx, cudaMemcpyAsync(hits, f->hits, uint64_t(f->w) * f->h * f->spp * sizeof(hrt_hit), cudaMemcpyDeviceToHost, s),
            "download hits");
     }
+    if (f->stats_pending) {  // an asynchronous trace: its status (and statistics) come with the download
+        TraceCounters c;
+        hrt_status st = read_counters(ctx, f->counters, &c, s);
+        f->stats_pending = false;
+        counters_to_stats(c, f->pending_primary, &f->stats);
+        return st;
+    }
     CK(ctx, cudaStreamSynchronize(s), "download frame");
     return HRT_OK;
 }
@@ -1284,8 +1318,7 @@ hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* c
                      hrt_frame* f, void* stream) {
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!tlas || !cam || !p || !f) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace: null argument");
-    if (f->spp == 0 || !(p->tmax > p->tmin)) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace: bad parameters");
-    if (p->shading > HRT_SHADE_LAMBERT_SHADOW) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace: unknown shading %u", p->shading);
+    if (hrt_status ps = check_params(ctx, p, "hrt_trace")) return ps;
     if (p->record_hits && !f->hits) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace: record_hits on a frame without hit records");
     DeviceSet ds(ctx->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1313,6 +1346,7 @@ hrt_status hrt_trace_rays(hrt_context* ctx, const hrt_tlas* tlas, const float* r
     if (!tlas || !p || (n && (!rays || !hits))) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays: null argument");
     if (memory != HRT_MEMORY_HOST && memory != HRT_MEMORY_DEVICE)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays: unknown memory kind");
+    if (hrt_status ps = check_params(ctx, p, "hrt_trace_rays")) return ps;
     if (n == 0) return HRT_OK;
     DeviceSet ds(ctx->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1336,8 +1370,8 @@ hrt_status hrt_trace_rays(hrt_context* ctx, const hrt_tlas* tlas, const float* r
         dh = th;
     }
     if (e == cudaSuccess)
-        e = launch_trace_rays(tlas->dev, tlas->n, dr, n, p->tmin, p->tmax, p->fp64_resolve, dh, ctr, tlas->quantised, s,
-                              ctx->sm_count);
+        e = launch_trace_rays(tlas->dev, tlas->n, dr, n, p->tmin, p->tmax, p->fp64_resolve, bounds_of(p), dh, ctr,
+                              tlas->quantised, s, ctx->sm_count);
     if (e == cudaSuccess && memory == HRT_MEMORY_HOST) e = cudaMemcpyAsync(hits, th, n * sizeof(hrt_hit), cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) {
         done();
@@ -1356,15 +1390,20 @@ hrt_status hrt_trace_rays_noalloc(hrt_context* ctx, const hrt_tlas* tlas, const 
     if (n > HRT_NOALLOC_MAX_RAYS)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays_noalloc: %llu rays; at most %u per call",
                     (unsigned long long)n, HRT_NOALLOC_MAX_RAYS);
+    if (hrt_status ps = check_params(ctx, p, "hrt_trace_rays_noalloc")) return ps;
     DeviceSet ds(ctx->device);
+    // the call copies through pageable host memory and synchronises the stream, neither of which
+    // a stream capture allows: refuse a capturing stream before enqueueing anything
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CK(ctx, cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap), "hrt_trace_rays_noalloc");
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays_noalloc: the stream is being captured");
     uint32_t err = 0;
     cudaError_t e = trace_rays_noalloc(ctx->device, tlas->dev, tlas->n, tlas->quantised, rays, n, p->tmin, p->tmax,
-                                       p->fp64_resolve, hits, static_cast<cudaStream_t>(stream), ctx->sm_count, &err);
+                                       p->fp64_resolve, bounds_of(p), hits, static_cast<cudaStream_t>(stream),
+                                       ctx->sm_count, &err);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "hrt_trace_rays_noalloc");
-    if (err & kErrStackOverflow)
-        return fail(ctx, HRT_ERR_STACK_OVERFLOW, "traversal stack of %d entries overflowed", kStackSize);
-    if (err & kErrTimeout) return fail(ctx, HRT_ERR_TIMEOUT, "a traversal exceeded %u steps", kMaxTraversalSteps);
-    return HRT_OK;
+    return error_status(ctx, err);
 }
 
 hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* p,
@@ -1372,6 +1411,7 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!scenes || !n || !p || !out) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_create: null or empty argument");
     *out = nullptr;
+    if (hrt_status ps = check_params(ctx, p, "hrt_batch_create")) return ps;
     DeviceSet ds(ctx->device);
     hrt_batch* b = new (std::nothrow) hrt_batch();
     if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_batch_create: host allocation");
@@ -1384,14 +1424,21 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
         hrt_batch_destroy(b);
         return st;
     }
-    // capture: per group, counter reset + the persistent trace launch (+ the FP64 pass)
+    // capture: per group, counter reset + the persistent trace launch (+ the FP64 pass); then the
+    // counters to page-locked host memory
     cudaStream_t cap = nullptr;
-    cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    cudaError_t e = cudaMallocHost(&b->host_ctr, b->plan.groups.size() * sizeof(TraceCounters));
+    if (e == cudaSuccess) memset(b->host_ctr, 0, b->plan.groups.size() * sizeof(TraceCounters));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
     Branches br;
     if (e == cudaSuccess) e = br.create();
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         cudaError_t e2 = enqueue_plan(b->plan, p, cap, ctx->sm_count, &br);
+        if (e2 == cudaSuccess)
+            e2 = cudaMemcpyAsync(b->host_ctr, b->plan.counters, b->plan.groups.size() * sizeof(TraceCounters),
+                                 cudaMemcpyDeviceToHost, cap);
         cudaError_t e3 = cudaStreamEndCapture(cap, &b->graph);
         e = e2 != cudaSuccess ? e2 : e3;
     }
@@ -1411,7 +1458,15 @@ hrt_status hrt_batch_launch(hrt_batch* b, void* stream) {
     hrt_context* ctx = b->ctx;
     DeviceSet ds(ctx->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (b->async && b->launched && cudaEventQuery(b->done) == cudaSuccess) {
+        // the previous replay has finished: report its device error before replaying again
+        uint32_t err = 0;
+        for (size_t g = 0; g < b->plan.groups.size(); ++g) err |= b->host_ctr[g].error;
+        if (hrt_status st = error_status(ctx, err)) return st;
+    }
     CK(ctx, cudaGraphLaunch(b->exec, s), "hrt_batch_launch");
+    CK(ctx, cudaEventRecord(b->done, s), "hrt_batch_launch");
+    b->launched = true;
     if (b->async) return HRT_OK;
     TraceCounters c;
     hrt_status st = read_plan_counters(ctx, b->plan, &c, s);
@@ -1456,7 +1511,14 @@ hrt_status hrt_batch_download(hrt_batch* b, float* const* rgba, void* stream, in
         CK(ctx, cudaMemcpyAsync(rgba[i], f->fb, uint64_t(f->w) * f->h * 16, cudaMemcpyDeviceToHost, s),
            "hrt_batch_download");
     }
-    if (synchronise) CK(ctx, cudaStreamSynchronize(s), "hrt_batch_download");
+    if (!synchronise) return HRT_OK;
+    CK(ctx, cudaStreamSynchronize(s), "hrt_batch_download");
+    // the replay before these copies has finished (same stream): its device error, if any
+    if (b->launched && cudaEventQuery(b->done) == cudaSuccess) {
+        uint32_t err = 0;
+        for (size_t g = 0; g < b->plan.groups.size(); ++g) err |= b->host_ctr[g].error;
+        return error_status(ctx, err);
+    }
     return HRT_OK;
 }
 
@@ -1464,6 +1526,7 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
                         uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms) {
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!scenes || !n || !base || !best) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_autotune: null or empty argument");
+    if (hrt_status ps = check_params(ctx, base, "hrt_autotune")) return ps;
     if (reps == 0) reps = 3;
     DeviceSet ds(ctx->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1547,6 +1610,8 @@ hrt_status hrt_batch_destroy(hrt_batch* b) {
     DeviceSet ds(b->ctx->device);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->host_ctr) cudaFreeHost(b->host_ctr);
     b->plan.release();
     delete b;
     return HRT_OK;

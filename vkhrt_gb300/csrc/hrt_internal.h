@@ -11,8 +11,8 @@
 namespace hrt {
 
 constexpr uint32_t kLeafFlag = 0x80000000u;
-constexpr int kStackSize = 64;          // traversal stack entries per ray
-constexpr uint32_t kMaxTraversalSteps = 1u << 16;  // per ray; exceeding it sets kErrTimeout
+constexpr int kStackSize = 64;          // traversal stack entries per ray (the most a launch may use)
+constexpr uint32_t kMaxTraversalSteps = 1u << 16;  // per ray by default; exceeding it sets kErrTimeout
 
 // Device error word bits (read back by the host after a launch).
 constexpr uint32_t kErrStackOverflow = 1u;
@@ -121,6 +121,8 @@ struct TraceLaunch {
     uint32_t refill;     // idle lanes of a warp that trigger a work fetch (0 = 16)
     uint32_t speculative;  // lanes holding a leaf keep traversing while others search
     uint32_t leaf_again;   // repeat the leaf phase while this many lanes hold leaves (0 = once)
+    uint32_t max_steps;    // traversal steps per ray (exceeding them sets kErrTimeout)
+    int32_t max_depth;     // stack entries per ray, <= kStackSize (exceeding them sets kErrStackOverflow)
     TraceCounters* counters;
     // Two-pass FP64 re-solve: the first pass lists the work items (pixels) that met a Phantom
     // candidate whose FP32 solve did not converge; the second re-renders just those with the
@@ -144,15 +146,21 @@ bool invert4(const double* m, double* out);
 // ---- launch wrappers (trace.cu) --------------------------------------------------------------
 cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count);
 cudaError_t prepare_frames();  // frame kernels' attributes (shared memory / L1 split), once per context
+// Per-ray traversal bounds of an explicit-ray launch.
+struct RayBounds {
+    uint32_t max_steps;
+    int32_t max_depth;
+};
 cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n,
-                              float tmin, float tmax, uint32_t fp64_resolve, hrt_hit* hits,
+                              float tmin, float tmax, uint32_t fp64_resolve, RayBounds bounds, hrt_hit* hits,
                               TraceCounters* counters, bool quantised_nodes, cudaStream_t s, int sm_count);
 
 // Closest hit for host rays through the static scratch array of trace.cu (no allocation);
 // error_word receives the device error bits.
 cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, uint32_t ninst, bool quantised_nodes,
                                const float* host_rays, uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
-                               hrt_hit* host_hits, cudaStream_t s, int sm_count, uint32_t* error_word);
+                               RayBounds bounds, hrt_hit* host_hits, cudaStream_t s, int sm_count,
+                               uint32_t* error_word);
 
 // ---- BVH build (build.cu) ----------------------------------------------------------------------
 // Voxel primitive record (HRT_BLAS_VOXELS): box lo + grid index (bits), box hi.

@@ -20,15 +20,17 @@ cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_
 }
 
 cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n, float tmin,
-                              float tmax, uint32_t fp64_resolve, hrt_hit* hits, TraceCounters* counters,
-                              bool quantised_nodes, cudaStream_t s, int sm_count) {
+                              float tmax, uint32_t fp64_resolve, RayBounds bounds, hrt_hit* hits,
+                              TraceCounters* counters, bool quantised_nodes, cudaStream_t s, int sm_count) {
     if (n == 0) return cudaSuccess;
     uint64_t blocks = (n + kThreads - 1) / kThreads;
     unsigned grid = unsigned(blocks < uint64_t(sm_count) * 16 ? blocks : uint64_t(sm_count) * 16);
     if (quantised_nodes)
-        trace_rays_kernel<true><<<grid, kThreads, 0, s>>>(inst, ninst, rays, n, tmin, tmax, fp64_resolve, hits, counters);
+        trace_rays_kernel<true><<<grid, kThreads, 0, s>>>(inst, ninst, rays, n, tmin, tmax, fp64_resolve, bounds, hits,
+                                                          counters);
     else
-        trace_rays_kernel<false><<<grid, kThreads, 0, s>>>(inst, ninst, rays, n, tmin, tmax, fp64_resolve, hits, counters);
+        trace_rays_kernel<false><<<grid, kThreads, 0, s>>>(inst, ninst, rays, n, tmin, tmax, fp64_resolve, bounds, hits,
+                                                           counters);
     return cudaGetLastError();
 }
 
@@ -49,7 +51,8 @@ void* g_noalloc_ptr[kMaxDevices];  // device address of g_noalloc_scratch per de
 
 cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, uint32_t ninst, bool quantised_nodes,
                                const float* host_rays, uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
-                               hrt_hit* host_hits, cudaStream_t s, int sm_count, uint32_t* error_word) {
+                               RayBounds bounds, hrt_hit* host_hits, cudaStream_t s, int sm_count,
+                               uint32_t* error_word) {
     *error_word = 0;
     if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
     void* base = nullptr;
@@ -71,7 +74,8 @@ cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, uint32_t nin
     cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(TraceCounters), s);  // the array keeps the last call's contents
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(drays, host_rays, n * 24, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && n)
-        e = launch_trace_rays(inst, ninst, drays, n, tmin, tmax, fp64_resolve, dhits, ctr, quantised_nodes, s, sm_count);
+        e = launch_trace_rays(inst, ninst, drays, n, tmin, tmax, fp64_resolve, bounds, dhits, ctr, quantised_nodes, s,
+                              sm_count);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(host_hits, dhits, n * sizeof(hrt_hit), cudaMemcpyDeviceToHost, s);
     TraceCounters c;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&c, ctr, sizeof(c), cudaMemcpyDeviceToHost, s);

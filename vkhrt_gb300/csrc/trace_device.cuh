@@ -16,8 +16,8 @@
 // (child_base, hit bits, internal-child mask) and parked leaf groups, one entry per visited
 // node at most. The explicit-ray kernel keeps a per-thread stack of (reference, entry
 // distance) with the hits of a node sorted by a sorting network. All waits are bounded: a full
-// stack or more than kMaxTraversalSteps steps ends the ray and sets a bit in the device error
-// word.
+// stack (the launch's max_depth entries, at most kStackSize) or more than the launch's max_steps
+// traversal steps ends the ray and sets a bit in the device error word.
 #pragma once
 #include <cuda_fp16.h>
 
@@ -822,12 +822,10 @@ __device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
     b = hi;
 }
 
-// Traverses one BLAS. any_hit: stop at the first accepted hit (shadow rays), skipping the
-// segment in slot `skip_slot` of instance `skip_inst` (both of its slots in a two-reference
-// BLAS).
+// Traverses one BLAS for the closest hit (explicit rays; the frame kernel has its own traversal).
 template <bool kQuant>
-__device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit& h, bool any_hit, uint32_t skip_inst,
-                         uint32_t skip_slot, bool fp64_resolve, Stats& st, uint32_t& err) {
+__device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit& h, bool fp64_resolve,
+                         RayBounds bounds, Stats& st, uint32_t& err) {
     if (B.nnodes == 0) return false;
     uint2 stack[kStackSize];
     int sp = 0;
@@ -835,22 +833,14 @@ __device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit
     bool found = false;
     uint32_t steps = 0;
     while (sp > 0) {
-        if (++steps > kMaxTraversalSteps) { err |= kErrTimeout; break; }
+        if (++steps > bounds.max_steps) { err |= kErrTimeout; break; }
         uint2 e = stack[--sp];
         if (__uint_as_float(e.y) > h.t) continue;
         if (e.x & kLeafFlag) {
             uint32_t first = (e.x & ~kLeafFlag) >> 2, cnt = (e.x & 3u) + 1u;
             for (uint32_t j = 0; j < cnt; ++j) {
-                uint32_t slot = first + j;
-                // the skipped segment's slots: its own and, with two references, its partner's
-                if (any_hit && inst == skip_inst &&
-                    (slot == skip_slot || (B.partner && slot == __ldg(&B.partner[skip_slot]))))
-                    continue;
                 ++st.prims;
-                if (leaf_test(B, slot, inst, R, h, fp64_resolve, st)) {
-                    found = true;
-                    if (any_hit) return true;
-                }
+                if (leaf_test(B, first + j, inst, R, h, fp64_resolve, st)) found = true;
             }
             continue;
         }
@@ -871,7 +861,7 @@ __device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit
         cswap(key[1], key[4]); cswap(key[3], key[6]);
         cswap(key[1], key[2]); cswap(key[3], key[4]); cswap(key[5], key[6]);
         int npush = __popc(mask);
-        if (sp + npush > kStackSize) { err |= kErrStackOverflow; break; }
+        if (sp + npush > bounds.max_depth) { err |= kErrStackOverflow; break; }
 #pragma unroll
         for (int k = 7; k >= 0; --k) {
             if (k >= npush) continue;
@@ -886,11 +876,10 @@ __device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit
     return found;
 }
 
-// World-space ray through every instance of a scene.
+// World-space ray through every instance of a scene: the closest hit.
 template <bool kQuant>
 __device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> wo, V3<float> wd, float tmin, float tmax,
-                            Hit& h, bool any_hit, uint32_t skip_inst, uint32_t skip_slot, bool fp64_resolve, Stats& st,
-                            uint32_t& err) {
+                            Hit& h, bool fp64_resolve, RayBounds bounds, Stats& st, uint32_t& err) {
     h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
     bool found = false;
     for (uint32_t i = 0; i < ninst; ++i) {
@@ -916,10 +905,7 @@ __device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> 
         }
         if (I.b.type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
         else if (I.b.type == HRT_BLAS_DOTS || I.b.type == HRT_BLAS_MESH) R.tr = make_triray(R.d);
-        if (traverse<kQuant>(I.b, i, R, h, any_hit, skip_inst, skip_slot, fp64_resolve, st, err)) {
-            found = true;
-            if (any_hit) return true;
-        }
+        if (traverse<kQuant>(I.b, i, R, h, fp64_resolve, bounds, st, err)) found = true;
     }
     return found;
 }
@@ -1346,7 +1332,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             if (!__any_sync(kFull, searching)) break;
             const bool want = searching || (spec && has_ray && leaf_bits && !stalled && more);
             if (!want) continue;
-            if (++steps > kMaxTraversalSteps) {
+            if (++steps > L.max_steps) {
                 err |= kErrTimeout;
                 sp = 0;
                 cur_bits = leaf_bits = 0;
@@ -1376,7 +1362,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             const uint32_t mask = test_node<kQuant, false>(nodes, child, R, h.t, nullptr, &base, nullptr, nullptr,
                                                            nullptr, &imask);
             const uint32_t ih = mask & imask, lh = mask & ~imask;
-            if (sp + 2 > kStackSize) {
+            if (sp + 2 > L.max_depth) {
                 err |= kErrStackOverflow;
                 sp = 0;
                 cur_bits = leaf_bits = 0;
@@ -1460,14 +1446,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
 template <bool kQuant>
 __global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance* inst, uint32_t ninst, const float* rays,
                                                               uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
-                                                              hrt_hit* hits, TraceCounters* ctr) {
+                                                              RayBounds bounds, hrt_hit* hits, TraceCounters* ctr) {
     Stats st{0, 0, 0, 0, 0};
     uint32_t err = 0;
     for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
         const float* r = rays + 6 * i;
         Hit h;
-        bool f = trace_scene<kQuant>(inst, ninst, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), tmin, tmax, h, false, 0, 0,
-                                     fp64_resolve != 0, st, err);
+        bool f = trace_scene<kQuant>(inst, ninst, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), tmin, tmax, h,
+                                     fp64_resolve != 0, bounds, st, err);
         hrt_hit o;
         o.t = f ? h.t : -1.0f;
         o.prim = f ? h.id : 0xffffffffu;
