@@ -1412,19 +1412,22 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         if (L.count_stats) { __syncwarp(); long long c = clock64(); cyc_leaf += c - clk; clk = c; }
         // ---- completion
         if (has_ray && !leaf_bits && sp == 0 && !(cur_bits & 0xffu)) {
-            if (err) {  // a bounded loop gave up: drop the task and stop taking work
+            if (err) {
+                // a bounded loop gave up: drop the task and raise the launch's error word; every
+                // warp (this one too) stops taking work at its next fetch, which reads the word,
+                // so fetch_done stays the same in all lanes of a warp (the warp-wide votes and
+                // shuffles of the loop need all 32 lanes)
                 atomicOr(&L.counters->error, err);
                 has_ray = false;
-                fetch_done = true;
-                continue;
+            } else {
+                bool more = false;
+                if (!(shadow && shadow_hit)) {
+                    const uint32_t n = L.scenes[si].ninst;
+                    while (++inst_cur < n)
+                        if (setup_instance(inst_cur)) { more = true; break; }
+                }
+                if (!more) finish_phase();
             }
-            bool more = false;
-            if (!(shadow && shadow_hit)) {
-                const uint32_t n = L.scenes[si].ninst;
-                while (++inst_cur < n)
-                    if (setup_instance(inst_cur)) { more = true; break; }
-            }
-            if (!more) finish_phase();
         }
     }
     if (kPass == 1) warp_add(&L.counters->shadow, shadow_rays);
