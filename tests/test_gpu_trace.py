@@ -236,11 +236,12 @@ def test_empty_scene_and_misses(ctx):
 def test_trace_rejects_bad_arguments(ctx):
     v, r, off = H.generate_strands(H.StrandParams(seed=60, nstrands=10, nverts=8))
     b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r, strand_offsets=off), ctx)
-    bq = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r, strand_offsets=off,
-                                                        precision=H.Precision.QUANTISED), ctx)
+    xf = np.eye(4, dtype=np.float32)
+    xf[0, 0] = 0.0  # singular
     with pytest.raises(H.HrtError) as e:
-        H.TopLevelAccelerationStructure([b, bq], ctx)
-    assert e.value.status == 6
+        H.TopLevelAccelerationStructure([H.BottomLevelAccelerationStructure(
+            H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r, strand_offsets=off, transform=xf), ctx)], ctx)
+    assert e.value.status == 1
     t = H.TopLevelAccelerationStructure([b], ctx)
     fr = H.Frame(ctx, 8, 8, 1, with_hits=False)
     with pytest.raises(H.HrtError) as e:

@@ -3,7 +3,7 @@
 Translation units compile in parallel:
   csrc/build.cu         --fmad=false (bit-exact BVH build)
   csrc/trace.cu         explicit-ray and no-allocation trace entry points
-  csrc/trace_frames.cu  frame kernels, once for FP32 nodes and once for 8-bit nodes
+  csrc/trace_frames.cu  frame kernels, once each for FP32 nodes, 8-bit nodes and per-instance formats
   csrc/api.cu           C ABI (host code)
   csrc/workload.cpp     synthetic strands and camera matrices (host, -ffp-contract=off)
 """
@@ -36,6 +36,7 @@ UNITS = {
     "trace": ("trace.cu", []),
     "trace_frames_f": ("trace_frames.cu", ["-DHRT_FRAMES_QUANT=0"]),
     "trace_frames_q": ("trace_frames.cu", ["-DHRT_FRAMES_QUANT=1"]),
+    "trace_frames_m": ("trace_frames.cu", ["-DHRT_FRAMES_QUANT=2"]),
     "api": ("api.cu", []),
     "workload": ("workload.cpp", ["-x", "c++", "-Xcompiler", "-ffp-contract=off"]),
 }

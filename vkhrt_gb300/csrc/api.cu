@@ -54,10 +54,20 @@ bool copy_u32(const uint32_t* src, uint64_t n, int32_t memory, std::vector<uint3
 struct hrt_tlas {
     hrt_context* ctx = nullptr;
     DevInstance* dev = nullptr;
-    uint32_t n = 0;
-    bool quantised = false;
-    uint32_t type_mask = 0;  // bit per hrt_geometry_type present
+    TlasNode* nodes = nullptr;  // instance BVH (null with fewer than two non-empty instances)
+    uint32_t n = 0, nnodes = 0;
+    uint32_t precision_mask = 0;  // bit per hrt_precision present
+    uint32_t type_mask = 0;       // bit per hrt_geometry_type present
 };
+
+namespace {
+// The node format a launch over BLASes of these precisions uses.
+int node_mode(uint32_t precision_mask) {
+    if (precision_mask == (1u << HRT_PRECISION_QUANTISED)) return kNodesQ;
+    if (precision_mask == 3u) return kNodesPerInstance;
+    return kNodesF;
+}
+}  // namespace
 
 struct hrt_frame {
     hrt_context* ctx = nullptr;
@@ -80,7 +90,7 @@ struct hrt_frame {
 // the groups run in stream order).
 struct ScenePlan {
     struct Group {
-        uint32_t first = 0, count = 0, type_mask = 0;
+        uint32_t first = 0, count = 0, type_mask = 0, precision_mask = 0;
         uint64_t work = 0;
     };
     std::vector<SceneLaunch> table;
@@ -88,7 +98,6 @@ struct ScenePlan {
     std::vector<Group> groups;
     uint64_t primary = 0, npix = 0, nsamp = 0, scap = 0;
     uint32_t max_spp = 1;
-    bool quant = false;
     SceneLaunch* dtable = nullptr;
     TraceCounters* counters = nullptr;
     uint32_t* list = nullptr;
@@ -211,6 +220,7 @@ void counters_to_stats(const TraceCounters& c, uint64_t primary, hrt_frame_stats
 
 void fill_scene(SceneLaunch& sl, const hrt_tlas* t, const hrt_camera* cam, hrt_frame* f, uint64_t work_begin) {
     sl.inst = t->dev;
+    sl.tlas = t->nodes;
     sl.ninst = t->n;
     sl.width = f->w;
     sl.height = f->h;
@@ -279,12 +289,9 @@ hrt_status make_plan(hrt_context* ctx, const char* who, const hrt_scene_desc* sc
                      bool need_hits, cudaStream_t s, ScenePlan& P) {
     for (uint32_t i = 0; i < n; ++i) {
         if (!scenes[i].tlas || !scenes[i].frame) return fail(ctx, HRT_ERR_INVALID_ARG, "%s: scene %u incomplete", who, i);
-        if (scenes[i].tlas->quantised != scenes[0].tlas->quantised)
-            return fail(ctx, HRT_ERR_UNSUPPORTED, "%s: scenes mix FP32 and quantised BLASes", who);
         if (need_hits && !scenes[i].frame->hits)
             return fail(ctx, HRT_ERR_INVALID_ARG, "%s: record_hits on a frame without hit records", who);
     }
-    P.quant = scenes[0].tlas->quantised;
     P.pos.assign(n, 0);
     auto key = [&](uint32_t i) -> uint32_t { return split ? prim_kind(scenes[i].tlas->type_mask) : 0u; };
     for (uint32_t k = 0; k < 4; ++k) {
@@ -296,6 +303,7 @@ hrt_status make_plan(hrt_context* ctx, const char* who, const hrt_scene_desc* sc
             fill_scene(sl, scenes[i].tlas, &scenes[i].camera, scenes[i].frame, G.work);
             G.work += sl.work_count;
             G.type_mask |= scenes[i].tlas->type_mask;
+            G.precision_mask |= scenes[i].tlas->precision_mask;
             P.pos[i] = uint32_t(P.table.size());
             P.table.push_back(sl);
             const hrt_frame* f = scenes[i].frame;
@@ -379,7 +387,7 @@ cudaError_t enqueue_plan(const ScenePlan& P, const hrt_trace_params* p, cudaStre
         if (e != cudaSuccess) return e;
         TraceLaunch L = make_launch(p, P.dtable + G.first, G.count, G.work, P.counters + g, G.type_mask, P.list,
                                     P.npix, P.scratch, P.scap, P.max_spp);
-        e = launch_trace(L, P.quant, gs[g], sm_count);
+        e = launch_trace(L, node_mode(G.precision_mask), gs[g], sm_count);
         if (e != cudaSuccess) return e;
     }
     for (int k = 0; k < naux && e == cudaSuccess; ++k) {
@@ -1148,24 +1156,70 @@ hrt_status hrt_blas_get(const hrt_blas* b, int32_t part, void* dst, uint64_t byt
     return HRT_OK;
 }
 
+namespace {
+// A float at most x (lo = true) or at least x (lo = false): the outward rounding of a box corner.
+float round_out(double x, bool lo) {
+    float f = float(x);
+    if (lo && double(f) > x) f = std::nextafter(f, -INFINITY);
+    if (!lo && double(f) < x) f = std::nextafter(f, INFINITY);
+    return f;
+}
+struct TlasItem {
+    float lo[3], hi[3];
+    double c[3];
+    uint32_t inst;
+};
+// Median-split binary BVH over items[l, r): the longest axis of the centroids' box, split at the
+// median centroid (ties by instance index, so the tree is deterministic). Returns the node index.
+uint32_t build_tlas_node(std::vector<TlasItem>& items, size_t l, size_t r, std::vector<TlasNode>& nodes) {
+    const uint32_t me = uint32_t(nodes.size());
+    nodes.emplace_back();
+    if (r - l == 1) {
+        TlasNode& n = nodes[me];
+        for (int k = 0; k < 3; ++k) { n.lo[k] = items[l].lo[k]; n.hi[k] = items[l].hi[k]; }
+        n.a = kLeafFlag | items[l].inst;
+        n.b = 0;
+        return me;
+    }
+    double clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t i = l; i < r; ++i)
+        for (int k = 0; k < 3; ++k) { clo[k] = std::min(clo[k], items[i].c[k]); chi[k] = std::max(chi[k], items[i].c[k]); }
+    int ax = 0;
+    for (int k = 1; k < 3; ++k)
+        if (chi[k] - clo[k] > chi[ax] - clo[ax]) ax = k;
+    const size_t mid = l + (r - l) / 2;
+    std::nth_element(items.begin() + l, items.begin() + mid, items.begin() + r, [ax](const TlasItem& x, const TlasItem& y) {
+        return x.c[ax] < y.c[ax] || (x.c[ax] == y.c[ax] && x.inst < y.inst);
+    });
+    const uint32_t left = build_tlas_node(items, l, mid, nodes);
+    const uint32_t right = build_tlas_node(items, mid, r, nodes);
+    TlasNode& n = nodes[me];
+    for (int k = 0; k < 3; ++k) {
+        n.lo[k] = std::min(nodes[left].lo[k], nodes[right].lo[k]);
+        n.hi[k] = std::max(nodes[left].hi[k], nodes[right].hi[k]);
+    }
+    n.a = left;
+    n.b = right;
+    return me;
+}
+}  // namespace
+
 hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint32_t n, void* stream, hrt_tlas** out) {
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!out || (n && !blases)) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_tlas_build: null argument");
     *out = nullptr;
+    if (n > kMaxInstances) return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_tlas_build: %u instances; the limit is 2^24", n);
     DeviceSet ds(ctx->device);
     std::vector<DevInstance> inst(n);
-    bool quant = false;
-    uint32_t type_mask = 0;
+    std::vector<TlasItem> items;
+    uint32_t precision_mask = 0, type_mask = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const hrt_blas* b = blases[i];
         if (!b) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_tlas_build: null BLAS %u", i);
-        bool q = b->precision == HRT_PRECISION_QUANTISED;
-        if (i == 0) quant = q;
-        else if (q != quant)
-            return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_tlas_build: FP32 and quantised BLASes cannot share a TLAS");
+        precision_mask |= 1u << b->precision;
+        type_mask |= 1u << b->type;
         DevInstance& d = inst[i];
         memset(&d, 0, sizeof(d));
-        type_mask |= 1u << b->type;
         d.b.nodes = b->out.nodes;
         d.b.prims = b->out.prims;
         d.b.verts = b->out.verts;
@@ -1185,24 +1239,58 @@ hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint3
             for (int c = 0; c < 4; ++c) d.w2o[4 * r + c] = float(iv[4 * c + r]);
         for (int r = 0; r < 3; ++r)
             for (int c = 0; c < 3; ++c) d.nrm[3 * r + c] = float(iv[4 * r + c]);  // (M^-1)^T
+        if (b->out.nnodes == 0) continue;  // nothing to hit: no TLAS leaf
+        // world box: the 8 corners of the object-space bounds through the transform (double),
+        // rounded outward
+        TlasItem it;
+        it.inst = i;
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int c = 0; c < 8; ++c) {
+            const double p[3] = {b->out.bounds[(c & 1) ? 3 : 0], b->out.bounds[(c & 2) ? 4 : 1], b->out.bounds[(c & 4) ? 5 : 2]};
+            for (int r = 0; r < 3; ++r) {
+                const double w = m[r] * p[0] + m[4 + r] * p[1] + m[8 + r] * p[2] + m[12 + r];
+                lo[r] = std::min(lo[r], w);
+                hi[r] = std::max(hi[r], w);
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            // a relative margin covers the double rounding of the transform
+            const double pad = 1e-12 * (std::fabs(lo[k]) + std::fabs(hi[k]));
+            it.lo[k] = round_out(lo[k] - pad, true);
+            it.hi[k] = round_out(hi[k] + pad, false);
+            it.c[k] = 0.5 * (lo[k] + hi[k]);
+        }
+        items.push_back(it);
+    }
+    std::vector<TlasNode> nodes;
+    if (items.size() >= 2) {
+        nodes.reserve(2 * items.size());
+        build_tlas_node(items, 0, items.size(), nodes);
     }
     hrt_tlas* t = new (std::nothrow) hrt_tlas();
     if (!t) return fail(ctx, HRT_ERR_OOM, "hrt_tlas_build: host allocation");
     t->ctx = ctx;
     t->n = n;
-    t->quantised = quant;
+    t->nnodes = uint32_t(nodes.size());
+    t->precision_mask = precision_mask;
     t->type_mask = type_mask;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaSuccess;
     if (n) {
-        cudaError_t e = cudaMalloc(&t->dev, n * sizeof(DevInstance));
+        e = cudaMalloc(&t->dev, n * sizeof(DevInstance));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(t->dev, inst.data(), n * sizeof(DevInstance), cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess && !nodes.empty()) {
+        e = cudaMalloc(&t->nodes, nodes.size() * sizeof(TlasNode));
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(t->dev, inst.data(), n * sizeof(DevInstance), cudaMemcpyHostToDevice,
-                                static_cast<cudaStream_t>(stream));
-        if (e == cudaSuccess) e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
-        if (e != cudaSuccess) {
-            if (t->dev) cudaFree(t->dev);
-            delete t;
-            return cuda_fail(ctx, e, "hrt_tlas_build");
-        }
+            e = cudaMemcpyAsync(t->nodes, nodes.data(), nodes.size() * sizeof(TlasNode), cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        if (t->dev) cudaFree(t->dev);
+        if (t->nodes) cudaFree(t->nodes);
+        delete t;
+        return cuda_fail(ctx, e, "hrt_tlas_build");
     }
     *out = t;
     return HRT_OK;
@@ -1212,6 +1300,7 @@ hrt_status hrt_tlas_destroy(hrt_tlas* t) {
     if (!t) return HRT_OK;
     DeviceSet ds(t->ctx->device);
     if (t->dev) cudaFree(t->dev);
+    if (t->nodes) cudaFree(t->nodes);
     delete t;
     return HRT_OK;
 }
@@ -1328,7 +1417,7 @@ hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* c
     CK(ctx, cudaMemsetAsync(f->counters, 0, sizeof(TraceCounters), s), "reset counters");
     TraceLaunch L = make_launch(p, f->dscene, 1, sl.work_count, f->counters, tlas->type_mask, f->resolve_list,
                                 uint64_t(f->w) * f->h, f->resolve_scratch, f->scratch_cap, f->spp);
-    CK(ctx, launch_trace(L, tlas->quantised, s, ctx->sm_count), "launch trace");
+    CK(ctx, launch_trace(L, node_mode(tlas->precision_mask), s, ctx->sm_count), "launch trace");
     f->pending_primary = uint64_t(f->w) * f->h * f->spp;
     f->stats_pending = true;
     if (p->async) return HRT_OK;
@@ -1370,8 +1459,8 @@ hrt_status hrt_trace_rays(hrt_context* ctx, const hrt_tlas* tlas, const float* r
         dh = th;
     }
     if (e == cudaSuccess)
-        e = launch_trace_rays(tlas->dev, tlas->n, dr, n, p->tmin, p->tmax, p->fp64_resolve, bounds_of(p), dh, ctr,
-                              tlas->quantised, s, ctx->sm_count);
+        e = launch_trace_rays(tlas->dev, tlas->nodes, tlas->n, dr, n, p->tmin, p->tmax, p->fp64_resolve, bounds_of(p),
+                              dh, ctr, s, ctx->sm_count);
     if (e == cudaSuccess && memory == HRT_MEMORY_HOST) e = cudaMemcpyAsync(hits, th, n * sizeof(hrt_hit), cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) {
         done();
@@ -1399,7 +1488,7 @@ hrt_status hrt_trace_rays_noalloc(hrt_context* ctx, const hrt_tlas* tlas, const 
     if (cap != cudaStreamCaptureStatusNone)
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays_noalloc: the stream is being captured");
     uint32_t err = 0;
-    cudaError_t e = trace_rays_noalloc(ctx->device, tlas->dev, tlas->n, tlas->quantised, rays, n, p->tmin, p->tmax,
+    cudaError_t e = trace_rays_noalloc(ctx->device, tlas->dev, tlas->nodes, tlas->n, rays, n, p->tmin, p->tmax,
                                        p->fp64_resolve, bounds_of(p), hits, static_cast<cudaStream_t>(stream),
                                        ctx->sm_count, &err);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "hrt_trace_rays_noalloc");

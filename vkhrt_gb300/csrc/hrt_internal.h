@@ -84,12 +84,31 @@ struct DevInstance {
     float w2o[12];   // world -> object, rows of a 3x4 affine matrix
     float nrm[9];    // object -> world normal matrix (inverse transpose, rows)
     uint32_t identity;
-    float wlo[3], whi[3];  // world-space bounds
 };
+
+// TLAS: a binary BVH over the instances' world-space boxes (the reference's driver-built
+// instance BVH, top_level_acceleration_structure.cpp:19-113), built on the host by median splits.
+// Node 0 is the root. Internal node: a = left child, b = right child; leaf: a = kLeafFlag |
+// instance index. A ray walks it with a stack of kTlasStack entries (the tree's depth is at most
+// ceil(log2(instances)) + 1, and instances are limited to 2^24).
+struct alignas(16) TlasNode {
+    float lo[3];
+    uint32_t a;
+    float hi[3];
+    uint32_t b;
+};
+static_assert(sizeof(TlasNode) == 32, "TlasNode layout");
+constexpr int kTlasStack = 32;
+constexpr uint32_t kMaxInstances = 1u << 24;
+
+// Node format of a launch's BLASes: every instance FP32, every instance 8-bit, or per instance
+// (a TLAS or a batch that mixes the two; the kernel branches on each instance's precision).
+enum NodeMode : int { kNodesF = 0, kNodesQ = 1, kNodesPerInstance = 2 };
 
 // One scene of a launch (a frame, or one scene of a batch).
 struct SceneLaunch {
     const DevInstance* inst;
+    const TlasNode* tlas;      // instance BVH (null for a scene of one instance)
     uint32_t ninst;
     uint32_t width, height, spp;
     uint32_t tiles_x;          // 8x4 pixel tiles per row
@@ -144,20 +163,20 @@ struct TraceLaunch {
 bool invert4(const double* m, double* out);
 
 // ---- launch wrappers (trace.cu) --------------------------------------------------------------
-cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count);
+cudaError_t launch_trace(const TraceLaunch& L, int node_mode, cudaStream_t s, int sm_count);
 cudaError_t prepare_frames();  // frame kernels' attributes (shared memory / L1 split), once per context
 // Per-ray traversal bounds of an explicit-ray launch.
 struct RayBounds {
     uint32_t max_steps;
     int32_t max_depth;
 };
-cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n,
-                              float tmin, float tmax, uint32_t fp64_resolve, RayBounds bounds, hrt_hit* hits,
-                              TraceCounters* counters, bool quantised_nodes, cudaStream_t s, int sm_count);
+cudaError_t launch_trace_rays(const DevInstance* inst, const TlasNode* tlas, uint32_t ninst, const float* rays,
+                              uint64_t n, float tmin, float tmax, uint32_t fp64_resolve, RayBounds bounds,
+                              hrt_hit* hits, TraceCounters* counters, cudaStream_t s, int sm_count);
 
 // Closest hit for host rays through the static scratch array of trace.cu (no allocation);
 // error_word receives the device error bits.
-cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, uint32_t ninst, bool quantised_nodes,
+cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, const TlasNode* tlas, uint32_t ninst,
                                const float* host_rays, uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
                                RayBounds bounds, hrt_hit* host_hits, cudaStream_t s, int sm_count,
                                uint32_t* error_word);

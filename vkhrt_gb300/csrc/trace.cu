@@ -2,35 +2,41 @@
 // closest hit for explicit rays, and the no-allocation variant with its static scratch.
 #include <mutex>
 
+#define HRT_RAY_KERNEL
 #include "trace_device.cuh"
 
 namespace hrt {
 
-cudaError_t launch_frames_f(const TraceLaunch& L, cudaStream_t s, int sm_count);  // trace_frames.cu
+// trace_frames.cu, compiled once per node mode: the frame kernels and their attributes (set once
+// per context)
+cudaError_t launch_frames_f(const TraceLaunch& L, cudaStream_t s, int sm_count);
 cudaError_t launch_frames_q(const TraceLaunch& L, cudaStream_t s, int sm_count);
-cudaError_t prepare_frames_f();  // trace_frames.cu: kernel attributes, once per context
+cudaError_t launch_frames_m(const TraceLaunch& L, cudaStream_t s, int sm_count);
+cudaError_t prepare_frames_f();
 cudaError_t prepare_frames_q();
+cudaError_t prepare_frames_m();
 cudaError_t prepare_frames() {
     cudaError_t e = prepare_frames_f();
-    return e == cudaSuccess ? prepare_frames_q() : e;
+    if (e == cudaSuccess) e = prepare_frames_q();
+    return e == cudaSuccess ? prepare_frames_m() : e;
 }
 
-cudaError_t launch_trace(const TraceLaunch& L, bool quantised_nodes, cudaStream_t s, int sm_count) {
-    return quantised_nodes ? launch_frames_q(L, s, sm_count) : launch_frames_f(L, s, sm_count);
+cudaError_t launch_trace(const TraceLaunch& L, int node_mode, cudaStream_t s, int sm_count) {
+    switch (node_mode) {
+        case kNodesQ: return launch_frames_q(L, s, sm_count);
+        case kNodesPerInstance: return launch_frames_m(L, s, sm_count);
+        default: return launch_frames_f(L, s, sm_count);
+    }
 }
 
-cudaError_t launch_trace_rays(const DevInstance* inst, uint32_t ninst, const float* rays, uint64_t n, float tmin,
-                              float tmax, uint32_t fp64_resolve, RayBounds bounds, hrt_hit* hits,
-                              TraceCounters* counters, bool quantised_nodes, cudaStream_t s, int sm_count) {
+cudaError_t launch_trace_rays(const DevInstance* inst, const TlasNode* tlas, uint32_t ninst, const float* rays,
+                              uint64_t n, float tmin, float tmax, uint32_t fp64_resolve, RayBounds bounds,
+                              hrt_hit* hits, TraceCounters* counters, cudaStream_t s, int sm_count) {
     if (n == 0) return cudaSuccess;
     uint64_t blocks = (n + kThreads - 1) / kThreads;
     unsigned grid = unsigned(blocks < uint64_t(sm_count) * 16 ? blocks : uint64_t(sm_count) * 16);
-    if (quantised_nodes)
-        trace_rays_kernel<true><<<grid, kThreads, 0, s>>>(inst, ninst, rays, n, tmin, tmax, fp64_resolve, bounds, hits,
-                                                          counters);
-    else
-        trace_rays_kernel<false><<<grid, kThreads, 0, s>>>(inst, ninst, rays, n, tmin, tmax, fp64_resolve, bounds, hits,
-                                                           counters);
+    trace_rays_kernel<<<grid, kThreads, 0, s>>>(inst, tlas, ninst, rays, n, tmin, tmax, fp64_resolve, bounds, hits,
+                                                counters);
     return cudaGetLastError();
 }
 
@@ -49,7 +55,7 @@ std::mutex g_noalloc_mutex;
 void* g_noalloc_ptr[kMaxDevices];  // device address of g_noalloc_scratch per device (null until set up)
 }  // namespace
 
-cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, uint32_t ninst, bool quantised_nodes,
+cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, const TlasNode* tlas, uint32_t ninst,
                                const float* host_rays, uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
                                RayBounds bounds, hrt_hit* host_hits, cudaStream_t s, int sm_count,
                                uint32_t* error_word) {
@@ -74,8 +80,7 @@ cudaError_t trace_rays_noalloc(int device, const DevInstance* inst, uint32_t nin
     cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(TraceCounters), s);  // the array keeps the last call's contents
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(drays, host_rays, n * 24, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && n)
-        e = launch_trace_rays(inst, ninst, drays, n, tmin, tmax, fp64_resolve, bounds, dhits, ctr, quantised_nodes, s,
-                              sm_count);
+        e = launch_trace_rays(inst, tlas, ninst, drays, n, tmin, tmax, fp64_resolve, bounds, dhits, ctr, s, sm_count);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(host_hits, dhits, n * sizeof(hrt_hit), cudaMemcpyDeviceToHost, s);
     TraceCounters c;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&c, ctr, sizeof(c), cudaMemcpyDeviceToHost, s);

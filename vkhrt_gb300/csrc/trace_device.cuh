@@ -808,6 +808,38 @@ __device__ __forceinline__ uint4 node_header(const void* nodes, uint32_t ni) {
     return make_uint4(t.x, t.y, m.x, m.y);
 }
 
+// The node test and header of either format: kNodes fixes it for the launch (kNodesF, kNodesQ), or
+// kNodesPerInstance picks it from the current instance (q).
+template <int kNodes>
+__device__ __forceinline__ uint32_t test_node_of(const void* nodes, bool q, uint32_t ni, const RayState& R, float tfar,
+                                                 uint32_t* base, uint32_t* imask) {
+    if (kNodes == kNodesPerInstance)
+        return q ? test_node<true, false>(nodes, ni, R, tfar, nullptr, base, nullptr, nullptr, nullptr, imask)
+                 : test_node<false, false>(nodes, ni, R, tfar, nullptr, base, nullptr, nullptr, nullptr, imask);
+    return test_node<kNodes == kNodesQ, false>(nodes, ni, R, tfar, nullptr, base, nullptr, nullptr, nullptr, imask);
+}
+template <int kNodes>
+__device__ __forceinline__ uint4 node_header_of(const void* nodes, bool q, uint32_t ni) {
+    if (kNodes == kNodesPerInstance) return q ? node_header<true>(nodes, ni) : node_header<false>(nodes, ni);
+    return node_header<kNodes == kNodesQ>(nodes, ni);
+}
+
+// A TLAS node's world box against the world ray (o, inv) within [tmin, tfar], with the relative
+// slack of the FP32 node test (rounding only admits extra boxes).
+__device__ __forceinline__ bool tlas_box_hit(const TlasNode* nodes, uint32_t ni, V3<float> o, V3<float> inv, float tmin,
+                                             float tfar, uint32_t* a, uint32_t* b) {
+    const float4 lo = __ldg(reinterpret_cast<const float4*>(nodes + ni));
+    const float4 hi = __ldg(reinterpret_cast<const float4*>(nodes + ni) + 1);
+    *a = __float_as_uint(lo.w);
+    *b = __float_as_uint(hi.w);
+    const float x0 = (lo.x - o.x) * inv.x, x1 = (hi.x - o.x) * inv.x;
+    const float y0 = (lo.y - o.y) * inv.y, y1 = (hi.y - o.y) * inv.y;
+    const float z0 = (lo.z - o.z) * inv.z, z1 = (hi.z - o.z) * inv.z;
+    const float n = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
+    const float f = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tfar));
+    return n <= f * (1.0f + 9.5367431640625e-07f);
+}
+
 // Slot-order mask -> traversal order for a ray of direction octant oct: bit i <- bit i ^ oct.
 __device__ __forceinline__ uint32_t oct_permute(uint32_t m, uint32_t oct) {
     if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
@@ -876,13 +908,34 @@ __device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit
     return found;
 }
 
-// World-space ray through every instance of a scene: the closest hit.
-template <bool kQuant>
-__device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> wo, V3<float> wd, float tmin, float tmax,
-                            Hit& h, bool fp64_resolve, RayBounds bounds, Stats& st, uint32_t& err) {
+// World-space ray through the instances of a scene (the TLAS's, or the one instance): the closest
+// hit. Each instance is traversed in its own node format.
+__device__ bool trace_scene(const DevInstance* insts, const TlasNode* tlas, uint32_t ninst, V3<float> wo, V3<float> wd,
+                            float tmin, float tmax, Hit& h, bool fp64_resolve, RayBounds bounds, Stats& st,
+                            uint32_t& err) {
     h = Hit{tmax, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0.0f, 0.0f, 0.0f, 0u};
     bool found = false;
-    for (uint32_t i = 0; i < ninst; ++i) {
+    uint32_t tstack[kTlasStack];
+    int tsp = 0;
+    const V3<float> winv = safe_inv(wd);
+    if (tlas) tstack[tsp++] = 0;
+    for (uint32_t k = 0;; ++k) {
+        uint32_t i;
+        if (tlas) {  // the next instance whose world box the ray meets before the closest hit
+            i = 0xffffffffu;
+            while (tsp > 0) {
+                uint32_t a, b;
+                if (!tlas_box_hit(tlas, tstack[--tsp], wo, winv, tmin, h.t, &a, &b)) continue;
+                if (a & kLeafFlag) { i = a & ~kLeafFlag; break; }
+                if (tsp + 2 > kTlasStack) { err |= kErrStackOverflow; tsp = 0; break; }
+                tstack[tsp++] = b;
+                tstack[tsp++] = a;
+            }
+            if (i == 0xffffffffu) break;
+        } else {
+            if (k >= ninst) break;
+            i = k;
+        }
         const DevInstance& I = insts[i];
         RayState R;
         if (I.identity) { R.o = wo; R.d = wd; }
@@ -905,7 +958,9 @@ __device__ bool trace_scene(const DevInstance* insts, uint32_t ninst, V3<float> 
         }
         if (I.b.type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
         else if (I.b.type == HRT_BLAS_DOTS || I.b.type == HRT_BLAS_MESH) R.tr = make_triray(R.d);
-        if (traverse<kQuant>(I.b, i, R, h, fp64_resolve, bounds, st, err)) found = true;
+        const bool f = I.b.precision == HRT_PRECISION_QUANTISED ? traverse<true>(I.b, i, R, h, fp64_resolve, bounds, st, err)
+                                                               : traverse<false>(I.b, i, R, h, fp64_resolve, bounds, st, err);
+        if (f) found = true;
     }
     return found;
 }
@@ -1079,7 +1134,7 @@ constexpr int kRefill = 16;
 
 // kPass 1: the frame (non-converged Phantom candidates flag their pixel); kPass 2: the listed
 // pixels again, with the FP64 re-solve inline (adds only the FP64 counts).
-template <bool kQuant, int kType, int kMinBlocks, int kPass>
+template <int kNodes, int kType, int kMinBlocks, int kPass>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch L) {
     __shared__ uint2 s_stack[kShort][kThreads];
     uint2 l_stack[kStackSize - kShort];
@@ -1104,6 +1159,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     int sp = 0;
     uint32_t steps = 0;
     const void* nodes = nullptr;                 // node array of the current instance's BLAS
+    bool qnodes = false;                         // its format (kNodesPerInstance launches)
+    uint32_t tstack[kTlasStack];                 // TLAS walk of a multi-instance scene (local memory)
+    int tsp = 0;
     uint32_t oct = 0;                            // direction octant of the object-space ray
     uint32_t cur_base = 0, cur_bits = 0;         // node group: hits in visiting order (bits 0-7), imask (8-15)
     uint32_t leaf_node = 0, leaf_bits = 0;       // untested leaf children of node leaf_node, visiting order
@@ -1140,10 +1198,40 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         if (type == HRT_BLAS_PHANTOM) R.F = make_frame(R.d);
         else if (type == HRT_BLAS_DOTS || type == HRT_BLAS_MESH) R.tr = make_triray(R.d);
         nodes = B.nodes;
+        if (kNodes == kNodesPerInstance) qnodes = B.precision == HRT_PRECISION_QUANTISED;
         oct = (R.inv.x < 0.0f ? 1u : 0u) | (R.inv.y < 0.0f ? 2u : 0u) | (R.inv.z < 0.0f ? 4u : 0u);
         cur_base = 0;  // the root as a group of one internal child in slot 0
         cur_bits = (1u << oct) | (1u << 8);
         return true;
+    };
+    // The ray's next instance: of a multi-instance scene, the next TLAS leaf whose world box the
+    // ray meets before its closest hit (set up, root pushed); of a one-instance scene, the next
+    // index. False when there is none.
+    auto next_instance = [&]() -> bool {
+        const SceneLaunch& S = L.scenes[si];
+        if (!S.tlas) {
+            while (++inst_cur < S.ninst)
+                if (setup_instance(inst_cur)) return true;
+            return false;
+        }
+        const V3<float> winv = safe_inv(wd);
+        while (tsp > 0) {
+            uint32_t a, b;
+            if (!tlas_box_hit(S.tlas, tstack[--tsp], wo, winv, cur_tmin, h.t, &a, &b)) continue;
+            if (a & kLeafFlag) {
+                inst_cur = a & ~kLeafFlag;
+                if (setup_instance(inst_cur)) return true;
+                continue;
+            }
+            if (tsp + 2 > kTlasStack) {  // deeper than a TLAS is built (bounded all the same)
+                err |= kErrStackOverflow;
+                tsp = 0;
+                return false;
+            }
+            tstack[tsp++] = b;
+            tstack[tsp++] = a;
+        }
+        return false;
     };
     auto start_ray = [&](V3<float> o, V3<float> d, float tmin, float tmax) {
         wo = o;
@@ -1154,9 +1242,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         cur_bits = 0;
         leaf_bits = 0;
         steps = 0;
-        const uint32_t n = L.scenes[si].ninst;
-        for (inst_cur = 0; inst_cur < n; ++inst_cur)
-            if (setup_instance(inst_cur)) break;
+        const SceneLaunch& S = L.scenes[si];
+        if (S.tlas) {
+            tsp = 0;
+            tstack[tsp++] = 0;
+            next_instance();
+        } else {
+            for (inst_cur = 0; inst_cur < S.ninst; ++inst_cur)
+                if (setup_instance(inst_cur)) break;
+        }
     };
     auto start_primary = [&]() {
         const SceneLaunch& S = L.scenes[si];
@@ -1359,8 +1453,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             const uint32_t child = cur_base + __popc((cur_bits >> 8) & ((1u << slot) - 1u));
             ++st.nodes;
             uint32_t base, imask;
-            const uint32_t mask = test_node<kQuant, false>(nodes, child, R, h.t, nullptr, &base, nullptr, nullptr,
-                                                           nullptr, &imask);
+            const uint32_t mask = test_node_of<kNodes>(nodes, qnodes, child, R, h.t, &base, &imask);
             const uint32_t ih = mask & imask, lh = mask & ~imask;
             if (sp + 2 > L.max_depth) {
                 err |= kErrStackOverflow;
@@ -1393,7 +1486,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             const DevBlas& B = L.scenes[si].inst[inst_cur].b;
             const uint32_t q = (__ffs(leaf_bits) - 1) ^ oct;
             leaf_bits &= leaf_bits - 1u;
-            const uint4 hd = node_header<kQuant>(nodes, leaf_node);
+            const uint4 hd = node_header_of<kNodes>(nodes, qnodes, leaf_node);
             const uint32_t m = ((q < 4 ? hd.z : hd.w) >> (8 * (q & 3))) & 0xffu;
             const uint32_t first = hd.y + (m & 31u), cnt = m >> 5;
             for (uint32_t j = 0; j < cnt; ++j) {
@@ -1420,12 +1513,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 atomicOr(&L.counters->error, err);
                 has_ray = false;
             } else {
-                bool more = false;
-                if (!(shadow && shadow_hit)) {
-                    const uint32_t n = L.scenes[si].ninst;
-                    while (++inst_cur < n)
-                        if (setup_instance(inst_cur)) { more = true; break; }
-                }
+                const bool more = !(shadow && shadow_hit) && next_instance();
                 if (!more) finish_phase();
             }
         }
@@ -1446,17 +1534,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     if (err) atomicOr(&L.counters->error, err);
 }
 
-template <bool kQuant>
-__global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance* inst, uint32_t ninst, const float* rays,
-                                                              uint64_t n, float tmin, float tmax, uint32_t fp64_resolve,
-                                                              RayBounds bounds, hrt_hit* hits, TraceCounters* ctr) {
+#ifdef HRT_RAY_KERNEL  // compiled by trace.cu only
+__global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance* inst, const TlasNode* tlas,
+                                                              uint32_t ninst, const float* rays, uint64_t n, float tmin,
+                                                              float tmax, uint32_t fp64_resolve, RayBounds bounds,
+                                                              hrt_hit* hits, TraceCounters* ctr) {
     Stats st{0, 0, 0, 0, 0};
     uint32_t err = 0;
     for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
         const float* r = rays + 6 * i;
         Hit h;
-        bool f = trace_scene<kQuant>(inst, ninst, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), tmin, tmax, h,
-                                     fp64_resolve != 0, bounds, st, err);
+        bool f = trace_scene(inst, tlas, ninst, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), tmin, tmax, h,
+                             fp64_resolve != 0, bounds, st, err);
         hrt_hit o;
         o.t = f ? h.t : -1.0f;
         o.prim = f ? h.id : 0xffffffffu;
@@ -1468,56 +1557,63 @@ __global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance*
     warp_add(&ctr->fp64_hits, st.h64);
     if (err) atomicOr(&ctr->error, err);
 }
+#endif
 
 // Shared memory / L1 split of the SM for a frame kernel: 40 % asks for the 100 KB shared
 // configuration, which holds up to five blocks' short stacks (17 KB each), and leaves the rest of
 // the array to L1 for the node and record loads (0.2-0.8 % faster than the default split; the
 // largest L1 split cuts the resident blocks, the largest shared split is 2-4 % slower). Set once
 // per kernel when the context is created (not during a graph capture).
-template <bool kQuant, int kType, int kMinBlocks, int kPass>
+template <int kNodes, int kType, int kMinBlocks, int kPass>
 cudaError_t set_carveout() {
-    return cudaFuncSetAttribute(frame_kernel<kQuant, kType, kMinBlocks, kPass>,
+    return cudaFuncSetAttribute(frame_kernel<kNodes, kType, kMinBlocks, kPass>,
                                 cudaFuncAttributePreferredSharedMemoryCarveout, 40);
 }
-template <bool kQuant>
+template <int kNodes>
 cudaError_t prepare_frame_kernels() {
     cudaError_t e = cudaSuccess;
-    auto all = [&](auto minb) {
-        constexpr int kB = decltype(minb)::value;
-        if (e == cudaSuccess) e = set_carveout<kQuant, HRT_BLAS_PHANTOM, kB, 1>();
-        if (e == cudaSuccess) e = set_carveout<kQuant, HRT_BLAS_LSS, kB, 1>();
-        if (e == cudaSuccess) e = set_carveout<kQuant, HRT_BLAS_DOTS, kB, 1>();
-        if (e == cudaSuccess) e = set_carveout<kQuant, kMixed, kB, 1>();
-    };
-    all(std::integral_constant<int, 3>{});
-    all(std::integral_constant<int, 4>{});
-    all(std::integral_constant<int, 5>{});
-    if (e == cudaSuccess) e = set_carveout<kQuant, HRT_BLAS_PHANTOM, 1, 2>();
-    if (e == cudaSuccess) e = set_carveout<kQuant, kMixed, 1, 2>();
-    return e;
+    if constexpr (kNodes == kNodesPerInstance) {  // the mixed-type kernel only
+        e = set_carveout<kNodes, kMixed, 4, 1>();
+        if (e == cudaSuccess) e = set_carveout<kNodes, kMixed, 1, 2>();
+        return e;
+    } else {
+        auto all = [&](auto minb) {
+            constexpr int kB = decltype(minb)::value;
+            if (e == cudaSuccess) e = set_carveout<kNodes, HRT_BLAS_PHANTOM, kB, 1>();
+            if (e == cudaSuccess) e = set_carveout<kNodes, HRT_BLAS_LSS, kB, 1>();
+            if (e == cudaSuccess) e = set_carveout<kNodes, HRT_BLAS_DOTS, kB, 1>();
+            if (e == cudaSuccess) e = set_carveout<kNodes, kMixed, kB, 1>();
+        };
+        all(std::integral_constant<int, 3>{});
+        all(std::integral_constant<int, 4>{});
+        all(std::integral_constant<int, 5>{});
+        if (e == cudaSuccess) e = set_carveout<kNodes, HRT_BLAS_PHANTOM, 1, 2>();
+        if (e == cudaSuccess) e = set_carveout<kNodes, kMixed, 1, 2>();
+        return e;
+    }
 }
 
-template <bool kQuant, int kType, int kMinBlocks, int kPass>
+template <int kNodes, int kType, int kMinBlocks, int kPass>
 cudaError_t launch_frame(const TraceLaunch& L, cudaStream_t s, int sm_count) {
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, frame_kernel<kQuant, kType, kMinBlocks, kPass>, kThreads, 0);
+        &per_sm, frame_kernel<kNodes, kType, kMinBlocks, kPass>, kThreads, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     unsigned grid = unsigned(sm_count * per_sm);
     uint64_t max_blocks = (L.total_work + kThreads - 1) / kThreads;
     if (grid > max_blocks) grid = unsigned(max_blocks ? max_blocks : 1);
-    frame_kernel<kQuant, kType, kMinBlocks, kPass><<<grid, kThreads, 0, s>>>(L);
+    frame_kernel<kNodes, kType, kMinBlocks, kPass><<<grid, kThreads, 0, s>>>(L);
     return cudaGetLastError();
 }
 
-template <bool kQuant, int kMinBlocks>
+template <int kNodes, int kMinBlocks>
 cudaError_t launch_kind(const TraceLaunch& L, cudaStream_t s, int sm_count) {
     switch (L.prim_kind) {  // one primitive type in every instance -> the specialised kernel
-        case HRT_BLAS_PHANTOM: return launch_frame<kQuant, HRT_BLAS_PHANTOM, kMinBlocks, 1>(L, s, sm_count);
-        case HRT_BLAS_LSS: return launch_frame<kQuant, HRT_BLAS_LSS, kMinBlocks, 1>(L, s, sm_count);
-        case HRT_BLAS_DOTS: return launch_frame<kQuant, HRT_BLAS_DOTS, kMinBlocks, 1>(L, s, sm_count);
-        default: return launch_frame<kQuant, kMixed, kMinBlocks, 1>(L, s, sm_count);
+        case HRT_BLAS_PHANTOM: return launch_frame<kNodes, HRT_BLAS_PHANTOM, kMinBlocks, 1>(L, s, sm_count);
+        case HRT_BLAS_LSS: return launch_frame<kNodes, HRT_BLAS_LSS, kMinBlocks, 1>(L, s, sm_count);
+        case HRT_BLAS_DOTS: return launch_frame<kNodes, HRT_BLAS_DOTS, kMinBlocks, 1>(L, s, sm_count);
+        default: return launch_frame<kNodes, kMixed, kMinBlocks, 1>(L, s, sm_count);
     }
 }
 
@@ -1548,12 +1644,13 @@ __global__ void __launch_bounds__(kThreads) resolve_average_kernel(TraceLaunch L
 }
 
 // The FP64 pass: only launches that hold Phantom BLASes can list pixels.
-template <bool kQuant>
+template <int kNodes>
 cudaError_t launch_resolve(const TraceLaunch& L, cudaStream_t s, int sm_count) {
     if (!L.fp64_resolve || !L.resolve_list) return cudaSuccess;
     cudaError_t e = cudaSuccess;
-    if (L.prim_kind == HRT_BLAS_PHANTOM) e = launch_frame<kQuant, HRT_BLAS_PHANTOM, 1, 2>(L, s, sm_count);
-    else if (L.prim_kind == kMixed) e = launch_frame<kQuant, kMixed, 1, 2>(L, s, sm_count);
+    if (kNodes != kNodesPerInstance && L.prim_kind == HRT_BLAS_PHANTOM)
+        e = launch_frame<kNodes, kNodes == kNodesPerInstance ? kMixed : HRT_BLAS_PHANTOM, 1, 2>(L, s, sm_count);
+    else if (kNodes == kNodesPerInstance || L.prim_kind == kMixed) e = launch_frame<kNodes, kMixed, 1, 2>(L, s, sm_count);
     else return cudaSuccess;
     if (e != cudaSuccess || !L.resolve_scratch) return e;
     resolve_average_kernel<<<unsigned(sm_count), kThreads, 0, s>>>(L);
