@@ -990,7 +990,7 @@ static std::atomic<int64_t> g_stat[4];
 // Closest-hit order: smaller t, then smaller instance, then smaller primitive id.
 template <class T>
 static bool intersect_prim(const Blas& b, uint32_t inst, uint32_t s, const tvec3<T>& o, const tvec3<T>& d, T tmin,
-                           HitT<T>* h, int resolve64) {
+                           HitT<T>* h, int resolve64, bool unit_dir) {
     bool better = false;
     auto take = [&](T t, uint32_t prim, T u, int r64) {
         if (!(t >= tmin) || !(t <= h->t)) return;
@@ -1002,20 +1002,29 @@ static bool intersect_prim(const Blas& b, uint32_t inst, uint32_t s, const tvec3
         const float* c = b.data.data() + 12 * s;
         Curve<T> cv{tvec3<T>(T(c[0]), T(c[1]), T(c[2])), tvec3<T>(T(c[3]), T(c[4]), T(c[5])),
                     tvec3<T>(T(c[6]), T(c[7]), T(c[8])), tvec3<T>(T(c[9]), T(c[10]), T(c[11]))};
-        Ray<T> ray{o, d};
+        // Prhi measures the hit as a length along the ray's unit direction (the reference runs it
+        // on the unit world ray, hair_intersection.rint:138-141). The object-space ray of a
+        // transformed instance is o + t d with |d| != 1: Prhi runs on the unit direction and its
+        // length becomes the parameter t = length / |d|, so hits compare across instances.
+        const T dlen = unit_dir ? T(1) : shim::length(d);
+        Ray<T> ray{o, unit_dir ? d : d * (T(1) / dlen)};
         int st;
         tvec3<T> nrm;
         bool shift = (resolve64 & 2) != 0, polish = (resolve64 & 4) != 0;
         T t = prhi(ray, cv, T(b.radius[2 * s]), T(b.radius[2 * s + 1]), &nrm, &st, shift, polish);
+        if (!unit_dir) t = t / dlen;
         if (st == kUnresolved || st == kUnresolvedNear) g_stat[st == kUnresolved ? 0 : 1]++;
         if (st == kHit) { take(t, s, T(0), 0); if (better) h->n = nrm; }
         else if (st == kUnresolvedNear && (resolve64 & 1)) {  // failed convergence test only
             Curve<double> cd{tvec3<double>(c[0], c[1], c[2]), tvec3<double>(c[3], c[4], c[5]),
                              tvec3<double>(c[6], c[7], c[8]), tvec3<double>(c[9], c[10], c[11])};
-            Ray<double> rd{tvec3<double>(o.x, o.y, o.z), tvec3<double>(d.x, d.y, d.z)};
+            const double dl2 = unit_dir ? 1.0 : double(dlen);
+            Ray<double> rd{tvec3<double>(o.x, o.y, o.z), tvec3<double>(double(ray.direction.x), double(ray.direction.y),
+                                                                      double(ray.direction.z))};
             int st2;
             tvec3<double> n2;
             double t2 = prhi(rd, cd, double(b.radius[2 * s]), double(b.radius[2 * s + 1]), &n2, &st2, shift, polish);
+            if (!unit_dir) t2 = t2 / dl2;
             if (st2 == kHit) {
                 g_stat[st == kUnresolved ? 2 : 3]++;
                 take(T(t2), s, T(0), 1);
@@ -1134,7 +1143,7 @@ static bool trace_one(const Scene& sc, const tvec3<T>& wo, const tvec3<T>& wd, T
                 uint32_t s = b.sorted[cur & 0x7fffffffu];
                 bool skip = any_hit && ii == skip_inst && s == skip_seg;
                 if (!skip) {
-                    if (intersect_prim(b, ii, s, o, d, tmin, &h, resolve64)) {
+                    if (intersect_prim(b, ii, s, o, d, tmin, &h, resolve64, in.identity)) {
                         found = true;
                         if (!in.identity) {
                             double pn[3] = {double(h.n.x), double(h.n.y), double(h.n.z)};

@@ -400,3 +400,27 @@ def test_shifted_origin_fp64_agrees_with_the_literal_fp64_prhi(orc, spread):
         near[:, :3] += near[:, 3:] * np.float32(dist - 0.3)
         c = sc.trace_rays(near, precision=6400)
         assert np.array_equal(c[1][c[0] >= 0], a[1][idx][c[0] >= 0]) and (c[0] >= 0).all()
+
+
+def test_scaled_instance_phantom_distances_are_ray_parameters(orc):
+    """A transformed instance's object-space ray is o + t d with |d| != 1 under scaling. The
+    oracle runs Prhi on the unit direction and converts its length to the parameter t, so a
+    uniformly scaled, rotated and moved Phantom instance hits exactly where the same curves
+    transformed into world space (radii scaled alike) are hit."""
+    import vkhrt_gb300 as H
+    from hairscene import aimed_rays, compare_hits, oracle_geometry
+    v, r, off = H.generate_strands(H.StrandParams(seed=90, nstrands=200, nverts=16), lib=H.bind_workload(orc))
+    lines, lrad = lines_from_strands(v, r, off)
+    curves, rad = oracle_geometry(orc, PHANTOM, lines, lrad)
+    s = 0.2
+    c, sn = np.cos(0.7), np.sin(0.7)
+    xf = np.array([[s * c, 0, s * sn, 0.3], [0, s, 0, -0.1], [-s * sn, 0, s * c, 0.2], [0, 0, 0, 1]], np.float64)
+    world = (curves.reshape(-1, 3).astype(np.float64) @ xf[:3, :3].T + xf[:3, 3]).reshape(-1, 12).astype(np.float32)
+    a = OracleScene(orc, [(PHANTOM, curves, rad)], [xf.astype(np.float32)])
+    b = OracleScene(orc, [(PHANTOM, world, (rad * np.float32(s)).astype(np.float32))])
+    wl = (lines.reshape(-1, 3).astype(np.float64) @ xf[:3, :3].T + xf[:3, 3]).reshape(-1, 6).astype(np.float32)
+    rays = aimed_rays(np.random.default_rng(2), wl, 10000, spread=0.001)
+    ta, pa, ia, _ = a.trace_rays(rays, precision=64)
+    tb, pb, ib, _ = b.trace_rays(rays, precision=64)
+    st = compare_hits(ta, pa, ia, tb, pb, ib)
+    assert st["hits"] > 2000 and st["agreement"] >= 0.999 and st["p9999_rel_t"] <= 1e-6, st

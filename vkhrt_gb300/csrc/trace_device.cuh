@@ -163,11 +163,13 @@ template <class T> struct PrhiOut {  // s = ts + sl
 
 // ray.glsl:13-17 MakeOrthonormalBasis; the RCC transform (ray.glsl:19-33) is the inverse of
 // [e1 e2 e3 | o], applied here as the transpose of the orthonormal frame after the translation.
-template <class T> struct Frame { V3<T> e1, e2, e3; T inv_dd; };
+// inv_len = 1 / |d|: distances along e3 are lengths, the ray's parameter is length / |d| (the
+// object-space direction of a scaled instance is not a unit vector).
+template <class T> struct Frame { V3<T> e1, e2, e3; T inv_len; };
 template <class T> __device__ __forceinline__ Frame<T> make_frame(V3<T> d) {
     Frame<T> f;
-    f.inv_dd = T(1) / dot(d, d);
-    f.e3 = normalize(d);
+    f.inv_len = rsq(dot(d, d));
+    f.e3 = f.inv_len * d;
     V3<T> w = f.e3;
     f.e2 = gabs(w.x) > gabs(w.y) ? normalize(mk(-w.z, T(0), w.x)) : normalize(mk(T(0), w.z, -w.y));
     f.e1 = cross(f.e2, w);
@@ -224,7 +226,7 @@ __device__ __forceinline__ PrhiOut<T> prhi_solve(const Frame<T>& F, const V3<T>*
             T s = prhi_div(b - (isect ? prhi_sqrt(det) : T(0)), cc);
             T dt = prhi_div(s * ax.z - cdd, ddd);
             if (isect && gabs(dt) < T(5e-5)) {
-                out.sl = s + c.z;
+                out.sl = (s + c.z) * F.inv_len;  // length along e3 -> the ray's parameter
                 out.s = out.sl + out.ts;
                 out.tc = t;
                 exhausted = false;
@@ -261,14 +263,16 @@ __device__ __forceinline__ PrhiOut<float> prhi_diff(const Frame<float>& F, V3<fl
                                                     V3<float> D1, V3<float> D2, V3<float> ch, float r0, float r1) {
     PrhiOut<float> out{0.0f, 0.0f, 0.0f, 0.0f, kMiss};
     const V3<float> cm = mk(fmaf(0.5f, ch.x, P0.x), fmaf(0.5f, ch.y, P0.y), fmaf(0.5f, ch.z, P0.z));
-    const float ts = dot(cm - o, d) * F.inv_dd;
+    const float ts = dot(cm - o, d) * (F.inv_len * F.inv_len);
     out.ts = ts;
     const V3<float> cr = cross(ch, D1 + D2);
     const float chch = dot(ch, ch);
     const float rmax = 0.375f * prhi_sqrt(prhi_div(dot(cr, cr), chch)) + gmax(r0, r1);
     V3<float> W[4];
     W[0] = mk(rel_coord(P0.x, o.x, ts, d.x), rel_coord(P0.y, o.y, ts, d.y), rel_coord(P0.z, o.z, ts, d.z));
-    if (!ray_cylinder0(d, W[0], ch, chch, rmax)) return out;
+    // the capped-cylinder test (cylinder.glsl) takes a unit direction: e3, the ray's own for a
+    // unit d, the normalised object-space direction of a scaled instance
+    if (!ray_cylinder0(F.e3, W[0], ch, chch, rmax)) return out;
     W[1] = W[0] + D1;
     W[2] = W[0] + D2;
     W[3] = W[0] + ch;
@@ -284,7 +288,7 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
     } else {
         PrhiOut<T> out{T(0), T(0), T(0), T(0), kMiss};
         V3<T> cm = T(0.5) * (P[0] + P[3]);
-        T ts = dot(cm - o, d) * F.inv_dd;
+        T ts = dot(cm - o, d) * (F.inv_len * F.inv_len);
         out.ts = ts;
         // the end points first: the bounding-cylinder early-out needs only them
         V3<T> W[4];
@@ -294,7 +298,7 @@ __device__ __forceinline__ PrhiOut<T> prhi(const Frame<T>& F, V3<T> o, V3<T> d, 
 #pragma unroll
         for (int k = 0; k < 4; k += 3)
             W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
-        if (!ray_cylinder(mk(T(0), T(0), T(0)), d, W[0], W[3], rmax)) return out;
+        if (!ray_cylinder(mk(T(0), T(0), T(0)), F.e3, W[0], W[3], rmax)) return out;
 #pragma unroll
         for (int k = 1; k < 3; ++k)
             W[k] = mk(rel_coord(P[k].x, o.x, ts, d.x), rel_coord(P[k].y, o.y, ts, d.y), rel_coord(P[k].z, o.z, ts, d.z));
