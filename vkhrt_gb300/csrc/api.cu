@@ -61,10 +61,11 @@ struct hrt_tlas {
 };
 
 namespace {
-// The node format a launch over BLASes of these precisions uses.
-int node_mode(uint32_t precision_mask) {
+// The frame-kernel build a launch uses: one node format when all its BLASes share it and every
+// scene has one instance; otherwise the build that walks TLASes and takes each instance's format.
+int node_mode(uint32_t precision_mask, bool any_tlas) {
+    if (any_tlas || precision_mask == 3u) return kNodesPerInstance;
     if (precision_mask == (1u << HRT_PRECISION_QUANTISED)) return kNodesQ;
-    if (precision_mask == 3u) return kNodesPerInstance;
     return kNodesF;
 }
 }  // namespace
@@ -91,6 +92,7 @@ struct hrt_frame {
 struct ScenePlan {
     struct Group {
         uint32_t first = 0, count = 0, type_mask = 0, precision_mask = 0;
+        bool any_tlas = false;
         uint64_t work = 0;
     };
     std::vector<SceneLaunch> table;
@@ -304,6 +306,7 @@ hrt_status make_plan(hrt_context* ctx, const char* who, const hrt_scene_desc* sc
             G.work += sl.work_count;
             G.type_mask |= scenes[i].tlas->type_mask;
             G.precision_mask |= scenes[i].tlas->precision_mask;
+            G.any_tlas |= scenes[i].tlas->nodes != nullptr;
             P.pos[i] = uint32_t(P.table.size());
             P.table.push_back(sl);
             const hrt_frame* f = scenes[i].frame;
@@ -387,7 +390,7 @@ cudaError_t enqueue_plan(const ScenePlan& P, const hrt_trace_params* p, cudaStre
         if (e != cudaSuccess) return e;
         TraceLaunch L = make_launch(p, P.dtable + G.first, G.count, G.work, P.counters + g, G.type_mask, P.list,
                                     P.npix, P.scratch, P.scap, P.max_spp);
-        e = launch_trace(L, node_mode(G.precision_mask), gs[g], sm_count);
+        e = launch_trace(L, node_mode(G.precision_mask, G.any_tlas), gs[g], sm_count);
         if (e != cudaSuccess) return e;
     }
     for (int k = 0; k < naux && e == cudaSuccess; ++k) {
@@ -1417,7 +1420,7 @@ hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* c
     CK(ctx, cudaMemsetAsync(f->counters, 0, sizeof(TraceCounters), s), "reset counters");
     TraceLaunch L = make_launch(p, f->dscene, 1, sl.work_count, f->counters, tlas->type_mask, f->resolve_list,
                                 uint64_t(f->w) * f->h, f->resolve_scratch, f->scratch_cap, f->spp);
-    CK(ctx, launch_trace(L, node_mode(tlas->precision_mask), s, ctx->sm_count), "launch trace");
+    CK(ctx, launch_trace(L, node_mode(tlas->precision_mask, tlas->nodes != nullptr), s, ctx->sm_count), "launch trace");
     f->pending_primary = uint64_t(f->w) * f->h * f->spp;
     f->stats_pending = true;
     if (p->async) return HRT_OK;

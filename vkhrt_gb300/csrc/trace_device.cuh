@@ -1163,8 +1163,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     int sp = 0;
     uint32_t steps = 0;
     const void* nodes = nullptr;                 // node array of the current instance's BLAS
-    bool qnodes = false;                         // its format (kNodesPerInstance launches)
-    uint32_t tstack[kTlasStack];                 // TLAS walk of a multi-instance scene (local memory)
+    // Multi-instance scenes (a TLAS) run in the kNodesPerInstance build only, so the builds for
+    // one node format keep the lean single-instance loop.
+    constexpr bool kTlas = kNodes == kNodesPerInstance;
+    bool qnodes = false;                         // the current instance's format (kNodesPerInstance)
+    uint32_t tstack[kTlas ? kTlasStack : 1];     // TLAS walk (local memory)
     int tsp = 0;
     uint32_t oct = 0;                            // direction octant of the object-space ray
     uint32_t cur_base = 0, cur_bits = 0;         // node group: hits in visiting order (bits 0-7), imask (8-15)
@@ -1208,34 +1211,27 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         cur_bits = (1u << oct) | (1u << 8);
         return true;
     };
-    // The ray's next instance: of a multi-instance scene, the next TLAS leaf whose world box the
-    // ray meets before its closest hit (set up, root pushed); of a one-instance scene, the next
-    // index. False when there is none.
-    auto next_instance = [&]() -> bool {
+    // The ray's next candidate instance: of a multi-instance scene, the next TLAS leaf whose world
+    // box the ray meets before its closest hit; of a one-instance scene, the next index. ~0u when
+    // there is none. (The completion step sets the candidate up; one call site keeps the kernel's
+    // code as compact as it was without a TLAS.)
+    auto advance = [&]() -> uint32_t {
         const SceneLaunch& S = L.scenes[si];
-        if (!S.tlas) {
-            while (++inst_cur < S.ninst)
-                if (setup_instance(inst_cur)) return true;
-            return false;
-        }
+        if (!kTlas || !S.tlas) return inst_cur + 1 < S.ninst ? inst_cur + 1 : 0xffffffffu;
         const V3<float> winv = safe_inv(wd);
         while (tsp > 0) {
             uint32_t a, b;
             if (!tlas_box_hit(S.tlas, tstack[--tsp], wo, winv, cur_tmin, h.t, &a, &b)) continue;
-            if (a & kLeafFlag) {
-                inst_cur = a & ~kLeafFlag;
-                if (setup_instance(inst_cur)) return true;
-                continue;
-            }
+            if (a & kLeafFlag) return a & ~kLeafFlag;
             if (tsp + 2 > kTlasStack) {  // deeper than a TLAS is built (bounded all the same)
                 err |= kErrStackOverflow;
                 tsp = 0;
-                return false;
+                break;
             }
             tstack[tsp++] = b;
             tstack[tsp++] = a;
         }
-        return false;
+        return 0xffffffffu;
     };
     auto start_ray = [&](V3<float> o, V3<float> d, float tmin, float tmax) {
         wo = o;
@@ -1247,10 +1243,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         leaf_bits = 0;
         steps = 0;
         const SceneLaunch& S = L.scenes[si];
-        if (S.tlas) {
+        if (kTlas && S.tlas) {  // the completion step walks the TLAS from its root
             tsp = 0;
             tstack[tsp++] = 0;
-            next_instance();
+            inst_cur = 0xffffffffu;
         } else {
             for (inst_cur = 0; inst_cur < S.ninst; ++inst_cur)
                 if (setup_instance(inst_cur)) break;
@@ -1517,7 +1513,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 atomicOr(&L.counters->error, err);
                 has_ray = false;
             } else {
-                const bool more = !(shadow && shadow_hit) && next_instance();
+                bool more = false;
+                if (!(shadow && shadow_hit))
+                    for (uint32_t i; (i = advance()) != 0xffffffffu;) {
+                        inst_cur = i;
+                        if (setup_instance(i)) { more = true; break; }
+                    }
                 if (!more) finish_phase();
             }
         }
