@@ -711,7 +711,7 @@ def run_single(args, dist):
     v, r, off = H.generate_strands(sp)
     blas = H.BottomLevelAccelerationStructure(
         H.BLASInput(type=cfg["type"], vertices=v, radius=r, strand_offsets=off, precision=cfg["precision"],
-                    max_leaf=args.max_leaf), ctx)
+                    max_leaf=args.max_leaf, width=args.node_width), ctx)
     tlas = H.TopLevelAccelerationStructure([blas], ctx)
     cam = H.scene_camera(w, h)
     frame = H.Frame(ctx, w, h, spp)
@@ -771,6 +771,8 @@ def main():
                     help="override the workload's BVH/primitive precision (profiling)")
     ap.add_argument("--variant", type=int, default=0, help="resident blocks per SM: 0/1 = 4, 2 = 3, 3 = 5")
     ap.add_argument("--max-leaf", type=int, default=1, help="primitives per BVH8 leaf (1..3)")
+    ap.add_argument("--node-width", type=int, default=0,
+                    help="BVH node fan-out 2..8 (0 = 8; a measurement knob)")
     ap.add_argument("--refill", type=int, default=8, help="idle lanes per warp that trigger a fetch (0 = 16)")
     ap.add_argument("--speculative", type=int, default=1, help="speculative traversal (0/1)")
     ap.add_argument("--leaf-again", type=int, default=4,

@@ -96,7 +96,8 @@ typedef struct hrt_blas_input {
     uint64_t nlines;                /* with line_indices */
     float const_radius;
     float transform[16];            /* object to world, column major (glm::mat4) */
-    uint32_t quant_chunk;           /* reserved, ignored (0) */
+    uint32_t width;                 /* BVH node fan-out, 2..8 (0 = 8): children per node of the
+                                       8-slot node formats (narrower trees are for measurement) */
     uint32_t flags;                 /* HRT_BUILD_* */
     /* HRT_BLAS_MESH (renderer.cpp:543-582): 3 vertex indices per triangle; triangle i reports
      * primitive id i. strand_offsets and line_indices must be NULL. */

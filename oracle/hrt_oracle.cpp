@@ -622,10 +622,11 @@ static void refit(Binary& bt, const Box* sorted_boxes, int64_t n) {
 // (k = 1..8) of its parent:
 //   a primitive: A for every k;
 //   dist(k) = min over j = 1..k-1 of cost(left, j) + cost(right, k - j)   (k >= 2);
-//   cost(x, 1) = A c when x holds c <= max_leaf primitives (a leaf slot), else A + dist(8);
+//   cost(x, 1) = A c when x holds c <= max_leaf primitives (a leaf slot), else A + dist(W);
 //   cost(x, k) = min(cost(x, k - 1), dist(k)).
-// Each wide node starts from a binary internal node b whose 8 slots go to its children as j and
-// 8 - j, j the least minimiser of cost(left, j) + cost(right, 8 - j); a child given k slots takes
+// W is the node fan-out (8 by default; a narrower tree uses W of the 8 slots). Each wide node
+// starts from a binary internal node b whose W slots go to its children as j and W - j, j the
+// least minimiser of cost(left, j) + cost(right, W - j); a child given k slots takes
 // the fewest k' <= k of the same cost and, with k' > 1, splits them again between its own
 // children, left before right. A child holding at most max_leaf primitives becomes a leaf (a
 // contiguous run of sorted primitives), a larger one a wide node of the next level. The
@@ -673,7 +674,7 @@ static void octant_slots(const Box& parent, const Box* const* kid_box, int n, in
     }
 }
 
-static void collapse(const Binary& bt, const Box* sorted_boxes, int64_t n, int max_leaf, Wide& w) {
+static void collapse(const Binary& bt, const Box* sorted_boxes, int64_t n, int max_leaf, int width, Wide& w) {
     w = Wide{};
     if (n <= 0) return;
     auto count = [&](uint32_t c) -> uint32_t {
@@ -711,7 +712,7 @@ static void collapse(const Binary& bt, const Box* sorted_boxes, int64_t n, int m
             const uint32_t cnt = count(x);
             const float a = sa_measure(bt.box[x]);
             float* c = &dpc[8 * size_t(x)];
-            c[0] = cnt <= uint32_t(max_leaf) ? a * float(cnt) : a + dist[8];
+            c[0] = cnt <= uint32_t(max_leaf) ? a * float(cnt) : a + dist[width];
             for (int k = 2; k <= 8; ++k) c[k - 1] = dist[k] < c[k - 2] ? dist[k] : c[k - 2];
         }
     }
@@ -735,8 +736,8 @@ static void collapse(const Binary& bt, const Box* sorted_boxes, int64_t n, int m
             if (b & 0x80000000u) kids[nk++] = b;
             else {
                 std::vector<std::pair<uint32_t, int>> work;  // (binary node, slots), left on top
-                const int j = split(b, 8);
-                work.push_back({bt.right[b], 8 - j});
+                const int j = split(b, width);
+                work.push_back({bt.right[b], width - j});
                 work.push_back({bt.left[b], j});
                 while (!work.empty()) {
                     auto [x, k] = work.back();
@@ -1417,9 +1418,12 @@ int64_t orc_voxelize(const float* lines, int64_t n, float r, float voxel_size, f
 // Collapse; returns the number of wide nodes. Outputs must hold max_nodes entries
 // (child_base, prim_base: max_nodes; meta: 8 max_nodes; cbox: 48 max_nodes floats;
 // prim_order: n). Quantised fields: qp (3 per node), qe (3), qlo/qhi (24 each).
+// max_leaf: primitives per leaf slot (1..3); bits 8-11 the node fan-out W (2..8; 0 = 8).
 int64_t orc_bvh8(const float* boxes, int64_t n, int max_leaf, int64_t max_nodes, uint32_t* child_base,
                  uint32_t* prim_base, uint8_t* meta, float* cbox, uint32_t* prim_order, float* qp, uint8_t* qe,
                  uint8_t* qlo, uint8_t* qhi) {
+    const int width = (max_leaf >> 8) & 15 ? (max_leaf >> 8) & 15 : 8;
+    max_leaf &= 0xff;
     const Box* bx = reinterpret_cast<const Box*>(boxes);
     std::vector<uint64_t> codes(n);
     morton_codes(bx, n, codes.data());
@@ -1432,7 +1436,7 @@ int64_t orc_bvh8(const float* boxes, int64_t n, int max_leaf, int64_t max_nodes,
     Binary bt;
     if (n >= 2) { karras(sk.data(), n, bt); refit(bt, sb.data(), n); }
     Wide w;
-    collapse(bt, sb.data(), n, max_leaf, w);
+    collapse(bt, sb.data(), n, max_leaf, width, w);
     int64_t nn = int64_t(w.child_base.size());
     if (nn > max_nodes) return -nn;
     for (int64_t i = 0; i < nn; ++i) {

@@ -22,7 +22,7 @@ NODEQ = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("imask", "u1"), ("child_base
 assert NODEF.itemsize == 224 and NODEQ.itemsize == 80
 
 
-def oracle_bvh(orc, boxes, max_leaf):
+def oracle_bvh(orc, boxes, max_leaf, width=8):
     n = len(boxes)
     out = dict(codes=np.zeros(n, np.uint64), srt=np.zeros(n, np.uint32), L=np.zeros(max(n - 1, 0), np.uint32),
                R=np.zeros(max(n - 1, 0), np.uint32), F=np.zeros(max(n - 1, 0), np.uint32),
@@ -33,7 +33,7 @@ def oracle_bvh(orc, boxes, max_leaf):
     w = dict(cb=np.zeros(mx, np.uint32), pb=np.zeros(mx, np.uint32), meta=np.zeros((mx, 8), np.uint8),
              cbox=np.zeros((mx, 8, 6), np.float32), order=np.zeros(n, np.uint32), qp=np.zeros((mx, 3), np.float32),
              qe=np.zeros((mx, 3), np.uint8), qlo=np.zeros((mx, 3, 8), np.uint8), qhi=np.zeros((mx, 3, 8), np.uint8))
-    nn = orc.orc_bvh8(P(boxes), n, max_leaf, mx, *[P(w[k]) for k in ("cb", "pb", "meta", "cbox", "order", "qp", "qe",
+    nn = orc.orc_bvh8(P(boxes), n, max_leaf | (width << 8), mx, *[P(w[k]) for k in ("cb", "pb", "meta", "cbox", "order", "qp", "qe",
                                                                     "qlo", "qhi")])
     out.update(w)
     out["nn"] = nn
@@ -48,10 +48,10 @@ def rebuild_curves(ent, first):
     return np.ascontiguousarray(np.concatenate([p1, p1 + (p2 - p0) * k, p2 - (p3 - p1) * k, p2], axis=1), np.float32)
 
 
-def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=None, const_radius=0.02):
+def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=None, const_radius=0.02, width=0):
     inp = H.BLASInput(type=H.BLASType(gtype), vertices=v, radius=r, strand_offsets=None if line_indices is not None else off,
                       line_indices=line_indices, precision=H.Precision(precision), max_leaf=max_leaf,
-                      const_radius=const_radius, keep_intermediate=True)
+                      const_radius=const_radius, keep_intermediate=True, width=width)
     blas = H.BottomLevelAccelerationStructure(inp, ctx)
     if line_indices is None:
         lines, lrad = lines_from_strands(v, r, off, const_radius)
@@ -77,7 +77,7 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
         assert np.ascontiguousarray(g[:, 6:]).tobytes() == rad.tobytes()
     else:
         assert blas.get(H.Part.DOTS_VERTICES, np.float32, (n, 36)).tobytes() == data.tobytes()
-    o = check_tree(blas, orc, ref_boxes(orc, gtype, data, rad, n), max_leaf, precision)
+    o = check_tree(blas, orc, ref_boxes(orc, gtype, data, rad, n), max_leaf, precision, width or 8)
     if quant_prims:
         # the strand vertex stream and each slot's first entry equal the oracle's, and the control
         # points and radii rebuilt from them are the FP32 curves bit for bit
@@ -92,12 +92,12 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
     return blas
 
 
-def check_tree(blas, orc, ref_boxes, max_leaf, precision):
+def check_tree(blas, orc, ref_boxes, max_leaf, precision, width=8):
     """Primitive boxes, Morton codes, sort, binary tree, BVH8 nodes (both encodings) and leaf
     order of a BLAS against the oracle built from the same boxes; returns the oracle's tree."""
     n = len(ref_boxes)
     assert blas.get(H.Part.PRIM_BOXES, np.float32, (n, 6)).tobytes() == ref_boxes.tobytes()
-    o = oracle_bvh(orc, ref_boxes, max_leaf)
+    o = oracle_bvh(orc, ref_boxes, max_leaf, width)
     assert np.array_equal(blas.get(H.Part.MORTON_SORTED, np.uint64, n), o["codes"])
     assert np.array_equal(blas.get(H.Part.SORTED_INDEX, np.uint32, n), o["srt"])
     if n >= 2:
@@ -130,6 +130,14 @@ def check_tree(blas, orc, ref_boxes, max_leaf, precision):
 def test_build_bit_exact(ctx, orc, gtype, precision):
     v, r, off = H.generate_strands(H.StrandParams(seed=5, nstrands=400, nverts=17))
     check_blas(ctx, orc, gtype, precision, v, r, off)
+
+
+@pytest.mark.parametrize("width", [2, 4, 6])
+def test_build_narrower_nodes_bit_exact(ctx, orc, width):
+    # a node fan-out below 8 (the collapse fills `width` of the 8 slots): same bit-exact pipeline
+    v, r, off = H.generate_strands(H.StrandParams(seed=6, nstrands=300, nverts=17))
+    check_blas(ctx, orc, PHANTOM, 1, v, r, off, width=width)
+    check_blas(ctx, orc, LSS, 0, v, r, off, width=width)
 
 
 @pytest.mark.parametrize("max_leaf", [2, 3])

@@ -617,3 +617,21 @@ def test_voxel_blas_serializes(ctx):
     assert (h1["t"] >= 0).sum() > 1000 and np.array_equal(h1, H.trace_rays(ctx, t2, rays))
     with pytest.raises(H.HrtError):
         b2.refit(v)
+
+
+@pytest.mark.parametrize("gtype", [PHANTOM, DOTS])
+def test_node_width_changes_no_hit(ctx, gtype):
+    """The BVH's node fan-out changes which nodes a ray visits, never its closest hit: BLASes of
+    width 4 and 8 give the same hits bit for bit, with more node visits at width 4."""
+    v, r, off = H.generate_strands(H.StrandParams(seed=70, nstrands=800, nverts=24))
+    out = {}
+    for width in (4, 8):
+        b = H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType(gtype), vertices=v, radius=r,
+                                                           strand_offsets=off, precision=H.Precision.QUANTISED,
+                                                           width=width), ctx)
+        t = H.TopLevelAccelerationStructure([b], ctx)
+        fr = H.Frame(ctx, 96, 64, 1, with_hits=True)
+        H.trace(ctx, t, H.scene_camera(96, 64), fr, H.trace_params(shading=2, record_hits=1, count_stats=1))
+        out[width] = (fr.download(hits=True)[1], fr.stats())
+    assert out[4][0].tobytes() == out[8][0].tobytes()
+    assert out[4][1]["nodes_visited"] > out[8][1]["nodes_visited"]

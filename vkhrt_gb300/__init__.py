@@ -30,7 +30,7 @@ class BLASInputC(ctypes.Structure):
     _fields_ = [("type", c_i32), ("precision", c_i32), ("memory", c_i32), ("max_leaf", c_u32),
                 ("vertices", c_p), ("radius", c_p), ("strand_offsets", c_p), ("line_indices", c_p),
                 ("nvertices", c_u64), ("nstrands", c_u64), ("nlines", c_u64), ("const_radius", c_f),
-                ("transform", c_f * 16), ("quant_chunk", c_u32), ("flags", c_u32), ("tri_indices", c_p),
+                ("transform", c_f * 16), ("width", c_u32), ("flags", c_u32), ("tri_indices", c_p),
                 ("ntris", c_u64), ("normals", c_p), ("voxel_size", c_f)]
 
 
@@ -201,6 +201,7 @@ class BLASInput:
     transform: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))  # object->world
     precision: Precision = Precision.FP32
     max_leaf: int = 1
+    width: int = 0                            # BVH node fan-out 2..8 (0 = 8)
     keep_intermediate: bool = False
     voxel_size: float = 0.0
 
@@ -247,6 +248,7 @@ class BottomLevelAccelerationStructure:
         c.precision = int(inp.precision)
         c.memory = 0
         c.max_leaf = inp.max_leaf
+        c.width = inp.width
         c.voxel_size = inp.voxel_size
         c.vertices = _ptr(v)
         c.nvertices = v.shape[0]

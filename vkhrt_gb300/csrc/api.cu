@@ -491,6 +491,8 @@ static hrt_status build_mesh(hrt_context* ctx, const hrt_blas_input* in, cudaStr
                     (unsigned long long)in->ntris);
     const uint32_t max_leaf = in->max_leaf ? in->max_leaf : 1;
     if (max_leaf > 3) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: max_leaf must be 1..3");
+    const uint32_t width = in->width ? in->width : 8;
+    if (width < 2 || width > 8) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: width must be 2..8");
     if (in->memory == HRT_MEMORY_HOST)
         for (uint64_t i = 0; i < 3 * in->ntris; ++i)
             if (in->tri_indices[i] >= in->nvertices)
@@ -557,7 +559,7 @@ static hrt_status build_mesh(hrt_context* ctx, const hrt_blas_input* in, cudaStr
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    BuildInput bi{in->type, in->precision, int(max_leaf), nullptr, nullptr, n, b->keep, tris, tnrm};
+    BuildInput bi{in->type, in->precision, int(max_leaf), int(width), nullptr, nullptr, n, b->keep, tris, tnrm};
     char msg[256] = {0};
     e = build_blas_device(bi, b->out, s, msg, sizeof(msg));
     cudaEventRecord(e1, s);
@@ -603,6 +605,8 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
         return fail(ctx, HRT_ERR_UNSUPPORTED, "hrt_blas_build: more than 2^32 - 1 vertices");
     uint32_t max_leaf = in->max_leaf ? in->max_leaf : 1;
     if (max_leaf > 3) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: max_leaf must be 1..3");
+    const uint32_t width = in->width ? in->width : 8;
+    if (width < 2 || width > 8) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: width must be 2..8");
     if (!in->radius && !(in->const_radius >= 0.0f))
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: const_radius must be >= 0");
     DeviceSet dset(ctx->device);
@@ -721,7 +725,7 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    BuildInput bi{in->type, in->precision, int(max_leaf), lines, lrad, nlines, b->keep};
+    BuildInput bi{in->type, in->precision, int(max_leaf), int(width), lines, lrad, nlines, b->keep};
     char msg[256] = {0};
     float* vox = nullptr;
     if (in->type == HRT_BLAS_VOXELS) {  // the lines become voxel boxes, the BVH primitives
@@ -797,7 +801,7 @@ hrt_status hrt_blas_refit(hrt_blas* b, const float* vertices, const float* per_v
         dv = const_cast<float*>(vertices);
         dp = const_cast<float*>(per_vertex);
     }
-    BuildInput bi{b->type, b->precision, int(b->max_leaf), nullptr, nullptr, n, b->keep};
+    BuildInput bi{b->type, b->precision, int(b->max_leaf), 8, nullptr, nullptr, n, b->keep};
     if (mesh) {
         if (e == cudaSuccess) e = cudaMalloc(&d0, n * 12);
         if (e == cudaSuccess) e = cudaMemcpyAsync(d0, b->tri_idx.data(), n * 12, cudaMemcpyHostToDevice, s);

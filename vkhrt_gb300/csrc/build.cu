@@ -565,13 +565,15 @@ __device__ __forceinline__ float sa_measure(const float* bx) {
 // Bottom-up box refit; the second child to arrive computes its parent. With dpc, the node's
 // collapse costs as well (dpc[8 node + k - 1], k = 1..8 slots; see collapse_expand_kernel):
 //   dist(k) = min over j = 1..k-1 of cost(left, j) + cost(right, k - j)     (k >= 2)
-//   cost(node, 1) = A c if it holds c <= max_leaf primitives (a leaf slot), else A + dist(8)
+//   cost(node, 1) = A c if it holds c <= max_leaf primitives (a leaf slot), else A + dist(W)
 //   cost(node, k) = min(cost(node, k - 1), dist(k))
-// with A the node's surface-area measure; a primitive costs its own measure for every k.
+// with A the node's surface-area measure and W the node fan-out (width, 8 by default); a
+// primitive costs its own measure for every k.
 // Node visits and primitive tests are weighted alike.
 __global__ void refit_kernel(const uint32_t* parent_leaf, const uint32_t* parent_int, const uint32_t* left,
                              const uint32_t* right, const uint32_t* first, const uint32_t* last, const float* sboxes,
-                             float* nboxes, uint32_t* visits, uint64_t n, uint32_t* err, float* dpc, int max_leaf) {
+                             float* nboxes, uint32_t* visits, uint64_t n, uint32_t* err, float* dpc, int max_leaf,
+                             int width) {
     uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= n) return;
     uint32_t node = parent_leaf[j];
@@ -611,7 +613,7 @@ __global__ void refit_kernel(const uint32_t* parent_leaf, const uint32_t* parent
             const uint32_t cnt = last[node] - first[node] + 1u;
             const float a = sa_measure(b);
             float cost[8];
-            cost[0] = cnt <= uint32_t(max_leaf) ? a * float(cnt) : a + dist[8];
+            cost[0] = cnt <= uint32_t(max_leaf) ? a * float(cnt) : a + dist[width];
             for (int k = 2; k <= 8; ++k) cost[k - 1] = dist[k] < cost[k - 2] ? dist[k] : cost[k - 2];
             for (int k = 0; k < 8; ++k) __stcg(dpc + 8 * uint64_t(node) + k, cost[k]);
         }
@@ -652,12 +654,12 @@ __device__ __forceinline__ int dp_split(const BinView& b, uint32_t x, int k) {
     return bj;
 }
 
-// Children of the wide node made from binary node b, by the collapse costs: b's 8 slots are
+// Children of the wide node made from binary node b, by the collapse costs: b's W slots are
 // split between its children; a child given k slots takes the fewest k' <= k of the same
 // cost, and with k' > 1 splits them again between its own children (left before right), so the
 // children come out in the binary tree's left-to-right order. A child holding at most max_leaf
 // primitives becomes a leaf slot; a larger one becomes a wide node of the next level.
-__global__ void collapse_expand_kernel(BinView bv, const uint32_t* level, uint32_t count, int max_leaf,
+__global__ void collapse_expand_kernel(BinView bv, const uint32_t* level, uint32_t count, int max_leaf, int width,
                                        uint32_t* kids, uint32_t* nk, uint32_t* nint, uint32_t* nprim) {
     uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= count) return;
@@ -668,8 +670,8 @@ __global__ void collapse_expand_kernel(BinView bv, const uint32_t* level, uint32
     else {
         uint32_t sx[8];
         int sk[8], sp = 0;
-        const int j = dp_split(bv, b, 8);
-        sx[sp] = bv.right[b]; sk[sp++] = 8 - j;
+        const int j = dp_split(bv, b, width);
+        sx[sp] = bv.right[b]; sk[sp++] = width - j;
         sx[sp] = bv.left[b]; sk[sp++] = j;
         while (sp > 0) {
             const uint32_t x = sx[--sp];
@@ -1250,7 +1252,7 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
         HRT_CK(cudaMemsetAsync(visits, 0, ni * 4, s));
         karras_kernel<<<grid_for(ni, T), T, 0, s>>>(codes, int64_t(n), left, right, first, last, pint, pleaf);
         refit_kernel<<<grid_for(n, T), T, 0, s>>>(pleaf, pint, left, right, first, last, sboxes, nboxes, visits, n, err,
-                                                  dpc, in.max_leaf);
+                                                  dpc, in.max_leaf, in.width);
         HRT_CK(cudaGetLastError());
     }
 
@@ -1276,7 +1278,8 @@ cudaError_t build_blas_device(const BuildInput& in, BuildOutput& out, cudaStream
     for (int level = 0; count > 0; ++level) {
         if (level > 4096) { snprintf(msg, msglen, "BVH8 collapse did not terminate"); return cudaErrorUnknown; }
         out.level_start.push_back(node_base);
-        collapse_expand_kernel<<<grid_for(count, T), T, 0, s>>>(bv, lvl_a, count, in.max_leaf, kids, nk, nint, nprim);
+        collapse_expand_kernel<<<grid_for(count, T), T, 0, s>>>(bv, lvl_a, count, in.max_leaf, in.width, kids, nk, nint,
+                                                                nprim);
         HRT_CK(cudaGetLastError());
         HRT_CK(device_scan<SumOp>(nint, int_off, count, false, totals, s));
         HRT_CK(device_scan<SumOp>(nprim, prim_off, count, false, totals + 1, s));

@@ -188,6 +188,7 @@ struct PrimVoxel {
 };
 struct BuildInput {
     int type, precision, max_leaf;
+    int width;            // BVH node fan-out, 2..8
     const float* lines;   // device, n x 6
     const float* lrad;    // device, n x 2 (per line end)
     uint64_t n;
