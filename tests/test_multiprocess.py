@@ -1,6 +1,8 @@
-"""Replica bookkeeping of bench.py on CPU ranks (gloo, world size 2): barrier, max over ranks,
-and the whole-job value N x rays / max time. The hair path shards no data across GPUs (rays
-are independent; each rank builds its own BVH and renders its own frames)."""
+"""Replicas on CPU ranks (gloo, world size 2): bench.py's bookkeeping (barrier, max over ranks,
+the whole-job value N x rays / max time), and the partition of a job (vkhrt_gb300.replicas):
+interleaved rows of a scene and the scenes of a batch dealt to ranks, each rank rendering its
+share and rank 0 gathering the framebuffers. Rays are independent, so the only exchange is that
+host-side gather."""
 import os
 import socket
 import sys
@@ -62,3 +64,81 @@ def test_single_process_dist_is_trivial():
     assert d.world == 1 and d.rank == 0 and d.max(3.5) == 3.5
     d.barrier()
     d.close()
+
+
+def test_scene_partition_is_balanced_and_deterministic():
+    sys.path.insert(0, ROOT)
+    from vkhrt_gb300.replicas import partition_scenes
+    work = [5, 90, 7, 40, 40, 3, 60, 12]
+    parts = partition_scenes(work, 3)
+    assert sorted(i for p in parts for i in p) == list(range(len(work)))
+    loads = [sum(work[i] for i in p) for p in parts]
+    assert max(loads) - min(loads) <= max(work)  # greedy largest-first
+    assert parts == partition_scenes(list(work), 3)
+    assert partition_scenes(work, 1) == [list(range(len(work)))]
+
+
+def _render_worker(rank, world, port, q):
+    """Renders this rank's share with the CPU oracle: the rows y = rank (mod world) of scene 0 and
+    the scenes dealt to it; rank 0 gathers and compares with its own single-rank renders."""
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import torch.distributed as dist
+
+    import vkhrt_gb300 as H
+    from hairscene import PHANTOM, LSS, OracleScene, lines_from_strands, load_oracle, oracle_geometry
+    from vkhrt_gb300.replicas import assemble_rows, gather_to_rank0, partition_scenes, row_pixels
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    orc = load_oracle()
+    lib = H.bind_workload(orc)
+    scenes = []
+    for k, (gt, ns, w, h) in enumerate([(PHANTOM, 150, 48, 40), (LSS, 200, 40, 32), (PHANTOM, 120, 32, 24),
+                                        (LSS, 90, 56, 24)]):
+        v, r, off = H.generate_strands(H.StrandParams(seed=400 + k, nstrands=ns, nverts=16), lib=lib)
+        lines, lrad = lines_from_strands(v, r, off)
+        vi, pi = H.camera_arrays(H.orbit_camera(w, h, 0.5 * k, 0.1, lib=lib))
+        scenes.append((OracleScene(orc, [(gt, *oracle_geometry(orc, gt, lines, lrad))]), vi, pi, w, h))
+
+    def render(sc, px=None):
+        osc, vi, pi, w, h = sc
+        return osc.render(vi, pi, w, h, shading=2, precision=64, pixel_list=px, threads=2)["fb"]
+
+    osc0, vi0, pi0, w0, h0 = scenes[0]
+    local = {("rows", rank, world): render(scenes[0], row_pixels(w0, h0, rank, world))}
+    mine = partition_scenes([w * h for (_, _, _, w, h) in scenes], world)[rank]
+    for i in mine:
+        local[("scene", i)] = render(scenes[i])
+    got = gather_to_rank0(local, dist)
+    ok = True
+    if rank == 0:
+        frame = assemble_rows(w0, h0, 4, {(k[1], k[2]): v for k, v in got.items() if k[0] == "rows"})
+        ok &= np.array_equal(frame.reshape(-1, 4), render(scenes[0]))
+        for i in range(len(scenes)):
+            ok &= np.array_equal(got[("scene", i)], render(scenes[i]))
+    else:
+        ok &= got is None
+    q.put((rank, bool(ok), mine))
+    dist.destroy_process_group()
+
+
+def test_partitioned_renders_gather_to_the_single_rank_frames():
+    """Two gloo ranks render disjoint shares (interleaved rows of one scene, and the scenes dealt
+    by work) with the CPU oracle; the frames gathered on rank 0 equal single-rank renders bit for
+    bit."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_render_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=300)
+        assert p.exitcode == 0
+    res = sorted(q.get(timeout=10) for _ in range(2))
+    assert all(ok for _, ok, _ in res)
+    assert sorted(i for _, _, mine in res for i in mine) == [0, 1, 2, 3]
