@@ -634,9 +634,12 @@ def run_batched(args, dist):
     dist.close()
 
 
-# Per-ray counters of the dominant kernel from an ncu capture (profiles/): DRAM bytes, L2 bytes
-# and warp instructions. None until a capture of the current kernel is summarised there.
-NCU_PER_RAY = None
+# Per-ray counters of the dominant kernel (the batch's quantised Phantom group) from one ncu
+# capture of that launch (profiles/frame_kernel_c5_phantom_group.md): DRAM bytes
+# (dram__bytes_read.sum + dram__bytes_write.sum), L2 bytes (lts__t_sectors.sum x 32) and warp
+# instructions (smsp__inst_executed.sum), each over the launch's 4,649,742 rays.
+NCU_PER_RAY = {"dram_bytes": 36.75e6 / 4649742, "l2_bytes": 96901879 * 32 / 4649742,
+               "warp_inst": 6718034768 / 4649742, "source": "profiles/frame_kernel_c5_phantom_group.md"}
 
 
 def measured_bounds(rays: int, ms: float, clk: dict) -> dict:
@@ -694,6 +697,52 @@ def batch_agreement_and_cpu(ctx, q, models, tuned, fb_timed):
                                        f"oracle, {secs:.1f} s, in the reference arm's row bands",
                              "fp64": {"value": round(rate64, 4),
                                       "sample": f"one of every {FP64_BANDS} rows ({rays64} rays), {secs64:.1f} s"}}}
+
+
+def run_batched_profile(args, dist):
+    """`--profile` on the batched workload: the quantised Phantom scenes alone as one batch (the
+    dominant kernel of the full batch, its Phantom group), replayed warmup + steps times for a
+    profiler, then counted. Parameters from the tune cache when it holds the batch's choice."""
+    import torch
+    import vkhrt_gb300 as H
+    torch.cuda.set_device(dist.local)
+    ctx = H.Context(dist.local)
+    models = [x for x in batch_models() if int(x[0]["type"]) == 0]
+    q = []
+    for m, v, r, off in models:
+        b = H.BottomLevelAccelerationStructure(H.BLASInput(type=m["type"], vertices=v, radius=r, strand_offsets=off,
+                                                           precision=H.Precision.QUANTISED), ctx)
+        t = H.TopLevelAccelerationStructure([b], ctx)
+        q.append((b, t, H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"]),
+                  H.Frame(ctx, m["width"], m["height"], m["spp"])))
+    fields = {}
+    if args.tune_cache and os.path.exists(args.tune_cache):
+        fields = {k: int(v) for k, v in json.load(open(args.tune_cache)).get(f"{BATCH_CONFIG}/quantised", {}).items()
+                  if k in H.TUNED_FIELDS}
+    p = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1}, **fields)
+    batch = H.Batch(ctx, [(t, cam, fr) for (_, t, cam, fr) in q], p)
+    for _ in range(args.warmup):
+        batch.launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        batch.launch()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(args.steps, 1)
+    rays = nodes = prims = 0
+    for (b, t, cam, fr) in q:  # counted after the replays, so a profiler's launch count starts with them
+        H.trace(ctx, t, cam, fr, H.trace_params(jitter=1, seed=17, shading=2, count_stats=1))
+        st = fr.stats()
+        rays += st["primary_rays"] + st["shadow_rays"]
+        nodes += st["nodes_visited"]
+        prims += st["prims_tested"]
+    print(json.dumps({"profile": "c5 Phantom group", "scenes": len(q), "ms_per_replay": round(ms, 3),
+                      "rays_per_replay": int(rays), "nodes_visited": int(nodes), "prims_tested": int(prims),
+                      "params": {k: int(getattr(p, k)) for k in H.TUNED_FIELDS},
+                      "device_bytes": int(sum(b.info["device_bytes"] for (b, *_r) in q))}), flush=True)
+    dist.close()
 
 
 # ------------------------------------------------------------------------------ one configuration
@@ -779,7 +828,7 @@ def main():
                     help="repeat the leaf phase while this many lanes hold leaves (0 = once)")
     ap.add_argument("--tune-cache", default=None, help="JSON file that keeps autotuner choices between runs")
     ap.add_argument("--profile", action="store_true",
-                    help="with --config: the timed launches only (no agreement or CPU legs)")
+                    help="the timed launches only, for a profiler (with the batched workload: its Phantom group)")
     args = ap.parse_args()
     for k in ("width", "height", "spp"):
         if getattr(args, k):
@@ -795,7 +844,10 @@ def main():
         dist.close()
         return
     if args.config == BATCH_CONFIG:
-        run_batched(args, dist)
+        if args.profile:
+            run_batched_profile(args, dist)
+        else:
+            run_batched(args, dist)
         return
     run_single(args, dist)
 
