@@ -7,6 +7,8 @@
  *                           <- include/top_level_acceleration_structure.hpp:9-24
  *   Render(context, tlas, camera, params, frame)  <- Renderer::Render -> traceRaysKHR
  *                              (source/renderer.cpp:83-166)
+ *   Batch (many scenes, one CUDA-graph replay per step; no counterpart in the reference, whose
+ *     renderer traces one scene per frame)
  *   LookAt(...)             <- FlyCamera::ViewMatrix/ProjectionMatrix (source/fly_camera.cpp:25-35)
  * Header only; links against libhrt.so. Where the reference logs and aborts on a failed call
  * (VkCheckResult, source/vk_common.cpp:5-15) these classes throw hrt::Error, which carries the
@@ -76,6 +78,7 @@ struct BLASInput {
     std::vector<float> normals;                       // HRT_BLAS_MESH, per vertex, or empty
     float constRadius = 0.02f;                        // geometry_processor.cpp:635
     float voxelSize = 0.0f;                           // HRT_BLAS_VOXELS (0 = 0.1)
+    uint32_t width = 0;                               // BVH node fan-out 2..8 (0 = 8)
 };
 
 class BottomLevelAccelerationStructure {
@@ -104,6 +107,7 @@ public:
         }
         b.normals = in.normals.empty() ? nullptr : in.normals.data();
         b.voxel_size = in.voxelSize;
+        b.width = in.width;
         for (int k = 0; k < 16; ++k) b.transform[k] = in.transform[k];
         _transform = in.transform;
         Check(ctx.Get(), hrt_blas_build(ctx.Get(), &b, stream, &_blas), "hrt_blas_build");
@@ -164,6 +168,8 @@ public:
     Frame& operator=(const Frame&) = delete;
 
     hrt_frame* Get() const { return _f; }
+    uint32_t Width() const { return _w; }
+    uint32_t Height() const { return _h; }
     // The framebuffer (width * height * 4 floats) and, when given, the hit records.
     std::vector<float> Download(std::vector<hrt_hit>* hits = nullptr, void* stream = nullptr) const {
         std::vector<float> rgba(size_t(_w) * _h * 4);
@@ -203,6 +209,52 @@ inline void Render(Context& ctx, const TopLevelAccelerationStructure& tlas, cons
                    const hrt_trace_params& params, Frame& frame, void* stream = nullptr) {
     Check(ctx.Get(), hrt_trace(ctx.Get(), tlas.Structure(), &cam, &params, frame.Get(), stream), "hrt_trace");
 }
+
+// Many scenes rendered by one replay of a captured CUDA graph: each scene is a TLAS, a camera
+// and the frame it renders into (its size and samples). The TLASes and frames must outlive the
+// batch. SetCameras moves the cameras without recapturing; Download reads every framebuffer.
+class Batch {
+public:
+    struct Scene {
+        const TopLevelAccelerationStructure* tlas;
+        hrt_camera camera;
+        Frame* frame;
+    };
+    Batch(Context& ctx, const std::vector<Scene>& scenes, const hrt_trace_params& params, void* stream = nullptr)
+        : _ctx(ctx.Get()) {
+        std::vector<hrt_scene_desc> d;
+        for (const Scene& s : scenes) {
+            d.push_back(hrt_scene_desc{s.tlas->Structure(), s.camera, s.frame->Get()});
+            _frames.push_back(s.frame);
+        }
+        Check(_ctx, hrt_batch_create(_ctx, d.data(), uint32_t(d.size()), &params, stream, &_b), "hrt_batch_create");
+    }
+    ~Batch() { hrt_batch_destroy(_b); }
+    Batch(const Batch&) = delete;
+    Batch& operator=(const Batch&) = delete;
+
+    void Launch(void* stream = nullptr) { Check(_ctx, hrt_batch_launch(_b, stream), "hrt_batch_launch"); }
+    void SetCameras(const std::vector<hrt_camera>& cams, void* stream = nullptr) {
+        Check(_ctx, hrt_batch_set_cameras(_b, cams.data(), uint32_t(cams.size()), stream), "hrt_batch_set_cameras");
+    }
+    // Every scene's framebuffer (width * height * 4 floats each), in creation order; waits for
+    // the copies.
+    std::vector<std::vector<float>> Download(void* stream = nullptr) {
+        std::vector<std::vector<float>> out(_frames.size());
+        std::vector<float*> dst(_frames.size());
+        for (size_t i = 0; i < _frames.size(); ++i) {
+            out[i].resize(size_t(_frames[i]->Width()) * _frames[i]->Height() * 4);
+            dst[i] = out[i].data();
+        }
+        Check(_ctx, hrt_batch_download(_b, dst.data(), stream, 1), "hrt_batch_download");
+        return out;
+    }
+
+private:
+    hrt_context* _ctx;
+    hrt_batch* _b = nullptr;
+    std::vector<Frame*> _frames;
+};
 
 }  // namespace hrt
 

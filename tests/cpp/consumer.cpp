@@ -5,7 +5,9 @@
 //                            strands, argument errors; prints "host ok <checksum>"
 //   consumer gpu <out.bin>   a Phantom BLAS and a translated LSS BLAS (both quantised) in one
 //                            TLAS, one 128x96 frame with Shade(), shadow rays and hit records;
-//                            writes width, height, the pixels and the hit records to out.bin
+//                            writes width, height, the pixels and the hit records to out.bin;
+//                            the same frame rendered through a two-scene Batch must match it
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -91,6 +93,18 @@ int Gpu(const char* path) {
     std::fwrite(rgba.data(), 4, rgba.size(), f);
     std::fwrite(hits.data(), sizeof(hrt_hit), hits.size(), f);
     std::fclose(f);
+    // the same scene through a batch (beside a second, smaller view): same pixels within the
+    // rounding of the separately compiled occupancy variants
+    hrt::Frame f0(ctx, w, h, 1), f1(ctx, 64, 48, 1);
+    hrt::Batch batch(ctx,
+                     {{&tlas, hrt::LookAt({0.0f, 0.0f, 3.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, 40.0f, float(w) / h), &f0},
+                      {&tlas, hrt::LookAt({1.0f, 0.5f, 2.5f}, {0.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, 40.0f, 4.0f / 3.0f), &f1}},
+                     p);
+    batch.Launch();
+    std::vector<std::vector<float>> got = batch.Download();
+    if (got.size() != 2 || got[0].size() != rgba.size() || got[1].size() != size_t(64) * 48 * 4) return 12;
+    for (size_t i = 0; i < rgba.size(); ++i)
+        if (!(std::fabs(got[0][i] - rgba[i]) <= 1e-6f)) return 13;
     size_t nhit = 0;
     for (const hrt_hit& x : hits) nhit += x.t >= 0.0f;
     std::printf("gpu ok %zu hits\n", nhit);
