@@ -700,24 +700,30 @@ def batch_agreement_and_cpu(ctx, q, models, tuned, fb_timed):
 
 
 def run_batched_profile(args, dist):
-    """`--profile` on the batched workload: the quantised Phantom scenes alone as one batch (the
-    dominant kernel of the full batch, its Phantom group), replayed warmup + steps times for a
-    profiler, then counted. Parameters from the tune cache when it holds the batch's choice."""
+    """`--profile` on the batched workload: the Phantom scenes alone as one batch (the dominant
+    kernel of the full batch, its Phantom group), quantised or with --precision fp32, replayed
+    warmup + steps times for a profiler, then counted. Parameters from the tune cache when it holds
+    the batch's choice for that precision, otherwise from --variant, --refill, --speculative and
+    --leaf-again."""
     import torch
     import vkhrt_gb300 as H
     torch.cuda.set_device(dist.local)
     ctx = H.Context(dist.local)
     models = [x for x in batch_models() if int(x[0]["type"]) == 0]
+    fp32 = args.precision == "fp32"
+    prec = H.Precision.FP32 if fp32 else H.Precision.QUANTISED
     q = []
     for m, v, r, off in models:
         b = H.BottomLevelAccelerationStructure(H.BLASInput(type=m["type"], vertices=v, radius=r, strand_offsets=off,
-                                                           precision=H.Precision.QUANTISED), ctx)
+                                                           precision=prec), ctx)
         t = H.TopLevelAccelerationStructure([b], ctx)
         q.append((b, t, H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"]),
                   H.Frame(ctx, m["width"], m["height"], m["spp"])))
-    fields = {}
+    fields = {"kernel_variant": args.variant, "refill": args.refill, "speculative": args.speculative,
+              "leaf_again": args.leaf_again}
     if args.tune_cache and os.path.exists(args.tune_cache):
-        fields = {k: int(v) for k, v in json.load(open(args.tune_cache)).get(f"{BATCH_CONFIG}/quantised", {}).items()
+        key = f"{BATCH_CONFIG}/{'fp32' if fp32 else 'quantised'}"
+        fields = {k: int(v) for k, v in json.load(open(args.tune_cache)).get(key, fields).items()
                   if k in H.TUNED_FIELDS}
     p = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1}, **fields)
     batch = H.Batch(ctx, [(t, cam, fr) for (_, t, cam, fr) in q], p)
@@ -738,7 +744,7 @@ def run_batched_profile(args, dist):
         rays += st["primary_rays"] + st["shadow_rays"]
         nodes += st["nodes_visited"]
         prims += st["prims_tested"]
-    print(json.dumps({"profile": "c5 Phantom group", "scenes": len(q), "ms_per_replay": round(ms, 3),
+    print(json.dumps({"profile": "c5 Phantom group", "precision": "fp32" if fp32 else "quantised", "scenes": len(q), "ms_per_replay": round(ms, 3),
                       "rays_per_replay": int(rays), "nodes_visited": int(nodes), "prims_tested": int(prims),
                       "params": {k: int(getattr(p, k)) for k in H.TUNED_FIELDS},
                       "device_bytes": int(sum(b.info["device_bytes"] for (b, *_r) in q))}), flush=True)

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HRT_ABI_VERSION 8
+#define HRT_ABI_VERSION 9
 
 typedef enum hrt_status {
     HRT_OK = 0,
@@ -109,6 +109,19 @@ typedef struct hrt_blas_input {
      * reference's); every filled voxel is a box primitive reporting its grid index
      * x + y res_x + z res_x res_y as primitive id. Per-vertex radii are not used. */
     float voxel_size;
+    /* Material of a HRT_BLAS_MESH (other types ignore it, as the reference's hair output does):
+     * the reference's Material albedo (include/resources/gpu_resources.hpp:160-180) as
+     * triangle_closest_hit.rchit:71-81 fetches it. albedo = albedo_factor x the albedo map sampled
+     * at the hit's texture coordinate, which interpolates texcoords with the hit's barycentrics
+     * (1 - u - v, u, v) like the normal (rchit:39); bilinear, repeat addressing, texel centres at
+     * ((i + 0.5) / width, (j + 0.5) / height), full resolution (the reference's default sampler,
+     * gpu_resources.hpp:44-62; a closest-hit shader has no derivatives, so mip level 0). The
+     * Lambert shading modes multiply their colour by albedo.rgb; HRT_SHADE_DEBUG, the reference's
+     * output (rchit:84), does not use it. `memory` applies to texcoords and albedo_map. */
+    const float* texcoords;         /* 2 floats per vertex, or NULL (no map lookup) */
+    float albedo_factor[4];         /* RGBA, default 1, 1, 1, 1 */
+    const float* albedo_map;        /* width x height RGBA floats, row-major, row 0 at v = 0, or NULL */
+    uint32_t albedo_map_width, albedo_map_height; /* each 1..16384 with a map */
 } hrt_blas_input;
 
 #define HRT_BUILD_KEEP_INTERMEDIATE 1u /* keep Morton codes, binary tree, boxes (hrt_blas_get) */
@@ -143,10 +156,12 @@ typedef enum hrt_blas_part {
     HRT_PART_DOTS_VERTICES = 10,/* float[nprims][36] (DOTS), the reference's 12 vertices/segment */
     HRT_PART_LSS = 11,          /* float[nprims][8]: p0 xyz, p1 xyz, r0, r1 */
     HRT_PART_QNODES = 12,       /* raw quantised nodes (80 B each); of an FP32 BLAS only when kept */
-    HRT_PART_STRAND_VERTICES = 13 /* float[nentries][4] quantised Phantom strand vertex stream:
+    HRT_PART_STRAND_VERTICES = 13,/* float[nentries][4] quantised Phantom strand vertex stream:
                                      per run of joined lines (each starting where the previous ends,
                                      with the same radius there) the point before it, its start,
                                      each line's end, the point after it; {x, y, z, radius} */
+    HRT_PART_TRI_TEXCOORDS = 14   /* float[ntris][6]: a textured mesh's texture coordinates per
+                                     triangle, in triangle order (u0 v0 u1 v1 u2 v2) */
 } hrt_blas_part;
 
 typedef struct hrt_camera {

@@ -34,9 +34,14 @@ public:
     hrt_status status;
 };
 
+// The error carries the context's message (or the status's name), prefixed with the call unless
+// the message already starts with it.
 inline void Check(const hrt_context* ctx, hrt_status s, const char* call) {
-    if (s != HRT_OK)
-        throw Error(s, std::string(call) + ": " + (ctx ? hrt_last_error(ctx) : hrt_status_string(s)));
+    if (s == HRT_OK) return;
+    const char* m = ctx ? hrt_last_error(ctx) : nullptr;
+    std::string msg = m && *m ? m : hrt_status_string(s);
+    if (msg.rfind(call, 0) != 0) msg = std::string(call) + ": " + msg;
+    throw Error(s, msg);
 }
 
 // One device (the compute part of the reference's VulkanContext).
@@ -79,6 +84,12 @@ struct BLASInput {
     float constRadius = 0.02f;                        // geometry_processor.cpp:635
     float voxelSize = 0.0f;                           // HRT_BLAS_VOXELS (0 = 0.1)
     uint32_t width = 0;                               // BVH node fan-out 2..8 (0 = 8)
+    // HRT_BLAS_MESH material (triangle_closest_hit.rchit:71-81): albedo factor, and a map
+    // (albedoMapWidth x albedoMapHeight RGBA floats, row 0 at v = 0) sampled at texCoords
+    std::vector<float> texCoords;                     // 2 floats per vertex, or empty
+    std::array<float, 4> albedoFactor = {1.0f, 1.0f, 1.0f, 1.0f};
+    std::vector<float> albedoMap;
+    uint32_t albedoMapWidth = 0, albedoMapHeight = 0;
 };
 
 class BottomLevelAccelerationStructure {
@@ -108,6 +119,11 @@ public:
         b.normals = in.normals.empty() ? nullptr : in.normals.data();
         b.voxel_size = in.voxelSize;
         b.width = in.width;
+        b.texcoords = in.texCoords.empty() ? nullptr : in.texCoords.data();
+        for (int k = 0; k < 4; ++k) b.albedo_factor[k] = in.albedoFactor[k];
+        b.albedo_map = in.albedoMap.empty() ? nullptr : in.albedoMap.data();
+        b.albedo_map_width = in.albedoMapWidth;
+        b.albedo_map_height = in.albedoMapHeight;
         for (int k = 0; k < 16; ++k) b.transform[k] = in.transform[k];
         _transform = in.transform;
         Check(ctx.Get(), hrt_blas_build(ctx.Get(), &b, stream, &_blas), "hrt_blas_build");

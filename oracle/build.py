@@ -84,6 +84,7 @@ def load() -> ctypes.CDLL:
         "orc_scene_destroy": (None, [P]),
         "orc_scene_add_blas": (i32, [P, i32, i64, P, P]),
         "orc_scene_add_instance": (i32, [P, i32, P]),
+        "orc_scene_set_material": (i32, [P, i32, P, P, P, u32, u32]),
         "orc_trace_rays": (None, [P, P, i64, f32, f32, i32, i32, P, P, P, P]),
         "orc_render": (None, [P, P, P, u32, u32, u32, i32, u32, f32, f32, i32, f32, i32, i32, i64, i64,
                               P, P, P, P, P, P, P, u32, u32]),

@@ -925,6 +925,10 @@ struct Blas {
     std::vector<uint32_t> sorted;     // sorted position -> primitive
     Binary bt;
     Box root;
+    // mesh material: albedo factor; with a map, texture coordinates per triangle (6 floats)
+    float albedo[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+    std::vector<float> uv, map;
+    uint32_t map_w = 0, map_h = 0;
 };
 struct Instance {
     int blas;
@@ -959,7 +963,8 @@ static void build_blas(Blas& b) {
 template <class T> struct HitT {
     T t;
     uint32_t inst, prim, seg;  // prim = reported primitive id; seg = BVH primitive (segment)
-    T u;                       // curve / segment parameter
+    T u;                       // curve / segment parameter (mesh: barycentric weight of v1)
+    T v;                       // mesh: barycentric weight of v2
     tvec3<T> n;                // world-space normal
     int resolved64;
 };
@@ -1055,6 +1060,7 @@ static bool intersect_prim(const Blas& b, uint32_t inst, uint32_t s, const tvec3
         if (t >= T(0)) {
             take(t, s, b1, 0);
             if (better) {
+                h->v = b2;
                 if (!b.radius.empty()) {
                     const float* m = b.radius.data() + 9 * s;
                     T w = T(1) - b1 - b2;
@@ -1491,6 +1497,26 @@ int orc_scene_add_instance(void* s, int blas, const float* xf) {
     return int(sc->inst.size() - 1);
 }
 
+// Material of a mesh BLAS: albedo factor (4 floats), and with a map (w x h RGBA floats, row 0 at
+// v = 0) the texture coordinates of each triangle (6 floats: u0 v0 u1 v1 u2 v2). Returns 0, or -1
+// when the BLAS is not a mesh.
+int orc_scene_set_material(void* s, int blas, const float* albedo4, const float* uv, const float* map, uint32_t w,
+                           uint32_t h) {
+    Blas& b = static_cast<Scene*>(s)->blas[blas];
+    if (b.type != kMesh) return -1;
+    for (int k = 0; k < 4; ++k) b.albedo[k] = albedo4[k];
+    b.uv.clear();
+    b.map.clear();
+    b.map_w = b.map_h = 0;
+    if (uv && map && w && h) {
+        b.uv.assign(uv, uv + 6 * b.nprim);
+        b.map.assign(map, map + size_t(w) * h * 4);
+        b.map_w = w;
+        b.map_h = h;
+    }
+    return 0;
+}
+
 // Closest hit for explicit rays (o[3], d[3] per ray, FP32 inputs).
 // precision: 32 = FP32, 64 = FP64, 3264 = FP32 with FP64 re-solve of unresolved candidates.
 // Outputs per ray: t (double, -1 miss), prim, inst, normal (3 doubles).
@@ -1554,6 +1580,34 @@ void env_color(const float* env, uint32_t ew, uint32_t eh, const T d[3], T out[3
     }
 }
 
+// triangle_closest_hit.rchit:71-81, restated: a mesh hit's albedo, the factor times the map at
+// the texture coordinate interpolated with the hit's barycentrics (1 - u - v, u, v); bilinear,
+// repeat addressing (the coordinate wrapped into [0, 1) first), texel centres at (i + 0.5) / size.
+extern "C++" template <class T> tvec3<T> mesh_albedo(const Blas& b, const HitT<T>& hh) {
+    tvec3<T> a(T(b.albedo[0]), T(b.albedo[1]), T(b.albedo[2]));
+    if (b.map.empty() || b.uv.empty()) return a;
+    const float* q = b.uv.data() + 6 * size_t(hh.prim);
+    const T u = hh.u, v = hh.v, w = T(1) - u - v;
+    T s = w * T(q[0]) + u * T(q[2]) + v * T(q[4]);
+    T t = w * T(q[1]) + u * T(q[3]) + v * T(q[5]);
+    s -= std::floor(s);
+    t -= std::floor(t);
+    const int64_t W = b.map_w, H = b.map_h;
+    const T x = s * T(W) - T(0.5), y = t * T(H) - T(0.5);
+    const T fx = std::floor(x), fy = std::floor(y), ax = x - fx, ay = y - fy;
+    const int64_t x0 = fx >= T(0) ? std::min<int64_t>(int64_t(fx), W - 1) : W - 1;
+    const int64_t y0 = fy >= T(0) ? std::min<int64_t>(int64_t(fy), H - 1) : H - 1;
+    const int64_t x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
+    T c[3];
+    for (int k = 0; k < 3; ++k) {
+        const T c00 = b.map[4 * (y0 * W + x0) + k], c10 = b.map[4 * (y0 * W + x1) + k];
+        const T c01 = b.map[4 * (y1 * W + x0) + k], c11 = b.map[4 * (y1 * W + x1) + k];
+        const T lo = c00 + ax * (c10 - c00), hi = c01 + ax * (c11 - c01);
+        c[k] = lo + ay * (hi - lo);
+    }
+    return tvec3<T>(a.x * c[0], a.y * c[1], a.z * c[2]);
+}
+
 void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t w, uint32_t h, uint32_t spp,
                 int jitter, uint32_t seed, float tmin, float tmax, int shading, float shadow_tmin, int precision,
                 int nthreads, int64_t first_pixel, int64_t npixels, const uint32_t* pixel_list, double* t_out,
@@ -1598,6 +1652,11 @@ void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t 
                         }
                         sh = lit ? 0 : 1;
                         tvec3<double> c3 = lit ? shade(hh.n) : tvec3<double>(0.3f, 0.3f, 0.3f);
+                        const Blas& hb = sc.blas[sc.inst[hh.inst].blas];
+                        if (hb.type == kMesh) {
+                            const tvec3<double> a = mesh_albedo(hb, hh);
+                            c3 = tvec3<double>(c3.x * a.x, c3.y * a.y, c3.z * a.z);
+                        }
                         col[0] = c3.x; col[1] = c3.y; col[2] = c3.z;
                     }
                 } else if (env) {
@@ -1625,6 +1684,11 @@ void orc_render(void* s, const float* view_inv, const float* proj_inv, uint32_t 
                         }
                         sh = lit ? 0 : 1;
                         v3f c3 = lit ? shade(hh.n) : v3f(0.3f, 0.3f, 0.3f);
+                        const Blas& hb = sc.blas[sc.inst[hh.inst].blas];
+                        if (hb.type == kMesh) {
+                            const v3f a = mesh_albedo(hb, hh);
+                            c3 = v3f(c3.x * a.x, c3.y * a.y, c3.z * a.z);
+                        }
                         cf[0] = c3.x; cf[1] = c3.y; cf[2] = c3.z;
                     }
                 } else if (env) {

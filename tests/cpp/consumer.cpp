@@ -96,10 +96,12 @@ int Gpu(const char* path) {
     // the same scene through a batch (beside a second, smaller view): same pixels within the
     // rounding of the separately compiled occupancy variants
     hrt::Frame f0(ctx, w, h, 1), f1(ctx, 64, 48, 1);
+    hrt_trace_params pb = p;
+    pb.record_hits = 0;  // the batch's frames keep no hit records
     hrt::Batch batch(ctx,
                      {{&tlas, hrt::LookAt({0.0f, 0.0f, 3.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, 40.0f, float(w) / h), &f0},
                       {&tlas, hrt::LookAt({1.0f, 0.5f, 2.5f}, {0.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, 40.0f, 4.0f / 3.0f), &f1}},
-                     p);
+                     pb);
     batch.Launch();
     std::vector<std::vector<float>> got = batch.Download();
     if (got.size() != 2 || got[0].size() != rgba.size() || got[1].size() != size_t(64) * 48 * 4) return 12;

@@ -89,6 +89,16 @@ class OracleScene:
             self._keep.append(xf)
             orc.orc_scene_add_instance(self.h, b, P(xf))
 
+    def set_material(self, blas: int, albedo=(1.0, 1.0, 1.0, 1.0), tri_uv=None, albedo_map=None):
+        """A mesh BLAS's material: albedo factor, and a map (h, w, 4) sampled at the per-triangle
+        texture coordinates tri_uv (ntris, 6)."""
+        a = np.ascontiguousarray(albedo, np.float32)
+        uv = None if tri_uv is None else np.ascontiguousarray(tri_uv, np.float32)
+        m = None if albedo_map is None else np.ascontiguousarray(albedo_map, np.float32)
+        self._keep += [a, uv, m]
+        h, w = (0, 0) if m is None else m.shape[:2]
+        assert self.orc.orc_scene_set_material(self.h, blas, P(a), P(uv), P(m), w, h) == 0
+
     def trace_rays(self, rays: np.ndarray, precision: int = 64, tmin=0.001, tmax=10000.0, threads: int = 0):
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[0]

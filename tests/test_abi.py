@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
 def test_abi_version_and_status_strings():
     import vkhrt_gb300 as H
     lib = H.load()
-    assert lib.hrt_abi_version() == 8
+    assert lib.hrt_abi_version() == 9 == H.ABI_VERSION
     assert lib.hrt_status_string(0) == b"ok"
     assert lib.hrt_status_string(4) == b"traversal stack overflow"
 
@@ -64,3 +64,34 @@ def test_camera_matches_glm_conventions():
     f = 1 / np.tan(np.radians(20))
     assert np.isclose(Pm[0, 0], f, rtol=1e-6) and np.isclose(Pm[1, 1], -f, rtol=1e-6)  # Y flipped
     assert np.isclose(Pm[3, 2], -1.0)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every ctypes mirror of an hrt.h structure has the C compiler's size and field offsets."""
+    import ctypes
+    import subprocess
+    import vkhrt_gb300 as H
+    mirrors = {"hrt_blas_input": H.BLASInputC, "hrt_blas_info": H.BLASInfoC, "hrt_camera": H.CameraC,
+               "hrt_trace_params": H.TraceParamsC, "hrt_frame_stats": H.FrameStatsC,
+               "hrt_scene_desc": H.SceneDescC, "hrt_strand_params": H.StrandParamsC}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "hrt.h"', "int main(void) {"]
+    for cname, cls in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            cf = "async" if f == "async_" else f
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {cf}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = str(tmp_path / "layout")
+    r = subprocess.run(["gcc", "-std=c11", "-I" + os.path.join(ROOT, "include"), str(src), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = {}
+    for line in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines():
+        cname, f, v = line.split()
+        got[(cname, f)] = int(v)
+    for cname, cls in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)

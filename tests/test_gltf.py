@@ -125,3 +125,96 @@ def test_gltf_errors(tmp_path):
                                                    "meshes": [{"primitives": [{"attributes": {}}]}]}))
     with pytest.raises(gltf.GltfError):
         gltf.load(str(tmp_path / "bad.gltf"))
+
+
+def _png(img: np.ndarray) -> bytes:
+    """An 8-bit PNG of img (h, w, c) whose rows use the filters None, Sub, Up, Average and Paeth in
+    turn (the PNG specification's predictors), so that decoding undoes each of them."""
+    import zlib
+    h, w, c = img.shape
+    ctype = {1: 0, 2: 4, 3: 2, 4: 6}[c]
+    rows = img.reshape(h, w * c).astype(np.int32)
+    out = bytearray()
+    prev = np.zeros(w * c, np.int32)
+    for y in range(h):
+        f = y % 5
+        cur = rows[y]
+        a = np.concatenate([np.zeros(c, np.int32), cur[:-c]])
+        b = prev
+        cc = np.concatenate([np.zeros(c, np.int32), prev[:-c]])
+        if f == 0:
+            pred = np.zeros_like(cur)
+        elif f == 1:
+            pred = a
+        elif f == 2:
+            pred = b
+        elif f == 3:
+            pred = (a + b) >> 1
+        else:
+            pa, pb, pc = np.abs(b - cc), np.abs(a - cc), np.abs(a + b - 2 * cc)
+            pred = np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, cc))
+        out.append(f)
+        out += ((cur - pred) & 255).astype(np.uint8).tobytes()
+        prev = cur
+
+    def chunk(kind, body):
+        return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, ctype, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(bytes(out))) + chunk(b"IEND", b""))
+
+
+@pytest.mark.parametrize("channels", [1, 2, 3, 4])
+def test_png_decoder_undoes_every_row_filter(channels):
+    rng = np.random.default_rng(channels)
+    img = rng.integers(0, 256, (11, 7, channels), dtype=np.uint8)
+    got = gltf.decode_png(_png(img))
+    assert got.shape == (11, 7, 4)
+    want = np.ones((11, 7, 4), np.float32)
+    px = img.astype(np.float32) / np.float32(255.0)
+    if channels <= 2:
+        want[..., :3] = px[..., :1]
+        if channels == 2:
+            want[..., 3] = px[..., 1]
+    else:
+        want[..., :channels] = px
+    assert np.array_equal(got, want)
+
+
+def test_gltf_mesh_material_and_texture(tmp_path):
+    """A textured quad: TEXCOORD_0 (normalised unsigned shorts), the base colour factor and an
+    embedded PNG base colour texture become the mesh BLAS's texcoords, albedo factor and map; an
+    image that is not a PNG leaves the map out with a note."""
+    v = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float32)
+    idx = np.array([0, 1, 2, 0, 2, 3], np.uint16)
+    tc = np.array([[0, 0], [65535, 0], [65535, 65535], [0, 65535]], np.uint16)
+    blob = v.tobytes() + idx.tobytes() + tc.tobytes()
+    img = np.random.default_rng(4).integers(0, 256, (3, 5, 4), dtype=np.uint8)
+    png = _png(img)
+    doc = {
+        "asset": {"version": "2.0"}, "scene": 0, "scenes": [{"nodes": [0]}], "nodes": [{"mesh": 0}],
+        "meshes": [{"primitives": [{"attributes": {"POSITION": 0, "TEXCOORD_0": 2}, "indices": 1, "material": 0}]}],
+        "materials": [{"pbrMetallicRoughness": {"baseColorFactor": [0.5, 0.25, 1.0, 1.0],
+                                                "baseColorTexture": {"index": 0}}}],
+        "textures": [{"source": 0}],
+        "images": [{"uri": "data:image/png;base64," + base64.b64encode(png).decode()}],
+        "buffers": [{"byteLength": len(blob), "uri": "data:application/octet-stream;base64," +
+                     base64.b64encode(blob).decode()}],
+        "bufferViews": [{"buffer": 0, "byteOffset": 0, "byteLength": 48},
+                        {"buffer": 0, "byteOffset": 48, "byteLength": 12},
+                        {"buffer": 0, "byteOffset": 60, "byteLength": 16}],
+        "accessors": [{"bufferView": 0, "componentType": 5126, "count": 4, "type": "VEC3"},
+                      {"bufferView": 1, "componentType": 5123, "count": 6, "type": "SCALAR"},
+                      {"bufferView": 2, "componentType": 5123, "count": 4, "type": "VEC2", "normalized": True}],
+    }
+    path = tmp_path / "quad.gltf"
+    path.write_text(json.dumps(doc))
+    (p,) = gltf.load(str(path))
+    assert p.kind == "triangles" and p.albedo_factor == (0.5, 0.25, 1.0, 1.0) and p.note == ""
+    assert np.array_equal(p.texcoords, np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32))
+    assert np.array_equal(p.albedo_map, img.astype(np.float32) / np.float32(255.0))
+    inp = p.blas_input()
+    assert inp.albedo_map is p.albedo_map and inp.texcoords is p.texcoords and inp.albedo_factor == p.albedo_factor
+    doc["images"] = [{"uri": "data:image/jpeg;base64," + base64.b64encode(b"\xff\xd8\xff").decode()}]
+    path.write_text(json.dumps(doc))
+    (q,) = gltf.load(str(path))
+    assert q.albedo_map is None and q.texcoords is None and "not a PNG" in q.note and q.albedo_factor[0] == 0.5

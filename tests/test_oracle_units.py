@@ -201,6 +201,64 @@ def test_mesh_triangle_known_answer(orc):
     assert boxes.tolist() == [[0, 0, 1, 1, 1, 1]]
 
 
+def _bilinear_repeat(m, s, t):
+    """Bilinear lookup with repeat addressing, texel centres at (i + 0.5) / size (numpy)."""
+    hgt, wid = m.shape[:2]
+    s = s - np.floor(s)
+    t = t - np.floor(t)
+    x, y = s * wid - 0.5, t * hgt - 0.5
+    fx, fy = np.floor(x), np.floor(y)
+    ax, ay = (x - fx)[:, None], (y - fy)[:, None]
+    x0, y0 = fx.astype(np.int64) % wid, fy.astype(np.int64) % hgt
+    x1, y1 = (x0 + 1) % wid, (y0 + 1) % hgt
+    m = m.astype(np.float64)
+    lo = m[y0, x0, :3] + ax * (m[y0, x1, :3] - m[y0, x0, :3])
+    hi = m[y1, x0, :3] + ax * (m[y1, x1, :3] - m[y1, x0, :3])
+    return lo + ay * (hi - lo)
+
+
+def test_mesh_material_albedo_known_answer(orc):
+    """triangle_closest_hit.rchit:71-81 restated: a quad in the z = 0 plane whose texture
+    coordinates are an affine function of position, stretched past [0, 1) and negative so the
+    repeat addressing wraps, with a 5 x 3 map. Lambert shading of a face normal along z gives the
+    ambient 0.3 times the albedo; the albedo must equal the factor times a numpy bilinear lookup
+    at the hit point's coordinate (FP64 oracle to 1e-9, FP32 oracle to 1e-5). Without a map the
+    albedo is the factor alone; HRT_SHADE_DEBUG ignores the material."""
+    from hairscene import OracleScene
+    import vkhrt_gb300 as H
+    quad = np.array([[-2, -2, 0], [2, -2, 0], [2, 2, 0], [-2, 2, 0]], np.float32)  # covers the view
+    tri = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    scale, off = np.array([2.5, 1.75]), np.array([-0.75, 0.3])
+    tc = ((quad[:, :2] + 2.0) * 0.25 * scale + off).astype(np.float32)
+    rng = np.random.default_rng(8)
+    amap = rng.uniform(0.1, 1.0, (3, 5, 4)).astype(np.float32)
+    factor = (0.9, 0.6, 0.8, 1.0)
+    osc = OracleScene(orc, [(3, quad[tri].reshape(-1, 9), None)])
+    osc.set_material(0, factor, tc[tri].reshape(-1, 6), amap)
+    w, h = 16, 12
+    vi, pi = H.camera_arrays(H.scene_camera(w, h, lib=H.bind_workload(orc)))
+    o64 = osc.render(vi, pi, w, h, shading=1, precision=64)
+    o32 = osc.render(vi, pi, w, h, shading=1, precision=32)
+    assert (o64["t"] > 0).all() and (o64["prim"] <= 1).all()
+    ro, rd = np.zeros(3, np.float32), np.zeros(3, np.float32)
+    hitp = []
+    for p in range(w * h):
+        orc.orc_raygen_f32(P(vi), P(pi), p % w, p // w, w, h, ctypes.c_float(0.5), ctypes.c_float(0.5), P(ro), P(rd))
+        hitp.append(ro.astype(np.float64) + o64["t"][p] * rd.astype(np.float64))
+    hitp = np.array(hitp)
+    uv = (hitp[:, :2] + 2.0) * 0.25 * scale + off
+    expect = 0.3 * np.asarray(factor[:3]) * _bilinear_repeat(amap, uv[:, 0], uv[:, 1])
+    assert np.abs(o64["fb"][:, :3] - expect).max() < 1e-6  # the FP32 framebuffer of FP64 colours
+    assert np.abs(o32["fb"][:, :3] - expect).max() < 1e-5
+    plain = OracleScene(orc, [(3, quad[tri].reshape(-1, 9), None)])
+    plain.set_material(0, factor)
+    assert np.allclose(plain.render(vi, pi, w, h, shading=1, precision=64)["fb"][:, :3],
+                       0.3 * np.asarray(factor[:3]), atol=1e-7)
+    dbg = osc.render(vi, pi, w, h, shading=0, precision=64)["fb"]
+    unlit = OracleScene(orc, [(3, quad[tri].reshape(-1, 9), None)]).render(vi, pi, w, h, shading=0, precision=64)["fb"]
+    assert np.array_equal(dbg, unlit)
+
+
 def test_environment_map_miss(orc):
     """miss.rmiss:17-37 on an empty scene: a constant map gives 1 - exp(-c) under gamma 1/2.2;
     a map that varies only in u shows the direction -> (u, v) mapping and the bilinear blend."""

@@ -26,12 +26,17 @@ LIB_PATH = os.path.join(_HERE, "libhrt.so")
 c_f, c_u32, c_i32, c_u64, c_p = ctypes.c_float, ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_void_p
 
 
+ABI_VERSION = 9  # HRT_ABI_VERSION of include/hrt.h that the structures below mirror
+
+
 class BLASInputC(ctypes.Structure):
     _fields_ = [("type", c_i32), ("precision", c_i32), ("memory", c_i32), ("max_leaf", c_u32),
                 ("vertices", c_p), ("radius", c_p), ("strand_offsets", c_p), ("line_indices", c_p),
                 ("nvertices", c_u64), ("nstrands", c_u64), ("nlines", c_u64), ("const_radius", c_f),
                 ("transform", c_f * 16), ("width", c_u32), ("flags", c_u32), ("tri_indices", c_p),
-                ("ntris", c_u64), ("normals", c_p), ("voxel_size", c_f)]
+                ("ntris", c_u64), ("normals", c_p), ("voxel_size", c_f), ("texcoords", c_p),
+                ("albedo_factor", c_f * 4), ("albedo_map", c_p), ("albedo_map_width", c_u32),
+                ("albedo_map_height", c_u32)]
 
 
 class BLASInfoC(ctypes.Structure):
@@ -133,6 +138,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.hrt_abi_version() != ABI_VERSION:  # the structures below follow this version of hrt.h
+        raise RuntimeError(f"{path} implements ABI {lib.hrt_abi_version()}, this binding ABI {ABI_VERSION}")
     _lib = lib
     return lib
 
@@ -182,14 +189,16 @@ class Part(enum.IntEnum):
     LSS = 11
     QNODES = 12
     STRAND_VERTICES = 13
+    TRI_TEXCOORDS = 14
 
 
 @dataclass
 class BLASInput:
     """Geometry of one BLAS (hrt_blas_input): hair (strand_offsets or line_indices) or, for
-    BLASType.eMesh, indexed triangles (tri_indices, optional per-vertex normals). BLASType.eVoxels
-    voxelises the strands' lines as capsules of radius const_radius on cubes of voxel_size (0 =
-    0.1); each filled voxel reports its grid index as primitive id."""
+    BLASType.eMesh, indexed triangles (tri_indices, optional per-vertex normals) and a material
+    (albedo_factor, and albedo_map sampled at texcoords; the Lambert shading modes multiply by the
+    albedo). BLASType.eVoxels voxelises the strands' lines as capsules of radius const_radius on
+    cubes of voxel_size (0 = 0.1); each filled voxel reports its grid index as primitive id."""
     type: BLASType
     vertices: np.ndarray                      # (nv, 3) float32
     radius: np.ndarray | None = None          # (nv,) float32 per vertex
@@ -204,6 +213,9 @@ class BLASInput:
     width: int = 0                            # BVH node fan-out 2..8 (0 = 8)
     keep_intermediate: bool = False
     voxel_size: float = 0.0
+    texcoords: np.ndarray | None = None       # (nv, 2) float32 (mesh)
+    albedo_factor: tuple = (1.0, 1.0, 1.0, 1.0)
+    albedo_map: np.ndarray | None = None      # (h, w, 4) float32 RGBA, row 0 at v = 0 (mesh)
 
 
 class Context:
@@ -275,6 +287,19 @@ class BottomLevelAccelerationStructure:
             nm = np.ascontiguousarray(inp.normals, dtype=np.float32).reshape(-1, 3)
             self._keep.append(nm)
             c.normals = _ptr(nm)
+        if inp.texcoords is not None:
+            tc = np.ascontiguousarray(inp.texcoords, dtype=np.float32).reshape(-1, 2)
+            self._keep.append(tc)
+            c.texcoords = _ptr(tc)
+        for k in range(4):
+            c.albedo_factor[k] = float(inp.albedo_factor[k])
+        if inp.albedo_map is not None:
+            am = np.ascontiguousarray(inp.albedo_map, dtype=np.float32)
+            if am.ndim != 3 or am.shape[2] != 4:
+                raise ValueError("albedo_map must be (height, width, 4)")
+            self._keep.append(am)
+            c.albedo_map = _ptr(am)
+            c.albedo_map_height, c.albedo_map_width = am.shape[0], am.shape[1]
         c.const_radius = inp.const_radius
         xf = np.asarray(inp.transform, dtype=np.float32).reshape(4, 4)
         for i, val in enumerate(xf.T.reshape(-1)):  # column major

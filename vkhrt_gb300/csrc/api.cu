@@ -36,6 +36,11 @@ struct hrt_blas {
     float const_radius = 0.0f;
     bool has_radius = false, has_normals = false;
     std::vector<uint32_t> line_off, vert_off, line_idx, tri_idx;
+    // mesh material (device copies owned by the BLAS)
+    float albedo[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+    float* uv = nullptr;  // float[ntris][6]
+    float4* albedo_map = nullptr;
+    uint32_t map_w = 0, map_h = 0;
 };
 
 namespace {
@@ -477,6 +482,43 @@ void hrt_blas_input_default(hrt_blas_input* in) {
     for (int k = 0; k < 4; ++k) in->transform[5 * k] = 1.0f;
 }
 
+// A mesh's material on the device: the albedo factor, and with a map and texture coordinates the
+// per-triangle coordinates (gathered on the host through the kept triangle indices) and the map.
+static hrt_status upload_material(hrt_context* ctx, const hrt_blas_input* in, hrt_blas* b) {
+    for (int k = 0; k < 4; ++k) b->albedo[k] = in->albedo_factor[k];
+    if (!in->albedo_map || !in->texcoords || b->nprims == 0) return HRT_OK;
+    const uint32_t w = in->albedo_map_width, h = in->albedo_map_height;
+    if (w < 1 || w > 16384 || h < 1 || h > 16384)
+        return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: albedo map of %ux%u texels; each side must be 1..16384",
+                    w, h);
+    const bool host = in->memory == HRT_MEMORY_HOST;
+    std::vector<float> tc;
+    const float* t = in->texcoords;
+    if (!host) {
+        tc.resize(2 * b->nvertices);
+        cudaError_t e = cudaMemcpy(tc.data(), in->texcoords, tc.size() * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "hrt_blas_build: read texcoords");
+        t = tc.data();
+    }
+    std::vector<float> uv(6 * b->nprims);
+    for (uint64_t i = 0; i < b->nprims; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const uint64_t v = b->tri_idx[3 * i + k];
+            uv[6 * i + 2 * k] = t[2 * v];
+            uv[6 * i + 2 * k + 1] = t[2 * v + 1];
+        }
+    const uint64_t map_bytes = uint64_t(w) * h * 16;
+    cudaError_t e = cudaMalloc(&b->uv, uv.size() * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(b->uv, uv.data(), uv.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->albedo_map, map_bytes);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->albedo_map, in->albedo_map, map_bytes, host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "hrt_blas_build: upload the material");
+    b->map_w = w;
+    b->map_h = h;
+    return HRT_OK;
+}
+
 // Builds a triangle-mesh BLAS: gathers the indexed triangles (and vertex normals) on the device
 // and runs the common BVH build over them.
 static hrt_status build_mesh(hrt_context* ctx, const hrt_blas_input* in, cudaStream_t s, hrt_blas** out) {
@@ -576,6 +618,11 @@ static hrt_status build_mesh(hrt_context* ctx, const hrt_blas_input* in, cudaStr
         return fail(ctx, HRT_ERR_CUDA, "BVH build: %s", m.empty() ? cudaGetErrorString(e) : m.c_str());
     }
     cleanup();
+    const hrt_status st = upload_material(ctx, in, b);
+    if (st != HRT_OK) {
+        hrt_blas_destroy(b);
+        return st;
+    }
     *out = b;
     return HRT_OK;
 }
@@ -855,6 +902,8 @@ hrt_status hrt_blas_destroy(hrt_blas* b) {
     if (!b) return HRT_OK;
     DeviceSet ds(b->ctx->device);
     free_build_output(b->out);
+    if (b->uv) cudaFree(b->uv);
+    if (b->albedo_map) cudaFree(b->albedo_map);
     delete b;
     return HRT_OK;
 }
@@ -887,14 +936,21 @@ struct SerialHeader {
     float const_radius;
     uint32_t has_radius, has_normals;
     uint64_t nlevels, n_line_off, n_vert_off, n_line_idx, n_tri_idx;
+    float albedo[4];          // mesh material: factor, then n_uv texture-coordinate floats and
+    uint32_t map_w, map_h;    // map_w x map_h RGBA texels after the arrays (none without a map)
+    uint64_t n_uv;
 };
-constexpr uint32_t kSerialVersion = 3;
+constexpr uint32_t kSerialVersion = 4;
+
+uint64_t material_bytes(const hrt_blas* b) {
+    return b->albedo_map ? b->nprims * 24 + uint64_t(b->map_w) * b->map_h * 16 : 0;
+}
 
 uint64_t serial_size(const hrt_blas* b) {
     const BuildOutput& o = b->out;
     return sizeof(SerialHeader) +
            4 * (o.level_start.size() + b->line_off.size() + b->vert_off.size() + b->line_idx.size() + b->tri_idx.size()) +
-           o.nnodes * o.node_bytes + o.nslots * o.prim_bytes + o.nverts * 16 + o.nslots * 4;
+           o.nnodes * o.node_bytes + o.nslots * o.prim_bytes + o.nverts * 16 + o.nslots * 4 + material_bytes(b);
 }
 
 // Reads a u32 array of n entries at *p, advancing it; false past the end.
@@ -984,6 +1040,10 @@ hrt_status hrt_blas_serialize(const hrt_blas* b, void* dst, uint64_t bytes) {
     h.n_vert_off = b->vert_off.size();
     h.n_line_idx = b->line_idx.size();
     h.n_tri_idx = b->tri_idx.size();
+    memcpy(h.albedo, b->albedo, sizeof(h.albedo));
+    h.map_w = b->albedo_map ? b->map_w : 0;
+    h.map_h = b->albedo_map ? b->map_h : 0;
+    h.n_uv = b->albedo_map ? 6 * b->nprims : 0;
     uint8_t* p = static_cast<uint8_t*>(dst);
     memcpy(p, &h, sizeof(h));
     p += sizeof(h);
@@ -994,7 +1054,9 @@ hrt_status hrt_blas_serialize(const hrt_blas* b, void* dst, uint64_t bytes) {
     struct { const void* src; uint64_t n; } parts[] = {{o.nodes, o.nnodes * o.node_bytes},
                                                       {o.prims, o.nslots * o.prim_bytes},
                                                       {o.verts, o.nverts * 16},
-                                                      {o.prim_ids, o.nslots * 4}};
+                                                      {o.prim_ids, o.nslots * 4},
+                                                      {b->uv, h.n_uv * 4},
+                                                      {b->albedo_map, uint64_t(h.map_w) * h.map_h * 16}};
     for (auto& q : parts) {
         if (q.n) CK(ctx, cudaMemcpy(p, q.src, q.n, cudaMemcpyDeviceToHost), "hrt_blas_serialize");
         p += q.n;
@@ -1022,7 +1084,10 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
         h.node_bytes != want_node || h.prim_bytes != want_prim || h.nprims >= (1ull << 29) || (h.nprims << ref_shift(h.type)) >= (1ull << 29) ||
         h.nnodes > (h.nprims << ref_shift(h.type)) + 1 ||
         h.nverts > 4 * h.nprims || (h.type == HRT_BLAS_PHANTOM && quant ? (h.nprims && h.nverts < h.nprims + 3) : h.nverts != 0) ||
-        (h.nprims && !h.nnodes) || h.max_leaf < 1 || h.max_leaf > 3)
+        (h.nprims && !h.nnodes) || h.max_leaf < 1 || h.max_leaf > 3 ||
+        (h.n_uv ? (h.type != HRT_BLAS_MESH || h.n_uv != 6 * h.nprims || h.map_w < 1 || h.map_w > 16384 || h.map_h < 1 ||
+                   h.map_h > 16384)
+                : (h.map_w || h.map_h)))
         return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_deserialize: inconsistent header");
     hrt_blas* b = new (std::nothrow) hrt_blas();
     if (!b) return fail(ctx, HRT_ERR_OOM, "hrt_blas_deserialize: host allocation");
@@ -1042,6 +1107,7 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
     b->const_radius = h.const_radius;
     b->has_radius = h.has_radius != 0;
     b->has_normals = h.has_normals != 0;
+    memcpy(b->albedo, h.albedo, sizeof(b->albedo));
     BuildOutput& o = b->out;
     if (!take_u32(p, end, h.nlevels, o.level_start) || !take_u32(p, end, h.n_line_off, b->line_off) ||
         !take_u32(p, end, h.n_vert_off, b->vert_off) || !take_u32(p, end, h.n_line_idx, b->line_idx) ||
@@ -1050,7 +1116,8 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
     const uint32_t shift = ref_shift(h.type);
     const uint64_t nslots = h.nprims << shift;
     const uint64_t nb = h.nnodes * h.node_bytes, pbytes = nslots * h.prim_bytes, rb = h.nverts * 16, ib = nslots * 4;
-    if (nb + pbytes + rb + ib > uint64_t(end - p)) return reject("truncated arrays");
+    const uint64_t ub = h.n_uv * 4, mb = uint64_t(h.map_w) * h.map_h * 16;
+    if (nb + pbytes + rb + ib + ub + mb > uint64_t(end - p)) return reject("truncated arrays");
     const uint8_t* nodes = p;
     const uint8_t* prims = p + nb;
     if (const char* why = check_tree(h.type, h.precision, nslots, h.nnodes, h.nverts, nodes, prims, o.level_start))
@@ -1082,7 +1149,10 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
                                                                      {reinterpret_cast<void**>(&o.prim_ids), prims + pbytes + rb, ib},
                                                                      {reinterpret_cast<void**>(&o.partner),
                                                                       reinterpret_cast<const uint8_t*>(partner.data()),
-                                                                      partner.size() * 4}};
+                                                                      partner.size() * 4},
+                                                                     {reinterpret_cast<void**>(&b->uv), prims + pbytes + rb + ib, ub},
+                                                                     {reinterpret_cast<void**>(&b->albedo_map),
+                                                                      prims + pbytes + rb + ib + ub, mb}};
     for (auto& q : parts) {
         if (!q.n || e != cudaSuccess) continue;
         e = cudaMalloc(q.dst, q.n);
@@ -1090,10 +1160,11 @@ hrt_status hrt_blas_deserialize(hrt_context* ctx, const void* src, uint64_t byte
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
-        free_build_output(b->out);
-        delete b;
+        hrt_blas_destroy(b);
         return cuda_fail(ctx, e, "hrt_blas_deserialize");
     }
+    b->map_w = h.map_w;
+    b->map_h = h.map_h;
     o.nslots = nslots;
     o.device_bytes = nb + pbytes + rb + ib + partner.size() * 4;
     *out = b;
@@ -1106,7 +1177,7 @@ hrt_status hrt_blas_get_info(const hrt_blas* b, hrt_blas_info* o) {
     o->nnodes = b->out.nnodes;
     o->node_bytes = b->out.node_bytes;
     o->prim_bytes = b->out.prim_bytes;
-    o->device_bytes = b->out.device_bytes;
+    o->device_bytes = b->out.device_bytes + material_bytes(b);
     memcpy(o->bounds, b->out.bounds, sizeof(o->bounds));
     o->build_ms = b->build_ms;
     return HRT_OK;
@@ -1138,6 +1209,7 @@ hrt_status hrt_blas_get(const hrt_blas* b, int32_t part, void* dst, uint64_t byt
         case HRT_PART_CURVES: src = o.curves; need = n * 48; break;
         case HRT_PART_LSS: src = b->type == HRT_BLAS_LSS ? o.geom : nullptr; need = n * 32; break;
         case HRT_PART_STRAND_VERTICES: src = o.verts; need = o.nverts * 16; break;
+        case HRT_PART_TRI_TEXCOORDS: src = b->uv; need = b->nprims * 24; break;
         case HRT_PART_DOTS_VERTICES: {
             if (b->type != HRT_BLAS_DOTS) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_get: not a DOTS BLAS");
             need = n * 144;
@@ -1238,6 +1310,11 @@ hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint3
         d.b.nprims = uint32_t(b->nprims);
         d.b.nnodes = uint32_t(b->out.nnodes);
         for (int k = 0; k < 3; ++k) { d.b.lo[k] = b->out.bounds[k]; d.b.hi[k] = b->out.bounds[3 + k]; }
+        for (int k = 0; k < 4; ++k) d.b.albedo[k] = b->albedo[k];
+        d.b.uv = b->uv;
+        d.b.albedo_map = b->albedo_map;
+        d.b.map_w = b->map_w;
+        d.b.map_h = b->map_h;
         d.identity = is_identity(b->transform) ? 1u : 0u;
         double m[16], iv[16];
         for (int k = 0; k < 16; ++k) m[k] = b->transform[k];

@@ -1078,6 +1078,36 @@ __device__ V3<float> env_color(const float4* env, uint32_t w, uint32_t h, V3<flo
     return mk(c[0], c[1], c[2]);
 }
 
+// triangle_closest_hit.rchit:71-81: the mesh material's albedo at a hit, albedo_factor x the
+// map at the interpolated texture coordinate (rchit:39, barycentrics (1 - u - v, u, v) with u, v
+// in h.u, h.ts). Bilinear with repeat addressing, texel centres at (i + 0.5) / size, row 0 at
+// v = 0; the coordinate is wrapped into [0, 1) first, and every texel index stays in the map.
+__device__ V3<float> mesh_albedo(const DevBlas& B, const Hit& h) {
+    V3<float> a = mk(B.albedo[0], B.albedo[1], B.albedo[2]);
+    if (!B.albedo_map || !B.uv) return a;
+    const float* q = B.uv + 6 * size_t(h.id);
+    const float u = h.u, v = h.ts, w = __fsub_rn(__fsub_rn(1.0f, u), v);
+    float s = fmaf(v, __ldg(q + 4), fmaf(u, __ldg(q + 2), __fmul_rn(w, __ldg(q))));
+    float t = fmaf(v, __ldg(q + 5), fmaf(u, __ldg(q + 3), __fmul_rn(w, __ldg(q + 1))));
+    s = __fsub_rn(s, floorf(s));
+    t = __fsub_rn(t, floorf(t));
+    const int W = int(B.map_w), H = int(B.map_h);
+    const float x = fmaf(s, float(W), -0.5f), y = fmaf(t, float(H), -0.5f);
+    const float fx = floorf(x), fy = floorf(y);
+    const float ax = __fsub_rn(x, fx), ay = __fsub_rn(y, fy);
+    // fx, fy in [-1, size - 1]; anything else (a NaN coordinate) takes the last texel
+    const int x0 = fx >= 0.0f ? min(int(fx), W - 1) : W - 1, y0 = fy >= 0.0f ? min(int(fy), H - 1) : H - 1;
+    const int x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
+    const float4* m = B.albedo_map;
+    const float4 c00 = __ldg(m + size_t(y0) * W + x0), c10 = __ldg(m + size_t(y0) * W + x1);
+    const float4 c01 = __ldg(m + size_t(y1) * W + x0), c11 = __ldg(m + size_t(y1) * W + x1);
+    auto lerp = [](float p, float r, float f) { return fmaf(f, __fsub_rn(r, p), p); };
+    a.x = __fmul_rn(a.x, lerp(lerp(c00.x, c10.x, ax), lerp(c01.x, c11.x, ax), ay));
+    a.y = __fmul_rn(a.y, lerp(lerp(c00.y, c10.y, ax), lerp(c01.y, c11.y, ax), ay));
+    a.z = __fmul_rn(a.z, lerp(lerp(c00.z, c10.z, ax), lerp(c01.z, c11.z, ax), ay));
+    return a;
+}
+
 // ray_gen.rgen:18-24, every operation rounded separately (matches the CPU restatement).
 __device__ void raygen(const float* V, const float* P, uint32_t px, uint32_t py, uint32_t w, uint32_t hgt, float jx,
                        float jy, V3<float>* o, V3<float>* d) {
@@ -1141,6 +1171,9 @@ constexpr int kRefill = 16;
 template <int kNodes, int kType, int kMinBlocks, int kPass>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch L) {
     __shared__ uint2 s_stack[kShort][kThreads];
+    // the hit's albedo while its shadow ray runs (mixed-type kernel: mesh materials), kept out of
+    // the registers the traversal needs
+    __shared__ float s_alb[kType == kMixed ? 3 : 1][kType == kMixed ? kThreads : 1];
     uint2 l_stack[kStackSize - kShort];
     const int tid = threadIdx.x, lane = tid & 31;
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -1266,6 +1299,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         shadow = false;
         start_ray(o, d, L.tmin, L.tmax);
     };
+    // shading.glsl Shade(): |n.l| light + ambient, times the albedo (1 except on meshes with a material)
+    auto add_shade = [&](float l) {
+        float c0 = fmaf(l, 0.4f, 0.3f), c1 = fmaf(l, 0.2f, 0.3f), c2 = fmaf(l, 0.1f, 0.3f);
+        if (kType == kMixed) {
+            c0 = __fmul_rn(c0, s_alb[0][tid]);
+            c1 = __fmul_rn(c1, s_alb[1][tid]);
+            c2 = __fmul_rn(c2, s_alb[2][tid]);
+        }
+        acc0 = __fadd_rn(acc0, c0);
+        acc1 = __fadd_rn(acc1, c1);
+        acc2 = __fadd_rn(acc2, c2);
+    };
     auto next_sample = [&]() {
         const SceneLaunch& S = L.scenes[si];
         ++sample;
@@ -1318,6 +1363,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             }
             V3<float> n = hit_normal(S.inst[h.inst], h, wo, wd);
             ndl = fabsf(n.y);  // shading.glsl: |dot(n, (0,-1,0))|
+            if (kType == kMixed) {  // meshes run in the mixed-type kernel only
+                const DevBlas& HB = S.inst[h.inst].b;
+                const V3<float> a = HB.type == HRT_BLAS_MESH ? mesh_albedo(HB, h) : mk(1.0f, 1.0f, 1.0f);
+                s_alb[0][tid] = a.x;
+                s_alb[1][tid] = a.y;
+                s_alb[2][tid] = a.z;
+            }
             if (L.shading == HRT_SHADE_LAMBERT_SHADOW) {
                 skip_inst = h.inst;
                 // the hit segment's slots: its own and, for two-reference BLASes, its partner's
@@ -1330,16 +1382,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 start_ray(hp, mk(0.0f, 1.0f, 0.0f), L.shadow_tmin, L.tmax);
                 return;
             }
-            acc0 = __fadd_rn(acc0, fmaf(ndl, 0.4f, 0.3f));
-            acc1 = __fadd_rn(acc1, fmaf(ndl, 0.2f, 0.3f));
-            acc2 = __fadd_rn(acc2, fmaf(ndl, 0.1f, 0.3f));
+            add_shade(ndl);
             next_sample();
             return;
         }
-        float lit = shadow_hit ? 0.0f : ndl;
-        acc0 = __fadd_rn(acc0, fmaf(lit, 0.4f, 0.3f));
-        acc1 = __fadd_rn(acc1, fmaf(lit, 0.2f, 0.3f));
-        acc2 = __fadd_rn(acc2, fmaf(lit, 0.1f, 0.3f));
+        add_shade(shadow_hit ? 0.0f : ndl);
         if (shadow_hit && L.record_hits && S.hits) S.hits[rec].flags = prim_flags | HRT_HIT_SHADOWED;
         shadow = false;
         next_sample();

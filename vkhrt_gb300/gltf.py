@@ -10,7 +10,12 @@ Every mesh primitive drawn by a node becomes one `Primitive`:
   n - 1 pairs (i, i + 1), as assimp's line faces do. An optional per-vertex scalar attribute
   `_RADIUS` (an application attribute; glTF has no standard hair radius) gives radii, otherwise
   the BLAS's constant radius applies.
-* TRIANGLES (mode 4, default) -> a triangle mesh with its NORMAL attribute when present.
+* TRIANGLES (mode 4, default) -> a triangle mesh with its NORMAL attribute when present, and its
+  material's albedo as the reference's loader reads it (model_loader.cpp:58-120): the base colour
+  factor, and the base colour texture sampled at its TEXCOORD_n. Texels are the image's 8-bit
+  values / 255, unconverted (the reference uploads them as R8G8B8A8_UNORM, model_loader.cpp:38).
+  PNG images (8-bit, not interlaced) are decoded here; other image formats leave the map out and
+  say so in `Primitive.note`.
 
 Each primitive carries the world matrix of its node (the product of the node path's matrices or
 TRS, column-vector convention, as glTF defines), which becomes the BLAS transform.
@@ -18,6 +23,7 @@ TRS, column-vector convention, as glTF defines), which becomes the BLAS transfor
 from __future__ import annotations
 
 import base64
+import zlib
 import json
 import os
 import struct
@@ -39,6 +45,10 @@ class Primitive:
     radius: np.ndarray | None = None   # (nv,) float32 (lines, from _RADIUS)
     normals: np.ndarray | None = None  # (nv, 3) float32 (triangles, from NORMAL)
     name: str = ""
+    texcoords: np.ndarray | None = None    # (nv, 2) float32 (triangles with a base colour texture)
+    albedo_factor: tuple = (1.0, 1.0, 1.0, 1.0)
+    albedo_map: np.ndarray | None = None   # (h, w, 4) float32, row 0 at v = 0
+    note: str = ""                         # why a texture was left out
 
     def blas_input(self, hair_type=None, **kw):
         """BLASInput for this primitive: lines as `hair_type` (BLASType.ePhantom, eLSS or eDOTS),
@@ -46,7 +56,8 @@ class Primitive:
         from . import BLASInput, BLASType
         if self.kind == "triangles":
             return BLASInput(type=BLASType.eMesh, vertices=self.vertices, tri_indices=self.indices,
-                             normals=self.normals, transform=self.transform, **kw)
+                             normals=self.normals, transform=self.transform, texcoords=self.texcoords,
+                             albedo_factor=self.albedo_factor, albedo_map=self.albedo_map, **kw)
         return BLASInput(type=BLASType(hair_type if hair_type is not None else BLASType.ePhantom),
                          vertices=self.vertices, radius=self.radius, line_indices=self.indices,
                          transform=self.transform, **kw)
@@ -134,10 +145,76 @@ def _node_matrix(node: dict) -> np.ndarray:
     return m
 
 
+def decode_png(data: bytes) -> np.ndarray:
+    """An 8-bit, non-interlaced PNG (grey, grey + alpha, RGB or RGBA) as (h, w, 4) float32 texels
+    = byte / 255, alpha 1 where the image has none. Unfilters the five PNG row filters (None, Sub,
+    Up, Average, Paeth) as the PNG specification defines them."""
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise GltfError("not a PNG image")
+    off, idat, hdr = 8, [], None
+    while off + 8 <= len(data):
+        n, kind = struct.unpack_from(">I4s", data, off)
+        body = data[off + 8:off + 8 + n]
+        if kind == b"IHDR":
+            hdr = struct.unpack(">IIBBBBB", body)
+        elif kind == b"IDAT":
+            idat.append(body)
+        elif kind == b"IEND":
+            break
+        off += 12 + n
+    if hdr is None:
+        raise GltfError("PNG without IHDR")
+    w, h, depth, ctype, _, _, interlace = hdr
+    channels = {0: 1, 2: 3, 4: 2, 6: 4}.get(ctype)
+    if depth != 8 or channels is None or interlace:
+        raise GltfError(f"PNG of bit depth {depth}, colour type {ctype}, interlace {interlace} is not supported")
+    raw = zlib.decompress(b"".join(idat))
+    stride = w * channels
+    if len(raw) != h * (stride + 1):
+        raise GltfError("PNG data size does not match its header")
+    img = np.zeros((h, stride), np.int32)
+    prev = np.zeros(stride, np.int32)
+    for y in range(h):
+        f = raw[y * (stride + 1)]
+        row = np.frombuffer(raw, np.uint8, stride, y * (stride + 1) + 1).astype(np.int32)
+        if f == 0:
+            cur = row
+        elif f == 1:  # Sub: a running sum per channel
+            cur = np.cumsum(row.reshape(w, channels), axis=0).reshape(-1) & 255
+        elif f == 2:
+            cur = (row + prev) & 255
+        elif f in (3, 4):  # these depend on the reconstructed byte to the left
+            cur = np.zeros(stride, np.int32)
+            for x in range(stride):
+                a = int(cur[x - channels]) if x >= channels else 0
+                b = int(prev[x])
+                c = int(prev[x - channels]) if x >= channels else 0
+                if f == 3:
+                    pred = (a + b) >> 1
+                else:
+                    pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                    pred = a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+                cur[x] = (int(row[x]) + pred) & 255
+        else:
+            raise GltfError(f"PNG row filter {f}")
+        img[y] = cur
+        prev = cur
+    px = img.reshape(h, w, channels).astype(np.float32) / np.float32(255.0)
+    out = np.ones((h, w, 4), np.float32)
+    if channels in (1, 2):
+        out[..., :3] = px[..., :1]
+        if channels == 2:
+            out[..., 3] = px[..., 1]
+    else:
+        out[..., :channels] = px
+    return out
+
+
 def load(path: str) -> list[Primitive]:
     """The primitives of the default scene (or of every root node), in node order."""
     doc, glb_bin = _read_container(path)
-    bufs = _buffers(doc, os.path.dirname(os.path.abspath(path)), glb_bin)
+    base_dir = os.path.dirname(os.path.abspath(path))
+    bufs = _buffers(doc, base_dir, glb_bin)
     nodes = doc.get("nodes", [])
     scenes = doc.get("scenes", [])
     if scenes:
@@ -158,13 +235,57 @@ def load(path: str) -> list[Primitive]:
         if "mesh" in node:
             mesh = doc["meshes"][node["mesh"]]
             for pi, prim in enumerate(mesh.get("primitives", [])):
-                out.extend(_primitive(doc, bufs, prim, world, f"{mesh.get('name', node.get('name', ''))}:{pi}"))
+                out.extend(_primitive(doc, bufs, prim, world, f"{mesh.get('name', node.get('name', ''))}:{pi}",
+                                      base_dir))
         for c in reversed(node.get("children", [])):
             stack.append((c, world))
     return out
 
 
-def _primitive(doc, bufs, prim, world, name) -> list[Primitive]:
+def _image(doc, bufs, base_dir, index) -> tuple[bytes, str]:
+    """An image's bytes and MIME type (from a file, a data URI or a buffer view)."""
+    im = doc["images"][index]
+    if "bufferView" in im:
+        view = doc["bufferViews"][im["bufferView"]]
+        start = view.get("byteOffset", 0)
+        return bufs[view["buffer"]][start:start + view["byteLength"]], im.get("mimeType", "")
+    uri = im.get("uri", "")
+    if uri.startswith("data:"):
+        head, body = uri.split(",", 1)
+        return base64.b64decode(body), head[5:].split(";")[0]
+    with open(os.path.join(base_dir, uri), "rb") as f:
+        data = f.read()
+    return data, "image/png" if uri.lower().endswith(".png") else ""
+
+
+def _material(doc, bufs, base_dir, prim, attrs, nverts):
+    """(albedo factor, texcoords, albedo map, note) of a triangle primitive's material."""
+    if "material" not in prim:
+        return (1.0, 1.0, 1.0, 1.0), None, None, ""
+    pbr = doc["materials"][prim["material"]].get("pbrMetallicRoughness", {})
+    factor = tuple(float(x) for x in pbr.get("baseColorFactor", [1.0, 1.0, 1.0, 1.0]))
+    tex = pbr.get("baseColorTexture")
+    if tex is None:
+        return factor, None, None, ""
+    key = f"TEXCOORD_{tex.get('texCoord', 0)}"
+    if key not in attrs:
+        return factor, None, None, f"base colour texture without {key}"
+    acc = doc["accessors"][attrs[key]]
+    tc = _accessor(doc, bufs, attrs[key]).astype(np.float32).reshape(-1, 2)
+    if acc.get("normalized"):  # unsigned byte / short texture coordinates
+        tc /= np.float32(np.iinfo(_COMPONENT[acc["componentType"]]).max)
+    if len(tc) != nverts:
+        raise GltfError(f"{key} has {len(tc)} entries for {nverts} vertices")
+    source = doc["textures"][tex["index"]].get("source")
+    if source is None:
+        return factor, None, None, "texture without an image source"
+    data, mime = _image(doc, bufs, base_dir, source)
+    if mime != "image/png" and data[:8] != b"\x89PNG\r\n\x1a\n":
+        return factor, None, None, f"image {source} ({mime or 'unknown type'}) is not a PNG: map left out"
+    return factor, np.ascontiguousarray(tc), decode_png(data), ""
+
+
+def _primitive(doc, bufs, prim, world, name, base_dir="") -> list[Primitive]:
     mode = prim.get("mode", TRIANGLES)
     attrs = prim.get("attributes", {})
     if "POSITION" not in attrs:
@@ -180,7 +301,9 @@ def _primitive(doc, bufs, prim, world, name) -> list[Primitive]:
     elif mode == TRIANGLES:
         nrm = (np.ascontiguousarray(_accessor(doc, bufs, attrs["NORMAL"]), np.float32).reshape(-1, 3)
                if "NORMAL" in attrs else None)
-        return [Primitive("triangles", v, idx[: len(idx) // 3 * 3].reshape(-1, 3), xf, normals=nrm, name=name)]
+        factor, tc, amap, note = _material(doc, bufs, base_dir, prim, attrs, len(v))
+        return [Primitive("triangles", v, idx[: len(idx) // 3 * 3].reshape(-1, 3), xf, normals=nrm, name=name,
+                          texcoords=tc, albedo_factor=factor, albedo_map=amap, note=note)]
     else:
         return []  # points, line loops, strips and fans of triangles are not hair or meshes here
     rad = (np.ascontiguousarray(_accessor(doc, bufs, attrs["_RADIUS"]), np.float32).reshape(-1)
