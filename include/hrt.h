@@ -43,7 +43,8 @@ typedef enum hrt_status {
     HRT_ERR_CUDA = 3,
     HRT_ERR_STACK_OVERFLOW = 4, /* traversal stack depth exceeded (device error word) */
     HRT_ERR_TIMEOUT = 5,        /* a bounded device loop hit its iteration cap */
-    HRT_ERR_UNSUPPORTED = 6
+    HRT_ERR_UNSUPPORTED = 6,
+    HRT_ERR_BOUNDS = 7          /* a device index check failed (builds with HRT_CHECKED only) */
 } hrt_status;
 
 typedef struct hrt_context hrt_context;

@@ -6,6 +6,9 @@ Translation units compile in parallel:
   csrc/trace_frames.cu  frame kernels, once each for FP32 nodes, 8-bit nodes and per-instance formats
   csrc/api.cu           C ABI (host code)
   csrc/workload.cpp     synthetic strands and camera matrices (host, -ffp-contract=off)
+
+build(checked=True) makes libhrt_checked.so instead: the same sources with -DHRT_CHECKED, whose
+kernels test every node, leaf-slot and stream index before loading and report HRT_ERR_BOUNDS.
 """
 from __future__ import annotations
 
@@ -19,6 +22,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhrt.so")
+BUILD_CHECKED = os.path.join(HERE, "_build_checked")
+LIB_CHECKED = os.path.join(HERE, "libhrt_checked.so")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -49,8 +54,8 @@ def _deps() -> list[str]:
     return out
 
 
-def _compile(nvcc: str, name: str, src: str, extra: list[str], verbose: bool) -> str:
-    obj = os.path.join(BUILD, name + ".o")
+def _compile(nvcc: str, name: str, src: str, extra: list[str], verbose: bool, build_dir: str = BUILD) -> str:
+    obj = os.path.join(build_dir, name + ".o")
     cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-I" + INCLUDE, "-I" + CSRC,
            "-Xcompiler", "-fPIC", *extra, "-c", src, "-o", obj]
     if verbose:
@@ -63,24 +68,27 @@ def _compile(nvcc: str, name: str, src: str, extra: list[str], verbose: bool) ->
     return obj
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile and link libhrt.so in-tree; a no-op when it is newer than its sources."""
-    if not force and os.path.exists(LIB):
-        t = os.path.getmtime(LIB)
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> str:
+    """Compile and link libhrt.so (or, checked, libhrt_checked.so) in-tree; a no-op when it is
+    newer than its sources."""
+    lib, build_dir = (LIB_CHECKED, BUILD_CHECKED) if checked else (LIB, BUILD)
+    if not force and os.path.exists(lib):
+        t = os.path.getmtime(lib)
         if all(os.path.getmtime(d) <= t for d in _deps()):
-            return LIB
-    os.makedirs(BUILD, exist_ok=True)
+            return lib
+    os.makedirs(build_dir, exist_ok=True)
     nvcc = _nvcc()
+    flag = ["-DHRT_CHECKED"] if checked else []
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        futs = [ex.submit(_compile, nvcc, name, os.path.join(CSRC, f), extra, verbose)
+        futs = [ex.submit(_compile, nvcc, name, os.path.join(CSRC, f), extra + flag, verbose, build_dir)
                 for name, (f, extra) in UNITS.items()]
         objs = [f.result() for f in futs]
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     r = subprocess.run([nvcc, *ARCH, "-shared", "-o", tmp, *objs], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

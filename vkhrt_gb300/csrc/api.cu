@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -184,6 +185,8 @@ bool is_identity(const float* m) {
 
 // The status a launch's device error word stands for.
 hrt_status error_status(hrt_context* ctx, uint32_t error) {
+    if (error & kErrBounds)
+        return fail(ctx, HRT_ERR_BOUNDS, "a device index check failed (a node, leaf slot or stream entry outside its array)");
     if (error & kErrStackOverflow)
         return fail(ctx, HRT_ERR_STACK_OVERFLOW, "a traversal overflowed its stack (max_depth entries, at most %d)",
                     kStackSize);
@@ -441,6 +444,7 @@ const char* hrt_status_string(hrt_status s) {
         case HRT_ERR_STACK_OVERFLOW: return "traversal stack overflow";
         case HRT_ERR_TIMEOUT: return "device loop iteration cap reached";
         case HRT_ERR_UNSUPPORTED: return "unsupported";
+        case HRT_ERR_BOUNDS: return "device index check failed";
     }
     return "unknown status";
 }
@@ -1309,6 +1313,13 @@ hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint3
         d.b.precision = uint32_t(b->precision);
         d.b.nprims = uint32_t(b->nprims);
         d.b.nnodes = uint32_t(b->out.nnodes);
+        d.b.nverts = uint32_t(b->out.nverts);
+#ifdef HRT_CHECKED
+        // test hook of the checked build: report fewer nodes than the BLAS holds, so traversal
+        // meets indices past the reported count (the loads there would still be inside the array)
+        if (const char* lim = getenv("HRT_CHECKED_NODE_LIMIT"))
+            d.b.nnodes = std::min<uint32_t>(d.b.nnodes, uint32_t(std::max(1L, strtol(lim, nullptr, 10))));
+#endif
         for (int k = 0; k < 3; ++k) { d.b.lo[k] = b->out.bounds[k]; d.b.hi[k] = b->out.bounds[3 + k]; }
         for (int k = 0; k < 4; ++k) d.b.albedo[k] = b->albedo[k];
         d.b.uv = b->uv;

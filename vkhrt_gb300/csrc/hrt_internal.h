@@ -17,6 +17,7 @@ constexpr uint32_t kMaxTraversalSteps = 1u << 16;  // per ray by default; exceed
 // Device error word bits (read back by the host after a launch).
 constexpr uint32_t kErrStackOverflow = 1u;
 constexpr uint32_t kErrTimeout = 2u;
+constexpr uint32_t kErrBounds = 4u;  // HRT_CHECKED builds: an index outside its array (the load skipped)
 
 // ---- BVH8 nodes -----------------------------------------------------------------------------
 // Both node formats describe the same tree (same children, same order):
@@ -76,6 +77,7 @@ struct DevBlas {
     const uint32_t* prim_ids; // slot -> reference id (segment index << ref_shift | half)
     const uint32_t* partner;  // slot -> the slot of the same segment's other reference (LSS, DOTS)
     uint32_t type, precision, nprims, nnodes, ref_shift;
+    uint32_t nverts;          // strand vertex stream entries (quantised Phantom)
     float lo[3], hi[3];
     // mesh material: albedo factor, and with both set the map sampled at the per-triangle
     // texture coordinates

@@ -858,6 +858,20 @@ __device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
     b = hi;
 }
 
+// HRT_CHECKED builds test each node index, leaf slot and strand-stream entry against its array
+// before the loads that use it, and stop the ray with kErrBounds instead of loading; other builds
+// compile the tests away.
+#ifdef HRT_CHECKED
+#define HRT_BAD_INDEX(cond) (cond)
+#else
+#define HRT_BAD_INDEX(cond) false
+#endif
+__device__ __forceinline__ bool bad_slot(const DevBlas& B, uint32_t slot) {
+    if (slot >= (B.nprims << B.ref_shift)) return true;
+    return B.type == HRT_BLAS_PHANTOM && B.precision == HRT_PRECISION_QUANTISED &&
+           uint64_t(__ldg(static_cast<const uint32_t*>(B.prims) + slot)) + 4u > B.nverts;
+}
+
 // Traverses one BLAS for the closest hit (explicit rays; the frame kernel has its own traversal).
 template <bool kQuant>
 __device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit& h, bool fp64_resolve,
@@ -875,10 +889,18 @@ __device__ bool traverse(const DevBlas& B, uint32_t inst, const RayState& R, Hit
         if (e.x & kLeafFlag) {
             uint32_t first = (e.x & ~kLeafFlag) >> 2, cnt = (e.x & 3u) + 1u;
             for (uint32_t j = 0; j < cnt; ++j) {
+                if (HRT_BAD_INDEX(bad_slot(B, first + j))) {
+                    err |= kErrBounds;
+                    return found;
+                }
                 ++st.prims;
                 if (leaf_test(B, first + j, inst, R, h, fp64_resolve, st)) found = true;
             }
             continue;
+        }
+        if (HRT_BAD_INDEX(e.x >= B.nnodes)) {
+            err |= kErrBounds;
+            break;
         }
         ++st.nodes;
         float tn[8];
@@ -930,7 +952,11 @@ __device__ bool trace_scene(const DevInstance* insts, const TlasNode* tlas, uint
             while (tsp > 0) {
                 uint32_t a, b;
                 if (!tlas_box_hit(tlas, tstack[--tsp], wo, winv, tmin, h.t, &a, &b)) continue;
-                if (a & kLeafFlag) { i = a & ~kLeafFlag; break; }
+                if (a & kLeafFlag) {
+                    i = a & ~kLeafFlag;
+                    if (HRT_BAD_INDEX(i >= ninst)) { err |= kErrBounds; i = 0xffffffffu; tsp = 0; }
+                    break;
+                }
                 if (tsp + 2 > kTlasStack) { err |= kErrStackOverflow; tsp = 0; break; }
                 tstack[tsp++] = b;
                 tstack[tsp++] = a;
@@ -1255,7 +1281,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
         while (tsp > 0) {
             uint32_t a, b;
             if (!tlas_box_hit(S.tlas, tstack[--tsp], wo, winv, cur_tmin, h.t, &a, &b)) continue;
-            if (a & kLeafFlag) return a & ~kLeafFlag;
+            if (a & kLeafFlag) {
+                if (HRT_BAD_INDEX((a & ~kLeafFlag) >= S.ninst)) {
+                    err |= kErrBounds;
+                    tsp = 0;
+                    break;
+                }
+                return a & ~kLeafFlag;
+            }
             if (tsp + 2 > kTlasStack) {  // deeper than a TLAS is built (bounded all the same)
                 err |= kErrStackOverflow;
                 tsp = 0;
@@ -1498,6 +1531,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             cur_bits &= ~(1u << i);
             const uint32_t slot = i ^ oct;
             const uint32_t child = cur_base + __popc((cur_bits >> 8) & ((1u << slot) - 1u));
+            if (HRT_BAD_INDEX(child >= L.scenes[si].inst[inst_cur].b.nnodes)) {
+                err |= kErrBounds;
+                sp = 0;
+                cur_bits = leaf_bits = 0;
+                continue;
+            }
             ++st.nodes;
             uint32_t base, imask;
             const uint32_t mask = test_node_of<kNodes>(nodes, qnodes, child, R, h.t, &base, &imask);
@@ -1539,6 +1578,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             for (uint32_t j = 0; j < cnt; ++j) {
                 uint32_t slot = first + j;
                 if (shadow && inst_cur == skip_inst && (slot == skip_slot || slot == skip_slot2)) continue;
+                if (HRT_BAD_INDEX(bad_slot(B, slot))) {
+                    err |= kErrBounds;
+                    sp = 0;
+                    cur_bits = leaf_bits = 0;
+                    break;
+                }
                 ++st.prims;
                 if (leaf_test<kType, kPass == 1>(B, slot, inst_cur, R, h, L.fp64_resolve != 0, st) && shadow) {
                     shadow_hit = true;
