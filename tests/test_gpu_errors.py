@@ -105,3 +105,29 @@ def test_bounds_beyond_the_stack_are_refused(ctx, orc):
     with pytest.raises(H.HrtError) as e:
         H.trace(ctx, tlas, H.scene_camera(16, 16), fr, H.trace_params(max_depth=65))
     assert e.value.status == INVALID
+
+
+def test_log_level_prints_builds_and_failures(tmp_path):
+    """HRT_LOG=2 prints one line per built BLAS and one per failure on stderr, prefixed [hrt]."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "import numpy as np, vkhrt_gb300 as H\n"
+            "ctx = H.Context(0)\n"
+            "v, r, off = H.generate_strands(H.StrandParams(seed=5, nstrands=40, nverts=8))\n"
+            "H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r,"
+            " strand_offsets=off), ctx)\n"
+            "try:\n"
+            "    H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.ePhantom, vertices=v, radius=r,"
+            " strand_offsets=off, width=9), ctx)\n"
+            "except H.HrtError as e:\n"
+            "    print('status', e.status)\n") % root
+    r = subprocess.run([sys.executable, "-c", code], env=dict(os.environ, HRT_LOG="2"), capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "status 1" in r.stdout
+    lines = [x for x in r.stderr.splitlines() if x.startswith("[hrt]")]
+    assert any("BLAS type 0 precision 0: 280 primitives" in x for x in lines), lines
+    assert any("error 1" in x and "width" in x for x in lines), lines

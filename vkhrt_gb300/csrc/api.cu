@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "hrt_internal.h"
 
 using namespace hrt;
@@ -139,17 +141,33 @@ struct hrt_batch {
 
 namespace {
 
+// Log level from the environment variable HRT_LOG: 0 (default) silent, 1 failures, 2 also each
+// build's summary; lines go to stderr with the prefix "[hrt]".
+int log_level() {
+    static const int level = [] {
+        const char* v = getenv("HRT_LOG");
+        return v ? int(strtol(v, nullptr, 10)) : 0;
+    }();
+    return level;
+}
+
 hrt_status fail(hrt_context* ctx, hrt_status s, const char* fmt, ...) {
-    if (ctx) {
-        char buf[512];
-        va_list ap;
-        va_start(ap, fmt);
-        vsnprintf(buf, sizeof(buf), fmt, ap);
-        va_end(ap);
-        ctx->last_error = buf;
-    }
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->last_error = buf;
+    if (log_level() >= 1) fprintf(stderr, "[hrt] error %d (%s): %s\n", int(s), hrt_status_string(s), buf);
     return s;
 }
+
+// An NVTX range over a public entry point, so that profilers show the library's calls on their
+// timelines (a no-op unless a profiler is attached).
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+};
 
 hrt_status cuda_fail(hrt_context* ctx, cudaError_t e, const char* what) {
     if (e == cudaErrorMemoryAllocation)
@@ -486,6 +504,14 @@ void hrt_blas_input_default(hrt_blas_input* in) {
     for (int k = 0; k < 4; ++k) in->transform[5 * k] = 1.0f;
 }
 
+// HRT_LOG >= 2: one line per built BLAS.
+static void log_build(const hrt_blas* b) {
+    if (log_level() < 2) return;
+    fprintf(stderr, "[hrt] BLAS type %d precision %d: %llu primitives, %llu nodes, %llu device bytes, %.3f ms\n",
+            b->type, b->precision, (unsigned long long)b->nprims, (unsigned long long)b->out.nnodes,
+            (unsigned long long)b->out.device_bytes, double(b->build_ms));
+}
+
 // A mesh's material on the device: the albedo factor, and with a map and texture coordinates the
 // per-triangle coordinates (gathered on the host through the kept triangle indices) and the map.
 static hrt_status upload_material(hrt_context* ctx, const hrt_blas_input* in, hrt_blas* b) {
@@ -627,11 +653,13 @@ static hrt_status build_mesh(hrt_context* ctx, const hrt_blas_input* in, cudaStr
         hrt_blas_destroy(b);
         return st;
     }
+    log_build(b);
     *out = b;
     return HRT_OK;
 }
 
 hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stream, hrt_blas** out) {
+    Range range("hrt_blas_build");
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!in || !out) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_blas_build: null input or output");
     *out = nullptr;
@@ -808,11 +836,13 @@ hrt_status hrt_blas_build(hrt_context* ctx, const hrt_blas_input* in, void* stre
     cudaEventDestroy(e1);
     if (vox) cudaFree(vox);
     cleanup();
+    log_build(b);
     *out = b;
     return HRT_OK;
 }
 
 hrt_status hrt_blas_refit(hrt_blas* b, const float* vertices, const float* per_vertex, int32_t memory, void* stream) {
+    Range range("hrt_blas_refit");
     if (!b) return HRT_ERR_INVALID_ARG;
     hrt_context* ctx = b->ctx;
     if (b->type == HRT_BLAS_VOXELS)
@@ -1288,6 +1318,7 @@ uint32_t build_tlas_node(std::vector<TlasItem>& items, size_t l, size_t r, std::
 }  // namespace
 
 hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint32_t n, void* stream, hrt_tlas** out) {
+    Range range("hrt_tlas_build");
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!out || (n && !blases)) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_tlas_build: null argument");
     *out = nullptr;
@@ -1500,6 +1531,7 @@ hrt_status hrt_frame_get_stats(const hrt_frame* cf, hrt_frame_stats* out) {
 
 hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* cam, const hrt_trace_params* p,
                      hrt_frame* f, void* stream) {
+    Range range("hrt_trace");
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!tlas || !cam || !p || !f) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace: null argument");
     if (hrt_status ps = check_params(ctx, p, "hrt_trace")) return ps;
@@ -1526,6 +1558,7 @@ hrt_status hrt_trace(hrt_context* ctx, const hrt_tlas* tlas, const hrt_camera* c
 
 hrt_status hrt_trace_rays(hrt_context* ctx, const hrt_tlas* tlas, const float* rays, uint64_t n, const hrt_trace_params* p,
                           hrt_hit* hits, int32_t memory, void* stream) {
+    Range range("hrt_trace_rays");
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!tlas || !p || (n && (!rays || !hits))) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_trace_rays: null argument");
     if (memory != HRT_MEMORY_HOST && memory != HRT_MEMORY_DEVICE)
@@ -1592,6 +1625,7 @@ hrt_status hrt_trace_rays_noalloc(hrt_context* ctx, const hrt_tlas* tlas, const 
 
 hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* p,
                             void* stream, hrt_batch** out) {
+    Range range("hrt_batch_create");
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!scenes || !n || !p || !out) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_batch_create: null or empty argument");
     *out = nullptr;
@@ -1638,6 +1672,7 @@ hrt_status hrt_batch_create(hrt_context* ctx, const hrt_scene_desc* scenes, uint
 }
 
 hrt_status hrt_batch_launch(hrt_batch* b, void* stream) {
+    Range range("hrt_batch_launch");
     if (!b) return HRT_ERR_INVALID_ARG;
     hrt_context* ctx = b->ctx;
     DeviceSet ds(ctx->device);
@@ -1708,6 +1743,7 @@ hrt_status hrt_batch_download(hrt_batch* b, float* const* rgba, void* stream, in
 
 hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* base,
                         uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms) {
+    Range range("hrt_autotune");
     if (!ctx) return HRT_ERR_INVALID_ARG;
     if (!scenes || !n || !base || !best) return fail(ctx, HRT_ERR_INVALID_ARG, "hrt_autotune: null or empty argument");
     if (hrt_status ps = check_params(ctx, base, "hrt_autotune")) return ps;
