@@ -54,7 +54,7 @@ def test_textured_mesh_frame_vs_oracle(ctx, orc, precision, shading, hair):
     fr, rgba, hits, o = render_both(ctx, tlas, osc, 200, 150, spp=1, shading=shading)
     st, px_ok, diff = frame_checks(rgba, hits, o, 1)
     mesh_px = (hits["inst"] == 0) & (hits["t"] >= 0)
-    assert mesh_px.sum() > 3000 and (not hair or (hits["inst"] == 1).sum() > 300)
+    assert mesh_px.sum() > 1500 and (not hair or (hits["inst"] == 1).sum() > 300)
     assert st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
     assert px_ok.mean() >= 0.999 and diff[px_ok].max() <= RGB_ABS
     # the map shows: without it the mesh pixels' colours move far beyond the bar
