@@ -995,6 +995,23 @@ __device__ bool trace_scene(const DevInstance* insts, const TlasNode* tlas, uint
     return found;
 }
 
+// Barycentric weights (of v1 and v2) of the hit point o + t d on a triangle, for shading. The
+// watertight test's weights come from coordinates relative to the ray origin, so for a small
+// triangle far from the camera they carry errors of about 2^-24 (distance / size)^2 (4e-4 at a
+// distance of 3 for a 0.05 triangle); here every vector is relative to v0, so the rounding is at
+// the triangle's scale. Falls back to the given weights for a degenerate triangle.
+__device__ __noinline__ void tri_weights(V3<float> v0, V3<float> v1, V3<float> v2, V3<float> o, V3<float> d, float t,
+                                            float* u, float* v) {
+    const V3<float> e1 = v1 - v0, e2 = v2 - v0;
+    const V3<float> w = mk(fmaf(t, d.x, o.x - v0.x), fmaf(t, d.y, o.y - v0.y), fmaf(t, d.z, o.z - v0.z));
+    const float d11 = dot_rn(e1, e1), d12 = dot_rn(e1, e2), d22 = dot_rn(e2, e2);
+    const float d1 = dot_rn(w, e1), d2 = dot_rn(w, e2);
+    const float den = fmaf(d11, d22, -__fmul_rn(d12, d12));
+    if (!(den > 0.0f)) return;
+    *u = __fdiv_rn(fmaf(d22, d1, -__fmul_rn(d12, d2)), den);
+    *v = __fdiv_rn(fmaf(d11, d2, -__fmul_rn(d12, d1)), den);
+}
+
 // Object-space normal of the final hit (closest-hit stage).
 __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo, V3<float> wd) {
     const DevBlas& B = I.b;
@@ -1049,7 +1066,9 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         const PrimTri* pr = static_cast<const PrimTri*>(B.prims) + h.slot;
         const float4 a = __ldg(&pr->a), b = __ldg(&pr->b), c = __ldg(&pr->c), d4 = __ldg(&pr->d), e4 = __ldg(&pr->e);
         if (__float_as_uint(e4.w)) {  // n0 = (b.w, c.w, d.x), n1 = d.yzw, n2 = e.xyz
-            const float u = h.u, v = h.ts, w = __fsub_rn(__fsub_rn(1.0f, u), v);
+            float u = h.u, v = h.ts;
+            tri_weights(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), mk(c.x, c.y, c.z), o, d, h.t, &u, &v);
+            const float w = __fsub_rn(__fsub_rn(1.0f, u), v);
             n = normalize_rn(mk(fmaf(v, e4.x, fmaf(u, d4.y, __fmul_rn(w, b.w))),
                                 fmaf(v, e4.y, fmaf(u, d4.z, __fmul_rn(w, c.w))),
                                 fmaf(v, e4.z, fmaf(u, d4.w, __fmul_rn(w, d4.x)))));
@@ -1105,14 +1124,25 @@ __device__ V3<float> env_color(const float4* env, uint32_t w, uint32_t h, V3<flo
 }
 
 // triangle_closest_hit.rchit:71-81: the mesh material's albedo at a hit, albedo_factor x the
-// map at the interpolated texture coordinate (rchit:39, barycentrics (1 - u - v, u, v) with u, v
-// in h.u, h.ts). Bilinear with repeat addressing, texel centres at (i + 0.5) / size, row 0 at
-// v = 0; the coordinate is wrapped into [0, 1) first, and every texel index stays in the map.
-__device__ V3<float> mesh_albedo(const DevBlas& B, const Hit& h) {
+// map at the interpolated texture coordinate (rchit:39, barycentrics (1 - u - v, u, v) of the hit
+// point, as for the normal). Bilinear with repeat addressing, texel centres at (i + 0.5) / size,
+// row 0 at v = 0; the coordinate is wrapped into [0, 1) first, and every texel index stays in the
+// map. wo, wd: the world ray.
+__device__ V3<float> mesh_albedo(const DevInstance& I, const Hit& h, V3<float> wo, V3<float> wd) {
+    const DevBlas& B = I.b;
     V3<float> a = mk(B.albedo[0], B.albedo[1], B.albedo[2]);
     if (!B.albedo_map || !B.uv) return a;
+    V3<float> o = wo, d = wd;
+    if (!I.identity) {
+        o = xform_point(I.w2o, wo);
+        d = xform_dir(I.w2o, wd);
+    }
+    const PrimTri* pr = static_cast<const PrimTri*>(B.prims) + h.slot;
+    const float4 p0 = __ldg(&pr->a), p1 = __ldg(&pr->b), p2 = __ldg(&pr->c);
+    float u = h.u, v = h.ts;
+    tri_weights(mk(p0.x, p0.y, p0.z), mk(p1.x, p1.y, p1.z), mk(p2.x, p2.y, p2.z), o, d, h.t, &u, &v);
     const float* q = B.uv + 6 * size_t(h.id);
-    const float u = h.u, v = h.ts, w = __fsub_rn(__fsub_rn(1.0f, u), v);
+    const float w = __fsub_rn(__fsub_rn(1.0f, u), v);
     float s = fmaf(v, __ldg(q + 4), fmaf(u, __ldg(q + 2), __fmul_rn(w, __ldg(q))));
     float t = fmaf(v, __ldg(q + 5), fmaf(u, __ldg(q + 3), __fmul_rn(w, __ldg(q + 1))));
     s = __fsub_rn(s, floorf(s));
@@ -1398,7 +1428,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
             ndl = fabsf(n.y);  // shading.glsl: |dot(n, (0,-1,0))|
             if (kType == kMixed) {  // meshes run in the mixed-type kernel only
                 const DevBlas& HB = S.inst[h.inst].b;
-                const V3<float> a = HB.type == HRT_BLAS_MESH ? mesh_albedo(HB, h) : mk(1.0f, 1.0f, 1.0f);
+                const V3<float> a = HB.type == HRT_BLAS_MESH ? mesh_albedo(S.inst[h.inst], h, wo, wd) : mk(1.0f, 1.0f, 1.0f);
                 s_alb[0][tid] = a.x;
                 s_alb[1][tid] = a.y;
                 s_alb[2][tid] = a.z;
