@@ -554,10 +554,11 @@ def test_serialized_blas_traces_identically(ctx, gtype, precision):
     bad[:4] = b"XXXX"
     with pytest.raises(H.HrtError):
         H.BottomLevelAccelerationStructure.load(bytes(bad), ctx)
-    # a node whose children lie past the tree: the header is 224 bytes, then five u32 tables
+    # a node whose children lie past the tree: the header is 256 bytes (its five table counts at
+    # byte 184), then the five u32 tables
     import struct
     ntab = sum(struct.unpack_from("<5Q", data, 184))
-    node0 = 224 + 4 * ntab
+    node0 = 256 + 4 * ntab
     bad = bytearray(data)
     struct.pack_into("<I", bad, node0 + (16 if precision == 1 else 192), 0x7FFFFFF0)
     with pytest.raises(H.HrtError) as e:
