@@ -77,7 +77,6 @@ struct DevBlas {
     const uint32_t* prim_ids; // slot -> reference id (segment index << ref_shift | half)
     const uint32_t* partner;  // slot -> the slot of the same segment's other reference (LSS, DOTS)
     uint32_t type, precision, nprims, nnodes, ref_shift;
-    uint32_t nverts;          // strand vertex stream entries (quantised Phantom)
     float lo[3], hi[3];
     // mesh material: albedo factor, and with both set the map sampled at the per-triangle
     // texture coordinates
@@ -85,6 +84,7 @@ struct DevBlas {
     const float* uv;          // float[ntris][6], triangle order, or null
     const float4* albedo_map; // map_w x map_h RGBA texels, row 0 at v = 0, or null
     uint32_t map_w, map_h;
+    uint32_t nverts;          // strand vertex stream entries (quantised Phantom)
 };
 
 struct DevInstance {

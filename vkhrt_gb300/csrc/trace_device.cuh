@@ -1012,9 +1012,12 @@ __device__ __noinline__ void tri_weights(V3<float> v0, V3<float> v1, V3<float> v
     *v = __fdiv_rn(fmaf(d11, d2, -__fmul_rn(d12, d1)), den);
 }
 
-// Object-space normal of the final hit (closest-hit stage).
+// Object-space normal of the final hit (closest-hit stage). kType: the launch's primitive type
+// (only that type's branch is compiled), or kMixed to branch on the BLAS.
+template <int kType>
 __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo, V3<float> wd) {
     const DevBlas& B = I.b;
+    const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
     V3<float> o = wo, d = wd;
     if (!I.identity) {
         const float* m = I.w2o;
@@ -1024,7 +1027,7 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
     // Normals are differences of points a hair radius apart; they are formed from the
     // full-precision vectors relative to the primitive's reference point o' = o + ts d.
     V3<float> n;
-    if (B.type == HRT_BLAS_PHANTOM) {
+    if (type == HRT_BLAS_PHANTOM) {
         // hair_intersection.rint:74-76: normalize(hit - curve(t))
         V3<float> P[4];
         float r0, r1;
@@ -1043,7 +1046,7 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         c.y = fmaf(b3, W[3].y, fmaf(b2, W[2].y, fmaf(b1, W[1].y, __fmul_rn(b0, W[0].y))));
         c.z = fmaf(b3, W[3].z, fmaf(b2, W[2].z, fmaf(b1, W[1].z, __fmul_rn(b0, W[0].z))));
         n = normalize_rn(mk(fmaf(h.sl, d.x, -c.x), fmaf(h.sl, d.y, -c.y), fmaf(h.sl, d.z, -c.z)));
-    } else if (B.type == HRT_BLAS_LSS) {
+    } else if (type == HRT_BLAS_LSS) {
         // triangle_closest_hit.rchit:43-58: hit - mix(p0, p1, u)
         const PrimLss* pr = static_cast<const PrimLss*>(B.prims) + h.slot;
         float4 a = __ldg(&pr->a), b = __ldg(&pr->b);
@@ -1053,14 +1056,14 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         const V3<float> ax = mk(__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z));
         n = normalize_rn(mk(fmaf(-h.u, ax.x, fmaf(h.sl, d.x, -w0.x)), fmaf(-h.u, ax.y, fmaf(h.sl, d.y, -w0.y)),
                             fmaf(-h.u, ax.z, fmaf(h.sl, d.z, -w0.z))));
-    } else if (B.type == HRT_BLAS_VOXELS) {
+    } else if (type == HRT_BLAS_VOXELS) {
         // the entry face's normal, facing the ray; h.u = +-(axis + 1), negative when the ray
         // runs along +axis
         const float u = h.u;
         const int ax = int(fabsf(u)) - 1;
         const float sg = u < 0.0f ? -1.0f : 1.0f;
         n = mk(ax == 0 ? sg : 0.0f, ax == 1 ? sg : 0.0f, ax == 2 ? sg : 0.0f);
-    } else if (B.type == HRT_BLAS_MESH) {
+    } else if (type == HRT_BLAS_MESH) {
         // triangle_closest_hit.rchit:19-41: vertex normals interpolated with the hit's
         // barycentrics (1 - u - v, u, v); without normals, the face normal
         const PrimTri* pr = static_cast<const PrimTri*>(B.prims) + h.slot;
@@ -1424,7 +1427,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 next_sample();
                 return;
             }
-            V3<float> n = hit_normal(S.inst[h.inst], h, wo, wd);
+            V3<float> n = hit_normal<kType>(S.inst[h.inst], h, wo, wd);
             ndl = fabsf(n.y);  // shading.glsl: |dot(n, (0,-1,0))|
             if (kType == kMixed) {  // meshes run in the mixed-type kernel only
                 const DevBlas& HB = S.inst[h.inst].b;
