@@ -638,8 +638,8 @@ def run_batched(args, dist):
 # capture of that launch (profiles/frame_kernel_c5_phantom_group.md): DRAM bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum), L2 bytes (lts__t_sectors.sum x 32) and warp
 # instructions (smsp__inst_executed.sum), each over the launch's 4,649,742 rays.
-NCU_PER_RAY = {"dram_bytes": 36.75e6 / 4649742, "l2_bytes": 96901879 * 32 / 4649742,
-               "warp_inst": 6718034768 / 4649742, "source": "profiles/frame_kernel_c5_phantom_group.md"}
+NCU_PER_RAY = {"dram_bytes": 36.94e6 / 4649742, "l2_bytes": 97210795 * 32 / 4649742,
+               "warp_inst": 6712892714 / 4649742, "source": "profiles/frame_kernel_c5_phantom_group.md"}
 
 
 def measured_bounds(rays: int, ms: float, clk: dict) -> dict:
