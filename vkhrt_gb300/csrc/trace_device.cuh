@@ -497,9 +497,11 @@ struct Stats { uint32_t nodes, prims, r64, h64, need64; };
 // operations of the curve kernel (GenerateCurves, tension 1: cp1 = p1 + (p2 - p0) / 6,
 // cp2 = p2 - (p3 - p1) / 6, each operation rounded separately), so they equal the FP32 curves bit
 // for bit, and its id is read from the slot map when a hit needs it (phantom_id).
+// kPrec: the record format when the launch fixes it (0 FP32, 1 quantised), -1 to read it from B.
+template <int kPrec = -1>
 __device__ __forceinline__ void load_phantom(const DevBlas& B, uint32_t slot, V3<float>* P, float* r0, float* r1,
                                              uint32_t* id) {
-    if (B.precision == HRT_PRECISION_QUANTISED) {
+    if (kPrec < 0 ? B.precision == HRT_PRECISION_QUANTISED : kPrec == 1) {
         const uint32_t e = __ldg(static_cast<const uint32_t*>(B.prims) + slot);
         const float4 v0 = __ldg(B.verts + e), v1 = __ldg(B.verts + e + 1), v2 = __ldg(B.verts + e + 2),
                      v3 = __ldg(B.verts + e + 3);
@@ -526,16 +528,18 @@ __device__ __forceinline__ void load_phantom(const DevBlas& B, uint32_t slot, V3
     }
 }
 // The reported id of the Phantom segment in `slot` (id_rec: what load_phantom returned).
+template <int kPrec = -1>
 __device__ __forceinline__ uint32_t phantom_id(const DevBlas& B, uint32_t slot, uint32_t id_rec) {
-    return B.precision == HRT_PRECISION_QUANTISED ? __ldg(&B.prim_ids[slot]) : id_rec;
+    return (kPrec < 0 ? B.precision == HRT_PRECISION_QUANTISED : kPrec == 1) ? __ldg(&B.prim_ids[slot]) : id_rec;
 }
 
 // Tests one leaf slot; returns true if it produced an accepted hit. kType is the primitive
 // type when every instance of the launch has the same one, kMixed to branch on the BLAS.
 // kFlag64: a non-converged Phantom candidate only sets st.need64 (the FP64 re-solve runs in a
-// later pass); otherwise it is re-solved here.
+// later pass); otherwise it is re-solved here. kPrec: the Phantom record format when the launch
+// fixes it (0 FP32, 1 quantised), -1 to read it from the BLAS.
 constexpr int kMixed = 3;
-template <int kType = kMixed, bool kFlag64 = false>
+template <int kType = kMixed, bool kFlag64 = false, int kPrec = -1>
 __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint32_t inst, const RayState& R, Hit& h,
                                           bool fp64_resolve, Stats& st) {
     const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
@@ -543,10 +547,10 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
         V3<float> P[4];
         float r0, r1;
         uint32_t id;
-        load_phantom(B, slot, P, &r0, &r1, &id);
+        load_phantom<kPrec>(B, slot, P, &r0, &r1, &id);
         PrhiOut<float> r = prhi(R.F, R.o, R.d, P, r0, r1);
         if (r.status == kHit) {
-            if (r.s >= R.tmin && r.s <= h.t && beats(r.s, inst, id = phantom_id(B, slot, id), h)) {
+            if (r.s >= R.tmin && r.s <= h.t && beats(r.s, inst, id = phantom_id<kPrec>(B, slot, id), h)) {
                 h = Hit{r.s, id, inst, slot, r.tc, r.ts, r.sl, 0u};
                 return true;
             }
@@ -562,7 +566,7 @@ __device__ __forceinline__ bool leaf_test(const DevBlas& B, uint32_t slot, uint3
             if (s64 > 0.0) {
                 ++st.h64;
                 float s = float(s64);
-                if (s >= R.tmin && s <= h.t && beats(s, inst, id = phantom_id(B, slot, id), h)) {
+                if (s >= R.tmin && s <= h.t && beats(s, inst, id = phantom_id<kPrec>(B, slot, id), h)) {
                     h = Hit{s, id, inst, slot, float(tc64), float(ts64), float(s64 - double(float(ts64))), HRT_HIT_FP64};
                     return true;
                 }
@@ -1013,8 +1017,8 @@ __device__ __noinline__ void tri_weights(V3<float> v0, V3<float> v1, V3<float> v
 }
 
 // Object-space normal of the final hit (closest-hit stage). kType: the launch's primitive type
-// (only that type's branch is compiled), or kMixed to branch on the BLAS.
-template <int kType>
+// (only that type's branch is compiled), or kMixed to branch on the BLAS; kPrec as for leaf_test.
+template <int kType, int kPrec = -1>
 __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo, V3<float> wd) {
     const DevBlas& B = I.b;
     const uint32_t type = kType == kMixed ? B.type : uint32_t(kType);
@@ -1032,7 +1036,7 @@ __device__ V3<float> hit_normal(const DevInstance& I, const Hit& h, V3<float> wo
         V3<float> P[4];
         float r0, r1;
         uint32_t id;
-        load_phantom(B, h.slot, P, &r0, &r1, &id);
+        load_phantom<kPrec>(B, h.slot, P, &r0, &r1, &id);
         float ts = h.ts;
         V3<float> W[4];
         for (int k = 0; k < 4; ++k)
@@ -1258,6 +1262,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     // Multi-instance scenes (a TLAS) run in the kNodesPerInstance build only, so the builds for
     // one node format keep the lean single-instance loop.
     constexpr bool kTlas = kNodes == kNodesPerInstance;
+    constexpr int kPrec = kNodes == kNodesF ? 0 : (kNodes == kNodesQ ? 1 : -1);  // Phantom record format
     bool qnodes = false;                         // the current instance's format (kNodesPerInstance)
     uint32_t tstack[kTlas ? kTlasStack : 1];     // TLAS walk (local memory)
     int tsp = 0;
@@ -1427,7 +1432,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                 next_sample();
                 return;
             }
-            V3<float> n = hit_normal<kType>(S.inst[h.inst], h, wo, wd);
+            V3<float> n = hit_normal<kType, kPrec>(S.inst[h.inst], h, wo, wd);
             ndl = fabsf(n.y);  // shading.glsl: |dot(n, (0,-1,0))|
             if (kType == kMixed) {  // meshes run in the mixed-type kernel only
                 const DevBlas& HB = S.inst[h.inst].b;
@@ -1618,7 +1623,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
                     break;
                 }
                 ++st.prims;
-                if (leaf_test<kType, kPass == 1>(B, slot, inst_cur, R, h, L.fp64_resolve != 0, st) && shadow) {
+                if (leaf_test<kType, kPass == 1, kPrec>(B, slot, inst_cur, R, h, L.fp64_resolve != 0, st) && shadow) {
                     shadow_hit = true;
                     sp = 0;
                     cur_bits = leaf_bits = 0;
