@@ -47,6 +47,9 @@ L2_BYTES = 129 * 1024 * 1024
 PRECISION_DESC = ("quantised (8-bit BVH8 boxes; Phantom segments as 4-byte indices into the strand vertex stream, "
                   "control points rebuilt from the FP32 vertices in the leaf)")
 DTYPE_DESC = "fp32 (8-bit node boxes)"
+BATCH_PRECISION_DESC = ("node format chosen by the autotuner: FP32 BVH8 boxes and records, or 8-bit boxes with "
+                        "Phantom segments as 4-byte indices into the strand vertex stream, whichever it times faster "
+                        "on the workload (the other is reported beside it)")
 ORACLE_DESC = "FP64 CPU restatement on the original FP32 strands"
 DATA_DESC = "synthetic: seeded strands (the reference's glTF hair assets are not available)"
 BATCH_CONFIG = "c5_batched"
@@ -343,7 +346,7 @@ def batch_config_block(models):
     return {"workload": f"{BATCH_CONFIG}: {len(models)} hair models (strands log-uniform in [2000, 200000], "
                         f"{{16,32,64,128}} vertices, Phantom/LSS/DOTS in turn), {nseg} segments, own cameras, "
                         f"256x256..1920x1080 at 1-4 spp ({px} primary samples), Shade + 1 shadow ray",
-            "segments": nseg, "scenes": len(models), "primary_samples": px, "precision": PRECISION_DESC,
+            "segments": nseg, "scenes": len(models), "primary_samples": px, "precision": BATCH_PRECISION_DESC,
             "l2": "inputs larger than L2 (BVHs + primitives resident, no flush)", "parallelism": "replicas"}
 
 
@@ -422,10 +425,11 @@ def kernels_per_replay(models, params) -> int:
 
 
 def run_batched(args, dist):
-    """All scenes in one CUDA-graph replay of the persistent kernels (autotuned) against 16
-    sequential plain FP32 launches, 16 sequential quantised launches, and the batch on FP32
-    BLASes; then the timed graph's output against the FP64 oracle, the CPU baseline and the
-    single configurations."""
+    """All scenes in one CUDA-graph replay of the persistent kernels, autotuned on FP32 and on
+    quantised BLASes; the node format whose tuned batch the autotuner timed faster is the line's
+    value, the other format's batch is reported beside it, with 16 sequential plain FP32 launches
+    and 16 sequential launches of the chosen format. Then the timed graph's output against the
+    FP64 oracle, the CPU baseline and the single configurations."""
     import torch
     import vkhrt_gb300 as H
     dev = dist.local
@@ -451,26 +455,37 @@ def run_batched(args, dist):
     t0 = time.perf_counter()
     q = build(H.Precision.QUANTISED, not args.no_cpu)
     build_wall = time.perf_counter() - t0
-    f = build(H.Precision.FP32, False)
+    f = build(H.Precision.FP32, not args.no_cpu)
     base = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1})
-    # ---- per-scene work counts (sequential, counted): rays and algorithmic bytes ----
+    # ---- per-scene work counts (sequential, counted): rays and algorithmic bytes per format ----
     rays_per_step = 0
     per_scene = []
-    for (b, t, cam, fr), m in zip(q, mlist):
+    for (b, t, cam, fr), (bf, tf, _, frf), m in zip(q, f, mlist):
         H.trace(ctx, t, cam, fr, H.trace_params(jitter=1, seed=17, shading=2, count_stats=1))
         st = fr.stats()
-        info = b.info
+        H.trace(ctx, tf, cam, frf, H.trace_params(jitter=1, seed=17, shading=2, count_stats=1))
+        stf = frf.stats()
         rays = st["primary_rays"] + st["shadow_rays"]
         rays_per_step += rays
-        alg = st["nodes_visited"] * info["node_bytes"] + st["prims_tested"] * prim_test_bytes(info, int(m["type"]), 1) \
-            + m["width"] * m["height"] * 16
+        alg = {}
+        for key, s_, bl, prec in (("quantised", st, b, 1), ("fp32", stf, bf, 0)):
+            alg[key] = s_["nodes_visited"] * bl.info["node_bytes"] + \
+                s_["prims_tested"] * prim_test_bytes(bl.info, int(m["type"]), prec) + m["width"] * m["height"] * 16
         per_scene.append({"type": m["type"].name[1:], "segments": m["nstrands"] * (m["nverts"] - 1),
                           "image": f"{m['width']}x{m['height']}", "spp": m["spp"], "rays": int(rays),
-                          "alg_bytes": int(alg), "fp64_resolves": int(st["fp64_resolves"])})
-    # ---- autotune the batch (untimed) ----
+                          "alg_bytes": {k: int(v) for k, v in alg.items()}, "fp64_resolves": int(st["fp64_resolves"])})
+    # ---- autotune the batch in both node formats (untimed); the faster tuned batch is the claim ----
     scenes_q = [(t, cam, fr) for (_, t, cam, fr) in q]
-    tuned, tune_ms = H.autotune(ctx, scenes_q, base, reps=2, cache=args.tune_cache, key=f"{BATCH_CONFIG}/quantised")
-    batch = H.Batch(ctx, scenes_q, tuned)
+    scenes_f = [(t, cam, fr) for (_, t, cam, fr) in f]
+    tuned_q, tune_ms_q = H.autotune(ctx, scenes_q, base, reps=2, cache=args.tune_cache, key=f"{BATCH_CONFIG}/quantised")
+    tuned_f, tune_ms_f = H.autotune(ctx, scenes_f, base, reps=2, cache=args.tune_cache, key=f"{BATCH_CONFIG}/fp32")
+    fmt = "fp32" if 0.0 < tune_ms_f < tune_ms_q else "quantised"
+    if args.precision:  # a fixed format instead of the autotuner's choice
+        fmt = args.precision
+    other = "quantised" if fmt == "fp32" else "fp32"
+    main, tuned, tune_ms = (f, tuned_f, tune_ms_f) if fmt == "fp32" else (q, tuned_q, tune_ms_q)
+    scenes_main = scenes_f if fmt == "fp32" else scenes_q
+    batch = H.Batch(ctx, scenes_main, tuned)
     cams_all = [cam for (_, _, cam, _) in q]
 
     def paced(b, nsteps, cams):
@@ -530,20 +545,21 @@ def run_batched(args, dist):
 
     plain_params = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1})
     ms_f32, lat_f32 = sequential(f, plain_params)
-    ms_q, lat_q = sequential(q, tuned)
-    # the batching pattern on FP32 BLASes too, so that precision and batching can be told apart
-    scenes_f = [(t, cam, fr) for (_, t, cam, fr) in f]
-    tuned_f, _ = H.autotune(ctx, scenes_f, base, reps=2, cache=args.tune_cache, key=f"{BATCH_CONFIG}/fp32")
-    batch_f = H.Batch(ctx, scenes_f, tuned_f)
-    paced(batch_f, args.warmup, cams_all)
-    ms_bf = timed(batch_f, args.steps, cams_all)
+    ms_seq, lat_seq = sequential(main, tuned)
+    # the batching pattern in the other node format too, so that precision and batching can be
+    # told apart
+    scenes_o = scenes_q if fmt == "fp32" else scenes_f
+    tuned_o = tuned_q if fmt == "fp32" else tuned_f
+    batch_o = H.Batch(ctx, scenes_o, tuned_o)
+    paced(batch_o, args.warmup, cams_all)
+    ms_bo = timed(batch_o, args.steps, cams_all)
     mem_q = sum(int(b.info["device_bytes"]) for (b, *_r) in q)
     mem_f = sum(int(b.info["device_bytes"]) for (b, *_r) in f)
-    del batch_f, scenes_f, f
-    # ---- the dominant kernel alone, for the roofline: the quantised Phantom scenes as one batch
-    # (the Phantom group's frame launch and its FP64 pass) ----
+    del batch_o, scenes_o
+    # ---- the dominant kernel alone, for the roofline: the Phantom scenes of the chosen format as
+    # one batch (the Phantom group's frame launch and its FP64 pass) ----
     ph = [i for i, m in enumerate(mlist) if int(m["type"]) == 0]
-    batch_ph = H.Batch(ctx, [scenes_q[i] for i in ph], tuned)
+    batch_ph = H.Batch(ctx, [scenes_main[i] for i in ph], tuned)
     cams_ph = [cams_all[i] for i in ph]
     paced(batch_ph, args.warmup, cams_ph)
     ms_ph = timed(batch_ph, args.steps, cams_ph)
@@ -552,24 +568,25 @@ def run_batched(args, dist):
         dist.close()
         return
     peak, peak_kind = load_peaks()
-    ph_bytes = sum(per_scene[i]["alg_bytes"] for i in ph)
+    ph_bytes = sum(per_scene[i]["alg_bytes"][fmt] for i in ph)
     ph_rays = sum(per_scene[i]["rays"] for i in ph)
     achieved = ph_bytes / (ms_ph * 1e-3) / 1e9
+    kname = "FP32 nodes" if fmt == "fp32" else "8-bit nodes"
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
-                "kernel": "frame_kernel<8-bit nodes, Phantom>: the Phantom group of the batch, timed alone",
+                "kernel": f"frame_kernel<{kname}, Phantom>: the Phantom group of the batch, timed alone",
                 "bytes_per_launch": int(ph_bytes), "launch_ms": round(ms_ph, 3), "rays_per_launch": int(ph_rays)}
-    roofline.update(measured_bounds(ph_rays, ms_ph, clk))
-    for d, a, b2 in zip(per_scene, lat_f32, lat_q):
+    roofline.update(measured_bounds(ph_rays, ms_ph, clk, fmt))
+    for d, a, b2 in zip(per_scene, lat_f32, lat_seq):
         d["plain_fp32_ms"] = round(float(a), 3)
-        d["quantised_ms"] = round(float(b2), 3)
+        d[f"{fmt}_ms"] = round(float(b2), 3)
     # ---- e2e: through the C ABI, each step's cameras in and every framebuffer out to pinned host
     # memory; two frame sets on two streams, so that step k's read-back overlaps step k+1's render
     # (the renders themselves stay in order: each waits for the previous one) ----
     tparams = H.trace_params(jitter=1, seed=17, shading=2, **{"async": 1},
                              **{k: getattr(tuned, k) for k in H.TUNED_FIELDS})
-    fsets = [[fr for (_, _, _, fr) in q], [H.Frame(ctx, m["width"], m["height"], m["spp"]) for m in mlist]]
-    e2e_batches = [H.Batch(ctx, [(t, cam, fr) for (_, t, cam, _), fr in zip(q, fs)], tparams) for fs in fsets]
+    fsets = [[fr for (_, _, _, fr) in main], [H.Frame(ctx, m["width"], m["height"], m["spp"]) for m in mlist]]
+    e2e_batches = [H.Batch(ctx, [(t, cam, fr) for (_, t, cam, _), fr in zip(main, fs)], tparams) for fs in fsets]
     pins = [[torch.empty((m["height"], m["width"], 4), dtype=torch.float32, pin_memory=True) for m in mlist]
             for _ in range(2)]
     streams = [torch.cuda.Stream(), torch.cuda.Stream()]
@@ -601,9 +618,12 @@ def run_batched(args, dist):
     d2h = sum(m["width"] * m["height"] * 16 for m in mlist)
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": DTYPE_DESC, "data": DATA_DESC, "config": batch_config_block(mlist),
+            "vs_baseline": None, "dtype": "fp32" if fmt == "fp32" else DTYPE_DESC, "data": DATA_DESC,
+            "config": batch_config_block(mlist),
             "rays_per_step": int(rays_per_step), "gpu_launches": args.steps * kernels_per_replay(mlist, tuned),
-            "autotuned": {k: int(getattr(tuned, k)) for k in H.TUNED_FIELDS} | {"mean_ms": round(tune_ms, 3)},
+            "autotuned": {"node_format": fmt} | {k: int(getattr(tuned, k)) for k in H.TUNED_FIELDS} |
+                         {"mean_ms": round(tune_ms, 3), "mean_ms_fp32": round(tune_ms_f, 3),
+                          "mean_ms_quantised": round(tune_ms_q, 3)},
             "clocks": clk,
             "e2e": {"value": round(rays_per_step / te / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": table_bytes,
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(te * 1e3, 3)},
@@ -613,16 +633,18 @@ def run_batched(args, dist):
             "per_scene_latency_ms": {"batched_all_scenes": round(ms, 3),
                                      "plain_fp32": [round(float(x), 2) for x in lat_f32]}}
     if not args.no_cpu:
-        line.update(batch_agreement_and_cpu(ctx, q, models, tuned, fb_timed))
-    del q, batch, scenes_q
+        line.update(batch_agreement_and_cpu(ctx, main, models, tuned, fb_timed))
+    del q, f, main, batch, scenes_q, scenes_f, scenes_main
     if not args.quick:
         orc = oracle_lib()
         line["configs"] = {name.split("_")[0]: run_config(ctx, name, args, orc) for name in SINGLE_CONFIGS}
     # the comparisons the metric names, last (the line is long; its end is what a log tail keeps)
-    line["sequential_quantised"] = {"value": round(rays_per_step / (ms_q * 1e-3) / 1e6, 3),
-                                    "ms_per_step": round(ms_q, 3)}
-    line["batched_fp32"] = {"value": round(rays_per_step / (ms_bf * 1e-3) / 1e6, 3), "ms_per_step": round(ms_bf, 3),
-                            "autotuned": {k: int(getattr(tuned_f, k)) for k in H.TUNED_FIELDS}}
+    line[f"sequential_{fmt}"] = {"value": round(rays_per_step / (ms_seq * 1e-3) / 1e6, 3),
+                                 "ms_per_step": round(ms_seq, 3), "what": "the 16 scenes as 16 launches of the tuned "
+                                                                          "kernels in the chosen node format"}
+    line[f"batched_{other}"] = {"value": round(rays_per_step / (ms_bo * 1e-3) / 1e6, 3), "ms_per_step": round(ms_bo, 3),
+                                "autotuned": {k: int(getattr(tuned_o, k)) for k in H.TUNED_FIELDS},
+                                "what": f"the same batch on {other} BLASes (the format the autotuner did not choose)"}
     line["plain_fp32"] = {"value": round(rays_per_step / (ms_f32 * 1e-3) / 1e6, 3), "ms_per_step": round(ms_f32, 3),
                           "what": "the same 16 scenes as 16 sequential launches of the FP32 tracer (FP32 nodes and "
                                   "records, no batching, no autotuning)"}
@@ -634,28 +656,34 @@ def run_batched(args, dist):
     dist.close()
 
 
-# Per-ray counters of the dominant kernel (the batch's quantised Phantom group) from one ncu
-# capture of that launch (profiles/frame_kernel_c5_phantom_group.md): DRAM bytes
-# (dram__bytes_read.sum + dram__bytes_write.sum), L2 bytes (lts__t_sectors.sum x 32) and warp
-# instructions (smsp__inst_executed.sum), each over the launch's 4,649,742 rays.
-NCU_PER_RAY = {"dram_bytes": 36.94e6 / 4649742, "l2_bytes": 97210795 * 32 / 4649742,
-               "warp_inst": 6712892714 / 4649742, "source": "profiles/frame_kernel_c5_phantom_group.md"}
+# Per-ray counters of the dominant kernel (the batch's Phantom group) in each node format, from
+# one ncu capture of that launch per format (profiles/frame_kernel_c5_phantom_group*.md): DRAM
+# bytes (dram__bytes_read.sum + dram__bytes_write.sum), L2 bytes (lts__t_sectors.sum x 32) and
+# warp instructions (smsp__inst_executed.sum), each over the launch's 4,649,742 rays.
+NCU_PER_RAY = {
+    "quantised": {"dram_bytes": 36.94e6 / 4649742, "l2_bytes": 97210795 * 32 / 4649742,
+                  "warp_inst": 6712892714 / 4649742, "source": "profiles/frame_kernel_c5_phantom_group.md"},
+    "fp32": {"dram_bytes": 59.65e6 / 4649742, "l2_bytes": 185948621 * 32 / 4649742,
+             "warp_inst": 5976378613 / 4649742,
+             "source": "profiles/frame_kernel_c5_phantom_group_fp32_vs_quantised.md"},
+}
 
 
-def measured_bounds(rays: int, ms: float, clk: dict) -> dict:
-    """DRAM traffic, achieved L2 bandwidth and the issue-rate fraction of the dominant kernel,
-    scaled from its ncu capture's per-ray counters to this launch."""
-    if not NCU_PER_RAY:
+def measured_bounds(rays: int, ms: float, clk: dict, fmt: str = "quantised") -> dict:
+    """DRAM traffic, achieved L2 bandwidth and the issue-rate fraction of the dominant kernel in
+    node format `fmt`, scaled from its ncu capture's per-ray counters to this launch."""
+    c = NCU_PER_RAY.get(fmt)
+    if not c:
         return {}
     sm_mhz = clk.get("sm_mhz") or 2070.0
-    dram = NCU_PER_RAY["dram_bytes"] * rays
-    l2 = NCU_PER_RAY["l2_bytes"] * rays
-    inst = NCU_PER_RAY["warp_inst"] * rays
+    dram = c["dram_bytes"] * rays
+    l2 = c["l2_bytes"] * rays
+    inst = c["warp_inst"] * rays
     issue_peak = 152 * 4 * sm_mhz * 1e6  # one warp instruction per scheduler per clock
     return {"traffic": int(dram), "l2": {"bytes_per_launch": int(l2), "achieved_gbs": round(l2 / (ms * 1e-3) / 1e9, 1)},
             "issue": {"warp_inst_per_launch": int(inst), "achieved_per_s": round(inst / (ms * 1e-3), 1),
                       "peak_per_s": issue_peak, "frac": round(inst / (ms * 1e-3) / issue_peak, 4)},
-            "counters_from": NCU_PER_RAY["source"]}
+            "counters_from": c["source"]}
 
 
 def batch_agreement_and_cpu(ctx, q, models, tuned, fb_timed):

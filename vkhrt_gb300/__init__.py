@@ -516,7 +516,8 @@ def autotune(ctx: Context, scenes: list[tuple[TopLevelAccelerationStructure, Cam
              params: TraceParamsC | None = None, reps: int = 3, cache: str | None = None,
              key: str | None = None) -> tuple[TraceParamsC, float]:
     """hrt_autotune on `scenes`; with `cache` (a JSON file) and `key`, a stored choice is reused
-    and a new one is stored. Returns (parameters, mean frame ms of the choice or -1 if cached)."""
+    and a new one is stored. Returns (parameters, mean frame ms of the choice, the stored one when
+    cached, or -1 when the cache holds none)."""
     import json
     base = params if params is not None else trace_params()
     if cache and key and os.path.exists(cache):
@@ -528,7 +529,7 @@ def autotune(ctx: Context, scenes: list[tuple[TopLevelAccelerationStructure, Cam
             best = TraceParamsC.from_buffer_copy(base)
             for f in TUNED_FIELDS:
                 setattr(best, f, int(stored[f]))
-            return best, -1.0
+            return best, float(stored.get("ms", -1.0))
     descs = (SceneDescC * len(scenes))()
     for i, (t, cam, fr) in enumerate(scenes):
         descs[i].tlas = t.handle
