@@ -285,7 +285,7 @@ def test_kernel_variants_and_autotune_give_identical_frames(ctx, tmp_path):
     bit) and pixels within 1e-6 (the occupancy variants are separate compilations of the FP32
     Phantom solver, whose last-bit rounding of the hit's curve parameter may differ, moving
     the shaded normal by a few ulps); the autotuner's choice is one of its candidates, and
-    cached choices are reused."""
+    cached choices (with their timing) are reused."""
     scenes = []
     for k, (gt, ns, w, h, spp) in enumerate([(PHANTOM, 300, 72, 40, 2), (LSS, 200, 48, 48, 1), (DOTS, 120, 40, 56, 3)]):
         v, r, off = H.generate_strands(H.StrandParams(seed=90 + k, nstrands=ns, nverts=32))
@@ -312,7 +312,7 @@ def test_kernel_variants_and_autotune_give_identical_frames(ctx, tmp_path):
     best, ms = H.autotune(ctx, sc, H.trace_params(shading=2, jitter=1, seed=5), reps=1, cache=cache, key="three")
     assert ms > 0 and best.kernel_variant in (1, 2, 3) and best.refill in (8, 16) and best.leaf_again in (2, 4, 8)
     again, ms2 = H.autotune(ctx, sc, H.trace_params(shading=2, jitter=1, seed=5), reps=1, cache=cache, key="three")
-    assert ms2 == -1.0 and all(getattr(again, f) == getattr(best, f) for f in H.TUNED_FIELDS)
+    assert abs(ms2 - ms) < 1e-3 and all(getattr(again, f) == getattr(best, f) for f in H.TUNED_FIELDS)  # the stored time
     p = H.trace_params(shading=2, record_hits=1, jitter=1, seed=5, **{f: getattr(best, f) for f in H.TUNED_FIELDS})
     batch = H.Batch(ctx, sc, p)
     batch.launch()
