@@ -1245,12 +1245,27 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) frame_kernel(TraceLaunch
     uint32_t shadow_rays = 0, err = 0;
 
     bool has_ray = false, fetch_done = false, per_sample = false;
-    uint32_t si = 0, px = 0, py = 0, sample = 0, g_cur = 0;
-    uint64_t item = 0;  // FP64 pass, one sample per lane: the scratch index of the sample
-    uint64_t pix = 0;
+    // a task's bookkeeping, touched once per sample: in shared memory, out of the registers the
+    // traversal needs
+    __shared__ uint32_t s_task[6][kThreads];
+    __shared__ uint64_t s_task64[2][kThreads];
+    __shared__ float s_acc[4][kThreads];
+    uint32_t& si = s_task[0][tid];
+    uint32_t& px = s_task[1][tid];
+    uint32_t& py = s_task[2][tid];
+    uint32_t& sample = s_task[3][tid];
+    uint32_t& g_cur = s_task[4][tid];
+    uint32_t& prim_flags = s_task[5][tid];
+    uint64_t& item = s_task64[0][tid];  // FP64 pass, one sample per lane: the scratch index of the sample
+    uint64_t& pix = s_task64[1][tid];
+    float& acc0 = s_acc[0][tid];
+    float& acc1 = s_acc[1][tid];
+    float& acc2 = s_acc[2][tid];
+    float& ndl = s_acc[3][tid];
+    si = px = py = sample = g_cur = prim_flags = 0;
+    item = pix = 0;
+    acc0 = acc1 = acc2 = ndl = 0.0f;
     bool shadow = false, shadow_hit = false;
-    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, ndl = 0.0f;
-    uint32_t prim_flags = 0;
     V3<float> wo = mk(0.0f, 0.0f, 0.0f), wd = mk(0.0f, 0.0f, 1.0f);
     float cur_tmin = 0.0f;
     RayState R;
@@ -1701,8 +1716,11 @@ __global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance*
 // per kernel when the context is created (not during a graph capture).
 template <int kNodes, int kType, int kMinBlocks, int kPass>
 cudaError_t set_carveout() {
+    // a block holds 23 KB of shared memory (16 KB of short stacks, 7 KB of task state) plus 1 KB
+    // the hardware reserves: 40 % of the 228 KB array (the 100 KB configuration) fits four
+    // blocks, 55 % (132 KB) five
     return cudaFuncSetAttribute(frame_kernel<kNodes, kType, kMinBlocks, kPass>,
-                                cudaFuncAttributePreferredSharedMemoryCarveout, 40);
+                                cudaFuncAttributePreferredSharedMemoryCarveout, kMinBlocks >= 5 ? 55 : 40);
 }
 template <int kNodes>
 cudaError_t prepare_frame_kernels() {
