@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define HRT_ABI_VERSION 9
+#define HRT_ABI_VERSION 10
 
 typedef enum hrt_status {
     HRT_OK = 0,
@@ -208,6 +208,10 @@ typedef struct hrt_trace_params {
      * returns HRT_ERR_TIMEOUT or HRT_ERR_STACK_OVERFLOW; the context stays usable. */
     uint32_t max_steps;
     uint32_t max_depth;
+    /* kernel_variant per primitive type, for a launch (or a batch group) whose BLASes all have one
+     * type: 4 bits per hrt_geometry_type t at bits 4t..4t+3, 0 = kernel_variant. hrt_autotune
+     * fills it when per-type variants beat one variant for all groups. */
+    uint32_t variant_by_type;
 } hrt_trace_params;
 
 typedef struct hrt_hit {
@@ -349,7 +353,7 @@ hrt_status hrt_batch_download(hrt_batch* b, float* const* rgba, void* stream, in
  * that), each `reps` times with plain launches after one warm-up, and writes the fastest into
  * `best` (a copy of `base` with kernel_variant, refill, speculative, leaf_again and split_types
  * replaced) and its mean frame time into `best_ms`. */
-#define HRT_AUTOTUNE_CANDIDATES 18u  /* 3 x 2 x 3 */
+#define HRT_AUTOTUNE_CANDIDATES 18u  /* 3 x 2 x 3, then up to 3 per primitive type (variant_by_type) */
 hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t n, const hrt_trace_params* base,
                         uint32_t reps, void* stream, hrt_trace_params* best, float* best_ms);
 

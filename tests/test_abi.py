@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
 def test_abi_version_and_status_strings():
     import vkhrt_gb300 as H
     lib = H.load()
-    assert lib.hrt_abi_version() == 9 == H.ABI_VERSION
+    assert lib.hrt_abi_version() == 10 == H.ABI_VERSION
     assert lib.hrt_status_string(0) == b"ok"
     assert lib.hrt_status_string(4) == b"traversal stack overflow"
 

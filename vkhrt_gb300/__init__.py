@@ -26,7 +26,7 @@ LIB_PATH = os.path.join(_HERE, "libhrt.so")
 c_f, c_u32, c_i32, c_u64, c_p = ctypes.c_float, ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_void_p
 
 
-ABI_VERSION = 9  # HRT_ABI_VERSION of include/hrt.h that the structures below mirror
+ABI_VERSION = 10  # HRT_ABI_VERSION of include/hrt.h that the structures below mirror
 
 
 class BLASInputC(ctypes.Structure):
@@ -53,7 +53,8 @@ class TraceParamsC(ctypes.Structure):
                 ("shading", c_u32), ("shadow_tmin", c_f), ("fp64_resolve", c_u32), ("record_hits", c_u32),
                 ("async_", c_u32), ("count_stats", c_u32), ("kernel_variant", c_u32), ("refill", c_u32),
                 ("speculative", c_u32), ("split_types", c_u32), ("env_map", c_p), ("env_width", c_u32),
-                ("env_height", c_u32), ("leaf_again", c_u32), ("max_steps", c_u32), ("max_depth", c_u32)]
+                ("env_height", c_u32), ("leaf_again", c_u32), ("max_steps", c_u32), ("max_depth", c_u32),
+                ("variant_by_type", c_u32)]
 
 
 class FrameStatsC(ctypes.Structure):
@@ -509,7 +510,7 @@ def trace_rays_noalloc(ctx: Context, tlas: TopLevelAccelerationStructure, rays: 
     return hits
 
 
-TUNED_FIELDS = ("kernel_variant", "refill", "speculative", "split_types", "leaf_again")
+TUNED_FIELDS = ("kernel_variant", "refill", "speculative", "split_types", "leaf_again", "variant_by_type")
 
 
 def autotune(ctx: Context, scenes: list[tuple[TopLevelAccelerationStructure, CameraC, Frame]],
@@ -528,7 +529,7 @@ def autotune(ctx: Context, scenes: list[tuple[TopLevelAccelerationStructure, Cam
         if stored:
             best = TraceParamsC.from_buffer_copy(base)
             for f in TUNED_FIELDS:
-                setattr(best, f, int(stored[f]))
+                setattr(best, f, int(stored.get(f, getattr(base, f))))
             return best, float(stored.get("ms", -1.0))
     descs = (SceneDescC * len(scenes))()
     for i, (t, cam, fr) in enumerate(scenes):

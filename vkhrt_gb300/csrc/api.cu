@@ -291,6 +291,8 @@ TraceLaunch make_launch(const hrt_trace_params* p, const SceneLaunch* ds, uint32
     L.record_hits = p->record_hits;
     L.count_stats = p->count_stats;
     L.variant = p->kernel_variant;
+    const uint32_t kind = prim_kind(type_mask);
+    if (kind < 3 && ((p->variant_by_type >> (4 * kind)) & 15u)) L.variant = (p->variant_by_type >> (4 * kind)) & 15u;
     L.refill = p->refill > 32 ? 32 : p->refill;
     L.speculative = p->speculative;
     L.leaf_again = p->leaf_again > 32 ? 32 : p->leaf_again;
@@ -1754,8 +1756,8 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
     ScenePlan plans[2];
     hrt_status st = make_plan(ctx, "hrt_autotune", scenes, n, false, false, s, plans[0]);
     uint32_t nplans = 1;
+    uint32_t kinds = 0;  // primitive types present
     if (st == HRT_OK) {
-        uint32_t kinds = 0;
         for (uint32_t i = 0; i < n; ++i) kinds |= scenes[i].tlas->type_mask;
         if (prim_kind(kinds) == 3) {
             st = make_plan(ctx, "hrt_autotune", scenes, n, true, false, s, plans[1]);
@@ -1818,6 +1820,42 @@ hrt_status hrt_autotune(hrt_context* ctx, const hrt_scene_desc* scenes, uint32_t
                         bp.count_stats = base->count_stats;
                     }
                 }
+    // per-type variants: with one launch per primitive type, each type's group may prefer
+    // another occupancy than the others (Phantom's long solve against LSS and DOTS)
+    if (e == cudaSuccess && bp.split_types && nplans == 2) {
+        for (uint32_t t = 0; t < 3 && e == cudaSuccess; ++t) {
+            if (!((kinds >> t) & 1u)) continue;
+            for (uint32_t v : variants) {
+                if (v == bp.kernel_variant) continue;
+                hrt_trace_params p = bp;
+                p.record_hits = 0;
+                p.count_stats = 0;
+                p.variant_by_type = (bp.variant_by_type & ~(15u << (4 * t))) | (v << (4 * t));
+                float tot = 0.0f;
+                for (uint32_t k = 0; k <= reps && e == cudaSuccess; ++k) {
+                    e = cudaEventRecord(e0, s);
+                    if (e == cudaSuccess) e = enqueue_plan(plans[1], &p, s, ctx->sm_count, &br);
+                    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                    float ms = 0.0f;
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                    if (k > 0) tot += ms;
+                }
+                if (e != cudaSuccess) break;
+                TraceCounters c;
+                st = read_plan_counters(ctx, plans[1], &c, s);
+                if (st != HRT_OK) {
+                    cleanup();
+                    return st;
+                }
+                const float mean = tot / float(reps);
+                if (mean < best_t) {
+                    best_t = mean;
+                    bp.variant_by_type = p.variant_by_type;
+                }
+            }
+        }
+    }
     cleanup();
     if (e != cudaSuccess) return cuda_fail(ctx, e, "hrt_autotune");
     *best = bp;
