@@ -1709,11 +1709,11 @@ __global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance*
 }
 #endif
 
-// Shared memory / L1 split of the SM for a frame kernel: 40 % asks for the 100 KB shared
-// configuration, which holds up to five blocks' short stacks (17 KB each), and leaves the rest of
-// the array to L1 for the node and record loads (0.2-0.8 % faster than the default split; the
-// largest L1 split cuts the resident blocks, the largest shared split is 2-4 % slower). Set once
-// per kernel when the context is created (not during a graph capture).
+// Shared memory / L1 split of the SM for a frame kernel: the smallest shared configuration that
+// holds the variant's resident blocks, so the rest of the array serves as L1 for the node and
+// record loads (0.2-0.8 % faster than the default split; the largest L1 split cuts the resident
+// blocks, the largest shared split is 2-4 % slower). Set once per kernel when the context is
+// created (not during a graph capture).
 template <int kNodes, int kType, int kMinBlocks, int kPass>
 cudaError_t set_carveout() {
     // a block holds 23 KB of shared memory (16 KB of short stacks, 7 KB of task state) plus 1 KB
