@@ -661,10 +661,10 @@ def run_batched(args, dist):
 # bytes (dram__bytes_read.sum + dram__bytes_write.sum), L2 bytes (lts__t_sectors.sum x 32) and
 # warp instructions (smsp__inst_executed.sum), each over the launch's 4,649,742 rays.
 NCU_PER_RAY = {
-    "quantised": {"dram_bytes": 36.94e6 / 4649742, "l2_bytes": 97210795 * 32 / 4649742,
-                  "warp_inst": 6712892714 / 4649742, "source": "profiles/frame_kernel_c5_phantom_group.md"},
-    "fp32": {"dram_bytes": 59.65e6 / 4649742, "l2_bytes": 185948621 * 32 / 4649742,
-             "warp_inst": 5976378613 / 4649742,
+    "quantised": {"dram_bytes": 36.93e6 / 4649742, "l2_bytes": 97101539 * 32 / 4649742,
+                  "warp_inst": 6621019102 / 4649742, "source": "profiles/frame_kernel_c5_phantom_group.md"},
+    "fp32": {"dram_bytes": 58.94e6 / 4649742, "l2_bytes": 181719966 * 32 / 4649742,
+             "warp_inst": 5963512049 / 4649742,
              "source": "profiles/frame_kernel_c5_phantom_group_fp32_vs_quantised.md"},
 }
 
