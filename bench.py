@@ -20,8 +20,10 @@ roofline. Per-scene details go to stderr.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
 
-Under torchrun (N > 1) every rank renders the full workload (replicas, weak scaling); rank 0
-prints the line. `--impl reference` times the CPU restatement of the reference's trace path
+Under torchrun (N > 1) every rank renders its own views of the workload: each scene's camera is
+turned about the vertical axis by 2 pi rank / N (rank_azimuth), so the ranks' work is disjoint and
+of the same size (replicas, weak scaling, no device collective); after the timed steps rank 0
+gathers every rank's framebuffers to its host (vkhrt_gb300.replicas) and prints the line. `--impl reference` times the CPU restatement of the reference's trace path
 (oracle/, FP32, all host threads; the oracle library alone, which also carries the workload
 generator) on one band of image rows of every scene per step.
 """
@@ -403,6 +405,12 @@ def run_config(ctx, name: str, args, orc) -> dict:
 
 
 # ------------------------------------------------------------------------------ batched (default)
+def rank_azimuth(azimuth: float, rank: int, world: int) -> float:
+    """The camera azimuth of a scene on `rank` of `world` (rank 0 keeps the scene's own)."""
+    import math
+    return azimuth + 2.0 * math.pi * rank / world
+
+
 def batch_models():
     """The 16 models of the batched workload, with strands generated (host arrays)."""
     import vkhrt_gb300 as H
@@ -447,7 +455,8 @@ def run_batched(args, dist):
                 H.BLASInput(type=m["type"], vertices=v, radius=r, strand_offsets=off, precision=precision,
                             max_leaf=args.max_leaf), ctx)
             t = H.TopLevelAccelerationStructure([b], ctx)
-            cam = H.orbit_camera(m["width"], m["height"], m["azimuth"], m["elevation"])
+            cam = H.orbit_camera(m["width"], m["height"], rank_azimuth(m["azimuth"], dist.rank, dist.world),
+                                 m["elevation"])
             out.append((b, t, cam, H.Frame(ctx, m["width"], m["height"], m["spp"], with_hits=with_hits)))
         return out
 
@@ -519,6 +528,10 @@ def run_batched(args, dist):
     # the timed replay's framebuffers, checked below against the oracle
     fb_timed = [np.zeros((m["height"], m["width"], 4), np.float32) for m in mlist]
     batch.download(fb_timed)
+    gathered = None
+    if dist.world > 1:  # every rank's views to rank 0's host
+        from vkhrt_gb300.replicas import gather_to_rank0
+        gathered = gather_to_rank0({(dist.rank, i): fb for i, fb in enumerate(fb_timed)}, dist.pg)
 
     def sequential(sc, params):
         """Mean over steps of the sum of per-scene launch times (each launch bracketed by events)."""
@@ -632,6 +645,10 @@ def run_batched(args, dist):
             "device_bytes": {"quantised": mem_q, "fp32": mem_f},
             "per_scene_latency_ms": {"batched_all_scenes": round(ms, 3),
                                      "plain_fp32": [round(float(x), 2) for x in lat_f32]}}
+    if gathered is not None:
+        line["replicas"] = {"ranks": dist.world, "frames_gathered_on_rank0": len(gathered),
+                            "bytes_gathered": int(sum(v.nbytes for v in gathered.values())),
+                            "views": "each scene's camera turned by 2 pi rank / N about the vertical axis"}
     if not args.no_cpu:
         line.update(batch_agreement_and_cpu(ctx, main, models, tuned, fb_timed))
     del q, f, main, batch, scenes_q, scenes_f, scenes_main

@@ -29,3 +29,12 @@ def test_batch_config_block_names_the_autotuned_format_choice():
     blk = bench.batch_config_block(models)
     assert blk["segments"] == 40 and blk["primary_samples"] == 24 and blk["scenes"] == 1
     assert blk["precision"] == bench.BATCH_PRECISION_DESC and "autotuner" in blk["precision"]
+
+
+def test_rank_views_are_disjoint_and_rank0_keeps_the_workload():
+    import math
+    import bench
+    assert bench.rank_azimuth(0.3, 0, 4) == 0.3
+    az = [bench.rank_azimuth(0.3, r, 4) % (2 * math.pi) for r in range(4)]
+    assert len({round(a, 9) for a in az}) == 4
+    assert abs(bench.rank_azimuth(0.3, 2, 4) - (0.3 + math.pi)) < 1e-12
