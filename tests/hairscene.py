@@ -55,11 +55,10 @@ def lines_from_strands(v: np.ndarray, r: np.ndarray | None, off: np.ndarray, con
             np.ascontiguousarray(np.concatenate(rs), np.float32))
 
 
-def oracle_geometry(orc, gtype: int, lines: np.ndarray, lrad: np.ndarray, quantised: bool = False):
+def oracle_geometry(orc, gtype: int, lines: np.ndarray, lrad: np.ndarray):
     """Geometry as the oracle restates it: (data, radius) in the layout orc_scene_add_blas takes.
     A quantised BLAS holds the same geometry (its Phantom leaves rebuild the FP32 curves from the
-    strand vertex stream), so `quantised` changes nothing: the oracle always traces the strands'
-    FP32 curves."""
+    strand vertex stream), so the oracle traces the strands' FP32 curves for either format."""
     n = lines.shape[0]
     if gtype == PHANTOM:
         curves = np.zeros((n, 12), np.float32)

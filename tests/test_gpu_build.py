@@ -63,7 +63,7 @@ def check_blas(ctx, orc, gtype, precision, v, r, off, max_leaf=1, line_indices=N
     n = len(lines)
     assert blas.info["nprims"] == n
     quant_prims = precision == 1 and gtype == PHANTOM
-    data, rad = oracle_geometry(orc, gtype, lines, lrad, quantised=quant_prims)
+    data, rad = oracle_geometry(orc, gtype, lines, lrad)
     if n == 0:
         assert blas.info["nnodes"] == 0
         return blas

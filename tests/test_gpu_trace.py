@@ -29,7 +29,7 @@ def make_scene(ctx, orc, gtype, precision=0, seed=21, ns=300, nv=17, radius=True
                     const_radius=const_radius, transform=xf), ctx)
     tlas = H.TopLevelAccelerationStructure([blas], ctx)
     lines, lrad = lines_from_strands(v, r, off, const_radius)
-    data, rad = oracle_geometry(orc, gtype, lines, lrad, quantised=(precision == 1 and gtype == PHANTOM))
+    data, rad = oracle_geometry(orc, gtype, lines, lrad)
     osc = OracleScene(orc, [(gtype, data, rad)], [None if transform is None else transform])
     return blas, tlas, osc, lines
 
@@ -408,7 +408,7 @@ def _mesh_scene(ctx, orc, precision, with_normals, hair=False):
             H.BLASInput(type=H.BLASType.ePhantom, vertices=hv, radius=hr, strand_offsets=hoff,
                         precision=H.Precision(precision)), ctx)
         lines, lrad = lines_from_strands(hv, hr, hoff)
-        hd, hrad = oracle_geometry(orc, PHANTOM, lines, lrad, quantised=precision == 1)
+        hd, hrad = oracle_geometry(orc, PHANTOM, lines, lrad)
         blases.append(hb)
         obl.append((PHANTOM, hd, hrad))
     tlas = H.TopLevelAccelerationStructure(blases, ctx)
@@ -453,7 +453,7 @@ def test_refit_trace_vs_fp64_oracle(ctx, orc, gtype, precision):
     blas.refit(v2, r)
     tlas = H.TopLevelAccelerationStructure([blas], ctx)  # TLASes copy the bounds: build after a refit
     lines, lrad = lines_from_strands(v2, r, off)
-    data, rad = oracle_geometry(orc, gtype, lines, lrad, quantised=(precision == 1 and gtype == PHANTOM))
+    data, rad = oracle_geometry(orc, gtype, lines, lrad)
     osc = OracleScene(orc, [(gtype, data, rad)])
     rays = aimed_rays(np.random.default_rng(13), lines, 20000, spread=0.006)
     g = H.trace_rays(ctx, tlas, rays)
