@@ -121,3 +121,26 @@ def test_albedo_map_sizes_are_checked(ctx, shape):
         H.BottomLevelAccelerationStructure(H.BLASInput(type=H.BLASType.eMesh, vertices=v, tri_indices=tri, texcoords=tc,
                                                        albedo_map=np.zeros(shape, np.float32)), ctx)
     assert e.value.status == 1
+
+
+def test_textured_mesh_instance_with_a_transform(ctx, orc):
+    """The albedo of a scaled, rotated and moved mesh instance: the shading weights come from the
+    object-space ray, as the oracle's do."""
+    rng = np.random.default_rng(71)
+    v, tri, nrm = sphere_mesh(rng, nu=NU, nv=NV)
+    tc = _sphere_uv()
+    amap = rng.uniform(0.05, 1.0, (9, 5, 4)).astype(np.float32)
+    factor = (0.8, 0.9, 0.6, 1.0)
+    c, s = np.cos(0.6), np.sin(0.6)
+    xf = np.array([[1.3 * c, 0, 1.3 * s, 0.2], [0, 1.3, 0, -0.1], [-1.3 * s, 0, 1.3 * c, 0.3], [0, 0, 0, 1]],
+                  np.float32)
+    mb = H.BottomLevelAccelerationStructure(
+        H.BLASInput(type=H.BLASType.eMesh, vertices=v, tri_indices=tri, normals=nrm, transform=xf,
+                    albedo_factor=factor, texcoords=tc, albedo_map=amap), ctx)
+    tlas = H.TopLevelAccelerationStructure([mb], ctx)
+    osc = OracleScene(orc, [(MESH, *mesh_oracle_data(v, tri, nrm))], [xf])
+    osc.set_material(0, factor, tc[tri].reshape(-1, 6), amap)
+    fr, rgba, hits, o = render_both(ctx, tlas, osc, 160, 120, spp=1, shading=2)
+    st, px_ok, diff = frame_checks(rgba, hits, o, 1)
+    assert st["hits"] > 2000 and st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
+    assert px_ok.mean() >= 0.999 and diff[px_ok].max() <= RGB_ABS
