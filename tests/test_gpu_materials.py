@@ -142,5 +142,5 @@ def test_textured_mesh_instance_with_a_transform(ctx, orc):
     osc.set_material(0, factor, tc[tri].reshape(-1, 6), amap)
     fr, rgba, hits, o = render_both(ctx, tlas, osc, 160, 120, spp=1, shading=2)
     st, px_ok, diff = frame_checks(rgba, hits, o, 1)
-    assert st["hits"] > 2000 and st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
+    assert st["hits"] > 1000 and st["agreement"] >= AGREE and st["p9999_rel_t"] <= T_REL
     assert px_ok.mean() >= 0.999 and diff[px_ok].max() <= RGB_ABS
