@@ -209,7 +209,8 @@ typedef struct hrt_trace_params {
     uint32_t max_steps;
     uint32_t max_depth;
     /* kernel_variant per primitive type, for a launch (or a batch group) whose BLASes all have one
-     * type: 4 bits per hrt_geometry_type t at bits 4t..4t+3, 0 = kernel_variant. hrt_autotune
+     * hair type: 4 bits per hrt_geometry_type t (Phantom, LSS, DOTS) at bits 4t..4t+3, 0 =
+     * kernel_variant; launches of meshes, voxels or mixed types use kernel_variant. hrt_autotune
      * fills it when per-type variants beat one variant for all groups. */
     uint32_t variant_by_type;
 } hrt_trace_params;
