@@ -323,8 +323,10 @@ hrt_status hrt_trace_rays_noalloc(hrt_context* ctx, const hrt_tlas* tlas, const 
                                   const hrt_trace_params* p, hrt_hit* hits, void* stream);
 
 /* ---- batched multi-scene rendering ---------------------------------------------------------
- * All scenes are traced by one persistent launch, captured once in a CUDA graph by
- * hrt_batch_create and replayed by hrt_batch_launch. */
+ * All scenes are traced by one persistent launch (or, with split_types, one per primitive
+ * type), captured once in a CUDA graph by hrt_batch_create and replayed by hrt_batch_launch. The
+ * launch takes the scenes' pixels longest job first (most samples per pixel, then most
+ * primitives), whatever their order in `scenes`; results do not depend on it. */
 typedef struct hrt_scene_desc {
     const hrt_tlas* tlas;
     hrt_camera camera;
