@@ -255,10 +255,11 @@ hrt_status hrt_blas_destroy(hrt_blas* blas);
  * motions (build anew then). TLASes that hold the BLAS must be built again afterwards (they
  * copy its bounds). No counterpart in the reference (it builds once). */
 hrt_status hrt_blas_refit(hrt_blas* blas, const float* vertices, const float* per_vertex, int32_t memory, void* stream);
-/* A built BLAS as bytes (host memory): tree, records, roots, slot map and the refit topology
- * (image version 2: LSS and DOTS records and slot-map entries are per BVH reference, two per
- * segment). hrt_blas_deserialize checks the image (header, sizes, every node's child and leaf
- * ranges, record roots, the slot map of two-reference BLASes) before anything reaches the device
+/* A built BLAS as bytes (host memory): tree, records, strand vertex stream, slot map, mesh
+ * material and the refit topology (image version 4; LSS and DOTS records and slot-map entries
+ * are per BVH reference, two per segment). hrt_blas_deserialize checks the image (header, sizes,
+ * every node's child and leaf ranges, quantised Phantom records inside the strand vertex stream,
+ * the slot map of two-reference BLASes, the material's sizes) before anything reaches the device
  * and rejects a corrupt one, or one of another version, with HRT_ERR_INVALID_ARG. No counterpart
  * in the reference (it rebuilds at every start). */
 uint64_t hrt_blas_serialized_size(const hrt_blas* blas);

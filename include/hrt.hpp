@@ -10,6 +10,8 @@
  *   Batch (many scenes, one CUDA-graph replay per step; no counterpart in the reference, whose
  *     renderer traces one scene per frame)
  *   LookAt(...)             <- FlyCamera::ViewMatrix/ProjectionMatrix (source/fly_camera.cpp:25-35)
+ *   TraceRays(...)          <- traceRayEXT for caller-supplied rays (shaders/ray_gen.rgen:34-45)
+ *   BLAS Serialize/Load/Refit (no counterpart: the reference rebuilds at every start)
  * Header only; links against libhrt.so. Where the reference logs and aborts on a failed call
  * (VkCheckResult, source/vk_common.cpp:5-15) these classes throw hrt::Error, which carries the
  * status and hrt_last_error's message; a caller that wants the reference's behaviour catches it,
@@ -94,7 +96,8 @@ struct BLASInput {
 
 class BottomLevelAccelerationStructure {
 public:
-    BottomLevelAccelerationStructure(const BLASInput& in, Context& ctx, void* stream = nullptr) : _type(TypeOf(in.geometry)) {
+    BottomLevelAccelerationStructure(const BLASInput& in, Context& ctx, void* stream = nullptr)
+        : _ctx(ctx.Get()), _type(TypeOf(in.geometry)) {
         hrt_blas_input b;
         hrt_blas_input_default(&b);
         b.type = in.geometry;
@@ -130,7 +133,28 @@ public:
     }
     ~BottomLevelAccelerationStructure() { hrt_blas_destroy(_blas); }
     BottomLevelAccelerationStructure(BottomLevelAccelerationStructure&& o) noexcept
-        : _blas(std::exchange(o._blas, nullptr)), _type(o._type), _transform(o._transform) {}
+        : _ctx(o._ctx), _blas(std::exchange(o._blas, nullptr)), _type(o._type), _transform(o._transform) {}
+
+    // A BLAS from the bytes of Serialize() (hrt_blas_deserialize checks them first).
+    static BottomLevelAccelerationStructure Load(Context& ctx, const std::vector<uint8_t>& image,
+                                                 void* stream = nullptr) {
+        hrt_blas* b = nullptr;
+        Check(ctx.Get(), hrt_blas_deserialize(ctx.Get(), image.data(), image.size(), stream, &b),
+              "hrt_blas_deserialize");
+        return BottomLevelAccelerationStructure(ctx.Get(), b);
+    }
+    // The BLAS as bytes (host memory), for Load in this or another process.
+    std::vector<uint8_t> Serialize() const {
+        std::vector<uint8_t> out(hrt_blas_serialized_size(_blas));
+        Check(_ctx, hrt_blas_serialize(_blas, out.data(), out.size()), "hrt_blas_serialize");
+        return out;
+    }
+    // New vertex positions (3 floats each) and radii (hair) or normals (mesh) exactly when the
+    // build had them; TLASes holding the BLAS must be built again afterwards.
+    void Refit(const std::vector<float>& positions, const std::vector<float>& perVertex, void* stream = nullptr) {
+        Check(_ctx, hrt_blas_refit(_blas, positions.data(), perVertex.empty() ? nullptr : perVertex.data(),
+                                   HRT_MEMORY_HOST, stream), "hrt_blas_refit");
+    }
     BottomLevelAccelerationStructure& operator=(BottomLevelAccelerationStructure&&) = delete;
     BottomLevelAccelerationStructure(const BottomLevelAccelerationStructure&) = delete;
     BottomLevelAccelerationStructure& operator=(const BottomLevelAccelerationStructure&) = delete;
@@ -145,6 +169,11 @@ public:
     }
 
 private:
+    BottomLevelAccelerationStructure(hrt_context* ctx, hrt_blas* b)
+        : _ctx(ctx), _blas(b), _type(TypeOf(hrt_geometry_type(hrt_blas_type(b)))) {
+        hrt_blas_transform(b, _transform.data());
+    }
+    hrt_context* _ctx = nullptr;
     hrt_blas* _blas = nullptr;
     BLASType _type;
     std::array<float, 16> _transform;
@@ -218,6 +247,17 @@ inline hrt_camera LookAt(const std::array<float, 3>& eye, const std::array<float
     Check(nullptr, hrt_camera_look_at(eye.data(), center.data(), up.data(), fovyDeg, aspect, znear, zfar, &c),
           "hrt_camera_look_at");
     return c;
+}
+
+// Closest hits of explicit rays (6 floats each: origin, direction), the reference's traceRayEXT
+// for caller-supplied rays (ray_gen.rgen:34-45).
+inline std::vector<hrt_hit> TraceRays(Context& ctx, const TopLevelAccelerationStructure& tlas,
+                                      const std::vector<float>& rays, const hrt_trace_params& params,
+                                      void* stream = nullptr) {
+    std::vector<hrt_hit> hits(rays.size() / 6);
+    Check(ctx.Get(), hrt_trace_rays(ctx.Get(), tlas.Structure(), rays.data(), hits.size(), &params, hits.data(),
+                                    HRT_MEMORY_HOST, stream), "hrt_trace_rays");
+    return hits;
 }
 
 // One frame: the reference's Renderer::Render for the hair path.

@@ -107,6 +107,34 @@ int Gpu(const char* path) {
     if (got.size() != 2 || got[0].size() != rgba.size() || got[1].size() != size_t(64) * 48 * 4) return 12;
     for (size_t i = 0; i < rgba.size(); ++i)
         if (!(std::fabs(got[0][i] - rgba[i]) <= 1e-6f)) return 13;
+    // the Phantom BLAS alone, and a copy of it through a serialised image: explicit rays give the
+    // same hits bit for bit; a refit copy still traces
+    std::vector<hrt::BottomLevelAccelerationStructure> one, loaded;
+    one.emplace_back(hair, ctx);
+    loaded.push_back(hrt::BottomLevelAccelerationStructure::Load(ctx, one[0].Serialize()));
+    if (loaded[0].Type() != hrt::BLASType::eHair || loaded[0].Transform() != one[0].Transform()) return 14;
+    hrt::TopLevelAccelerationStructure t_one(one, ctx), t_loaded(loaded, ctx);
+    std::vector<float> rays;
+    for (int i = 0; i < 64; ++i)
+        for (int j = 0; j < 64; ++j) {
+            const float x = -0.6f + 1.2f * float(i) / 63.0f, y = -0.2f + 1.2f * float(j) / 63.0f;
+            rays.insert(rays.end(), {x, y, 3.0f, 0.0f, 0.0f, -1.0f});
+        }
+    const std::vector<hrt_hit> h1 = hrt::TraceRays(ctx, t_one, rays, p), h2 = hrt::TraceRays(ctx, t_loaded, rays, p);
+    size_t rhit = 0;
+    for (size_t i = 0; i < h1.size(); ++i) {
+        if (std::memcmp(&h1[i], &h2[i], sizeof(hrt_hit)) != 0) return 15;
+        rhit += h1[i].t >= 0.0f;
+    }
+    if (rhit < 20) return 16;
+    std::vector<float> moved = a.v;
+    for (size_t i = 1; i < moved.size(); i += 3) moved[i] += 0.01f;
+    loaded[0].Refit(moved, a.r);
+    hrt::TopLevelAccelerationStructure t_moved(loaded, ctx);
+    const std::vector<hrt_hit> h3 = hrt::TraceRays(ctx, t_moved, rays, p);
+    size_t mhit = 0;
+    for (const hrt_hit& x : h3) mhit += x.t >= 0.0f;
+    if (mhit < 20) return 17;
     size_t nhit = 0;
     for (const hrt_hit& x : hits) nhit += x.t >= 0.0f;
     std::printf("gpu ok %zu hits\n", nhit);
