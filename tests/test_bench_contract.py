@@ -38,3 +38,18 @@ def test_rank_views_are_disjoint_and_rank0_keeps_the_workload():
     az = [bench.rank_azimuth(0.3, r, 4) % (2 * math.pi) for r in range(4)]
     assert len({round(a, 9) for a in az}) == 4
     assert abs(bench.rank_azimuth(0.3, 2, 4) - (0.3 + math.pi)) < 1e-12
+
+
+def test_autotune_cache_returns_stored_choice_and_timing(tmp_path):
+    """A cached choice comes back with its stored timing and no device work; fields a cache
+    written by an earlier version lacks keep the base parameters' values."""
+    import json
+    import vkhrt_gb300 as H
+    cache = tmp_path / "tune.json"
+    cache.write_text(json.dumps({"k": {"kernel_variant": 3, "refill": 16, "speculative": 1, "split_types": 1,
+                                       "leaf_again": 2, "ms": 23.5}}))
+    base = H.trace_params(shading=2)
+    best, ms = H.autotune(None, [], base, cache=str(cache), key="k")
+    assert ms == 23.5
+    assert (best.kernel_variant, best.refill, best.split_types, best.leaf_again) == (3, 16, 1, 2)
+    assert best.variant_by_type == base.variant_by_type == 0 and best.shading == 2
