@@ -1716,11 +1716,23 @@ __global__ void __launch_bounds__(kThreads) trace_rays_kernel(const DevInstance*
 // created (not during a graph capture).
 template <int kNodes, int kType, int kMinBlocks, int kPass>
 cudaError_t set_carveout() {
-    // a block holds 23 KB of shared memory (16 KB of short stacks, 7 KB of task state) plus 1 KB
-    // the hardware reserves: 40 % of the 228 KB array (the 100 KB configuration) fits four
-    // blocks, 55 % (132 KB) five
-    return cudaFuncSetAttribute(frame_kernel<kNodes, kType, kMinBlocks, kPass>,
-                                cudaFuncAttributePreferredSharedMemoryCarveout, kMinBlocks >= 5 ? 55 : 40);
+    // A block holds its static shared memory (16 KB of short stacks, 7 KB of task state, 1.5 KB
+    // more for the mixed-type kernel's albedo) plus 1 KB the hardware reserves. The smallest of
+    // the SM's shared-memory configurations from 100 KB up that holds kMinBlocks of them is asked
+    // for as a percentage of the 228 KB array, rounded up so that it maps to that configuration:
+    // 100 KB for four blocks of the hair kernels, 132 KB for five, or for four mixed-type blocks.
+    auto* k = frame_kernel<kNodes, kType, kMinBlocks, kPass>;
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k);
+    if (e != cudaSuccess) return e;
+    const size_t need = size_t(kMinBlocks) * (fa.sharedSizeBytes + 1024);
+    int kb = 228;
+    for (int c : {100, 132, 164, 196, 228})
+        if (size_t(c) * 1024 >= need) {
+            kb = c;
+            break;
+        }
+    return cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (kb * 100 + 227) / 228);
 }
 template <int kNodes>
 cudaError_t prepare_frame_kernels() {
