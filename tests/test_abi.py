@@ -34,6 +34,7 @@ def test_abi_version_and_status_strings():
     assert lib.hrt_abi_version() == 10 == H.ABI_VERSION
     assert lib.hrt_status_string(0) == b"ok"
     assert lib.hrt_status_string(4) == b"traversal stack overflow"
+    assert lib.hrt_status_string(7) == b"device index check failed"
 
 
 def test_strand_generator_is_deterministic():

@@ -218,3 +218,24 @@ def test_gltf_mesh_material_and_texture(tmp_path):
     path.write_text(json.dumps(doc))
     (q,) = gltf.load(str(path))
     assert q.albedo_map is None and q.texcoords is None and "not a PNG" in q.note and q.albedo_factor[0] == 0.5
+
+
+def test_gltf_material_factor_without_texture(tmp_path):
+    """A material with a base colour factor and no texture: the factor alone, no texture
+    coordinates or map."""
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    blob = v.tobytes()
+    doc = {
+        "asset": {"version": "2.0"}, "nodes": [{"mesh": 0}],
+        "meshes": [{"primitives": [{"attributes": {"POSITION": 0}, "material": 0}]}],
+        "materials": [{"pbrMetallicRoughness": {"baseColorFactor": [0.2, 0.4, 0.6, 1.0]}}],
+        "buffers": [{"byteLength": len(blob), "uri": "data:application/octet-stream;base64," +
+                     base64.b64encode(blob).decode()}],
+        "bufferViews": [{"buffer": 0, "byteOffset": 0, "byteLength": 36}],
+        "accessors": [{"bufferView": 0, "componentType": 5126, "count": 3, "type": "VEC3"}],
+    }
+    path = tmp_path / "tri.gltf"
+    path.write_text(json.dumps(doc))
+    (p,) = gltf.load(str(path))
+    assert p.albedo_factor == (0.2, 0.4, 0.6, 1.0) and p.albedo_map is None and p.texcoords is None
+    assert p.indices.tolist() == [[0, 1, 2]]
